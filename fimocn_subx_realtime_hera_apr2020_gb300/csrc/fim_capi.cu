@@ -1,0 +1,978 @@
+// C-ABI of the GB300 FIM dynamics step (declared in include/fim_gpu.h).
+//
+// The context owns the device copy of the grid tables, the derived per-cell
+// and per-level fields of dyn_init, the AB3 step parameters, the per-member
+// status words and the scratch buffers of the routines.  Entry points mirror
+// the reference subroutines' argument lists; fields are device pointers, or
+// host pointers staged through the device when the context was created with
+// host_pointers = 1.  Nothing here aborts: every failure is a status code.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/fim_gpu.h"
+#include "fim_internal.h"
+
+using namespace fim;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct fim_state {
+  void* f[FIM_NFIELDS] = {};
+  size_t count[FIM_NFIELDS] = {};  // elements per member
+  double* sums = nullptr;          // [M][8+T]
+  cudaGraphExec_t graph = nullptr;
+  long long graph_kernels = 0;
+};
+
+struct fim_ctx {
+  fim_config cfg{};
+  int prec = FIM_PREC_F64;
+  int N = 0, L = 0, T = 0, M = 1;
+  size_t esz = 8;
+  cudaStream_t stream = nullptr;
+  std::vector<void*> owned;  // device allocations freed at destroy
+  Grid<double> gd{};
+  Grid<float> gf{};
+  Strides str{};
+  Knobs kn{};
+  std::vector<double> thetac, dpsig;
+  void* d_thetac = nullptr;
+  StepParams h_sp{};
+  StepParams* d_sp = nullptr;
+  int* d_flags = nullptr;
+  long long launches = 0;
+  // scratch (sized for all members)
+  void *antifx = nullptr, *delp_lo = nullptr, *p_plus = nullptr, *p_mnus = nullptr, *r_plus = nullptr,
+       *r_mnus = nullptr;
+  void *t_antiflx = nullptr, *t_trmin = nullptr, *t_trmax = nullptr, *t_trcr_lo = nullptr, *t_rp = nullptr,
+       *t_rm = nullptr;
+  int tchunk = 0;
+  void *du = nullptr, *dv = nullptr, *wu = nullptr, *wv = nullptr;
+  void *exsmo = nullptr, *exsmo2 = nullptr;
+  double* gs_partial = nullptr;
+  double* gs_sums = nullptr;  // per-routine globsum output [M][8+T]
+  std::string err;
+};
+
+namespace {
+
+int set_err(fim_ctx* c, int code, const char* what, cudaError_t e = cudaSuccess) {
+  if (c) {
+    char buf[512];
+    if (e != cudaSuccess) snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+    else snprintf(buf, sizeof buf, "%s", what);
+    c->err = buf;
+  }
+  return code;
+}
+
+#define CK(call, what)                                   \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) {                             \
+      if (e_ == cudaErrorMemoryAllocation) {             \
+        cudaGetLastError();                              \
+        return set_err(c, FIM_ENOMEM, what, e_);         \
+      }                                                  \
+      return set_err(c, FIM_ECUDA, what, e_);            \
+    }                                                    \
+  } while (0)
+
+int dalloc(fim_ctx* c, void** p, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return set_err(c, e == cudaErrorMemoryAllocation ? FIM_ENOMEM : FIM_ECUDA, "cudaMalloc", e);
+  }
+  c->owned.push_back(*p);
+  return FIM_OK;
+}
+
+template <typename R>
+int upload_conv(fim_ctx* c, const double* src, size_t n, const R** dst) {
+  std::vector<R> tmp(n);
+  for (size_t q = 0; q < n; q++) tmp[q] = (R)src[q];
+  void* p;
+  int rc = dalloc(c, &p, n * sizeof(R));
+  if (rc) return rc;
+  CK(cudaMemcpy(p, tmp.data(), n * sizeof(R), cudaMemcpyHostToDevice), "upload table");
+  *dst = (const R*)p;
+  return FIM_OK;
+}
+
+int upload_int(fim_ctx* c, const std::vector<int>& v, const int** dst) {
+  void* p;
+  int rc = dalloc(c, &p, v.size() * sizeof(int));
+  if (rc) return rc;
+  CK(cudaMemcpy(p, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice), "upload int table");
+  *dst = (const int*)p;
+  return FIM_OK;
+}
+
+template <typename R>
+Grid<R>& grid_of(fim_ctx* c);
+template <>
+Grid<double>& grid_of<double>(fim_ctx* c) { return c->gd; }
+template <>
+Grid<float>& grid_of<float>(fim_ctx* c) { return c->gf; }
+
+template <typename R>
+int build_grid(fim_ctx* c, const fim_grid_desc* g, const std::vector<double>& rarea, const std::vector<double>& corio,
+               const std::vector<double>& grnd, const std::vector<double>& dfflen, const std::vector<double>& biharw,
+               const std::vector<double>& smoo, const std::vector<int>& prox, const std::vector<int>& proxs,
+               const std::vector<int>& nprox) {
+  Grid<R>& G = grid_of<R>(c);
+  const int N = c->N;
+  G.N = N; G.L = c->L; G.T = c->T;
+  int rc;
+  { const int* t_; if ((rc = upload_int(c, prox, &t_))) return rc; G.prox = t_; }
+  { const int* t_; if ((rc = upload_int(c, proxs, &t_))) return rc; G.proxs = t_; }
+  { const int* t_; if ((rc = upload_int(c, nprox, &t_))) return rc; G.nprox = t_; }
+  { const R* t_; if ((rc = upload_conv<R>(c, g->cs, (size_t)N * 24, &t_))) return rc; G.cs = t_; }
+  { const R* t_; if ((rc = upload_conv<R>(c, g->sn, (size_t)N * 24, &t_))) return rc; G.sn = t_; }
+  { const R* t_; if ((rc = upload_conv<R>(c, g->sidevec_c, (size_t)N * 12, &t_))) return rc; G.svc = t_; }
+  { const R* t_; if ((rc = upload_conv<R>(c, g->sidevec_e, (size_t)N * 12, &t_))) return rc; G.sve = t_; }
+  { const R* t_; if ((rc = upload_conv<R>(c, g->sideln, (size_t)N * 6, &t_))) return rc; G.sideln = t_; }
+  { const R* t_; if ((rc = upload_conv<R>(c, g->area, (size_t)N, &t_))) return rc; G.area = t_; }
+  { const R* t_; if ((rc = upload_conv<R>(c, rarea.data(), (size_t)N, &t_))) return rc; G.rarea = t_; }
+  { const R* t_; if ((rc = upload_conv<R>(c, corio.data(), (size_t)N, &t_))) return rc; G.corio = t_; }
+  { const R* t_; if ((rc = upload_conv<R>(c, grnd.data(), (size_t)N, &t_))) return rc; G.grndspd = t_; }
+  { const R* t_; if ((rc = upload_conv<R>(c, g->hfcoef, (size_t)N * 36, &t_))) return rc; G.hfcoef = t_; }
+  { const double* t_; if ((rc = upload_conv<double>(c, g->area, (size_t)N, &t_))) return rc; G.area_d = t_; }
+  { const R* t_; if ((rc = upload_conv<R>(c, dfflen.data(), (size_t)c->L, &t_))) return rc; G.dfflen = t_; }
+  { const R* t_; if ((rc = upload_conv<R>(c, biharw.data(), (size_t)c->L, &t_))) return rc; G.biharw = t_; }
+  { const R* t_; if ((rc = upload_conv<R>(c, smoo.data(), (size_t)c->L + 1, &t_))) return rc; G.smoo = t_; }
+  { const R* t_; if ((rc = upload_conv<R>(c, c->thetac.data(), (size_t)c->L, &t_))) return rc; G.thetac = t_; }
+  { const R* t_; if ((rc = upload_conv<R>(c, c->dpsig.data(), (size_t)c->L, &t_))) return rc; G.dpsig = t_; }
+  return FIM_OK;
+}
+
+Launch make_launch(fim_ctx* c, int members) {
+  Launch l;
+  l.stream = c->stream;
+  l.members = members;
+  l.sp = c->d_sp;
+  l.flags = c->d_flags;
+  l.counter = &c->launches;
+  return l;
+}
+
+int push_sp(fim_ctx* c) {
+  StepParams tmp = c->h_sp;  // pageable source: staged before the call returns
+  CK(cudaMemcpyAsync(c->d_sp, &tmp, sizeof(StepParams), cudaMemcpyHostToDevice, c->stream), "push step params");
+  return FIM_OK;
+}
+
+int check_launch(fim_ctx* c, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_err(c, FIM_ECUDA, what, e);
+  return FIM_OK;
+}
+
+// host abstart mirror (abstart.F90:33-65, 0-based slots)
+void host_abstart(StepParams& p, int its) {
+  p.its = its;
+  p.nf = (p.nf + 1) % 3;
+  p.of = (p.of + 1) % 3;
+  p.vof = (p.vof + 1) % 3;
+  if (its == 1) { p.ab1 = p.dt; p.ab2 = 0.; p.ab3 = 0.; }
+  if (its == 2) { p.ab1 = p.dt * 1.5; p.ab2 = -p.dt * .5; p.ab3 = 0.; }
+  if (its == 3) { p.ab1 = p.dt * 23. / 12.; p.ab2 = -p.dt * 16. / 12.; p.ab3 = p.dt * 5. / 12.; }
+}
+
+// ---- scratch --------------------------------------------------------------
+int ensure(fim_ctx* c, void** p, size_t elems) {
+  if (*p) return FIM_OK;
+  return dalloc(c, p, elems * c->esz);
+}
+
+int ensure_cnuity(fim_ctx* c, int members) {
+  const size_t NL = (size_t)c->N * c->L * members;
+  int rc;
+  if ((rc = ensure(c, &c->antifx, NL * 6))) return rc;
+  if ((rc = ensure(c, &c->delp_lo, NL))) return rc;
+  if ((rc = ensure(c, &c->p_plus, NL))) return rc;
+  if ((rc = ensure(c, &c->p_mnus, NL))) return rc;
+  if ((rc = ensure(c, &c->r_plus, NL))) return rc;
+  if ((rc = ensure(c, &c->r_mnus, NL))) return rc;
+  return FIM_OK;
+}
+
+int ensure_trcadv(fim_ctx* c, int members) {
+  if (c->t_antiflx) return FIM_OK;
+  const size_t NL = (size_t)c->N * c->L;
+  // bound the tracer chunk so the six scratch fields take at most ~12 GB
+  size_t per_tracer = NL * members * 11 * c->esz;
+  int tch = c->T;
+  while (tch > 1 && per_tracer * tch > (size_t)12 << 30) tch = (tch + 1) / 2;
+  c->tchunk = tch;
+  const size_t n = NL * members * tch;
+  int rc;
+  if ((rc = ensure(c, &c->t_antiflx, n * 6))) return rc;
+  if ((rc = ensure(c, &c->t_trmin, n))) return rc;
+  if ((rc = ensure(c, &c->t_trmax, n))) return rc;
+  if ((rc = ensure(c, &c->t_trcr_lo, n))) return rc;
+  if ((rc = ensure(c, &c->t_rp, n))) return rc;
+  if ((rc = ensure(c, &c->t_rm, n))) return rc;
+  return FIM_OK;
+}
+
+int ensure_momtum(fim_ctx* c, int members) {
+  const size_t NL = (size_t)c->N * c->L * members;
+  int rc;
+  if ((rc = ensure(c, &c->du, NL))) return rc;
+  if ((rc = ensure(c, &c->dv, NL))) return rc;
+  if (c->kn.biharm) {
+    if ((rc = ensure(c, &c->wu, NL))) return rc;
+    if ((rc = ensure(c, &c->wv, NL))) return rc;
+  }
+  return FIM_OK;
+}
+
+int ensure_hybgen(fim_ctx* c, int members) {
+  const size_t NI = (size_t)c->N * (c->L + 1) * members;
+  int rc;
+  if ((rc = ensure(c, &c->exsmo, NI))) return rc;
+  if ((rc = ensure(c, &c->exsmo2, NI))) return rc;
+  return FIM_OK;
+}
+
+int ensure_globsum(fim_ctx* c, int members) {
+  if (c->gs_partial) return FIM_OK;
+  int rc;
+  if ((rc = dalloc(c, (void**)&c->gs_partial, globsum_partials(c->N, c->L, c->T, members) * sizeof(double)))) return rc;
+  if ((rc = dalloc(c, (void**)&c->gs_sums, (size_t)members * (8 + c->T) * sizeof(double)))) return rc;
+  return FIM_OK;
+}
+
+// ---- host-pointer staging -------------------------------------------------
+struct Stager {
+  fim_ctx* c;
+  bool host;
+  std::vector<void*> bufs;
+  struct Out { void* host; void* dev; size_t bytes; };
+  std::vector<Out> outs;
+  int rc = FIM_OK;
+  explicit Stager(fim_ctx* c_) : c(c_), host(c_->cfg.host_pointers != 0) {}
+  ~Stager() {
+    for (void* p : bufs) cudaFreeAsync(p, c->stream);
+  }
+  // intent: 0 in, 1 inout, 2 out
+  template <typename R>
+  R* map(const R* p, size_t n, int intent) {
+    if (!host || p == nullptr) return const_cast<R*>(p);
+    void* d = nullptr;
+    cudaError_t e = cudaMallocAsync(&d, n * sizeof(R) + 16, c->stream);
+    if (e != cudaSuccess) { cudaGetLastError(); rc = set_err(c, FIM_ENOMEM, "stage alloc", e); return nullptr; }
+    bufs.push_back(d);
+    if (intent != 2) {
+      e = cudaMemcpyAsync(d, p, n * sizeof(R), cudaMemcpyHostToDevice, c->stream);
+      if (e != cudaSuccess) { rc = set_err(c, FIM_ECUDA, "stage in", e); return nullptr; }
+    } else {
+      cudaMemsetAsync(d, 0, n * sizeof(R), c->stream);
+    }
+    if (intent != 0) outs.push_back({(void*)p, d, n * sizeof(R)});
+    return (R*)d;
+  }
+  int finish() {
+    if (rc) return rc;
+    for (auto& o : outs) {
+      cudaError_t e = cudaMemcpyAsync(o.host, o.dev, o.bytes, cudaMemcpyDeviceToHost, c->stream);
+      if (e != cudaSuccess) return set_err(c, FIM_ECUDA, "stage out", e);
+    }
+    if (host) {
+      cudaError_t e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) return set_err(c, FIM_ECUDA, "stage sync", e);
+    }
+    return FIM_OK;
+  }
+};
+
+template <typename R>
+int check_prec(fim_ctx* c) {
+  if (!c) return FIM_EINVAL;
+  if ((sizeof(R) == 8) != (c->prec == FIM_PREC_F64))
+    return set_err(c, FIM_EINVAL, "entry-point family does not match the context precision");
+  return FIM_OK;
+}
+
+// ---- per-routine implementations -----------------------------------------
+template <typename R>
+int edgvar_impl(fim_ctx* c, int which, const R* u_vel, const R* v_vel, const R* delp, const R* pres,
+                const R* montg, const R* tracr, R* u_edg, R* v_edg, R* dp_edg, R* lp_edg, R* mont_edg,
+                R* uvsq_edg, R* trc_edg) {
+  int rc = check_prec<R>(c);
+  if (rc) return rc;
+  const size_t NL = (size_t)c->N * c->L, NI = (size_t)c->N * (c->L + 1), NE = NL * 6;
+  Stager s(c);
+  const R* du = s.map(u_vel, NL, 0);
+  const R* dv = s.map(v_vel, NL, 0);
+  const R* ddp = s.map(delp, NL, 0);
+  const R* dpr = s.map(pres, NI, 0);
+  const R* dmo = s.map(montg, NL, 0);
+  const R* dtr = s.map(tracr, NL * c->T, 0);
+  const int io = which == 1 ? 2 : 1;
+  R* due = s.map(u_edg, NE, io);
+  R* dve = s.map(v_edg, NE, io);
+  R* dde = s.map(dp_edg, NE, 1);
+  R* dle = s.map(lp_edg, NE, io);
+  R* dme = s.map(mont_edg, NE, io);
+  R* dqe = s.map(uvsq_edg, NE, io);
+  R* dte = s.map(trc_edg, NE * c->T, 1);
+  if (s.rc) return s.rc;
+  Launch l = make_launch(c, 1);
+  Grid<R>& g = grid_of<R>(c);
+  if (which == 1)
+    launch_edgvar1<R>(l, g, c->str, c->kn.hi_order, du, dv, ddp, dpr, dmo, dtr, due, dve, dde, dle, dme, dqe, dte);
+  else
+    launch_edgvar3<R>(l, g, c->str, ddp, dtr, dde, dte);
+  if ((rc = check_launch(c, which == 1 ? "edgvar1" : "edgvar3"))) return rc;
+  return s.finish();
+}
+
+template <typename R>
+int cnuity_impl(fim_ctx* c, const R* u_velo, const R* v_velo, const R* u_edg, const R* v_edg, const R* dp_edg,
+                const R* lp_edg, R* delp, R* pres, R* exner, R* dp_tndcy, R* dplo_tndcy, R* massfx, R* omega) {
+  int rc = check_prec<R>(c);
+  if (rc) return rc;
+  if ((rc = ensure_cnuity(c, c->M))) return rc;
+  const size_t NL = (size_t)c->N * c->L, NI = (size_t)c->N * (c->L + 1), NE = NL * 6;
+  Stager s(c);
+  const R* a = s.map(u_velo, NL, 0);
+  const R* b = s.map(v_velo, NL, 0);
+  const R* ue = s.map(u_edg, NE, 0);
+  const R* ve = s.map(v_edg, NE, 0);
+  const R* de = s.map(dp_edg, NE, 0);
+  const R* le = s.map(lp_edg, NE, 0);
+  R* dp = s.map(delp, NL, 1);
+  R* pr = s.map(pres, NI, 1);
+  R* ex = s.map(exner, NI, 1);
+  R* dt = s.map(dp_tndcy, NL * 3, 1);
+  R* dl = s.map(dplo_tndcy, NL * 3, 1);
+  R* mf = s.map(massfx, NE * 3, 1);
+  R* om = s.map(omega, NL, 2);
+  if (s.rc) return s.rc;
+  if ((rc = push_sp(c))) return rc;
+  CnuityScratch<R> w{(R*)c->antifx, (R*)c->delp_lo, (R*)c->p_plus, (R*)c->p_mnus, (R*)c->r_plus, (R*)c->r_mnus};
+  launch_cnuity<R>(make_launch(c, 1), grid_of<R>(c), c->str, w, a, b, ue, ve, de, le, dp, pr, ex, dt, dl, mf, om);
+  if ((rc = check_launch(c, "cnuity"))) return rc;
+  return s.finish();
+}
+
+template <typename R>
+int trcadv_impl(fim_ctx* c, const R* trcr_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trclo_tdcy, const R* massfx,
+                const R* delp) {
+  int rc = check_prec<R>(c);
+  if (rc) return rc;
+  if ((rc = ensure_trcadv(c, c->M))) return rc;
+  const size_t NL = (size_t)c->N * c->L, NE = NL * 6;
+  Stager s(c);
+  const R* te = s.map(trcr_edg, NE * c->T, 0);
+  R* tr = s.map(tracr, NL * c->T, 1);
+  R* td = s.map(trcdp, NL * c->T, 1);
+  R* tt = s.map(trc_tdcy, NL * 3 * c->T, 1);
+  R* tl = s.map(trclo_tdcy, NL * 3 * c->T, 1);
+  const R* mf = s.map(massfx, NE * 3, 0);
+  const R* dp = s.map(delp, NL, 0);
+  if (s.rc) return s.rc;
+  if ((rc = push_sp(c))) return rc;
+  TrcadvScratch<R> w{(R*)c->t_antiflx, (R*)c->t_trmin, (R*)c->t_trmax, (R*)c->t_trcr_lo, (R*)c->t_rp, (R*)c->t_rm,
+                     c->tchunk};
+  launch_trcadv<R>(make_launch(c, 1), grid_of<R>(c), c->str, w, te, tr, td, tt, tl, mf, dp);
+  if ((rc = check_launch(c, "trcadv"))) return rc;
+  return s.finish();
+}
+
+template <typename R>
+int momtum_impl(fim_ctx* c, R* u_velo, R* v_velo, const R* exner, R* relvor, const R* u_edg, const R* v_edg,
+                const R* trcr_edg, const R* mont_edg, const R* uvsq_edg, R* u_tndcy, R* v_tndcy, const R* dp3d) {
+  int rc = check_prec<R>(c);
+  if (rc) return rc;
+  if ((rc = ensure_momtum(c, c->M))) return rc;
+  const size_t NL = (size_t)c->N * c->L, NI = (size_t)c->N * (c->L + 1), NE = NL * 6;
+  Stager s(c);
+  R* u = s.map(u_velo, NL, 1);
+  R* v = s.map(v_velo, NL, 1);
+  const R* ex = s.map(exner, NI, 0);
+  R* rv = s.map(relvor, NL, 2);
+  const R* ue = s.map(u_edg, NE, 0);
+  const R* ve = s.map(v_edg, NE, 0);
+  const R* te = s.map(trcr_edg, NE, 0);  // only tracer 1 (theta) is read
+  const R* me = s.map(mont_edg, NE, 0);
+  const R* qe = s.map(uvsq_edg, NE, 0);
+  R* ut = s.map(u_tndcy, NL * 3, 1);
+  R* vt = s.map(v_tndcy, NL * 3, 1);
+  const R* dp = s.map(dp3d, NL, 0);
+  if (s.rc) return s.rc;
+  if ((rc = push_sp(c))) return rc;
+  MomtumScratch<R> w{(R*)c->du, (R*)c->dv, (R*)c->wu, (R*)c->wv};
+  launch_momtum<R>(make_launch(c, 1), grid_of<R>(c), c->str, c->kn, w, u, v, ex, rv, ue, ve, te, me, qe, ut, vt, dp);
+  if ((rc = check_launch(c, "momtum"))) return rc;
+  return s.finish();
+}
+
+template <typename R>
+int hybgen_impl(fim_ctx* c, int its, const R* targt, R* us3d, R* vs3d, R* tr3d, R* sdot, R* ex3d, R* dp3d,
+                R* pr3d) {
+  int rc = check_prec<R>(c);
+  if (rc) return rc;
+  if (c->L > kMaxL) return set_err(c, FIM_EINVAL, "nvl exceeds the column-kernel limit");
+  if ((rc = ensure_hybgen(c, c->M))) return rc;
+  const size_t NL = (size_t)c->N * c->L, NI = (size_t)c->N * (c->L + 1);
+  Stager s(c);
+  const R* tg = targt ? s.map(targt, (size_t)c->L, 0) : grid_of<R>(c).thetac;
+  R* u = s.map(us3d, NL, 1);
+  R* v = s.map(vs3d, NL, 1);
+  R* tr = s.map(tr3d, NL * c->T, 1);
+  R* sd = s.map(sdot, NI, 2);
+  R* ex = s.map(ex3d, NI, 1);
+  R* dp = s.map(dp3d, NL, 1);
+  R* pr = s.map(pr3d, NI, 1);
+  if (s.rc) return s.rc;
+  c->h_sp.its = its;
+  if ((rc = push_sp(c))) return rc;
+  HybgenScratch<R> w{(R*)c->exsmo, (R*)c->exsmo2};
+  launch_hybgen<R>(make_launch(c, 1), grid_of<R>(c), c->str, c->kn, w, tg, u, v, tr, sd, ex, dp, pr);
+  if ((rc = check_launch(c, "hybgen"))) return rc;
+  return s.finish();
+}
+
+template <typename R>
+int hystat_impl(fim_ctx* c, int its, R* ph3d, const R* ex3d, R* mp3d, const R* dp3d, R* tr3d, R* trdp, R* psrf,
+                R* ptdcy) {
+  int rc = check_prec<R>(c);
+  if (rc) return rc;
+  const size_t NL = (size_t)c->N * c->L, NI = (size_t)c->N * (c->L + 1);
+  Stager s(c);
+  R* ph = s.map(ph3d, NI, 1);
+  const R* ex = s.map(ex3d, NI, 0);
+  R* mp = s.map(mp3d, NL, 2);
+  const R* dp = s.map(dp3d, NL, 0);
+  R* tr = s.map(tr3d, NL * c->T, 1);
+  R* td = s.map(trdp, NL * c->T, 2);
+  R* ps = s.map(psrf, (size_t)c->N, 1);
+  R* pt = s.map(ptdcy, (size_t)c->N * 2, 1);
+  if (s.rc) return s.rc;
+  c->h_sp.its = its;
+  if ((rc = push_sp(c))) return rc;
+  launch_hystat<R>(make_launch(c, 1), grid_of<R>(c), c->str, ph, ex, mp, dp, tr, td, ps, pt);
+  if ((rc = check_launch(c, "hystat"))) return rc;
+  return s.finish();
+}
+
+template <typename R>
+int globsum_impl(fim_ctx* c, const R* dp3d, const R* tr, const R* rn2d, const R* rc2d, const R* pr3d,
+                 const R* ex3d, const R* qf2d, double* qtrcr, fim_budget* out) {
+  int rc = check_prec<R>(c);
+  if (rc) return rc;
+  if (c->T > 32) return set_err(c, FIM_EINVAL, "globsum supports at most 32 tracers");
+  if ((rc = ensure_globsum(c, c->M))) return rc;
+  const size_t NL = (size_t)c->N * c->L, NI = (size_t)c->N * (c->L + 1);
+  Stager s(c);
+  const R* dp = s.map(dp3d, NL, 0);
+  const R* t = s.map(tr, NL * c->T, 0);
+  const R* rn = s.map(rn2d, (size_t)c->N, 0);
+  const R* rcp = s.map(rc2d, (size_t)c->N, 0);
+  const R* pr = s.map(pr3d, NI, 0);
+  const R* ex = s.map(ex3d, NI, 0);
+  const R* qf = s.map(qf2d, (size_t)c->N, 0);
+  if (s.rc) return s.rc;
+  if ((rc = push_sp(c))) return rc;
+  launch_globsum<R>(make_launch(c, 1), grid_of<R>(c), c->str, dp, t, rn, rcp, pr, ex, qf, c->gs_partial, c->gs_sums);
+  if ((rc = check_launch(c, "globsum"))) return rc;
+  if ((rc = s.finish())) return rc;
+  std::vector<double> h(8 + c->T);
+  CK(cudaMemcpyAsync(h.data(), c->gs_sums, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "globsum out");
+  CK(cudaStreamSynchronize(c->stream), "globsum sync");
+  if (qtrcr) for (int q = 0; q < c->T; q++) qtrcr[q] = h[8 + q];
+  if (out) {
+    out->qmass = h[0]; out->qmsqv = h[1]; out->qmsqw = h[2]; out->qmso3 = h[3];
+    out->qmste = h[4]; out->qmstr = h[5]; out->qmstrn = h[6]; out->qmstrc = h[7];
+  }
+  return FIM_OK;
+}
+
+// ---- fused step over the device-resident state ---------------------------
+template <typename R>
+R* F(fim_state* st, int f) { return (R*)st->f[f]; }
+
+template <typename R>
+int enqueue_step(fim_ctx* c, fim_state* st) {
+  const int M = c->M;
+  Launch l = make_launch(c, M);
+  Grid<R>& g = grid_of<R>(c);
+  const Strides& s = c->str;
+  launch_step_begin(l, c->d_sp);
+  launch_edgvar1<R>(l, g, s, c->kn.hi_order, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_DP3D),
+                    F<R>(st, FIM_PR3D), F<R>(st, FIM_MP3D), F<R>(st, FIM_TR3D), F<R>(st, FIM_U_EDG),
+                    F<R>(st, FIM_V_EDG), F<R>(st, FIM_DP_EDG), F<R>(st, FIM_LP_EDG), F<R>(st, FIM_MONT_EDG),
+                    F<R>(st, FIM_UVSQ_EDG), F<R>(st, FIM_TRC_EDG));
+  if (c->kn.hi_order)
+    launch_edgvar3<R>(l, g, s, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), F<R>(st, FIM_DP_EDG), F<R>(st, FIM_TRC_EDG));
+  CnuityScratch<R> cw{(R*)c->antifx, (R*)c->delp_lo, (R*)c->p_plus, (R*)c->p_mnus, (R*)c->r_plus, (R*)c->r_mnus};
+  launch_cnuity<R>(l, g, s, cw, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_U_EDG), F<R>(st, FIM_V_EDG),
+                   F<R>(st, FIM_DP_EDG), F<R>(st, FIM_LP_EDG), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D),
+                   F<R>(st, FIM_EX3D), F<R>(st, FIM_DP_TDCY), F<R>(st, FIM_DPL_TDCY), F<R>(st, FIM_MASSFX),
+                   F<R>(st, FIM_WS3D));
+  TrcadvScratch<R> tw{(R*)c->t_antiflx, (R*)c->t_trmin, (R*)c->t_trmax, (R*)c->t_trcr_lo, (R*)c->t_rp,
+                      (R*)c->t_rm, c->tchunk};
+  launch_trcadv<R>(l, g, s, tw, F<R>(st, FIM_TRC_EDG), F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP),
+                   F<R>(st, FIM_TRC_TDCY), F<R>(st, FIM_TRL_TDCY), F<R>(st, FIM_MASSFX), F<R>(st, FIM_DP3D));
+  MomtumScratch<R> mw{(R*)c->du, (R*)c->dv, (R*)c->wu, (R*)c->wv};
+  launch_momtum<R>(l, g, s, c->kn, mw, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_EX3D),
+                   F<R>(st, FIM_RELVOR), F<R>(st, FIM_U_EDG), F<R>(st, FIM_V_EDG), F<R>(st, FIM_TRC_EDG),
+                   F<R>(st, FIM_MONT_EDG), F<R>(st, FIM_UVSQ_EDG), F<R>(st, FIM_U_TDCY), F<R>(st, FIM_V_TDCY),
+                   F<R>(st, FIM_DP3D));
+  HybgenScratch<R> hw{(R*)c->exsmo, (R*)c->exsmo2};
+  launch_hybgen<R>(l, g, s, c->kn, hw, g.thetac, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_TR3D),
+                   F<R>(st, FIM_SDOT), F<R>(st, FIM_EX3D), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D));
+  launch_hystat<R>(l, g, s, F<R>(st, FIM_PH3D), F<R>(st, FIM_EX3D), F<R>(st, FIM_MP3D), F<R>(st, FIM_DP3D),
+                   F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP), F<R>(st, FIM_PSRF), F<R>(st, FIM_PTDCY));
+  launch_globsum<R>(l, g, s, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), (const R*)nullptr, (const R*)nullptr,
+                    F<R>(st, FIM_PR3D), F<R>(st, FIM_EX3D), (const R*)nullptr, c->gs_partial, st->sums);
+  return FIM_OK;
+}
+
+int ensure_all(fim_ctx* c) {
+  int rc;
+  if ((rc = ensure_cnuity(c, c->M))) return rc;
+  if ((rc = ensure_trcadv(c, c->M))) return rc;
+  if ((rc = ensure_momtum(c, c->M))) return rc;
+  if ((rc = ensure_hybgen(c, c->M))) return rc;
+  if ((rc = ensure_globsum(c, c->M))) return rc;
+  return FIM_OK;
+}
+
+template <typename R>
+int state_init_impl(fim_ctx* c, fim_state* st) {
+  int rc;
+  if ((rc = ensure_all(c))) return rc;
+  Launch l = make_launch(c, c->M);
+  Grid<R>& g = grid_of<R>(c);
+  c->h_sp.its = 0;
+  if ((rc = push_sp(c))) return rc;
+  HybgenScratch<R> hw{(R*)c->exsmo, (R*)c->exsmo2};
+  launch_hybgen<R>(l, g, c->str, c->kn, hw, g.thetac, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_TR3D),
+                   F<R>(st, FIM_SDOT), F<R>(st, FIM_EX3D), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D));
+  launch_prdp_from_ex<R>(l, g, c->str, F<R>(st, FIM_EX3D), F<R>(st, FIM_PR3D), F<R>(st, FIM_DP3D));
+  const size_t M = c->M;
+  CK(cudaMemsetAsync(st->f[FIM_PSRF], 0, M * st->count[FIM_PSRF] * c->esz, c->stream), "zero psrf");
+  CK(cudaMemsetAsync(st->f[FIM_PTDCY], 0, M * st->count[FIM_PTDCY] * c->esz, c->stream), "zero ptdcy");
+  launch_hystat<R>(l, g, c->str, F<R>(st, FIM_PH3D), F<R>(st, FIM_EX3D), F<R>(st, FIM_MP3D), F<R>(st, FIM_DP3D),
+                   F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP), F<R>(st, FIM_PSRF), F<R>(st, FIM_PTDCY));
+  const int zero[] = {FIM_U_TDCY, FIM_V_TDCY, FIM_DP_TDCY, FIM_DPL_TDCY, FIM_TRC_TDCY, FIM_TRL_TDCY, FIM_MASSFX};
+  for (int f : zero) CK(cudaMemsetAsync(st->f[f], 0, M * st->count[f] * c->esz, c->stream), "zero tendencies");
+  // dyn_init.F90:1092-1094: nf,of,vof = 0,2,1 (Fortran), one abstart before use
+  c->h_sp.nf = -1;
+  c->h_sp.of = 1;
+  c->h_sp.vof = 0;
+  c->h_sp.ab1 = c->h_sp.ab2 = c->h_sp.ab3 = 0.;
+  if ((rc = push_sp(c))) return rc;
+  if ((rc = check_launch(c, "state init"))) return rc;
+  CK(cudaStreamSynchronize(c->stream), "state init sync");
+  return FIM_OK;
+}
+
+}  // namespace
+
+// ============================== extern "C" ==================================
+extern "C" {
+
+int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out) {
+  if (!g || !cfg || !out) return FIM_EINVAL;
+  *out = nullptr;
+  if (cfg->nvl < 4 || cfg->nvl > kMaxL || cfg->ntra < 4 || cfg->ntra > 32 || g->nip < 12 || cfg->dt <= 0.)
+    return FIM_EINVAL;
+  if (cfg->flux_conserv_schm != 1) return FIM_ENOTSUP;
+  if (cfg->pure_sig) return FIM_ENOTSUP;
+  if (cfg->remap_optn < 1 || cfg->remap_optn > 3) return FIM_EINVAL;
+  if (cfg->precision != FIM_PREC_F64 && cfg->precision != FIM_PREC_F32) return FIM_EINVAL;
+  if (!cfg->thetac || !cfg->dpsig || !g->prox || !g->proxs || !g->nprox || !g->area || !g->cs || !g->sn ||
+      !g->sidevec_c || !g->sidevec_e || !g->sideln || !g->hfcoef || !g->lat)
+    return FIM_EINVAL;
+  fim_ctx* c = new (std::nothrow) fim_ctx;
+  if (!c) return FIM_ENOMEM;
+  c->cfg = *cfg;
+  c->prec = cfg->precision;
+  c->esz = c->prec == FIM_PREC_F64 ? 8 : 4;
+  c->N = g->nip;
+  c->L = cfg->nvl;
+  c->T = cfg->ntra;
+  c->M = cfg->members < 1 ? 1 : cfg->members;
+  c->thetac.assign(cfg->thetac, cfg->thetac + c->L);
+  c->dpsig.assign(cfg->dpsig, cfg->dpsig + c->L);
+  c->str = make_strides(c->N, c->L, c->T);
+  const int N = c->N, L = c->L;
+  // 0-based index tables; validate the Fortran numbering
+  std::vector<int> prox(N * 6), proxs(N * 6), nprox(N);
+  for (int i = 0; i < N; i++) {
+    nprox[i] = g->nprox[i];
+    if (nprox[i] != 5 && nprox[i] != 6) { delete c; return FIM_EINVAL; }
+    for (int e = 0; e < 6; e++) {
+      int p = g->prox[i * 6 + e] - 1;
+      if (p < 0 || p >= N) { delete c; return FIM_EINVAL; }
+      prox[i * 6 + e] = p;
+      int q = g->proxs[i * 6 + e];
+      proxs[i * 6 + e] = (e < nprox[i]) ? q - 1 : -1;
+      if (e < nprox[i] && (q < 1 || q > 6)) { delete c; return FIM_EINVAL; }
+    }
+  }
+  // derived fields (dyn_init.F90:309-338,752-767)
+  std::vector<double> rarea(N), corio(N), grnd(N), dfflen(L), biharw(L), smoo(L + 1, 0.0);
+  for (int i = 0; i < N; i++) {
+    corio[i] = kOmegx2 * std::sin(g->lat[i]);
+    rarea[i] = 1. / g->area[i];
+    grnd[i] = kEarthRad * 2. * kPi * std::cos(g->lat[i]) / 86164.;
+  }
+  const int ndamp = (int)(0.1 * L);
+  for (int k = 1; k <= L; k++) {
+    double wgt = std::max(0., (double)(k - L + ndamp) / (double)ndamp);
+    dfflen[k - 1] = cfg->dt * (cfg->veldff_bkgnd * (1. - wgt) + std::max(cfg->veldff_bkgnd, cfg->veldff_boost) * wgt);
+  }
+  double dmax = dfflen[0];
+  for (int k = 1; k < L; k++) dmax = std::max(dmax, dfflen[k]);
+  for (int k = cfg->kbl + 2; k <= L; k++) {
+    double d1 = (double)((cfg->kbl + 1) - k), d2 = (double)((L + 1) - k);
+    smoo[k - 1] = cfg->dt * cfg->intfc_smooth * (d1 * d1 / (9. + d1 * d1)) * (d2 * d2 / (9. + d2 * d2));
+  }
+  int biharm = 0;
+  for (int k = 1; k <= L; k++) {
+    double w = 0.;
+    if (k >= cfg->biharm_frst && k <= cfg->biharm_last) w = 1.;
+    if (cfg->biharm_frst > 1 && cfg->biharm_frst < L) w = std::max(0., std::min(1., .5 + .2 * (double)(k - cfg->biharm_frst)));
+    if (cfg->biharm_last > 1 && cfg->biharm_last < L) w = std::max(0., std::min(1., .5 + .2 * (double)(cfg->biharm_last - k)));
+    biharw[k - 1] = w;
+    if (w > 0.) biharm = 1;
+    dfflen[k - 1] = dfflen[k - 1] * (1. + 4. * w * w);
+  }
+  c->kn.kbl = cfg->kbl;
+  c->kn.miglim = cfg->miglim;
+  c->kn.remap_optn = cfg->remap_optn;
+  c->kn.hi_order = cfg->hi_order_flux_comp ? 1 : 0;
+  c->kn.intfc_smooth = cfg->intfc_smooth;
+  c->kn.slak = cfg->slak;
+  c->kn.ptop = cfg->ptop;
+  c->kn.thktop = cfg->thktop;
+  c->kn.rleigh = cfg->rleigh;
+  c->kn.rlthresh = cfg->rlthresh;
+  c->kn.rltaper = cfg->rltaper;
+  c->kn.dfflen_max = dmax;
+  c->kn.biharm = biharm;
+
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return FIM_ECUDA;
+  }
+  int rc = (c->prec == FIM_PREC_F64)
+               ? build_grid<double>(c, g, rarea, corio, grnd, dfflen, biharw, smoo, prox, proxs, nprox)
+               : build_grid<float>(c, g, rarea, corio, grnd, dfflen, biharw, smoo, prox, proxs, nprox);
+  if (!rc) rc = dalloc(c, (void**)&c->d_sp, sizeof(StepParams));
+  if (!rc) rc = dalloc(c, (void**)&c->d_flags, sizeof(int) * c->M);
+  if (!rc) {
+    c->h_sp = StepParams{0, -1, 1, 0, 0., 0., 0., cfg->dt};
+    if (cudaMemset(c->d_flags, 0, sizeof(int) * c->M) != cudaSuccess) rc = FIM_ECUDA;
+    if (!rc) rc = push_sp(c);
+  }
+  if (rc) {
+    fim_ctx_destroy(c);
+    return rc;
+  }
+  *out = c;
+  return FIM_OK;
+}
+
+int fim_ctx_destroy(fim_ctx* c) {
+  if (!c) return FIM_EINVAL;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (void* p : c->owned) cudaFree(p);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return FIM_OK;
+}
+
+const char* fim_ctx_last_error(const fim_ctx* c) { return c ? c->err.c_str() : "null context"; }
+void* fim_ctx_stream(fim_ctx* c) { return c ? (void*)c->stream : nullptr; }
+int64_t fim_launch_count(const fim_ctx* c) { return c ? c->launches : -1; }
+
+int fim_get_ab(const fim_ctx* c, int* nf, int* of, int* vof, double* ab1, double* ab2, double* ab3) {
+  if (!c) return FIM_EINVAL;
+  if (nf) *nf = c->h_sp.nf + 1;
+  if (of) *of = c->h_sp.of + 1;
+  if (vof) *vof = c->h_sp.vof + 1;
+  if (ab1) *ab1 = c->h_sp.ab1;
+  if (ab2) *ab2 = c->h_sp.ab2;
+  if (ab3) *ab3 = c->h_sp.ab3;
+  return FIM_OK;
+}
+
+int fim_set_ab(fim_ctx* c, int nf, int of, int vof, double ab1, double ab2, double ab3) {
+  if (!c || nf < 1 || nf > 3 || of < 1 || of > 3 || vof < 1 || vof > 3) return FIM_EINVAL;
+  c->h_sp.nf = nf - 1;
+  c->h_sp.of = of - 1;
+  c->h_sp.vof = vof - 1;
+  c->h_sp.ab1 = ab1;
+  c->h_sp.ab2 = ab2;
+  c->h_sp.ab3 = ab3;
+  return push_sp(c);
+}
+
+int fim_abstart(fim_ctx* c, int its, int its_start, int* nf, int* of, int* vof, double* adbash1, double* adbash2,
+                double* adbash3) {
+  (void)its_start;
+  if (!c || its < 1) return FIM_EINVAL;
+  host_abstart(c->h_sp, its);
+  int rc = push_sp(c);
+  if (rc) return rc;
+  return fim_get_ab(c, nf, of, vof, adbash1, adbash2, adbash3);
+}
+
+#define EDGVAR_ARGS_R(R)                                                                                      \
+  fim_ctx *c, int its, const R *u_vel, const R *v_vel, const R *delp, const R *pres, const R *exner,       \
+      const R *geop, const R *montg, const R *tracr, R *u_edg, R *v_edg, R *dp_edg, R *lp_edg, R *geop_edg, \
+      R *mont_edg, R *uvsq_edg, R *trc_edg
+
+int fim_edgvar1_r8(EDGVAR_ARGS_R(double)) {
+  (void)its; (void)exner; (void)geop; (void)geop_edg;
+  return edgvar_impl<double>(c, 1, u_vel, v_vel, delp, pres, montg, tracr, u_edg, v_edg, dp_edg, lp_edg, mont_edg,
+                             uvsq_edg, trc_edg);
+}
+int fim_edgvar1_r4(EDGVAR_ARGS_R(float)) {
+  (void)its; (void)exner; (void)geop; (void)geop_edg;
+  return edgvar_impl<float>(c, 1, u_vel, v_vel, delp, pres, montg, tracr, u_edg, v_edg, dp_edg, lp_edg, mont_edg,
+                            uvsq_edg, trc_edg);
+}
+int fim_edgvar3_r8(EDGVAR_ARGS_R(double)) {
+  (void)its; (void)exner; (void)geop; (void)geop_edg;
+  return edgvar_impl<double>(c, 3, u_vel, v_vel, delp, pres, montg, tracr, u_edg, v_edg, dp_edg, lp_edg, mont_edg,
+                             uvsq_edg, trc_edg);
+}
+int fim_edgvar3_r4(EDGVAR_ARGS_R(float)) {
+  (void)its; (void)exner; (void)geop; (void)geop_edg;
+  return edgvar_impl<float>(c, 3, u_vel, v_vel, delp, pres, montg, tracr, u_edg, v_edg, dp_edg, lp_edg, mont_edg,
+                            uvsq_edg, trc_edg);
+}
+
+int fim_cnuity_r8(fim_ctx* c, int its, const double* u_velo, const double* v_velo, const double* u_edg,
+                  const double* v_edg, const double* dp_edg, const double* lp_edg, double* delp, double* pres,
+                  double* exner, double* dp_tndcy, double* dplo_tndcy, double* massfx, double* omega) {
+  (void)its;
+  return cnuity_impl<double>(c, u_velo, v_velo, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner, dp_tndcy,
+                             dplo_tndcy, massfx, omega);
+}
+int fim_cnuity_r4(fim_ctx* c, int its, const float* u_velo, const float* v_velo, const float* u_edg,
+                  const float* v_edg, const float* dp_edg, const float* lp_edg, float* delp, float* pres,
+                  float* exner, float* dp_tndcy, float* dplo_tndcy, float* massfx, float* omega) {
+  (void)its;
+  return cnuity_impl<float>(c, u_velo, v_velo, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner, dp_tndcy,
+                            dplo_tndcy, massfx, omega);
+}
+
+int fim_trcadv_r8(fim_ctx* c, int its, const double* trcr_edg, double* tracr, double* trcdp, double* trc_tdcy,
+                  double* trclo_tdcy, const double* massfx, const double* delp) {
+  (void)its;
+  return trcadv_impl<double>(c, trcr_edg, tracr, trcdp, trc_tdcy, trclo_tdcy, massfx, delp);
+}
+int fim_trcadv_r4(fim_ctx* c, int its, const float* trcr_edg, float* tracr, float* trcdp, float* trc_tdcy,
+                  float* trclo_tdcy, const float* massfx, const float* delp) {
+  (void)its;
+  return trcadv_impl<float>(c, trcr_edg, tracr, trcdp, trc_tdcy, trclo_tdcy, massfx, delp);
+}
+
+int fim_momtum_r8(fim_ctx* c, int its, double* u_velo, double* v_velo, const double* exner, double* relvor,
+                  const double* u_edg, const double* v_edg, const double* trcr_edg, const double* geop_edg,
+                  const double* mont_edg, const double* uvsq_edg, double* u_tndcy, double* v_tndcy,
+                  const double* dp3d) {
+  (void)its; (void)geop_edg;
+  return momtum_impl<double>(c, u_velo, v_velo, exner, relvor, u_edg, v_edg, trcr_edg, mont_edg, uvsq_edg, u_tndcy,
+                             v_tndcy, dp3d);
+}
+int fim_momtum_r4(fim_ctx* c, int its, float* u_velo, float* v_velo, const float* exner, float* relvor,
+                  const float* u_edg, const float* v_edg, const float* trcr_edg, const float* geop_edg,
+                  const float* mont_edg, const float* uvsq_edg, float* u_tndcy, float* v_tndcy, const float* dp3d) {
+  (void)its; (void)geop_edg;
+  return momtum_impl<float>(c, u_velo, v_velo, exner, relvor, u_edg, v_edg, trcr_edg, mont_edg, uvsq_edg, u_tndcy,
+                            v_tndcy, dp3d);
+}
+
+int fim_hybgen_r8(fim_ctx* c, int its, const double* targt, double* us3d, double* vs3d, double* tr3d, double* sdot,
+                  double* ex3d, double* dp3d, double* pr3d) {
+  return hybgen_impl<double>(c, its, targt, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d);
+}
+int fim_hybgen_r4(fim_ctx* c, int its, const float* targt, float* us3d, float* vs3d, float* tr3d, float* sdot,
+                  float* ex3d, float* dp3d, float* pr3d) {
+  return hybgen_impl<float>(c, its, targt, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d);
+}
+
+int fim_hystat_r8(fim_ctx* c, int its, double* ph3d, const double* ex3d, double* mp3d, const double* dp3d,
+                  double* tr3d, double* trdp, double* psrf, double* ptdcy) {
+  return hystat_impl<double>(c, its, ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy);
+}
+int fim_hystat_r4(fim_ctx* c, int its, float* ph3d, const float* ex3d, float* mp3d, const float* dp3d, float* tr3d,
+                  float* trdp, float* psrf, float* ptdcy) {
+  return hystat_impl<float>(c, its, ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy);
+}
+
+int fim_globsum_r8(fim_ctx* c, int its, const double* dp3d, const double* tr, const double* rn2d, const double* rc2d,
+                   const double* pr3d, const double* ex3d, const double* qf2d, double* qtrcr, fim_budget* out) {
+  (void)its;
+  return globsum_impl<double>(c, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d, qtrcr, out);
+}
+int fim_globsum_r4(fim_ctx* c, int its, const float* dp3d, const float* tr, const float* rn2d, const float* rc2d,
+                   const float* pr3d, const float* ex3d, const float* qf2d, double* qtrcr, fim_budget* out) {
+  (void)its;
+  return globsum_impl<float>(c, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d, qtrcr, out);
+}
+
+// ---- state ------------------------------------------------------------------
+int fim_state_alloc(fim_ctx* c, fim_state** out) {
+  if (!c || !out) return FIM_EINVAL;
+  fim_state* st = new (std::nothrow) fim_state;
+  if (!st) return FIM_ENOMEM;
+  const size_t N = c->N, L = c->L, T = c->T, NL = N * L, NI = N * (L + 1);
+  const size_t cnt[FIM_NFIELDS] = {
+      NL, NL, NL, NI, NI, NI, NL, NL * T,          // us vs dp pr ex ph mp tr
+      NL * T, NL * 3, NL * 3, NL * 3, NL * 3,      // trdp u_tdcy v_tdcy dp_tdcy dpl_tdcy
+      NL * 3 * T, NL * 3 * T, NL * 6 * 3,          // trc_tdcy trl_tdcy massfx
+      NL, NI, NL, N, N * 2,                        // ws sdot relvor psrf ptdcy
+      NL * 6, NL * 6, NL * 6, NL * 6, NL * 6, NL * 6, NL * 6,  // edge fields
+      NL * 6 * T};
+  for (int f = 0; f < FIM_NFIELDS; f++) {
+    st->count[f] = cnt[f];
+    int rc = dalloc(c, &st->f[f], cnt[f] * c->M * c->esz);
+    if (rc) { delete st; return rc; }
+    cudaMemsetAsync(st->f[f], 0, cnt[f] * c->M * c->esz, c->stream);
+  }
+  int rc = dalloc(c, (void**)&st->sums, (size_t)c->M * (8 + c->T) * sizeof(double));
+  if (rc) { delete st; return rc; }
+  if ((rc = ensure_all(c))) { delete st; return rc; }
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) { delete st; return set_err(c, FIM_ECUDA, "state alloc"); }
+  *out = st;
+  return FIM_OK;
+}
+
+int fim_state_free(fim_ctx* c, fim_state* st) {
+  if (!c || !st) return FIM_EINVAL;
+  cudaStreamSynchronize(c->stream);
+  if (st->graph) cudaGraphExecDestroy(st->graph);
+  for (int f = 0; f < FIM_NFIELDS; f++) {
+    for (auto it = c->owned.begin(); it != c->owned.end(); ++it)
+      if (*it == st->f[f]) { cudaFree(*it); c->owned.erase(it); break; }
+  }
+  for (auto it = c->owned.begin(); it != c->owned.end(); ++it)
+    if (*it == st->sums) { cudaFree(*it); c->owned.erase(it); break; }
+  delete st;
+  return FIM_OK;
+}
+
+int fim_state_field(fim_ctx* c, fim_state* st, int field, int member, void** dptr, int64_t* count) {
+  if (!c || !st || field < 0 || field >= FIM_NFIELDS || member < 0 || member >= c->M) return FIM_EINVAL;
+  if (dptr) *dptr = (char*)st->f[field] + (size_t)member * st->count[field] * c->esz;
+  if (count) *count = (int64_t)st->count[field];
+  return FIM_OK;
+}
+
+int fim_state_upload(fim_ctx* c, fim_state* st, int field, int member, const void* host) {
+  void* d;
+  int64_t n;
+  int rc = fim_state_field(c, st, field, member, &d, &n);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(d, host, (size_t)n * c->esz, cudaMemcpyHostToDevice, c->stream), "state upload");
+  return FIM_OK;
+}
+
+int fim_state_download(fim_ctx* c, fim_state* st, int field, int member, void* host) {
+  void* d;
+  int64_t n;
+  int rc = fim_state_field(c, st, field, member, &d, &n);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(host, d, (size_t)n * c->esz, cudaMemcpyDeviceToHost, c->stream), "state download");
+  return FIM_OK;
+}
+
+int fim_state_init(fim_ctx* c, fim_state* st) {
+  if (!c || !st) return FIM_EINVAL;
+  return c->prec == FIM_PREC_F64 ? state_init_impl<double>(c, st) : state_init_impl<float>(c, st);
+}
+
+int fim_step(fim_ctx* c, fim_state* st, int its, int use_graph) {
+  if (!c || !st || its < 1) return FIM_EINVAL;
+  int rc = ensure_all(c);
+  if (rc) return rc;
+  if (c->h_sp.its != its - 1) {
+    c->h_sp.its = its - 1;
+    if ((rc = push_sp(c))) return rc;
+  }
+  if (use_graph) {
+    if (!st->graph) {
+      // the step is its-invariant: every step-dependent scalar is read from
+      // the device parameter block that k_step_begin advances
+      cudaGraph_t graph;
+      long long before = c->launches;
+      CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+      rc = c->prec == FIM_PREC_F64 ? enqueue_step<double>(c, st) : enqueue_step<float>(c, st);
+      cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+      if (rc) return rc;
+      if (e != cudaSuccess) return set_err(c, FIM_ECUDA, "end capture", e);
+      st->graph_kernels = c->launches - before;
+      c->launches = before;
+      e = cudaGraphInstantiate(&st->graph, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) { st->graph = nullptr; return set_err(c, FIM_ECUDA, "graph instantiate", e); }
+    }
+    CK(cudaGraphLaunch(st->graph, c->stream), "graph launch");
+    c->launches += st->graph_kernels;
+  } else {
+    rc = c->prec == FIM_PREC_F64 ? enqueue_step<double>(c, st) : enqueue_step<float>(c, st);
+    if (rc) return rc;
+    if ((rc = check_launch(c, "step"))) return rc;
+  }
+  host_abstart(c->h_sp, its);
+  return FIM_OK;
+}
+
+int fim_state_budget(fim_ctx* c, fim_state* st, int member, double* qtrcr, fim_budget* out) {
+  if (!c || !st || member < 0 || member >= c->M) return FIM_EINVAL;
+  std::vector<double> h(8 + c->T);
+  CK(cudaMemcpyAsync(h.data(), st->sums + (size_t)member * (8 + c->T), h.size() * sizeof(double),
+                     cudaMemcpyDeviceToHost, c->stream), "budget");
+  CK(cudaStreamSynchronize(c->stream), "budget sync");
+  if (qtrcr) for (int q = 0; q < c->T; q++) qtrcr[q] = h[8 + q];
+  if (out) {
+    out->qmass = h[0]; out->qmsqv = h[1]; out->qmsqw = h[2]; out->qmso3 = h[3];
+    out->qmste = h[4]; out->qmstr = h[5]; out->qmstrn = h[6]; out->qmstrc = h[7];
+  }
+  return FIM_OK;
+}
+
+int fim_check(fim_ctx* c, fim_state* st, int* flags) {
+  (void)st;
+  if (!c) return FIM_EINVAL;
+  std::vector<int> h(c->M);
+  CK(cudaMemcpyAsync(h.data(), c->d_flags, sizeof(int) * c->M, cudaMemcpyDeviceToHost, c->stream), "flags");
+  CK(cudaMemsetAsync(c->d_flags, 0, sizeof(int) * c->M, c->stream), "flags reset");
+  CK(cudaStreamSynchronize(c->stream), "flags sync");
+  int f = 0;
+  for (int v : h) f |= v;
+  if (flags) *flags = f;
+  return (f & kFlagBadDp) ? FIM_ENUMERIC : FIM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,749 @@
+// Column kernels of the FIM dynamics step: hybgen (regrid_1d, dffusn_lev,
+// remap_1d with restp_1d, equilb, inflate, pcwise), hystat, globsum.
+//
+// hybgen's column logic is serial in k with data-dependent branches, so it
+// runs one thread per column over per-thread column arrays; the 1-ring
+// interface smoothing between regrid and remap is a (level, cell) stencil.
+// hystat's bottom-up Montgomery/geopotential recursion is a warp scan in FP64.
+// globsum accumulates per thread (FP64, or float-float compensated sums in the
+// FP32 build, whose error is that of an FP64 sum) and reduces per block into a
+// deterministic partial buffer.
+#include "fim_internal.h"
+
+namespace fim {
+
+template <typename R> __device__ __forceinline__ R cmax(R a, R b) { return a > b ? a : b; }
+template <typename R> __device__ __forceinline__ R cmin(R a, R b) { return a < b ? a : b; }
+template <typename R> __device__ __forceinline__ R cabs(R a) { return a < R(0) ? -a : a; }
+
+constexpr int kColBlock = 128;
+constexpr int kBlock2 = 256;
+inline unsigned nblocks(long long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+// ---------------------------------------------------------------- hybgen --
+// restp_1d (hybgen.F90:792-890)
+template <typename R, int ML>
+__device__ void restp_1d(const R* thold, const R* pkold, int kold, R* thnew, R* pknew, const R* targt,
+                         int knew, int* bad) {
+  R oldth[ML];
+  oldth[kold - 1] = thold[kold - 1];
+  for (int k = kold; k >= 2; k--) oldth[k - 2] = cmin(oldth[k - 1], thold[k - 2]);
+  for (int k = 0; k < knew; k++) thnew[k] = targt[k];
+  thnew[0] = cmin(cmin(oldth[0], oldth[kold - 1]), targt[0]);
+  thnew[knew - 1] = cmax(cmax(oldth[0], oldth[kold - 1]), targt[knew - 1]);
+  pknew[0] = pkold[0];
+  pknew[knew] = pkold[kold];
+  R colint = R(0), colscl = R(0), cloutt = R(0);
+  for (int k = 0; k < kold; k++) {
+    colint = colint + oldth[k] * (pkold[k + 1] - pkold[k]);
+    colscl = colscl + cabs(oldth[k] * (pkold[k + 1] - pkold[k]));
+  }
+  int ko = 0;
+  for (int k = 0; k < knew - 1; k++) {
+    R pinteg = R(0), tha, thb = thnew[k];
+    for (;;) {
+      tha = thb;
+      thb = cmin(thnew[k + 1], cmax(thnew[k], oldth[ko]));
+      pinteg = pinteg + pkold[ko] * (thb - tha);
+      if (oldth[ko] < thnew[k + 1]) {
+        if (ko < kold - 1) { ko++; continue; }
+        tha = thb;
+        thb = thnew[k + 1];
+        pinteg = pinteg + pkold[kold] * (thb - tha);
+      }
+      break;
+    }
+    pknew[k + 1] = pknew[k];
+    if (thnew[k + 1] > thnew[k]) pknew[k + 1] = pinteg / (thnew[k + 1] - thnew[k]);
+    cloutt = cloutt + thnew[k] * (pknew[k + 1] - pknew[k]);
+  }
+  cloutt = cloutt + thnew[knew - 1] * (pknew[knew] - pknew[knew - 1]);
+  if (sizeof(R) == 8 && cabs(cloutt - colint) > cmax(R(1.e-33), R(1.e-6) * colscl)) *bad = 1;
+}
+
+// equilb scenario 1 (hybgen.F90:1316-1363); in place on pres
+template <typename R>
+__device__ void equilb(const R* thet, R* pnew, int kk, R slak) {
+  const R thin = R(kRd) / R(kP1000);
+  for (int k = 3; k <= kk - 2; k++) {
+    if (pnew[k - 3] > pnew[0] - thin) continue;
+    const R dp1 = pnew[k - 3] - pnew[k - 2];
+    const R dp2 = pnew[k - 2] - pnew[k - 1];
+    const R dp3 = pnew[k - 1] - pnew[k];
+    const R dp4 = pnew[k] - pnew[k + 1];
+    const R dp5 = pnew[k + 1] - pnew[k + 2];
+    const R th2 = thet[k - 2], th3 = thet[k - 1], th4 = thet[k];
+    if (dp2 > dp1 && dp4 > dp5) {
+      const R goal = R(.5) * (dp3 + cmin(dp2, dp4));
+      if (dp2 > goal && dp4 > goal) {
+        R dis3 = cmin(dp2 - goal, goal - dp3) * slak;
+        R dis4 = cmin(dp4 - goal, goal - dp3) * slak;
+        if (th3 > th2 && th4 > th3) {
+          const R ratio = (th4 - th3) / (th3 - th2);
+          if (ratio > R(1)) dis4 = dis3 / ratio;
+          else dis3 = dis4 * ratio;
+        }
+        pnew[k - 1] = pnew[k - 1] + dis3;
+        pnew[k] = pnew[k] - dis4;
+      }
+    }
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ R cushn(R a, R b) {
+  const R m = cmin(a, R(2) * b);
+  return R(.25) * (m * m) / b + cmax(a, R(2) * b) - b;
+}
+
+// inflate (hybgen.F90:893-1007)
+template <typename R>
+__device__ void inflate(const Knobs& kn, const R* dpsig, int L, R psurf, R* exner) {
+  const R thin = R(kRd) / R(kP1000);
+  const R rd = R(kRd), p1000 = R(kP1000), cp = R(kCp);
+  R dpsum = R(0);
+  const R extop = cp * pow(R(kn.ptop) / p1000, rd / cp);
+  const R top = R(.2);
+  const R shrink = cmin(R(1), (psurf / p1000 - top) / (R(1) - top));
+  int last = 1;
+  for (int k = 1; k <= L - 1; k++) {
+    R dp0 = rd * dpsig[k - 1] / p1000 * shrink;
+    dpsum = dpsum + dp0;
+    const R exold = exner[k];
+    if (k <= kn.kbl) {
+      last = k + 1;
+      exner[k] = exner[k - 1] - dp0;
+    } else {
+      if (k > last) {
+        dp0 = dp0 / cmin(R(10), R(1.25) * R(ldexp(1.0, k - last)));
+        dp0 = cmax(dp0, rd * R(100) / p1000);
+      }
+      const R dp1 = cushn(cmax(R(0), exner[k - 1] - cmin(exold, exner[0] - dpsum)), dp0);
+      if (exner[k - 1] - dp1 < exold - thin) {
+        if (k == last) last = k + 1;
+        exner[k] = cmax(extop, exner[k - 1] - dp1);
+      }
+    }
+  }
+  if (kn.thktop > 0.) {
+    const R thk = R(kn.thktop);
+    for (int k = L; k >= 2; k--) {
+      R q = exner[k - 1] / cp;
+      q = q * q * sqrt(q);
+      const R dk = R(.25) * R(L - k);
+      const R dp0 = rd * thk / p1000 * (R(1) / (R(1) + dk * dk)) / q;
+      const R exold = exner[k - 1];
+      const R dp1 = cushn(cmax(R(0), exold - exner[k]), dp0);
+      if (exner[k] + dp1 > exold + thin) exner[k - 1] = exner[k] + dp1;
+      if (exner[k - 1] < exner[k - 2] - dp0) break;
+    }
+  }
+}
+
+// regrid_1d (hybgen.F90:207-512, hybrid-isentropic branch) for one column:
+// thcol (L) and excol (L+1) are overwritten; excol ends as the new Exner fcn.
+template <typename R, int ML>
+__device__ void regrid_1d(const Knobs& kn, const R* targt, const R* dpsig, int L, int its, R* thcol, R* excol,
+                          R prcol0, int* bad) {
+  const R thin = R(kRd) / R(kP1000), tolrnce = R(0.001), dffudt = R(.1);
+  const R eqlb_slak = R(.1) * R(its) / (R(10) + R(its));
+  R exwrk[ML + 1], exnew[ML + 1], thnew[ML], heatfx[ML];
+  for (int k = 0; k < L; k++)
+    if (excol[k] < excol[k + 1] - thin) excol[k + 1] = excol[k];
+  for (int k = L - 2; k >= 0; k--) thcol[k] = cmin(thcol[k], thcol[k + 1]);
+  for (int k = 0; k <= L; k++) exwrk[k] = excol[k];
+  const R tt = targt[L - 1];
+  for (int k = L; k >= 2; k--) {
+    if (thcol[k - 1] <= tt + tolrnce) break;
+    const R wgt1 = cmax(R(0), exwrk[k - 2] - exwrk[k - 1]);
+    const R wgt2 = cmax(thin, exwrk[k - 1] - exwrk[k]);
+    const R tr = (thcol[k - 2] * wgt1 + thcol[k - 1] * wgt2) / (wgt1 + wgt2);
+    if (tr > tt - tolrnce) {
+      exwrk[k - 1] = exwrk[L];
+      for (int k1 = k - 1; k1 <= L; k1++) thcol[k1 - 1] = tr;
+    } else {
+      exwrk[k - 1] = cmin(exwrk[k - 2], cmax(exwrk[k], (exwrk[k - 1] * (thcol[k - 1] - thcol[k - 2]) +
+                                                         exwrk[k] * (tt - thcol[k - 1])) /
+                                                            (tt - thcol[k - 2])));
+      for (int k1 = k; k1 <= L; k1++) thcol[k1 - 1] = tt;
+      break;
+    }
+  }
+  restp_1d<R, ML>(thcol, exwrk, L, thnew, exnew, targt, L, bad);
+  heatfx[L - 1] = R(0);
+  heatfx[0] = R(0);
+  const R grv = R(kGrvity);
+  for (int iter = 1; iter <= 3; iter++) {
+    for (int k = 0; k <= L; k++) exwrk[k] = exnew[k];
+    for (int k = 2; k <= L - 1; k++) {
+      heatfx[k - 1] = R(0);
+      if (exwrk[k - 1] < exwrk[0] - R(.01) && exwrk[k] > exwrk[L] + R(.01)) {
+        const R cnv = grv / targt[k - 1];
+        heatfx[k - 1] = dffudt * cnv * cnv * R(.5) * (targt[k] - targt[k - 2]) / cmax(R(.03) * cnv, exwrk[k - 1] - exwrk[k]);
+      }
+    }
+    for (int k = 1; k <= L - 1; k++) {
+      if (exwrk[k] < exwrk[0] - R(.01) && exwrk[k] > exwrk[L] + R(.01))
+        exnew[k] = cmax(exwrk[k + 1], cmin(exwrk[k - 1], exwrk[k] + (heatfx[k] - heatfx[k - 1]) / (targt[k] - targt[k - 1])));
+    }
+    bool event = false;
+    for (int k = 2; k <= L + 1; k++)
+      if (exnew[k - 1] > exnew[k - 2] + thin) event = true;
+    if (!event) break;
+  }
+  equilb<R>(thnew, exnew, L, eqlb_slak);
+  inflate<R>(kn, dpsig, L, prcol0, exnew);
+  for (int k = 0; k <= L; k++) excol[k] = exnew[k];
+}
+
+// pcwise (hybgen.F90:1010-1279): 1-D PCM/PLM/PPM remap of yold from cell
+// boundaries xold to xnew.  Returns true when the column-integral check fails
+// (evaluated in the FP64 build only).
+template <typename R, int ML>
+__device__ bool pcwise(int kk, const R* xold, const R* yold, const R* xnew, R* ynew, int miglim, int remap_optn) {
+  R delz[ML + 1], fco[ML], fcn[ML], vertfx[ML + 1], fldnew[ML], a[ML], b[ML], cc[ML];
+  const R athird = R(1) / R(3), small = R(1.e-22);
+  const bool flip = !(xold[0] < xold[kk]);
+  for (int k = 0; k <= kk; k++) delz[k] = flip ? (-xnew[k]) - (-xold[k]) : xnew[k] - xold[k];
+  for (int k = 0; k < kk; k++) {
+    fco[k] = flip ? cmax(R(0), (-xold[k + 1]) - (-xold[k])) : cmax(R(0), xold[k + 1] - xold[k]);
+    fcn[k] = flip ? cmax(R(0), (-xnew[k + 1]) - (-xnew[k])) : cmax(R(0), xnew[k + 1] - xnew[k]);
+  }
+  R bfore = R(0), colscl = R(0);
+  for (int k = 0; k < kk; k++) {
+    bfore = bfore + yold[k] * fco[k];
+    colscl = colscl + cabs(yold[k] * fco[k]);
+  }
+  for (int k = 0; k < kk; k++) fldnew[k] = yold[k];
+  for (int k = kk - 2; k >= 0; k--) fldnew[k] = (fldnew[k] * fco[k] + fldnew[k + 1] * small) / (fco[k] + small);
+  for (int k = 1; k < kk; k++) fldnew[k] = (fldnew[k] * fco[k] + fldnew[k - 1] * small) / (fco[k] + small);
+  a[0] = fldnew[0]; b[0] = R(0); cc[0] = R(0);
+  a[kk - 1] = fldnew[kk - 1]; b[kk - 1] = R(0); cc[kk - 1] = R(0);
+  for (int k = 1; k < kk - 1; k++) {
+    if (remap_optn == 1) {
+      a[k] = fldnew[k]; b[k] = R(0); cc[k] = R(0);
+    } else if (remap_optn == 2) {
+      a[k] = fldnew[k];
+      b[k] = R(0);
+      if (fldnew[k] <= cmin(fldnew[k - 1], fldnew[k + 1]) || fldnew[k] >= cmax(fldnew[k - 1], fldnew[k + 1])) {
+        b[k] = R(0);
+      } else if ((fldnew[k + 1] - fldnew[k - 1]) * (fldnew[k - 1] + fldnew[k + 1] - R(2) * fldnew[k]) > R(0)) {
+        b[k] = fldnew[k] - fldnew[k - 1];
+      } else {
+        b[k] = fldnew[k + 1] - fldnew[k];
+      }
+      cc[k] = R(0);
+    } else {
+      const R yl = (cmax(small, fco[k - 1]) * fldnew[k] + cmax(small, fco[k]) * fldnew[k - 1]) /
+                   (cmax(small, fco[k - 1]) + cmax(small, fco[k]));
+      const R yr = (cmax(small, fco[k + 1]) * fldnew[k] + cmax(small, fco[k]) * fldnew[k + 1]) /
+                   (cmax(small, fco[k + 1]) + cmax(small, fco[k]));
+      a[k] = R(1.5) * fldnew[k] - R(.25) * (yl + yr);
+      b[k] = yr - yl;
+      cc[k] = R(6) * (R(.5) * (yl + yr) - fldnew[k]);
+      if (cabs(yr - yl) < R(6) * cabs(R(.5) * (yl + yr) - fldnew[k])) {
+        if (cabs(yr - yl) > R(2) * cabs(R(.5) * (yl + yr) - fldnew[k])) {
+          if ((yr - yl) * (R(.5) * (yl + yr) - fldnew[k]) > R(0)) {
+            a[k] = R(.25) * (R(3) * fldnew[k] + yl);
+            cc[k] = R(3) * (fldnew[k] - yl);
+            b[k] = cc[k];
+          } else {
+            a[k] = R(.25) * (R(3) * fldnew[k] + yr);
+            cc[k] = R(3) * (fldnew[k] - yr);
+            b[k] = -cc[k];
+          }
+        } else {
+          a[k] = fldnew[k]; b[k] = R(0); cc[k] = R(0);
+        }
+      }
+    }
+  }
+  for (int k = 1; k < kk; k++) {
+    R slab = R(0), amount = R(0);
+    vertfx[k] = R(0);
+    const R dz = delz[k];
+    if (miglim == 1) {
+      if (dz > R(0)) {
+        const int lyr = k;
+        if (fco[lyr] > R(0)) {
+          const R dslab = cmin(slab + fco[lyr], dz) - cmin(slab, dz);
+          const R dx = dslab / fco[lyr];
+          const R fcdx = a[lyr] + b[lyr] * R(.5) * (dx - R(1)) + cc[lyr] * (R(.25) - dx * (R(.5) - dx * athird));
+          amount = amount + fcdx * dslab;
+          slab = slab + dslab;
+        }
+      } else if (dz < R(0)) {
+        const int lyr = k - 1;
+        if (fco[lyr] > R(0)) {
+          const R dslab = cmin(slab + fco[lyr], -dz) - cmin(slab, -dz);
+          const R dx = dslab / fco[lyr];
+          const R fcdx = a[lyr] + b[lyr] * R(.5) * (R(1) - dx) + cc[lyr] * (R(.25) - dx * (R(.5) - dx * athird));
+          amount = amount + fcdx * dslab;
+          slab = slab + dslab;
+        }
+      }
+    } else {
+      if (dz > R(0)) {
+        int lyr = k - 1;
+        for (;;) {
+          lyr = lyr + 1;
+          if (slab >= dz) break;
+          if (fco[lyr] > R(0)) {
+            const R dslab = cmin(slab + fco[lyr], dz) - cmin(slab, dz);
+            const R dx = dslab / fco[lyr];
+            const R fcdx = a[lyr] + b[lyr] * R(.5) * (dx - R(1)) + cc[lyr] * (R(.25) - dx * (R(.5) - dx * athird));
+            amount = amount + fcdx * dslab;
+            slab = slab + dslab;
+          }
+          if (!(lyr < kk - 1)) break;
+        }
+      } else if (dz < R(0)) {
+        int lyr = k;
+        for (;;) {
+          lyr = lyr - 1;
+          if (slab >= -dz) break;
+          if (fco[lyr] > R(0)) {
+            const R dslab = cmin(slab + fco[lyr], -dz) - cmin(slab, -dz);
+            const R dx = dslab / fco[lyr];
+            const R fcdx = a[lyr] + b[lyr] * R(.5) * (R(1) - dx) + cc[lyr] * (R(.25) - dx * (R(.5) - dx * athird));
+            amount = amount + fcdx * dslab;
+            slab = slab + dslab;
+          }
+          if (!(lyr > 0)) break;
+        }
+      }
+    }
+    if (slab != R(0)) vertfx[k] = -dz * amount / slab;
+  }
+  vertfx[0] = R(0);
+  vertfx[kk] = R(0);
+  R after = R(0);
+  for (int k = 0; k < kk; k++) {
+    const R amount = fldnew[k] * fco[k] - (vertfx[k + 1] - vertfx[k]);
+    ynew[k] = (amount + fldnew[k] * small) / (fcn[k] + small);
+    after = after + amount;
+  }
+  return sizeof(R) == 8 && cabs(bfore - after) > cmax(R(1.e-33), R(1.e-11) * colscl);
+}
+
+template <typename R, int ML>
+__global__ void __launch_bounds__(kColBlock) k_regrid(Grid<R> g, Strides s, Knobs kn,
+    const StepParams* __restrict__ sp, const R* __restrict__ targt, const R* __restrict__ tr3d,
+    const R* __restrict__ ex3d, const R* __restrict__ pr3d, R* __restrict__ exsmo, int* __restrict__ flags) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int N = g.N, L = g.L, L1 = L + 1;
+  if (i >= N) return;
+  const size_t m = blockIdx.y;
+  tr3d += m * s.tr; ex3d += m * s.intf; pr3d += m * s.intf; exsmo += m * s.intf;
+  R thcol[ML], excol[ML + 1];
+  for (int k = 0; k < L; k++) thcol[k] = tr3d[(size_t)i * L + k];
+  for (int k = 0; k <= L; k++) excol[k] = ex3d[(size_t)i * L1 + k];
+  int bad = 0;
+  regrid_1d<R, ML>(kn, targt, g.dpsig, L, sp->its, thcol, excol, pr3d[(size_t)i * L1], &bad);
+  for (int k = 0; k <= L; k++) exsmo[(size_t)i * L1 + k] = excol[k];
+  if (bad) atomicOr(flags + m, kFlagColumnIntegral);
+}
+
+// dffusn_lev (dffusn.F90:37-58 with dffusn_lev.exe) on interfaces kbl+2..nvl,
+// out of place so every cell reads the unsmoothed neighbours.
+template <typename R>
+__global__ void __launch_bounds__(kBlock2) k_dffusn_lev(Grid<R> g, Strides s, int k1, int k2,
+    const R* __restrict__ fld, R* __restrict__ out) {
+  const int N = g.N, L1 = g.L + 1;
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= N * L1) return;
+  const int i = gid / L1, k = gid - i * L1;
+  const size_t m = blockIdx.y;
+  fld += m * s.intf; out += m * s.intf;
+  const size_t c = (size_t)i * L1 + k;
+  R val = fld[c];
+  if (k >= k1 && k <= k2) {
+    R flxdv = R(0);
+    const int np = g.nprox[i];
+    for (int e = 0; e < np; e++) {
+      const int ipx = g.prox[i * 6 + e];
+      flxdv = flxdv + (val - fld[(size_t)ipx * L1 + k]) * g.sideln[i * 6 + e];
+    }
+    const R factor = -g.smoo[k] * g.rarea[i];
+    val = val + flxdv * factor;
+  }
+  out[c] = val;
+}
+
+// remap_1d (hybgen.F90:515-789) followed by the hybgen bookkeeping
+// (hybgen.F90:189-191): new u, v, tracers, Exner, pressure, thickness, sdot.
+template <typename R, int ML>
+__global__ void __launch_bounds__(kColBlock) k_remap(Grid<R> g, Strides s, Knobs kn,
+    const StepParams* __restrict__ sp, const R* __restrict__ targt, const R* __restrict__ exsmo,
+    R* __restrict__ us3d, R* __restrict__ vs3d, R* __restrict__ tr3d, R* __restrict__ sdot,
+    R* __restrict__ ex3d, R* __restrict__ dp3d, R* __restrict__ pr3d, int* __restrict__ flags) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
+  if (i >= N) return;
+  const size_t m = blockIdx.y;
+  exsmo += m * s.intf; us3d += m * s.cell; vs3d += m * s.cell; tr3d += m * s.tr; sdot += m * s.intf;
+  ex3d += m * s.intf; dp3d += m * s.cell; pr3d += m * s.intf;
+  const int its = sp->its;
+  const R cp = R(kCp), rd = R(kRd), p1000 = R(kP1000), small = R(1.e-6);
+  R exold[ML + 1], exnew[ML + 1], prcol[ML + 1], prnew[ML + 1], pk1col[ML + 1], pk1new[ML + 1];
+  R yold[ML], ynew[ML], dpcol[ML];
+  for (int k = 0; k <= L; k++) {
+    exold[k] = ex3d[(size_t)i * L1 + k];
+    prcol[k] = pr3d[(size_t)i * L1 + k];
+    exnew[k] = exsmo[(size_t)i * L1 + k];
+  }
+  for (int k = 0; k <= L; k++) pk1col[k] = exold[k] * prcol[k] / cp;
+  if (kn.intfc_smooth > 0.) inflate<R>(kn, g.dpsig, L, prcol[0], exnew);
+  if (its > 0) {
+    const R sl = R(kn.slak);
+    for (int k = 0; k <= L; k++) exnew[k] = sl * exnew[k] + (R(1) - sl) * exold[k];
+  }
+  const int mg = kn.miglim;
+  if (mg > 0) {
+    for (int k = 1 + mg; k <= L + 1 - mg; k++)
+      exnew[k - 1] = cmax(R(.0001) * exold[k - 1] + R(.9999) * exold[k - 1 + mg],
+                          cmin(R(.0001) * exold[k - 1] + R(.9999) * exold[k - 1 - mg], exnew[k - 1]));
+    for (int k = 2; k <= mg; k++) {
+      exnew[k - 1] = cmin(exold[0], exnew[k - 1]);
+      exnew[L - k] = cmax(exold[L], exnew[L - k]);
+    }
+  }
+  for (int k = L; k >= 0; k--) prnew[k] = p1000 * pow(exnew[k] / cp, cp / rd);
+  for (int k = 0; k < L; k++) dpcol[k] = prnew[k] - prnew[k + 1];
+  for (int k = 0; k <= L; k++) pk1new[k] = exnew[k] * prnew[k] / cp;
+  prnew[L] = prcol[L];
+  pk1new[L] = pk1col[L];
+  prnew[0] = prcol[0];
+  pk1new[0] = pk1col[0];
+  bool bad = false;
+  // u and v
+  for (int f = 0; f < 2; f++) {
+    R* col = (f == 0 ? us3d : vs3d) + (size_t)i * L;
+    for (int k = 0; k < L; k++) yold[k] = col[k];
+    bad |= pcwise<R, ML>(L, prcol, yold, prnew, ynew, mg, kn.remap_optn);
+    for (int k = 0; k < L; k++) col[k] = ynew[k];
+  }
+  // tracers 2..ntra in pressure, with the optional massless-layer fill
+  for (int t = 1; t < T; t++) {
+    R* col = tr3d + ((size_t)t * N + i) * L;
+    for (int k = 0; k < L; k++) yold[k] = col[k];
+    bad |= pcwise<R, ML>(L, prcol, yold, prnew, ynew, mg, kn.remap_optn);
+    if (kn.thktop == 0.) {
+      for (int k = 3; k <= L; k++) {
+        const R qq = R(1) / (dpcol[k - 1] + small);
+        ynew[k - 1] = (ynew[k - 1] * dpcol[k - 1] + ynew[k - 2] * small) * qq;
+      }
+    }
+    for (int k = 0; k < L; k++) col[k] = ynew[k];
+  }
+  // potential temperature in p^(kappa+1), then the target redistribution
+  {
+    R* col = tr3d + (size_t)i * L;
+    for (int k = 0; k < L; k++) yold[k] = col[k];
+    bad |= pcwise<R, ML>(L, pk1col, yold, pk1new, ynew, mg, kn.remap_optn);
+    for (int k = L; k >= 3; k--) {
+      const R dplo = cmax(pk1new[k - 2] - pk1new[k - 1], pk1new[0] * small);
+      const R dpup = cmax(pk1new[k - 1] - pk1new[k], pk1new[0] * small);
+      const R tha = ynew[k - 2], thb = ynew[k - 1];
+      const R devilo = (tha - targt[k - 2]) * dplo;
+      const R deviup = (thb - targt[k - 1]) * dpup;
+      if (deviup > R(0) && devilo < R(0)) {
+        ynew[k - 2] = tha + cmin(deviup, -devilo) / dplo;
+        ynew[k - 1] = thb - cmin(deviup, -devilo) / dpup;
+      } else if (deviup < R(0) && devilo > R(0)) {
+        ynew[k - 2] = tha - cmin(devilo, -deviup) / dplo;
+        ynew[k - 1] = thb + cmin(devilo, -deviup) / dpup;
+      }
+    }
+    if (sizeof(R) == 8) {
+      R colin = R(0), clout = R(0), colscl = R(0);
+      for (int k = 0; k < L; k++) {
+        colin = colin + yold[k] * (pk1col[k] - pk1col[k + 1]);
+        clout = clout + ynew[k] * (pk1new[k] - pk1new[k + 1]);
+        colscl = colscl + cabs(yold[k] * (pk1col[k] - pk1col[k + 1]));
+      }
+      if (cabs(clout - colin) > cmax(R(1.e-33), R(2.e-6) * colscl)) bad = true;
+    }
+    for (int k = 0; k < L; k++) col[k] = ynew[k];
+  }
+  for (int k = 0; k < L; k++)
+    if (exnew[k] < exnew[k + 1]) exnew[k + 1] = exnew[k];
+  for (int k = 0; k <= L; k++) {
+    sdot[(size_t)i * L1 + k] = exnew[k] - exold[k];
+    ex3d[(size_t)i * L1 + k] = exnew[k];
+    pr3d[(size_t)i * L1 + k] = prnew[k];
+  }
+  for (int k = 0; k < L; k++) dp3d[(size_t)i * L + k] = dpcol[k];
+  if (bad) atomicOr(flags + m, kFlagColumnIntegral);
+}
+
+// ---------------------------------------------------------------- hystat --
+// hystat (hystat.F90:53-109): one warp per column; surface pressure sum and
+// the bottom-up Montgomery potential / geopotential recursion are FP64 warp
+// scans; humidity floors and tracer x thickness per level.
+template <typename R>
+__global__ void __launch_bounds__(kBlock2) k_hystat(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
+    R* __restrict__ ph3d, const R* __restrict__ ex3d, R* __restrict__ mp3d, const R* __restrict__ dp3d,
+    R* __restrict__ tr3d, R* __restrict__ trdp, R* __restrict__ psrf, R* __restrict__ ptdcy) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
+  if (warp >= N) return;
+  const int i = warp;
+  const size_t m = blockIdx.y;
+  ph3d += m * s.intf; ex3d += m * s.intf; mp3d += m * s.cell; dp3d += m * s.cell; tr3d += m * s.tr;
+  trdp += m * s.tr; psrf += m * s.col; ptdcy += m * 2 * s.col;
+  const int its = sp->its;
+  const size_t NL = (size_t)N * L;
+  // surface pressure: sum of all layer thicknesses
+  double ps = 0.0;
+  for (int k = lane; k < L; k += 32) ps += (double)dp3d[(size_t)i * L + k];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) ps += __shfl_xor_sync(0xffffffffu, ps, off);
+  if (lane == 0) {
+    const R work = psrf[i];
+    const R pn = R(ps);
+    psrf[i] = pn;
+    if (its > 0) ptdcy[(size_t)(its % 2) * N + i] = pn - work;
+  }
+  double carry = 0.0;
+  const double ph0 = (double)ph3d[(size_t)i * L1];
+  for (int base = 0; base < L; base += 32) {
+    const int k = base + lane;
+    const bool act = k < L;
+    double term = 0.0, th = 0.0, exk1 = 0.0;
+    if (act) {
+      th = (double)tr3d[(size_t)i * L + k];
+      const double ex = (double)ex3d[(size_t)i * L1 + k];
+      exk1 = (double)ex3d[(size_t)i * L1 + k + 1];
+      if (k == 0) term = ex * th + ph0;
+      else term = ex * (th - (double)tr3d[(size_t)i * L + k - 1]);
+    }
+    double sc = term;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const double a = __shfl_up_sync(0xffffffffu, sc, off);
+      if (lane >= off) sc += a;
+    }
+    const double mp = carry + sc;
+    if (act) {
+      mp3d[(size_t)i * L + k] = R(mp);
+      ph3d[(size_t)i * L1 + k + 1] = R(mp - th * exk1);
+    }
+    carry += __shfl_sync(0xffffffffu, sc, 31);
+  }
+  const R qvmin = R(kQvmin), qwmin = R(kQwmin);
+  for (int k = lane; k < L; k += 32) {
+    const size_t c = (size_t)i * L + k;
+    const R dp = dp3d[c];
+    for (int t = 0; t < T; t++) {
+      R x = tr3d[(size_t)t * NL + c];
+      if (t == 1) { x = cmax(qvmin, x); tr3d[(size_t)t * NL + c] = x; }
+      if (t == 2) { x = cmax(qwmin, x); tr3d[(size_t)t * NL + c] = x; }
+      trdp[(size_t)t * NL + c] = x * dp;
+    }
+  }
+}
+
+// --------------------------------------------------------------- globsum --
+// float-float compensated accumulator (Knuth two-sum), ~48-bit significand
+struct FF {
+  float hi, lo;
+  __device__ void add(float x) {
+    const float s = hi + x;
+    const float bp = s - hi;
+    const float err = (hi - (s - bp)) + (x - bp);
+    hi = s;
+    lo += err;
+  }
+  __device__ double value() const { return (double)hi + (double)lo; }
+};
+template <typename R> struct Acc;
+template <> struct Acc<double> {
+  double v = 0.0;
+  __device__ void add(double x) { v += x; }
+  __device__ double value() const { return v; }
+};
+template <> struct Acc<float> {
+  FF f{0.f, 0.f};
+  __device__ void add(float x) { f.add(x); }
+  __device__ double value() const { return f.value(); }
+};
+
+constexpr int kMaxT = 32;
+constexpr int kGsBlocks = 152 * 4;
+
+// Level sums: slot 0 = sum(area*dp), slot 1+t = sum(area*dp*tr_t).
+template <typename R>
+__global__ void __launch_bounds__(kBlock2) k_globsum_levels(Grid<R> g, Strides s, const R* __restrict__ dp3d,
+    const R* __restrict__ tr, double* __restrict__ partial) {
+  const int N = g.N, L = g.L, T = g.T;
+  const size_t m = blockIdx.y;
+  dp3d += m * s.cell; tr += m * s.tr;
+  const size_t NL = (size_t)N * L;
+  Acc<R> acc[kMaxT + 1];
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < NL; idx += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / L);
+    const R ad = g.area[i] * dp3d[idx];
+    acc[0].add(ad);
+#pragma unroll
+    for (int t = 0; t < kMaxT; t++)
+      if (t < T) acc[1 + t].add(ad * tr[(size_t)t * NL + idx]);
+  }
+  __shared__ double red[kBlock2 / 32];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  double* out = partial + (m * gridDim.x + blockIdx.x) * (kMaxT + 1);
+#pragma unroll
+  for (int q = 0; q < kMaxT + 1; q++) {
+    if (q > T) break;
+    double v = acc[q].value();
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (lane == 0) red[wib] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < kBlock2 / 32; w++) t += red[w];
+      out[q] = t;
+    }
+    __syncthreads();
+  }
+}
+
+// Column sums (globsum.F90:81-85) and the final reduction of the partials.
+template <typename R>
+__global__ void k_globsum_final(Grid<R> g, Strides s, const StepParams* __restrict__ sp, const R* __restrict__ tr,
+    const R* __restrict__ rn2d, const R* __restrict__ rc2d, const R* __restrict__ pr3d, const R* __restrict__ ex3d,
+    const R* __restrict__ qf2d, const double* __restrict__ partial, int nblk, double* __restrict__ sums) {
+  const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
+  const size_t m = blockIdx.x;
+  tr += m * s.tr; pr3d += m * s.intf; ex3d += m * s.intf;
+  __shared__ double red[4][kBlock2];
+  double sr = 0., src = 0., srn = 0., se = 0.;
+  const double dt = sp->dt, rdcp = kRd / kCp;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const double a = g.area_d[i];
+    const double rn = rn2d ? (double)rn2d[m * s.col + i] : 0.0;
+    const double rc = rc2d ? (double)rc2d[m * s.col + i] : 0.0;
+    const double qf = qf2d ? (double)qf2d[m * s.col + i] : 0.0;
+    sr += a * rn;
+    src += a * rc;
+    srn += a * (rn - rc);
+    const double den = (double)pr3d[(size_t)i * L1] / (rdcp * (double)ex3d[(size_t)i * L1] * (double)tr[(size_t)i * L]);
+    se += a * den * qf * dt / (1.25 * 2.5e6);
+  }
+  red[0][threadIdx.x] = sr; red[1][threadIdx.x] = src; red[2][threadIdx.x] = srn; red[3][threadIdx.x] = se;
+  __syncthreads();
+  double* out = sums + m * (8 + T);
+  if (threadIdx.x < 4) {
+    double t = 0.;
+    for (int q = 0; q < (int)blockDim.x; q++) t += red[threadIdx.x][q];
+    // qmstr (sumr), qmstrn (sumrn), qmstrc (sumrc), qmste (sume)
+    const int slot = threadIdx.x == 0 ? 5 : threadIdx.x == 1 ? 7 : threadIdx.x == 2 ? 6 : 4;
+    out[slot] = t;
+  }
+  for (int q = threadIdx.x; q <= T; q += blockDim.x) {
+    double t = 0.;
+    for (int b = 0; b < nblk; b++) t += partial[(m * nblk + b) * (kMaxT + 1) + q];
+    if (q == 0) out[0] = t / kGrvity;
+    else {
+      out[8 + (q - 1)] = t;
+      if (q == 2) out[1] = t / kGrvity;
+      if (q == 3) out[2] = t / kGrvity;
+      if (q == 4) out[3] = t / kGrvity;
+    }
+  }
+}
+
+// pressure and thickness from Exner (dyn_init.F90:895-906)
+template <typename R>
+__global__ void __launch_bounds__(kBlock2) k_prdp_from_ex(Grid<R> g, Strides s, const R* __restrict__ ex3d,
+    R* __restrict__ pr3d, R* __restrict__ dp3d) {
+  const int N = g.N, L = g.L, L1 = L + 1;
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= N * L1) return;
+  const int i = gid / L1, k = gid - i * L1;
+  const size_t m = blockIdx.y;
+  ex3d += m * s.intf; pr3d += m * s.intf; dp3d += m * s.cell;
+  const R cp = R(kCp), rd = R(kRd), p1000 = R(kP1000);
+  const R p = p1000 * pow(ex3d[(size_t)i * L1 + k] / cp, cp / rd);
+  pr3d[(size_t)i * L1 + k] = p;
+  if (k < L) {
+    const R pu = p1000 * pow(ex3d[(size_t)i * L1 + k + 1] / cp, cp / rd);
+    dp3d[(size_t)i * L + k] = p - pu;
+  }
+}
+
+#define COUNT(l) do { if ((l).counter) ++*(l).counter; } while (0)
+
+template <typename R>
+void launch_hybgen(const Launch& l, const Grid<R>& g, const Strides& s, const Knobs& kn, const HybgenScratch<R>& w,
+                   const R* targt, R* us3d, R* vs3d, R* tr3d, R* sdot, R* ex3d, R* dp3d, R* pr3d) {
+  dim3 gc(nblocks(g.N, kColBlock), l.members);
+  if (g.L <= 64) {
+    k_regrid<R, 64><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, tr3d, ex3d, pr3d, w.exsmo, l.flags);
+  } else {
+    k_regrid<R, kMaxL><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, tr3d, ex3d, pr3d, w.exsmo, l.flags);
+  }
+  COUNT(l);
+  const R* ex_in = w.exsmo;
+  if (kn.intfc_smooth > 0.) {
+    dim3 gs(nblocks((long long)g.N * (g.L + 1), kBlock2), l.members);
+    // Fortran levels kbl+2..nvl -> 0-based interfaces kbl+1..nvl-1
+    k_dffusn_lev<R><<<gs, kBlock2, 0, l.stream>>>(g, s, kn.kbl + 1, g.L - 1, w.exsmo, w.exsmo2);
+    COUNT(l);
+    ex_in = w.exsmo2;
+  }
+  if (g.L <= 64) {
+    k_remap<R, 64><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d,
+                                                    dp3d, pr3d, l.flags);
+  } else {
+    k_remap<R, kMaxL><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d,
+                                                       dp3d, pr3d, l.flags);
+  }
+  COUNT(l);
+}
+
+template <typename R>
+void launch_hystat(const Launch& l, const Grid<R>& g, const Strides& s, R* ph3d, const R* ex3d, R* mp3d,
+                   const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy) {
+  dim3 gw(nblocks((long long)g.N * 32, kBlock2), l.members);
+  k_hystat<R><<<gw, kBlock2, 0, l.stream>>>(g, s, l.sp, ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy);
+  COUNT(l);
+}
+
+size_t globsum_partials(int N, int L, int T, int members) {
+  (void)N; (void)L; (void)T;
+  return (size_t)members * kGsBlocks * (kMaxT + 1);
+}
+
+template <typename R>
+void launch_globsum(const Launch& l, const Grid<R>& g, const Strides& s, const R* dp3d, const R* tr,
+                    const R* rn2d, const R* rc2d, const R* pr3d, const R* ex3d, const R* qf2d,
+                    double* partial, double* sums) {
+  dim3 gl(kGsBlocks, l.members);
+  k_globsum_levels<R><<<gl, kBlock2, 0, l.stream>>>(g, s, dp3d, tr, partial);
+  COUNT(l);
+  k_globsum_final<R><<<l.members, kBlock2, 0, l.stream>>>(g, s, l.sp, tr, rn2d, rc2d, pr3d, ex3d, qf2d, partial,
+                                                           kGsBlocks, sums);
+  COUNT(l);
+}
+
+template <typename R>
+void launch_prdp_from_ex(const Launch& l, const Grid<R>& g, const Strides& s, const R* ex3d, R* pr3d, R* dp3d) {
+  dim3 gs(nblocks((long long)g.N * (g.L + 1), kBlock2), l.members);
+  k_prdp_from_ex<R><<<gs, kBlock2, 0, l.stream>>>(g, s, ex3d, pr3d, dp3d);
+  COUNT(l);
+}
+
+#define INSTANTIATE(R)                                                                                       \
+  template void launch_hybgen<R>(const Launch&, const Grid<R>&, const Strides&, const Knobs&,               \
+                                 const HybgenScratch<R>&, const R*, R*, R*, R*, R*, R*, R*, R*);            \
+  template void launch_hystat<R>(const Launch&, const Grid<R>&, const Strides&, R*, const R*, R*, const R*, \
+                                 R*, R*, R*, R*);                                                           \
+  template void launch_globsum<R>(const Launch&, const Grid<R>&, const Strides&, const R*, const R*,        \
+                                  const R*, const R*, const R*, const R*, const R*, double*, double*);      \
+  template void launch_prdp_from_ex<R>(const Launch&, const Grid<R>&, const Strides&, const R*, R*, R*);
+INSTANTIATE(float)
+INSTANTIATE(double)
+
+}  // namespace fim

@@ -1,0 +1,155 @@
+// Internal declarations shared by the kernels and the C-ABI layer.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+namespace fim {
+
+// Physical constants of FIMsrc/cntl/module_constants.F90:14-27.
+constexpr double kPi = 3.14159265;
+constexpr double kEarthRad = 6371220.;
+constexpr double kOmegx2 = 1.4584e-4;
+constexpr double kGrvity = 9.80665;
+constexpr double kP1000 = 100000.;
+constexpr double kCp = 1004.6855;
+constexpr double kRd = 287.0586;
+constexpr double kQvmin = 1.e-10;
+constexpr double kQwmin = 1.e-10;
+
+// Largest layer count the column kernels accept.
+constexpr int kMaxL = 128;
+
+// Step-dependent scalars that the reference keeps in module_variables
+// (nf, of, vof, adbash1..3) plus the step number used by hybgen and hystat.
+// They live in device memory so a captured step graph can be replayed.
+struct StepParams {
+  int its;
+  int nf, of, vof;      // 0-based AB3 slots
+  double ab1, ab2, ab3; // AB3 weights (s)
+  double dt;
+};
+
+// device status bits
+enum : int {
+  kFlagBadDp = 1,       // non-positive or NaN layer thickness after cnuity
+  kFlagColumnIntegral = 2,  // hybgen column-integral conservation check failed
+  kFlagNaN = 4,
+};
+
+// Grid tables on the device, metric tables in the compute type R.
+template <typename R>
+struct Grid {
+  int N, L, T;
+  const int* __restrict__ prox;   // [N*6] 0-based
+  const int* __restrict__ proxs;  // [N*6] 0-based (pentagon slot 5 = -1)
+  const int* __restrict__ nprox;  // [N]
+  const R* __restrict__ cs;       // [N*6*4]
+  const R* __restrict__ sn;
+  const R* __restrict__ svc;      // sidevec_c [N*6*2]
+  const R* __restrict__ sve;      // sidevec_e [N*6*2]
+  const R* __restrict__ sideln;   // [N*6]
+  const R* __restrict__ area;     // [N]
+  const R* __restrict__ rarea;
+  const R* __restrict__ corio;
+  const R* __restrict__ grndspd;
+  const R* __restrict__ hfcoef;   // [N*6*6]: hfcoef[(i*6+edge)*6+j]
+  const double* __restrict__ area_d;  // [N] double areas for budgets
+  // per-level tables
+  const R* __restrict__ dfflen;   // [L]
+  const R* __restrict__ biharw;   // [L]
+  const R* __restrict__ smoo;     // [L+1]
+  const R* __restrict__ thetac;   // [L]
+  const R* __restrict__ dpsig;    // [L]
+};
+
+struct Knobs {
+  int kbl, miglim, remap_optn, hi_order;
+  double intfc_smooth, slak, ptop, thktop, rleigh, rlthresh, rltaper;
+  double dfflen_max;
+  int biharm;  // any biharw > 0
+};
+
+// Per-member element strides of the state arrays.
+struct Strides {
+  size_t cell;   // L*N
+  size_t intf;   // (L+1)*N
+  size_t edge;   // 6*L*N
+  size_t ab;     // 3*L*N
+  size_t tr;     // T*L*N
+  size_t trab;   // 3*T*L*N
+  size_t tredg;  // 6*T*L*N
+  size_t mf;     // 3*6*L*N
+  size_t col;    // N
+};
+
+inline Strides make_strides(int N, int L, int T) {
+  Strides s;
+  s.cell = (size_t)L * N;
+  s.intf = (size_t)(L + 1) * N;
+  s.edge = (size_t)6 * L * N;
+  s.ab = (size_t)3 * L * N;
+  s.tr = (size_t)T * L * N;
+  s.trab = (size_t)3 * T * L * N;
+  s.tredg = (size_t)6 * T * L * N;
+  s.mf = (size_t)18 * L * N;
+  s.col = (size_t)N;
+  return s;
+}
+
+// Launch context handed to every launcher.
+struct Launch {
+  cudaStream_t stream;
+  int members;         // gridDim.y
+  const StepParams* sp;  // device
+  int* flags;          // device status word per member [members]
+  long long* counter;  // host launch counter
+};
+
+// ---- launchers (instantiated for float and double) ----------------------
+template <typename R>
+void launch_edgvar1(const Launch&, const Grid<R>&, const Strides&, int hi_order, const R* u,
+                    const R* v, const R* delp, const R* pres, const R* montg, const R* tracr,
+                    R* u_edg, R* v_edg, R* dp_edg, R* lp_edg, R* mont_edg, R* uvsq_edg, R* trc_edg);
+template <typename R>
+void launch_edgvar3(const Launch&, const Grid<R>&, const Strides&, const R* delp, const R* tracr,
+                    R* dp_edg, R* trc_edg);
+template <typename R>
+struct CnuityScratch { R *antifx, *delp_lo, *p_plus, *p_mnus, *r_plus, *r_mnus; };
+template <typename R>
+void launch_cnuity(const Launch&, const Grid<R>&, const Strides&, const CnuityScratch<R>&, const R* u,
+                   const R* v, const R* u_edg, const R* v_edg, const R* dp_edg, const R* lp_edg,
+                   R* delp, R* pres, R* exner, R* dp_tndcy, R* dplo_tndcy, R* massfx, R* omega);
+template <typename R>
+struct TrcadvScratch { R *antiflx, *trmin, *trmax, *trcr_lo, *r_plus, *r_mnus; int tchunk; };
+template <typename R>
+void launch_trcadv(const Launch&, const Grid<R>&, const Strides&, const TrcadvScratch<R>&,
+                   const R* trc_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx,
+                   const R* delp);
+template <typename R>
+struct MomtumScratch { R *du, *dv, *wu, *wv; };
+template <typename R>
+void launch_momtum(const Launch&, const Grid<R>&, const Strides&, const Knobs&, const MomtumScratch<R>&,
+                   R* u, R* v, const R* exner, R* relvor, const R* u_edg, const R* v_edg,
+                   const R* trc_edg, const R* mont_edg, const R* uvsq_edg, R* u_tndcy, R* v_tndcy,
+                   const R* dp3d);
+template <typename R>
+struct HybgenScratch { R *exsmo, *exsmo2; };
+template <typename R>
+void launch_hybgen(const Launch&, const Grid<R>&, const Strides&, const Knobs&, const HybgenScratch<R>&,
+                   const R* targt, R* us3d, R* vs3d, R* tr3d, R* sdot, R* ex3d, R* dp3d, R* pr3d);
+template <typename R>
+void launch_hystat(const Launch&, const Grid<R>&, const Strides&, R* ph3d, const R* ex3d, R* mp3d,
+                   const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy);
+// sums per member: [member][8 + T] doubles; partial buffer sized by globsum_partials()
+template <typename R>
+void launch_globsum(const Launch&, const Grid<R>&, const Strides&, const R* dp3d, const R* tr,
+                    const R* rn2d, const R* rc2d, const R* pr3d, const R* ex3d, const R* qf2d,
+                    double* partial, double* sums);
+size_t globsum_partials(int N, int L, int T, int members);
+template <typename R>
+void launch_prdp_from_ex(const Launch&, const Grid<R>&, const Strides&, const R* ex3d, R* pr3d, R* dp3d);
+void launch_step_begin(const Launch&, StepParams* sp);
+
+}  // namespace fim

@@ -1,0 +1,222 @@
+"""Host-side mirror of the reference dycore interface over the C-ABI.
+
+`Dycore` owns one fim_ctx (grid tables uploaded once) and exposes the
+reference subroutines under their own names and argument order:
+abstart, edgvar1, edgvar3, cnuity, trcadv, momtum, hybgen, hystat, globsum
+(FIMsrc/fim/horizontal/dyn_run.F90:119-425).  Arrays are torch CUDA tensors
+(device-resident mode) or numpy arrays (host_pointers mode), flat in the
+reference layout.  `DycoreState` is the library-owned device state that the
+fused step advances; with use_graph=True each step replays one CUDA graph.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .config import FimConfig
+from .grid import Grid
+
+FIELDS = _lib.FIELDS
+
+
+def _ptr(a):
+    """Raw pointer of a torch tensor or numpy array (None -> NULL)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+class Dycore:
+    def __init__(self, grid: Grid, cfg: FimConfig):
+        self.lib = _lib.load()
+        self.grid = grid
+        self.cfg = cfg
+        self._desc = grid.desc()
+        self._ccfg = cfg.to_c()
+        ctx = ctypes.c_void_p()
+        _lib.check(self.lib.fim_ctx_create(ctypes.byref(self._desc), ctypes.byref(self._ccfg), ctypes.byref(ctx)),
+                   "fim_ctx_create")
+        self.ctx = ctx
+        self.N, self.L, self.T = grid.nip, cfg.nvl, cfg.ntra
+        self._sfx = "_r8" if cfg.precision == "f64" else "_r4"
+
+    def close(self):
+        if self.ctx:
+            self.lib.fim_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- sizes of the reference arrays ----
+    def sizes(self):
+        N, L, T = self.N, self.L, self.T
+        return dict(cell=N * L, intf=N * (L + 1), edge=6 * N * L, ab=3 * N * L, tr=T * N * L,
+                    trab=3 * T * N * L, tredg=6 * T * N * L, mf=18 * N * L, col=N)
+
+    @property
+    def stream(self):
+        return self.lib.fim_ctx_stream(self.ctx)
+
+    def launches(self):
+        return self.lib.fim_launch_count(self.ctx)
+
+    def _call(self, name, *args):
+        fn = getattr(self.lib, name + self._sfx)
+        _lib.check(fn(self.ctx, *args), name, self.ctx)
+
+    def sync(self):
+        import torch
+        torch.cuda.synchronize()
+
+    # ---- AB3 bookkeeping (module_variables nf, of, vof, adbash1..3) ----
+    def abstart(self, its, its_start=1):
+        nf, of, vof = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        a1, a2, a3 = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _lib.check(self.lib.fim_abstart(self.ctx, its, its_start, ctypes.byref(nf), ctypes.byref(of),
+                                        ctypes.byref(vof), ctypes.byref(a1), ctypes.byref(a2), ctypes.byref(a3)),
+                   "fim_abstart", self.ctx)
+        return nf.value, of.value, vof.value, a1.value, a2.value, a3.value
+
+    def set_ab(self, nf, of, vof, ab1, ab2, ab3):
+        _lib.check(self.lib.fim_set_ab(self.ctx, nf, of, vof, ab1, ab2, ab3), "fim_set_ab", self.ctx)
+
+    def get_ab(self):
+        v = [ctypes.c_int() for _ in range(3)] + [ctypes.c_double() for _ in range(3)]
+        _lib.check(self.lib.fim_get_ab(self.ctx, *[ctypes.byref(x) for x in v]), "fim_get_ab", self.ctx)
+        return tuple(x.value for x in v)
+
+    # ---- the reference routines ----
+    def edgvar1(self, its, u_vel, v_vel, delp, pres, exner, geop, montg, tracr, u_edg, v_edg, dp_edg, lp_edg,
+                geop_edg, mont_edg, uvsq_edg, trc_edg):
+        self._call("fim_edgvar1", its, *map(_ptr, (u_vel, v_vel, delp, pres, exner, geop, montg, tracr, u_edg,
+                                                     v_edg, dp_edg, lp_edg, geop_edg, mont_edg, uvsq_edg, trc_edg)))
+
+    def edgvar3(self, its, u_vel, v_vel, delp, pres, exner, geop, montg, tracr, u_edg, v_edg, dp_edg, lp_edg,
+                geop_edg, mont_edg, uvsq_edg, trc_edg):
+        self._call("fim_edgvar3", its, *map(_ptr, (u_vel, v_vel, delp, pres, exner, geop, montg, tracr, u_edg,
+                                                     v_edg, dp_edg, lp_edg, geop_edg, mont_edg, uvsq_edg, trc_edg)))
+
+    def cnuity(self, its, u_velo, v_velo, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner, dp_tndcy, dplo_tndcy,
+               massfx, omega):
+        self._call("fim_cnuity", its, *map(_ptr, (u_velo, v_velo, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner,
+                                                    dp_tndcy, dplo_tndcy, massfx, omega)))
+
+    def trcadv(self, its, trcr_edg, tracr, trcdp, trc_tdcy, trclo_tdcy, massfx, delp):
+        self._call("fim_trcadv", its, *map(_ptr, (trcr_edg, tracr, trcdp, trc_tdcy, trclo_tdcy, massfx, delp)))
+
+    def momtum(self, its, u_velo, v_velo, exner, relvor, u_edg, v_edg, trcr_edg, geop_edg, mont_edg, uvsq_edg,
+               u_tndcy, v_tndcy, dp3d):
+        self._call("fim_momtum", its, *map(_ptr, (u_velo, v_velo, exner, relvor, u_edg, v_edg, trcr_edg, geop_edg,
+                                                    mont_edg, uvsq_edg, u_tndcy, v_tndcy, dp3d)))
+
+    def hybgen(self, its, targt, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d):
+        self._call("fim_hybgen", its, *map(_ptr, (targt, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d)))
+
+    def hystat(self, its, ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy):
+        self._call("fim_hystat", its, *map(_ptr, (ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy)))
+
+    def globsum(self, its, dp3d, tr, pr3d, ex3d, rn2d=None, rc2d=None, qf2d=None):
+        qtrcr = np.zeros(self.T, np.float64)
+        b = _lib.Budget()
+        self._call("fim_globsum", its, *map(_ptr, (dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d)), qtrcr.ctypes.data,
+                   ctypes.byref(b))
+        return qtrcr, {n: getattr(b, n) for n, _ in _lib.Budget._fields_}
+
+    def state(self):
+        return DycoreState(self)
+
+
+class DycoreState:
+    """Library-owned device state of all members (module_variables arrays)."""
+
+    def __init__(self, dyc: Dycore):
+        self.dyc = dyc
+        self.lib = dyc.lib
+        st = ctypes.c_void_p()
+        _lib.check(self.lib.fim_state_alloc(dyc.ctx, ctypes.byref(st)), "fim_state_alloc", dyc.ctx)
+        self.st = st
+        self.its = 0
+
+    def free(self):
+        if self.st:
+            self.lib.fim_state_free(self.dyc.ctx, self.st)
+            self.st = None
+
+    def field_ptr(self, name, member=0):
+        p = ctypes.c_void_p()
+        n = ctypes.c_int64()
+        _lib.check(self.lib.fim_state_field(self.dyc.ctx, self.st, _lib.FIELD_ID[name], member, ctypes.byref(p),
+                                            ctypes.byref(n)), "fim_state_field", self.dyc.ctx)
+        return p.value, n.value
+
+    def tensor(self, name, member=0):
+        """Zero-copy torch view of one member's field."""
+        import torch
+        ptr, n = self.field_ptr(name, member)
+        dt = torch.float64 if self.dyc.cfg.precision == "f64" else torch.float32
+        return _torch_from_ptr(ptr, n, dt)
+
+    def upload(self, name, host, member=0):
+        ptr, n = self.field_ptr(name, member)
+        host = np.ascontiguousarray(host, dtype=self.dyc.cfg.dtype) if isinstance(host, np.ndarray) else host
+        if isinstance(host, np.ndarray) and host.size != n:
+            raise ValueError("%s: %d elements, expected %d" % (name, host.size, n))
+        _lib.check(self.lib.fim_state_upload(self.dyc.ctx, self.st, _lib.FIELD_ID[name], member, _ptr(host)),
+                   "fim_state_upload", self.dyc.ctx)
+        if isinstance(host, np.ndarray):
+            self.dyc.sync()
+
+    def download(self, name, member=0, out=None):
+        ptr, n = self.field_ptr(name, member)
+        if out is None:
+            out = np.empty(n, self.dyc.cfg.dtype)
+        _lib.check(self.lib.fim_state_download(self.dyc.ctx, self.st, _lib.FIELD_ID[name], member, _ptr(out)),
+                   "fim_state_download", self.dyc.ctx)
+        self.dyc.sync()
+        return out
+
+    def load(self, fields, member=0):
+        for k, v in fields.items():
+            self.upload(k, v, member)
+
+    def init(self):
+        _lib.check(self.lib.fim_state_init(self.dyc.ctx, self.st), "fim_state_init", self.dyc.ctx)
+        self.its = 0
+
+    def step(self, its=None, use_graph=False):
+        its = self.its + 1 if its is None else its
+        _lib.check(self.lib.fim_step(self.dyc.ctx, self.st, its, 1 if use_graph else 0), "fim_step", self.dyc.ctx)
+        self.its = its
+
+    def budget(self, member=0):
+        qtrcr = np.zeros(self.dyc.T, np.float64)
+        b = _lib.Budget()
+        _lib.check(self.lib.fim_state_budget(self.dyc.ctx, self.st, member, qtrcr.ctypes.data, ctypes.byref(b)),
+                   "fim_state_budget", self.dyc.ctx)
+        return qtrcr, {n: getattr(b, n) for n, _ in _lib.Budget._fields_}
+
+    def check(self):
+        flags = ctypes.c_int()
+        rc = self.lib.fim_check(self.dyc.ctx, self.st, ctypes.byref(flags))
+        return rc, flags.value
+
+
+def _torch_from_ptr(ptr, n, dtype):
+    """Wrap device memory owned by the library as a torch tensor (no copy)."""
+    import torch
+
+    class _Holder:
+        pass
+
+    h = _Holder()
+    esz = 8 if dtype == torch.float64 else 4
+    typestr = "<f8" if esz == 8 else "<f4"
+    h.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False), "version": 2,
+                                  "strides": None}
+    return torch.as_tensor(h, device="cuda")

@@ -1,0 +1,243 @@
+/*
+ * fim_gpu.h -- C-ABI of the GB300 horizontal dynamics step of FIM
+ * (Flow-following finite-volume Icosahedral Model).
+ *
+ * Every routine of the reference dycore step has one entry point here with the
+ * reference's Fortran argument order, so the Fortran driver dyn_run can call it
+ * through an iso_c_binding interface.  Arrays keep the reference layout:
+ * column-major with the level index fastest, e.g. u(nvl,nip),
+ * pres(nvl+1,nip), u_edg(nvl,6,nip), tracr(nvl,nip,ntra),
+ * trc_tdcy(nvl,nip,3,ntra), massfx(nvl,6,nip,3).
+ *
+ * Two families of entry points exist: the *_r8 family takes double fields
+ * (a real*8 build of the caller, the FP64 context), the *_r4 family float
+ * fields (the reference's default -r4 build, the FP32-mixed context).
+ * Field pointers are device pointers when the context was created with
+ * host_pointers == 0 (the fast, device-resident mode) and host pointers
+ * otherwise (each call then stages its inputs and outputs through the device).
+ *
+ * All functions return a status code and never abort the process.
+ * The AB3 (Adams-Bashforth) time-slot indices and weights that the reference
+ * keeps in module_variables live in the context; fim_abstart_* advances them.
+ */
+#ifndef FIM_GPU_H
+#define FIM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FIM_OK 0
+#define FIM_EINVAL 1      /* bad argument, size or configuration */
+#define FIM_ENOMEM 2      /* device or host allocation failed */
+#define FIM_ECUDA 3       /* a CUDA runtime call failed */
+#define FIM_ENUMERIC 4    /* NaN or non-positive layer thickness detected */
+#define FIM_ETIMEDOUT 5   /* a bounded device-side wait gave up */
+#define FIM_ENOTSUP 6     /* option of the reference that this build does not implement */
+
+#define FIM_PREC_F64 0    /* every field and every operation in double */
+#define FIM_PREC_F32 1    /* FP32 fields and arithmetic, FP64 column scans and budgets */
+
+/*
+ * Grid tables, in the layout of FIMsrc/cntl/module_constants.F90:45-104 with
+ * Fortran (1-based) cell and edge numbers.  Filled by fim_grid_build or by the
+ * caller from its own glvl.dat (FIMsrc/fim/horizontal/dyn_init.F90:373-549).
+ */
+typedef struct fim_grid_desc {
+  int glvl;
+  int nip;                 /* 10*4^glvl+2 */
+  int32_t *nprox;          /* nprox(nip): 5 or 6 */
+  int32_t *prox;           /* prox(6,nip): neighbour across edge; prox(6)=prox(5) at pentagons */
+  int32_t *proxs;          /* proxs(6,nip): the neighbour's number of the shared edge */
+  double *lat, *lon;       /* lat(nip), lon(nip) in radians (may be NULL for ctx creation: then corio/grndspd need them) */
+  double *area;            /* area(nip) m^2 */
+  double *cs, *sn;         /* cs(4,6,nip), sn(4,6,nip) */
+  double *sidevec_c;       /* sidevec_c(2,6,nip) */
+  double *sidevec_e;       /* sidevec_e(2,6,nip) */
+  double *sideln;          /* sideln(6,nip) */
+  double *rprox_ln;        /* rprox_ln(6,nip) */
+  double *corner_xy;       /* corner_xy(6,2,nip), optional */
+  double *hfcoef;          /* hfcoef(6,6,nip) */
+} fim_grid_desc;
+
+/* Namelist knobs used on the path (FIMsrc/cntl/fimnamelist.F90:95-119,
+ * FIMsrc/cntl/module_control.F90:97-100), reference defaults in brackets. */
+typedef struct fim_config {
+  int nvl;                 /* layers */
+  int ntra;                /* class-A tracers, slot 1 = potential temperature (>= 4) */
+  int precision;           /* FIM_PREC_F64 or FIM_PREC_F32 */
+  int members;             /* ensemble members sharing the grid (>= 1) */
+  int host_pointers;       /* 1: entry points receive host arrays */
+  double dt;               /* time step, s */
+  int kbl;                 /* [2] fixed-depth layers near the surface */
+  int flux_conserv_schm;   /* must be 1 (FCT cnuity) */
+  int hi_order_flux_comp;  /* [1] edgvar3 supplies dp_edg and tracers 2..ntra */
+  double intfc_smooth;     /* [30] m/s */
+  double slak;             /* [0.5] */
+  int miglim;              /* [1] */
+  int remap_optn;          /* [2] 1 PCM, 2 PLM, 3 PPM */
+  double ptop;             /* [30] Pa */
+  double thktop;           /* [30] Pa */
+  double veldff_bkgnd;     /* [0.3] */
+  double veldff_boost;     /* [3] */
+  int biharm_frst, biharm_last; /* [0,0] */
+  double rleigh;           /* [2] 1/day */
+  double rlthresh;         /* [90] m/s */
+  double rltaper;          /* [0.4] */
+  int pure_sig;            /* [0]; 1 is not supported (FIM_ENOTSUP) */
+  const double *thetac;    /* thetac(nvl): hybgen target potential temperature */
+  const double *dpsig;     /* dpsig(nvl): minimum layer thickness, Pa */
+} fim_config;
+
+typedef struct fim_ctx fim_ctx;
+
+/* Global budget sums of FIMsrc/fim/horizontal/globsum.F90:39-130 (real*8). */
+typedef struct fim_budget {
+  double qmass, qmsqv, qmsqw, qmso3, qmste, qmstr, qmstrn, qmstrc;
+} fim_budget;
+
+/* ---- grid ------------------------------------------------------------- */
+/* nip of an icosahedral grid level; -1 for an unsupported level */
+int fim_grid_nip(int glvl);
+/* Build the level-glvl grid into caller buffers sized by g->nip
+ * (FIMsrc/prep/grid/icos.F90, GridGen.F90, getlvl.F90). */
+int fim_grid_build(int glvl, fim_grid_desc *g);
+
+/* ---- context ---------------------------------------------------------- */
+/* Upload the grid tables and derived fields (dyn_init.F90:311-338,545-549,
+ * 752-767) and fix the configuration; replaces GPUinit/copytoGPUinit
+ * (FIMsrc/fim/horizontal/cuda/GPUinit.cu:12-54, dyn_init.F90:199,1198). */
+int fim_ctx_create(const fim_grid_desc *grid, const fim_config *cfg, fim_ctx **out);
+int fim_ctx_destroy(fim_ctx *ctx);
+/* last CUDA error text of the context (GetLastError.cu:6-14 replacement) */
+const char *fim_ctx_last_error(const fim_ctx *ctx);
+/* device stream the context launches on (a cudaStream_t) */
+void *fim_ctx_stream(fim_ctx *ctx);
+/* AB3 slots (Fortran numbering 1..3) and weights of the context */
+int fim_get_ab(const fim_ctx *ctx, int *nf, int *of, int *vof, double *ab1, double *ab2, double *ab3);
+int fim_set_ab(fim_ctx *ctx, int nf, int of, int vof, double ab1, double ab2, double ab3);
+
+/* ---- per-routine entry points, reference argument order -------------- */
+/* FIMsrc/fim/horizontal/abstart.F90:14-68 */
+int fim_abstart(fim_ctx *ctx, int its, int its_start, int *nf, int *of, int *vof,
+                double *adbash1, double *adbash2, double *adbash3);
+
+/* FIMsrc/fim/horizontal/edgvar1.F90:27-29 (eqwgt, janjic=0 branches) */
+int fim_edgvar1_r8(fim_ctx *ctx, int its, const double *u_vel, const double *v_vel,
+                   const double *delp, const double *pres, const double *exner,
+                   const double *geop, const double *montg, const double *tracr,
+                   double *u_edg, double *v_edg, double *dp_edg, double *lp_edg,
+                   double *geop_edg, double *mont_edg, double *uvsq_edg, double *trc_edg);
+int fim_edgvar1_r4(fim_ctx *ctx, int its, const float *u_vel, const float *v_vel,
+                   const float *delp, const float *pres, const float *exner,
+                   const float *geop, const float *montg, const float *tracr,
+                   float *u_edg, float *v_edg, float *dp_edg, float *lp_edg,
+                   float *geop_edg, float *mont_edg, float *uvsq_edg, float *trc_edg);
+
+/* FIMsrc/fim/horizontal/edgvar3.F90:25-27 */
+int fim_edgvar3_r8(fim_ctx *ctx, int its, const double *u_vel, const double *v_vel,
+                   const double *delp, const double *pres, const double *exner,
+                   const double *geop, const double *montg, const double *tracr,
+                   double *u_edg, double *v_edg, double *dp_edg, double *lp_edg,
+                   double *geop_edg, double *mont_edg, double *uvsq_edg, double *trc_edg);
+int fim_edgvar3_r4(fim_ctx *ctx, int its, const float *u_vel, const float *v_vel,
+                   const float *delp, const float *pres, const float *exner,
+                   const float *geop, const float *montg, const float *tracr,
+                   float *u_edg, float *v_edg, float *dp_edg, float *lp_edg,
+                   float *geop_edg, float *mont_edg, float *uvsq_edg, float *trc_edg);
+
+/* FIMsrc/fim/horizontal/cnuity.F90:23-25 (cnuity1..5) */
+int fim_cnuity_r8(fim_ctx *ctx, int its, const double *u_velo, const double *v_velo,
+                  const double *u_edg, const double *v_edg, const double *dp_edg,
+                  const double *lp_edg, double *delp, double *pres, double *exner,
+                  double *dp_tndcy, double *dplo_tndcy, double *massfx, double *omega);
+int fim_cnuity_r4(fim_ctx *ctx, int its, const float *u_velo, const float *v_velo,
+                  const float *u_edg, const float *v_edg, const float *dp_edg,
+                  const float *lp_edg, float *delp, float *pres, float *exner,
+                  float *dp_tndcy, float *dplo_tndcy, float *massfx, float *omega);
+
+/* FIMsrc/fim/horizontal/trcadv.F90:19-20 (trcadv1..3, all tracers) */
+int fim_trcadv_r8(fim_ctx *ctx, int its, const double *trcr_edg, double *tracr, double *trcdp,
+                  double *trc_tdcy, double *trclo_tdcy, const double *massfx, const double *delp);
+int fim_trcadv_r4(fim_ctx *ctx, int its, const float *trcr_edg, float *tracr, float *trcdp,
+                  float *trc_tdcy, float *trclo_tdcy, const float *massfx, const float *delp);
+
+/* FIMsrc/fim/horizontal/momtum.F90:16-18 (dissip, del4prep, momtum1) */
+int fim_momtum_r8(fim_ctx *ctx, int its, double *u_velo, double *v_velo, const double *exner,
+                  double *relvor, const double *u_edg, const double *v_edg,
+                  const double *trcr_edg, const double *geop_edg, const double *mont_edg,
+                  const double *uvsq_edg, double *u_tndcy, double *v_tndcy, const double *dp3d);
+int fim_momtum_r4(fim_ctx *ctx, int its, float *u_velo, float *v_velo, const float *exner,
+                  float *relvor, const float *u_edg, const float *v_edg,
+                  const float *trcr_edg, const float *geop_edg, const float *mont_edg,
+                  const float *uvsq_edg, float *u_tndcy, float *v_tndcy, const float *dp3d);
+
+/* FIMsrc/fim/horizontal/hybgen.F90:20-26 (regrid_1d, dffusn_lev, remap_1d);
+ * targt may be NULL to use the context's thetac */
+int fim_hybgen_r8(fim_ctx *ctx, int its, const double *targt, double *us3d, double *vs3d,
+                  double *tr3d, double *sdot, double *ex3d, double *dp3d, double *pr3d);
+int fim_hybgen_r4(fim_ctx *ctx, int its, const float *targt, float *us3d, float *vs3d,
+                  float *tr3d, float *sdot, float *ex3d, float *dp3d, float *pr3d);
+
+/* FIMsrc/fim/horizontal/hystat.F90:23-24 */
+int fim_hystat_r8(fim_ctx *ctx, int its, double *ph3d, const double *ex3d, double *mp3d,
+                  const double *dp3d, double *tr3d, double *trdp, double *psrf, double *ptdcy);
+int fim_hystat_r4(fim_ctx *ctx, int its, float *ph3d, const float *ex3d, float *mp3d,
+                  const float *dp3d, float *tr3d, float *trdp, float *psrf, float *ptdcy);
+
+/* FIMsrc/fim/horizontal/globsum.F90:39; rn2d, rc2d, qf2d may be NULL (zero);
+ * qtrcr(ntra) and the budget are double in both families */
+int fim_globsum_r8(fim_ctx *ctx, int its, const double *dp3d, const double *tr,
+                   const double *rn2d, const double *rc2d, const double *pr3d,
+                   const double *ex3d, const double *qf2d, double *qtrcr, fim_budget *out);
+int fim_globsum_r4(fim_ctx *ctx, int its, const float *dp3d, const float *tr,
+                   const float *rn2d, const float *rc2d, const float *pr3d,
+                   const float *ex3d, const float *qf2d, double *qtrcr, fim_budget *out);
+
+/* ---- device-resident state and the fused step ------------------------ */
+/* Prognostic and work arrays of FIMsrc/cntl/module_variables.F90:23-91 for all
+ * members of the context, owned by the library. */
+typedef struct fim_state fim_state;
+
+/* field identifiers for fim_state_field */
+enum fim_field {
+  FIM_US3D = 0, FIM_VS3D, FIM_DP3D, FIM_PR3D, FIM_EX3D, FIM_PH3D, FIM_MP3D, FIM_TR3D,
+  FIM_TRDP, FIM_U_TDCY, FIM_V_TDCY, FIM_DP_TDCY, FIM_DPL_TDCY, FIM_TRC_TDCY, FIM_TRL_TDCY,
+  FIM_MASSFX, FIM_WS3D, FIM_SDOT, FIM_RELVOR, FIM_PSRF, FIM_PTDCY,
+  FIM_U_EDG, FIM_V_EDG, FIM_DP_EDG, FIM_LP_EDG, FIM_MONT_EDG, FIM_UVSQ_EDG, FIM_GEOP_EDG,
+  FIM_TRC_EDG, FIM_NFIELDS
+};
+
+int fim_state_alloc(fim_ctx *ctx, fim_state **out);
+int fim_state_free(fim_ctx *ctx, fim_state *st);
+/* device pointer and element count of one member's field */
+int fim_state_field(fim_ctx *ctx, fim_state *st, int field, int member, void **dptr, int64_t *count);
+/* host <-> device copy of one member's field (element type per precision) */
+int fim_state_upload(fim_ctx *ctx, fim_state *st, int field, int member, const void *host);
+int fim_state_download(fim_ctx *ctx, fim_state *st, int field, int member, void *host);
+
+/* dyn_init.F90:870-906,1037-1094 for every member: trdp, hybgen(its=0),
+ * pressure/thickness from Exner, hystat(its=0), zero tendencies, AB3 slots */
+int fim_state_init(fim_ctx *ctx, fim_state *st);
+
+/* One dynamics step of every member in dyn_run order (dyn_run.F90:329-425
+ * followed by hybgen/hystat/globsum of dyn_run.F90:119-150 for the same its).
+ * use_graph != 0 captures the step once as a CUDA graph and replays it. */
+int fim_step(fim_ctx *ctx, fim_state *st, int its, int use_graph);
+
+/* Member budgets after the last step (qmass, tracer integrals qtrcr(ntra)). */
+int fim_state_budget(fim_ctx *ctx, fim_state *st, int member, double *qtrcr, fim_budget *out);
+
+/* Accumulated device-side status flags (NaN / non-positive thickness); resets them. */
+int fim_check(fim_ctx *ctx, fim_state *st, int *flags);
+
+/* Kernel launches issued since the context was created (own kernels only). */
+int64_t fim_launch_count(const fim_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FIM_GPU_H */

@@ -1,0 +1,80 @@
+/*
+ * CPU oracle of the FIM horizontal dynamics step -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C, double-precision restatement of the reference Fortran routines
+ * (the .F90 files of FIMsrc/fim/horizontal), loop for loop, used by the test suite, the
+ * smoke check and the CPU-baseline leg of bench.py as the checker.  The
+ * product library never links or calls it.
+ *
+ * Parity status: UNPINNED.  The reference ships no golden vectors or unit
+ * fixtures for this path and cannot be compiled here (Fortran, no compiler);
+ * the restatement is pinned only by the reference's own in-code invariants
+ * (column-integral conservation in hybgen, FCT positivity/monotonicity,
+ * global mass conservation) which the tests check.
+ *
+ * Index conventions: 0-based, reference layout with the level index fastest.
+ *   cell field (nvl,nip):        f[i*nvl + k]
+ *   interface field (nvl+1,nip): f[i*(nvl+1) + k]
+ *   edge field (nvl,6,nip):      f[(i*6 + e)*nvl + k]
+ *   AB3 field (nvl,nip,3):       f[(s*nip + i)*nvl + k]
+ *   tracers (nvl,nip,ntra):      f[(t*nip + i)*nvl + k]
+ *   tracer AB3 (nvl,nip,3,ntra): f[((t*3 + s)*nip + i)*nvl + k]
+ *   tracer edges (nvl,6,nip,ntra): f[((t*nip + i)*6 + e)*nvl + k]
+ *   massfx (nvl,6,nip,3):        f[((s*nip + i)*6 + e)*nvl + k]
+ * Grid tables are 0-based: prox[i*6+e], proxs[i*6+e], cs[(i*6+e)*4+q], ...
+ */
+#ifndef FIM_ORACLE_H
+#define FIM_ORACLE_H
+
+typedef struct orc_ctx {
+  int nip, nvl, ntra;
+  const int *prox, *proxs, *nprox;
+  const double *cs, *sn, *sidevec_c, *sidevec_e, *sideln, *area, *rarea, *corio, *grndspd;
+  const double *hfcoef;
+  double dt;
+  int kbl, hi_order, miglim, remap_optn;
+  double intfc_smooth, slak, ptop, thktop, rleigh, rlthresh, rltaper;
+  const double *thetac, *dpsig;         /* [nvl] */
+  const double *dfflen, *biharw;        /* [nvl] */
+  const double *smoo_coeff;             /* [nvl+1] */
+  double dfflen_max;
+  int nf, of, vof;                      /* 0-based AB3 slots */
+  double ab1, ab2, ab3;
+  long diag_flags;                      /* conservation-check failures seen */
+} orc_ctx;
+
+void orc_derived(int nip, int nvl, int kbl, double dt, double intfc_smooth,
+                 double veldff_bkgnd, double veldff_boost, int biharm_frst, int biharm_last,
+                 const double *lat, const double *area, const double *sideln,
+                 double *rarea, double *corio, double *grndspd, double *dfflen,
+                 double *biharw, double *smoo_coeff, double *dfflen_max);
+
+void orc_abstart(orc_ctx *c, int its);
+void orc_edgvar1(const orc_ctx *c, const double *u, const double *v, const double *delp,
+                 const double *pres, const double *exner, const double *geop,
+                 const double *montg, const double *tracr, double *u_edg, double *v_edg,
+                 double *dp_edg, double *lp_edg, double *geop_edg, double *mont_edg,
+                 double *uvsq_edg, double *trc_edg);
+void orc_edgvar3(const orc_ctx *c, const double *delp, const double *tracr,
+                 double *dp_edg, double *trc_edg);
+void orc_cnuity(const orc_ctx *c, const double *u, const double *v, const double *u_edg,
+                const double *v_edg, const double *dp_edg, const double *lp_edg, double *delp,
+                double *pres, double *exner, double *dp_tndcy, double *dplo_tndcy,
+                double *massfx, double *omega);
+void orc_trcadv(const orc_ctx *c, const double *trc_edg, double *tracr, double *trcdp,
+                double *trc_tdcy, double *trl_tdcy, const double *massfx, const double *delp);
+void orc_momtum(const orc_ctx *c, double *u, double *v, const double *exner, double *relvor,
+                const double *u_edg, const double *v_edg, const double *trc_edg,
+                const double *mont_edg, const double *uvsq_edg, double *u_tndcy,
+                double *v_tndcy, const double *dp3d);
+void orc_hybgen(orc_ctx *c, int its, const double *targt, double *us3d, double *vs3d,
+                double *tr3d, double *sdot, double *ex3d, double *dp3d, double *pr3d);
+void orc_hystat(const orc_ctx *c, int its, double *ph3d, const double *ex3d, double *mp3d,
+                const double *dp3d, double *tr3d, double *trdp, double *psrf, double *ptdcy);
+void orc_globsum(const orc_ctx *c, const double *dp3d, const double *tr, const double *rn2d,
+                 const double *rc2d, const double *pr3d, const double *ex3d,
+                 const double *qf2d, double *qtrcr, double *sums8);
+/* pressure and thickness from Exner after the start-up hybgen (dyn_init.F90:895-906) */
+void orc_prdp_from_ex(const orc_ctx *c, const double *ex3d, double *pr3d, double *dp3d);
+
+#endif
