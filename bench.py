@@ -1,0 +1,391 @@
+"""Benchmark of the FIM horizontal dynamics step on GB300.
+
+Workload (default): glvl 8 (655,362 cells), nvl 64, 20 tracers + theta,
+dt 72 s, FP32-mixed, seeded synthetic balanced state; one "step" is one
+fused dycore step (abstart, edgvar1, edgvar3, cnuity, trcadv, momtum,
+hybgen + dffusn_lev, hystat, globsum) replayed as one CUDA graph.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line (rank 0).  value = cell-level-steps/s of all ranks
+(replicas: one independent state per GPU), timed with CUDA events on the
+library's stream, max over ranks.  The state (~60 GB) is far larger than L2,
+so no flush is needed between steps.  The reference arm times the CPU oracle
+(the C restatement of the reference's Fortran routines) on a level-6 sample
+of the same workload with all host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests")]
+
+METRIC = "cell-level-steps/s at glvl 8 nvl 64, FP32-mixed vs FP64; served p50/p99 latency"
+UNIT = "cell-level-steps/s"
+
+# Algorithmic words per cell-level per step that each kernel must read and
+# write once (own-column values; neighbour values are re-reads served by
+# L1/L2), summed over the tracers it handles.  Used for roofline.achieved.
+WORDS = {
+    "k_edgvar1": lambda T: 41, "k_edgvar3_own": lambda T: 7 * T, "k_edgvar3_avg": lambda T: 12 * T,
+    "k_cnuity12": lambda T: 37, "k_cnuity3": lambda T: 8, "k_cnuity4": lambda T: 26, "k_cnuity5": lambda T: 14,
+    "k_trcadv1": lambda T: 27 * T, "k_trcadv2": lambda T: 16 * T, "k_trcadv3": lambda T: 18 * T,
+    "k_dissip": lambda T: 5, "k_del4prep": lambda T: 4, "k_momtum1": lambda T: 44,
+    "k_regrid": lambda T: 3, "k_dffusn_lev": lambda T: 2, "k_remap": lambda T: 2 * T + 10,
+    "k_hystat": lambda T: 2 * T + 7, "k_globsum_levels": lambda T: T + 1,
+}
+
+E2E_FIELDS = ["us3d", "vs3d", "dp3d", "pr3d", "ex3d", "ph3d", "mp3d", "tr3d", "trdp", "u_tdcy", "v_tdcy",
+              "dp_tdcy", "dpl_tdcy", "trc_tdcy", "trl_tdcy", "ws3d", "sdot", "relvor", "psrf", "ptdcy"]
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            time.sleep(0.3)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self):
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        sm, mx, reasons = [], [], set()
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def max_over_ranks(x, ws, backend_device):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=backend_device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ------------------------------------------------------------------ GPU arm --
+def make_state(F, grid, cfg, wl, dtype):
+    dyc = F.Dycore(grid, cfg)
+    st = dyc.state()
+    for m in range(cfg.members):
+        fields = F.synthetic_state(grid, cfg, seed=wl["seed"] + m, sigma_ps=wl["sigma_ps"], noise=wl["noise"],
+                                   dtype=dtype)
+        st.load(fields, member=m)
+        del fields
+    st.init()
+    return dyc, st
+
+
+def timed_steps(torch, dyc, st, k, graph=True):
+    stream = torch.cuda.ExternalStream(dyc.stream)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    n0 = dyc.launches()
+    a.record(stream)
+    for _ in range(k):
+        st.step(use_graph=graph)
+    b.record(stream)
+    b.synchronize()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / k, dyc.launches() - n0
+
+
+def gpu_arm(args, ws, rank, local):
+    import torch
+    import fimocn_subx_realtime_hera_apr2020_gb300 as F
+
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    wl = dict(F.WORKLOADS[args.workload])
+    members = args.members or wl.get("members", 1)
+    grid = F.Grid.cached(wl["glvl"])
+    N, L, T = grid.nip, wl["nvl"], wl["ntra"]
+    units = N * L * members  # cell-levels per step per GPU
+    cfg = F.FimConfig(nvl=L, ntra=T, dt=wl["dt"], precision="f32", members=members)
+    dyc, st = make_state(F, grid, cfg, wl, np.float32)
+    for _ in range(args.warmup):
+        st.step(use_graph=True)
+    torch.cuda.synchronize()
+    barrier(ws)
+    with Clocks(local) as clk:
+        ms, launches = timed_steps(torch, dyc, st, args.steps, graph=True)
+    barrier(ws)
+    ms_max = max_over_ranks(ms, ws, torch.device("cuda", local))
+    value = units * ws / (ms_max * 1e-3)
+    rc, flags = st.check()
+    if rc != 0:
+        raise SystemExit("device status flags %d after the timed steps" % flags)
+
+    # per-kernel times (events on the library stream), direct launches
+    dyc.profile(True)
+    kp = max(2, min(args.steps, 5))
+    for _ in range(kp):
+        st.step(use_graph=False)
+    torch.cuda.synchronize()
+    prof = dyc.profile_report()
+    dyc.profile(False)
+    peak, peak_kind = peaks()
+    w = 4
+    total = sum(v[1] for v in prof.values())
+    kernels = {}
+    for name, (n, tms) in prof.items():
+        if name not in WORDS:
+            continue
+        bytes_launch = WORDS[name](T) * w * N * L * members * kp / n
+        avg = tms / n
+        kernels[name] = {"launches": n, "ms_total": tms, "share": tms / total, "ms_avg": avg,
+                         "alg_bytes": bytes_launch, "gbs": bytes_launch / (avg * 1e-3) / 1e9}
+    dom = max(kernels, key=lambda k: kernels[k]["ms_total"])
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get(args.workload, {}).get(dom)
+        except Exception:
+            traffic = None
+    roof = {"bound": "hbm", "kernel": dom, "achieved": kernels[dom]["gbs"], "peak": peak, "unit": "GB/s",
+            "frac": kernels[dom]["gbs"] / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": traffic, "alg_bytes_per_launch": kernels[dom]["alg_bytes"]}
+
+    # end to end through the C-ABI with host buffers: upload the state, step, download it
+    e2e = None
+    if not args.no_e2e:
+        bufs = {}
+        for f in E2E_FIELDS:
+            ptr, n = st.field_ptr(f, 0)
+            bufs[f] = torch.empty(n * members, dtype=torch.float32, pin_memory=True)
+            for m in range(members):
+                st.download(f, m, out=bufs[f][m * n:(m + 1) * n].numpy())
+        bytes_step = sum(b.numel() * 4 for b in bufs.values())
+        stream = torch.cuda.ExternalStream(dyc.stream)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ke = max(1, min(args.steps, 5))
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(ke):
+            for f, buf in bufs.items():
+                n = buf.numel() // members
+                for m in range(members):
+                    _check(dyc.lib.fim_state_upload(dyc.ctx, st.st, F.dycore._lib.FIELD_ID[f], m,
+                                                    buf.data_ptr() + m * n * 4), "upload")
+            st.step(use_graph=True)
+            for f, buf in bufs.items():
+                n = buf.numel() // members
+                for m in range(members):
+                    _check(dyc.lib.fim_state_download(dyc.ctx, st.st, F.dycore._lib.FIELD_ID[f], m,
+                                                      buf.data_ptr() + m * n * 4), "download")
+        b.record(stream)
+        b.synchronize()
+        e_ms = a.elapsed_time(b) / ke
+        e_ms = max_over_ranks(e_ms, ws, torch.device("cuda", local))
+        e2e = {"value": units * ws / (e_ms * 1e-3), "unit": UNIT, "ms_per_step": e_ms,
+               "h2d_bytes_per_step": bytes_step, "d2h_bytes_per_step": bytes_step,
+               "path": "fim_state_upload -> fim_step -> fim_state_download (pinned host buffers)"}
+        del bufs
+    qtrcr, bud = st.budget()
+    st.free()
+    dyc.close()
+    torch.cuda.synchronize()
+
+    # plain FP64 GPU step at the same workload
+    fp64 = None
+    if args.fp64_steps > 0:
+        cfg64 = F.FimConfig(nvl=L, ntra=T, dt=wl["dt"], precision="f64", members=members)
+        d64, s64 = make_state(F, grid, cfg64, wl, np.float64)
+        s64.step(use_graph=True)
+        ms64, _ = timed_steps(torch, d64, s64, args.fp64_steps, graph=True)
+        ms64 = max_over_ranks(ms64, ws, torch.device("cuda", local))
+        fp64 = {"value": units * ws / (ms64 * 1e-3), "ms_per_step": ms64, "steps": args.fp64_steps,
+                "fp32_mixed_speedup": ms64 / ms_max}
+        s64.free()
+        d64.close()
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu = cpu_baseline(args, threads_all=True)
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (FP64 column scans and budget sums)",
+            "data": "synthetic seeded balanced state (no dataset: the reference's GFS initial state is not "
+                    "in the tree)",
+            "config": {"workload": args.workload, "glvl": wl["glvl"], "nip": N, "nvl": L, "ntra": T,
+                       "dt": wl["dt"], "members_per_gpu": members, "precision": "fp32-mixed",
+                       "cuda_graph": True, "parallelism": "replicas" if ws > 1 else "single",
+                       "l2": "no flush: state and edge fields (~60 GB) far exceed the 129 MB L2"},
+            "gpu_launches": launches, "clocks": clk.summary(), "roofline": roof, "e2e": e2e,
+            "cpu_baseline": cpu, "fp64": fp64, "kernels": kernels,
+            "budget": {"qmass": bud["qmass"], "qtrcr_theta": qtrcr[0]}}
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError("%s failed with status %d" % (what, rc))
+
+
+# -------------------------------------------------------------- CPU oracle --
+def oracle_rate(glvl, L, T, dt, steps, threads, seed=3000):
+    import oracle as orc
+    import fimocn_subx_realtime_hera_apr2020_gb300 as F
+    from helpers import oracle_for
+
+    orc.set_threads(threads)
+    grid = F.Grid.cached(glvl)
+    cfg = F.FimConfig(nvl=L, ntra=T, dt=dt)
+    fields = F.synthetic_state(grid, cfg, seed=seed, sigma_ps=200.0, noise=0.0)
+    o = oracle_for(grid, cfg)
+    s = o.init_state(o.new_state(fields))
+    o.step(s, 1)  # warm-up
+    t0 = time.perf_counter()
+    for its in range(2, 2 + steps):
+        o.step(s, its)
+    dt_s = (time.perf_counter() - t0) / steps
+    return grid.nip * L / dt_s, dt_s
+
+
+def cpu_baseline(args, threads_all=True):
+    cores = os.cpu_count() or 1
+    L, T = 64, 21
+    v_all, s_all = oracle_rate(6, L, T, 72.0, 2, cores)
+    v_one, s_one = oracle_rate(5, L, T, 72.0, 1, 1)
+    return {"value": v_all, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "CPU oracle (C restatement of the reference Fortran routines, OpenMP) on glvl 6 "
+                      "(40,962 cells), nvl 64, 21 tracers: 2 steps after 1 warm-up, %.2f s/step" % s_all,
+            "value_1thread": v_one,
+            "sample_1thread": "glvl 5 (10,242 cells), nvl 64, 21 tracers, 1 step, %.2f s/step" % s_one}
+
+
+def reference_arm(args, ws, rank):
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    import oracle as orc
+    import fimocn_subx_realtime_hera_apr2020_gb300 as F
+    from helpers import oracle_for
+
+    orc.set_threads(cores)
+    glvl, L, T = 6, 64, 21
+    grid = F.Grid.cached(glvl)
+    cfg = F.FimConfig(nvl=L, ntra=T, dt=72.0)
+    fields = F.synthetic_state(grid, cfg, seed=3000, sigma_ps=200.0, noise=0.0)
+    o = oracle_for(grid, cfg)
+    s = o.init_state(o.new_state(fields))
+    its = 0
+    for _ in range(args.warmup):
+        its += 1
+        o.step(s, its)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        its += 1
+        o.step(s, its)
+    sec = (time.perf_counter() - t0) / args.steps
+    value = grid.nip * L / sec
+    sample = ("CPU oracle (C restatement of the reference Fortran dycore routines, OpenMP, %d threads) on a "
+              "glvl-6 sample (40,962 cells) of the glvl-8 workload, nvl 64, 21 tracers, dt 72 s" % cores)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic seeded balanced state",
+            "config": {"workload": args.workload, "sample_glvl": glvl, "nip": grid.nip, "nvl": L, "ntra": T},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="glvl8_nvl64_t20")
+    p.add_argument("--members", type=int, default=0)
+    p.add_argument("--fp64-steps", type=int, default=2)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    args = p.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        reference_arm(args, ws, rank)
+        return
+    gpu_arm(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -68,9 +68,15 @@ _SIGS = {
     "fim_state_download": ([_VP, _VP, _I, _I, _VP], _I),
     "fim_state_init": ([_VP, _VP], _I),
     "fim_step": ([_VP, _VP, _I, _I], _I),
+    "fim_step_active": ([_VP, _VP, _I], _I),
+    "fim_state_init_member": ([_VP, _VP, _I], _I),
+    "fim_member_set_active": ([_VP, _VP, _I, _I], _I),
+    "fim_member_its": ([_VP, _I], _I),
     "fim_state_budget": ([_VP, _VP, _I, _VP, _VP], _I),
     "fim_check": ([_VP, _VP, _VP], _I),
     "fim_launch_count": ([_VP], ctypes.c_int64),
+    "fim_profile_enable": ([_VP, _I], _I),
+    "fim_profile_report": ([_VP, ctypes.c_char_p, _I], _I),
 }
 _ROUTINES = {
     "fim_edgvar1": [_VP, _I] + [_VP] * 16,

@@ -34,6 +34,7 @@ struct fim_state {
   void* f[FIM_NFIELDS] = {};
   size_t count[FIM_NFIELDS] = {};  // elements per member
   double* sums = nullptr;          // [M][8+T]
+  double* mpd = nullptr;           // FP32-mixed: FP64 Montgomery potential [M][nvl*nip]
   cudaGraphExec_t graph = nullptr;
   long long graph_kernels = 0;
 };
@@ -51,7 +52,7 @@ struct fim_ctx {
   Knobs kn{};
   std::vector<double> thetac, dpsig;
   void* d_thetac = nullptr;
-  StepParams h_sp{};
+  std::vector<StepParams> h_sp;  // one per member
   StepParams* d_sp = nullptr;
   int* d_flags = nullptr;
   long long launches = 0;
@@ -61,10 +62,14 @@ struct fim_ctx {
   void *t_antiflx = nullptr, *t_trmin = nullptr, *t_trmax = nullptr, *t_trcr_lo = nullptr, *t_rp = nullptr,
        *t_rm = nullptr;
   int tchunk = 0;
+  void *f_trcr_lo = nullptr, *f_sp = nullptr, *f_sm = nullptr, *f_trold = nullptr, *f_rp = nullptr,
+       *f_rm = nullptr;
+  int ftchunk = 0;
   void *du = nullptr, *dv = nullptr, *wu = nullptr, *wv = nullptr;
   void *exsmo = nullptr, *exsmo2 = nullptr;
   double* gs_partial = nullptr;
   double* gs_sums = nullptr;  // per-routine globsum output [M][8+T]
+  Prof prof;
   std::string err;
 };
 
@@ -155,6 +160,17 @@ int build_grid(fim_ctx* c, const fim_grid_desc* g, const std::vector<double>& ra
   { const R* t_; if ((rc = upload_conv<R>(c, grnd.data(), (size_t)N, &t_))) return rc; G.grndspd = t_; }
   { const R* t_; if ((rc = upload_conv<R>(c, g->hfcoef, (size_t)N * 36, &t_))) return rc; G.hfcoef = t_; }
   { const double* t_; if ((rc = upload_conv<double>(c, g->area, (size_t)N, &t_))) return rc; G.area_d = t_; }
+  {
+    std::vector<double> sv((size_t)N * 2, 0.0);
+    for (int i = 0; i < N; i++)
+      for (int e = 0; e < nprox[i]; e++) {
+        sv[(size_t)i * 2 + 0] += g->sidevec_c[((size_t)i * 6 + e) * 2 + 0];
+        sv[(size_t)i * 2 + 1] += g->sidevec_c[((size_t)i * 6 + e) * 2 + 1];
+      }
+    const double* t_;
+    if ((rc = upload_conv<double>(c, sv.data(), sv.size(), &t_))) return rc;
+    G.svsum = t_;
+  }
   { const R* t_; if ((rc = upload_conv<R>(c, dfflen.data(), (size_t)c->L, &t_))) return rc; G.dfflen = t_; }
   { const R* t_; if ((rc = upload_conv<R>(c, biharw.data(), (size_t)c->L, &t_))) return rc; G.biharw = t_; }
   { const R* t_; if ((rc = upload_conv<R>(c, smoo.data(), (size_t)c->L + 1, &t_))) return rc; G.smoo = t_; }
@@ -170,13 +186,28 @@ Launch make_launch(fim_ctx* c, int members) {
   l.sp = c->d_sp;
   l.flags = c->d_flags;
   l.counter = &c->launches;
+  l.prof = &c->prof;
   return l;
 }
 
 int push_sp(fim_ctx* c) {
-  StepParams tmp = c->h_sp;  // pageable source: staged before the call returns
-  CK(cudaMemcpyAsync(c->d_sp, &tmp, sizeof(StepParams), cudaMemcpyHostToDevice, c->stream), "push step params");
+  // pageable source: the copy is staged before cudaMemcpyAsync returns
+  CK(cudaMemcpyAsync(c->d_sp, c->h_sp.data(), sizeof(StepParams) * c->h_sp.size(), cudaMemcpyHostToDevice,
+                     c->stream), "push step params");
   return FIM_OK;
+}
+
+// the post-dyn_init parameters of one member (dyn_init.F90:1092-1094:
+// nf,of,vof = 0,2,1 in Fortran numbering, i.e. one abstart before use)
+void reset_member(fim_ctx* c, int m) {
+  StepParams& p = c->h_sp[m];
+  p.its = 0;
+  p.nf = -1;
+  p.of = 1;
+  p.vof = 0;
+  p.ab1 = p.ab2 = p.ab3 = 0.;
+  p.dt = c->cfg.dt;
+  p.active = 1;
 }
 
 int check_launch(fim_ctx* c, const char* what) {
@@ -230,6 +261,24 @@ int ensure_trcadv(fim_ctx* c, int members) {
   if ((rc = ensure(c, &c->t_trcr_lo, n))) return rc;
   if ((rc = ensure(c, &c->t_rp, n))) return rc;
   if ((rc = ensure(c, &c->t_rm, n))) return rc;
+  return FIM_OK;
+}
+
+int ensure_trc_fused(fim_ctx* c, int members) {
+  if (c->f_trcr_lo) return FIM_OK;
+  const size_t NL = (size_t)c->N * c->L;
+  size_t per_tracer = NL * members * 6 * c->esz;
+  int tch = c->T;
+  while (tch > 1 && per_tracer * tch > (size_t)12 << 30) tch = (tch + 1) / 2;
+  c->ftchunk = tch;
+  const size_t n = NL * members * tch;
+  int rc;
+  if ((rc = ensure(c, &c->f_trcr_lo, n))) return rc;
+  if ((rc = ensure(c, &c->f_sp, n))) return rc;
+  if ((rc = ensure(c, &c->f_sm, n))) return rc;
+  if ((rc = ensure(c, &c->f_trold, n))) return rc;
+  if ((rc = ensure(c, &c->f_rp, n))) return rc;
+  if ((rc = ensure(c, &c->f_rm, n))) return rc;
   return FIM_OK;
 }
 
@@ -341,7 +390,7 @@ int edgvar_impl(fim_ctx* c, int which, const R* u_vel, const R* v_vel, const R* 
   if (which == 1)
     launch_edgvar1<R>(l, g, c->str, c->kn.hi_order, du, dv, ddp, dpr, dmo, dtr, due, dve, dde, dle, dme, dqe, dte);
   else
-    launch_edgvar3<R>(l, g, c->str, ddp, dtr, dde, dte);
+    launch_edgvar3<R>(l, g, c->str, ddp, dtr, dde, dte, c->kn.hi_order ? c->T : 1);
   if ((rc = check_launch(c, which == 1 ? "edgvar1" : "edgvar3"))) return rc;
   return s.finish();
 }
@@ -445,7 +494,7 @@ int hybgen_impl(fim_ctx* c, int its, const R* targt, R* us3d, R* vs3d, R* tr3d, 
   R* dp = s.map(dp3d, NL, 1);
   R* pr = s.map(pr3d, NI, 1);
   if (s.rc) return s.rc;
-  c->h_sp.its = its;
+  for (auto& p : c->h_sp) p.its = its;
   if ((rc = push_sp(c))) return rc;
   HybgenScratch<R> w{(R*)c->exsmo, (R*)c->exsmo2};
   launch_hybgen<R>(make_launch(c, 1), grid_of<R>(c), c->str, c->kn, w, tg, u, v, tr, sd, ex, dp, pr);
@@ -469,7 +518,7 @@ int hystat_impl(fim_ctx* c, int its, R* ph3d, const R* ex3d, R* mp3d, const R* d
   R* ps = s.map(psrf, (size_t)c->N, 1);
   R* pt = s.map(ptdcy, (size_t)c->N * 2, 1);
   if (s.rc) return s.rc;
-  c->h_sp.its = its;
+  for (auto& p : c->h_sp) p.its = its;
   if ((rc = push_sp(c))) return rc;
   launch_hystat<R>(make_launch(c, 1), grid_of<R>(c), c->str, ph, ex, mp, dp, tr, td, ps, pt);
   if ((rc = check_launch(c, "hystat"))) return rc;
@@ -522,28 +571,41 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
   launch_edgvar1<R>(l, g, s, c->kn.hi_order, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_DP3D),
                     F<R>(st, FIM_PR3D), F<R>(st, FIM_MP3D), F<R>(st, FIM_TR3D), F<R>(st, FIM_U_EDG),
                     F<R>(st, FIM_V_EDG), F<R>(st, FIM_DP_EDG), F<R>(st, FIM_LP_EDG), F<R>(st, FIM_MONT_EDG),
-                    F<R>(st, FIM_UVSQ_EDG), F<R>(st, FIM_TRC_EDG));
-  if (c->kn.hi_order)
-    launch_edgvar3<R>(l, g, s, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), F<R>(st, FIM_DP_EDG), F<R>(st, FIM_TRC_EDG));
+                    F<R>(st, FIM_UVSQ_EDG), F<R>(st, FIM_TRC_EDG), st->mpd);
+  if (c->kn.hi_order) {
+    // dp edges with edgvar3's two-sided average; tracer edges keep the
+    // own-side values, averaged where the fused tracer kernels use them
+    launch_edgvar3<R>(l, g, s, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), F<R>(st, FIM_DP_EDG), F<R>(st, FIM_TRC_EDG),
+                      1);
+    launch_tracer_own<R>(l, g, s, F<R>(st, FIM_TR3D), F<R>(st, FIM_TRC_EDG));
+  }
   CnuityScratch<R> cw{(R*)c->antifx, (R*)c->delp_lo, (R*)c->p_plus, (R*)c->p_mnus, (R*)c->r_plus, (R*)c->r_mnus};
   launch_cnuity<R>(l, g, s, cw, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_U_EDG), F<R>(st, FIM_V_EDG),
                    F<R>(st, FIM_DP_EDG), F<R>(st, FIM_LP_EDG), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D),
                    F<R>(st, FIM_EX3D), F<R>(st, FIM_DP_TDCY), F<R>(st, FIM_DPL_TDCY), F<R>(st, FIM_MASSFX),
                    F<R>(st, FIM_WS3D));
-  TrcadvScratch<R> tw{(R*)c->t_antiflx, (R*)c->t_trmin, (R*)c->t_trmax, (R*)c->t_trcr_lo, (R*)c->t_rp,
-                      (R*)c->t_rm, c->tchunk};
-  launch_trcadv<R>(l, g, s, tw, F<R>(st, FIM_TRC_EDG), F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP),
-                   F<R>(st, FIM_TRC_TDCY), F<R>(st, FIM_TRL_TDCY), F<R>(st, FIM_MASSFX), F<R>(st, FIM_DP3D));
+  if (c->kn.hi_order) {
+    TrcFusedScratch<R> fw{(R*)c->f_trcr_lo, (R*)c->f_sp, (R*)c->f_sm, (R*)c->f_trold, (R*)c->f_rp, (R*)c->f_rm,
+                          c->ftchunk};
+    launch_tracers_fused<R>(l, g, s, fw, F<R>(st, FIM_TRC_EDG), F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP),
+                            F<R>(st, FIM_TRC_TDCY), F<R>(st, FIM_TRL_TDCY), F<R>(st, FIM_MASSFX),
+                            F<R>(st, FIM_DP3D));
+  } else {
+    TrcadvScratch<R> tw{(R*)c->t_antiflx, (R*)c->t_trmin, (R*)c->t_trmax, (R*)c->t_trcr_lo, (R*)c->t_rp,
+                        (R*)c->t_rm, c->tchunk};
+    launch_trcadv<R>(l, g, s, tw, F<R>(st, FIM_TRC_EDG), F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP),
+                     F<R>(st, FIM_TRC_TDCY), F<R>(st, FIM_TRL_TDCY), F<R>(st, FIM_MASSFX), F<R>(st, FIM_DP3D));
+  }
   MomtumScratch<R> mw{(R*)c->du, (R*)c->dv, (R*)c->wu, (R*)c->wv};
   launch_momtum<R>(l, g, s, c->kn, mw, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_EX3D),
                    F<R>(st, FIM_RELVOR), F<R>(st, FIM_U_EDG), F<R>(st, FIM_V_EDG), F<R>(st, FIM_TRC_EDG),
                    F<R>(st, FIM_MONT_EDG), F<R>(st, FIM_UVSQ_EDG), F<R>(st, FIM_U_TDCY), F<R>(st, FIM_V_TDCY),
-                   F<R>(st, FIM_DP3D));
+                   F<R>(st, FIM_DP3D), st->mpd, st->mpd ? F<R>(st, FIM_TR3D) : nullptr);
   HybgenScratch<R> hw{(R*)c->exsmo, (R*)c->exsmo2};
   launch_hybgen<R>(l, g, s, c->kn, hw, g.thetac, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_TR3D),
                    F<R>(st, FIM_SDOT), F<R>(st, FIM_EX3D), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D));
   launch_hystat<R>(l, g, s, F<R>(st, FIM_PH3D), F<R>(st, FIM_EX3D), F<R>(st, FIM_MP3D), F<R>(st, FIM_DP3D),
-                   F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP), F<R>(st, FIM_PSRF), F<R>(st, FIM_PTDCY));
+                   F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP), F<R>(st, FIM_PSRF), F<R>(st, FIM_PTDCY), st->mpd);
   launch_globsum<R>(l, g, s, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), (const R*)nullptr, (const R*)nullptr,
                     F<R>(st, FIM_PR3D), F<R>(st, FIM_EX3D), (const R*)nullptr, c->gs_partial, st->sums);
   return FIM_OK;
@@ -552,7 +614,9 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
 int ensure_all(fim_ctx* c) {
   int rc;
   if ((rc = ensure_cnuity(c, c->M))) return rc;
-  if ((rc = ensure_trcadv(c, c->M))) return rc;
+  if (c->kn.hi_order) {
+    if ((rc = ensure_trc_fused(c, c->M))) return rc;
+  } else if ((rc = ensure_trcadv(c, c->M))) return rc;
   if ((rc = ensure_momtum(c, c->M))) return rc;
   if ((rc = ensure_hybgen(c, c->M))) return rc;
   if ((rc = ensure_globsum(c, c->M))) return rc;
@@ -560,29 +624,34 @@ int ensure_all(fim_ctx* c) {
 }
 
 template <typename R>
-int state_init_impl(fim_ctx* c, fim_state* st) {
+R* FM(fim_ctx* c, fim_state* st, int f, int m) { return (R*)st->f[f] + (size_t)m * st->count[f]; }
+
+// dyn_init.F90:870-906,1037-1094 for members [m0, m0+nm)
+template <typename R>
+int state_init_impl(fim_ctx* c, fim_state* st, int m0, int nm) {
   int rc;
   if ((rc = ensure_all(c))) return rc;
-  Launch l = make_launch(c, c->M);
-  Grid<R>& g = grid_of<R>(c);
-  c->h_sp.its = 0;
+  for (int m = m0; m < m0 + nm; m++) {
+    c->h_sp[m].its = 0;
+    c->h_sp[m].active = 1;
+  }
   if ((rc = push_sp(c))) return rc;
+  Launch l = make_launch(c, nm);
+  l.sp = c->d_sp + m0;
+  l.flags = c->d_flags + m0;
+  Grid<R>& g = grid_of<R>(c);
   HybgenScratch<R> hw{(R*)c->exsmo, (R*)c->exsmo2};
-  launch_hybgen<R>(l, g, c->str, c->kn, hw, g.thetac, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_TR3D),
-                   F<R>(st, FIM_SDOT), F<R>(st, FIM_EX3D), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D));
-  launch_prdp_from_ex<R>(l, g, c->str, F<R>(st, FIM_EX3D), F<R>(st, FIM_PR3D), F<R>(st, FIM_DP3D));
-  const size_t M = c->M;
-  CK(cudaMemsetAsync(st->f[FIM_PSRF], 0, M * st->count[FIM_PSRF] * c->esz, c->stream), "zero psrf");
-  CK(cudaMemsetAsync(st->f[FIM_PTDCY], 0, M * st->count[FIM_PTDCY] * c->esz, c->stream), "zero ptdcy");
-  launch_hystat<R>(l, g, c->str, F<R>(st, FIM_PH3D), F<R>(st, FIM_EX3D), F<R>(st, FIM_MP3D), F<R>(st, FIM_DP3D),
-                   F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP), F<R>(st, FIM_PSRF), F<R>(st, FIM_PTDCY));
+  auto P = [&](int f) { return FM<R>(c, st, f, m0); };
+  launch_hybgen<R>(l, g, c->str, c->kn, hw, g.thetac, P(FIM_US3D), P(FIM_VS3D), P(FIM_TR3D), P(FIM_SDOT),
+                   P(FIM_EX3D), P(FIM_DP3D), P(FIM_PR3D));
+  launch_prdp_from_ex<R>(l, g, c->str, P(FIM_EX3D), P(FIM_PR3D), P(FIM_DP3D));
+  CK(cudaMemsetAsync(P(FIM_PSRF), 0, nm * st->count[FIM_PSRF] * c->esz, c->stream), "zero psrf");
+  CK(cudaMemsetAsync(P(FIM_PTDCY), 0, nm * st->count[FIM_PTDCY] * c->esz, c->stream), "zero ptdcy");
+  launch_hystat<R>(l, g, c->str, P(FIM_PH3D), P(FIM_EX3D), P(FIM_MP3D), P(FIM_DP3D), P(FIM_TR3D), P(FIM_TRDP),
+                   P(FIM_PSRF), P(FIM_PTDCY), st->mpd ? st->mpd + (size_t)m0 * st->count[FIM_MP3D] : nullptr);
   const int zero[] = {FIM_U_TDCY, FIM_V_TDCY, FIM_DP_TDCY, FIM_DPL_TDCY, FIM_TRC_TDCY, FIM_TRL_TDCY, FIM_MASSFX};
-  for (int f : zero) CK(cudaMemsetAsync(st->f[f], 0, M * st->count[f] * c->esz, c->stream), "zero tendencies");
-  // dyn_init.F90:1092-1094: nf,of,vof = 0,2,1 (Fortran), one abstart before use
-  c->h_sp.nf = -1;
-  c->h_sp.of = 1;
-  c->h_sp.vof = 0;
-  c->h_sp.ab1 = c->h_sp.ab2 = c->h_sp.ab3 = 0.;
+  for (int f : zero) CK(cudaMemsetAsync(P(f), 0, nm * st->count[f] * c->esz, c->stream), "zero tendencies");
+  for (int m = m0; m < m0 + nm; m++) reset_member(c, m);
   if ((rc = push_sp(c))) return rc;
   if ((rc = check_launch(c, "state init"))) return rc;
   CK(cudaStreamSynchronize(c->stream), "state init sync");
@@ -684,10 +753,11 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
   int rc = (c->prec == FIM_PREC_F64)
                ? build_grid<double>(c, g, rarea, corio, grnd, dfflen, biharw, smoo, prox, proxs, nprox)
                : build_grid<float>(c, g, rarea, corio, grnd, dfflen, biharw, smoo, prox, proxs, nprox);
-  if (!rc) rc = dalloc(c, (void**)&c->d_sp, sizeof(StepParams));
+  if (!rc) rc = dalloc(c, (void**)&c->d_sp, sizeof(StepParams) * c->M);
   if (!rc) rc = dalloc(c, (void**)&c->d_flags, sizeof(int) * c->M);
   if (!rc) {
-    c->h_sp = StepParams{0, -1, 1, 0, 0., 0., 0., cfg->dt};
+    c->h_sp.assign(c->M, StepParams{});
+    for (int m = 0; m < c->M; m++) reset_member(c, m);
     if (cudaMemset(c->d_flags, 0, sizeof(int) * c->M) != cudaSuccess) rc = FIM_ECUDA;
     if (!rc) rc = push_sp(c);
   }
@@ -714,23 +784,26 @@ int64_t fim_launch_count(const fim_ctx* c) { return c ? c->launches : -1; }
 
 int fim_get_ab(const fim_ctx* c, int* nf, int* of, int* vof, double* ab1, double* ab2, double* ab3) {
   if (!c) return FIM_EINVAL;
-  if (nf) *nf = c->h_sp.nf + 1;
-  if (of) *of = c->h_sp.of + 1;
-  if (vof) *vof = c->h_sp.vof + 1;
-  if (ab1) *ab1 = c->h_sp.ab1;
-  if (ab2) *ab2 = c->h_sp.ab2;
-  if (ab3) *ab3 = c->h_sp.ab3;
+  const StepParams& p = c->h_sp[0];
+  if (nf) *nf = p.nf + 1;
+  if (of) *of = p.of + 1;
+  if (vof) *vof = p.vof + 1;
+  if (ab1) *ab1 = p.ab1;
+  if (ab2) *ab2 = p.ab2;
+  if (ab3) *ab3 = p.ab3;
   return FIM_OK;
 }
 
 int fim_set_ab(fim_ctx* c, int nf, int of, int vof, double ab1, double ab2, double ab3) {
   if (!c || nf < 1 || nf > 3 || of < 1 || of > 3 || vof < 1 || vof > 3) return FIM_EINVAL;
-  c->h_sp.nf = nf - 1;
-  c->h_sp.of = of - 1;
-  c->h_sp.vof = vof - 1;
-  c->h_sp.ab1 = ab1;
-  c->h_sp.ab2 = ab2;
-  c->h_sp.ab3 = ab3;
+  for (auto& p : c->h_sp) {
+    p.nf = nf - 1;
+    p.of = of - 1;
+    p.vof = vof - 1;
+    p.ab1 = ab1;
+    p.ab2 = ab2;
+    p.ab3 = ab3;
+  }
   return push_sp(c);
 }
 
@@ -738,7 +811,7 @@ int fim_abstart(fim_ctx* c, int its, int its_start, int* nf, int* of, int* vof, 
                 double* adbash3) {
   (void)its_start;
   if (!c || its < 1) return FIM_EINVAL;
-  host_abstart(c->h_sp, its);
+  for (auto& p : c->h_sp) host_abstart(p, its);
   int rc = push_sp(c);
   if (rc) return rc;
   return fim_get_ab(c, nf, of, vof, adbash1, adbash2, adbash3);
@@ -862,6 +935,10 @@ int fim_state_alloc(fim_ctx* c, fim_state** out) {
   }
   int rc = dalloc(c, (void**)&st->sums, (size_t)c->M * (8 + c->T) * sizeof(double));
   if (rc) { delete st; return rc; }
+  if (c->prec == FIM_PREC_F32) {
+    if ((rc = dalloc(c, (void**)&st->mpd, (size_t)c->M * cnt[FIM_MP3D] * sizeof(double)))) { delete st; return rc; }
+    cudaMemsetAsync(st->mpd, 0, (size_t)c->M * cnt[FIM_MP3D] * sizeof(double), c->stream);
+  }
   if ((rc = ensure_all(c))) { delete st; return rc; }
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) { delete st; return set_err(c, FIM_ECUDA, "state alloc"); }
   *out = st;
@@ -876,8 +953,9 @@ int fim_state_free(fim_ctx* c, fim_state* st) {
     for (auto it = c->owned.begin(); it != c->owned.end(); ++it)
       if (*it == st->f[f]) { cudaFree(*it); c->owned.erase(it); break; }
   }
-  for (auto it = c->owned.begin(); it != c->owned.end(); ++it)
-    if (*it == st->sums) { cudaFree(*it); c->owned.erase(it); break; }
+  for (void* extra : {(void*)st->sums, (void*)st->mpd})
+    for (auto it = c->owned.begin(); it != c->owned.end(); ++it)
+      if (extra && *it == extra) { cudaFree(*it); c->owned.erase(it); break; }
   delete st;
   return FIM_OK;
 }
@@ -909,21 +987,34 @@ int fim_state_download(fim_ctx* c, fim_state* st, int field, int member, void* h
 
 int fim_state_init(fim_ctx* c, fim_state* st) {
   if (!c || !st) return FIM_EINVAL;
-  return c->prec == FIM_PREC_F64 ? state_init_impl<double>(c, st) : state_init_impl<float>(c, st);
+  return c->prec == FIM_PREC_F64 ? state_init_impl<double>(c, st, 0, c->M)
+                                 : state_init_impl<float>(c, st, 0, c->M);
 }
 
-int fim_step(fim_ctx* c, fim_state* st, int its, int use_graph) {
-  if (!c || !st || its < 1) return FIM_EINVAL;
-  int rc = ensure_all(c);
-  if (rc) return rc;
-  if (c->h_sp.its != its - 1) {
-    c->h_sp.its = its - 1;
-    if ((rc = push_sp(c))) return rc;
-  }
+int fim_state_init_member(fim_ctx* c, fim_state* st, int member) {
+  if (!c || !st || member < 0 || member >= c->M) return FIM_EINVAL;
+  return c->prec == FIM_PREC_F64 ? state_init_impl<double>(c, st, member, 1)
+                                 : state_init_impl<float>(c, st, member, 1);
+}
+
+int fim_member_set_active(fim_ctx* c, fim_state* st, int member, int active) {
+  (void)st;
+  if (!c || member < 0 || member >= c->M) return FIM_EINVAL;
+  c->h_sp[member].active = active ? 1 : 0;
+  return push_sp(c);
+}
+
+int fim_member_its(const fim_ctx* c, int member) {
+  if (!c || member < 0 || member >= c->M) return -1;
+  return c->h_sp[member].its;
+}
+
+static int run_step(fim_ctx* c, fim_state* st, int use_graph) {
+  int rc;
   if (use_graph) {
     if (!st->graph) {
       // the step is its-invariant: every step-dependent scalar is read from
-      // the device parameter block that k_step_begin advances
+      // the per-member device parameter block that k_step_begin advances
       cudaGraph_t graph;
       long long before = c->launches;
       CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
@@ -944,8 +1035,29 @@ int fim_step(fim_ctx* c, fim_state* st, int its, int use_graph) {
     if (rc) return rc;
     if ((rc = check_launch(c, "step"))) return rc;
   }
-  host_abstart(c->h_sp, its);
+  for (auto& p : c->h_sp)
+    if (p.active) host_abstart(p, p.its + 1);
   return FIM_OK;
+}
+
+int fim_step(fim_ctx* c, fim_state* st, int its, int use_graph) {
+  if (!c || !st || its < 1) return FIM_EINVAL;
+  int rc = ensure_all(c);
+  if (rc) return rc;
+  bool dirty = false;
+  for (auto& p : c->h_sp) {
+    if (!p.active) { p.active = 1; dirty = true; }
+    if (p.its != its - 1) { p.its = its - 1; dirty = true; }
+  }
+  if (dirty && (rc = push_sp(c))) return rc;
+  return run_step(c, st, use_graph);
+}
+
+int fim_step_active(fim_ctx* c, fim_state* st, int use_graph) {
+  if (!c || !st) return FIM_EINVAL;
+  int rc = ensure_all(c);
+  if (rc) return rc;
+  return run_step(c, st, use_graph);
 }
 
 int fim_state_budget(fim_ctx* c, fim_state* st, int member, double* qtrcr, fim_budget* out) {
@@ -959,6 +1071,28 @@ int fim_state_budget(fim_ctx* c, fim_state* st, int member, double* qtrcr, fim_b
     out->qmass = h[0]; out->qmsqv = h[1]; out->qmsqw = h[2]; out->qmso3 = h[3];
     out->qmste = h[4]; out->qmstr = h[5]; out->qmstrn = h[6]; out->qmstrc = h[7];
   }
+  return FIM_OK;
+}
+
+int fim_profile_enable(fim_ctx* c, int on) {
+  if (!c) return FIM_EINVAL;
+  if (!on) c->prof.collect();
+  c->prof.on = on != 0;
+  return FIM_OK;
+}
+
+int fim_profile_report(fim_ctx* c, char* buf, int len) {
+  if (!c || !buf || len <= 0) return FIM_EINVAL;
+  c->prof.collect();
+  std::string out;
+  char line[256];
+  for (auto& kv : c->prof.agg) {
+    snprintf(line, sizeof line, "%s %lld %.6f\n", kv.first.c_str(), kv.second.first, kv.second.second);
+    out += line;
+  }
+  if ((int)out.size() + 1 > len) return FIM_EINVAL;
+  memcpy(buf, out.c_str(), out.size() + 1);
+  c->prof.agg.clear();
   return FIM_OK;
 }
 

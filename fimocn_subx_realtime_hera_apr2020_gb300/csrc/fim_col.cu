@@ -334,6 +334,8 @@ __global__ void __launch_bounds__(kColBlock) k_regrid(Grid<R> g, Strides s, Knob
   const int N = g.N, L = g.L, L1 = L + 1;
   if (i >= N) return;
   const size_t m = blockIdx.y;
+  sp += m;
+  if (!sp->active) return;
   tr3d += m * s.tr; ex3d += m * s.intf; pr3d += m * s.intf; exsmo += m * s.intf;
   R thcol[ML], excol[ML + 1];
   for (int k = 0; k < L; k++) thcol[k] = tr3d[(size_t)i * L + k];
@@ -381,6 +383,8 @@ __global__ void __launch_bounds__(kColBlock) k_remap(Grid<R> g, Strides s, Knobs
   const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
   if (i >= N) return;
   const size_t m = blockIdx.y;
+  sp += m;
+  if (!sp->active) return;
   exsmo += m * s.intf; us3d += m * s.cell; vs3d += m * s.cell; tr3d += m * s.tr; sdot += m * s.intf;
   ex3d += m * s.intf; dp3d += m * s.cell; pr3d += m * s.intf;
   const int its = sp->its;
@@ -484,14 +488,18 @@ __global__ void __launch_bounds__(kColBlock) k_remap(Grid<R> g, Strides s, Knobs
 template <typename R>
 __global__ void __launch_bounds__(kBlock2) k_hystat(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     R* __restrict__ ph3d, const R* __restrict__ ex3d, R* __restrict__ mp3d, const R* __restrict__ dp3d,
-    R* __restrict__ tr3d, R* __restrict__ trdp, R* __restrict__ psrf, R* __restrict__ ptdcy) {
+    R* __restrict__ tr3d, R* __restrict__ trdp, R* __restrict__ psrf, R* __restrict__ ptdcy,
+    double* __restrict__ mpd) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
   if (warp >= N) return;
   const int i = warp;
   const size_t m = blockIdx.y;
+  sp += m;
+  if (!sp->active) return;
   ph3d += m * s.intf; ex3d += m * s.intf; mp3d += m * s.cell; dp3d += m * s.cell; tr3d += m * s.tr;
   trdp += m * s.tr; psrf += m * s.col; ptdcy += m * 2 * s.col;
+  if (mpd) mpd += m * s.cell;
   const int its = sp->its;
   const size_t NL = (size_t)N * L;
   // surface pressure: sum of all layer thicknesses
@@ -527,6 +535,7 @@ __global__ void __launch_bounds__(kBlock2) k_hystat(Grid<R> g, Strides s, const 
     const double mp = carry + sc;
     if (act) {
       mp3d[(size_t)i * L + k] = R(mp);
+      if (mpd) mpd[(size_t)i * L + k] = mp;
       ph3d[(size_t)i * L1 + k + 1] = R(mp - th * exk1);
     }
     carry += __shfl_sync(0xffffffffu, sc, 31);
@@ -616,6 +625,8 @@ __global__ void k_globsum_final(Grid<R> g, Strides s, const StepParams* __restri
     const R* __restrict__ qf2d, const double* __restrict__ partial, int nblk, double* __restrict__ sums) {
   const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
   const size_t m = blockIdx.x;
+  sp += m;
+  if (!sp->active) return;
   tr += m * s.tr; pr3d += m * s.intf; ex3d += m * s.intf;
   __shared__ double red[4][kBlock2];
   double sr = 0., src = 0., srn = 0., se = 0.;
@@ -673,42 +684,47 @@ __global__ void __launch_bounds__(kBlock2) k_prdp_from_ex(Grid<R> g, Strides s, 
   }
 }
 
-#define COUNT(l) do { if ((l).counter) ++*(l).counter; } while (0)
 
 template <typename R>
 void launch_hybgen(const Launch& l, const Grid<R>& g, const Strides& s, const Knobs& kn, const HybgenScratch<R>& w,
                    const R* targt, R* us3d, R* vs3d, R* tr3d, R* sdot, R* ex3d, R* dp3d, R* pr3d) {
   dim3 gc(nblocks(g.N, kColBlock), l.members);
   if (g.L <= 64) {
+    FIM_KBEGIN(l, "k_regrid");
     k_regrid<R, 64><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, tr3d, ex3d, pr3d, w.exsmo, l.flags);
   } else {
+    FIM_KBEGIN(l, "k_regrid");
     k_regrid<R, kMaxL><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, tr3d, ex3d, pr3d, w.exsmo, l.flags);
   }
-  COUNT(l);
+  FIM_KEND(l);
   const R* ex_in = w.exsmo;
   if (kn.intfc_smooth > 0.) {
     dim3 gs(nblocks((long long)g.N * (g.L + 1), kBlock2), l.members);
     // Fortran levels kbl+2..nvl -> 0-based interfaces kbl+1..nvl-1
+    FIM_KBEGIN(l, "k_dffusn_lev");
     k_dffusn_lev<R><<<gs, kBlock2, 0, l.stream>>>(g, s, kn.kbl + 1, g.L - 1, w.exsmo, w.exsmo2);
-    COUNT(l);
+    FIM_KEND(l);
     ex_in = w.exsmo2;
   }
   if (g.L <= 64) {
+    FIM_KBEGIN(l, "k_remap");
     k_remap<R, 64><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d,
                                                     dp3d, pr3d, l.flags);
   } else {
+    FIM_KBEGIN(l, "k_remap");
     k_remap<R, kMaxL><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d,
                                                        dp3d, pr3d, l.flags);
   }
-  COUNT(l);
+  FIM_KEND(l);
 }
 
 template <typename R>
 void launch_hystat(const Launch& l, const Grid<R>& g, const Strides& s, R* ph3d, const R* ex3d, R* mp3d,
-                   const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy) {
+                   const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy, double* mpd) {
   dim3 gw(nblocks((long long)g.N * 32, kBlock2), l.members);
-  k_hystat<R><<<gw, kBlock2, 0, l.stream>>>(g, s, l.sp, ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy);
-  COUNT(l);
+  FIM_KBEGIN(l, "k_hystat");
+  k_hystat<R><<<gw, kBlock2, 0, l.stream>>>(g, s, l.sp, ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy, mpd);
+  FIM_KEND(l);
 }
 
 size_t globsum_partials(int N, int L, int T, int members) {
@@ -721,25 +737,28 @@ void launch_globsum(const Launch& l, const Grid<R>& g, const Strides& s, const R
                     const R* rn2d, const R* rc2d, const R* pr3d, const R* ex3d, const R* qf2d,
                     double* partial, double* sums) {
   dim3 gl(kGsBlocks, l.members);
+  FIM_KBEGIN(l, "k_globsum_levels");
   k_globsum_levels<R><<<gl, kBlock2, 0, l.stream>>>(g, s, dp3d, tr, partial);
-  COUNT(l);
+  FIM_KEND(l);
+  FIM_KBEGIN(l, "k_globsum_final");
   k_globsum_final<R><<<l.members, kBlock2, 0, l.stream>>>(g, s, l.sp, tr, rn2d, rc2d, pr3d, ex3d, qf2d, partial,
                                                            kGsBlocks, sums);
-  COUNT(l);
+  FIM_KEND(l);
 }
 
 template <typename R>
 void launch_prdp_from_ex(const Launch& l, const Grid<R>& g, const Strides& s, const R* ex3d, R* pr3d, R* dp3d) {
   dim3 gs(nblocks((long long)g.N * (g.L + 1), kBlock2), l.members);
+  FIM_KBEGIN(l, "k_prdp_from_ex");
   k_prdp_from_ex<R><<<gs, kBlock2, 0, l.stream>>>(g, s, ex3d, pr3d, dp3d);
-  COUNT(l);
+  FIM_KEND(l);
 }
 
 #define INSTANTIATE(R)                                                                                       \
   template void launch_hybgen<R>(const Launch&, const Grid<R>&, const Strides&, const Knobs&,               \
                                  const HybgenScratch<R>&, const R*, R*, R*, R*, R*, R*, R*, R*);            \
   template void launch_hystat<R>(const Launch&, const Grid<R>&, const Strides&, R*, const R*, R*, const R*, \
-                                 R*, R*, R*, R*);                                                           \
+                                 R*, R*, R*, R*, double*);                                                  \
   template void launch_globsum<R>(const Launch&, const Grid<R>&, const Strides&, const R*, const R*,        \
                                   const R*, const R*, const R*, const R*, const R*, double*, double*);      \
   template void launch_prdp_from_ex<R>(const Launch&, const Grid<R>&, const Strides&, const R*, R*, R*);

@@ -42,11 +42,12 @@ __global__ void __launch_bounds__(kBlock) k_edgvar1(Grid<R> g, Strides s, int hi
     const R* __restrict__ u, const R* __restrict__ v, const R* __restrict__ delp,
     const R* __restrict__ pres, const R* __restrict__ montg, const R* __restrict__ tracr,
     R* __restrict__ u_edg, R* __restrict__ v_edg, R* __restrict__ dp_edg, R* __restrict__ lp_edg,
-    R* __restrict__ mont_edg, R* __restrict__ uvsq_edg, R* __restrict__ trc_edg) {
+    R* __restrict__ mont_edg, R* __restrict__ uvsq_edg, R* __restrict__ trc_edg, const double* __restrict__ mpd) {
   int i, k;
   if (!cell_level(g.N, g.L, i, k)) return;
   const int L = g.L, N = g.N, L1 = L + 1;
   const size_t m = blockIdx.y;
+  if (mpd) mpd += m * s.cell;
   u += m * s.cell; v += m * s.cell; delp += m * s.cell; pres += m * s.intf;
   montg += m * s.cell; tracr += m * s.tr;
   u_edg += m * s.edge; v_edg += m * s.edge; dp_edg += m * s.edge; lp_edg += m * s.edge;
@@ -87,8 +88,15 @@ __global__ void __launch_bounds__(kBlock) k_edgvar1(Grid<R> g, Strides s, int hi
     lp_edg[o] = (p1a + p1b + pres[(size_t)i2 * L1 + k] + pres[(size_t)i2 * L1 + k + 1] +
                  half * (pres[(size_t)i3t * L1 + k] + pres[(size_t)i3t * L1 + k + 1] +
                          pres[(size_t)i3l * L1 + k] + pres[(size_t)i3l * L1 + k + 1])) * divby6;
-    mont_edg[o] = (two * (m1 + montg[(size_t)i2 * L + k]) + montg[(size_t)i3t * L + k] +
-                   montg[(size_t)i3l * L + k]) * divby6;
+    if (mpd) {
+      // edge minus cell value from FP64 differences (no cancellation in FP32)
+      const double mc = mpd[(size_t)i * L + k];
+      mont_edg[o] = R((2.0 * (mpd[(size_t)i2 * L + k] - mc) + (mpd[(size_t)i3t * L + k] - mc) +
+                       (mpd[(size_t)i3l * L + k] - mc)) * (1.0 / 6.0));
+    } else {
+      mont_edg[o] = (two * (m1 + montg[(size_t)i2 * L + k]) + montg[(size_t)i3t * L + k] +
+                     montg[(size_t)i3l * L + k]) * divby6;
+    }
     uvsq_edg[o] = half * (ue * ue + ve * ve);
   }
   const int ntr = hi_order ? 1 : g.T;
@@ -177,6 +185,8 @@ __global__ void __launch_bounds__(kBlock) k_cnuity12(Grid<R> g, Strides s, const
   if (!cell_level(g.N, g.L, i, k)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
+  sp += m;
+  if (!sp->active) return;
   u_edg += m * s.edge; v_edg += m * s.edge; dp_edg += m * s.edge; delp += m * s.cell;
   massfx += m * s.mf; dplo_tndcy += m * s.ab; antifx += m * s.edge; delp_lo += m * s.cell;
   p_plus += m * s.cell; p_mnus += m * s.cell;
@@ -225,6 +235,8 @@ __global__ void __launch_bounds__(kBlock) k_cnuity3(Grid<R> g, Strides s, const 
   if (!cell_level(g.N, g.L, i, k)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
+  sp += m;
+  if (!sp->active) return;
   delp_lo += m * s.cell; delp += m * s.cell; dp_tndcy += m * s.ab;
   p_plus += m * s.cell; p_mnus += m * s.cell; r_plus += m * s.cell; r_mnus += m * s.cell;
   const int of = sp->of, vof = sp->vof;
@@ -260,6 +272,8 @@ __global__ void __launch_bounds__(kBlock) k_cnuity4(Grid<R> g, Strides s, const 
   if (!cell_level(g.N, g.L, i, k)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
+  sp += m;
+  if (!sp->active) return;
   antifx += m * s.edge; r_plus += m * s.cell; r_mnus += m * s.cell; massfx += m * s.mf;
   dplo_tndcy += m * s.ab; dp_tndcy += m * s.ab; delp += m * s.cell;
   const int nf = sp->nf, of = sp->of, vof = sp->vof;
@@ -299,6 +313,8 @@ __global__ void __launch_bounds__(kBlock) k_cnuity5(Grid<R> g, Strides s, const 
   if (warp >= N) return;
   const int i = warp;
   const size_t m = blockIdx.y;
+  sp += m;
+  if (!sp->active) return;
   pres += m * s.intf; delp += m * s.cell; exner += m * s.intf; dp_tndcy += m * s.ab;
   omega += m * s.cell; lp_edg += m * s.edge; u += m * s.cell; v += m * s.cell;
   const int nf = sp->nf, of = sp->of, vof = sp->vof;
@@ -362,6 +378,8 @@ __global__ void __launch_bounds__(kBlock) k_trcadv1(Grid<R> g, Strides s, const 
   if (!cell_level(g.N, g.L, i, k)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
+  sp += m;
+  if (!sp->active) return;
   const int tz = blockIdx.z, t = t0 + tz;
   const size_t NL = (size_t)N * L;
   massfx += m * s.mf; delp += m * s.cell;
@@ -417,6 +435,8 @@ __global__ void __launch_bounds__(kBlock) k_trcadv2(Grid<R> g, Strides s, const 
   if (!cell_level(g.N, g.L, i, k)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
+  sp += m;
+  if (!sp->active) return;
   const int tz = blockIdx.z, t = t0 + tz;
   const size_t NL = (size_t)N * L;
   delp += m * s.cell;
@@ -465,6 +485,8 @@ __global__ void __launch_bounds__(kBlock) k_trcadv3(Grid<R> g, Strides s, const 
   if (!cell_level(g.N, g.L, i, k)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
+  sp += m;
+  if (!sp->active) return;
   const int tz = blockIdx.z, t = t0 + tz;
   const size_t NL = (size_t)N * L;
   delp += m * s.cell;
@@ -578,7 +600,7 @@ __global__ void __launch_bounds__(kBlock) k_momtum1(Grid<R> g, Strides s, Knobs 
     R* __restrict__ u, R* __restrict__ v, const R* __restrict__ du, const R* __restrict__ dv,
     const R* __restrict__ exner, R* __restrict__ relvor, const R* __restrict__ u_edg, const R* __restrict__ v_edg,
     const R* __restrict__ trc_edg, const R* __restrict__ mont_edg, const R* __restrict__ uvsq_edg,
-    R* __restrict__ u_tndcy, R* __restrict__ v_tndcy) {
+    R* __restrict__ u_tndcy, R* __restrict__ v_tndcy, const double* __restrict__ mpd, const R* __restrict__ tr0) {
   __shared__ R top[kBlock / 32][3][2];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -586,11 +608,15 @@ __global__ void __launch_bounds__(kBlock) k_momtum1(Grid<R> g, Strides s, Knobs 
   if (warp >= N) return;
   const int i = warp;
   const size_t m = blockIdx.y;
+  sp += m;
+  if (!sp->active) return;
   u += m * s.cell; v += m * s.cell; exner += m * s.intf; relvor += m * s.cell;
   u_edg += m * s.edge; v_edg += m * s.edge; trc_edg += m * s.tredg; mont_edg += m * s.edge;
   uvsq_edg += m * s.edge; u_tndcy += m * s.ab; v_tndcy += m * s.ab;
   const bool have_d = du != nullptr;
   if (have_d) { du += m * s.cell; dv += m * s.cell; }
+  const bool split = mpd != nullptr;
+  if (split) { mpd += m * s.cell; tr0 += m * s.tr; }
   const int nf = sp->nf, of = sp->of, vof = sp->vof;
   const R ab1 = R(sp->ab1), ab2 = R(sp->ab2), ab3 = R(sp->ab3);
   const size_t NL = (size_t)N * L;
@@ -608,15 +634,49 @@ __global__ void __launch_bounds__(kBlock) k_momtum1(Grid<R> g, Strides s, Knobs 
       if (have_d) { uu = uu + du[c]; vv = vv + dv[c]; }
       const R exm = R(0.5) * (exner[(size_t)i * L1 + k] + exner[(size_t)i * L1 + k + 1]);
       R pgfx = R(0), pgfy = R(0), rv = R(0);
-      for (int e = 0; e < np; e++) {
-        const R* svc = g.svc + (i * 6 + e) * 2;
-        const R* sve = g.sve + (i * 6 + e) * 2;
-        const size_t o = ((size_t)i * 6 + e) * L + k;
-        const R mu = mont_edg[o] + uvsq_edg[o];
-        const R th = trc_edg[o];
-        pgfx = pgfx - mu * svc[1] + exm * th * svc[1];
-        pgfy = pgfy + mu * svc[0] - exm * th * svc[0];
-        rv = rv + (sve[0] * u_edg[o] + sve[1] * v_edg[o]);
+      if (!split) {
+        for (int e = 0; e < np; e++) {
+          const R* svc = g.svc + (i * 6 + e) * 2;
+          const R* sve = g.sve + (i * 6 + e) * 2;
+          const size_t o = ((size_t)i * 6 + e) * L + k;
+          const R mu = mont_edg[o] + uvsq_edg[o];
+          const R th = trc_edg[o];
+          pgfx = pgfx - mu * svc[1] + exm * th * svc[1];
+          pgfy = pgfy + mu * svc[0] - exm * th * svc[0];
+          rv = rv + (sve[0] * u_edg[o] + sve[1] * v_edg[o]);
+        }
+      } else {
+        // FP32-mixed: the same line integrals with the cell values split off,
+        // sum_e (M_e + K_e - exm th_e) s_e
+        //   = sum_e (dM_e + K_e - exm dth_e) s_e + (M_c - exm th_c) sum_e s_e,
+        // dM_e, dth_e the edge-minus-cell values (edgvar1's weights applied to
+        // neighbour differences); the large cell term is formed in FP64.
+        const int* pr = g.prox + i * 6;
+        const R thc = tr0[(size_t)i * L + k];
+        R dth[6];
+#pragma unroll
+        for (int j = 0; j < 6; j++) dth[j] = (j < np) ? tr0[(size_t)pr[j] * L + k] - thc : R(0);
+        const R divby6 = R(1) / R(6);
+        for (int e = 0; e < np; e++) {
+          const R* svc = g.svc + (i * 6 + e) * 2;
+          const R* sve = g.sve + (i * 6 + e) * 2;
+          const size_t o = ((size_t)i * 6 + e) * L + k;
+          const int et = e == 0 ? np - 1 : e - 1, el = e == np - 1 ? 0 : e + 1;
+          R dte = R(0);
+#pragma unroll
+          for (int j = 0; j < 6; j++) {
+            if (j == e) dte = dte + R(2) * dth[j];
+            if (j == et || j == el) dte = dte + dth[j];
+          }
+          dte = dte * divby6;
+          const R w = mont_edg[o] + uvsq_edg[o] - exm * dte;
+          pgfx = pgfx - w * svc[1];
+          pgfy = pgfy + w * svc[0];
+          rv = rv + (sve[0] * u_edg[o] + sve[1] * v_edg[o]);
+        }
+        const double cell = mpd[(size_t)i * L + k] - (double)exm * (double)thc;
+        pgfx = pgfx - R(cell * g.svsum[i * 2 + 1]);
+        pgfy = pgfy + R(cell * g.svsum[i * 2 + 0]);
       }
       pgfx = pgfx * rar;
       pgfy = pgfy * rar;
@@ -661,8 +721,10 @@ __global__ void __launch_bounds__(kBlock) k_momtum1(Grid<R> g, Strides s, Knobs 
 
 // abstart (abstart.F90:33-65) advanced on the device so a captured step graph
 // can be replayed: its += 1, rotate the AB3 slots, set the weights.
-__global__ void k_step_begin(StepParams* sp) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__global__ void k_step_begin(StepParams* sp, int members) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= members || !sp[m].active) return;
+  sp += m;
   StepParams p = *sp;
   p.its += 1;
   p.nf = (p.nf + 1) % 3;
@@ -675,26 +737,29 @@ __global__ void k_step_begin(StepParams* sp) {
 }
 
 // ---------------------------- launchers -----------------------------------
-#define COUNT(l) do { if ((l).counter) ++*(l).counter; } while (0)
 
 template <typename R>
 void launch_edgvar1(const Launch& l, const Grid<R>& g, const Strides& s, int hi_order, const R* u,
                     const R* v, const R* delp, const R* pres, const R* montg, const R* tracr,
-                    R* u_edg, R* v_edg, R* dp_edg, R* lp_edg, R* mont_edg, R* uvsq_edg, R* trc_edg) {
+                    R* u_edg, R* v_edg, R* dp_edg, R* lp_edg, R* mont_edg, R* uvsq_edg, R* trc_edg,
+                    const double* mpd) {
   dim3 grid(blocks_for((long long)g.N * g.L), l.members);
+  FIM_KBEGIN(l, "k_edgvar1");
   k_edgvar1<R><<<grid, kBlock, 0, l.stream>>>(g, s, hi_order, u, v, delp, pres, montg, tracr, u_edg, v_edg,
-                                               dp_edg, lp_edg, mont_edg, uvsq_edg, trc_edg);
-  COUNT(l);
+                                               dp_edg, lp_edg, mont_edg, uvsq_edg, trc_edg, mpd);
+  FIM_KEND(l);
 }
 
 template <typename R>
 void launch_edgvar3(const Launch& l, const Grid<R>& g, const Strides& s, const R* delp, const R* tracr,
-                    R* dp_edg, R* trc_edg) {
-  dim3 grid(blocks_for((long long)g.N * g.L), l.members, g.T);
+                    R* dp_edg, R* trc_edg, int nfields) {
+  dim3 grid(blocks_for((long long)g.N * g.L), l.members, nfields);
+  FIM_KBEGIN(l, "k_edgvar3_own");
   k_edgvar3_own<R><<<grid, kBlock, 0, l.stream>>>(g, s, delp, tracr, dp_edg, trc_edg);
-  COUNT(l);
+  FIM_KEND(l);
+  FIM_KBEGIN(l, "k_edgvar3_avg");
   k_edgvar3_avg<R><<<grid, kBlock, 0, l.stream>>>(g, s, dp_edg, trc_edg);
-  COUNT(l);
+  FIM_KEND(l);
 }
 
 template <typename R>
@@ -702,18 +767,22 @@ void launch_cnuity(const Launch& l, const Grid<R>& g, const Strides& s, const Cn
                    const R* v, const R* u_edg, const R* v_edg, const R* dp_edg, const R* lp_edg,
                    R* delp, R* pres, R* exner, R* dp_tndcy, R* dplo_tndcy, R* massfx, R* omega) {
   dim3 grid(blocks_for((long long)g.N * g.L), l.members);
+  FIM_KBEGIN(l, "k_cnuity12");
   k_cnuity12<R><<<grid, kBlock, 0, l.stream>>>(g, s, l.sp, u_edg, v_edg, dp_edg, delp, massfx, dplo_tndcy,
                                                 w.antifx, w.delp_lo, w.p_plus, w.p_mnus);
-  COUNT(l);
+  FIM_KEND(l);
+  FIM_KBEGIN(l, "k_cnuity3");
   k_cnuity3<R><<<grid, kBlock, 0, l.stream>>>(g, s, l.sp, w.delp_lo, delp, dp_tndcy, w.p_plus, w.p_mnus,
                                                w.r_plus, w.r_mnus);
-  COUNT(l);
+  FIM_KEND(l);
+  FIM_KBEGIN(l, "k_cnuity4");
   k_cnuity4<R><<<grid, kBlock, 0, l.stream>>>(g, s, l.sp, w.antifx, w.r_plus, w.r_mnus, massfx, dplo_tndcy,
                                                dp_tndcy, delp, l.flags);
-  COUNT(l);
+  FIM_KEND(l);
   dim3 gw(blocks_for((long long)g.N * 32), l.members);
+  FIM_KBEGIN(l, "k_cnuity5");
   k_cnuity5<R><<<gw, kBlock, 0, l.stream>>>(g, s, l.sp, pres, delp, exner, dp_tndcy, omega, lp_edg, u, v);
-  COUNT(l);
+  FIM_KEND(l);
 }
 
 template <typename R>
@@ -724,15 +793,18 @@ void launch_trcadv(const Launch& l, const Grid<R>& g, const Strides& s, const Tr
   for (int t0 = 0; t0 < g.T; t0 += w.tchunk) {
     const int nt = (g.T - t0 < w.tchunk) ? g.T - t0 : w.tchunk;
     dim3 grid(blocks_for((long long)g.N * g.L), l.members, nt);
+    FIM_KBEGIN(l, "k_trcadv1");
     k_trcadv1<R><<<grid, kBlock, 0, l.stream>>>(g, s, l.sp, t0, massfx, trc_edg, tracr, trcdp, trl_tdcy, delp,
                                                  w.antiflx, w.trmin, w.trmax, w.trcr_lo, scs);
-    COUNT(l);
+    FIM_KEND(l);
+    FIM_KBEGIN(l, "k_trcadv2");
     k_trcadv2<R><<<grid, kBlock, 0, l.stream>>>(g, s, l.sp, t0, trc_tdcy, delp, w.antiflx, w.trmin, w.trmax,
                                                  w.trcr_lo, w.r_plus, w.r_mnus, scs);
-    COUNT(l);
+    FIM_KEND(l);
+    FIM_KBEGIN(l, "k_trcadv3");
     k_trcadv3<R><<<grid, kBlock, 0, l.stream>>>(g, s, l.sp, t0, trc_tdcy, trl_tdcy, trcdp, tracr, delp,
                                                  w.antiflx, w.r_mnus, w.r_plus, w.trmin, w.trmax, scs);
-    COUNT(l);
+    FIM_KEND(l);
   }
 }
 
@@ -740,7 +812,7 @@ template <typename R>
 void launch_momtum(const Launch& l, const Grid<R>& g, const Strides& s, const Knobs& kn, const MomtumScratch<R>& w,
                    R* u, R* v, const R* exner, R* relvor, const R* u_edg, const R* v_edg,
                    const R* trc_edg, const R* mont_edg, const R* uvsq_edg, R* u_tndcy, R* v_tndcy,
-                   const R* dp3d) {
+                   const R* dp3d, const double* mpd, const R* tr0) {
   dim3 grid(blocks_for((long long)g.N * g.L), l.members);
   const R* du = nullptr;
   const R* dv = nullptr;
@@ -748,31 +820,37 @@ void launch_momtum(const Launch& l, const Grid<R>& g, const Strides& s, const Kn
     const R* wu = nullptr;
     const R* wv = nullptr;
     if (kn.biharm) {
+      FIM_KBEGIN(l, "k_del4prep");
       k_del4prep<R><<<grid, kBlock, 0, l.stream>>>(g, s, u, v, w.wu, w.wv);
-      COUNT(l);
+      FIM_KEND(l);
       wu = w.wu;
       wv = w.wv;
     }
+    FIM_KBEGIN(l, "k_dissip");
     k_dissip<R><<<grid, kBlock, 0, l.stream>>>(g, s, u, v, wu, wv, dp3d, w.du, w.dv);
-    COUNT(l);
+    FIM_KEND(l);
     du = w.du;
     dv = w.dv;
   }
   dim3 gw(blocks_for((long long)g.N * 32), l.members);
+  FIM_KBEGIN(l, "k_momtum1");
   k_momtum1<R><<<gw, kBlock, 0, l.stream>>>(g, s, kn, l.sp, u, v, du, dv, exner, relvor, u_edg, v_edg, trc_edg,
-                                             mont_edg, uvsq_edg, u_tndcy, v_tndcy);
-  COUNT(l);
+                                             mont_edg, uvsq_edg, u_tndcy, v_tndcy, mpd, tr0);
+  FIM_KEND(l);
 }
 
 void launch_step_begin(const Launch& l, StepParams* sp) {
-  k_step_begin<<<1, 32, 0, l.stream>>>(sp);
-  COUNT(l);
+  FIM_KBEGIN(l, "k_step_begin");
+  k_step_begin<<<(l.members + 31) / 32, 32, 0, l.stream>>>(sp, l.members);
+  FIM_KEND(l);
 }
 
 #define INSTANTIATE(R)                                                                                          \
   template void launch_edgvar1<R>(const Launch&, const Grid<R>&, const Strides&, int, const R*, const R*,      \
-                                  const R*, const R*, const R*, const R*, R*, R*, R*, R*, R*, R*, R*);         \
-  template void launch_edgvar3<R>(const Launch&, const Grid<R>&, const Strides&, const R*, const R*, R*, R*); \
+                                  const R*, const R*, const R*, const R*, R*, R*, R*, R*, R*, R*, R*,          \
+                                  const double*);                                                             \
+  template void launch_edgvar3<R>(const Launch&, const Grid<R>&, const Strides&, const R*, const R*, R*, R*,  \
+                                  int);                                                                      \
   template void launch_cnuity<R>(const Launch&, const Grid<R>&, const Strides&, const CnuityScratch<R>&,      \
                                  const R*, const R*, const R*, const R*, const R*, const R*, R*, R*, R*, R*,  \
                                  R*, R*, R*);                                                                 \
@@ -780,7 +858,7 @@ void launch_step_begin(const Launch& l, StepParams* sp) {
                                  const R*, R*, R*, R*, R*, const R*, const R*);                               \
   template void launch_momtum<R>(const Launch&, const Grid<R>&, const Strides&, const Knobs&,                 \
                                  const MomtumScratch<R>&, R*, R*, const R*, R*, const R*, const R*, const R*, \
-                                 const R*, const R*, R*, R*, const R*);
+                                 const R*, const R*, R*, R*, const R*, const double*, const R*);
 INSTANTIATE(float)
 INSTANTIATE(double)
 

@@ -4,6 +4,9 @@
 #include <cuda_runtime.h>
 #include <cstddef>
 #include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
 
 namespace fim {
 
@@ -24,11 +27,15 @@ constexpr int kMaxL = 128;
 // Step-dependent scalars that the reference keeps in module_variables
 // (nf, of, vof, adbash1..3) plus the step number used by hybgen and hystat.
 // They live in device memory so a captured step graph can be replayed.
+// One block per ensemble member (indexed by the member, blockIdx.y in the
+// kernels), so members of one batch can be at different steps.
 struct StepParams {
   int its;
   int nf, of, vof;      // 0-based AB3 slots
   double ab1, ab2, ab3; // AB3 weights (s)
   double dt;
+  int active;           // 0: the member's slot is idle, kernels skip it
+  int pad_;
 };
 
 // device status bits
@@ -56,6 +63,7 @@ struct Grid {
   const R* __restrict__ grndspd;
   const R* __restrict__ hfcoef;   // [N*6*6]: hfcoef[(i*6+edge)*6+j]
   const double* __restrict__ area_d;  // [N] double areas for budgets
+  const double* __restrict__ svsum;   // [N*2] sum over edges of sidevec_c(1:2)
   // per-level tables
   const R* __restrict__ dfflen;   // [L]
   const R* __restrict__ biharw;   // [L]
@@ -98,6 +106,44 @@ inline Strides make_strides(int N, int L, int T) {
   return s;
 }
 
+// Per-kernel timing with CUDA events on the launching stream (bench only).
+struct Prof {
+  bool on = false;
+  struct Rec { const char* name; cudaEvent_t a, b; };
+  std::vector<Rec> pending;
+  std::vector<cudaEvent_t> pool;
+  std::map<std::string, std::pair<long long, double>> agg;  // name -> (launches, ms)
+  cudaEvent_t get() {
+    if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+  void begin(const char* name, cudaStream_t s) {
+    Rec r{name, get(), get()};
+    cudaEventRecord(r.a, s);
+    pending.push_back(r);
+  }
+  void end(cudaStream_t s) { cudaEventRecord(pending.back().b, s); }
+  void collect() {
+    for (auto& r : pending) {
+      cudaEventSynchronize(r.b);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, r.a, r.b);
+      auto& a = agg[r.name];
+      a.first += 1;
+      a.second += ms;
+      pool.push_back(r.a);
+      pool.push_back(r.b);
+    }
+    pending.clear();
+  }
+  ~Prof() {
+    for (auto& r : pending) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+
 // Launch context handed to every launcher.
 struct Launch {
   cudaStream_t stream;
@@ -105,16 +151,28 @@ struct Launch {
   const StepParams* sp;  // device
   int* flags;          // device status word per member [members]
   long long* counter;  // host launch counter
+  Prof* prof = nullptr;  // per-kernel event timing when enabled
 };
 
+#define FIM_KBEGIN(l, name) do { if ((l).prof && (l).prof->on) (l).prof->begin(name, (l).stream); } while (0)
+#define FIM_KEND(l)                                                      \
+  do {                                                                   \
+    if ((l).prof && (l).prof->on) (l).prof->end((l).stream);             \
+    if ((l).counter) ++*(l).counter;                                     \
+  } while (0)
+
 // ---- launchers (instantiated for float and double) ----------------------
+// mpd (FP32-mixed step only, may be null): FP64 copy of the Montgomery
+// potential; mont_edg then holds the edge value minus the cell value.
 template <typename R>
 void launch_edgvar1(const Launch&, const Grid<R>&, const Strides&, int hi_order, const R* u,
                     const R* v, const R* delp, const R* pres, const R* montg, const R* tracr,
-                    R* u_edg, R* v_edg, R* dp_edg, R* lp_edg, R* mont_edg, R* uvsq_edg, R* trc_edg);
+                    R* u_edg, R* v_edg, R* dp_edg, R* lp_edg, R* mont_edg, R* uvsq_edg, R* trc_edg,
+                    const double* mpd = nullptr);
+// nfields: 1 = dp only, T = dp and tracers 2..ntra (edgvar3's full output)
 template <typename R>
 void launch_edgvar3(const Launch&, const Grid<R>&, const Strides&, const R* delp, const R* tracr,
-                    R* dp_edg, R* trc_edg);
+                    R* dp_edg, R* trc_edg, int nfields);
 template <typename R>
 struct CnuityScratch { R *antifx, *delp_lo, *p_plus, *p_mnus, *r_plus, *r_mnus; };
 template <typename R>
@@ -127,13 +185,25 @@ template <typename R>
 void launch_trcadv(const Launch&, const Grid<R>&, const Strides&, const TrcadvScratch<R>&,
                    const R* trc_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx,
                    const R* delp);
+// fused tracer path of the step (fim_trc.cu)
+template <typename R>
+struct TrcFusedScratch { R *trcr_lo, *s_plus, *s_mnus, *trold, *r_plus, *r_mnus; int tchunk; };
+template <typename R>
+void launch_tracer_own(const Launch&, const Grid<R>&, const Strides&, const R* tracr, R* trc_edg);
+template <typename R>
+void launch_tracers_fused(const Launch&, const Grid<R>&, const Strides&, const TrcFusedScratch<R>&,
+                          R* trc_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx,
+                          const R* delp);
 template <typename R>
 struct MomtumScratch { R *du, *dv, *wu, *wv; };
+// With mpd != null (FP32-mixed step) the pressure-gradient line integrals use
+// the cell values split off (see k_momtum1): tr0 = potential temperature
+// cells, svsum = per-cell sums of sidevec_c.
 template <typename R>
 void launch_momtum(const Launch&, const Grid<R>&, const Strides&, const Knobs&, const MomtumScratch<R>&,
                    R* u, R* v, const R* exner, R* relvor, const R* u_edg, const R* v_edg,
                    const R* trc_edg, const R* mont_edg, const R* uvsq_edg, R* u_tndcy, R* v_tndcy,
-                   const R* dp3d);
+                   const R* dp3d, const double* mpd = nullptr, const R* tr0 = nullptr);
 template <typename R>
 struct HybgenScratch { R *exsmo, *exsmo2; };
 template <typename R>
@@ -141,7 +211,7 @@ void launch_hybgen(const Launch&, const Grid<R>&, const Strides&, const Knobs&, 
                    const R* targt, R* us3d, R* vs3d, R* tr3d, R* sdot, R* ex3d, R* dp3d, R* pr3d);
 template <typename R>
 void launch_hystat(const Launch&, const Grid<R>&, const Strides&, R* ph3d, const R* ex3d, R* mp3d,
-                   const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy);
+                   const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy, double* mpd = nullptr);
 // sums per member: [member][8 + T] doubles; partial buffer sized by globsum_partials()
 template <typename R>
 void launch_globsum(const Launch&, const Grid<R>&, const Strides&, const R* dp3d, const R* tr,
@@ -150,6 +220,6 @@ void launch_globsum(const Launch&, const Grid<R>&, const Strides&, const R* dp3d
 size_t globsum_partials(int N, int L, int T, int members);
 template <typename R>
 void launch_prdp_from_ex(const Launch&, const Grid<R>&, const Strides&, const R* ex3d, R* pr3d, R* dp3d);
-void launch_step_begin(const Launch&, StepParams* sp);
+void launch_step_begin(const Launch&, StepParams* sp);  // advances every active member
 
 }  // namespace fim

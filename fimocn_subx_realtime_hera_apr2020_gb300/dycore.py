@@ -66,9 +66,35 @@ class Dycore:
     def launches(self):
         return self.lib.fim_launch_count(self.ctx)
 
+    def profile(self, on):
+        _lib.check(self.lib.fim_profile_enable(self.ctx, 1 if on else 0), "fim_profile_enable", self.ctx)
+
+    def profile_report(self):
+        """{kernel: (launches, total ms)} since the last report."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        _lib.check(self.lib.fim_profile_report(self.ctx, buf, len(buf)), "fim_profile_report", self.ctx)
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, n, ms = line.split()
+            out[name] = (int(n), float(ms))
+        return out
+
     def _call(self, name, *args):
+        """Run one entry point.  Device arrays written by torch on its own
+        stream are complete before the library's stream starts, and the
+        library's results are complete when the call returns."""
         fn = getattr(self.lib, name + self._sfx)
+        device = not self.cfg.host_pointers
+        if device:
+            import torch
+            torch.cuda.current_stream().synchronize()
         _lib.check(fn(self.ctx, *args), name, self.ctx)
+        if device:
+            self.sync_stream()
+
+    def sync_stream(self):
+        import torch
+        torch.cuda.ExternalStream(self.stream).synchronize()
 
     def sync(self):
         import torch
@@ -193,6 +219,23 @@ class DycoreState:
         its = self.its + 1 if its is None else its
         _lib.check(self.lib.fim_step(self.dyc.ctx, self.st, its, 1 if use_graph else 0), "fim_step", self.dyc.ctx)
         self.its = its
+
+    def init_member(self, member):
+        """Initialise (dyn_init) and activate one member slot after its upload."""
+        _lib.check(self.lib.fim_state_init_member(self.dyc.ctx, self.st, member), "fim_state_init_member",
+                   self.dyc.ctx)
+
+    def set_active(self, member, active):
+        _lib.check(self.lib.fim_member_set_active(self.dyc.ctx, self.st, member, 1 if active else 0),
+                   "fim_member_set_active", self.dyc.ctx)
+
+    def member_its(self, member):
+        return self.lib.fim_member_its(self.dyc.ctx, member)
+
+    def step_active(self, use_graph=True):
+        """Advance every active member by one step (each at its own its)."""
+        _lib.check(self.lib.fim_step_active(self.dyc.ctx, self.st, 1 if use_graph else 0), "fim_step_active",
+                   self.dyc.ctx)
 
     def budget(self, member=0):
         qtrcr = np.zeros(self.dyc.T, np.float64)

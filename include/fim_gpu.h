@@ -211,6 +211,9 @@ enum fim_field {
   FIM_TRC_EDG, FIM_NFIELDS
 };
 
+/* After a fused step the edge work fields are in the step's internal form:
+ * trc_edg of tracers 2..ntra holds the own-side reconstructions (edgvar3
+ * loop 1) and, in an FP32 context, mont_edg holds edge-minus-cell values. */
 int fim_state_alloc(fim_ctx *ctx, fim_state **out);
 int fim_state_free(fim_ctx *ctx, fim_state *st);
 /* device pointer and element count of one member's field */
@@ -228,11 +231,27 @@ int fim_state_init(fim_ctx *ctx, fim_state *st);
  * use_graph != 0 captures the step once as a CUDA graph and replays it. */
 int fim_step(fim_ctx *ctx, fim_state *st, int its, int use_graph);
 
+/* Continuous batching: every member slot carries its own step counter and
+ * AB3 slots, so members of one batch can start at different times.
+ * fim_state_init_member initialises one slot (after its fields were
+ * uploaded) and activates it; fim_step_active advances every active slot by
+ * one step; idle slots are skipped by the kernels. */
+int fim_state_init_member(fim_ctx *ctx, fim_state *st, int member);
+int fim_member_set_active(fim_ctx *ctx, fim_state *st, int member, int active);
+int fim_member_its(const fim_ctx *ctx, int member);
+int fim_step_active(fim_ctx *ctx, fim_state *st, int use_graph);
+
 /* Member budgets after the last step (qmass, tracer integrals qtrcr(ntra)). */
 int fim_state_budget(fim_ctx *ctx, fim_state *st, int member, double *qtrcr, fim_budget *out);
 
 /* Accumulated device-side status flags (NaN / non-positive thickness); resets them. */
 int fim_check(fim_ctx *ctx, fim_state *st, int *flags);
+
+/* Per-kernel CUDA-event timing on the context stream (for measurement;
+ * steps must run without graph replay while it is on). */
+int fim_profile_enable(fim_ctx *ctx, int on);
+/* "kernel launches total_ms" lines accumulated since the last report */
+int fim_profile_report(fim_ctx *ctx, char *buf, int len);
 
 /* Kernel launches issued since the context was created (own kernels only). */
 int64_t fim_launch_count(const fim_ctx *ctx);

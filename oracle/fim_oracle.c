@@ -9,6 +9,18 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* thread count of the OpenMP loops (the timed CPU baseline runs 1 and all cores) */
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
 
 /* FIMsrc/cntl/module_constants.F90:14-27 */
 static const double PI = 3.14159265;

@@ -49,6 +49,7 @@ void orc_derived(int nip, int nvl, int kbl, double dt, double intfc_smooth,
                  double *rarea, double *corio, double *grndspd, double *dfflen,
                  double *biharw, double *smoo_coeff, double *dfflen_max);
 
+void orc_set_threads(int n);
 void orc_abstart(orc_ctx *c, int its);
 void orc_edgvar1(const orc_ctx *c, const double *u, const double *v, const double *delp,
                  const double *pres, const double *exner, const double *geop,

@@ -60,6 +60,7 @@ def load():
             "orc_hystat": [P, I] + [P] * 8,
             "orc_globsum": [P] * 10,
             "orc_prdp_from_ex": [P] * 4,
+            "orc_set_threads": [I],
         }
         for name, args in sigs.items():
             fn = getattr(lib, name)
@@ -67,6 +68,10 @@ def load():
             fn.restype = None
         _lib = lib
     return _lib
+
+
+def set_threads(n):
+    load().orc_set_threads(int(n))
 
 
 def _p(a):

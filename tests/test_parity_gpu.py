@@ -1,0 +1,234 @@
+"""GPU parity: every routine and the fused step against the CPU oracle.
+
+FP64 path: relative L2 per field <= 1e-12 after one step (the parity bar).
+FP32-mixed path: relative L2 per prognostic field <= 1e-5 after one step.
+All calls go through the C-ABI (libfimgpu.so) via the package's host mirror.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import fimocn_subx_realtime_hera_apr2020_gb300 as F  # noqa: E402
+from helpers import PROGNOSTIC, make_case, oracle_for, rel_l2  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 1e-5
+
+
+def dev(a, dtype=torch.float64):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device="cuda", dtype=dtype)
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.double().cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def case4():
+    """Level-4 grid, nvl 38, 4 tracers + theta, noisy wind (the CPU-sized workload)."""
+    grid, cfg, fields = make_case(glvl=4, nvl=38, ntra=5, dt=400.0, seed=1000, noise=1.0)
+    o = oracle_for(grid, cfg)
+    s = o.init_state(o.new_state(fields))
+    return grid, cfg, fields, o, s
+
+
+def test_routines_fp64(case4):
+    """Each routine fed the oracle's inputs reproduces the oracle's outputs."""
+    grid, cfg, fields, o0, s0 = case4
+    o = oracle_for(grid, cfg)
+    s = {k: v.copy() for k, v in s0.items()}
+    dyc = F.Dycore(grid, cfg)
+    errs = {}
+    for its in range(1, 5):
+        o.abstart(its)
+        dyc.set_ab(o.c.nf + 1, o.c.of + 1, o.c.vof + 1, o.c.ab1, o.c.ab2, o.c.ab3)
+        # edgvar1
+        names = ["us3d", "vs3d", "dp3d", "pr3d", "ex3d", "ph3d", "mp3d", "tr3d", "u_edg", "v_edg", "dp_edg",
+                 "lp_edg", "geop_edg", "mont_edg", "uvsq_edg", "trc_edg"]
+        g = {n: dev(s[n]) for n in names}
+        o.edgvar1(*[s[n] for n in names])
+        dyc.edgvar1(its, *[g[n] for n in names])
+        for n in ["u_edg", "v_edg", "lp_edg", "mont_edg", "uvsq_edg", "trc_edg"]:
+            errs[("edgvar1", n)] = max(errs.get(("edgvar1", n), 0), rel_l2(host(g[n]), s[n]))
+        # edgvar3
+        g = {n: dev(s[n]) for n in names}
+        o.edgvar3(s["dp3d"], s["tr3d"], s["dp_edg"], s["trc_edg"])
+        dyc.edgvar3(its, *[g[n] for n in names])
+        for n in ["dp_edg", "trc_edg"]:
+            errs[("edgvar3", n)] = max(errs.get(("edgvar3", n), 0), rel_l2(host(g[n]), s[n]))
+        # cnuity
+        names = ["us3d", "vs3d", "u_edg", "v_edg", "dp_edg", "lp_edg", "dp3d", "pr3d", "ex3d", "dp_tdcy",
+                 "dpl_tdcy", "massfx", "ws3d"]
+        g = {n: dev(s[n]) for n in names}
+        o.cnuity(*[s[n] for n in names])
+        dyc.cnuity(its, *[g[n] for n in names])
+        for n in ["dp3d", "pr3d", "ex3d", "dp_tdcy", "dpl_tdcy", "massfx", "ws3d"]:
+            errs[("cnuity", n)] = max(errs.get(("cnuity", n), 0), rel_l2(host(g[n]), s[n]))
+        # trcadv
+        names = ["trc_edg", "tr3d", "trdp", "trc_tdcy", "trl_tdcy", "massfx", "dp3d"]
+        g = {n: dev(s[n]) for n in names}
+        o.trcadv(*[s[n] for n in names])
+        dyc.trcadv(its, *[g[n] for n in names])
+        for n in ["tr3d", "trdp", "trc_tdcy", "trl_tdcy"]:
+            errs[("trcadv", n)] = max(errs.get(("trcadv", n), 0), rel_l2(host(g[n]), s[n]))
+        # momtum
+        onames = ["us3d", "vs3d", "ex3d", "relvor", "u_edg", "v_edg", "trc_edg", "mont_edg", "uvsq_edg",
+                  "u_tdcy", "v_tdcy", "dp3d"]
+        g = {n: dev(s[n]) for n in onames + ["geop_edg"]}
+        o.momtum(*[s[n] for n in onames])
+        dyc.momtum(its, g["us3d"], g["vs3d"], g["ex3d"], g["relvor"], g["u_edg"], g["v_edg"], g["trc_edg"],
+                   g["geop_edg"], g["mont_edg"], g["uvsq_edg"], g["u_tdcy"], g["v_tdcy"], g["dp3d"])
+        for n in ["us3d", "vs3d", "relvor", "u_tdcy", "v_tdcy"]:
+            errs[("momtum", n)] = max(errs.get(("momtum", n), 0), rel_l2(host(g[n]), s[n]))
+        # hybgen
+        names = ["us3d", "vs3d", "tr3d", "sdot", "ex3d", "dp3d", "pr3d"]
+        g = {n: dev(s[n]) for n in names}
+        o.hybgen(its, *[s[n] for n in names])
+        dyc.hybgen(its, None, *[g[n] for n in names])
+        for n in ["us3d", "vs3d", "tr3d", "ex3d", "dp3d", "pr3d"]:
+            errs[("hybgen", n)] = max(errs.get(("hybgen", n), 0), rel_l2(host(g[n]), s[n]))
+        # hystat
+        names = ["ph3d", "ex3d", "mp3d", "dp3d", "tr3d", "trdp", "psrf", "ptdcy"]
+        g = {n: dev(s[n]) for n in names}
+        o.hystat(its, *[s[n] for n in names])
+        dyc.hystat(its, *[g[n] for n in names])
+        for n in ["ph3d", "mp3d", "tr3d", "trdp", "psrf"]:
+            errs[("hystat", n)] = max(errs.get(("hystat", n), 0), rel_l2(host(g[n]), s[n]))
+        # globsum
+        qo, bo = o.globsum(s["dp3d"], s["tr3d"], s["pr3d"], s["ex3d"])
+        qg, bg = dyc.globsum(its, dev(s["dp3d"]), dev(s["tr3d"]), dev(s["pr3d"]), dev(s["ex3d"]))
+        errs[("globsum", "qtrcr")] = max(errs.get(("globsum", "qtrcr"), 0), rel_l2(qg, qo))
+        errs[("globsum", "qmass")] = max(errs.get(("globsum", "qmass"), 0), abs(bg["qmass"] / bo["qmass"] - 1))
+    bad = {k: v for k, v in errs.items() if not v <= TOL64}
+    assert not bad, bad
+
+
+def _gpu_state(grid, cfg, fields, members=1, member_fields=None):
+    dyc = F.Dycore(grid, cfg)
+    st = dyc.state()
+    for m in range(members):
+        st.load(member_fields[m] if member_fields else fields, member=m)
+    st.init()
+    return dyc, st
+
+
+def test_state_init_fp64(case4):
+    grid, cfg, fields, o, s = case4
+    dyc, st = _gpu_state(grid, cfg, fields)
+    for n in PROGNOSTIC:
+        assert rel_l2(st.download(n), s[n]) <= TOL64, n
+
+
+def test_fused_step_fp64(case4):
+    grid, cfg, fields, o0, s0 = case4
+    o = oracle_for(grid, cfg)
+    s = o.init_state(o.new_state(fields))
+    dyc, st = _gpu_state(grid, cfg, fields)
+    for its in range(1, 4):
+        qo, bo = o.step(s, its)
+        st.step(its)
+        errs = {n: rel_l2(st.download(n), s[n]) for n in PROGNOSTIC + ["ws3d", "relvor", "sdot"]}
+        if its == 1:
+            bad = {k: v for k, v in errs.items() if not v <= TOL64}
+            assert not bad, bad
+        qg, bg = st.budget()
+        assert abs(bg["qmass"] / bo["qmass"] - 1) < 1e-12
+        assert rel_l2(qg, qo) < 1e-11
+    rc, flags = st.check()
+    assert rc == 0 and flags == 0
+
+
+def test_graph_replay_matches_direct(case4):
+    grid, cfg, fields, _, _ = case4
+    d1, s1 = _gpu_state(grid, cfg, fields)
+    d2, s2 = _gpu_state(grid, cfg, fields)
+    for its in range(1, 5):
+        s1.step(its, use_graph=False)
+        s2.step(its, use_graph=True)
+    for n in PROGNOSTIC:
+        assert np.array_equal(s1.download(n), s2.download(n)), n
+
+
+def test_members_independent():
+    grid, cfg, fields = make_case(glvl=3, nvl=38, ntra=5, dt=400.0, seed=11, noise=1.0)
+    f2 = F.synthetic_state(grid, cfg, seed=12, sigma_ps=100.0, noise=0.5)
+    cfg3 = F.FimConfig(nvl=38, ntra=5, dt=400.0, members=2)
+    d, st = _gpu_state(grid, cfg3, None, members=2, member_fields=[fields, f2])
+    da, sa = _gpu_state(grid, F.FimConfig(nvl=38, ntra=5, dt=400.0), fields)
+    db, sb = _gpu_state(grid, F.FimConfig(nvl=38, ntra=5, dt=400.0), f2)
+    for its in (1, 2, 3):
+        st.step(its)
+        sa.step(its)
+        sb.step(its)
+    for n in PROGNOSTIC:
+        assert np.array_equal(st.download(n, 0), sa.download(n)), n
+        assert np.array_equal(st.download(n, 1), sb.download(n)), n
+
+
+def test_fp32_mixed_one_step(case4):
+    grid, cfg, fields, o0, s0 = case4
+    o = oracle_for(grid, cfg)
+    s = o.init_state(o.new_state(fields))
+    cfg32 = F.FimConfig(nvl=cfg.nvl, ntra=cfg.ntra, dt=cfg.dt, precision="f32")
+    dyc, st = _gpu_state(grid, cfg32, fields)
+    for n in PROGNOSTIC:
+        assert rel_l2(st.download(n), s[n]) <= TOL32, ("init", n)
+    o.step(s, 1)
+    st.step(1)
+    errs = {n: rel_l2(st.download(n), s[n]) for n in PROGNOSTIC}
+    bad = {k: v for k, v in errs.items() if not v <= TOL32}
+    assert not bad, bad
+
+
+def test_host_pointer_mode(case4):
+    """host_pointers=1 stages numpy arrays through the device; same results."""
+    grid, cfg, fields, o0, s0 = case4
+    cfgh = F.FimConfig(nvl=cfg.nvl, ntra=cfg.ntra, dt=cfg.dt, host_pointers=True)
+    dh = F.Dycore(grid, cfgh)
+    dd = F.Dycore(grid, cfg)
+    s = {k: v.copy() for k, v in s0.items()}
+    for d in (dh, dd):
+        d.abstart(1)
+    names = ["us3d", "vs3d", "dp3d", "pr3d", "ex3d", "ph3d", "mp3d", "tr3d", "u_edg", "v_edg", "dp_edg",
+             "lp_edg", "geop_edg", "mont_edg", "uvsq_edg", "trc_edg"]
+    hs = {n: s[n].copy() for n in names}
+    gs = {n: dev(s[n]) for n in names}
+    dh.edgvar1(1, *[hs[n] for n in names])
+    dd.edgvar1(1, *[gs[n] for n in names])
+    for n in ["u_edg", "v_edg", "lp_edg", "trc_edg"]:
+        assert np.array_equal(hs[n], host(gs[n])), n
+
+
+def test_fused_step_matches_routine_sequence(case4):
+    """fim_step (fused tracer kernels, graph) == the per-routine entry points
+    called in dyn_run order on the same state, bit for bit."""
+    grid, cfg, fields, o0, s0 = case4
+    dyc, st = _gpu_state(grid, cfg, fields)
+    d2 = F.Dycore(grid, cfg)
+    names = ["us3d", "vs3d", "dp3d", "pr3d", "ex3d", "ph3d", "mp3d", "tr3d", "trdp", "u_tdcy", "v_tdcy",
+             "dp_tdcy", "dpl_tdcy", "trc_tdcy", "trl_tdcy", "massfx", "ws3d", "sdot", "relvor", "psrf", "ptdcy",
+             "u_edg", "v_edg", "dp_edg", "lp_edg", "mont_edg", "uvsq_edg", "geop_edg", "trc_edg"]
+    g = {n: dev(st.download(n)) for n in names}
+    d2.set_ab(3, 2, 1, 0.0, 0.0, 0.0)  # the post-init slots (Fortran 0,2,1 before the first abstart)
+    for its in range(1, 5):
+        st.step(its, use_graph=True)
+        d2.abstart(its)
+        d2.edgvar1(its, g["us3d"], g["vs3d"], g["dp3d"], g["pr3d"], g["ex3d"], g["ph3d"], g["mp3d"], g["tr3d"],
+                   g["u_edg"], g["v_edg"], g["dp_edg"], g["lp_edg"], g["geop_edg"], g["mont_edg"], g["uvsq_edg"],
+                   g["trc_edg"])
+        d2.edgvar3(its, g["us3d"], g["vs3d"], g["dp3d"], g["pr3d"], g["ex3d"], g["ph3d"], g["mp3d"], g["tr3d"],
+                   g["u_edg"], g["v_edg"], g["dp_edg"], g["lp_edg"], g["geop_edg"], g["mont_edg"], g["uvsq_edg"],
+                   g["trc_edg"])
+        d2.cnuity(its, g["us3d"], g["vs3d"], g["u_edg"], g["v_edg"], g["dp_edg"], g["lp_edg"], g["dp3d"],
+                  g["pr3d"], g["ex3d"], g["dp_tdcy"], g["dpl_tdcy"], g["massfx"], g["ws3d"])
+        d2.trcadv(its, g["trc_edg"], g["tr3d"], g["trdp"], g["trc_tdcy"], g["trl_tdcy"], g["massfx"], g["dp3d"])
+        d2.momtum(its, g["us3d"], g["vs3d"], g["ex3d"], g["relvor"], g["u_edg"], g["v_edg"], g["trc_edg"],
+                  g["geop_edg"], g["mont_edg"], g["uvsq_edg"], g["u_tdcy"], g["v_tdcy"], g["dp3d"])
+        d2.hybgen(its, None, g["us3d"], g["vs3d"], g["tr3d"], g["sdot"], g["ex3d"], g["dp3d"], g["pr3d"])
+        d2.hystat(its, g["ph3d"], g["ex3d"], g["mp3d"], g["dp3d"], g["tr3d"], g["trdp"], g["psrf"], g["ptdcy"])
+        for n in PROGNOSTIC + ["ws3d", "relvor", "sdot", "trc_tdcy", "trl_tdcy", "massfx"]:
+            assert np.array_equal(st.download(n), host(g[n])), (its, n)
