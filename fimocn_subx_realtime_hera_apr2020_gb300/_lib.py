@@ -83,6 +83,7 @@ _ROUTINES = {
     "fim_edgvar3": [_VP, _I] + [_VP] * 16,
     "fim_cnuity": [_VP, _I] + [_VP] * 13,
     "fim_trcadv": [_VP, _I] + [_VP] * 7,
+    "fim_mass_adv": [_VP, _I] + [_VP] * 12,
     "fim_momtum": [_VP, _I] + [_VP] * 13,
     "fim_hybgen": [_VP, _I] + [_VP] * 8,
     "fim_hystat": [_VP, _I] + [_VP] * 8,

@@ -35,6 +35,7 @@ struct fim_state {
   size_t count[FIM_NFIELDS] = {};  // elements per member
   double* sums = nullptr;          // [M][8+T]
   double* mpd = nullptr;           // FP32-mixed: FP64 Montgomery potential [M][nvl*nip]
+  void* thold = nullptr;           // FP32-mixed: theta seen by edgvar1 this step [M][nvl*nip]
   cudaGraphExec_t graph = nullptr;
   long long graph_kernels = 0;
 };
@@ -425,6 +426,34 @@ int cnuity_impl(fim_ctx* c, const R* u_velo, const R* v_velo, const R* u_edg, co
 }
 
 template <typename R>
+int massadv_impl(fim_ctx* c, const R* u_velo, const R* v_velo, const R* u_edg, const R* v_edg, R* dp_edg,
+                 const R* lp_edg, R* delp, R* pres, R* exner, R* dp_tndcy, R* massfx, R* omega) {
+  int rc = check_prec<R>(c);
+  if (rc) return rc;
+  if ((rc = ensure_cnuity(c, c->M))) return rc;
+  const size_t NL = (size_t)c->N * c->L, NI = (size_t)c->N * (c->L + 1), NE = NL * 6;
+  Stager s(c);
+  const R* a = s.map(u_velo, NL, 0);
+  const R* b = s.map(v_velo, NL, 0);
+  const R* ue = s.map(u_edg, NE, 0);
+  const R* ve = s.map(v_edg, NE, 0);
+  R* de = s.map(dp_edg, NE, 1);
+  const R* le = s.map(lp_edg, NE, 0);
+  R* dp = s.map(delp, NL, 1);
+  R* pr = s.map(pres, NI, 1);
+  R* ex = s.map(exner, NI, 1);
+  R* dt = s.map(dp_tndcy, NL * 3, 1);
+  R* mf = s.map(massfx, NE * 3, 1);
+  R* om = s.map(omega, NL, 2);
+  if (s.rc) return s.rc;
+  if ((rc = push_sp(c))) return rc;
+  CnuityScratch<R> w{(R*)c->antifx, (R*)c->delp_lo, (R*)c->p_plus, (R*)c->p_mnus, (R*)c->r_plus, (R*)c->r_mnus};
+  launch_massadv<R>(make_launch(c, 1), grid_of<R>(c), c->str, w, a, b, ue, ve, de, le, dp, pr, ex, dt, mf, om);
+  if ((rc = check_launch(c, "mass_adv"))) return rc;
+  return s.finish();
+}
+
+template <typename R>
 int trcadv_impl(fim_ctx* c, const R* trcr_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trclo_tdcy, const R* massfx,
                 const R* delp) {
   int rc = check_prec<R>(c);
@@ -571,7 +600,7 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
   launch_edgvar1<R>(l, g, s, c->kn.hi_order, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_DP3D),
                     F<R>(st, FIM_PR3D), F<R>(st, FIM_MP3D), F<R>(st, FIM_TR3D), F<R>(st, FIM_U_EDG),
                     F<R>(st, FIM_V_EDG), F<R>(st, FIM_DP_EDG), F<R>(st, FIM_LP_EDG), F<R>(st, FIM_MONT_EDG),
-                    F<R>(st, FIM_UVSQ_EDG), F<R>(st, FIM_TRC_EDG), st->mpd);
+                    F<R>(st, FIM_UVSQ_EDG), F<R>(st, FIM_TRC_EDG), st->mpd, (R*)st->thold);
   if (c->kn.hi_order) {
     // dp edges with edgvar3's two-sided average; tracer edges keep the
     // own-side values, averaged where the fused tracer kernels use them
@@ -580,10 +609,15 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
     launch_tracer_own<R>(l, g, s, F<R>(st, FIM_TR3D), F<R>(st, FIM_TRC_EDG));
   }
   CnuityScratch<R> cw{(R*)c->antifx, (R*)c->delp_lo, (R*)c->p_plus, (R*)c->p_mnus, (R*)c->r_plus, (R*)c->r_mnus};
-  launch_cnuity<R>(l, g, s, cw, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_U_EDG), F<R>(st, FIM_V_EDG),
-                   F<R>(st, FIM_DP_EDG), F<R>(st, FIM_LP_EDG), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D),
-                   F<R>(st, FIM_EX3D), F<R>(st, FIM_DP_TDCY), F<R>(st, FIM_DPL_TDCY), F<R>(st, FIM_MASSFX),
-                   F<R>(st, FIM_WS3D));
+  if (c->cfg.flux_conserv_schm == 1)
+    launch_cnuity<R>(l, g, s, cw, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_U_EDG), F<R>(st, FIM_V_EDG),
+                     F<R>(st, FIM_DP_EDG), F<R>(st, FIM_LP_EDG), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D),
+                     F<R>(st, FIM_EX3D), F<R>(st, FIM_DP_TDCY), F<R>(st, FIM_DPL_TDCY), F<R>(st, FIM_MASSFX),
+                     F<R>(st, FIM_WS3D));
+  else
+    launch_massadv<R>(l, g, s, cw, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_U_EDG), F<R>(st, FIM_V_EDG),
+                      F<R>(st, FIM_DP_EDG), F<R>(st, FIM_LP_EDG), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D),
+                      F<R>(st, FIM_EX3D), F<R>(st, FIM_DP_TDCY), F<R>(st, FIM_MASSFX), F<R>(st, FIM_WS3D));
   if (c->kn.hi_order) {
     TrcFusedScratch<R> fw{(R*)c->f_trcr_lo, (R*)c->f_sp, (R*)c->f_sm, (R*)c->f_trold, (R*)c->f_rp, (R*)c->f_rm,
                           c->ftchunk};
@@ -600,7 +634,7 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
   launch_momtum<R>(l, g, s, c->kn, mw, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_EX3D),
                    F<R>(st, FIM_RELVOR), F<R>(st, FIM_U_EDG), F<R>(st, FIM_V_EDG), F<R>(st, FIM_TRC_EDG),
                    F<R>(st, FIM_MONT_EDG), F<R>(st, FIM_UVSQ_EDG), F<R>(st, FIM_U_TDCY), F<R>(st, FIM_V_TDCY),
-                   F<R>(st, FIM_DP3D), st->mpd, st->mpd ? F<R>(st, FIM_TR3D) : nullptr);
+                   F<R>(st, FIM_DP3D), st->mpd, (const R*)st->thold);
   HybgenScratch<R> hw{(R*)c->exsmo, (R*)c->exsmo2};
   launch_hybgen<R>(l, g, s, c->kn, hw, g.thetac, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_TR3D),
                    F<R>(st, FIM_SDOT), F<R>(st, FIM_EX3D), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D));
@@ -668,7 +702,7 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
   *out = nullptr;
   if (cfg->nvl < 4 || cfg->nvl > kMaxL || cfg->ntra < 4 || cfg->ntra > 32 || g->nip < 12 || cfg->dt <= 0.)
     return FIM_EINVAL;
-  if (cfg->flux_conserv_schm != 1) return FIM_ENOTSUP;
+  if (cfg->flux_conserv_schm != 1 && cfg->flux_conserv_schm != 2) return FIM_ENOTSUP;
   if (cfg->pure_sig) return FIM_ENOTSUP;
   if (cfg->remap_optn < 1 || cfg->remap_optn > 3) return FIM_EINVAL;
   if (cfg->precision != FIM_PREC_F64 && cfg->precision != FIM_PREC_F32) return FIM_EINVAL;
@@ -858,6 +892,21 @@ int fim_cnuity_r4(fim_ctx* c, int its, const float* u_velo, const float* v_velo,
                             dplo_tndcy, massfx, omega);
 }
 
+int fim_mass_adv_r8(fim_ctx* c, int its, const double* u_velo, const double* v_velo, const double* u_edg,
+                    const double* v_edg, double* dp_edg, const double* lp_edg, double* delp, double* pres,
+                    double* exner, double* dp_tndcy, double* massfx, double* omega) {
+  (void)its;
+  return massadv_impl<double>(c, u_velo, v_velo, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner, dp_tndcy, massfx,
+                              omega);
+}
+int fim_mass_adv_r4(fim_ctx* c, int its, const float* u_velo, const float* v_velo, const float* u_edg,
+                    const float* v_edg, float* dp_edg, const float* lp_edg, float* delp, float* pres, float* exner,
+                    float* dp_tndcy, float* massfx, float* omega) {
+  (void)its;
+  return massadv_impl<float>(c, u_velo, v_velo, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner, dp_tndcy, massfx,
+                             omega);
+}
+
 int fim_trcadv_r8(fim_ctx* c, int its, const double* trcr_edg, double* tracr, double* trcdp, double* trc_tdcy,
                   double* trclo_tdcy, const double* massfx, const double* delp) {
   (void)its;
@@ -937,6 +986,7 @@ int fim_state_alloc(fim_ctx* c, fim_state** out) {
   if (rc) { delete st; return rc; }
   if (c->prec == FIM_PREC_F32) {
     if ((rc = dalloc(c, (void**)&st->mpd, (size_t)c->M * cnt[FIM_MP3D] * sizeof(double)))) { delete st; return rc; }
+    if ((rc = dalloc(c, &st->thold, (size_t)c->M * cnt[FIM_MP3D] * c->esz))) { delete st; return rc; }
     cudaMemsetAsync(st->mpd, 0, (size_t)c->M * cnt[FIM_MP3D] * sizeof(double), c->stream);
   }
   if ((rc = ensure_all(c))) { delete st; return rc; }
@@ -953,7 +1003,7 @@ int fim_state_free(fim_ctx* c, fim_state* st) {
     for (auto it = c->owned.begin(); it != c->owned.end(); ++it)
       if (*it == st->f[f]) { cudaFree(*it); c->owned.erase(it); break; }
   }
-  for (void* extra : {(void*)st->sums, (void*)st->mpd})
+  for (void* extra : {(void*)st->sums, (void*)st->mpd, st->thold})
     for (auto it = c->owned.begin(); it != c->owned.end(); ++it)
       if (extra && *it == extra) { cudaFree(*it); c->owned.erase(it); break; }
   delete st;

@@ -42,12 +42,18 @@ __global__ void __launch_bounds__(kBlock) k_edgvar1(Grid<R> g, Strides s, int hi
     const R* __restrict__ u, const R* __restrict__ v, const R* __restrict__ delp,
     const R* __restrict__ pres, const R* __restrict__ montg, const R* __restrict__ tracr,
     R* __restrict__ u_edg, R* __restrict__ v_edg, R* __restrict__ dp_edg, R* __restrict__ lp_edg,
-    R* __restrict__ mont_edg, R* __restrict__ uvsq_edg, R* __restrict__ trc_edg, const double* __restrict__ mpd) {
+    R* __restrict__ mont_edg, R* __restrict__ uvsq_edg, R* __restrict__ trc_edg, const double* __restrict__ mpd,
+    R* __restrict__ thold) {
   int i, k;
   if (!cell_level(g.N, g.L, i, k)) return;
   const int L = g.L, N = g.N, L1 = L + 1;
   const size_t m = blockIdx.y;
   if (mpd) mpd += m * s.cell;
+  if (thold) {
+    // the potential temperature of this step's edge values, for momtum1
+    thold += m * s.cell;
+    thold[(size_t)i * L + k] = tracr[m * s.tr + (size_t)i * L + k];
+  }
   u += m * s.cell; v += m * s.cell; delp += m * s.cell; pres += m * s.intf;
   montg += m * s.cell; tracr += m * s.tr;
   u_edg += m * s.edge; v_edg += m * s.edge; dp_edg += m * s.edge; lp_edg += m * s.edge;
@@ -306,8 +312,9 @@ __global__ void __launch_bounds__(kBlock) k_cnuity4(Grid<R> g, Strides s, const 
 // v.grad(p) term per level.
 template <typename R>
 __global__ void __launch_bounds__(kBlock) k_cnuity5(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
-    R* __restrict__ pres, const R* __restrict__ delp, R* __restrict__ exner, const R* __restrict__ dp_tndcy,
-    R* __restrict__ omega, const R* __restrict__ lp_edg, const R* __restrict__ u, const R* __restrict__ v) {
+    R* __restrict__ pres, R* __restrict__ delp, R* __restrict__ exner, const R* __restrict__ dp_tndcy,
+    R* __restrict__ omega, const R* __restrict__ lp_edg, const R* __restrict__ u, const R* __restrict__ v,
+    int ab3_delp) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int N = g.N, L = g.L, L1 = L + 1;
   if (warp >= N) return;
@@ -332,9 +339,16 @@ __global__ void __launch_bounds__(kBlock) k_cnuity5(Grid<R> g, Strides s, const 
     R lyr = R(0);
     if (act) {
       const size_t c = (size_t)i * L + k;
+      const R tnf = dp_tndcy[(size_t)nf * N * L + c], tof = dp_tndcy[(size_t)of * N * L + c],
+              tvf = dp_tndcy[(size_t)vof * N * L + c];
+      if (ab3_delp) {
+        // massflux_newdepth's AB3 thickness update (massadv_compute.F90:85-91)
+        R dn = delp[c] + ab1 * tnf + ab2 * tof + ab3 * tvf;
+        dn = dn > R(0) ? dn : R(0);
+        delp[c] = dn;
+      }
       d = (double)delp[c];
-      lyr = (ab1 * dp_tndcy[(size_t)nf * N * L + c] + ab2 * dp_tndcy[(size_t)of * N * L + c] +
-             ab3 * dp_tndcy[(size_t)vof * N * L + c]) / dt;
+      lyr = (ab1 * tnf + ab2 * tof + ab3 * tvf) / dt;
       lt = (double)lyr;
     }
     double sd = d, sl = lt;
@@ -365,6 +379,136 @@ __global__ void __launch_bounds__(kBlock) k_cnuity5(Grid<R> g, Strides s, const 
     carry_p += __shfl_sync(0xffffffffu, sd, 31);
     carry_c += __shfl_sync(0xffffffffu, sl, 31);
   }
+}
+
+// --------------------------------------------------------------------------
+// mass_adv (flux_conserv_schm = 2, the reference default): flux_limiter.F90
+// edgeNormVel + limiter (M1 branch).  k_massadv_lim: bounded edge thickness
+// q* per edge and the outflow bounds q_min_out/q_max_out per cell
+// (flux_limiter.F90:149-233).  k_massadv_flux: limited edge thickness with
+// the upwind cell's bounds, mass flux, dp tendency (flux_limiter.F90:247-259,
+// massadv_compute.F90:45-83); the AB3 thickness update runs in k_cnuity5.
+template <typename R>
+__device__ __forceinline__ void ma_edge(const Grid<R>& g, int i, int k, int e, int np, const R* u_edg,
+                                        const R* v_edg, const R* dp_edg, const R* delp, R& vn, R& qs, int& ipx) {
+  const int L = g.L;
+  const int* pr = g.prox + i * 6;
+  ipx = pr[e];
+  const int nbm1 = pr[e == 0 ? np - 1 : e - 1], nbp1 = pr[e == np - 1 ? 0 : e + 1];
+  const R* sv = g.sve + (i * 6 + e) * 2;
+  const size_t o = ((size_t)i * 6 + e) * L + k;
+  vn = sv[1] * u_edg[o] - sv[0] * v_edg[o];
+  const R a = delp[(size_t)i * L + k], b = delp[(size_t)ipx * L + k], c = delp[(size_t)nbm1 * L + k],
+          d = delp[(size_t)nbp1 * L + k];
+  const R qmn = rmin(rmin(rmin(a, b), c), d), qmx = rmax(rmax(rmax(a, b), c), d);
+  qs = rmax(qmn, rmin(qmx, dp_edg[o]));
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlock) k_massadv_lim(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
+    const R* __restrict__ u_edg, const R* __restrict__ v_edg, const R* __restrict__ dp_edg,
+    const R* __restrict__ delp, const R* __restrict__ dp_tndcy, R* __restrict__ qmin_out, R* __restrict__ qmax_out) {
+  int i, k;
+  if (!cell_level(g.N, g.L, i, k)) return;
+  const int L = g.L, N = g.N;
+  const size_t m = blockIdx.y;
+  sp += m;
+  if (!sp->active) return;
+  u_edg += m * s.edge; v_edg += m * s.edge; dp_edg += m * s.edge; delp += m * s.cell; dp_tndcy += m * s.ab;
+  qmin_out += m * s.cell; qmax_out += m * s.cell;
+  const int of = sp->of, vof = sp->vof;
+  const R ab1 = R(sp->ab1), ab2 = R(sp->ab2), ab3 = R(sp->ab3), dt = R(sp->dt);
+  const size_t c = (size_t)i * L + k;
+  const R gv = delp[c], rar = g.rarea[i];
+  const int np = g.nprox[i];
+  R qminin = sizeof(R) == 8 ? R(1.79769313486231571e308) : R(3.40282347e38f), qmaxin = R(0);
+  R cqmin = R(0), cqmax = R(0), cin = R(0), cout = R(0);
+  for (int e = 0; e < np; e++) {
+    R vn, qs;
+    int ipx;
+    ma_edge(g, i, k, e, np, u_edg, v_edg, dp_edg, delp, vn, qs, ipx);
+    const R cn = rabs(vn) * dt * rar;
+    if (vn > R(0)) {
+      cout = cout + cn;
+    } else {
+      const R gx = delp[(size_t)ipx * L + k];
+      const R qmn = rmin(qs, gx), qmx = rmax(qs, gx);
+      cin = cin + cn;
+      qminin = rmin(qminin, qmn);
+      qmaxin = rmax(qmaxin, qmx);
+      cqmin = cqmin + cn * qmn;
+      cqmax = cqmax + cn * qmx;
+    }
+  }
+  const R qmin_next = rmin(gv, qminin), qmax_next = rmax(gv, qmaxin);
+  if (cout != R(0)) {
+    const R to = dp_tndcy[(size_t)of * N * L + c], tv = dp_tndcy[(size_t)vof * N * L + c];
+    qmin_out[c] = (gv + ab1 / dt * cqmax - qmax_next * (R(1) + cin - cout) + ab2 * to + ab3 * tv) / cout / ab1 * dt;
+    qmax_out[c] = (gv + ab1 / dt * cqmin - qmin_next * (R(1) + cin - cout) + ab2 * to + ab3 * tv) / cout / ab1 * dt;
+  } else {
+    qmin_out[c] = R(-100000.0);
+    qmax_out[c] = R(100000.0);
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlock) k_massadv_flux(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
+    const R* __restrict__ u_edg, const R* __restrict__ v_edg, R* __restrict__ dp_edg, const R* __restrict__ delp,
+    const R* __restrict__ qmin_out, const R* __restrict__ qmax_out, R* __restrict__ massfx, R* __restrict__ dp_tndcy) {
+  int i, k;
+  if (!cell_level(g.N, g.L, i, k)) return;
+  const int L = g.L, N = g.N;
+  const size_t m = blockIdx.y;
+  sp += m;
+  if (!sp->active) return;
+  u_edg += m * s.edge; v_edg += m * s.edge; dp_edg += m * s.edge; delp += m * s.cell; dp_tndcy += m * s.ab;
+  qmin_out += m * s.cell; qmax_out += m * s.cell; massfx += m * s.mf;
+  const int nf = sp->nf;
+  R* mfn = massfx + (size_t)nf * N * 6 * L;
+  const int np = g.nprox[i];
+  R vnv[6], dpe[6];
+#pragma unroll
+  for (int e = 0; e < 6; e++) {
+    if (e < np) {
+      R vn, qs;
+      int ipx;
+      ma_edge(g, i, k, e, np, u_edg, v_edg, dp_edg, delp, vn, qs, ipx);
+      const size_t cs = (size_t)(vn > R(0) ? i : ipx) * L + k;
+      vnv[e] = vn;
+      dpe[e] = rmax(qmin_out[cs], rmin(qmax_out[cs], qs));
+    }
+  }
+  R t = R(0);
+#pragma unroll
+  for (int e = 0; e < 6; e++) {
+    if (e < np) {
+      const size_t o = ((size_t)i * 6 + e) * L + k;
+      dp_edg[o] = dpe[e];
+      const R mf = vnv[e] * dpe[e];
+      mfn[o] = mf;
+      t = t + mf;
+    }
+  }
+  dp_tndcy[(size_t)nf * N * L + (size_t)i * L + k] = -t * g.rarea[i];
+}
+
+template <typename R>
+void launch_massadv(const Launch& l, const Grid<R>& g, const Strides& s, const CnuityScratch<R>& w, const R* u,
+                    const R* v, const R* u_edg, const R* v_edg, R* dp_edg, const R* lp_edg, R* delp, R* pres,
+                    R* exner, R* dp_tndcy, R* massfx, R* omega) {
+  dim3 grid(blocks_for((long long)g.N * g.L), l.members);
+  FIM_KBEGIN(l, "k_massadv_lim");
+  k_massadv_lim<R><<<grid, kBlock, 0, l.stream>>>(g, s, l.sp, u_edg, v_edg, dp_edg, delp, dp_tndcy, w.r_plus,
+                                                   w.r_mnus);
+  FIM_KEND(l);
+  FIM_KBEGIN(l, "k_massadv_flux");
+  k_massadv_flux<R><<<grid, kBlock, 0, l.stream>>>(g, s, l.sp, u_edg, v_edg, dp_edg, delp, w.r_plus, w.r_mnus,
+                                                    massfx, dp_tndcy);
+  FIM_KEND(l);
+  dim3 gw(blocks_for((long long)g.N * 32), l.members);
+  FIM_KBEGIN(l, "k_cnuity5");
+  k_cnuity5<R><<<gw, kBlock, 0, l.stream>>>(g, s, l.sp, pres, delp, exner, dp_tndcy, omega, lp_edg, u, v, 1);
+  FIM_KEND(l);
 }
 
 // --------------------------------------------------------------------------
@@ -616,7 +760,7 @@ __global__ void __launch_bounds__(kBlock) k_momtum1(Grid<R> g, Strides s, Knobs 
   const bool have_d = du != nullptr;
   if (have_d) { du += m * s.cell; dv += m * s.cell; }
   const bool split = mpd != nullptr;
-  if (split) { mpd += m * s.cell; tr0 += m * s.tr; }
+  if (split) { mpd += m * s.cell; tr0 += m * s.cell; }
   const int nf = sp->nf, of = sp->of, vof = sp->vof;
   const R ab1 = R(sp->ab1), ab2 = R(sp->ab2), ab3 = R(sp->ab3);
   const size_t NL = (size_t)N * L;
@@ -742,11 +886,11 @@ template <typename R>
 void launch_edgvar1(const Launch& l, const Grid<R>& g, const Strides& s, int hi_order, const R* u,
                     const R* v, const R* delp, const R* pres, const R* montg, const R* tracr,
                     R* u_edg, R* v_edg, R* dp_edg, R* lp_edg, R* mont_edg, R* uvsq_edg, R* trc_edg,
-                    const double* mpd) {
+                    const double* mpd, R* thold) {
   dim3 grid(blocks_for((long long)g.N * g.L), l.members);
   FIM_KBEGIN(l, "k_edgvar1");
   k_edgvar1<R><<<grid, kBlock, 0, l.stream>>>(g, s, hi_order, u, v, delp, pres, montg, tracr, u_edg, v_edg,
-                                               dp_edg, lp_edg, mont_edg, uvsq_edg, trc_edg, mpd);
+                                               dp_edg, lp_edg, mont_edg, uvsq_edg, trc_edg, mpd, thold);
   FIM_KEND(l);
 }
 
@@ -781,7 +925,7 @@ void launch_cnuity(const Launch& l, const Grid<R>& g, const Strides& s, const Cn
   FIM_KEND(l);
   dim3 gw(blocks_for((long long)g.N * 32), l.members);
   FIM_KBEGIN(l, "k_cnuity5");
-  k_cnuity5<R><<<gw, kBlock, 0, l.stream>>>(g, s, l.sp, pres, delp, exner, dp_tndcy, omega, lp_edg, u, v);
+  k_cnuity5<R><<<gw, kBlock, 0, l.stream>>>(g, s, l.sp, pres, delp, exner, dp_tndcy, omega, lp_edg, u, v, 0);
   FIM_KEND(l);
 }
 
@@ -848,12 +992,15 @@ void launch_step_begin(const Launch& l, StepParams* sp) {
 #define INSTANTIATE(R)                                                                                          \
   template void launch_edgvar1<R>(const Launch&, const Grid<R>&, const Strides&, int, const R*, const R*,      \
                                   const R*, const R*, const R*, const R*, R*, R*, R*, R*, R*, R*, R*,          \
-                                  const double*);                                                             \
+                                  const double*, R*);                                                         \
   template void launch_edgvar3<R>(const Launch&, const Grid<R>&, const Strides&, const R*, const R*, R*, R*,  \
                                   int);                                                                      \
   template void launch_cnuity<R>(const Launch&, const Grid<R>&, const Strides&, const CnuityScratch<R>&,      \
                                  const R*, const R*, const R*, const R*, const R*, const R*, R*, R*, R*, R*,  \
                                  R*, R*, R*);                                                                 \
+  template void launch_massadv<R>(const Launch&, const Grid<R>&, const Strides&, const CnuityScratch<R>&,     \
+                                  const R*, const R*, const R*, const R*, R*, const R*, R*, R*, R*, R*, R*,   \
+                                  R*);                                                                       \
   template void launch_trcadv<R>(const Launch&, const Grid<R>&, const Strides&, const TrcadvScratch<R>&,      \
                                  const R*, R*, R*, R*, R*, const R*, const R*);                               \
   template void launch_momtum<R>(const Launch&, const Grid<R>&, const Strides&, const Knobs&,                 \

@@ -168,7 +168,7 @@ template <typename R>
 void launch_edgvar1(const Launch&, const Grid<R>&, const Strides&, int hi_order, const R* u,
                     const R* v, const R* delp, const R* pres, const R* montg, const R* tracr,
                     R* u_edg, R* v_edg, R* dp_edg, R* lp_edg, R* mont_edg, R* uvsq_edg, R* trc_edg,
-                    const double* mpd = nullptr);
+                    const double* mpd = nullptr, R* thold = nullptr);
 // nfields: 1 = dp only, T = dp and tracers 2..ntra (edgvar3's full output)
 template <typename R>
 void launch_edgvar3(const Launch&, const Grid<R>&, const Strides&, const R* delp, const R* tracr,
@@ -179,6 +179,11 @@ template <typename R>
 void launch_cnuity(const Launch&, const Grid<R>&, const Strides&, const CnuityScratch<R>&, const R* u,
                    const R* v, const R* u_edg, const R* v_edg, const R* dp_edg, const R* lp_edg,
                    R* delp, R* pres, R* exner, R* dp_tndcy, R* dplo_tndcy, R* massfx, R* omega);
+// flux_conserv_schm = 2 (the bounds use the r_plus/r_mnus scratch slots)
+template <typename R>
+void launch_massadv(const Launch&, const Grid<R>&, const Strides&, const CnuityScratch<R>&, const R* u,
+                    const R* v, const R* u_edg, const R* v_edg, R* dp_edg, const R* lp_edg, R* delp, R* pres,
+                    R* exner, R* dp_tndcy, R* massfx, R* omega);
 template <typename R>
 struct TrcadvScratch { R *antiflx, *trmin, *trmax, *trcr_lo, *r_plus, *r_mnus; int tchunk; };
 template <typename R>
@@ -197,8 +202,8 @@ void launch_tracers_fused(const Launch&, const Grid<R>&, const Strides&, const T
 template <typename R>
 struct MomtumScratch { R *du, *dv, *wu, *wv; };
 // With mpd != null (FP32-mixed step) the pressure-gradient line integrals use
-// the cell values split off (see k_momtum1): tr0 = potential temperature
-// cells, svsum = per-cell sums of sidevec_c.
+// the cell values split off (see k_momtum1): tr0 = the potential temperature
+// edgvar1 saw (thold), svsum = per-cell sums of sidevec_c.
 template <typename R>
 void launch_momtum(const Launch&, const Grid<R>&, const Strides&, const Knobs&, const MomtumScratch<R>&,
                    R* u, R* v, const R* exner, R* relvor, const R* u_edg, const R* v_edg,

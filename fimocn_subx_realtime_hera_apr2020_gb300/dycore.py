@@ -133,6 +133,11 @@ class Dycore:
         self._call("fim_cnuity", its, *map(_ptr, (u_velo, v_velo, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner,
                                                     dp_tndcy, dplo_tndcy, massfx, omega)))
 
+    def mass_adv(self, its, u_velo, v_velo, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner, dp_tndcy, massfx,
+                 omega):
+        self._call("fim_mass_adv", its, *map(_ptr, (u_velo, v_velo, u_edg, v_edg, dp_edg, lp_edg, delp, pres,
+                                                      exner, dp_tndcy, massfx, omega)))
+
     def trcadv(self, its, trcr_edg, tracr, trcdp, trc_tdcy, trclo_tdcy, massfx, delp):
         self._call("fim_trcadv", its, *map(_ptr, (trcr_edg, tracr, trcdp, trc_tdcy, trclo_tdcy, massfx, delp)))
 

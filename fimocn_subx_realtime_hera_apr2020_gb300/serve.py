@@ -1,0 +1,212 @@
+"""Forecast-advance serving with continuous batching.
+
+A request asks to advance a seeded balanced state on grid level glvl with
+nvl layers and ntra tracers by `steps` dynamics steps.  Requests of the same
+(glvl, nvl, ntra, precision) share a pool: one context whose ensemble slots
+are the batch, advanced together by one fused launch sequence per step
+(fim_step_active, one CUDA-graph replay).  Every slot carries its own step
+counter and AB3 slots, so a request admitted while others are mid-forecast
+joins at the next step boundary; a finished slot is freed for the next
+request.  Pools are created while free HBM allows (admission by memory) and
+each pool runs on its own stream, so different grids overlap on the device.
+States stay resident in HBM for the whole forecast.
+"""
+import heapq
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .config import FimConfig, default_dt
+from .dycore import Dycore
+from .grid import Grid
+from .state import synthetic_state
+
+
+@dataclass(order=True)
+class Request:
+    arrival: float
+    rid: int = field(compare=False)
+    glvl: int = field(compare=False)
+    nvl: int = field(compare=False)
+    ntra: int = field(compare=False)
+    steps: int = field(compare=False)
+    seed: int = field(compare=False, default=0)
+    t_admit: float = field(compare=False, default=None)
+    t_done: float = field(compare=False, default=None)
+    result: dict = field(compare=False, default=None)
+
+    @property
+    def key(self):
+        return (self.glvl, self.nvl, self.ntra)
+
+    @property
+    def work(self):
+        """cell-level-steps of the request"""
+        return (10 * 4 ** self.glvl + 2) * self.nvl * self.steps
+
+
+def state_bytes(glvl, nvl, ntra, precision):
+    """Device bytes of one member slot (state, edge fields, scratch)."""
+    nip = 10 * 4 ** glvl + 2
+    w = 8 if precision == "f64" else 4
+    words = 6 + 4 + 2 * ntra + 12 + 6 * ntra + 18 + 7 * 6 + 6 * ntra + 6 * ntra + 20
+    return int(nip * nvl * words * w * 1.1)
+
+
+class Pool:
+    """One batched context (all slots share the grid and the configuration)."""
+
+    def __init__(self, key, precision, slots, collect):
+        import torch
+        glvl, nvl, ntra = key
+        self.key = key
+        self.grid = Grid.cached(glvl)
+        self.cfg = FimConfig(nvl=nvl, ntra=ntra, dt=default_dt(glvl), precision=precision, members=slots)
+        self.dyc = Dycore(self.grid, self.cfg)
+        self.st = self.dyc.state()
+        for m in range(slots):
+            self.st.set_active(m, False)
+        self.slots = [None] * slots
+        self.collect = collect
+        self.stream = torch.cuda.ExternalStream(self.dyc.stream)
+
+    def free_slot(self):
+        for i, r in enumerate(self.slots):
+            if r is None:
+                return i
+        return -1
+
+    def admit(self, req, now):
+        m = self.free_slot()
+        fields = synthetic_state(self.grid, self.cfg, seed=req.seed, sigma_ps=200.0, noise=0.5,
+                                 dtype=self.cfg.dtype)
+        self.st.load(fields, member=m)
+        self.st.init_member(m)  # dyn_init for this slot only; activates it
+        req.t_admit = now
+        self.slots[m] = req
+
+    def active(self):
+        return any(r is not None for r in self.slots)
+
+    def step(self):
+        self.st.step_active(use_graph=True)
+
+    def finished(self):
+        done = []
+        for m, r in enumerate(self.slots):
+            if r is not None and self.st.member_its(m) >= r.steps:
+                done.append(m)
+        return done
+
+    def retire(self, m, now):
+        r = self.slots[m]
+        res = {}
+        if self.collect:
+            for name in self.collect:
+                res[name] = self.st.download(name, m)
+        qtrcr, bud = self.st.budget(m)
+        res["qmass"] = bud["qmass"]
+        r.result = res
+        r.t_done = now
+        self.st.set_active(m, False)
+        self.slots[m] = None
+        return r
+
+    def close(self):
+        self.st.free()
+        self.dyc.close()
+
+
+class Server:
+    """Continuous-batching request loop over resident device states."""
+
+    def __init__(self, precision="f32", slots=8, hbm_fraction=0.8, collect=("us3d", "tr3d")):
+        self.precision = precision
+        self.slots = slots
+        self.hbm_fraction = hbm_fraction
+        self.collect = collect
+        self.pools = {}
+
+    def _free_hbm(self):
+        import torch
+        free, total = torch.cuda.mem_get_info()
+        return free - (1 - self.hbm_fraction) * total
+
+    def _pool_for(self, req):
+        p = self.pools.get(req.key)
+        if p is not None:
+            return p
+        need = state_bytes(req.glvl, req.nvl, req.ntra, self.precision) * self.slots
+        if need > self._free_hbm():
+            # evict idle pools first, then refuse for now (the request waits)
+            for k in [k for k, v in self.pools.items() if not v.active()]:
+                self.pools.pop(k).close()
+            if need > self._free_hbm():
+                return None
+        p = Pool(req.key, self.precision, self.slots, self.collect)
+        self.pools[req.key] = p
+        return p
+
+    def run(self, requests, realtime=True):
+        """Serve `requests` (arrival in seconds from start); returns them done."""
+        import torch
+        pending = list(requests)
+        heapq.heapify(pending)
+        waiting = []
+        done = []
+        t0 = time.perf_counter()
+        now = lambda: time.perf_counter() - t0  # noqa: E731
+        while pending or waiting or any(p.active() for p in self.pools.values()):
+            t = now()
+            while pending and (pending[0].arrival <= t or not realtime):
+                waiting.append(heapq.heappop(pending))
+                if not realtime:
+                    break
+            still = []
+            for r in waiting:
+                p = self._pool_for(r)
+                if p is not None and p.free_slot() >= 0:
+                    p.admit(r, now())
+                else:
+                    still.append(r)
+            waiting = still
+            busy = [p for p in self.pools.values() if p.active()]
+            if not busy:
+                if pending and realtime:
+                    time.sleep(max(0.0, min(pending[0].arrival - now(), 0.01)))
+                continue
+            for p in busy:
+                p.step()  # enqueued on the pool's own stream: pools overlap
+            for p in busy:
+                p.stream.synchronize()
+                for m in p.finished():
+                    done.append(p.retire(m, now()))
+        torch.cuda.synchronize()
+        return done
+
+    def close(self):
+        for p in self.pools.values():
+            p.close()
+        self.pools = {}
+
+
+def poisson_requests(n, rate, seed, glvls=(5, 6, 7), nvls=(38, 64), tracers=(4, 20), steps=(24, 240)):
+    """Seeded Poisson arrival stream of the served workload mix."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate)
+        out.append(Request(arrival=t, rid=i, glvl=int(rng.choice(glvls)), nvl=int(rng.choice(nvls)),
+                           ntra=int(rng.integers(tracers[0], tracers[1] + 1)) + 1,
+                           steps=int(rng.integers(steps[0], steps[1] + 1)), seed=5000 + i))
+    return out
+
+
+def latency_stats(done):
+    lat = np.array([r.t_done - r.arrival for r in done])
+    work = sum(r.work for r in done)
+    span = max(r.t_done for r in done) - min(r.arrival for r in done)
+    return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "mean_s": float(lat.mean()), "requests": len(done), "cell_level_steps_per_s": work / span}

@@ -73,7 +73,7 @@ typedef struct fim_config {
   int host_pointers;       /* 1: entry points receive host arrays */
   double dt;               /* time step, s */
   int kbl;                 /* [2] fixed-depth layers near the surface */
-  int flux_conserv_schm;   /* must be 1 (FCT cnuity) */
+  int flux_conserv_schm;   /* 1: FCT cnuity; 2: mass_adv flux limiter (the reference default) */
   int hi_order_flux_comp;  /* [1] edgvar3 supplies dp_edg and tracers 2..ntra */
   double intfc_smooth;     /* [30] m/s */
   double slak;             /* [0.5] */
@@ -158,6 +158,18 @@ int fim_cnuity_r4(fim_ctx *ctx, int its, const float *u_velo, const float *v_vel
                   const float *u_edg, const float *v_edg, const float *dp_edg,
                   const float *lp_edg, float *delp, float *pres, float *exner,
                   float *dp_tndcy, float *dplo_tndcy, float *massfx, float *omega);
+
+/* FIMsrc/fim/horizontal/massadv.F90:21-23 (flux_conserv_schm = 2, the
+ * reference default: flux limiter of flux_limiter.F90 + update_pres);
+ * dp_edg is limited in place */
+int fim_mass_adv_r8(fim_ctx *ctx, int its, const double *u_velo, const double *v_velo,
+                    const double *u_edg, const double *v_edg, double *dp_edg, const double *lp_edg,
+                    double *delp, double *pres, double *exner, double *dp_tndcy, double *massfx,
+                    double *omega);
+int fim_mass_adv_r4(fim_ctx *ctx, int its, const float *u_velo, const float *v_velo,
+                    const float *u_edg, const float *v_edg, float *dp_edg, const float *lp_edg,
+                    float *delp, float *pres, float *exner, float *dp_tndcy, float *massfx,
+                    float *omega);
 
 /* FIMsrc/fim/horizontal/trcadv.F90:19-20 (trcadv1..3, all tracers) */
 int fim_trcadv_r8(fim_ctx *ctx, int its, const double *trcr_edg, double *tracr, double *trcdp,

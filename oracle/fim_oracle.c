@@ -359,6 +359,123 @@ void orc_cnuity(const orc_ctx *c, const double *u, const double *v, const double
   free(vnorm); free(antifx); free(delp_lo); free(r_plus); free(r_mnus);
 }
 
+/* massadv.F90:58-118 (flux_conserv_schm=2): flux_limiter.F90 edgeNormVel
+ * (68-92) and limiter (120-262, M1 branch), massadv_compute.F90
+ * massflux_newdepth (22-95) and update_pres (97-170, identical to cnuity5) */
+void orc_mass_adv(const orc_ctx *c, const double *u, const double *v, const double *u_edg,
+                  const double *v_edg, double *dp_edg, const double *lp_edg, double *delp,
+                  double *pres, double *exner, double *dp_tndcy, double *massfx, double *omega) {
+  const int N = c->nip, L = c->nvl;
+  const int nf = c->nf, of = c->of, vof = c->vof;
+  const double ab1 = c->ab1, ab2 = c->ab2, ab3 = c->ab3, dt = c->dt;
+  const size_t NE = (size_t)N * 6 * L, NC = (size_t)N * L;
+  double *vnorm = (double *)calloc(NE, sizeof(double));
+  double *c_num = (double *)calloc(NE, sizeof(double));
+  double *q_star = (double *)calloc(NE, sizeof(double));
+  double *q_min_out = (double *)malloc(sizeof(double) * NC);
+  double *q_max_out = (double *)malloc(sizeof(double) * NC);
+  const double max_out_bound = 100000.0;
+#pragma omp parallel for schedule(static)
+  for (int ipn = 0; ipn < N; ipn++)
+    for (int edg = 0; edg < c->nprox[ipn]; edg++) {
+      const double *sv = c->sidevec_e + (ipn * 6 + edg) * 2;
+      for (int k = 0; k < L; k++) {
+        vnorm[E3(k, edg, ipn)] = sv[1] * u_edg[E3(k, edg, ipn)] - sv[0] * v_edg[E3(k, edg, ipn)];
+        c_num[E3(k, edg, ipn)] = fabs(vnorm[E3(k, edg, ipn)]) * dt * c->rarea[ipn];
+      }
+    }
+#pragma omp parallel for schedule(static)
+  for (int ipn = 0; ipn < N; ipn++) {
+    const int np = c->nprox[ipn];
+    for (int edg = 0; edg < np; edg++) {
+      const int nbm1 = c->prox[ipn * 6 + (edg - 1 + np) % np], nbp1 = c->prox[ipn * 6 + (edg + 1) % np];
+      const int ipx = c->prox[ipn * 6 + edg];
+      for (int k = 0; k < L; k++) {
+        double qmn = dmin(dmin(dmin(delp[C2(k, ipn)], delp[C2(k, ipx)]), delp[C2(k, nbm1)]), delp[C2(k, nbp1)]);
+        double qmx = dmax(dmax(dmax(delp[C2(k, ipn)], delp[C2(k, ipx)]), delp[C2(k, nbm1)]), delp[C2(k, nbp1)]);
+        q_star[E3(k, edg, ipn)] = dmax(qmn, dmin(qmx, dp_edg[E3(k, edg, ipn)]));
+      }
+    }
+    for (int k = 0; k < L; k++) {
+      double qminin = 1.79769313486231571e308, qmaxin = 0.0, cqmin = 0.0, cqmax = 0.0, cin = 0.0, cout = 0.0;
+      const double g = delp[C2(k, ipn)];
+      for (int edg = 0; edg < np; edg++) {
+        const size_t o = E3(k, edg, ipn);
+        const int ipx = c->prox[ipn * 6 + edg];
+        double qmn, qmx;
+        if (vnorm[o] > 0) {
+          qmn = dmin(q_star[o], g);
+          qmx = dmax(q_star[o], g);
+          cout = cout + c_num[o];
+        } else {
+          qmn = dmin(q_star[o], delp[C2(k, ipx)]);
+          qmx = dmax(q_star[o], delp[C2(k, ipx)]);
+          cin = cin + c_num[o];
+          qminin = dmin(qminin, qmn);
+          qmaxin = dmax(qmaxin, qmx);
+          cqmin = cqmin + c_num[o] * qmn;
+          cqmax = cqmax + c_num[o] * qmx;
+        }
+      }
+      const double qmin_next = dmin(g, qminin), qmax_next = dmax(g, qmaxin);
+      if (cout != 0.0) {
+        q_min_out[C2(k, ipn)] = (g + ab1 / dt * cqmax - qmax_next * (1.0 + cin - cout) +
+                                 ab2 * dp_tndcy[S3(k, ipn, of)] + ab3 * dp_tndcy[S3(k, ipn, vof)]) / cout / ab1 * dt;
+        q_max_out[C2(k, ipn)] = (g + ab1 / dt * cqmin - qmin_next * (1.0 + cin - cout) +
+                                 ab2 * dp_tndcy[S3(k, ipn, of)] + ab3 * dp_tndcy[S3(k, ipn, vof)]) / cout / ab1 * dt;
+      } else {
+        q_min_out[C2(k, ipn)] = -max_out_bound;
+        q_max_out[C2(k, ipn)] = max_out_bound;
+      }
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (int ipn = 0; ipn < N; ipn++)
+    for (int edg = 0; edg < c->nprox[ipn]; edg++) {
+      const int ipx = c->prox[ipn * 6 + edg];
+      for (int k = 0; k < L; k++) {
+        const size_t o = E3(k, edg, ipn);
+        const int src = vnorm[o] > 0 ? ipn : ipx;
+        dp_edg[o] = dmax(q_min_out[C2(k, src)], dmin(q_max_out[C2(k, src)], q_star[o]));
+      }
+    }
+#pragma omp parallel for schedule(static)
+  for (int ipn = 0; ipn < N; ipn++) {
+    for (int edg = 0; edg < c->nprox[ipn]; edg++)
+      for (int k = 0; k < L; k++) massfx[MF(k, edg, ipn, nf)] = vnorm[E3(k, edg, ipn)] * dp_edg[E3(k, edg, ipn)];
+    for (int k = 0; k < L; k++) {
+      double t = 0.;
+      for (int edg = 0; edg < c->nprox[ipn]; edg++) t = t + massfx[MF(k, edg, ipn, nf)];
+      t = -t * c->rarea[ipn];
+      dp_tndcy[S3(k, ipn, nf)] = t;
+      double d = delp[C2(k, ipn)] + ab1 * t + ab2 * dp_tndcy[S3(k, ipn, of)] + ab3 * dp_tndcy[S3(k, ipn, vof)];
+      delp[C2(k, ipn)] = dmax(d, 0.0);
+    }
+  }
+  free(vnorm); free(c_num); free(q_star); free(q_min_out); free(q_max_out);
+  /* update_pres (massadv_compute.F90:131-167) is cnuity5 */
+  const double rdcp = RD / CP;
+#pragma omp parallel for schedule(static)
+  for (int ipn = 0; ipn < N; ipn++) {
+    double coltend = 0.;
+    for (int k = L - 1; k >= 0; k--) {
+      pres[I2(k, ipn)] = pres[I2(k + 1, ipn)] + delp[C2(k, ipn)];
+      exner[I2(k, ipn)] = CP * pow(pres[I2(k, ipn)] / P1000, rdcp);
+      double lyrtend = (ab1 * dp_tndcy[S3(k, ipn, nf)] + ab2 * dp_tndcy[S3(k, ipn, of)] +
+                        ab3 * dp_tndcy[S3(k, ipn, vof)]) / dt;
+      omega[C2(k, ipn)] = coltend + 0.5 * lyrtend;
+      coltend = coltend + lyrtend;
+      double dpdx = 0., dpdy = 0.;
+      for (int edg = 0; edg < c->nprox[ipn]; edg++) {
+        const double *sv = c->sidevec_c + (ipn * 6 + edg) * 2;
+        dpdx = dpdx + lp_edg[E3(k, edg, ipn)] * sv[1];
+        dpdy = dpdy - lp_edg[E3(k, edg, ipn)] * sv[0];
+      }
+      omega[C2(k, ipn)] = omega[C2(k, ipn)] + (u[C2(k, ipn)] * dpdx + v[C2(k, ipn)] * dpdy) * c->rarea[ipn];
+    }
+  }
+}
+
 /* trcadv.F90:95-207 driving trcadv_compute.F90 trcadv1..trcadv3 */
 void orc_trcadv(const orc_ctx *c, const double *trc_edg, double *tracr, double *trcdp,
                 double *trc_tdcy, double *trl_tdcy, const double *massfx, const double *delp) {

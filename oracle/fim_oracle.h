@@ -33,6 +33,7 @@ typedef struct orc_ctx {
   const double *hfcoef;
   double dt;
   int kbl, hi_order, miglim, remap_optn;
+  int flux_schm;                        /* 1 FCT cnuity, 2 mass_adv flux limiter */
   double intfc_smooth, slak, ptop, thktop, rleigh, rlthresh, rltaper;
   const double *thetac, *dpsig;         /* [nvl] */
   const double *dfflen, *biharw;        /* [nvl] */
@@ -62,6 +63,9 @@ void orc_cnuity(const orc_ctx *c, const double *u, const double *v, const double
                 const double *v_edg, const double *dp_edg, const double *lp_edg, double *delp,
                 double *pres, double *exner, double *dp_tndcy, double *dplo_tndcy,
                 double *massfx, double *omega);
+void orc_mass_adv(const orc_ctx *c, const double *u, const double *v, const double *u_edg,
+                  const double *v_edg, double *dp_edg, const double *lp_edg, double *delp,
+                  double *pres, double *exner, double *dp_tndcy, double *massfx, double *omega);
 void orc_trcadv(const orc_ctx *c, const double *trc_edg, double *tracr, double *trcdp,
                 double *trc_tdcy, double *trl_tdcy, const double *massfx, const double *delp);
 void orc_momtum(const orc_ctx *c, double *u, double *v, const double *exner, double *relvor,

@@ -22,7 +22,7 @@ class OrcCtx(ctypes.Structure):
                 ("cs", _VP), ("sn", _VP), ("sidevec_c", _VP), ("sidevec_e", _VP), ("sideln", _VP),
                 ("area", _VP), ("rarea", _VP), ("corio", _VP), ("grndspd", _VP), ("hfcoef", _VP),
                 ("dt", ctypes.c_double), ("kbl", ctypes.c_int), ("hi_order", ctypes.c_int),
-                ("miglim", ctypes.c_int), ("remap_optn", ctypes.c_int),
+                ("miglim", ctypes.c_int), ("remap_optn", ctypes.c_int), ("flux_schm", ctypes.c_int),
                 ("intfc_smooth", ctypes.c_double), ("slak", ctypes.c_double), ("ptop", ctypes.c_double),
                 ("thktop", ctypes.c_double), ("rleigh", ctypes.c_double), ("rlthresh", ctypes.c_double),
                 ("rltaper", ctypes.c_double),
@@ -55,6 +55,7 @@ def load():
             "orc_edgvar3": [P] * 5,
             "orc_cnuity": [P] * 14,
             "orc_trcadv": [P] * 8,
+            "orc_mass_adv": [P] * 13,
             "orc_momtum": [P] * 13,
             "orc_hybgen": [P, I] + [P] * 8,
             "orc_hystat": [P, I] + [P] * 8,
@@ -107,6 +108,7 @@ class Oracle:
         c.rarea, c.corio, c.grndspd = _p(self.rarea), _p(self.corio), _p(self.grndspd)
         c.dt, c.kbl, c.hi_order = cfg.dt, cfg.kbl, cfg.hi_order_flux_comp
         c.miglim, c.remap_optn = cfg.miglim, cfg.remap_optn
+        c.flux_schm = cfg.flux_conserv_schm
         c.intfc_smooth, c.slak, c.ptop, c.thktop = cfg.intfc_smooth, cfg.slak, cfg.ptop, cfg.thktop
         c.rleigh, c.rlthresh, c.rltaper = cfg.rleigh, cfg.rlthresh, cfg.rltaper
         c.thetac, c.dpsig = _p(cfg.thetac), _p(cfg.dpsig)
@@ -135,6 +137,10 @@ class Oracle:
     def cnuity(self, u, v, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner, dp_tndcy, dplo_tndcy, massfx, omega):
         self.lib.orc_cnuity(ctypes.byref(self.c), *map(_p, (u, v, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner,
                                                              dp_tndcy, dplo_tndcy, massfx, omega)))
+
+    def mass_adv(self, u, v, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner, dp_tndcy, massfx, omega):
+        self.lib.orc_mass_adv(ctypes.byref(self.c), *map(_p, (u, v, u_edg, v_edg, dp_edg, lp_edg, delp, pres,
+                                                               exner, dp_tndcy, massfx, omega)))
 
     def trcadv(self, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp):
         self.lib.orc_trcadv(ctypes.byref(self.c), *map(_p, (trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx,
@@ -194,8 +200,12 @@ class Oracle:
                      s["trc_edg"])
         if self.cfg.hi_order_flux_comp:
             self.edgvar3(s["dp3d"], s["tr3d"], s["dp_edg"], s["trc_edg"])
-        self.cnuity(s["us3d"], s["vs3d"], s["u_edg"], s["v_edg"], s["dp_edg"], s["lp_edg"], s["dp3d"], s["pr3d"],
-                    s["ex3d"], s["dp_tdcy"], s["dpl_tdcy"], s["massfx"], s["ws3d"])
+        if self.cfg.flux_conserv_schm == 1:
+            self.cnuity(s["us3d"], s["vs3d"], s["u_edg"], s["v_edg"], s["dp_edg"], s["lp_edg"], s["dp3d"],
+                        s["pr3d"], s["ex3d"], s["dp_tdcy"], s["dpl_tdcy"], s["massfx"], s["ws3d"])
+        else:
+            self.mass_adv(s["us3d"], s["vs3d"], s["u_edg"], s["v_edg"], s["dp_edg"], s["lp_edg"], s["dp3d"],
+                          s["pr3d"], s["ex3d"], s["dp_tdcy"], s["massfx"], s["ws3d"])
         self.trcadv(s["trc_edg"], s["tr3d"], s["trdp"], s["trc_tdcy"], s["trl_tdcy"], s["massfx"], s["dp3d"])
         self.momtum(s["us3d"], s["vs3d"], s["ex3d"], s["relvor"], s["u_edg"], s["v_edg"], s["trc_edg"],
                     s["mont_edg"], s["uvsq_edg"], s["u_tdcy"], s["v_tdcy"], s["dp3d"])

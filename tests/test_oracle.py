@@ -92,3 +92,14 @@ def test_regression_fixture():
     now = compute()
     for k in ref.files:
         assert rel_l2(now[k], ref[k]) < 1e-13, k
+
+
+def test_mass_adv_conserves_mass():
+    grid, cfg, fields = make_case(glvl=3, nvl=38, ntra=5, dt=400.0, seed=9, noise=1.0, flux_conserv_schm=2)
+    o = oracle_for(grid, cfg)
+    s = o.init_state(o.new_state(fields))
+    _, b0 = o.globsum(s["dp3d"], s["tr3d"], s["pr3d"], s["ex3d"])
+    for its in range(1, 6):
+        _, b = o.step(s, its)
+        assert abs(b["qmass"] / b0["qmass"] - 1) < 1e-12
+    assert s["dp3d"].min() >= 0.0 and o.diag_flags == 0
