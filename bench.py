@@ -34,7 +34,11 @@ UNIT = "cell-level-steps/s"
 # write once (own-column values; neighbour values are re-reads served by
 # L1/L2), summed over the tracers it handles.  Used for roofline.achieved.
 WORDS = {
-    "k_edgvar1": lambda T: 41, "k_edgvar3_own": lambda T: 7 * T, "k_edgvar3_avg": lambda T: 12 * T,
+    # the fused step averages only the layer thickness in edgvar3; the
+    # tracers' edge values come from k_tr_own and are averaged in k_tr_lo/hi
+    "k_edgvar1": lambda T: 41, "k_edgvar3_own": lambda T: 7, "k_edgvar3_avg": lambda T: 12,
+    "k_tr_own": lambda T: 7 * (T - 1), "k_tr_lo": lambda T: 15 * T + 7, "k_tr_lim": lambda T: 8 * T + 1,
+    "k_tr_hi": lambda T: 17 * T + 7,
     "k_cnuity12": lambda T: 37, "k_cnuity3": lambda T: 8, "k_cnuity4": lambda T: 26, "k_cnuity5": lambda T: 14,
     "k_trcadv1": lambda T: 27 * T, "k_trcadv2": lambda T: 16 * T, "k_trcadv3": lambda T: 18 * T,
     "k_dissip": lambda T: 5, "k_del4prep": lambda T: 4, "k_momtum1": lambda T: 44,
@@ -367,6 +371,33 @@ def reference_arm(args, ws, rank):
     print(json.dumps(line))
 
 
+def serve_arm(args, ws, rank, local):
+    """Served forecast-advance requests: a seeded Poisson stream of the mixed
+    glvl 5/6/7, nvl 38/64, 4-20 tracer workload, continuous batching."""
+    import torch
+    from fimocn_subx_realtime_hera_apr2020_gb300.serve import Server, latency_stats, poisson_requests
+
+    torch.cuda.set_device(local)
+    reqs = poisson_requests(args.serve, rate=args.serve_rate, seed=5000, steps=(args.serve_min_steps,
+                                                                                 args.serve_max_steps))
+    out = {}
+    for prec in ("f32", "f64") if args.serve_fp64 else ("f32",):
+        srv = Server(precision=prec, slots=args.serve_slots, collect=())
+        done = srv.run(reqs, realtime=True)
+        srv.close()
+        out[prec] = latency_stats(done)
+        for r in reqs:
+            r.t_admit = r.t_done = r.result = None
+    line = {"metric": "served forecast-advance latency (p50/p99) and aggregate cell-level-steps/s",
+            "value": out["f32"]["p50_s"], "unit": "s", "higher_is_better": False,
+            "config": {"requests": args.serve, "rate_per_s": args.serve_rate, "slots_per_pool": args.serve_slots,
+                       "glvl": [5, 6, 7], "nvl": [38, 64], "tracers": [4, 20],
+                       "steps": [args.serve_min_steps, args.serve_max_steps]},
+            "serve": out}
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -378,12 +409,21 @@ def main():
     p.add_argument("--fp64-steps", type=int, default=2)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--serve", type=int, default=0, help="run the serving benchmark with this many requests")
+    p.add_argument("--serve-rate", type=float, default=20.0)
+    p.add_argument("--serve-slots", type=int, default=8)
+    p.add_argument("--serve-min-steps", type=int, default=24)
+    p.add_argument("--serve-max-steps", type=int, default=240)
+    p.add_argument("--serve-fp64", action="store_true")
     args = p.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     ws, rank, local = dist_env()
     if args.impl == "reference":
         reference_arm(args, ws, rank)
+        return
+    if args.serve:
+        serve_arm(args, ws, rank, local)
         return
     gpu_arm(args, ws, rank, local)
 

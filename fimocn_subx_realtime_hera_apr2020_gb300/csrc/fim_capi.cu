@@ -702,6 +702,8 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
   *out = nullptr;
   if (cfg->nvl < 4 || cfg->nvl > kMaxL || cfg->ntra < 4 || cfg->ntra > 32 || g->nip < 12 || cfg->dt <= 0.)
     return FIM_EINVAL;
+  // kernels index one member's edge field (nvl x 6 x nip) with 32-bit offsets
+  if ((long long)g->nip * 6 * (cfg->nvl + 1) > 2147483647LL) return FIM_EINVAL;
   if (cfg->flux_conserv_schm != 1 && cfg->flux_conserv_schm != 2) return FIM_ENOTSUP;
   if (cfg->pure_sig) return FIM_ENOTSUP;
   if (cfg->remap_optn < 1 || cfg->remap_optn > 3) return FIM_EINVAL;

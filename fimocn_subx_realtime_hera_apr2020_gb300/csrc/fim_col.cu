@@ -581,16 +581,26 @@ template <> struct Acc<float> {
 constexpr int kMaxT = 32;
 constexpr int kGsBlocks = 152 * 4;
 
-// Level sums: slot 0 = sum(area*dp), slot 1+t = sum(area*dp*tr_t).
+// Slots of one block's partial sums: 0 = sum(area*dp), 1+t = sum(area*dp*tr_t)
+// (level sums), kMaxT+1.. = the column sums of globsum.F90:81-85
+// (rain, convective rain, non-convective rain, latent energy).
+constexpr int kGsCol = kMaxT + 1;
+constexpr int kGsSlots = kMaxT + 5;
+
 template <typename R>
-__global__ void __launch_bounds__(kBlock2) k_globsum_levels(Grid<R> g, Strides s, const R* __restrict__ dp3d,
-    const R* __restrict__ tr, double* __restrict__ partial) {
-  const int N = g.N, L = g.L, T = g.T;
+__global__ void __launch_bounds__(kBlock2) k_globsum_levels(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
+    const R* __restrict__ dp3d, const R* __restrict__ tr, const R* __restrict__ rn2d, const R* __restrict__ rc2d,
+    const R* __restrict__ pr3d, const R* __restrict__ ex3d, const R* __restrict__ qf2d,
+    double* __restrict__ partial) {
+  const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
   const size_t m = blockIdx.y;
-  dp3d += m * s.cell; tr += m * s.tr;
+  sp += m;
+  if (!sp->active) return;
+  dp3d += m * s.cell; tr += m * s.tr; pr3d += m * s.intf; ex3d += m * s.intf;
   const size_t NL = (size_t)N * L;
+  const size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, gstride = (size_t)gridDim.x * blockDim.x;
   Acc<R> acc[kMaxT + 1];
-  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < NL; idx += (size_t)gridDim.x * blockDim.x) {
+  for (size_t idx = gid; idx < NL; idx += gstride) {
     const int i = (int)(idx / L);
     const R ad = g.area[i] * dp3d[idx];
     acc[0].add(ad);
@@ -598,13 +608,26 @@ __global__ void __launch_bounds__(kBlock2) k_globsum_levels(Grid<R> g, Strides s
     for (int t = 0; t < kMaxT; t++)
       if (t < T) acc[1 + t].add(ad * tr[(size_t)t * NL + idx]);
   }
+  double col[4] = {0., 0., 0., 0.};
+  const double dt = sp->dt, rdcp = kRd / kCp;
+  for (size_t i = gid; i < (size_t)N; i += gstride) {
+    const double a = g.area_d[i];
+    const double rn = rn2d ? (double)rn2d[m * s.col + i] : 0.0;
+    const double rc = rc2d ? (double)rc2d[m * s.col + i] : 0.0;
+    const double qf = qf2d ? (double)qf2d[m * s.col + i] : 0.0;
+    col[0] += a * rn;
+    col[1] += a * rc;
+    col[2] += a * (rn - rc);
+    const double den = (double)pr3d[i * L1] / (rdcp * (double)ex3d[i * L1] * (double)tr[i * L]);
+    col[3] += a * den * qf * dt / (1.25 * 2.5e6);
+  }
   __shared__ double red[kBlock2 / 32];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  double* out = partial + (m * gridDim.x + blockIdx.x) * (kMaxT + 1);
+  double* out = partial + (m * gridDim.x + blockIdx.x) * kGsSlots;
 #pragma unroll
-  for (int q = 0; q < kMaxT + 1; q++) {
-    if (q > T) break;
-    double v = acc[q].value();
+  for (int q = 0; q < kGsSlots; q++) {
+    if (q > T && q < kGsCol) continue;
+    double v = q < kGsCol ? acc[q].value() : col[q - kGsCol];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     if (lane == 0) red[wib] = v;
@@ -618,49 +641,33 @@ __global__ void __launch_bounds__(kBlock2) k_globsum_levels(Grid<R> g, Strides s
   }
 }
 
-// Column sums (globsum.F90:81-85) and the final reduction of the partials.
+// Final reduction of the block partials; one warp per output slot.
 template <typename R>
-__global__ void k_globsum_final(Grid<R> g, Strides s, const StepParams* __restrict__ sp, const R* __restrict__ tr,
-    const R* __restrict__ rn2d, const R* __restrict__ rc2d, const R* __restrict__ pr3d, const R* __restrict__ ex3d,
-    const R* __restrict__ qf2d, const double* __restrict__ partial, int nblk, double* __restrict__ sums) {
-  const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
+__global__ void k_globsum_final(const StepParams* __restrict__ sp, int T, const double* __restrict__ partial,
+                                int nblk, double* __restrict__ sums) {
   const size_t m = blockIdx.x;
   sp += m;
   if (!sp->active) return;
-  tr += m * s.tr; pr3d += m * s.intf; ex3d += m * s.intf;
-  __shared__ double red[4][kBlock2];
-  double sr = 0., src = 0., srn = 0., se = 0.;
-  const double dt = sp->dt, rdcp = kRd / kCp;
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
-    const double a = g.area_d[i];
-    const double rn = rn2d ? (double)rn2d[m * s.col + i] : 0.0;
-    const double rc = rc2d ? (double)rc2d[m * s.col + i] : 0.0;
-    const double qf = qf2d ? (double)qf2d[m * s.col + i] : 0.0;
-    sr += a * rn;
-    src += a * rc;
-    srn += a * (rn - rc);
-    const double den = (double)pr3d[(size_t)i * L1] / (rdcp * (double)ex3d[(size_t)i * L1] * (double)tr[(size_t)i * L]);
-    se += a * den * qf * dt / (1.25 * 2.5e6);
-  }
-  red[0][threadIdx.x] = sr; red[1][threadIdx.x] = src; red[2][threadIdx.x] = srn; red[3][threadIdx.x] = se;
-  __syncthreads();
+  const int lane = threadIdx.x & 31;
   double* out = sums + m * (8 + T);
-  if (threadIdx.x < 4) {
+  for (int j = threadIdx.x >> 5; j < T + 5; j += blockDim.x >> 5) {
+    const int q = j <= T ? j : kGsCol + (j - T - 1);
     double t = 0.;
-    for (int q = 0; q < (int)blockDim.x; q++) t += red[threadIdx.x][q];
-    // qmstr (sumr), qmstrn (sumrn), qmstrc (sumrc), qmste (sume)
-    const int slot = threadIdx.x == 0 ? 5 : threadIdx.x == 1 ? 7 : threadIdx.x == 2 ? 6 : 4;
-    out[slot] = t;
-  }
-  for (int q = threadIdx.x; q <= T; q += blockDim.x) {
-    double t = 0.;
-    for (int b = 0; b < nblk; b++) t += partial[(m * nblk + b) * (kMaxT + 1) + q];
-    if (q == 0) out[0] = t / kGrvity;
-    else {
+    for (int b = lane; b < nblk; b += 32) t += partial[(m * nblk + b) * kGsSlots + q];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    if (lane != 0) continue;
+    if (q == 0) {
+      out[0] = t / kGrvity;
+    } else if (q <= T) {
       out[8 + (q - 1)] = t;
       if (q == 2) out[1] = t / kGrvity;
       if (q == 3) out[2] = t / kGrvity;
       if (q == 4) out[3] = t / kGrvity;
+    } else {
+      // qmstr (sumr), qmstrc (sumrc), qmstrn (sumrn), qmste (sume)
+      const int c = q - kGsCol;
+      out[c == 0 ? 5 : c == 1 ? 7 : c == 2 ? 6 : 4] = t;
     }
   }
 }
@@ -729,7 +736,7 @@ void launch_hystat(const Launch& l, const Grid<R>& g, const Strides& s, R* ph3d,
 
 size_t globsum_partials(int N, int L, int T, int members) {
   (void)N; (void)L; (void)T;
-  return (size_t)members * kGsBlocks * (kMaxT + 1);
+  return (size_t)members * kGsBlocks * kGsSlots;
 }
 
 template <typename R>
@@ -738,11 +745,10 @@ void launch_globsum(const Launch& l, const Grid<R>& g, const Strides& s, const R
                     double* partial, double* sums) {
   dim3 gl(kGsBlocks, l.members);
   FIM_KBEGIN(l, "k_globsum_levels");
-  k_globsum_levels<R><<<gl, kBlock2, 0, l.stream>>>(g, s, dp3d, tr, partial);
+  k_globsum_levels<R><<<gl, kBlock2, 0, l.stream>>>(g, s, l.sp, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d, partial);
   FIM_KEND(l);
   FIM_KBEGIN(l, "k_globsum_final");
-  k_globsum_final<R><<<l.members, kBlock2, 0, l.stream>>>(g, s, l.sp, tr, rn2d, rc2d, pr3d, ex3d, qf2d, partial,
-                                                           kGsBlocks, sums);
+  k_globsum_final<R><<<l.members, kBlock2, 0, l.stream>>>(l.sp, g.T, partial, kGsBlocks, sums);
   FIM_KEND(l);
 }
 

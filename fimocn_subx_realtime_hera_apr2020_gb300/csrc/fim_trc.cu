@@ -12,10 +12,8 @@
 //   k_tr_hi    trcadv3: recomputes each antidiffusive flux, clips it with the
 //              own/neighbour limiters, AB3 update of tracer x thickness, new tracer.
 //
-// One thread per (level, cell) loops over the tracers, so the mass fluxes and
-// the donor-cell coefficients of its six edges are loaded once for all
-// tracers.  Every flux is formed from the same operands in the same order as
-// the per-routine kernels, so results are bit-identical to them.
+// Every flux is formed from the same operands in the same order as the
+// per-routine kernels, so results are bit-identical to them.
 #include "fim_internal.h"
 
 namespace fim {
@@ -66,103 +64,76 @@ __global__ void __launch_bounds__(kTB) k_tr_own(Grid<R> g, Strides s, const R* _
   }
 }
 
-// Per-edge operands shared by all tracers of a (level, cell).
-template <typename R>
-struct EdgeOps {
-  int np;
-  int ipx[6];
-  size_t own[6], mir[6];  // offsets of own and neighbour's edge slot
-  R mf[6], a[6], b[6];    // massfx(nf), mf+|mf|, mx+|mx|
-};
-
-template <typename R>
-__device__ __forceinline__ void load_edges(const Grid<R>& g, const R* mfn, int i, int k, EdgeOps<R>& E) {
-  const int L = g.L;
-  E.np = g.nprox[i];
-#pragma unroll
-  for (int e = 0; e < 6; e++) {
-    if (e < E.np) {
-      const int ipx = g.prox[i * 6 + e], edx = g.proxs[i * 6 + e];
-      E.ipx[e] = ipx;
-      E.own[e] = ((size_t)i * 6 + e) * L + k;
-      E.mir[e] = ((size_t)ipx * 6 + edx) * L + k;
-      const R m = mfn[E.own[e]], mx = mfn[E.mir[e]];
-      E.mf[e] = m;
-      E.a[e] = m + tabs(m);
-      E.b[e] = mx + tabs(mx);
-    }
-  }
+// One thread per (level, cell, tracer).  The tracer is the fastest-varying
+// part of the block index, so the blocks of one cell range and all tracers of
+// a chunk run back to back and the mass fluxes they share are L2 hits.
+__device__ __forceinline__ bool clt(int N, int L, int nt, int& i, int& k, int& tz) {
+  tz = blockIdx.x % nt;
+  const int cb = blockIdx.x / nt;
+  const int gid = cb * blockDim.x + threadIdx.x;
+  if (gid >= N * L) return false;
+  i = gid / L;
+  k = gid - i * L;
+  return true;
 }
 
-// tracer t's averaged edge value on edge e (t = 0: edgvar1's value)
-template <typename R>
-__device__ __forceinline__ R edge_value(const R* te, int t, const EdgeOps<R>& E, int e) {
-  return (t == 0) ? te[E.own[e]] : R(0.5) * (te[E.own[e]] + te[E.mir[e]]);
-}
-
-// trcadv1 for all tracers + the S+/S- sums of trcadv2 + copy of the old tracer
+// trcadv1 + the S+/S- sums of trcadv2 + copy of the old tracer
 template <typename R>
 __global__ void __launch_bounds__(kTB) k_tr_lo(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     int t0, int nt, const R* __restrict__ massfx, const R* __restrict__ trc_edg, const R* __restrict__ tracr,
     const R* __restrict__ trcdp, R* __restrict__ trl_tdcy, const R* __restrict__ delp,
     R* __restrict__ trcr_lo, R* __restrict__ s_plus, R* __restrict__ s_mnus, R* __restrict__ trold,
     size_t sc) {
-  int i, k;
-  if (!cl(g.N, g.L, i, k)) return;
+  int i, k, tz;
+  if (!clt(g.N, g.L, nt, i, k, tz)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active) return;
+  const int t = t0 + tz;
   const size_t NL = (size_t)N * L;
-  massfx += m * s.mf; trc_edg += m * s.tredg; tracr += m * s.tr; trcdp += m * s.tr;
-  trl_tdcy += m * s.trab; delp += m * s.cell;
-  const size_t so = m * nt * sc;
-  trcr_lo += so; s_plus += so; s_mnus += so; trold += so;
   const int nf = sp->nf, of = sp->of, vof = sp->vof;
+  const R* mfn = massfx + m * s.mf + (size_t)nf * 6 * NL;
+  const R* te = trc_edg + m * s.tredg + (size_t)t * 6 * NL;
+  const R* tr = tracr + m * s.tr + (size_t)t * NL;
+  R* tl = trl_tdcy + m * s.trab + (size_t)t * 3 * NL;
   const R ab1 = R(sp->ab1), ab2 = R(sp->ab2), ab3 = R(sp->ab3);
   const R thshld = R(1.e-11), half = R(0.5);
-  EdgeOps<R> E;
-  load_edges(g, massfx + (size_t)nf * N * 6 * L, i, k, E);
-  const size_t c = (size_t)i * L + k;
-  const R rar = g.rarea[i];
-  const R dpc = tmax(thshld, delp[c]);
+  const int c = i * L + k;
+  const int np = g.nprox[i];
   const int* pr = g.prox + i * 6;
-  for (int tz = 0; tz < nt; tz++) {
-    const int t = t0 + tz;
-    const R* tr = tracr + (size_t)t * NL;
-    const R* te = trc_edg + (size_t)t * 6 * NL;
-    const R tri = tr[c];
-    R sumlo = R(0), sp_ = R(0), sm_ = R(0);
+  const int* ps = g.proxs + i * 6;
+  const R tri = tr[c];
+  R sumlo = R(0), sp_ = R(0), sm_ = R(0), mx = tri, mn = tri;
 #pragma unroll
-    for (int e = 0; e < 6; e++) {
-      if (e < E.np) {
-        const R hi = E.mf[e] * edge_value(te, t, E, e);
-        const R lo = half * (E.a[e] * tri - E.b[e] * tr[(size_t)E.ipx[e] * L + k]);
-        const R anti = hi - lo;
-        sumlo = sumlo + lo;
-        sp_ = sp_ - tmin(R(0), anti);
-        sm_ = sm_ + tmax(R(0), anti);
-      }
+  for (int e = 0; e < 6; e++) {
+    const int ipx = pr[e];
+    const R trx = tr[ipx * L + k];
+    mx = tmax(mx, trx);
+    mn = tmin(mn, trx);
+    if (e < np) {
+      const int own = (i * 6 + e) * L + k, mir = (ipx * 6 + ps[e]) * L + k;
+      const R mf = mfn[own], mfx = mfn[mir];
+      const R tev = (t == 0) ? te[own] : half * (te[own] + te[mir]);
+      const R hi = mf * tev;
+      const R lo = half * ((mf + tabs(mf)) * tri - (mfx + tabs(mfx)) * trx);
+      const R anti = hi - lo;
+      sumlo = sumlo + lo;
+      sp_ = sp_ - tmin(R(0), anti);
+      sm_ = sm_ + tmax(R(0), anti);
     }
-    R* tl = trl_tdcy + (size_t)t * 3 * NL;
-    const R tn = -sumlo * rar;
-    tl[(size_t)nf * NL + c] = tn;
-    const R lo = trcdp[(size_t)t * NL + c] + ab1 * tn + ab2 * tl[(size_t)of * NL + c] + ab3 * tl[(size_t)vof * NL + c];
-    R mx = tri, mn = tri;
-#pragma unroll
-    for (int e = 0; e < 6; e++) {
-      const R x = tr[(size_t)pr[e] * L + k];
-      mx = tmax(mx, x);
-      mn = tmin(mn, x);
-    }
-    mx = tmax(R(0), mx);
-    mn = tmax(R(0), mn);
-    const size_t q = (size_t)tz * sc + c;
-    trcr_lo[q] = tmax(mn, tmin(mx, lo / dpc));
-    s_plus[q] = sp_;
-    s_mnus[q] = sm_;
-    trold[q] = tri;
   }
+  const R tn = -sumlo * g.rarea[i];
+  tl[(size_t)nf * NL + c] = tn;
+  const R lo = trcdp[m * s.tr + (size_t)t * NL + c] + ab1 * tn + ab2 * tl[(size_t)of * NL + c] +
+               ab3 * tl[(size_t)vof * NL + c];
+  mx = tmax(R(0), mx);
+  mn = tmax(R(0), mn);
+  const size_t q = (m * nt + tz) * sc + c;
+  trcr_lo[q] = tmax(mn, tmin(mx, lo / tmax(thshld, delp[m * s.cell + c])));
+  s_plus[q] = sp_;
+  s_mnus[q] = sm_;
+  trold[q] = tri;
 }
 
 // trcadv2: Q+/Q- and the limiters R+/R-; the relaxed bounds are
@@ -173,45 +144,40 @@ __global__ void __launch_bounds__(kTB) k_tr_lim(Grid<R> g, Strides s, const Step
     int t0, int nt, const R* __restrict__ trc_tdcy, const R* __restrict__ delp, const R* __restrict__ trold,
     const R* __restrict__ trcr_lo, const R* __restrict__ s_plus, const R* __restrict__ s_mnus,
     R* __restrict__ r_plus, R* __restrict__ r_mnus, size_t sc) {
-  int i, k;
-  if (!cl(g.N, g.L, i, k)) return;
+  int i, k, tz;
+  if (!clt(g.N, g.L, nt, i, k, tz)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active) return;
+  const int t = t0 + tz;
   const size_t NL = (size_t)N * L;
-  trc_tdcy += m * s.trab; delp += m * s.cell;
-  const size_t so = m * nt * sc;
-  trold += so; trcr_lo += so; s_plus += so; s_mnus += so; r_plus += so; r_mnus += so;
   const int of = sp->of, vof = sp->vof;
   const R ab1 = R(sp->ab1), ab2 = R(sp->ab2), ab3 = R(sp->ab3);
   const R thshld = R(1.e-11);
-  const size_t c = (size_t)i * L + k;
+  const int c = i * L + k;
+  const size_t so = (m * nt + tz) * sc;
+  const R* to = trold + so;
+  const R* lo = trcr_lo + so;
   const int* pr = g.prox + i * 6;
-  const R dp = delp[c];
-  const R ar = g.area[i];
-  for (int tz = 0; tz < nt; tz++) {
-    const int t = t0 + tz;
-    const R* to = trold + (size_t)tz * sc;
-    const R* lo = trcr_lo + (size_t)tz * sc;
-    const R lc = lo[c];
-    R mx = tmax(to[c], lc), mn = tmin(to[c], lc);
+  const R lc = lo[c];
+  R mx = tmax(to[c], lc), mn = tmin(to[c], lc);
 #pragma unroll
-    for (int e = 0; e < 6; e++) {
-      const size_t cx = (size_t)pr[e] * L + k;
-      mx = tmax(mx, tmax(to[cx], lo[cx]));
-      mn = tmin(mn, tmin(to[cx], lo[cx]));
-    }
-    mx = tmax(R(0), mx);
-    mn = tmax(R(0), mn);
-    const R* tc = trc_tdcy + (size_t)t * 3 * NL;
-    const R tof = tc[(size_t)of * NL + c], tvf = tc[(size_t)vof * NL + c];
-    const R q_plus = ((mx - lc) * dp - (ab2 * tmin(R(0), tof) + ab3 * tmax(R(0), tvf))) / ab1 * ar;
-    const R q_mnus = ((lc - mn) * dp + (ab2 * tmax(R(0), tof) + ab3 * tmin(R(0), tvf))) / ab1 * ar;
-    const size_t q = (size_t)tz * sc + c;
-    r_plus[q] = tmax(R(0), tmin(R(1), q_plus / tmax(s_plus[q], thshld)));
-    r_mnus[q] = tmax(R(0), tmin(R(1), q_mnus / tmax(s_mnus[q], thshld)));
+  for (int e = 0; e < 6; e++) {
+    const int cx = pr[e] * L + k;
+    const R a = to[cx], b = lo[cx];
+    mx = tmax(mx, tmax(a, b));
+    mn = tmin(mn, tmin(a, b));
   }
+  mx = tmax(R(0), mx);
+  mn = tmax(R(0), mn);
+  const R* tc = trc_tdcy + m * s.trab + (size_t)t * 3 * NL;
+  const R tof = tc[(size_t)of * NL + c], tvf = tc[(size_t)vof * NL + c];
+  const R dp = delp[m * s.cell + c], ar = g.area[i];
+  const R q_plus = ((mx - lc) * dp - (ab2 * tmin(R(0), tof) + ab3 * tmax(R(0), tvf))) / ab1 * ar;
+  const R q_mnus = ((lc - mn) * dp + (ab2 * tmax(R(0), tof) + ab3 * tmin(R(0), tvf))) / ab1 * ar;
+  r_plus[so + c] = tmax(R(0), tmin(R(1), q_plus / tmax(s_plus[so + c], thshld)));
+  r_mnus[so + c] = tmax(R(0), tmin(R(1), q_mnus / tmax(s_mnus[so + c], thshld)));
 }
 
 // trcadv3: clip the recomputed antidiffusive fluxes, AB3 update, new tracer
@@ -221,66 +187,59 @@ __global__ void __launch_bounds__(kTB) k_tr_hi(Grid<R> g, Strides s, const StepP
     R* __restrict__ trcdp, R* __restrict__ trc_tdcy, const R* __restrict__ trl_tdcy, const R* __restrict__ delp,
     const R* __restrict__ trold, const R* __restrict__ trcr_lo, const R* __restrict__ r_plus,
     const R* __restrict__ r_mnus, size_t sc) {
-  int i, k;
-  if (!cl(g.N, g.L, i, k)) return;
+  int i, k, tz;
+  if (!clt(g.N, g.L, nt, i, k, tz)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active) return;
+  const int t = t0 + tz;
   const size_t NL = (size_t)N * L;
-  massfx += m * s.mf; trc_edg += m * s.tredg; tracr += m * s.tr; trcdp += m * s.tr;
-  trc_tdcy += m * s.trab; trl_tdcy += m * s.trab; delp += m * s.cell;
-  const size_t so = m * nt * sc;
-  trold += so; trcr_lo += so; r_plus += so; r_mnus += so;
   const int nf = sp->nf, of = sp->of, vof = sp->vof;
   const R ab1 = R(sp->ab1), ab2 = R(sp->ab2), ab3 = R(sp->ab3);
   const R thshld = R(1.e-11), half = R(0.5);
-  EdgeOps<R> E;
-  load_edges(g, massfx + (size_t)nf * N * 6 * L, i, k, E);
-  const size_t c = (size_t)i * L + k;
-  const R rar = g.rarea[i];
-  const R dpc = tmax(thshld, delp[c]);
+  const R* mfn = massfx + m * s.mf + (size_t)nf * 6 * NL;
+  const R* te = trc_edg + m * s.tredg + (size_t)t * 6 * NL;
+  const size_t so = (m * nt + tz) * sc;
+  const R* to = trold + so;
+  const R* lo = trcr_lo + so;
+  const R* rp = r_plus + so;
+  const R* rm = r_mnus + so;
+  const int c = i * L + k;
+  const int np = g.nprox[i];
   const int* pr = g.prox + i * 6;
-  for (int tz = 0; tz < nt; tz++) {
-    const int t = t0 + tz;
-    const R* to = trold + (size_t)tz * sc;
-    const R* te = trc_edg + (size_t)t * 6 * NL;
-    const R* rp = r_plus + (size_t)tz * sc;
-    const R* rm = r_mnus + (size_t)tz * sc;
-    const R tri = to[c];
-    const R rpc = rp[c], rmc = rm[c];
-    R at = R(0);
+  const int* ps = g.proxs + i * 6;
+  const R tri = to[c], rpc = rp[c], rmc = rm[c], lc = lo[c];
+  R at = R(0), mx = tmax(tri, lc), mn = tmin(tri, lc);
 #pragma unroll
-    for (int e = 0; e < 6; e++) {
-      if (e < E.np) {
-        const size_t cx = (size_t)E.ipx[e] * L + k;
-        const R hi = E.mf[e] * edge_value(te, t, E, e);
-        const R lo = half * (E.a[e] * tri - E.b[e] * to[cx]);
-        R a = hi - lo;
-        if (a >= R(0)) a = a * tmin(rmc, rp[cx]);
-        else a = a * tmin(rpc, rm[cx]);
-        at = at + a;
-      }
+  for (int e = 0; e < 6; e++) {
+    const int ipx = pr[e];
+    const int cx = ipx * L + k;
+    const R trx = to[cx], lox = lo[cx];
+    mx = tmax(mx, tmax(trx, lox));
+    mn = tmin(mn, tmin(trx, lox));
+    if (e < np) {
+      const int own = (i * 6 + e) * L + k, mir = (ipx * 6 + ps[e]) * L + k;
+      const R mf = mfn[own], mfx = mfn[mir];
+      const R tev = (t == 0) ? te[own] : half * (te[own] + te[mir]);
+      const R hi = mf * tev;
+      const R lo_ = half * ((mf + tabs(mf)) * tri - (mfx + tabs(mfx)) * trx);
+      R a = hi - lo_;
+      if (a >= R(0)) a = a * tmin(rmc, rp[cx]);
+      else a = a * tmin(rpc, rm[cx]);
+      at = at + a;
     }
-    // bounds of trcadv2, recomputed (max/min are exact)
-    const R* lo_ = trcr_lo + (size_t)tz * sc;
-    R mx = tmax(tri, lo_[c]), mn = tmin(tri, lo_[c]);
-#pragma unroll
-    for (int e = 0; e < 6; e++) {
-      const size_t cx = (size_t)pr[e] * L + k;
-      mx = tmax(mx, tmax(to[cx], lo_[cx]));
-      mn = tmin(mn, tmin(to[cx], lo_[cx]));
-    }
-    mx = tmax(R(0), mx);
-    mn = tmax(R(0), mn);
-    at = -at * rar;
-    R* tc = trc_tdcy + (size_t)t * 3 * NL;
-    const R tn = trl_tdcy[(size_t)t * 3 * NL + (size_t)nf * NL + c] + at;
-    tc[(size_t)nf * NL + c] = tn;
-    const R td = trcdp[(size_t)t * NL + c] + ab1 * tn + ab2 * tc[(size_t)of * NL + c] + ab3 * tc[(size_t)vof * NL + c];
-    trcdp[(size_t)t * NL + c] = td;
-    tracr[(size_t)t * NL + c] = tmax(mn, tmin(mx, td / dpc));
   }
+  mx = tmax(R(0), mx);
+  mn = tmax(R(0), mn);
+  at = -at * g.rarea[i];
+  R* tc = trc_tdcy + m * s.trab + (size_t)t * 3 * NL;
+  const R tn = trl_tdcy[m * s.trab + (size_t)t * 3 * NL + (size_t)nf * NL + c] + at;
+  tc[(size_t)nf * NL + c] = tn;
+  R* td = trcdp + m * s.tr + (size_t)t * NL;
+  const R tdn = td[c] + ab1 * tn + ab2 * tc[(size_t)of * NL + c] + ab3 * tc[(size_t)vof * NL + c];
+  td[c] = tdn;
+  tracr[m * s.tr + (size_t)t * NL + c] = tmax(mn, tmin(mx, tdn / tmax(thshld, delp[m * s.cell + c])));
 }
 
 template <typename R>
@@ -288,9 +247,9 @@ void launch_tracers_fused(const Launch& l, const Grid<R>& g, const Strides& s, c
                           R* trc_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx,
                           const R* delp) {
   const size_t sc = (size_t)g.N * g.L;
-  dim3 grid(tblocks((long long)g.N * g.L), l.members);
   for (int t0 = 0; t0 < g.T; t0 += w.tchunk) {
     const int nt = (g.T - t0 < w.tchunk) ? g.T - t0 : w.tchunk;
+    dim3 grid(tblocks((long long)g.N * g.L) * nt, l.members);
     FIM_KBEGIN(l, "k_tr_lo");
     k_tr_lo<R><<<grid, kTB, 0, l.stream>>>(g, s, l.sp, t0, nt, massfx, trc_edg, tracr, trcdp, trl_tdcy, delp,
                                             w.trcr_lo, w.s_plus, w.s_mnus, w.trold, sc);

@@ -32,6 +32,7 @@ class Request:
     ntra: int = field(compare=False)
     steps: int = field(compare=False)
     seed: int = field(compare=False, default=0)
+    t_queue: float = field(compare=False, default=None)
     t_admit: float = field(compare=False, default=None)
     t_done: float = field(compare=False, default=None)
     result: dict = field(compare=False, default=None)
@@ -160,7 +161,11 @@ class Server:
         while pending or waiting or any(p.active() for p in self.pools.values()):
             t = now()
             while pending and (pending[0].arrival <= t or not realtime):
-                waiting.append(heapq.heappop(pending))
+                r = heapq.heappop(pending)
+                # latency counts from arrival, or from entry into the queue
+                # when arrivals are not replayed in real time
+                r.t_queue = r.arrival if realtime else t
+                waiting.append(r)
                 if not realtime:
                     break
             still = []
@@ -205,8 +210,8 @@ def poisson_requests(n, rate, seed, glvls=(5, 6, 7), nvls=(38, 64), tracers=(4, 
 
 
 def latency_stats(done):
-    lat = np.array([r.t_done - r.arrival for r in done])
+    lat = np.array([r.t_done - r.t_queue for r in done])
     work = sum(r.work for r in done)
-    span = max(r.t_done for r in done) - min(r.arrival for r in done)
+    span = max(r.t_done for r in done) - min(r.t_queue for r in done)
     return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
             "mean_s": float(lat.mean()), "requests": len(done), "cell_level_steps_per_s": work / span}
