@@ -77,6 +77,7 @@ _SIGS = {
     "fim_launch_count": ([_VP], ctypes.c_int64),
     "fim_profile_enable": ([_VP, _I], _I),
     "fim_profile_report": ([_VP, ctypes.c_char_p, _I], _I),
+    "fim_cnuity_noalloc": ([_VP, _I] + [_VP] * 13, _I),
 }
 _ROUTINES = {
     "fim_edgvar1": [_VP, _I] + [_VP] * 16,

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -1162,3 +1163,93 @@ int fim_check(fim_ctx* c, fim_state* st, int* flags) {
 }
 
 }  // extern "C"
+
+// ---- cnuity without allocation ---------------------------------------------
+// fim_cnuity_r8/_r4 allocate their FCT scratch (the antidiffusive fluxes, the
+// low-order thickness and the four limiter fields: 11 values per cell-level)
+// on the context's first call.  fim_cnuity_noalloc takes that scratch from one
+// array that is part of the loaded library image instead, for callers that may
+// not allocate device memory while they run: a host model whose device memory
+// is carved up once by its own pool at start-up, a memory-capped process, or a
+// time loop that cannot afford the device-wide synchronisation of cudaMalloc.
+// Each GPU that loads this library holds the array (kCnuityStaticBytes) until
+// the process exits.  Every call on a device shares it and it keeps the
+// previous call's contents; the cnuity kernels write every scratch value they
+// read before reading it, so nothing is cleared.  Calls whose kernels overlap
+// on the GPU (two streams, two contexts, two host threads) race on it.
+namespace {
+
+constexpr size_t kCnuityStaticBytes = size_t(64) << 20;
+constexpr int kStaticMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_cnuity_static[kCnuityStaticBytes];
+
+std::mutex g_static_mu;
+void* g_static_addr[kStaticMaxDevices] = {};
+
+// Device address of g_cnuity_static on the current device, looked up once per
+// device (the host-side name is only a handle for the runtime, not an address).
+int cnuity_static_addr(fim_ctx* c, unsigned char** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return set_err(c, FIM_ECUDA, "cudaGetDevice", e);
+  if (dev < 0 || dev >= kStaticMaxDevices) return set_err(c, FIM_EINVAL, "device ordinal beyond 63");
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (!g_static_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_cnuity_static);
+    if (e != cudaSuccess) return set_err(c, FIM_ECUDA, "cudaGetSymbolAddress(static cnuity scratch)", e);
+    g_static_addr[dev] = p;
+  }
+  *out = (unsigned char*)g_static_addr[dev];
+  return FIM_OK;
+}
+
+size_t round256(size_t b) { return (b + 255) / 256 * 256; }
+
+template <typename R>
+int cnuity_noalloc_impl(fim_ctx* c, const void* u_velo, const void* v_velo, const void* u_edg, const void* v_edg,
+                        const void* dp_edg, const void* lp_edg, void* delp, void* pres, void* exner, void* dp_tndcy,
+                        void* dplo_tndcy, void* massfx, void* omega) {
+  if (c->cfg.host_pointers)
+    return set_err(c, FIM_EINVAL, "fim_cnuity_noalloc takes device pointers only (host_pointers context)");
+  // like fim_cnuity_r8/_r4 the call advances member 0 only
+  const size_t cells = (size_t)c->N * c->L;
+  const size_t one = round256(cells * sizeof(R)), six = round256(cells * 6 * sizeof(R));
+  const size_t need = six + 5 * one;
+  if (need > kCnuityStaticBytes) {
+    char msg[200];
+    snprintf(msg, sizeof msg,
+             "fim_cnuity_noalloc: this grid needs %zu bytes of scratch, the static array holds %zu "
+             "(11 x nip x nvl values)", need, kCnuityStaticBytes);
+    return set_err(c, FIM_EINVAL, msg);
+  }
+  const void* ptrs[] = {u_velo, v_velo, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner, dp_tndcy, dplo_tndcy,
+                        massfx, omega};
+  for (const void* p : ptrs)
+    if (!p) return set_err(c, FIM_EINVAL, "fim_cnuity_noalloc: null field pointer");
+  unsigned char* base = nullptr;
+  int rc = cnuity_static_addr(c, &base);
+  if (rc) return rc;
+  if ((rc = push_sp(c))) return rc;
+  CnuityScratch<R> w{(R*)base, (R*)(base + six), (R*)(base + six + one), (R*)(base + six + 2 * one),
+                     (R*)(base + six + 3 * one), (R*)(base + six + 4 * one)};
+  launch_cnuity<R>(make_launch(c, 1), grid_of<R>(c), c->str, w, (const R*)u_velo, (const R*)v_velo,
+                   (const R*)u_edg, (const R*)v_edg, (const R*)dp_edg, (const R*)lp_edg, (R*)delp, (R*)pres,
+                   (R*)exner, (R*)dp_tndcy, (R*)dplo_tndcy, (R*)massfx, (R*)omega);
+  return check_launch(c, "cnuity (static scratch)");
+}
+
+}  // namespace
+
+extern "C" int fim_cnuity_noalloc(fim_ctx* c, int its, const void* u_velo, const void* v_velo, const void* u_edg,
+                                  const void* v_edg, const void* dp_edg, const void* lp_edg, void* delp, void* pres,
+                                  void* exner, void* dp_tndcy, void* dplo_tndcy, void* massfx, void* omega) {
+  (void)its;
+  if (!c) return FIM_EINVAL;
+  if (c->prec == FIM_PREC_F64)
+    return cnuity_noalloc_impl<double>(c, u_velo, v_velo, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner,
+                                       dp_tndcy, dplo_tndcy, massfx, omega);
+  return cnuity_noalloc_impl<float>(c, u_velo, v_velo, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner, dp_tndcy,
+                                    dplo_tndcy, massfx, omega);
+}

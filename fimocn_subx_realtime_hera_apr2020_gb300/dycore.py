@@ -133,6 +133,18 @@ class Dycore:
         self._call("fim_cnuity", its, *map(_ptr, (u_velo, v_velo, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner,
                                                     dp_tndcy, dplo_tndcy, massfx, omega)))
 
+    def cnuity_noalloc(self, its, u_velo, v_velo, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner, dp_tndcy,
+                       dplo_tndcy, massfx, omega):
+        """cnuity with its scratch in the library's static array (device
+        pointers only; no device allocation by the call)."""
+        import torch
+        torch.cuda.current_stream().synchronize()
+        _lib.check(self.lib.fim_cnuity_noalloc(self.ctx, its, *map(_ptr, (u_velo, v_velo, u_edg, v_edg, dp_edg,
+                                                                            lp_edg, delp, pres, exner, dp_tndcy,
+                                                                            dplo_tndcy, massfx, omega))),
+                   "fim_cnuity_noalloc", self.ctx)
+        self.sync_stream()
+
     def mass_adv(self, its, u_velo, v_velo, u_edg, v_edg, dp_edg, lp_edg, delp, pres, exner, dp_tndcy, massfx,
                  omega):
         self._call("fim_mass_adv", its, *map(_ptr, (u_velo, v_velo, u_edg, v_edg, dp_edg, lp_edg, delp, pres,

@@ -159,6 +159,24 @@ int fim_cnuity_r4(fim_ctx *ctx, int its, const float *u_velo, const float *v_vel
                   const float *lp_edg, float *delp, float *pres, float *exner,
                   float *dp_tndcy, float *dplo_tndcy, float *massfx, float *omega);
 
+/* Allocation-free cnuity (no counterpart in the reference).  For callers that
+ * may not allocate device memory while they run: fim_cnuity_r8/_r4 allocate
+ * their FCT scratch on the first call; this entry point takes it from one
+ * static 64 MiB array in the library image instead (every GPU that loads the
+ * library holds it until exit).  Same arguments as fim_cnuity_r8 (context in
+ * FIM_PREC_F64) or fim_cnuity_r4 (FIM_PREC_F32), passed as untyped device
+ * pointers; host_pointers contexts are rejected.  Like those, it advances
+ * member 0.  The scratch takes 11 x nip x nvl values: glvl 5 / nvl 64 fits in
+ * FP64, glvl 6 / nvl 64 does not fit in either precision and is rejected with
+ * FIM_EINVAL.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) and should come before any stream
+ * capture.  All calls on a device share the array: calls whose kernels
+ * overlap on the GPU race. */
+int fim_cnuity_noalloc(fim_ctx *ctx, int its, const void *u_velo, const void *v_velo,
+                       const void *u_edg, const void *v_edg, const void *dp_edg,
+                       const void *lp_edg, void *delp, void *pres, void *exner,
+                       void *dp_tndcy, void *dplo_tndcy, void *massfx, void *omega);
+
 /* FIMsrc/fim/horizontal/massadv.F90:21-23 (flux_conserv_schm = 2, the
  * reference default: flux limiter of flux_limiter.F90 + update_pres);
  * dp_edg is limited in place */
