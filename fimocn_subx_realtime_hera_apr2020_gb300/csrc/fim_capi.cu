@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -67,6 +68,7 @@ struct fim_ctx {
   void *f_trcr_lo = nullptr, *f_sp = nullptr, *f_sm = nullptr, *f_trold = nullptr, *f_rp = nullptr,
        *f_rm = nullptr;
   int ftchunk = 0;
+  int trc_vk = 0;  // levels per thread of the fused tracer kernels (0: widest that nvl allows)
   void *du = nullptr, *dv = nullptr, *wu = nullptr, *wv = nullptr;
   void *exsmo = nullptr, *exsmo2 = nullptr;
   double* gs_partial = nullptr;
@@ -301,6 +303,8 @@ int ensure_hybgen(fim_ctx* c, int members) {
   int rc;
   if ((rc = ensure(c, &c->exsmo, NI))) return rc;
   if ((rc = ensure(c, &c->exsmo2, NI))) return rc;
+  const int e = c->prec == FIM_PREC_F64 ? prepare_hybgen<double>(c->L) : prepare_hybgen<float>(c->L);
+  if (e) return set_err(c, FIM_ECUDA, "hybgen kernel attributes", (cudaError_t)e);
   return FIM_OK;
 }
 
@@ -607,7 +611,7 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
     // own-side values, averaged where the fused tracer kernels use them
     launch_edgvar3<R>(l, g, s, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), F<R>(st, FIM_DP_EDG), F<R>(st, FIM_TRC_EDG),
                       1);
-    launch_tracer_own<R>(l, g, s, F<R>(st, FIM_TR3D), F<R>(st, FIM_TRC_EDG));
+    launch_tracer_own<R>(l, g, s, F<R>(st, FIM_TR3D), F<R>(st, FIM_TRC_EDG), c->trc_vk);
   }
   CnuityScratch<R> cw{(R*)c->antifx, (R*)c->delp_lo, (R*)c->p_plus, (R*)c->p_mnus, (R*)c->r_plus, (R*)c->r_mnus};
   if (c->cfg.flux_conserv_schm == 1)
@@ -621,7 +625,7 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
                       F<R>(st, FIM_EX3D), F<R>(st, FIM_DP_TDCY), F<R>(st, FIM_MASSFX), F<R>(st, FIM_WS3D));
   if (c->kn.hi_order) {
     TrcFusedScratch<R> fw{(R*)c->f_trcr_lo, (R*)c->f_sp, (R*)c->f_sm, (R*)c->f_trold, (R*)c->f_rp, (R*)c->f_rm,
-                          c->ftchunk};
+                          c->ftchunk, c->trc_vk};
     launch_tracers_fused<R>(l, g, s, fw, F<R>(st, FIM_TRC_EDG), F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP),
                             F<R>(st, FIM_TRC_TDCY), F<R>(st, FIM_TRL_TDCY), F<R>(st, FIM_MASSFX),
                             F<R>(st, FIM_DP3D));
@@ -724,6 +728,8 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
   c->thetac.assign(cfg->thetac, cfg->thetac + c->L);
   c->dpsig.assign(cfg->dpsig, cfg->dpsig + c->L);
   c->str = make_strides(c->N, c->L, c->T);
+  // FIM_TRC_VK=1|2|4 pins the levels per thread of the fused tracer kernels
+  if (const char* v = getenv("FIM_TRC_VK")) c->trc_vk = atoi(v);
   const int N = c->N, L = c->L;
   // 0-based index tables; validate the Fortran numbering
   std::vector<int> prox(N * 6), proxs(N * 6), nprox(N);

@@ -481,6 +481,255 @@ __global__ void __launch_bounds__(kColBlock) k_remap(Grid<R> g, Strides s, Knobs
   if (bad) atomicOr(flags + m, kFlagColumnIntegral);
 }
 
+// ------------------------------------------------- remap, warp per column --
+// remap_1d for the default knobs (PLM, remap_optn = 2; one-layer migration,
+// miglim = 1) with one warp per column and one lane per remapped field (u, v,
+// tracers 2..ntra in pressure, theta in p^(kappa+1)).  The column's fields sit
+// in a shared-memory tile, lane = field, loaded and stored coalesced along the
+// levels; each lane runs pcwise's recurrences on its own tile column, where
+// the thread-per-column kernel keeps ~30 column arrays per thread in local
+// memory.  Operations and their order per field are those of pcwise above.
+constexpr int kTS = 33;   // tile row stride (32 fields + 1: conflict-free transposes)
+constexpr int kWarpsRemap = 4;
+
+template <typename R, int ML>
+struct RemapSm {
+  R tile[ML * kTS];
+  R dz_p[ML + 1], fo_p[ML], fn_p[ML];   // delz, fco, fcn in pressure
+  R dz_k[ML + 1], fo_k[ML], fn_k[ML];   // the same in p^(kappa+1)
+  R exold[ML + 1], exnew[ML + 1], prcol[ML + 1], prnew[ML + 1], pk1col[ML + 1], pk1new[ML + 1];
+  R dpcol[ML];
+};
+
+// PLM slope of layer lyr (pcwise remap_optn = 2); y has stride kTS
+template <typename R>
+__device__ __forceinline__ R plm_b(const R* y, int lyr, int kk) {
+  if (lyr < 1 || lyr > kk - 2) return R(0);
+  const R f = y[lyr * kTS], fm = y[(lyr - 1) * kTS], fp = y[(lyr + 1) * kTS];
+  if (f <= cmin(fm, fp) || f >= cmax(fm, fp)) return R(0);
+  if ((fp - fm) * (fm + fp - R(2) * f) > R(0)) return f - fm;
+  return fp - f;
+}
+
+// vertfx(k), 1 <= k <= kk-1, of pcwise with miglim = 1 and PLM coefficients
+template <typename R>
+__device__ __forceinline__ R plm_flux(const R* y, const R* dz, const R* fco, int k, int kk) {
+  const R athird = R(1) / R(3);
+  R slab = R(0), amount = R(0);
+  const R d = dz[k];
+  if (d > R(0)) {
+    const int lyr = k;
+    if (fco[lyr] > R(0)) {
+      const R a = y[lyr * kTS], b = plm_b(y, lyr, kk), cc = R(0);
+      const R dslab = cmin(slab + fco[lyr], d) - cmin(slab, d);
+      const R dx = dslab / fco[lyr];
+      const R fcdx = a + b * R(.5) * (dx - R(1)) + cc * (R(.25) - dx * (R(.5) - dx * athird));
+      amount = amount + fcdx * dslab;
+      slab = slab + dslab;
+    }
+  } else if (d < R(0)) {
+    const int lyr = k - 1;
+    if (fco[lyr] > R(0)) {
+      const R a = y[lyr * kTS], b = plm_b(y, lyr, kk), cc = R(0);
+      const R dslab = cmin(slab + fco[lyr], -d) - cmin(slab, -d);
+      const R dx = dslab / fco[lyr];
+      const R fcdx = a + b * R(.5) * (R(1) - dx) + cc * (R(.25) - dx * (R(.5) - dx * athird));
+      amount = amount + fcdx * dslab;
+      slab = slab + dslab;
+    }
+  }
+  return slab != R(0) ? -d * amount / slab : R(0);
+}
+
+// pcwise (PLM, miglim = 1) in place on one lane's tile column y (stride kTS).
+// Returns true when the column-integral check fails (FP64 build only).
+template <typename R>
+__device__ bool pcwise_lane(int kk, R* y, const R* dz, const R* fco, const R* fcn) {
+  const R small = R(1.e-22);
+  R bfore = R(0), colscl = R(0);
+  if (sizeof(R) == 8) {
+    for (int k = 0; k < kk; k++) {
+      bfore = bfore + y[k * kTS] * fco[k];
+      colscl = colscl + cabs(y[k * kTS] * fco[k]);
+    }
+  }
+  for (int k = kk - 2; k >= 0; k--) y[k * kTS] = (y[k * kTS] * fco[k] + y[(k + 1) * kTS] * small) / (fco[k] + small);
+  for (int k = 1; k < kk; k++) y[k * kTS] = (y[k * kTS] * fco[k] + y[(k - 1) * kTS] * small) / (fco[k] + small);
+  // flux and update in one pass; slot k-1 takes its new value once no later
+  // flux reads its old one
+  R after = R(0), vprev = R(0), pend = R(0);
+  for (int k = 0; k < kk; k++) {
+    const R vnext = (k + 1 < kk) ? plm_flux(y, dz, fco, k + 1, kk) : R(0);
+    const R f = y[k * kTS];
+    const R amount = f * fco[k] - (vnext - vprev);
+    const R yn = (amount + f * small) / (fcn[k] + small);
+    after = after + amount;
+    if (k > 0) y[(k - 1) * kTS] = pend;
+    pend = yn;
+    vprev = vnext;
+  }
+  y[(kk - 1) * kTS] = pend;
+  return sizeof(R) == 8 && cabs(bfore - after) > cmax(R(1.e-33), R(1.e-11) * colscl);
+}
+
+template <typename R, int ML>
+__global__ void __launch_bounds__(32 * kWarpsRemap) k_remap_w(Grid<R> g, Strides s, Knobs kn,
+    const StepParams* __restrict__ sp, const R* __restrict__ targt, const R* __restrict__ exsmo,
+    R* __restrict__ us3d, R* __restrict__ vs3d, R* __restrict__ tr3d, R* __restrict__ sdot,
+    R* __restrict__ ex3d, R* __restrict__ dp3d, R* __restrict__ pr3d, int* __restrict__ flags) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int i = blockIdx.x * kWarpsRemap + wib;
+  const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
+  if (i >= N) return;
+  const size_t m = blockIdx.y;
+  sp += m;
+  if (!sp->active) return;
+  RemapSm<R, ML>& S = reinterpret_cast<RemapSm<R, ML>*>(smraw)[wib];
+  exsmo += m * s.intf; us3d += m * s.cell; vs3d += m * s.cell; tr3d += m * s.tr; sdot += m * s.intf;
+  ex3d += m * s.intf; dp3d += m * s.cell; pr3d += m * s.intf;
+  const int its = sp->its;
+  const R cp = R(kCp), rd = R(kRd), p1000 = R(kP1000), small = R(1.e-6);
+  const size_t ci = (size_t)i * L1;
+  for (int k = lane; k <= L; k += 32) {
+    const R eo = ex3d[ci + k], pc = pr3d[ci + k];
+    S.exold[k] = eo;
+    S.prcol[k] = pc;
+    S.exnew[k] = exsmo[ci + k];
+    S.pk1col[k] = eo * pc / cp;
+  }
+  __syncwarp();
+  if (kn.intfc_smooth > 0.) {
+    if (lane == 0) inflate<R>(kn, g.dpsig, L, S.prcol[0], S.exnew);
+    __syncwarp();
+  }
+  if (its > 0) {
+    const R sl = R(kn.slak);
+    for (int k = lane; k <= L; k += 32) S.exnew[k] = sl * S.exnew[k] + (R(1) - sl) * S.exold[k];
+    __syncwarp();
+  }
+  // miglim = 1: exnew(2..nvl) between the neighbouring old interfaces
+  for (int k = 2 + lane; k <= L; k += 32)
+    S.exnew[k - 1] = cmax(R(.0001) * S.exold[k - 1] + R(.9999) * S.exold[k],
+                          cmin(R(.0001) * S.exold[k - 1] + R(.9999) * S.exold[k - 2], S.exnew[k - 1]));
+  __syncwarp();
+  for (int k = lane; k <= L; k += 32) S.prnew[k] = p1000 * pow(S.exnew[k] / cp, cp / rd);
+  __syncwarp();
+  for (int k = lane; k <= L; k += 32) {
+    if (k < L) S.dpcol[k] = S.prnew[k] - S.prnew[k + 1];
+    S.pk1new[k] = S.exnew[k] * S.prnew[k] / cp;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    S.prnew[L] = S.prcol[L];
+    S.pk1new[L] = S.pk1col[L];
+    S.prnew[0] = S.prcol[0];
+    S.pk1new[0] = S.pk1col[0];
+  }
+  __syncwarp();
+  // delz, fco, fcn of both coordinates (pcwise's first two loops)
+  {
+    const bool fp = !(S.prcol[0] < S.prcol[L]), fk = !(S.pk1col[0] < S.pk1col[L]);
+    for (int k = lane; k <= L; k += 32) {
+      S.dz_p[k] = fp ? (-S.prnew[k]) - (-S.prcol[k]) : S.prnew[k] - S.prcol[k];
+      S.dz_k[k] = fk ? (-S.pk1new[k]) - (-S.pk1col[k]) : S.pk1new[k] - S.pk1col[k];
+      if (k < L) {
+        S.fo_p[k] = fp ? cmax(R(0), (-S.prcol[k + 1]) - (-S.prcol[k])) : cmax(R(0), S.prcol[k + 1] - S.prcol[k]);
+        S.fn_p[k] = fp ? cmax(R(0), (-S.prnew[k + 1]) - (-S.prnew[k])) : cmax(R(0), S.prnew[k + 1] - S.prnew[k]);
+        S.fo_k[k] = fk ? cmax(R(0), (-S.pk1col[k + 1]) - (-S.pk1col[k])) : cmax(R(0), S.pk1col[k + 1] - S.pk1col[k]);
+        S.fn_k[k] = fk ? cmax(R(0), (-S.pk1new[k + 1]) - (-S.pk1new[k])) : cmax(R(0), S.pk1new[k + 1] - S.pk1new[k]);
+      }
+    }
+  }
+  __syncwarp();
+  // fields: 0 = u, 1 = v, 2..T = tracers 2..ntra, T+1 = theta
+  const int F = T + 2;
+  bool bad = false;
+  for (int base = 0; base < F; base += 32) {
+    const int nf = (F - base < 32) ? F - base : 32;
+    for (int q = 0; q < nf; q++) {
+      const int f = base + q;
+      const R* col = f == 0 ? us3d + (size_t)i * L : f == 1 ? vs3d + (size_t)i * L
+                   : f <= T ? tr3d + ((size_t)(f - 1) * N + i) * L : tr3d + (size_t)i * L;
+      for (int k = lane; k < L; k += 32) S.tile[k * kTS + q] = col[k];
+    }
+    __syncwarp();
+    if (lane < nf) {
+      const int f = base + lane;
+      R* y = S.tile + lane;
+      if (f <= T) {
+        bad |= pcwise_lane<R>(L, y, S.dz_p, S.fo_p, S.fn_p);
+        if (f >= 2 && kn.thktop == 0.) {
+          for (int k = 3; k <= L; k++) {
+            const R qq = R(1) / (S.dpcol[k - 1] + small);
+            y[(k - 1) * kTS] = (y[(k - 1) * kTS] * S.dpcol[k - 1] + y[(k - 2) * kTS] * small) * qq;
+          }
+        }
+      } else {
+        R colin = R(0), colscl = R(0);
+        if (sizeof(R) == 8) {
+          for (int k = 0; k < L; k++) {
+            colin = colin + y[k * kTS] * (S.pk1col[k] - S.pk1col[k + 1]);
+            colscl = colscl + cabs(y[k * kTS] * (S.pk1col[k] - S.pk1col[k + 1]));
+          }
+        }
+        bad |= pcwise_lane<R>(L, y, S.dz_k, S.fo_k, S.fn_k);
+        for (int k = L; k >= 3; k--) {
+          const R dplo = cmax(S.pk1new[k - 2] - S.pk1new[k - 1], S.pk1new[0] * small);
+          const R dpup = cmax(S.pk1new[k - 1] - S.pk1new[k], S.pk1new[0] * small);
+          const R tha = y[(k - 2) * kTS], thb = y[(k - 1) * kTS];
+          const R devilo = (tha - targt[k - 2]) * dplo;
+          const R deviup = (thb - targt[k - 1]) * dpup;
+          if (deviup > R(0) && devilo < R(0)) {
+            y[(k - 2) * kTS] = tha + cmin(deviup, -devilo) / dplo;
+            y[(k - 1) * kTS] = thb - cmin(deviup, -devilo) / dpup;
+          } else if (deviup < R(0) && devilo > R(0)) {
+            y[(k - 2) * kTS] = tha - cmin(devilo, -deviup) / dplo;
+            y[(k - 1) * kTS] = thb + cmin(devilo, -deviup) / dpup;
+          }
+        }
+        if (sizeof(R) == 8) {
+          R clout = R(0);
+          for (int k = 0; k < L; k++) clout = clout + y[k * kTS] * (S.pk1new[k] - S.pk1new[k + 1]);
+          if (cabs(clout - colin) > cmax(R(1.e-33), R(2.e-6) * colscl)) bad = true;
+        }
+      }
+    }
+    __syncwarp();
+    for (int q = 0; q < nf; q++) {
+      const int f = base + q;
+      R* col = f == 0 ? us3d + (size_t)i * L : f == 1 ? vs3d + (size_t)i * L
+             : f <= T ? tr3d + ((size_t)(f - 1) * N + i) * L : tr3d + (size_t)i * L;
+      for (int k = lane; k < L; k += 32) col[k] = S.tile[k * kTS + q];
+    }
+    __syncwarp();
+  }
+  if (lane == 0)
+    for (int k = 0; k < L; k++)
+      if (S.exnew[k] < S.exnew[k + 1]) S.exnew[k + 1] = S.exnew[k];
+  __syncwarp();
+  for (int k = lane; k <= L; k += 32) {
+    sdot[ci + k] = S.exnew[k] - S.exold[k];
+    ex3d[ci + k] = S.exnew[k];
+    pr3d[ci + k] = S.prnew[k];
+    if (k < L) dp3d[(size_t)i * L + k] = S.dpcol[k];
+  }
+  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flags + m, kFlagColumnIntegral);
+}
+
+template <typename R, int ML>
+size_t remap_w_smem() { return sizeof(RemapSm<R, ML>) * kWarpsRemap; }
+
+template <typename R>
+int prepare_hybgen(int L) {
+  cudaError_t e;
+  if (L <= 64) e = cudaFuncSetAttribute(k_remap_w<R, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)remap_w_smem<R, 64>());
+  else e = cudaFuncSetAttribute(k_remap_w<R, kMaxL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)remap_w_smem<R, kMaxL>());
+  return e == cudaSuccess ? 0 : (int)e;
+}
+
 // ---------------------------------------------------------------- hystat --
 // hystat (hystat.F90:53-109): one warp per column; surface pressure sum and
 // the bottom-up Montgomery potential / geopotential recursion are FP64 warp
@@ -713,7 +962,16 @@ void launch_hybgen(const Launch& l, const Grid<R>& g, const Strides& s, const Kn
     FIM_KEND(l);
     ex_in = w.exsmo2;
   }
-  if (g.L <= 64) {
+  if (kn.remap_optn == 2 && kn.miglim == 1) {
+    dim3 gw(nblocks(g.N, kWarpsRemap), l.members);
+    FIM_KBEGIN(l, "k_remap");
+    if (g.L <= 64)
+      k_remap_w<R, 64><<<gw, 32 * kWarpsRemap, remap_w_smem<R, 64>(), l.stream>>>(
+          g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags);
+    else
+      k_remap_w<R, kMaxL><<<gw, 32 * kWarpsRemap, remap_w_smem<R, kMaxL>(), l.stream>>>(
+          g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags);
+  } else if (g.L <= 64) {
     FIM_KBEGIN(l, "k_remap");
     k_remap<R, 64><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d,
                                                     dp3d, pr3d, l.flags);
@@ -761,6 +1019,7 @@ void launch_prdp_from_ex(const Launch& l, const Grid<R>& g, const Strides& s, co
 }
 
 #define INSTANTIATE(R)                                                                                       \
+  template int prepare_hybgen<R>(int);                                                                       \
   template void launch_hybgen<R>(const Launch&, const Grid<R>&, const Strides&, const Knobs&,               \
                                  const HybgenScratch<R>&, const R*, R*, R*, R*, R*, R*, R*, R*);            \
   template void launch_hystat<R>(const Launch&, const Grid<R>&, const Strides&, R*, const R*, R*, const R*, \

@@ -192,9 +192,9 @@ void launch_trcadv(const Launch&, const Grid<R>&, const Strides&, const TrcadvSc
                    const R* delp);
 // fused tracer path of the step (fim_trc.cu)
 template <typename R>
-struct TrcFusedScratch { R *trcr_lo, *s_plus, *s_mnus, *trold, *r_plus, *r_mnus; int tchunk; };
+struct TrcFusedScratch { R *trcr_lo, *s_plus, *s_mnus, *trold, *r_plus, *r_mnus; int tchunk; int vk; };
 template <typename R>
-void launch_tracer_own(const Launch&, const Grid<R>&, const Strides&, const R* tracr, R* trc_edg);
+void launch_tracer_own(const Launch&, const Grid<R>&, const Strides&, const R* tracr, R* trc_edg, int vk);
 template <typename R>
 void launch_tracers_fused(const Launch&, const Grid<R>&, const Strides&, const TrcFusedScratch<R>&,
                           R* trc_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx,
@@ -211,6 +211,10 @@ void launch_momtum(const Launch&, const Grid<R>&, const Strides&, const Knobs&, 
                    const R* dp3d, const double* mpd = nullptr, const R* tr0 = nullptr);
 template <typename R>
 struct HybgenScratch { R *exsmo, *exsmo2; };
+// one-time launch attributes of the hybgen kernels (shared-memory size);
+// returns a cudaError_t value
+template <typename R>
+int prepare_hybgen(int L);
 template <typename R>
 void launch_hybgen(const Launch&, const Grid<R>&, const Strides&, const Knobs&, const HybgenScratch<R>&,
                    const R* targt, R* us3d, R* vs3d, R* tr3d, R* sdot, R* ex3d, R* dp3d, R* pr3d);

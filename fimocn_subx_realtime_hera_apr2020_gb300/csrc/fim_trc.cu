@@ -14,6 +14,9 @@
 //
 // Every flux is formed from the same operands in the same order as the
 // per-routine kernels, so results are bit-identical to them.
+#include <cstdint>
+#include <initializer_list>
+
 #include "fim_internal.h"
 
 namespace fim {
@@ -25,67 +28,109 @@ template <typename R> __device__ __forceinline__ R tabs(R a) { return a < R(0) ?
 constexpr int kTB = 256;
 inline unsigned tblocks(long long n) { return (unsigned)((n + kTB - 1) / kTB); }
 
-__device__ __forceinline__ bool cl(int N, int L, int& i, int& k) {
-  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= N * L) return false;
-  i = gid / L;
-  k = gid - i * L;
-  return true;
+// VK consecutive levels per thread, moved with one 4/8/16-byte access
+template <typename R, int VK> struct VecOf;
+template <typename R> struct VecOf<R, 1> { using T = R; };
+template <> struct VecOf<float, 2> { using T = float2; };
+template <> struct VecOf<float, 4> { using T = float4; };
+template <> struct VecOf<double, 2> { using T = double2; };
+
+template <int VK, typename R>
+__device__ __forceinline__ void ldv(const R* p, R (&r)[VK]) {
+  if constexpr (VK == 1) {
+    r[0] = *p;
+  } else if constexpr (VK == 2) {
+    const typename VecOf<R, 2>::T t = *reinterpret_cast<const typename VecOf<R, 2>::T*>(p);
+    r[0] = t.x; r[1] = t.y;
+  } else {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    r[0] = t.x; r[1] = t.y; r[2] = t.z; r[3] = t.w;
+  }
 }
 
+template <int VK, typename R>
+__device__ __forceinline__ void stv(R* p, const R (&r)[VK]) {
+  if constexpr (VK == 1) {
+    *p = r[0];
+  } else if constexpr (VK == 2) {
+    typename VecOf<R, 2>::T t; t.x = r[0]; t.y = r[1];
+    *reinterpret_cast<typename VecOf<R, 2>::T*>(p) = t;
+  } else {
+    float4 t; t.x = r[0]; t.y = r[1]; t.z = r[2]; t.w = r[3];
+    *reinterpret_cast<float4*>(p) = t;
+  }
+}
+
+#define FOR_V _Pragma("unroll") for (int j = 0; j < VK; j++)
+
 // own-side least-squares edge values of tracers 1..T-1 (0-based), z = tracer
-template <typename R>
+template <typename R, int VK>
 __global__ void __launch_bounds__(kTB) k_tr_own(Grid<R> g, Strides s, const R* __restrict__ tracr,
                                                 R* __restrict__ trc_edg) {
-  int i, k;
-  if (!cl(g.N, g.L, i, k)) return;
-  const int L = g.L, N = g.N;
+  const int L = g.L, N = g.N, LV = L / VK;
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= N * LV) return;
+  const int i = gid / LV, k = (gid - i * LV) * VK;
   const size_t m = blockIdx.y;
   const int t = blockIdx.z + 1;
   const R* src = tracr + m * s.tr + (size_t)t * N * L;
   R* dst = trc_edg + m * s.tredg + (size_t)t * N * 6 * L;
   const int np = g.nprox[i];
   const int* pr = g.prox + i * 6;
-  const R bc = src[(size_t)i * L + k];
-  R d[6];
+  R bc[VK];
+  ldv<VK>(src + i * L + k, bc);
+  R d[6][VK];
 #pragma unroll
-  for (int j = 0; j < 6; j++) d[j] = (j < np) ? src[(size_t)pr[j] * L + k] - bc : R(0);
+  for (int e = 0; e < 6; e++) {
+    if (e < np) {
+      ldv<VK>(src + pr[e] * L + k, d[e]);
+      FOR_V d[e][j] = d[e][j] - bc[j];
+    } else {
+      FOR_V d[e][j] = R(0);
+    }
+  }
   const R* hf = g.hfcoef + (size_t)i * 36;
 #pragma unroll
   for (int ie = 0; ie < 6; ie++) {
-    R val = R(0);
+    R val[VK];
+    FOR_V val[j] = R(0);
     if (ie < np) {
-      val = bc;
+      FOR_V val[j] = bc[j];
 #pragma unroll
-      for (int j = 0; j < 6; j++)
-        if (j < np) val = val + d[j] * hf[ie * 6 + j];
+      for (int e = 0; e < 6; e++)
+        if (e < np) {
+          const R h = hf[ie * 6 + e];
+          FOR_V val[j] = val[j] + d[e][j] * h;
+        }
     }
-    dst[((size_t)i * 6 + ie) * L + k] = val;
+    stv<VK>(dst + (i * 6 + ie) * L + k, val);
   }
 }
 
-// One thread per (level, cell, tracer).  The tracer is the fastest-varying
+// One thread per (VK levels, cell, tracer).  The tracer is the fastest-varying
 // part of the block index, so the blocks of one cell range and all tracers of
 // a chunk run back to back and the mass fluxes they share are L2 hits.
+template <int VK>
 __device__ __forceinline__ bool clt(int N, int L, int nt, int& i, int& k, int& tz) {
   tz = blockIdx.x % nt;
   const int cb = blockIdx.x / nt;
+  const int LV = L / VK;
   const int gid = cb * blockDim.x + threadIdx.x;
-  if (gid >= N * L) return false;
-  i = gid / L;
-  k = gid - i * L;
+  if (gid >= N * LV) return false;
+  i = gid / LV;
+  k = (gid - i * LV) * VK;
   return true;
 }
 
 // trcadv1 + the S+/S- sums of trcadv2 + copy of the old tracer
-template <typename R>
+template <typename R, int VK>
 __global__ void __launch_bounds__(kTB) k_tr_lo(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     int t0, int nt, const R* __restrict__ massfx, const R* __restrict__ trc_edg, const R* __restrict__ tracr,
     const R* __restrict__ trcdp, R* __restrict__ trl_tdcy, const R* __restrict__ delp,
     R* __restrict__ trcr_lo, R* __restrict__ s_plus, R* __restrict__ s_mnus, R* __restrict__ trold,
     size_t sc) {
   int i, k, tz;
-  if (!clt(g.N, g.L, nt, i, k, tz)) return;
+  if (!clt<VK>(g.N, g.L, nt, i, k, tz)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
   sp += m;
@@ -103,49 +148,66 @@ __global__ void __launch_bounds__(kTB) k_tr_lo(Grid<R> g, Strides s, const StepP
   const int np = g.nprox[i];
   const int* pr = g.prox + i * 6;
   const int* ps = g.proxs + i * 6;
-  const R tri = tr[c];
-  R sumlo = R(0), sp_ = R(0), sm_ = R(0), mx = tri, mn = tri;
+  R tri[VK], sumlo[VK], sp_[VK], sm_[VK], mx[VK], mn[VK];
+  ldv<VK>(tr + c, tri);
+  FOR_V { sumlo[j] = R(0); sp_[j] = R(0); sm_[j] = R(0); mx[j] = tri[j]; mn[j] = tri[j]; }
 #pragma unroll
   for (int e = 0; e < 6; e++) {
     const int ipx = pr[e];
-    const R trx = tr[ipx * L + k];
-    mx = tmax(mx, trx);
-    mn = tmin(mn, trx);
+    R trx[VK];
+    ldv<VK>(tr + ipx * L + k, trx);
+    FOR_V { mx[j] = tmax(mx[j], trx[j]); mn[j] = tmin(mn[j], trx[j]); }
     if (e < np) {
       const int own = (i * 6 + e) * L + k, mir = (ipx * 6 + ps[e]) * L + k;
-      const R mf = mfn[own], mfx = mfn[mir];
-      const R tev = (t == 0) ? te[own] : half * (te[own] + te[mir]);
-      const R hi = mf * tev;
-      const R lo = half * ((mf + tabs(mf)) * tri - (mfx + tabs(mfx)) * trx);
-      const R anti = hi - lo;
-      sumlo = sumlo + lo;
-      sp_ = sp_ - tmin(R(0), anti);
-      sm_ = sm_ + tmax(R(0), anti);
+      R mf[VK], mfx[VK], tev[VK];
+      ldv<VK>(mfn + own, mf);
+      ldv<VK>(mfn + mir, mfx);
+      ldv<VK>(te + own, tev);
+      if (t != 0) {
+        R tem[VK];
+        ldv<VK>(te + mir, tem);
+        FOR_V tev[j] = half * (tev[j] + tem[j]);
+      }
+      FOR_V {
+        const R hi = mf[j] * tev[j];
+        const R lo = half * ((mf[j] + tabs(mf[j])) * tri[j] - (mfx[j] + tabs(mfx[j])) * trx[j]);
+        const R anti = hi - lo;
+        sumlo[j] = sumlo[j] + lo;
+        sp_[j] = sp_[j] - tmin(R(0), anti);
+        sm_[j] = sm_[j] + tmax(R(0), anti);
+      }
     }
   }
-  const R tn = -sumlo * g.rarea[i];
-  tl[(size_t)nf * NL + c] = tn;
-  const R lo = trcdp[m * s.tr + (size_t)t * NL + c] + ab1 * tn + ab2 * tl[(size_t)of * NL + c] +
-               ab3 * tl[(size_t)vof * NL + c];
-  mx = tmax(R(0), mx);
-  mn = tmax(R(0), mn);
+  const R rar = g.rarea[i];
+  R tn[VK], tlo[VK], tlv[VK], td[VK], dp[VK], out[VK];
+  FOR_V tn[j] = -sumlo[j] * rar;
+  stv<VK>(tl + (size_t)nf * NL + c, tn);
+  ldv<VK>(tl + (size_t)of * NL + c, tlo);
+  ldv<VK>(tl + (size_t)vof * NL + c, tlv);
+  ldv<VK>(trcdp + m * s.tr + (size_t)t * NL + c, td);
+  ldv<VK>(delp + m * s.cell + c, dp);
   const size_t q = (m * nt + tz) * sc + c;
-  trcr_lo[q] = tmax(mn, tmin(mx, lo / tmax(thshld, delp[m * s.cell + c])));
-  s_plus[q] = sp_;
-  s_mnus[q] = sm_;
-  trold[q] = tri;
+  FOR_V {
+    const R lo = td[j] + ab1 * tn[j] + ab2 * tlo[j] + ab3 * tlv[j];
+    const R hx = tmax(R(0), mx[j]), hn = tmax(R(0), mn[j]);
+    out[j] = tmax(hn, tmin(hx, lo / tmax(thshld, dp[j])));
+  }
+  stv<VK>(trcr_lo + q, out);
+  stv<VK>(s_plus + q, sp_);
+  stv<VK>(s_mnus + q, sm_);
+  stv<VK>(trold + q, tri);
 }
 
 // trcadv2: Q+/Q- and the limiters R+/R-; the relaxed bounds are
 // max/min over the 1-ring of the old tracer and of trcr_lo (exact operations,
 // so any association gives the reference's values).
-template <typename R>
+template <typename R, int VK>
 __global__ void __launch_bounds__(kTB) k_tr_lim(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     int t0, int nt, const R* __restrict__ trc_tdcy, const R* __restrict__ delp, const R* __restrict__ trold,
     const R* __restrict__ trcr_lo, const R* __restrict__ s_plus, const R* __restrict__ s_mnus,
     R* __restrict__ r_plus, R* __restrict__ r_mnus, size_t sc) {
   int i, k, tz;
-  if (!clt(g.N, g.L, nt, i, k, tz)) return;
+  if (!clt<VK>(g.N, g.L, nt, i, k, tz)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
   sp += m;
@@ -160,35 +222,46 @@ __global__ void __launch_bounds__(kTB) k_tr_lim(Grid<R> g, Strides s, const Step
   const R* to = trold + so;
   const R* lo = trcr_lo + so;
   const int* pr = g.prox + i * 6;
-  const R lc = lo[c];
-  R mx = tmax(to[c], lc), mn = tmin(to[c], lc);
+  R lc[VK], tc0[VK], mx[VK], mn[VK];
+  ldv<VK>(lo + c, lc);
+  ldv<VK>(to + c, tc0);
+  FOR_V { mx[j] = tmax(tc0[j], lc[j]); mn[j] = tmin(tc0[j], lc[j]); }
 #pragma unroll
   for (int e = 0; e < 6; e++) {
     const int cx = pr[e] * L + k;
-    const R a = to[cx], b = lo[cx];
-    mx = tmax(mx, tmax(a, b));
-    mn = tmin(mn, tmin(a, b));
+    R a[VK], b[VK];
+    ldv<VK>(to + cx, a);
+    ldv<VK>(lo + cx, b);
+    FOR_V { mx[j] = tmax(mx[j], tmax(a[j], b[j])); mn[j] = tmin(mn[j], tmin(a[j], b[j])); }
   }
-  mx = tmax(R(0), mx);
-  mn = tmax(R(0), mn);
   const R* tc = trc_tdcy + m * s.trab + (size_t)t * 3 * NL;
-  const R tof = tc[(size_t)of * NL + c], tvf = tc[(size_t)vof * NL + c];
-  const R dp = delp[m * s.cell + c], ar = g.area[i];
-  const R q_plus = ((mx - lc) * dp - (ab2 * tmin(R(0), tof) + ab3 * tmax(R(0), tvf))) / ab1 * ar;
-  const R q_mnus = ((lc - mn) * dp + (ab2 * tmax(R(0), tof) + ab3 * tmin(R(0), tvf))) / ab1 * ar;
-  r_plus[so + c] = tmax(R(0), tmin(R(1), q_plus / tmax(s_plus[so + c], thshld)));
-  r_mnus[so + c] = tmax(R(0), tmin(R(1), q_mnus / tmax(s_mnus[so + c], thshld)));
+  R tof[VK], tvf[VK], dp[VK], spl[VK], smn[VK], rp[VK], rm[VK];
+  ldv<VK>(tc + (size_t)of * NL + c, tof);
+  ldv<VK>(tc + (size_t)vof * NL + c, tvf);
+  ldv<VK>(delp + m * s.cell + c, dp);
+  ldv<VK>(s_plus + so + c, spl);
+  ldv<VK>(s_mnus + so + c, smn);
+  const R ar = g.area[i];
+  FOR_V {
+    const R hx = tmax(R(0), mx[j]), hn = tmax(R(0), mn[j]);
+    const R q_plus = ((hx - lc[j]) * dp[j] - (ab2 * tmin(R(0), tof[j]) + ab3 * tmax(R(0), tvf[j]))) / ab1 * ar;
+    const R q_mnus = ((lc[j] - hn) * dp[j] + (ab2 * tmax(R(0), tof[j]) + ab3 * tmin(R(0), tvf[j]))) / ab1 * ar;
+    rp[j] = tmax(R(0), tmin(R(1), q_plus / tmax(spl[j], thshld)));
+    rm[j] = tmax(R(0), tmin(R(1), q_mnus / tmax(smn[j], thshld)));
+  }
+  stv<VK>(r_plus + so + c, rp);
+  stv<VK>(r_mnus + so + c, rm);
 }
 
 // trcadv3: clip the recomputed antidiffusive fluxes, AB3 update, new tracer
-template <typename R>
+template <typename R, int VK>
 __global__ void __launch_bounds__(kTB) k_tr_hi(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     int t0, int nt, const R* __restrict__ massfx, const R* __restrict__ trc_edg, R* __restrict__ tracr,
     R* __restrict__ trcdp, R* __restrict__ trc_tdcy, const R* __restrict__ trl_tdcy, const R* __restrict__ delp,
     const R* __restrict__ trold, const R* __restrict__ trcr_lo, const R* __restrict__ r_plus,
     const R* __restrict__ r_mnus, size_t sc) {
   int i, k, tz;
-  if (!clt(g.N, g.L, nt, i, k, tz)) return;
+  if (!clt<VK>(g.N, g.L, nt, i, k, tz)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
   sp += m;
@@ -209,75 +282,136 @@ __global__ void __launch_bounds__(kTB) k_tr_hi(Grid<R> g, Strides s, const StepP
   const int np = g.nprox[i];
   const int* pr = g.prox + i * 6;
   const int* ps = g.proxs + i * 6;
-  const R tri = to[c], rpc = rp[c], rmc = rm[c], lc = lo[c];
-  R at = R(0), mx = tmax(tri, lc), mn = tmin(tri, lc);
+  R tri[VK], rpc[VK], rmc[VK], lc[VK], at[VK], mx[VK], mn[VK];
+  ldv<VK>(to + c, tri);
+  ldv<VK>(rp + c, rpc);
+  ldv<VK>(rm + c, rmc);
+  ldv<VK>(lo + c, lc);
+  FOR_V { at[j] = R(0); mx[j] = tmax(tri[j], lc[j]); mn[j] = tmin(tri[j], lc[j]); }
 #pragma unroll
   for (int e = 0; e < 6; e++) {
     const int ipx = pr[e];
     const int cx = ipx * L + k;
-    const R trx = to[cx], lox = lo[cx];
-    mx = tmax(mx, tmax(trx, lox));
-    mn = tmin(mn, tmin(trx, lox));
+    R trx[VK], lox[VK];
+    ldv<VK>(to + cx, trx);
+    ldv<VK>(lo + cx, lox);
+    FOR_V { mx[j] = tmax(mx[j], tmax(trx[j], lox[j])); mn[j] = tmin(mn[j], tmin(trx[j], lox[j])); }
     if (e < np) {
       const int own = (i * 6 + e) * L + k, mir = (ipx * 6 + ps[e]) * L + k;
-      const R mf = mfn[own], mfx = mfn[mir];
-      const R tev = (t == 0) ? te[own] : half * (te[own] + te[mir]);
-      const R hi = mf * tev;
-      const R lo_ = half * ((mf + tabs(mf)) * tri - (mfx + tabs(mfx)) * trx);
-      R a = hi - lo_;
-      if (a >= R(0)) a = a * tmin(rmc, rp[cx]);
-      else a = a * tmin(rpc, rm[cx]);
-      at = at + a;
+      R mf[VK], mfx[VK], tev[VK], rpx[VK], rmx[VK];
+      ldv<VK>(mfn + own, mf);
+      ldv<VK>(mfn + mir, mfx);
+      ldv<VK>(te + own, tev);
+      if (t != 0) {
+        R tem[VK];
+        ldv<VK>(te + mir, tem);
+        FOR_V tev[j] = half * (tev[j] + tem[j]);
+      }
+      ldv<VK>(rp + cx, rpx);
+      ldv<VK>(rm + cx, rmx);
+      FOR_V {
+        const R hi = mf[j] * tev[j];
+        const R lo_ = half * ((mf[j] + tabs(mf[j])) * tri[j] - (mfx[j] + tabs(mfx[j])) * trx[j]);
+        R a = hi - lo_;
+        if (a >= R(0)) a = a * tmin(rmc[j], rpx[j]);
+        else a = a * tmin(rpc[j], rmx[j]);
+        at[j] = at[j] + a;
+      }
     }
   }
-  mx = tmax(R(0), mx);
-  mn = tmax(R(0), mn);
-  at = -at * g.rarea[i];
+  const R rar = g.rarea[i];
   R* tc = trc_tdcy + m * s.trab + (size_t)t * 3 * NL;
-  const R tn = trl_tdcy[m * s.trab + (size_t)t * 3 * NL + (size_t)nf * NL + c] + at;
-  tc[(size_t)nf * NL + c] = tn;
   R* td = trcdp + m * s.tr + (size_t)t * NL;
-  const R tdn = td[c] + ab1 * tn + ab2 * tc[(size_t)of * NL + c] + ab3 * tc[(size_t)vof * NL + c];
-  td[c] = tdn;
-  tracr[m * s.tr + (size_t)t * NL + c] = tmax(mn, tmin(mx, tdn / tmax(thshld, delp[m * s.cell + c])));
+  R tl[VK], tof[VK], tvf[VK], tdv[VK], dp[VK], tn[VK], out[VK];
+  ldv<VK>(trl_tdcy + m * s.trab + (size_t)t * 3 * NL + (size_t)nf * NL + c, tl);
+  FOR_V tn[j] = tl[j] + (-at[j] * rar);
+  stv<VK>(tc + (size_t)nf * NL + c, tn);
+  ldv<VK>(tc + (size_t)of * NL + c, tof);
+  ldv<VK>(tc + (size_t)vof * NL + c, tvf);
+  ldv<VK>(td + c, tdv);
+  ldv<VK>(delp + m * s.cell + c, dp);
+  FOR_V {
+    tdv[j] = tdv[j] + ab1 * tn[j] + ab2 * tof[j] + ab3 * tvf[j];
+    const R hx = tmax(R(0), mx[j]), hn = tmax(R(0), mn[j]);
+    out[j] = tmax(hn, tmin(hx, tdv[j] / tmax(thshld, dp[j])));
+  }
+  stv<VK>(td + c, tdv);
+  stv<VK>(tracr + m * s.tr + (size_t)t * NL + c, out);
+}
+
+#undef FOR_V
+
+template <typename R, int VK>
+void tracers_fused_vk(const Launch& l, const Grid<R>& g, const Strides& s, const TrcFusedScratch<R>& w,
+                      R* trc_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx, const R* delp) {
+  const size_t sc = (size_t)g.N * g.L;
+  for (int t0 = 0; t0 < g.T; t0 += w.tchunk) {
+    const int nt = (g.T - t0 < w.tchunk) ? g.T - t0 : w.tchunk;
+    dim3 grid(tblocks((long long)g.N * (g.L / VK)) * nt, l.members);
+    FIM_KBEGIN(l, "k_tr_lo");
+    k_tr_lo<R, VK><<<grid, kTB, 0, l.stream>>>(g, s, l.sp, t0, nt, massfx, trc_edg, tracr, trcdp, trl_tdcy, delp,
+                                                w.trcr_lo, w.s_plus, w.s_mnus, w.trold, sc);
+    FIM_KEND(l);
+    FIM_KBEGIN(l, "k_tr_lim");
+    k_tr_lim<R, VK><<<grid, kTB, 0, l.stream>>>(g, s, l.sp, t0, nt, trc_tdcy, delp, w.trold, w.trcr_lo,
+                                                 w.s_plus, w.s_mnus, w.r_plus, w.r_mnus, sc);
+    FIM_KEND(l);
+    FIM_KBEGIN(l, "k_tr_hi");
+    k_tr_hi<R, VK><<<grid, kTB, 0, l.stream>>>(g, s, l.sp, t0, nt, massfx, trc_edg, tracr, trcdp, trc_tdcy,
+                                                trl_tdcy, delp, w.trold, w.trcr_lo, w.r_plus, w.r_mnus, sc);
+    FIM_KEND(l);
+  }
+}
+
+// Levels per thread: 16-byte accesses where nvl allows; every array offset
+// is then a multiple of VK elements, and every base is a cudaMalloc'd field
+// (256-byte aligned), checked here.
+template <typename R>
+int tracer_vk(const Grid<R>& g, std::initializer_list<const void*> ptrs, int want) {
+  int vk = want > 0 ? want : (int)(16 / sizeof(R));
+  if ((int)sizeof(R) * vk > 16) vk = (int)(16 / sizeof(R));
+  while (vk > 1 && g.L % vk != 0) vk /= 2;
+  for (const void* p : ptrs)
+    while (vk > 1 && ((uintptr_t)p % (vk * sizeof(R))) != 0) vk /= 2;
+  return vk;
 }
 
 template <typename R>
 void launch_tracers_fused(const Launch& l, const Grid<R>& g, const Strides& s, const TrcFusedScratch<R>& w,
                           R* trc_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx,
                           const R* delp) {
-  const size_t sc = (size_t)g.N * g.L;
-  for (int t0 = 0; t0 < g.T; t0 += w.tchunk) {
-    const int nt = (g.T - t0 < w.tchunk) ? g.T - t0 : w.tchunk;
-    dim3 grid(tblocks((long long)g.N * g.L) * nt, l.members);
-    FIM_KBEGIN(l, "k_tr_lo");
-    k_tr_lo<R><<<grid, kTB, 0, l.stream>>>(g, s, l.sp, t0, nt, massfx, trc_edg, tracr, trcdp, trl_tdcy, delp,
-                                            w.trcr_lo, w.s_plus, w.s_mnus, w.trold, sc);
-    FIM_KEND(l);
-    FIM_KBEGIN(l, "k_tr_lim");
-    k_tr_lim<R><<<grid, kTB, 0, l.stream>>>(g, s, l.sp, t0, nt, trc_tdcy, delp, w.trold, w.trcr_lo, w.s_plus,
-                                             w.s_mnus, w.r_plus, w.r_mnus, sc);
-    FIM_KEND(l);
-    FIM_KBEGIN(l, "k_tr_hi");
-    k_tr_hi<R><<<grid, kTB, 0, l.stream>>>(g, s, l.sp, t0, nt, massfx, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy,
-                                            delp, w.trold, w.trcr_lo, w.r_plus, w.r_mnus, sc);
-    FIM_KEND(l);
-  }
+  const int vk = tracer_vk(g, {trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp, w.trcr_lo, w.s_plus,
+                               w.s_mnus, w.trold, w.r_plus, w.r_mnus}, w.vk);
+  if (vk == 4)
+    tracers_fused_vk<R, (sizeof(R) == 4 ? 4 : 2)>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx,
+                                                  delp);
+  else if (vk == 2)
+    tracers_fused_vk<R, 2>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp);
+  else
+    tracers_fused_vk<R, 1>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp);
+}
+
+template <typename R, int VK>
+void tracer_own_vk(const Launch& l, const Grid<R>& g, const Strides& s, const R* tracr, R* trc_edg) {
+  dim3 grid(tblocks((long long)g.N * (g.L / VK)), l.members, g.T - 1);
+  FIM_KBEGIN(l, "k_tr_own");
+  k_tr_own<R, VK><<<grid, kTB, 0, l.stream>>>(g, s, tracr, trc_edg);
+  FIM_KEND(l);
 }
 
 template <typename R>
-void launch_tracer_own(const Launch& l, const Grid<R>& g, const Strides& s, const R* tracr, R* trc_edg) {
+void launch_tracer_own(const Launch& l, const Grid<R>& g, const Strides& s, const R* tracr, R* trc_edg, int want) {
   if (g.T < 2) return;
-  dim3 grid(tblocks((long long)g.N * g.L), l.members, g.T - 1);
-  FIM_KBEGIN(l, "k_tr_own");
-  k_tr_own<R><<<grid, kTB, 0, l.stream>>>(g, s, tracr, trc_edg);
-  FIM_KEND(l);
+  const int vk = tracer_vk(g, {tracr, trc_edg}, want);
+  if (vk == 4) tracer_own_vk<R, (sizeof(R) == 4 ? 4 : 2)>(l, g, s, tracr, trc_edg);
+  else if (vk == 2) tracer_own_vk<R, 2>(l, g, s, tracr, trc_edg);
+  else tracer_own_vk<R, 1>(l, g, s, tracr, trc_edg);
 }
 
 #define INSTANTIATE(R)                                                                                        \
   template void launch_tracers_fused<R>(const Launch&, const Grid<R>&, const Strides&,                       \
                                         const TrcFusedScratch<R>&, R*, R*, R*, R*, R*, const R*, const R*);  \
-  template void launch_tracer_own<R>(const Launch&, const Grid<R>&, const Strides&, const R*, R*);
+  template void launch_tracer_own<R>(const Launch&, const Grid<R>&, const Strides&, const R*, R*, int);
 INSTANTIATE(float)
 INSTANTIATE(double)
 
