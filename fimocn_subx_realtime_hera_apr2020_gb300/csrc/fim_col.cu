@@ -8,6 +8,8 @@
 // globsum accumulates per thread (FP64, or float-float compensated sums in the
 // FP32 build, whose error is that of an FP64 sum) and reduces per block into a
 // deterministic partial buffer.
+#include <cstdint>
+
 #include "fim_internal.h"
 
 namespace fim {
@@ -115,7 +117,7 @@ __device__ void inflate(const Knobs& kn, const R* dpsig, int L, R psurf, R* exne
       exner[k] = exner[k - 1] - dp0;
     } else {
       if (k > last) {
-        dp0 = dp0 / cmin(R(10), R(1.25) * R(ldexp(1.0, k - last)));
+        dp0 = dp0 / cmin(R(10), R(1.25) * ldexp(R(1), k - last));
         dp0 = cmax(dp0, rd * R(100) / p1000);
       }
       const R dp1 = cushn(cmax(R(0), exner[k - 1] - cmin(exold, exner[0] - dpsum)), dp0);
@@ -483,20 +485,36 @@ __global__ void __launch_bounds__(kColBlock) k_remap(Grid<R> g, Strides s, Knobs
 
 // ------------------------------------------------- remap, warp per column --
 // remap_1d for the default knobs (PLM, remap_optn = 2; one-layer migration,
-// miglim = 1) with one warp per column and one lane per remapped field (u, v,
-// tracers 2..ntra in pressure, theta in p^(kappa+1)).  The column's fields sit
-// in a shared-memory tile, lane = field, loaded and stored coalesced along the
-// levels; each lane runs pcwise's recurrences on its own tile column, where
-// the thread-per-column kernel keeps ~30 column arrays per thread in local
-// memory.  Operations and their order per field are those of pcwise above.
+// miglim = 1).
+//  k_inflate: inflate, the one serial recursion of the column set-up, lane =
+//             column over 32 columns per warp staged in shared memory;
+//  k_remap_w: one warp per column: lanes over levels build the new interfaces
+//             and the remap geometry, then lane = field (u, v, tracers
+//             2..ntra in pressure, theta in p^(kappa+1)) runs pcwise's
+//             recurrences on its column of a shared-memory tile that is
+//             loaded and stored coalesced.
+// With one-layer migration the donor layer, slab width and dx of every
+// interface depend on the coordinate only, so they are formed once per column
+// and each field's flux pass is branch-free; all fields run one instruction
+// stream (theta differs only in the geometry it reads).  Divisions by the
+// coordinate thicknesses (fco + small, fcn + small) become products with
+// reciprocals formed once per column: results differ from pcwise above by
+// rounding.
 constexpr int kTS = 33;   // tile row stride (32 fields + 1: conflict-free transposes)
 constexpr int kWarpsRemap = 4;
+constexpr int kWarpsInflate = 4;
+
+template <typename R, int ML>
+struct RemapGeo {          // one coordinate (pressure or p^(kappa+1))
+  R fo[ML], rfo[ML], rfn[ML];    // fco, 1/(fco+small), 1/(fcn+small)
+  R hx[ML + 1], dsl[ML + 1], nd[ML + 1];  // interface k: (dx-1) or (1-dx), slab width, -delz
+  int ly[ML + 1];                // donor layer of interface k
+};
 
 template <typename R, int ML>
 struct RemapSm {
-  R tile[ML * kTS];
-  R dz_p[ML + 1], fo_p[ML], fn_p[ML];   // delz, fco, fcn in pressure
-  R dz_k[ML + 1], fo_k[ML], fn_k[ML];   // the same in p^(kappa+1)
+  R tile[ML * kTS];              // field values, lane = field
+  RemapGeo<R, ML> gp, gk;
   R exold[ML + 1], exnew[ML + 1], prcol[ML + 1], prnew[ML + 1], pk1col[ML + 1], pk1new[ML + 1];
   R dpcol[ML];
 };
@@ -506,63 +524,86 @@ template <typename R>
 __device__ __forceinline__ R plm_b(const R* y, int lyr, int kk) {
   if (lyr < 1 || lyr > kk - 2) return R(0);
   const R f = y[lyr * kTS], fm = y[(lyr - 1) * kTS], fp = y[(lyr + 1) * kTS];
-  if (f <= cmin(fm, fp) || f >= cmax(fm, fp)) return R(0);
-  if ((fp - fm) * (fm + fp - R(2) * f) > R(0)) return f - fm;
-  return fp - f;
+  const R d1 = f - fm, d2 = fp - f;
+  const R b = ((fp - fm) * (fm + fp - R(2) * f) > R(0)) ? d1 : d2;
+  return (f <= cmin(fm, fp) || f >= cmax(fm, fp)) ? R(0) : b;
 }
 
-// vertfx(k), 1 <= k <= kk-1, of pcwise with miglim = 1 and PLM coefficients
-template <typename R>
-__device__ __forceinline__ R plm_flux(const R* y, const R* dz, const R* fco, int k, int kk) {
-  const R athird = R(1) / R(3);
-  R slab = R(0), amount = R(0);
-  const R d = dz[k];
-  if (d > R(0)) {
-    const int lyr = k;
-    if (fco[lyr] > R(0)) {
-      const R a = y[lyr * kTS], b = plm_b(y, lyr, kk), cc = R(0);
-      const R dslab = cmin(slab + fco[lyr], d) - cmin(slab, d);
-      const R dx = dslab / fco[lyr];
-      const R fcdx = a + b * R(.5) * (dx - R(1)) + cc * (R(.25) - dx * (R(.5) - dx * athird));
-      amount = amount + fcdx * dslab;
-      slab = slab + dslab;
-    }
-  } else if (d < R(0)) {
-    const int lyr = k - 1;
-    if (fco[lyr] > R(0)) {
-      const R a = y[lyr * kTS], b = plm_b(y, lyr, kk), cc = R(0);
-      const R dslab = cmin(slab + fco[lyr], -d) - cmin(slab, -d);
-      const R dx = dslab / fco[lyr];
-      const R fcdx = a + b * R(.5) * (R(1) - dx) + cc * (R(.25) - dx * (R(.5) - dx * athird));
-      amount = amount + fcdx * dslab;
-      slab = slab + dslab;
-    }
+// pcwise's coordinate quantities for xold -> xnew, lanes over levels
+template <typename R, int ML>
+__device__ void remap_geo(int L, int lane, const R* xold, const R* xnew, RemapGeo<R, ML>& G) {
+  const R small = R(1.e-22);
+  const bool flip = !(xold[0] < xold[L]);
+  for (int k = lane; k < L; k += 32) {
+    const R fo = flip ? cmax(R(0), (-xold[k + 1]) - (-xold[k])) : cmax(R(0), xold[k + 1] - xold[k]);
+    const R fn = flip ? cmax(R(0), (-xnew[k + 1]) - (-xnew[k])) : cmax(R(0), xnew[k + 1] - xnew[k]);
+    G.fo[k] = fo;
+    G.rfo[k] = R(1) / (fo + small);
+    G.rfn[k] = R(1) / (fn + small);
   }
-  return slab != R(0) ? -d * amount / slab : R(0);
+  __syncwarp();
+  for (int k = lane; k <= L; k += 32) {
+    const R d = flip ? (-xnew[k]) - (-xold[k]) : xnew[k] - xold[k];
+    int lyr = 0;
+    R hx = R(0), dsl = R(0);
+    if (k >= 1 && k <= L - 1 && d != R(0)) {
+      lyr = d > R(0) ? k : k - 1;
+      const R fl = G.fo[lyr];
+      if (fl > R(0)) {
+        const R dd = d > R(0) ? d : -d;
+        dsl = cmin(R(0) + fl, dd) - cmin(R(0), dd);
+        const R dx = dsl / fl;
+        hx = d > R(0) ? dx - R(1) : R(1) - dx;
+      }
+    }
+    G.ly[k] = lyr;
+    G.hx[k] = hx;
+    G.dsl[k] = dsl;
+    G.nd[k] = -d;
+  }
+}
+
+// vertfx(k) of one field; 0 where no mass crosses interface k
+template <typename R, int ML>
+__device__ __forceinline__ R lane_flux(const R* y, const RemapGeo<R, ML>& G, int k, int kk) {
+  const R dsl = G.dsl[k];
+  const int lyr = G.ly[k];
+  const R a = y[lyr * kTS], b = plm_b(y, lyr, kk);
+  const R fcdx = a + b * R(.5) * G.hx[k];
+  const R amount = fcdx * dsl;
+  return dsl != R(0) ? G.nd[k] * amount / dsl : R(0);
 }
 
 // pcwise (PLM, miglim = 1) in place on one lane's tile column y (stride kTS).
 // Returns true when the column-integral check fails (FP64 build only).
-template <typename R>
-__device__ bool pcwise_lane(int kk, R* y, const R* dz, const R* fco, const R* fcn) {
+template <typename R, int ML>
+__device__ bool pcwise_lane(int kk, R* y, const RemapGeo<R, ML>& G) {
   const R small = R(1.e-22);
   R bfore = R(0), colscl = R(0);
   if (sizeof(R) == 8) {
     for (int k = 0; k < kk; k++) {
-      bfore = bfore + y[k * kTS] * fco[k];
-      colscl = colscl + cabs(y[k * kTS] * fco[k]);
+      bfore = bfore + y[k * kTS] * G.fo[k];
+      colscl = colscl + cabs(y[k * kTS] * G.fo[k]);
     }
   }
-  for (int k = kk - 2; k >= 0; k--) y[k * kTS] = (y[k * kTS] * fco[k] + y[(k + 1) * kTS] * small) / (fco[k] + small);
-  for (int k = 1; k < kk; k++) y[k * kTS] = (y[k * kTS] * fco[k] + y[(k - 1) * kTS] * small) / (fco[k] + small);
+  R nb = y[(kk - 1) * kTS];
+  for (int k = kk - 2; k >= 0; k--) {
+    nb = (y[k * kTS] * G.fo[k] + nb * small) * G.rfo[k];
+    y[k * kTS] = nb;
+  }
+  nb = y[0];
+  for (int k = 1; k < kk; k++) {
+    nb = (y[k * kTS] * G.fo[k] + nb * small) * G.rfo[k];
+    y[k * kTS] = nb;
+  }
   // flux and update in one pass; slot k-1 takes its new value once no later
   // flux reads its old one
   R after = R(0), vprev = R(0), pend = R(0);
   for (int k = 0; k < kk; k++) {
-    const R vnext = (k + 1 < kk) ? plm_flux(y, dz, fco, k + 1, kk) : R(0);
+    const R vnext = (k + 1 < kk) ? lane_flux<R, ML>(y, G, k + 1, kk) : R(0);
     const R f = y[k * kTS];
-    const R amount = f * fco[k] - (vnext - vprev);
-    const R yn = (amount + f * small) / (fcn[k] + small);
+    const R amount = f * G.fo[k] - (vnext - vprev);
+    const R yn = (amount + f * small) * G.rfn[k];
     after = after + amount;
     if (k > 0) y[(k - 1) * kTS] = pend;
     pend = yn;
@@ -572,6 +613,27 @@ __device__ bool pcwise_lane(int kk, R* y, const R* dz, const R* fco, const R* fc
   return sizeof(R) == 8 && cabs(bfore - after) > cmax(R(1.e-33), R(1.e-11) * colscl);
 }
 
+// inflate (hybgen.F90:893-1007) of 32 columns per warp, lane = column
+template <typename R, int ML>
+__global__ void __launch_bounds__(32 * kWarpsInflate) k_inflate(Grid<R> g, Strides s, Knobs kn,
+    const StepParams* __restrict__ sp, const R* __restrict__ pr3d, R* __restrict__ exn) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int N = g.N, L = g.L, L1 = L + 1;
+  const int i0 = (blockIdx.x * kWarpsInflate + wib) * 32;
+  if (i0 >= N) return;
+  const int ncol = (N - i0 < 32) ? N - i0 : 32;
+  const size_t m = blockIdx.y;
+  if (!sp[m].active) return;
+  pr3d += m * s.intf; exn += m * s.intf;
+  R* col = reinterpret_cast<R*>(smraw) + (size_t)wib * (32 * (ML + 1) + 1);
+  for (int q = lane; q < ncol * L1; q += 32) col[q] = exn[(size_t)i0 * L1 + q];
+  __syncwarp();
+  if (lane < ncol) inflate<R>(kn, g.dpsig, L, pr3d[(size_t)(i0 + lane) * L1], col + lane * L1);
+  __syncwarp();
+  for (int q = lane; q < ncol * L1; q += 32) exn[(size_t)i0 * L1 + q] = col[q];
+}
+
 template <typename R, int ML>
 __global__ void __launch_bounds__(32 * kWarpsRemap) k_remap_w(Grid<R> g, Strides s, Knobs kn,
     const StepParams* __restrict__ sp, const R* __restrict__ targt, const R* __restrict__ exsmo,
@@ -579,8 +641,8 @@ __global__ void __launch_bounds__(32 * kWarpsRemap) k_remap_w(Grid<R> g, Strides
     R* __restrict__ ex3d, R* __restrict__ dp3d, R* __restrict__ pr3d, int* __restrict__ flags) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int i = blockIdx.x * kWarpsRemap + wib;
   const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
+  const int i = blockIdx.x * kWarpsRemap + wib;
   if (i >= N) return;
   const size_t m = blockIdx.y;
   sp += m;
@@ -593,21 +655,17 @@ __global__ void __launch_bounds__(32 * kWarpsRemap) k_remap_w(Grid<R> g, Strides
   const size_t ci = (size_t)i * L1;
   for (int k = lane; k <= L; k += 32) {
     const R eo = ex3d[ci + k], pc = pr3d[ci + k];
+    R en = exsmo[ci + k];
+    if (its > 0) {
+      const R sl = R(kn.slak);
+      en = sl * en + (R(1) - sl) * eo;
+    }
     S.exold[k] = eo;
     S.prcol[k] = pc;
-    S.exnew[k] = exsmo[ci + k];
+    S.exnew[k] = en;
     S.pk1col[k] = eo * pc / cp;
   }
   __syncwarp();
-  if (kn.intfc_smooth > 0.) {
-    if (lane == 0) inflate<R>(kn, g.dpsig, L, S.prcol[0], S.exnew);
-    __syncwarp();
-  }
-  if (its > 0) {
-    const R sl = R(kn.slak);
-    for (int k = lane; k <= L; k += 32) S.exnew[k] = sl * S.exnew[k] + (R(1) - sl) * S.exold[k];
-    __syncwarp();
-  }
   // miglim = 1: exnew(2..nvl) between the neighbouring old interfaces
   for (int k = 2 + lane; k <= L; k += 32)
     S.exnew[k - 1] = cmax(R(.0001) * S.exold[k - 1] + R(.9999) * S.exold[k],
@@ -627,20 +685,8 @@ __global__ void __launch_bounds__(32 * kWarpsRemap) k_remap_w(Grid<R> g, Strides
     S.pk1new[0] = S.pk1col[0];
   }
   __syncwarp();
-  // delz, fco, fcn of both coordinates (pcwise's first two loops)
-  {
-    const bool fp = !(S.prcol[0] < S.prcol[L]), fk = !(S.pk1col[0] < S.pk1col[L]);
-    for (int k = lane; k <= L; k += 32) {
-      S.dz_p[k] = fp ? (-S.prnew[k]) - (-S.prcol[k]) : S.prnew[k] - S.prcol[k];
-      S.dz_k[k] = fk ? (-S.pk1new[k]) - (-S.pk1col[k]) : S.pk1new[k] - S.pk1col[k];
-      if (k < L) {
-        S.fo_p[k] = fp ? cmax(R(0), (-S.prcol[k + 1]) - (-S.prcol[k])) : cmax(R(0), S.prcol[k + 1] - S.prcol[k]);
-        S.fn_p[k] = fp ? cmax(R(0), (-S.prnew[k + 1]) - (-S.prnew[k])) : cmax(R(0), S.prnew[k + 1] - S.prnew[k]);
-        S.fo_k[k] = fk ? cmax(R(0), (-S.pk1col[k + 1]) - (-S.pk1col[k])) : cmax(R(0), S.pk1col[k + 1] - S.pk1col[k]);
-        S.fn_k[k] = fk ? cmax(R(0), (-S.pk1new[k + 1]) - (-S.pk1new[k])) : cmax(R(0), S.pk1new[k + 1] - S.pk1new[k]);
-      }
-    }
-  }
+  remap_geo<R, ML>(L, lane, S.prcol, S.prnew, S.gp);
+  remap_geo<R, ML>(L, lane, S.pk1col, S.pk1new, S.gk);
   __syncwarp();
   // fields: 0 = u, 1 = v, 2..T = tracers 2..ntra, T+1 = theta
   const int F = T + 2;
@@ -656,24 +702,23 @@ __global__ void __launch_bounds__(32 * kWarpsRemap) k_remap_w(Grid<R> g, Strides
     __syncwarp();
     if (lane < nf) {
       const int f = base + lane;
+      const bool theta = f == T + 1;
       R* y = S.tile + lane;
-      if (f <= T) {
-        bad |= pcwise_lane<R>(L, y, S.dz_p, S.fo_p, S.fn_p);
-        if (f >= 2 && kn.thktop == 0.) {
-          for (int k = 3; k <= L; k++) {
-            const R qq = R(1) / (S.dpcol[k - 1] + small);
-            y[(k - 1) * kTS] = (y[(k - 1) * kTS] * S.dpcol[k - 1] + y[(k - 2) * kTS] * small) * qq;
-          }
+      R colin = R(0), colscl = R(0);
+      if (sizeof(R) == 8 && theta) {
+        for (int k = 0; k < L; k++) {
+          colin = colin + y[k * kTS] * (S.pk1col[k] - S.pk1col[k + 1]);
+          colscl = colscl + cabs(y[k * kTS] * (S.pk1col[k] - S.pk1col[k + 1]));
         }
-      } else {
-        R colin = R(0), colscl = R(0);
-        if (sizeof(R) == 8) {
-          for (int k = 0; k < L; k++) {
-            colin = colin + y[k * kTS] * (S.pk1col[k] - S.pk1col[k + 1]);
-            colscl = colscl + cabs(y[k * kTS] * (S.pk1col[k] - S.pk1col[k + 1]));
-          }
+      }
+      bad |= pcwise_lane<R, ML>(L, y, theta ? S.gk : S.gp);
+      if (f >= 2 && !theta && kn.thktop == 0.) {
+        for (int k = 3; k <= L; k++) {
+          const R qq = R(1) / (S.dpcol[k - 1] + small);
+          y[(k - 1) * kTS] = (y[(k - 1) * kTS] * S.dpcol[k - 1] + y[(k - 2) * kTS] * small) * qq;
         }
-        bad |= pcwise_lane<R>(L, y, S.dz_k, S.fo_k, S.fn_k);
+      }
+      if (theta) {
         for (int k = L; k >= 3; k--) {
           const R dplo = cmax(S.pk1new[k - 2] - S.pk1new[k - 1], S.pk1new[0] * small);
           const R dpup = cmax(S.pk1new[k - 1] - S.pk1new[k], S.pk1new[0] * small);
@@ -704,29 +749,49 @@ __global__ void __launch_bounds__(32 * kWarpsRemap) k_remap_w(Grid<R> g, Strides
     }
     __syncwarp();
   }
-  if (lane == 0)
-    for (int k = 0; k < L; k++)
-      if (S.exnew[k] < S.exnew[k + 1]) S.exnew[k + 1] = S.exnew[k];
-  __syncwarp();
-  for (int k = lane; k <= L; k += 32) {
-    sdot[ci + k] = S.exnew[k] - S.exold[k];
-    ex3d[ci + k] = S.exnew[k];
-    pr3d[ci + k] = S.prnew[k];
-    if (k < L) dp3d[(size_t)i * L + k] = S.dpcol[k];
+  // exnew made non-increasing downward: prefix minimum over the interfaces
+  R carry = S.exnew[0];
+  for (int kb = 0; kb <= L; kb += 32) {
+    const int k = kb + lane;
+    R v = k <= L ? S.exnew[k] : carry;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const R o = __shfl_up_sync(0xffffffffu, v, off);
+      if (lane >= off) v = cmin(v, o);
+    }
+    v = cmin(v, carry);
+    if (k <= L) {
+      sdot[ci + k] = v - S.exold[k];
+      ex3d[ci + k] = v;
+      pr3d[ci + k] = S.prnew[k];
+      if (k < L) dp3d[(size_t)i * L + k] = S.dpcol[k];
+    }
+    carry = __shfl_sync(0xffffffffu, v, 31);
   }
   if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flags + m, kFlagColumnIntegral);
 }
 
 template <typename R, int ML>
 size_t remap_w_smem() { return sizeof(RemapSm<R, ML>) * kWarpsRemap; }
+template <typename R, int ML>
+size_t inflate_smem() { return sizeof(R) * (32 * (ML + 1) + 1) * kWarpsInflate; }
 
 template <typename R>
 int prepare_hybgen(int L) {
   cudaError_t e;
-  if (L <= 64) e = cudaFuncSetAttribute(k_remap_w<R, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)remap_w_smem<R, 64>());
-  else e = cudaFuncSetAttribute(k_remap_w<R, kMaxL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)remap_w_smem<R, kMaxL>());
+  if (L <= 64) {
+    e = cudaFuncSetAttribute(k_remap_w<R, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)remap_w_smem<R, 64>());
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_inflate<R, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)inflate_smem<R, 64>());
+  } else {
+    e = cudaFuncSetAttribute(k_remap_w<R, kMaxL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)remap_w_smem<R, kMaxL>());
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_inflate<R, kMaxL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)inflate_smem<R, kMaxL>());
+  }
   return e == cudaSuccess ? 0 : (int)e;
 }
 
@@ -836,7 +901,28 @@ constexpr int kGsBlocks = 152 * 4;
 constexpr int kGsCol = kMaxT + 1;
 constexpr int kGsSlots = kMaxT + 5;
 
-template <typename R>
+// Level sums of one group of kGsGroup slots (blockIdx.z), VK levels per
+// access; group 0 also forms the column sums.
+constexpr int kGsGroup = 8;
+
+template <typename R, int VK> struct GsVec;
+template <typename R> struct GsVec<R, 1> {
+  static __device__ __forceinline__ void ld(const R* p, R (&r)[1]) { r[0] = *p; }
+};
+template <> struct GsVec<float, 4> {
+  static __device__ __forceinline__ void ld(const float* p, float (&r)[4]) {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    r[0] = t.x; r[1] = t.y; r[2] = t.z; r[3] = t.w;
+  }
+};
+template <> struct GsVec<double, 2> {
+  static __device__ __forceinline__ void ld(const double* p, double (&r)[2]) {
+    const double2 t = *reinterpret_cast<const double2*>(p);
+    r[0] = t.x; r[1] = t.y;
+  }
+};
+
+template <typename R, int VK>
 __global__ void __launch_bounds__(kBlock2) k_globsum_levels(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     const R* __restrict__ dp3d, const R* __restrict__ tr, const R* __restrict__ rn2d, const R* __restrict__ rc2d,
     const R* __restrict__ pr3d, const R* __restrict__ ex3d, const R* __restrict__ qf2d,
@@ -845,38 +931,59 @@ __global__ void __launch_bounds__(kBlock2) k_globsum_levels(Grid<R> g, Strides s
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active) return;
+  const int q0 = blockIdx.z * kGsGroup;  // first level slot of this group
   dp3d += m * s.cell; tr += m * s.tr; pr3d += m * s.intf; ex3d += m * s.intf;
-  const size_t NL = (size_t)N * L;
+  const size_t NL = (size_t)N * L, NV = NL / VK;
+  const int LV = L / VK;
   const size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, gstride = (size_t)gridDim.x * blockDim.x;
-  Acc<R> acc[kMaxT + 1];
-  for (size_t idx = gid; idx < NL; idx += gstride) {
-    const int i = (int)(idx / L);
-    const R ad = g.area[i] * dp3d[idx];
-    acc[0].add(ad);
+  Acc<R> acc[kGsGroup];
+  for (size_t v = gid; v < NV; v += gstride) {
+    const size_t idx = v * VK;
+    const R ar = g.area[(int)v / LV];
+    R dp[VK], ad[VK];
+    GsVec<R, VK>::ld(dp3d + idx, dp);
 #pragma unroll
-    for (int t = 0; t < kMaxT; t++)
-      if (t < T) acc[1 + t].add(ad * tr[(size_t)t * NL + idx]);
+    for (int j = 0; j < VK; j++) ad[j] = ar * dp[j];
+#pragma unroll
+    for (int u = 0; u < kGsGroup; u++) {
+      const int q = q0 + u;
+      if (q > T) break;
+      if (q == 0) {
+#pragma unroll
+        for (int j = 0; j < VK; j++) acc[u].add(ad[j]);
+      } else {
+        R x[VK];
+        GsVec<R, VK>::ld(tr + (size_t)(q - 1) * NL + idx, x);
+#pragma unroll
+        for (int j = 0; j < VK; j++) acc[u].add(ad[j] * x[j]);
+      }
+    }
   }
   double col[4] = {0., 0., 0., 0.};
-  const double dt = sp->dt, rdcp = kRd / kCp;
-  for (size_t i = gid; i < (size_t)N; i += gstride) {
-    const double a = g.area_d[i];
-    const double rn = rn2d ? (double)rn2d[m * s.col + i] : 0.0;
-    const double rc = rc2d ? (double)rc2d[m * s.col + i] : 0.0;
-    const double qf = qf2d ? (double)qf2d[m * s.col + i] : 0.0;
-    col[0] += a * rn;
-    col[1] += a * rc;
-    col[2] += a * (rn - rc);
-    const double den = (double)pr3d[i * L1] / (rdcp * (double)ex3d[i * L1] * (double)tr[i * L]);
-    col[3] += a * den * qf * dt / (1.25 * 2.5e6);
+  if (blockIdx.z == 0) {
+    const double dt = sp->dt, rdcp = kRd / kCp;
+    for (size_t i = gid; i < (size_t)N; i += gstride) {
+      const double a = g.area_d[i];
+      const double rn = rn2d ? (double)rn2d[m * s.col + i] : 0.0;
+      const double rc = rc2d ? (double)rc2d[m * s.col + i] : 0.0;
+      const double qf = qf2d ? (double)qf2d[m * s.col + i] : 0.0;
+      col[0] += a * rn;
+      col[1] += a * rc;
+      col[2] += a * (rn - rc);
+      const double den = (double)pr3d[i * L1] / (rdcp * (double)ex3d[i * L1] * (double)tr[i * L]);
+      col[3] += a * den * qf * dt / (1.25 * 2.5e6);
+    }
   }
   __shared__ double red[kBlock2 / 32];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   double* out = partial + (m * gridDim.x + blockIdx.x) * kGsSlots;
 #pragma unroll
-  for (int q = 0; q < kGsSlots; q++) {
-    if (q > T && q < kGsCol) continue;
-    double v = q < kGsCol ? acc[q].value() : col[q - kGsCol];
+  for (int u = 0; u < kGsGroup + 4; u++) {
+    // both conditions are uniform across the block
+    if (u >= kGsGroup && blockIdx.z != 0) break;
+    if (u < kGsGroup && q0 + u > T) continue;
+    const int q = u < kGsGroup ? q0 + u : kGsCol + (u - kGsGroup);
+    double v = u < kGsGroup ? acc[u < kGsGroup ? u : 0].value() : col[u < kGsGroup ? 0 : u - kGsGroup];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     if (lane == 0) red[wib] = v;
@@ -963,6 +1070,18 @@ void launch_hybgen(const Launch& l, const Grid<R>& g, const Strides& s, const Kn
     ex_in = w.exsmo2;
   }
   if (kn.remap_optn == 2 && kn.miglim == 1) {
+    if (kn.intfc_smooth > 0.) {
+      // ex_in is the smoothing scratch here: inflate it in place
+      dim3 gi(nblocks(g.N, 32 * kWarpsInflate), l.members);
+      FIM_KBEGIN(l, "k_inflate");
+      if (g.L <= 64)
+        k_inflate<R, 64><<<gi, 32 * kWarpsInflate, inflate_smem<R, 64>(), l.stream>>>(g, s, kn, l.sp, pr3d,
+                                                                                      w.exsmo2);
+      else
+        k_inflate<R, kMaxL><<<gi, 32 * kWarpsInflate, inflate_smem<R, kMaxL>(), l.stream>>>(g, s, kn, l.sp, pr3d,
+                                                                                            w.exsmo2);
+      FIM_KEND(l);
+    }
     dim3 gw(nblocks(g.N, kWarpsRemap), l.members);
     FIM_KBEGIN(l, "k_remap");
     if (g.L <= 64)
@@ -1001,9 +1120,16 @@ template <typename R>
 void launch_globsum(const Launch& l, const Grid<R>& g, const Strides& s, const R* dp3d, const R* tr,
                     const R* rn2d, const R* rc2d, const R* pr3d, const R* ex3d, const R* qf2d,
                     double* partial, double* sums) {
-  dim3 gl(kGsBlocks, l.members);
+  dim3 gl(kGsBlocks, l.members, (g.T + 1 + kGsGroup - 1) / kGsGroup);
   FIM_KBEGIN(l, "k_globsum_levels");
-  k_globsum_levels<R><<<gl, kBlock2, 0, l.stream>>>(g, s, l.sp, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d, partial);
+  constexpr int VK = sizeof(R) == 4 ? 4 : 2;
+  const bool vec = g.L % VK == 0 && (uintptr_t)dp3d % (VK * sizeof(R)) == 0 && (uintptr_t)tr % (VK * sizeof(R)) == 0;
+  if (vec)
+    k_globsum_levels<R, VK><<<gl, kBlock2, 0, l.stream>>>(g, s, l.sp, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d,
+                                                          partial);
+  else
+    k_globsum_levels<R, 1><<<gl, kBlock2, 0, l.stream>>>(g, s, l.sp, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d,
+                                                         partial);
   FIM_KEND(l);
   FIM_KBEGIN(l, "k_globsum_final");
   k_globsum_final<R><<<l.members, kBlock2, 0, l.stream>>>(l.sp, g.T, partial, kGsBlocks, sums);
