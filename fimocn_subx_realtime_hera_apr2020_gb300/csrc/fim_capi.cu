@@ -36,7 +36,7 @@ struct fim_state {
   void* f[FIM_NFIELDS] = {};
   size_t count[FIM_NFIELDS] = {};  // elements per member
   double* sums = nullptr;          // [M][8+T]
-  double* mpd = nullptr;           // FP32-mixed: FP64 Montgomery potential [M][nvl*nip]
+  float2* mpf = nullptr;           // FP32-mixed: float-float Montgomery potential [M][nvl*nip]
   void* thold = nullptr;           // FP32-mixed: theta seen by edgvar1 this step [M][nvl*nip]
   cudaGraphExec_t graph = nullptr;
   long long graph_kernels = 0;
@@ -171,8 +171,8 @@ int build_grid(fim_ctx* c, const fim_grid_desc* g, const std::vector<double>& ra
         sv[(size_t)i * 2 + 0] += g->sidevec_c[((size_t)i * 6 + e) * 2 + 0];
         sv[(size_t)i * 2 + 1] += g->sidevec_c[((size_t)i * 6 + e) * 2 + 1];
       }
-    const double* t_;
-    if ((rc = upload_conv<double>(c, sv.data(), sv.size(), &t_))) return rc;
+    const R* t_;
+    if ((rc = upload_conv<R>(c, sv.data(), sv.size(), &t_))) return rc;
     G.svsum = t_;
   }
   { const R* t_; if ((rc = upload_conv<R>(c, dfflen.data(), (size_t)c->L, &t_))) return rc; G.dfflen = t_; }
@@ -605,7 +605,7 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
   launch_edgvar1<R>(l, g, s, c->kn.hi_order, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_DP3D),
                     F<R>(st, FIM_PR3D), F<R>(st, FIM_MP3D), F<R>(st, FIM_TR3D), F<R>(st, FIM_U_EDG),
                     F<R>(st, FIM_V_EDG), F<R>(st, FIM_DP_EDG), F<R>(st, FIM_LP_EDG), F<R>(st, FIM_MONT_EDG),
-                    F<R>(st, FIM_UVSQ_EDG), F<R>(st, FIM_TRC_EDG), st->mpd, (R*)st->thold);
+                    F<R>(st, FIM_UVSQ_EDG), F<R>(st, FIM_TRC_EDG), st->mpf, (R*)st->thold);
   if (c->kn.hi_order) {
     // dp edges with edgvar3's two-sided average; tracer edges keep the
     // own-side values, averaged where the fused tracer kernels use them
@@ -639,12 +639,12 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
   launch_momtum<R>(l, g, s, c->kn, mw, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_EX3D),
                    F<R>(st, FIM_RELVOR), F<R>(st, FIM_U_EDG), F<R>(st, FIM_V_EDG), F<R>(st, FIM_TRC_EDG),
                    F<R>(st, FIM_MONT_EDG), F<R>(st, FIM_UVSQ_EDG), F<R>(st, FIM_U_TDCY), F<R>(st, FIM_V_TDCY),
-                   F<R>(st, FIM_DP3D), st->mpd, (const R*)st->thold);
+                   F<R>(st, FIM_DP3D), st->mpf, (const R*)st->thold);
   HybgenScratch<R> hw{(R*)c->exsmo, (R*)c->exsmo2};
   launch_hybgen<R>(l, g, s, c->kn, hw, g.thetac, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_TR3D),
                    F<R>(st, FIM_SDOT), F<R>(st, FIM_EX3D), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D));
   launch_hystat<R>(l, g, s, F<R>(st, FIM_PH3D), F<R>(st, FIM_EX3D), F<R>(st, FIM_MP3D), F<R>(st, FIM_DP3D),
-                   F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP), F<R>(st, FIM_PSRF), F<R>(st, FIM_PTDCY), st->mpd);
+                   F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP), F<R>(st, FIM_PSRF), F<R>(st, FIM_PTDCY), st->mpf);
   launch_globsum<R>(l, g, s, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), (const R*)nullptr, (const R*)nullptr,
                     F<R>(st, FIM_PR3D), F<R>(st, FIM_EX3D), (const R*)nullptr, c->gs_partial, st->sums);
   return FIM_OK;
@@ -687,7 +687,7 @@ int state_init_impl(fim_ctx* c, fim_state* st, int m0, int nm) {
   CK(cudaMemsetAsync(P(FIM_PSRF), 0, nm * st->count[FIM_PSRF] * c->esz, c->stream), "zero psrf");
   CK(cudaMemsetAsync(P(FIM_PTDCY), 0, nm * st->count[FIM_PTDCY] * c->esz, c->stream), "zero ptdcy");
   launch_hystat<R>(l, g, c->str, P(FIM_PH3D), P(FIM_EX3D), P(FIM_MP3D), P(FIM_DP3D), P(FIM_TR3D), P(FIM_TRDP),
-                   P(FIM_PSRF), P(FIM_PTDCY), st->mpd ? st->mpd + (size_t)m0 * st->count[FIM_MP3D] : nullptr);
+                   P(FIM_PSRF), P(FIM_PTDCY), st->mpf ? st->mpf + (size_t)m0 * st->count[FIM_MP3D] : nullptr);
   const int zero[] = {FIM_U_TDCY, FIM_V_TDCY, FIM_DP_TDCY, FIM_DPL_TDCY, FIM_TRC_TDCY, FIM_TRL_TDCY, FIM_MASSFX};
   for (int f : zero) CK(cudaMemsetAsync(P(f), 0, nm * st->count[f] * c->esz, c->stream), "zero tendencies");
   for (int m = m0; m < m0 + nm; m++) reset_member(c, m);
@@ -994,9 +994,9 @@ int fim_state_alloc(fim_ctx* c, fim_state** out) {
   int rc = dalloc(c, (void**)&st->sums, (size_t)c->M * (8 + c->T) * sizeof(double));
   if (rc) { delete st; return rc; }
   if (c->prec == FIM_PREC_F32) {
-    if ((rc = dalloc(c, (void**)&st->mpd, (size_t)c->M * cnt[FIM_MP3D] * sizeof(double)))) { delete st; return rc; }
+    if ((rc = dalloc(c, (void**)&st->mpf, (size_t)c->M * cnt[FIM_MP3D] * sizeof(float2)))) { delete st; return rc; }
     if ((rc = dalloc(c, &st->thold, (size_t)c->M * cnt[FIM_MP3D] * c->esz))) { delete st; return rc; }
-    cudaMemsetAsync(st->mpd, 0, (size_t)c->M * cnt[FIM_MP3D] * sizeof(double), c->stream);
+    cudaMemsetAsync(st->mpf, 0, (size_t)c->M * cnt[FIM_MP3D] * sizeof(float2), c->stream);
   }
   if ((rc = ensure_all(c))) { delete st; return rc; }
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) { delete st; return set_err(c, FIM_ECUDA, "state alloc"); }
@@ -1012,7 +1012,7 @@ int fim_state_free(fim_ctx* c, fim_state* st) {
     for (auto it = c->owned.begin(); it != c->owned.end(); ++it)
       if (*it == st->f[f]) { cudaFree(*it); c->owned.erase(it); break; }
   }
-  for (void* extra : {(void*)st->sums, (void*)st->mpd, st->thold})
+  for (void* extra : {(void*)st->sums, (void*)st->mpf, st->thold})
     for (auto it = c->owned.begin(); it != c->owned.end(); ++it)
       if (extra && *it == extra) { cudaFree(*it); c->owned.erase(it); break; }
   delete st;

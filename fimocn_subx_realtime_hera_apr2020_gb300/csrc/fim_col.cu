@@ -797,13 +797,15 @@ int prepare_hybgen(int L) {
 
 // ---------------------------------------------------------------- hystat --
 // hystat (hystat.F90:53-109): one warp per column; surface pressure sum and
-// the bottom-up Montgomery potential / geopotential recursion are FP64 warp
-// scans; humidity floors and tracer x thickness per level.
+// the bottom-up Montgomery potential / geopotential recursion are warp scans
+// in FP64 (FP64 build) or float-float (FP32-mixed build, which also keeps the
+// (hi, lo) Montgomery potential for the pressure gradient); humidity floors
+// and tracer x thickness per level.
 template <typename R>
 __global__ void __launch_bounds__(kBlock2) k_hystat(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     R* __restrict__ ph3d, const R* __restrict__ ex3d, R* __restrict__ mp3d, const R* __restrict__ dp3d,
     R* __restrict__ tr3d, R* __restrict__ trdp, R* __restrict__ psrf, R* __restrict__ ptdcy,
-    double* __restrict__ mpd) {
+    float2* __restrict__ mpf) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
   if (warp >= N) return;
@@ -813,46 +815,92 @@ __global__ void __launch_bounds__(kBlock2) k_hystat(Grid<R> g, Strides s, const 
   if (!sp->active) return;
   ph3d += m * s.intf; ex3d += m * s.intf; mp3d += m * s.cell; dp3d += m * s.cell; tr3d += m * s.tr;
   trdp += m * s.tr; psrf += m * s.col; ptdcy += m * 2 * s.col;
-  if (mpd) mpd += m * s.cell;
+  if (mpf) mpf += m * s.cell;
   const int its = sp->its;
   const size_t NL = (size_t)N * L;
-  // surface pressure: sum of all layer thicknesses
-  double ps = 0.0;
-  for (int k = lane; k < L; k += 32) ps += (double)dp3d[(size_t)i * L + k];
+  if constexpr (sizeof(R) == 4) {
+    // float-float sums and scan (FP64-accurate on the FP32 pipes)
+    FF2 ps{0.f, 0.f};
+    for (int k = lane; k < L; k += 32) ps = ff_add(ps, FF2{dp3d[(size_t)i * L + k], 0.f});
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) ps += __shfl_xor_sync(0xffffffffu, ps, off);
-  if (lane == 0) {
-    const R work = psrf[i];
-    const R pn = R(ps);
-    psrf[i] = pn;
-    if (its > 0) ptdcy[(size_t)(its % 2) * N + i] = pn - work;
-  }
-  double carry = 0.0;
-  const double ph0 = (double)ph3d[(size_t)i * L1];
-  for (int base = 0; base < L; base += 32) {
-    const int k = base + lane;
-    const bool act = k < L;
-    double term = 0.0, th = 0.0, exk1 = 0.0;
-    if (act) {
-      th = (double)tr3d[(size_t)i * L + k];
-      const double ex = (double)ex3d[(size_t)i * L1 + k];
-      exk1 = (double)ex3d[(size_t)i * L1 + k + 1];
-      if (k == 0) term = ex * th + ph0;
-      else term = ex * (th - (double)tr3d[(size_t)i * L + k - 1]);
+    for (int off = 16; off > 0; off >>= 1) ps = ff_add(ps, ff_shfl_xor(ps, off));
+    if (lane == 0) {
+      const R work = psrf[i];
+      const R pn = ps.hi;
+      psrf[i] = pn;
+      if (its > 0) ptdcy[(size_t)(its % 2) * N + i] = pn - work;
     }
-    double sc = term;
+    FF2 carry{0.f, 0.f};
+    const float ph0 = ph3d[(size_t)i * L1];
+    for (int base = 0; base < L; base += 32) {
+      const int k = base + lane;
+      const bool act = k < L;
+      FF2 term{0.f, 0.f};
+      float th = 0.f, exk1 = 0.f;
+      if (act) {
+        th = tr3d[(size_t)i * L + k];
+        const float ex = ex3d[(size_t)i * L1 + k];
+        exk1 = ex3d[(size_t)i * L1 + k + 1];
+        if (k == 0) {
+          term = ff_add(two_prod(ex, th), FF2{ph0, 0.f});
+        } else {
+          const FF2 d = two_sum(th, -tr3d[(size_t)i * L + k - 1]);
+          term = ff_add(two_prod(ex, d.hi), FF2{ex * d.lo, 0.f});
+        }
+      }
+      FF2 sc = term;
 #pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      const double a = __shfl_up_sync(0xffffffffu, sc, off);
-      if (lane >= off) sc += a;
+      for (int off = 1; off < 32; off <<= 1) {
+        const FF2 a = ff_shfl_up(sc, off);
+        if (lane >= off) sc = ff_add(sc, a);
+      }
+      const FF2 mp = ff_add(carry, sc);
+      if (act) {
+        mp3d[(size_t)i * L + k] = mp.hi;
+        if (mpf) mpf[(size_t)i * L + k] = make_float2(mp.hi, mp.lo);
+        const FF2 ph = ff_add(mp, ff_neg(two_prod(th, exk1)));
+        ph3d[(size_t)i * L1 + k + 1] = ph.hi;
+      }
+      carry = ff_add(carry, ff_shfl(sc, 31));
     }
-    const double mp = carry + sc;
-    if (act) {
-      mp3d[(size_t)i * L + k] = R(mp);
-      if (mpd) mpd[(size_t)i * L + k] = mp;
-      ph3d[(size_t)i * L1 + k + 1] = R(mp - th * exk1);
+  } else {
+    // surface pressure: sum of all layer thicknesses
+    double ps = 0.0;
+    for (int k = lane; k < L; k += 32) ps += (double)dp3d[(size_t)i * L + k];
+  #pragma unroll
+    for (int off = 16; off > 0; off >>= 1) ps += __shfl_xor_sync(0xffffffffu, ps, off);
+    if (lane == 0) {
+      const R work = psrf[i];
+      const R pn = R(ps);
+      psrf[i] = pn;
+      if (its > 0) ptdcy[(size_t)(its % 2) * N + i] = pn - work;
     }
-    carry += __shfl_sync(0xffffffffu, sc, 31);
+    double carry = 0.0;
+    const double ph0 = (double)ph3d[(size_t)i * L1];
+    for (int base = 0; base < L; base += 32) {
+      const int k = base + lane;
+      const bool act = k < L;
+      double term = 0.0, th = 0.0, exk1 = 0.0;
+      if (act) {
+        th = (double)tr3d[(size_t)i * L + k];
+        const double ex = (double)ex3d[(size_t)i * L1 + k];
+        exk1 = (double)ex3d[(size_t)i * L1 + k + 1];
+        if (k == 0) term = ex * th + ph0;
+        else term = ex * (th - (double)tr3d[(size_t)i * L + k - 1]);
+      }
+      double sc = term;
+  #pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const double a = __shfl_up_sync(0xffffffffu, sc, off);
+        if (lane >= off) sc += a;
+      }
+      const double mp = carry + sc;
+      if (act) {
+        mp3d[(size_t)i * L + k] = R(mp);
+          ph3d[(size_t)i * L1 + k + 1] = R(mp - th * exk1);
+      }
+      carry += __shfl_sync(0xffffffffu, sc, 31);
+    }
   }
   const R qvmin = R(kQvmin), qwmin = R(kQwmin);
   for (int k = lane; k < L; k += 32) {
@@ -1104,10 +1152,10 @@ void launch_hybgen(const Launch& l, const Grid<R>& g, const Strides& s, const Kn
 
 template <typename R>
 void launch_hystat(const Launch& l, const Grid<R>& g, const Strides& s, R* ph3d, const R* ex3d, R* mp3d,
-                   const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy, double* mpd) {
+                   const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy, float2* mpf) {
   dim3 gw(nblocks((long long)g.N * 32, kBlock2), l.members);
   FIM_KBEGIN(l, "k_hystat");
-  k_hystat<R><<<gw, kBlock2, 0, l.stream>>>(g, s, l.sp, ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy, mpd);
+  k_hystat<R><<<gw, kBlock2, 0, l.stream>>>(g, s, l.sp, ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy, mpf);
   FIM_KEND(l);
 }
 
@@ -1149,7 +1197,7 @@ void launch_prdp_from_ex(const Launch& l, const Grid<R>& g, const Strides& s, co
   template void launch_hybgen<R>(const Launch&, const Grid<R>&, const Strides&, const Knobs&,               \
                                  const HybgenScratch<R>&, const R*, R*, R*, R*, R*, R*, R*, R*);            \
   template void launch_hystat<R>(const Launch&, const Grid<R>&, const Strides&, R*, const R*, R*, const R*, \
-                                 R*, R*, R*, R*, double*);                                                  \
+                                 R*, R*, R*, R*, float2*);                                                  \
   template void launch_globsum<R>(const Launch&, const Grid<R>&, const Strides&, const R*, const R*,        \
                                   const R*, const R*, const R*, const R*, const R*, double*, double*);      \
   template void launch_prdp_from_ex<R>(const Launch&, const Grid<R>&, const Strides&, const R*, R*, R*);

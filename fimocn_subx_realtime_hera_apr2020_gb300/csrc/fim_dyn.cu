@@ -42,13 +42,13 @@ __global__ void __launch_bounds__(kBlock) k_edgvar1(Grid<R> g, Strides s, int hi
     const R* __restrict__ u, const R* __restrict__ v, const R* __restrict__ delp,
     const R* __restrict__ pres, const R* __restrict__ montg, const R* __restrict__ tracr,
     R* __restrict__ u_edg, R* __restrict__ v_edg, R* __restrict__ dp_edg, R* __restrict__ lp_edg,
-    R* __restrict__ mont_edg, R* __restrict__ uvsq_edg, R* __restrict__ trc_edg, const double* __restrict__ mpd,
+    R* __restrict__ mont_edg, R* __restrict__ uvsq_edg, R* __restrict__ trc_edg, const float2* __restrict__ mpf,
     R* __restrict__ thold) {
   int i, k;
   if (!cell_level(g.N, g.L, i, k)) return;
   const int L = g.L, N = g.N, L1 = L + 1;
   const size_t m = blockIdx.y;
-  if (mpd) mpd += m * s.cell;
+  if (mpf) mpf += m * s.cell;
   if (thold) {
     // the potential temperature of this step's edge values, for momtum1
     thold += m * s.cell;
@@ -94,11 +94,11 @@ __global__ void __launch_bounds__(kBlock) k_edgvar1(Grid<R> g, Strides s, int hi
     lp_edg[o] = (p1a + p1b + pres[(size_t)i2 * L1 + k] + pres[(size_t)i2 * L1 + k + 1] +
                  half * (pres[(size_t)i3t * L1 + k] + pres[(size_t)i3t * L1 + k + 1] +
                          pres[(size_t)i3l * L1 + k] + pres[(size_t)i3l * L1 + k + 1])) * divby6;
-    if (mpd) {
-      // edge minus cell value from FP64 differences (no cancellation in FP32)
-      const double mc = mpd[(size_t)i * L + k];
-      mont_edg[o] = R((2.0 * (mpd[(size_t)i2 * L + k] - mc) + (mpd[(size_t)i3t * L + k] - mc) +
-                       (mpd[(size_t)i3l * L + k] - mc)) * (1.0 / 6.0));
+    if (mpf) {
+      // edge minus cell value from float-float differences (no cancellation)
+      const float2 mc = mpf[(size_t)i * L + k];
+      mont_edg[o] = R((2.f * ff_diff(mpf[(size_t)i2 * L + k], mc) + ff_diff(mpf[(size_t)i3t * L + k], mc) +
+                       ff_diff(mpf[(size_t)i3l * L + k], mc)) * (1.f / 6.f));
     } else {
       mont_edg[o] = (two * (m1 + montg[(size_t)i2 * L + k]) + montg[(size_t)i3t * L + k] +
                      montg[(size_t)i3l * L + k]) * divby6;
@@ -329,6 +329,57 @@ __global__ void __launch_bounds__(kBlock) k_cnuity5(Grid<R> g, Strides s, const 
   const R cp = R(kCp), p1000 = R(kP1000), rdcp = R(kRd) / R(kCp);
   const int np = g.nprox[i];
   const R rar = g.rarea[i];
+  if constexpr (sizeof(R) == 4) {
+    // float-float column sums (FP64-accurate on the FP32 pipes)
+    FF2 carry_p{pres[(size_t)i * L1 + L], 0.f}, carry_c{0.f, 0.f};
+    for (int base = 0; base < L; base += 32) {
+      const int j = base + lane;
+      const bool act = j < L;
+      const int k = L - 1 - j;
+      float d = 0.f, lyr = 0.f;
+      if (act) {
+        const size_t c = (size_t)i * L + k;
+        const R tnf = dp_tndcy[(size_t)nf * N * L + c], tof = dp_tndcy[(size_t)of * N * L + c],
+                tvf = dp_tndcy[(size_t)vof * N * L + c];
+        if (ab3_delp) {
+          // massflux_newdepth's AB3 thickness update (massadv_compute.F90:85-91)
+          R dn = delp[c] + ab1 * tnf + ab2 * tof + ab3 * tvf;
+          dn = dn > R(0) ? dn : R(0);
+          delp[c] = dn;
+        }
+        d = delp[c];
+        lyr = (ab1 * tnf + ab2 * tof + ab3 * tvf) / dt;
+      }
+      FF2 sd{d, 0.f}, sl{lyr, 0.f};
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const FF2 a = ff_shfl_up(sd, off), b = ff_shfl_up(sl, off);
+        if (lane >= off) { sd = ff_add(sd, a); sl = ff_add(sl, b); }
+      }
+      if (act) {
+        const size_t c = (size_t)i * L + k;
+        const FF2 p = ff_add(carry_p, sd);
+        const R pr = p.hi;
+        pres[(size_t)i * L1 + k] = pr;
+        exner[(size_t)i * L1 + k] = cp * pow(pr / p1000, rdcp);
+        // omega = (integral of layers above) + half of this layer
+        const FF2 above = ff_add(carry_c, ff_add(sl, FF2{-lyr, 0.f}));
+        R om = R(above.hi + above.lo) + R(0.5) * lyr;
+        R dpdx = R(0), dpdy = R(0);
+        for (int e = 0; e < np; e++) {
+          const R* sv = g.svc + (i * 6 + e) * 2;
+          const R lp = lp_edg[((size_t)i * 6 + e) * L + k];
+          dpdx = dpdx + lp * sv[1];
+          dpdy = dpdy - lp * sv[0];
+        }
+        om = om + (u[c] * dpdx + v[c] * dpdy) * rar;
+        omega[c] = om;
+      }
+      carry_p = ff_add(carry_p, ff_shfl(sd, 31));
+      carry_c = ff_add(carry_c, ff_shfl(sl, 31));
+    }
+    return;
+  }
   double carry_p = (double)pres[(size_t)i * L1 + L];
   double carry_c = 0.0;
   for (int base = 0; base < L; base += 32) {
@@ -744,7 +795,7 @@ __global__ void __launch_bounds__(kBlock) k_momtum1(Grid<R> g, Strides s, Knobs 
     R* __restrict__ u, R* __restrict__ v, const R* __restrict__ du, const R* __restrict__ dv,
     const R* __restrict__ exner, R* __restrict__ relvor, const R* __restrict__ u_edg, const R* __restrict__ v_edg,
     const R* __restrict__ trc_edg, const R* __restrict__ mont_edg, const R* __restrict__ uvsq_edg,
-    R* __restrict__ u_tndcy, R* __restrict__ v_tndcy, const double* __restrict__ mpd, const R* __restrict__ tr0) {
+    R* __restrict__ u_tndcy, R* __restrict__ v_tndcy, const float2* __restrict__ mpf, const R* __restrict__ tr0) {
   __shared__ R top[kBlock / 32][3][2];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -759,8 +810,8 @@ __global__ void __launch_bounds__(kBlock) k_momtum1(Grid<R> g, Strides s, Knobs 
   uvsq_edg += m * s.edge; u_tndcy += m * s.ab; v_tndcy += m * s.ab;
   const bool have_d = du != nullptr;
   if (have_d) { du += m * s.cell; dv += m * s.cell; }
-  const bool split = mpd != nullptr;
-  if (split) { mpd += m * s.cell; tr0 += m * s.cell; }
+  const bool split = mpf != nullptr;
+  if (split) { mpf += m * s.cell; tr0 += m * s.cell; }
   const int nf = sp->nf, of = sp->of, vof = sp->vof;
   const R ab1 = R(sp->ab1), ab2 = R(sp->ab2), ab3 = R(sp->ab3);
   const size_t NL = (size_t)N * L;
@@ -818,9 +869,12 @@ __global__ void __launch_bounds__(kBlock) k_momtum1(Grid<R> g, Strides s, Knobs 
           pgfy = pgfy + w * svc[0];
           rv = rv + (sve[0] * u_edg[o] + sve[1] * v_edg[o]);
         }
-        const double cell = mpd[(size_t)i * L + k] - (double)exm * (double)thc;
-        pgfx = pgfx - R(cell * g.svsum[i * 2 + 1]);
-        pgfy = pgfy + R(cell * g.svsum[i * 2 + 0]);
+        // Montgomery potential minus exner x theta, cancellation-free
+        const float2 mp = mpf[(size_t)i * L + k];
+        const FF2 cf = ff_add(FF2{mp.x, mp.y}, ff_neg(two_prod(float(exm), float(thc))));
+        const R cell = R(cf.hi + cf.lo);
+        pgfx = pgfx - cell * g.svsum[i * 2 + 1];
+        pgfy = pgfy + cell * g.svsum[i * 2 + 0];
       }
       pgfx = pgfx * rar;
       pgfy = pgfy * rar;
@@ -886,11 +940,11 @@ template <typename R>
 void launch_edgvar1(const Launch& l, const Grid<R>& g, const Strides& s, int hi_order, const R* u,
                     const R* v, const R* delp, const R* pres, const R* montg, const R* tracr,
                     R* u_edg, R* v_edg, R* dp_edg, R* lp_edg, R* mont_edg, R* uvsq_edg, R* trc_edg,
-                    const double* mpd, R* thold) {
+                    const float2* mpf, R* thold) {
   dim3 grid(blocks_for((long long)g.N * g.L), l.members);
   FIM_KBEGIN(l, "k_edgvar1");
   k_edgvar1<R><<<grid, kBlock, 0, l.stream>>>(g, s, hi_order, u, v, delp, pres, montg, tracr, u_edg, v_edg,
-                                               dp_edg, lp_edg, mont_edg, uvsq_edg, trc_edg, mpd, thold);
+                                               dp_edg, lp_edg, mont_edg, uvsq_edg, trc_edg, mpf, thold);
   FIM_KEND(l);
 }
 
@@ -956,7 +1010,7 @@ template <typename R>
 void launch_momtum(const Launch& l, const Grid<R>& g, const Strides& s, const Knobs& kn, const MomtumScratch<R>& w,
                    R* u, R* v, const R* exner, R* relvor, const R* u_edg, const R* v_edg,
                    const R* trc_edg, const R* mont_edg, const R* uvsq_edg, R* u_tndcy, R* v_tndcy,
-                   const R* dp3d, const double* mpd, const R* tr0) {
+                   const R* dp3d, const float2* mpf, const R* tr0) {
   dim3 grid(blocks_for((long long)g.N * g.L), l.members);
   const R* du = nullptr;
   const R* dv = nullptr;
@@ -979,7 +1033,7 @@ void launch_momtum(const Launch& l, const Grid<R>& g, const Strides& s, const Kn
   dim3 gw(blocks_for((long long)g.N * 32), l.members);
   FIM_KBEGIN(l, "k_momtum1");
   k_momtum1<R><<<gw, kBlock, 0, l.stream>>>(g, s, kn, l.sp, u, v, du, dv, exner, relvor, u_edg, v_edg, trc_edg,
-                                             mont_edg, uvsq_edg, u_tndcy, v_tndcy, mpd, tr0);
+                                             mont_edg, uvsq_edg, u_tndcy, v_tndcy, mpf, tr0);
   FIM_KEND(l);
 }
 
@@ -992,7 +1046,7 @@ void launch_step_begin(const Launch& l, StepParams* sp) {
 #define INSTANTIATE(R)                                                                                          \
   template void launch_edgvar1<R>(const Launch&, const Grid<R>&, const Strides&, int, const R*, const R*,      \
                                   const R*, const R*, const R*, const R*, R*, R*, R*, R*, R*, R*, R*,          \
-                                  const double*, R*);                                                         \
+                                  const float2*, R*);                                                         \
   template void launch_edgvar3<R>(const Launch&, const Grid<R>&, const Strides&, const R*, const R*, R*, R*,  \
                                   int);                                                                      \
   template void launch_cnuity<R>(const Launch&, const Grid<R>&, const Strides&, const CnuityScratch<R>&,      \
@@ -1005,7 +1059,7 @@ void launch_step_begin(const Launch& l, StepParams* sp) {
                                  const R*, R*, R*, R*, R*, const R*, const R*);                               \
   template void launch_momtum<R>(const Launch&, const Grid<R>&, const Strides&, const Knobs&,                 \
                                  const MomtumScratch<R>&, R*, R*, const R*, R*, const R*, const R*, const R*, \
-                                 const R*, const R*, R*, R*, const R*, const double*, const R*);
+                                 const R*, const R*, R*, R*, const R*, const float2*, const R*);
 INSTANTIATE(float)
 INSTANTIATE(double)
 

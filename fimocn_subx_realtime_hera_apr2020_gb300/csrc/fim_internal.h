@@ -63,7 +63,7 @@ struct Grid {
   const R* __restrict__ grndspd;
   const R* __restrict__ hfcoef;   // [N*6*6]: hfcoef[(i*6+edge)*6+j]
   const double* __restrict__ area_d;  // [N] double areas for budgets
-  const double* __restrict__ svsum;   // [N*2] sum over edges of sidevec_c(1:2)
+  const R* __restrict__ svsum;        // [N*2] sum over edges of sidevec_c(1:2), summed in FP64
   // per-level tables
   const R* __restrict__ dfflen;   // [L]
   const R* __restrict__ biharw;   // [L]
@@ -161,14 +161,54 @@ struct Launch {
     if ((l).counter) ++*(l).counter;                                     \
   } while (0)
 
+
+// ---- float-float arithmetic (FP32-mixed build) ----------------------------
+// A value hi + lo with |lo| <= ulp(hi)/2 carries ~48 significant bits on the
+// FP32 pipes, which GB300 runs at 64x its FP64 rate.  two_sum and two_prod are
+// exact (Knuth; Dekker with a fused multiply-add); ff_add is the usual
+// double-float sum with one renormalisation.
+struct FF2 {
+  float hi, lo;
+};
+__device__ __forceinline__ FF2 two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ FF2 two_prod(float a, float b) {
+  const float p = a * b;
+  return {p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ FF2 ff_add(FF2 a, FF2 b) {
+  const FF2 s = two_sum(a.hi, b.hi);
+  const float e = s.lo + (a.lo + b.lo);
+  const float hi = s.hi + e;
+  return {hi, e - (hi - s.hi)};
+}
+__device__ __forceinline__ FF2 ff_neg(FF2 a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ FF2 ff_shfl_up(FF2 a, int off) {
+  return {__shfl_up_sync(0xffffffffu, a.hi, off), __shfl_up_sync(0xffffffffu, a.lo, off)};
+}
+__device__ __forceinline__ FF2 ff_shfl(FF2 a, int src) {
+  return {__shfl_sync(0xffffffffu, a.hi, src), __shfl_sync(0xffffffffu, a.lo, src)};
+}
+__device__ __forceinline__ FF2 ff_shfl_xor(FF2 a, int m) {
+  return {__shfl_xor_sync(0xffffffffu, a.hi, m), __shfl_xor_sync(0xffffffffu, a.lo, m)};
+}
+// (x.hi + x.lo) - (y.hi + y.lo) rounded once to float
+__device__ __forceinline__ float ff_diff(float2 x, float2 y) {
+  const FF2 d = two_sum(x.x, -y.x);
+  return d.hi + (d.lo + (x.y - y.y));
+}
+
 // ---- launchers (instantiated for float and double) ----------------------
-// mpd (FP32-mixed step only, may be null): FP64 copy of the Montgomery
-// potential; mont_edg then holds the edge value minus the cell value.
+// mpf (FP32-mixed step only, may be null): float-float copy (hi, lo) of the
+// Montgomery potential; mont_edg then holds the edge value minus the cell value.
 template <typename R>
 void launch_edgvar1(const Launch&, const Grid<R>&, const Strides&, int hi_order, const R* u,
                     const R* v, const R* delp, const R* pres, const R* montg, const R* tracr,
                     R* u_edg, R* v_edg, R* dp_edg, R* lp_edg, R* mont_edg, R* uvsq_edg, R* trc_edg,
-                    const double* mpd = nullptr, R* thold = nullptr);
+                    const float2* mpf = nullptr, R* thold = nullptr);
 // nfields: 1 = dp only, T = dp and tracers 2..ntra (edgvar3's full output)
 template <typename R>
 void launch_edgvar3(const Launch&, const Grid<R>&, const Strides&, const R* delp, const R* tracr,
@@ -201,14 +241,14 @@ void launch_tracers_fused(const Launch&, const Grid<R>&, const Strides&, const T
                           const R* delp);
 template <typename R>
 struct MomtumScratch { R *du, *dv, *wu, *wv; };
-// With mpd != null (FP32-mixed step) the pressure-gradient line integrals use
+// With mpf != null (FP32-mixed step) the pressure-gradient line integrals use
 // the cell values split off (see k_momtum1): tr0 = the potential temperature
 // edgvar1 saw (thold), svsum = per-cell sums of sidevec_c.
 template <typename R>
 void launch_momtum(const Launch&, const Grid<R>&, const Strides&, const Knobs&, const MomtumScratch<R>&,
                    R* u, R* v, const R* exner, R* relvor, const R* u_edg, const R* v_edg,
                    const R* trc_edg, const R* mont_edg, const R* uvsq_edg, R* u_tndcy, R* v_tndcy,
-                   const R* dp3d, const double* mpd = nullptr, const R* tr0 = nullptr);
+                   const R* dp3d, const float2* mpf = nullptr, const R* tr0 = nullptr);
 template <typename R>
 struct HybgenScratch { R *exsmo, *exsmo2; };
 // one-time launch attributes of the hybgen kernels (shared-memory size);
@@ -220,7 +260,7 @@ void launch_hybgen(const Launch&, const Grid<R>&, const Strides&, const Knobs&, 
                    const R* targt, R* us3d, R* vs3d, R* tr3d, R* sdot, R* ex3d, R* dp3d, R* pr3d);
 template <typename R>
 void launch_hystat(const Launch&, const Grid<R>&, const Strides&, R* ph3d, const R* ex3d, R* mp3d,
-                   const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy, double* mpd = nullptr);
+                   const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy, float2* mpf = nullptr);
 // sums per member: [member][8 + T] doubles; partial buffer sized by globsum_partials()
 template <typename R>
 void launch_globsum(const Launch&, const Grid<R>&, const Strides&, const R* dp3d, const R* tr,
