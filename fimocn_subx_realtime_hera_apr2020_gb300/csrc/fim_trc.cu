@@ -25,7 +25,10 @@ template <typename R> __device__ __forceinline__ R tmax(R a, R b) { return a > b
 template <typename R> __device__ __forceinline__ R tmin(R a, R b) { return a < b ? a : b; }
 template <typename R> __device__ __forceinline__ R tabs(R a) { return a < R(0) ? -a : a; }
 
-constexpr int kTB = 256;
+// 128-thread blocks capped at 64 registers a thread: 32 warps resident per SM
+// keep enough loads in flight for these gather-heavy, latency-bound kernels
+constexpr int kTB = 128;
+constexpr int kTBMin = 8;
 inline unsigned tblocks(long long n) { return (unsigned)((n + kTB - 1) / kTB); }
 
 // VK consecutive levels per thread, moved with one 4/8/16-byte access
@@ -65,7 +68,7 @@ __device__ __forceinline__ void stv(R* p, const R (&r)[VK]) {
 
 // own-side least-squares edge values of tracers 1..T-1 (0-based), z = tracer
 template <typename R, int VK>
-__global__ void __launch_bounds__(kTB) k_tr_own(Grid<R> g, Strides s, const R* __restrict__ tracr,
+__global__ void __launch_bounds__(kTB, kTBMin) k_tr_own(Grid<R> g, Strides s, const R* __restrict__ tracr,
                                                 R* __restrict__ trc_edg) {
   const int L = g.L, N = g.N, LV = L / VK;
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -124,7 +127,7 @@ __device__ __forceinline__ bool clt(int N, int L, int nt, int& i, int& k, int& t
 
 // trcadv1 + the S+/S- sums of trcadv2 + copy of the old tracer
 template <typename R, int VK>
-__global__ void __launch_bounds__(kTB) k_tr_lo(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
+__global__ void __launch_bounds__(kTB, kTBMin) k_tr_lo(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     int t0, int nt, const R* __restrict__ massfx, const R* __restrict__ trc_edg, const R* __restrict__ tracr,
     const R* __restrict__ trcdp, R* __restrict__ trl_tdcy, const R* __restrict__ delp,
     R* __restrict__ trcr_lo, R* __restrict__ s_plus, R* __restrict__ s_mnus, R* __restrict__ trold,
@@ -202,7 +205,7 @@ __global__ void __launch_bounds__(kTB) k_tr_lo(Grid<R> g, Strides s, const StepP
 // max/min over the 1-ring of the old tracer and of trcr_lo (exact operations,
 // so any association gives the reference's values).
 template <typename R, int VK>
-__global__ void __launch_bounds__(kTB) k_tr_lim(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
+__global__ void __launch_bounds__(kTB, kTBMin) k_tr_lim(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     int t0, int nt, const R* __restrict__ trc_tdcy, const R* __restrict__ delp, const R* __restrict__ trold,
     const R* __restrict__ trcr_lo, const R* __restrict__ s_plus, const R* __restrict__ s_mnus,
     R* __restrict__ r_plus, R* __restrict__ r_mnus, size_t sc) {
@@ -255,7 +258,7 @@ __global__ void __launch_bounds__(kTB) k_tr_lim(Grid<R> g, Strides s, const Step
 
 // trcadv3: clip the recomputed antidiffusive fluxes, AB3 update, new tracer
 template <typename R, int VK>
-__global__ void __launch_bounds__(kTB) k_tr_hi(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
+__global__ void __launch_bounds__(kTB, kTBMin) k_tr_hi(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     int t0, int nt, const R* __restrict__ massfx, const R* __restrict__ trc_edg, R* __restrict__ tracr,
     R* __restrict__ trcdp, R* __restrict__ trc_tdcy, const R* __restrict__ trl_tdcy, const R* __restrict__ delp,
     const R* __restrict__ trold, const R* __restrict__ trcr_lo, const R* __restrict__ r_plus,
