@@ -509,7 +509,13 @@ struct RemapGeo {          // one coordinate (pressure or p^(kappa+1))
   R fo[ML], rfo[ML], rfn[ML];    // fco, 1/(fco+small), 1/(fcn+small)
   R hx[ML + 1], dsl[ML + 1], nd[ML + 1];  // interface k: (dx-1) or (1-dx), slab width, -delz
   int ly[ML + 1];                // donor layer of interface k
+  int thin;                      // some layer is thin enough for the massless-layer fill to matter
 };
+
+// pcwise's massless-layer fill moves y(k) by (y(k+-1) - y(k)) * 1e-22 / fco(k):
+// below the rounding of either precision unless fco(k) is under ~1e-4.
+template <typename R>
+__device__ __forceinline__ R fill_thin() { return R(1.2e-4); }
 
 template <typename R, int ML>
 struct RemapSm {
@@ -519,28 +525,22 @@ struct RemapSm {
   R dpcol[ML];
 };
 
-// PLM slope of layer lyr (pcwise remap_optn = 2); y has stride kTS
-template <typename R>
-__device__ __forceinline__ R plm_b(const R* y, int lyr, int kk) {
-  if (lyr < 1 || lyr > kk - 2) return R(0);
-  const R f = y[lyr * kTS], fm = y[(lyr - 1) * kTS], fp = y[(lyr + 1) * kTS];
-  const R d1 = f - fm, d2 = fp - f;
-  const R b = ((fp - fm) * (fm + fp - R(2) * f) > R(0)) ? d1 : d2;
-  return (f <= cmin(fm, fp) || f >= cmax(fm, fp)) ? R(0) : b;
-}
-
 // pcwise's coordinate quantities for xold -> xnew, lanes over levels
 template <typename R, int ML>
 __device__ void remap_geo(int L, int lane, const R* xold, const R* xnew, RemapGeo<R, ML>& G) {
   const R small = R(1.e-22);
   const bool flip = !(xold[0] < xold[L]);
+  bool thin = false;
   for (int k = lane; k < L; k += 32) {
     const R fo = flip ? cmax(R(0), (-xold[k + 1]) - (-xold[k])) : cmax(R(0), xold[k + 1] - xold[k]);
     const R fn = flip ? cmax(R(0), (-xnew[k + 1]) - (-xnew[k])) : cmax(R(0), xnew[k + 1] - xnew[k]);
     G.fo[k] = fo;
     G.rfo[k] = R(1) / (fo + small);
     G.rfn[k] = R(1) / (fn + small);
+    thin = thin || fo < fill_thin<R>();
   }
+  thin = __any_sync(0xffffffffu, thin);
+  if (lane == 0) G.thin = thin ? 1 : 0;
   __syncwarp();
   for (int k = lane; k <= L; k += 32) {
     const R d = flip ? (-xnew[k]) - (-xold[k]) : xnew[k] - xold[k];
@@ -563,18 +563,19 @@ __device__ void remap_geo(int L, int lane, const R* xold, const R* xnew, RemapGe
   }
 }
 
-// vertfx(k) of one field; 0 where no mass crosses interface k
-template <typename R, int ML>
-__device__ __forceinline__ R lane_flux(const R* y, const RemapGeo<R, ML>& G, int k, int kk) {
-  const R dsl = G.dsl[k];
-  const int lyr = G.ly[k];
-  const R a = y[lyr * kTS], b = plm_b(y, lyr, kk);
-  const R fcdx = a + b * R(.5) * G.hx[k];
-  const R amount = fcdx * dsl;
-  return dsl != R(0) ? G.nd[k] * amount / dsl : R(0);
+// PLM slope of a layer from its filled value f and its neighbours' fm, fp
+template <typename R>
+__device__ __forceinline__ R plm_slope(R fm, R f, R fp) {
+  const R b = ((fp - fm) * (fm + fp - R(2) * f) > R(0)) ? f - fm : fp - f;
+  return (f <= cmin(fm, fp) || f >= cmax(fm, fp)) ? R(0) : b;
 }
 
 // pcwise (PLM, miglim = 1) in place on one lane's tile column y (stride kTS).
+// The backward massless-layer fill is one pass (skipped for columns without
+// thin layers, where it only rounds); the forward fill, the PLM slopes, the
+// interface fluxes and the update are a second pass over a three-value window
+// held in registers, which writes slot k as soon as its new value is known
+// (later steps read only slots above k).
 // Returns true when the column-integral check fails (FP64 build only).
 template <typename R, int ML>
 __device__ bool pcwise_lane(int kk, R* y, const RemapGeo<R, ML>& G) {
@@ -586,30 +587,42 @@ __device__ bool pcwise_lane(int kk, R* y, const RemapGeo<R, ML>& G) {
       colscl = colscl + cabs(y[k * kTS] * G.fo[k]);
     }
   }
-  R nb = y[(kk - 1) * kTS];
-  for (int k = kk - 2; k >= 0; k--) {
-    nb = (y[k * kTS] * G.fo[k] + nb * small) * G.rfo[k];
-    y[k * kTS] = nb;
+  const bool fill = G.thin != 0;
+  if (fill) {
+    R nb = y[(kk - 1) * kTS];
+    for (int k = kk - 2; k >= 0; k--) {
+      nb = (y[k * kTS] * G.fo[k] + nb * small) * G.rfo[k];
+      y[k * kTS] = nb;
+    }
   }
-  nb = y[0];
-  for (int k = 1; k < kk; k++) {
-    nb = (y[k * kTS] * G.fo[k] + nb * small) * G.rfo[k];
-    y[k * kTS] = nb;
-  }
-  // flux and update in one pass; slot k-1 takes its new value once no later
-  // flux reads its old one
-  R after = R(0), vprev = R(0), pend = R(0);
+  // window: y0 = filled(k), y1 = filled(k+1); bk = slope of layer k
+  R y0 = y[0];
+  R y1 = fill ? (y[kTS] * G.fo[1] + y0 * small) * G.rfo[1] : y[kTS];
+  R bk = R(0);
+  R after = R(0), vprev = R(0);
   for (int k = 0; k < kk; k++) {
-    const R vnext = (k + 1 < kk) ? lane_flux<R, ML>(y, G, k + 1, kk) : R(0);
-    const R f = y[k * kTS];
-    const R amount = f * G.fo[k] - (vnext - vprev);
-    const R yn = (amount + f * small) * G.rfn[k];
+    R y2 = y1;
+    if (k + 2 < kk) {
+      y2 = y[(k + 2) * kTS];
+      if (fill) y2 = (y2 * G.fo[k + 2] + y1 * small) * G.rfo[k + 2];
+    }
+    const R bk1 = (k + 1 >= 1 && k + 1 <= kk - 2) ? plm_slope(y0, y1, y2) : R(0);
+    R vnext = R(0);
+    if (k + 1 < kk) {
+      const R dsl = G.dsl[k + 1];
+      const bool up = G.ly[k + 1] == k + 1;
+      const R a = up ? y1 : y0, b = up ? bk1 : bk;
+      // one donor layer: vertfx = -dz * (fcdx * slab) / slab = -dz * fcdx
+      vnext = dsl != R(0) ? G.nd[k + 1] * (a + b * R(.5) * G.hx[k + 1]) : R(0);
+    }
+    const R amount = y0 * G.fo[k] - (vnext - vprev);
     after = after + amount;
-    if (k > 0) y[(k - 1) * kTS] = pend;
-    pend = yn;
+    y[k * kTS] = (amount + y0 * small) * G.rfn[k];
+    y0 = y1;
+    y1 = y2;
+    bk = bk1;
     vprev = vnext;
   }
-  y[(kk - 1) * kTS] = pend;
   return sizeof(R) == 8 && cabs(bfore - after) > cmax(R(1.e-33), R(1.e-11) * colscl);
 }
 
