@@ -3,8 +3,9 @@
 Workload (default): glvl 8 (655,362 cells), nvl 64, 20 tracers + theta,
 dt 45 s (FIM's glvl-8 step; 72 s exceeds the scheme's stability limit),
 FP32-mixed, seeded synthetic balanced state; one "step" is one
-fused dycore step (abstart, edgvar1, edgvar3, cnuity, trcadv, momtum,
-hybgen + dffusn_lev, hystat, globsum) replayed as one CUDA graph.
+fused dyn_run iteration (hybgen + dffusn_lev and hystat of the previous step,
+abstart, edgvar1, edgvar3, cnuity, trcadv, momtum, globsum) replayed as one
+CUDA graph.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 

@@ -602,6 +602,15 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
   Grid<R>& g = grid_of<R>(c);
   const Strides& s = c->str;
   launch_step_begin(l, c->d_sp);
+  // dyn_run.F90:119-132: the step opens with hybgen and hystat of step its-1
+  // (skipped at a member's first step, after dyn_init's own adjustment)
+  Launch lb = l;
+  lb.boundary = 1;
+  HybgenScratch<R> hw{(R*)c->exsmo, (R*)c->exsmo2};
+  launch_hybgen<R>(lb, g, s, c->kn, hw, g.thetac, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_TR3D),
+                   F<R>(st, FIM_SDOT), F<R>(st, FIM_EX3D), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D));
+  launch_hystat<R>(lb, g, s, F<R>(st, FIM_PH3D), F<R>(st, FIM_EX3D), F<R>(st, FIM_MP3D), F<R>(st, FIM_DP3D),
+                   F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP), F<R>(st, FIM_PSRF), F<R>(st, FIM_PTDCY), st->mpf);
   launch_edgvar1<R>(l, g, s, c->kn.hi_order, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_DP3D),
                     F<R>(st, FIM_PR3D), F<R>(st, FIM_MP3D), F<R>(st, FIM_TR3D), F<R>(st, FIM_U_EDG),
                     F<R>(st, FIM_V_EDG), F<R>(st, FIM_DP_EDG), F<R>(st, FIM_LP_EDG), F<R>(st, FIM_MONT_EDG),
@@ -640,11 +649,7 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
                    F<R>(st, FIM_RELVOR), F<R>(st, FIM_U_EDG), F<R>(st, FIM_V_EDG), F<R>(st, FIM_TRC_EDG),
                    F<R>(st, FIM_MONT_EDG), F<R>(st, FIM_UVSQ_EDG), F<R>(st, FIM_U_TDCY), F<R>(st, FIM_V_TDCY),
                    F<R>(st, FIM_DP3D), st->mpf, (const R*)st->thold);
-  HybgenScratch<R> hw{(R*)c->exsmo, (R*)c->exsmo2};
-  launch_hybgen<R>(l, g, s, c->kn, hw, g.thetac, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_TR3D),
-                   F<R>(st, FIM_SDOT), F<R>(st, FIM_EX3D), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D));
-  launch_hystat<R>(l, g, s, F<R>(st, FIM_PH3D), F<R>(st, FIM_EX3D), F<R>(st, FIM_MP3D), F<R>(st, FIM_DP3D),
-                   F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP), F<R>(st, FIM_PSRF), F<R>(st, FIM_PTDCY), st->mpf);
+  // budgets of the state the step returns
   launch_globsum<R>(l, g, s, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), (const R*)nullptr, (const R*)nullptr,
                     F<R>(st, FIM_PR3D), F<R>(st, FIM_EX3D), (const R*)nullptr, c->gs_partial, st->sums);
   return FIM_OK;
@@ -1066,6 +1071,37 @@ int fim_member_set_active(fim_ctx* c, fim_state* st, int member, int active) {
 int fim_member_its(const fim_ctx* c, int member) {
   if (!c || member < 0 || member >= c->M) return -1;
   return c->h_sp[member].its;
+}
+
+int fim_member_get_step(const fim_ctx* c, int member, int* itsm1, int* nf, int* of, int* vof, double* ab1,
+                        double* ab2, double* ab3) {
+  if (!c || member < 0 || member >= c->M) return FIM_EINVAL;
+  const StepParams& p = c->h_sp[member];
+  if (itsm1) *itsm1 = p.its;
+  if (nf) *nf = p.nf + 1;
+  if (of) *of = p.of + 1;
+  if (vof) *vof = p.vof + 1;
+  if (ab1) *ab1 = p.ab1;
+  if (ab2) *ab2 = p.ab2;
+  if (ab3) *ab3 = p.ab3;
+  return FIM_OK;
+}
+
+int fim_member_set_step(fim_ctx* c, int member, int itsm1, int nf, int of, int vof, double ab1, double ab2,
+                        double ab3) {
+  if (!c || member < 0 || member >= c->M || itsm1 < 0 || nf < 1 || nf > 3 || of < 1 || of > 3 || vof < 1 ||
+      vof > 3)
+    return FIM_EINVAL;
+  StepParams& p = c->h_sp[member];
+  p.its = itsm1;
+  p.nf = nf - 1;
+  p.of = of - 1;
+  p.vof = vof - 1;
+  p.ab1 = ab1;
+  p.ab2 = ab2;
+  p.ab3 = ab3;
+  p.active = 1;
+  return push_sp(c);
 }
 
 static int run_step(fim_ctx* c, fim_state* st, int use_graph) {

@@ -331,19 +331,20 @@ __device__ bool pcwise(int kk, const R* xold, const R* yold, const R* xnew, R* y
 template <typename R, int ML>
 __global__ void __launch_bounds__(kColBlock) k_regrid(Grid<R> g, Strides s, Knobs kn,
     const StepParams* __restrict__ sp, const R* __restrict__ targt, const R* __restrict__ tr3d,
-    const R* __restrict__ ex3d, const R* __restrict__ pr3d, R* __restrict__ exsmo, int* __restrict__ flags) {
+    const R* __restrict__ ex3d, const R* __restrict__ pr3d, R* __restrict__ exsmo, int* __restrict__ flags,
+    int bnd) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int N = g.N, L = g.L, L1 = L + 1;
   if (i >= N) return;
   const size_t m = blockIdx.y;
   sp += m;
-  if (!sp->active) return;
+  if (!sp->active || (bnd && sp->its <= 1)) return;
   tr3d += m * s.tr; ex3d += m * s.intf; pr3d += m * s.intf; exsmo += m * s.intf;
   R thcol[ML], excol[ML + 1];
   for (int k = 0; k < L; k++) thcol[k] = tr3d[(size_t)i * L + k];
   for (int k = 0; k <= L; k++) excol[k] = ex3d[(size_t)i * L1 + k];
   int bad = 0;
-  regrid_1d<R, ML>(kn, targt, g.dpsig, L, sp->its, thcol, excol, pr3d[(size_t)i * L1], &bad);
+  regrid_1d<R, ML>(kn, targt, g.dpsig, L, sp->its - bnd, thcol, excol, pr3d[(size_t)i * L1], &bad);
   for (int k = 0; k <= L; k++) exsmo[(size_t)i * L1 + k] = excol[k];
   if (bad) atomicOr(flags + m, kFlagColumnIntegral);
 }
@@ -351,13 +352,15 @@ __global__ void __launch_bounds__(kColBlock) k_regrid(Grid<R> g, Strides s, Knob
 // dffusn_lev (dffusn.F90:37-58 with dffusn_lev.exe) on interfaces kbl+2..nvl,
 // out of place so every cell reads the unsmoothed neighbours.
 template <typename R>
-__global__ void __launch_bounds__(kBlock2) k_dffusn_lev(Grid<R> g, Strides s, int k1, int k2,
-    const R* __restrict__ fld, R* __restrict__ out) {
+__global__ void __launch_bounds__(kBlock2) k_dffusn_lev(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
+    int bnd, int k1, int k2, const R* __restrict__ fld, R* __restrict__ out) {
   const int N = g.N, L1 = g.L + 1;
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= N * L1) return;
   const int i = gid / L1, k = gid - i * L1;
   const size_t m = blockIdx.y;
+  sp += m;
+  if (!sp->active || (bnd && sp->its <= 1)) return;
   fld += m * s.intf; out += m * s.intf;
   const size_t c = (size_t)i * L1 + k;
   R val = fld[c];
@@ -380,16 +383,16 @@ template <typename R, int ML>
 __global__ void __launch_bounds__(kColBlock) k_remap(Grid<R> g, Strides s, Knobs kn,
     const StepParams* __restrict__ sp, const R* __restrict__ targt, const R* __restrict__ exsmo,
     R* __restrict__ us3d, R* __restrict__ vs3d, R* __restrict__ tr3d, R* __restrict__ sdot,
-    R* __restrict__ ex3d, R* __restrict__ dp3d, R* __restrict__ pr3d, int* __restrict__ flags) {
+    R* __restrict__ ex3d, R* __restrict__ dp3d, R* __restrict__ pr3d, int* __restrict__ flags, int bnd) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
   if (i >= N) return;
   const size_t m = blockIdx.y;
   sp += m;
-  if (!sp->active) return;
+  if (!sp->active || (bnd && sp->its <= 1)) return;
   exsmo += m * s.intf; us3d += m * s.cell; vs3d += m * s.cell; tr3d += m * s.tr; sdot += m * s.intf;
   ex3d += m * s.intf; dp3d += m * s.cell; pr3d += m * s.intf;
-  const int its = sp->its;
+  const int its = sp->its - bnd;
   const R cp = R(kCp), rd = R(kRd), p1000 = R(kP1000), small = R(1.e-6);
   R exold[ML + 1], exnew[ML + 1], prcol[ML + 1], prnew[ML + 1], pk1col[ML + 1], pk1new[ML + 1];
   R yold[ML], ynew[ML], dpcol[ML];
@@ -629,7 +632,7 @@ __device__ bool pcwise_lane(int kk, R* y, const RemapGeo<R, ML>& G) {
 // inflate (hybgen.F90:893-1007) of 32 columns per warp, lane = column
 template <typename R, int ML>
 __global__ void __launch_bounds__(32 * kWarpsInflate) k_inflate(Grid<R> g, Strides s, Knobs kn,
-    const StepParams* __restrict__ sp, const R* __restrict__ pr3d, R* __restrict__ exn) {
+    const StepParams* __restrict__ sp, const R* __restrict__ pr3d, R* __restrict__ exn, int bnd) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int N = g.N, L = g.L, L1 = L + 1;
@@ -637,7 +640,7 @@ __global__ void __launch_bounds__(32 * kWarpsInflate) k_inflate(Grid<R> g, Strid
   if (i0 >= N) return;
   const int ncol = (N - i0 < 32) ? N - i0 : 32;
   const size_t m = blockIdx.y;
-  if (!sp[m].active) return;
+  if (!sp[m].active || (bnd && sp[m].its <= 1)) return;
   pr3d += m * s.intf; exn += m * s.intf;
   R* col = reinterpret_cast<R*>(smraw) + (size_t)wib * (32 * (ML + 1) + 1);
   for (int q = lane; q < ncol * L1; q += 32) col[q] = exn[(size_t)i0 * L1 + q];
@@ -651,7 +654,7 @@ template <typename R, int ML>
 __global__ void __launch_bounds__(32 * kWarpsRemap) k_remap_w(Grid<R> g, Strides s, Knobs kn,
     const StepParams* __restrict__ sp, const R* __restrict__ targt, const R* __restrict__ exsmo,
     R* __restrict__ us3d, R* __restrict__ vs3d, R* __restrict__ tr3d, R* __restrict__ sdot,
-    R* __restrict__ ex3d, R* __restrict__ dp3d, R* __restrict__ pr3d, int* __restrict__ flags) {
+    R* __restrict__ ex3d, R* __restrict__ dp3d, R* __restrict__ pr3d, int* __restrict__ flags, int bnd) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
@@ -659,11 +662,11 @@ __global__ void __launch_bounds__(32 * kWarpsRemap) k_remap_w(Grid<R> g, Strides
   if (i >= N) return;
   const size_t m = blockIdx.y;
   sp += m;
-  if (!sp->active) return;
+  if (!sp->active || (bnd && sp->its <= 1)) return;
   RemapSm<R, ML>& S = reinterpret_cast<RemapSm<R, ML>*>(smraw)[wib];
   exsmo += m * s.intf; us3d += m * s.cell; vs3d += m * s.cell; tr3d += m * s.tr; sdot += m * s.intf;
   ex3d += m * s.intf; dp3d += m * s.cell; pr3d += m * s.intf;
-  const int its = sp->its;
+  const int its = sp->its - bnd;
   const R cp = R(kCp), rd = R(kRd), p1000 = R(kP1000), small = R(1.e-6);
   const size_t ci = (size_t)i * L1;
   for (int k = lane; k <= L; k += 32) {
@@ -818,18 +821,18 @@ template <typename R>
 __global__ void __launch_bounds__(kBlock2) k_hystat(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     R* __restrict__ ph3d, const R* __restrict__ ex3d, R* __restrict__ mp3d, const R* __restrict__ dp3d,
     R* __restrict__ tr3d, R* __restrict__ trdp, R* __restrict__ psrf, R* __restrict__ ptdcy,
-    float2* __restrict__ mpf) {
+    float2* __restrict__ mpf, int bnd) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
   if (warp >= N) return;
   const int i = warp;
   const size_t m = blockIdx.y;
   sp += m;
-  if (!sp->active) return;
+  if (!sp->active || (bnd && sp->its <= 1)) return;
   ph3d += m * s.intf; ex3d += m * s.intf; mp3d += m * s.cell; dp3d += m * s.cell; tr3d += m * s.tr;
   trdp += m * s.tr; psrf += m * s.col; ptdcy += m * 2 * s.col;
   if (mpf) mpf += m * s.cell;
-  const int its = sp->its;
+  const int its = sp->its - bnd;
   const size_t NL = (size_t)N * L;
   if constexpr (sizeof(R) == 4) {
     // float-float sums and scan (FP64-accurate on the FP32 pipes)
@@ -1115,10 +1118,12 @@ void launch_hybgen(const Launch& l, const Grid<R>& g, const Strides& s, const Kn
   dim3 gc(nblocks(g.N, kColBlock), l.members);
   if (g.L <= 64) {
     FIM_KBEGIN(l, "k_regrid");
-    k_regrid<R, 64><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, tr3d, ex3d, pr3d, w.exsmo, l.flags);
+    k_regrid<R, 64><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, tr3d, ex3d, pr3d, w.exsmo, l.flags,
+                                                     l.boundary);
   } else {
     FIM_KBEGIN(l, "k_regrid");
-    k_regrid<R, kMaxL><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, tr3d, ex3d, pr3d, w.exsmo, l.flags);
+    k_regrid<R, kMaxL><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, tr3d, ex3d, pr3d, w.exsmo,
+                                                        l.flags, l.boundary);
   }
   FIM_KEND(l);
   const R* ex_in = w.exsmo;
@@ -1126,7 +1131,8 @@ void launch_hybgen(const Launch& l, const Grid<R>& g, const Strides& s, const Kn
     dim3 gs(nblocks((long long)g.N * (g.L + 1), kBlock2), l.members);
     // Fortran levels kbl+2..nvl -> 0-based interfaces kbl+1..nvl-1
     FIM_KBEGIN(l, "k_dffusn_lev");
-    k_dffusn_lev<R><<<gs, kBlock2, 0, l.stream>>>(g, s, kn.kbl + 1, g.L - 1, w.exsmo, w.exsmo2);
+    k_dffusn_lev<R><<<gs, kBlock2, 0, l.stream>>>(g, s, l.sp, l.boundary, kn.kbl + 1, g.L - 1, w.exsmo,
+                                                   w.exsmo2);
     FIM_KEND(l);
     ex_in = w.exsmo2;
   }
@@ -1137,28 +1143,28 @@ void launch_hybgen(const Launch& l, const Grid<R>& g, const Strides& s, const Kn
       FIM_KBEGIN(l, "k_inflate");
       if (g.L <= 64)
         k_inflate<R, 64><<<gi, 32 * kWarpsInflate, inflate_smem<R, 64>(), l.stream>>>(g, s, kn, l.sp, pr3d,
-                                                                                      w.exsmo2);
+                                                                                      w.exsmo2, l.boundary);
       else
         k_inflate<R, kMaxL><<<gi, 32 * kWarpsInflate, inflate_smem<R, kMaxL>(), l.stream>>>(g, s, kn, l.sp, pr3d,
-                                                                                            w.exsmo2);
+                                                                                            w.exsmo2, l.boundary);
       FIM_KEND(l);
     }
     dim3 gw(nblocks(g.N, kWarpsRemap), l.members);
     FIM_KBEGIN(l, "k_remap");
     if (g.L <= 64)
       k_remap_w<R, 64><<<gw, 32 * kWarpsRemap, remap_w_smem<R, 64>(), l.stream>>>(
-          g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags);
+          g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags, l.boundary);
     else
       k_remap_w<R, kMaxL><<<gw, 32 * kWarpsRemap, remap_w_smem<R, kMaxL>(), l.stream>>>(
-          g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags);
+          g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags, l.boundary);
   } else if (g.L <= 64) {
     FIM_KBEGIN(l, "k_remap");
     k_remap<R, 64><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d,
-                                                    dp3d, pr3d, l.flags);
+                                                    dp3d, pr3d, l.flags, l.boundary);
   } else {
     FIM_KBEGIN(l, "k_remap");
     k_remap<R, kMaxL><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d,
-                                                       dp3d, pr3d, l.flags);
+                                                       dp3d, pr3d, l.flags, l.boundary);
   }
   FIM_KEND(l);
 }
@@ -1168,7 +1174,8 @@ void launch_hystat(const Launch& l, const Grid<R>& g, const Strides& s, R* ph3d,
                    const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy, float2* mpf) {
   dim3 gw(nblocks((long long)g.N * 32, kBlock2), l.members);
   FIM_KBEGIN(l, "k_hystat");
-  k_hystat<R><<<gw, kBlock2, 0, l.stream>>>(g, s, l.sp, ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy, mpf);
+  k_hystat<R><<<gw, kBlock2, 0, l.stream>>>(g, s, l.sp, ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy, mpf,
+                                             l.boundary);
   FIM_KEND(l);
 }
 

@@ -152,6 +152,10 @@ struct Launch {
   int* flags;          // device status word per member [members]
   long long* counter;  // host launch counter
   Prof* prof = nullptr;  // per-kernel event timing when enabled
+  // 1 for the column adjustment that opens a step (dyn_run's hybgen/hystat
+  // of step its-1): the column kernels then act for its-1 and skip a member
+  // at its first step, where dyn_init's adjustment stands in
+  int boundary = 0;
 };
 
 #define FIM_KBEGIN(l, name) do { if ((l).prof && (l).prof->on) (l).prof->begin(name, (l).stream); } while (0)

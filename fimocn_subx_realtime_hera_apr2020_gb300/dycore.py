@@ -249,6 +249,38 @@ class DycoreState:
     def member_its(self, member):
         return self.lib.fim_member_its(self.dyc.ctx, member)
 
+    def get_step(self, member=0):
+        """(itsm1, nf, of, vof, (adbash1, adbash2, adbash3)) of one member."""
+        v = [ctypes.c_int() for _ in range(4)] + [ctypes.c_double() for _ in range(3)]
+        _lib.check(self.lib.fim_member_get_step(self.dyc.ctx, member, *[ctypes.byref(x) for x in v]),
+                   "fim_member_get_step", self.dyc.ctx)
+        return v[0].value, v[1].value, v[2].value, v[3].value, (v[4].value, v[5].value, v[6].value)
+
+    def set_step(self, member, itsm1, nf, of, vof, adbash):
+        _lib.check(self.lib.fim_member_set_step(self.dyc.ctx, member, itsm1, nf, of, vof, *adbash),
+                   "fim_member_set_step", self.dyc.ctx)
+        self.its = itsm1
+
+    def save_restart(self, path, member=0, extras=None):
+        """Write one member's state as the dynamics section of a FIM restart
+        file (restart_io); returns itsm1."""
+        from .restart_io import STATE_FIELDS, write_restart
+        itsm1, nf, of, vof, ab = self.get_step(member)
+        fields = {n: self.download(n, member) for n in STATE_FIELDS}
+        write_restart(path, self.dyc.grid, self.dyc.cfg, itsm1, nf, of, vof, ab, fields, extras=extras)
+        return itsm1
+
+    def load_restart(self, path, member=0):
+        """Restore one member from a restart file; its next step is itsm1+1.
+        Returns the file's contents (restart_io.read_restart)."""
+        from .restart_io import read_restart
+        cfg = self.dyc.cfg
+        r = read_restart(path, self.dyc.grid.nip, cfg.nvl, cfg.ntra)
+        for n, a in r["fields"].items():
+            self.upload(n, a, member)
+        self.set_step(member, r["itsm1"], r["nf"], r["of"], r["vof"], r["adbash"])
+        return r
+
     def step_active(self, use_graph=True):
         """Advance every active member by one step (each at its own its)."""
         _lib.check(self.lib.fim_step_active(self.dyc.ctx, self.st, 1 if use_graph else 0), "fim_step_active",

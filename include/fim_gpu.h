@@ -256,8 +256,12 @@ int fim_state_download(fim_ctx *ctx, fim_state *st, int field, int member, void 
  * pressure/thickness from Exner, hystat(its=0), zero tendencies, AB3 slots */
 int fim_state_init(fim_ctx *ctx, fim_state *st);
 
-/* One dynamics step of every member in dyn_run order (dyn_run.F90:329-425
- * followed by hybgen/hystat/globsum of dyn_run.F90:119-150 for the same its).
+/* One dyn_run iteration of every member (dyn_run.F90:119-425): hybgen and
+ * hystat of step its-1 (from a member's second step on; dyn_init's stand in
+ * before the first), then abstart, edgvar1, edgvar3, cnuity or mass_adv,
+ * trcadv and momtum of step its, then the globsum budgets of the resulting
+ * state.  The state between calls is therefore the reference's state between
+ * dyn_run calls, which is what its restart files hold.
  * use_graph != 0 captures the step once as a CUDA graph and replays it. */
 int fim_step(fim_ctx *ctx, fim_state *st, int its, int use_graph);
 
@@ -269,6 +273,16 @@ int fim_step(fim_ctx *ctx, fim_state *st, int its, int use_graph);
 int fim_state_init_member(fim_ctx *ctx, fim_state *st, int member);
 int fim_member_set_active(fim_ctx *ctx, fim_state *st, int member, int active);
 int fim_member_its(const fim_ctx *ctx, int member);
+
+/* Step state of one member for restart files: the completed step count
+ * (itsm1, restart.F90:58), the AB3 slots nf/of/vof in Fortran numbering and
+ * the weights adbash1..3 (the first record of restart_dyn.F90:37/114).
+ * fim_member_set_step restores them and activates the member; its next step
+ * is itsm1+1 (restart.F90:125), with the weights abstart would carry on. */
+int fim_member_get_step(const fim_ctx *ctx, int member, int *itsm1, int *nf, int *of, int *vof,
+                        double *adbash1, double *adbash2, double *adbash3);
+int fim_member_set_step(fim_ctx *ctx, int member, int itsm1, int nf, int of, int vof,
+                        double adbash1, double adbash2, double adbash3);
 int fim_step_active(fim_ctx *ctx, fim_state *st, int use_graph);
 
 /* Member budgets after the last step (qmass, tracer integrals qtrcr(ntra)). */

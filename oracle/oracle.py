@@ -193,8 +193,14 @@ class Oracle:
         return s
 
     def step(self, s, its):
-        """dyn_run order for one step, hybgen/hystat/globsum of the same its last."""
+        """One dyn_run iteration (dyn_run.F90:119-425): hybgen and hystat of
+        step its-1 (from the second step on), then the horizontal dynamics of
+        step its; returns the budgets of the resulting state (globsum)."""
         self.abstart(its)
+        if its > 1:
+            self.hybgen(its - 1, s["us3d"], s["vs3d"], s["tr3d"], s["sdot"], s["ex3d"], s["dp3d"], s["pr3d"])
+            self.hystat(its - 1, s["ph3d"], s["ex3d"], s["mp3d"], s["dp3d"], s["tr3d"], s["trdp"], s["psrf"],
+                        s["ptdcy"])
         self.edgvar1(s["us3d"], s["vs3d"], s["dp3d"], s["pr3d"], s["ex3d"], s["ph3d"], s["mp3d"], s["tr3d"],
                      s["u_edg"], s["v_edg"], s["dp_edg"], s["lp_edg"], s["geop_edg"], s["mont_edg"], s["uvsq_edg"],
                      s["trc_edg"])
@@ -209,6 +215,4 @@ class Oracle:
         self.trcadv(s["trc_edg"], s["tr3d"], s["trdp"], s["trc_tdcy"], s["trl_tdcy"], s["massfx"], s["dp3d"])
         self.momtum(s["us3d"], s["vs3d"], s["ex3d"], s["relvor"], s["u_edg"], s["v_edg"], s["trc_edg"],
                     s["mont_edg"], s["uvsq_edg"], s["u_tdcy"], s["v_tdcy"], s["dp3d"])
-        self.hybgen(its, s["us3d"], s["vs3d"], s["tr3d"], s["sdot"], s["ex3d"], s["dp3d"], s["pr3d"])
-        self.hystat(its, s["ph3d"], s["ex3d"], s["mp3d"], s["dp3d"], s["tr3d"], s["trdp"], s["psrf"], s["ptdcy"])
         return self.globsum(s["dp3d"], s["tr3d"], s["pr3d"], s["ex3d"])
