@@ -15,7 +15,7 @@ STATUS_NAMES = {0: "FIM_OK", 1: "FIM_EINVAL", 2: "FIM_ENOMEM", 3: "FIM_ECUDA", 4
 
 FIELDS = ["us3d", "vs3d", "dp3d", "pr3d", "ex3d", "ph3d", "mp3d", "tr3d", "trdp", "u_tdcy", "v_tdcy",
           "dp_tdcy", "dpl_tdcy", "trc_tdcy", "trl_tdcy", "massfx", "ws3d", "sdot", "relvor", "psrf", "ptdcy",
-          "u_edg", "v_edg", "dp_edg", "lp_edg", "mont_edg", "uvsq_edg", "geop_edg", "trc_edg"]
+          "u_edg", "v_edg", "dp_edg", "lp_edg", "mont_edg", "uvsq_edg", "geop_edg", "trc_edg", "cumufx", "dpinit"]
 FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
 
 c_int_p = ctypes.POINTER(ctypes.c_int32)
@@ -40,7 +40,8 @@ class Config(ctypes.Structure):
                 ("veldff_bkgnd", ctypes.c_double), ("veldff_boost", ctypes.c_double),
                 ("biharm_frst", ctypes.c_int), ("biharm_last", ctypes.c_int), ("rleigh", ctypes.c_double),
                 ("rlthresh", ctypes.c_double), ("rltaper", ctypes.c_double), ("pure_sig", ctypes.c_int),
-                ("thetac", ctypes.c_void_p), ("dpsig", ctypes.c_void_p)]
+                ("thetac", ctypes.c_void_p), ("dpsig", ctypes.c_void_p), ("ntrb", ctypes.c_int),
+                ("dtratio", ctypes.c_int)]
 
 
 class Budget(ctypes.Structure):
@@ -91,6 +92,9 @@ _ROUTINES = {
     "fim_hybgen": [_VP, _I] + [_VP] * 8,
     "fim_hystat": [_VP, _I] + [_VP] * 8,
     "fim_globsum": [_VP, _I] + [_VP] * 9,
+    "fim_transp0": [_VP, _I] + [_VP] * 3,
+    "fim_transp1": [_VP, _I] + [_VP] * 2,
+    "fim_transp2": [_VP, _I] + [_VP] * 4,
 }
 for _name, _args in _ROUTINES.items():
     for _sfx in ("_r8", "_r4"):

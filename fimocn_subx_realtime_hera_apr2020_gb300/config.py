@@ -55,6 +55,8 @@ class FimConfig:
     rlthresh: float = 90.0
     rltaper: float = 0.4
     pure_sig: int = 0
+    ntrb: int = 0                   # class-B tracers (transported every dtratio steps by fct3d)
+    dtratio: int = 6
     thetac: np.ndarray = field(default=None, repr=False)
     dpsig: np.ndarray = field(default=None, repr=False)
 

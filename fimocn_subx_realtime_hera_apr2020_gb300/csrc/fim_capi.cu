@@ -69,6 +69,9 @@ struct fim_ctx {
        *f_rm = nullptr;
   int ftchunk = 0;
   int trc_vk = 0;  // levels per thread of the fused tracer kernels (0: widest that nvl allows)
+  int TB = 0, dtratio = 6;  // class-B tracers and their time-step ratio
+  void *cb_w = nullptr, *cb_F = nullptr, *cb_V = nullptr, *cb_fmx = nullptr, *cb_fmn = nullptr,
+       *cb_flo = nullptr, *cb_flp = nullptr, *cb_fln = nullptr;
   void *du = nullptr, *dv = nullptr, *wu = nullptr, *wv = nullptr;
   void *exsmo = nullptr, *exsmo2 = nullptr;
   double* gs_partial = nullptr;
@@ -312,8 +315,27 @@ int ensure_globsum(fim_ctx* c, int members) {
   if (c->gs_partial) return FIM_OK;
   int rc;
   if ((rc = dalloc(c, (void**)&c->gs_partial, globsum_partials(c->N, c->L, c->T, members) * sizeof(double)))) return rc;
-  if ((rc = dalloc(c, (void**)&c->gs_sums, (size_t)members * (8 + c->T) * sizeof(double)))) return rc;
+  if ((rc = dalloc(c, (void**)&c->gs_sums, (size_t)members * (8 + c->T + c->TB) * sizeof(double)))) return rc;
   return FIM_OK;
+}
+
+int ensure_classb(fim_ctx* c, int members) {
+  if (c->TB <= 0 || c->cb_w) return FIM_OK;
+  const size_t NL = (size_t)c->N * c->L * members, NB = NL * c->TB;
+  int rc;
+  if ((rc = ensure(c, &c->cb_w, NL))) return rc;
+  void** f[] = {&c->cb_F, &c->cb_V, &c->cb_fmx, &c->cb_fmn, &c->cb_flo, &c->cb_flp, &c->cb_fln};
+  for (void** p : f)
+    if ((rc = ensure(c, p, NB))) return rc;
+  const int e = c->prec == FIM_PREC_F64 ? prepare_classb<double>(c->L) : prepare_classb<float>(c->L);
+  if (e) return set_err(c, FIM_ECUDA, "class-B kernel attributes", (cudaError_t)e);
+  return FIM_OK;
+}
+
+template <typename R>
+ClassBScratch<R> classb_scratch(fim_ctx* c) {
+  return ClassBScratch<R>{(R*)c->cb_w, (R*)c->cb_F, (R*)c->cb_V, (R*)c->cb_fmx, (R*)c->cb_fmn, (R*)c->cb_flo,
+                          (R*)c->cb_flp, (R*)c->cb_fln};
 }
 
 // ---- host-pointer staging -------------------------------------------------
@@ -564,12 +586,12 @@ int globsum_impl(fim_ctx* c, const R* dp3d, const R* tr, const R* rn2d, const R*
                  const R* ex3d, const R* qf2d, double* qtrcr, fim_budget* out) {
   int rc = check_prec<R>(c);
   if (rc) return rc;
-  if (c->T > 32) return set_err(c, FIM_EINVAL, "globsum supports at most 32 tracers");
+  const int ntr = c->T + c->TB;
   if ((rc = ensure_globsum(c, c->M))) return rc;
   const size_t NL = (size_t)c->N * c->L, NI = (size_t)c->N * (c->L + 1);
   Stager s(c);
   const R* dp = s.map(dp3d, NL, 0);
-  const R* t = s.map(tr, NL * c->T, 0);
+  const R* t = s.map(tr, NL * ntr, 0);
   const R* rn = s.map(rn2d, (size_t)c->N, 0);
   const R* rcp = s.map(rc2d, (size_t)c->N, 0);
   const R* pr = s.map(pr3d, NI, 0);
@@ -577,18 +599,69 @@ int globsum_impl(fim_ctx* c, const R* dp3d, const R* tr, const R* rn2d, const R*
   const R* qf = s.map(qf2d, (size_t)c->N, 0);
   if (s.rc) return s.rc;
   if ((rc = push_sp(c))) return rc;
-  launch_globsum<R>(make_launch(c, 1), grid_of<R>(c), c->str, dp, t, rn, rcp, pr, ex, qf, c->gs_partial, c->gs_sums);
+  launch_globsum<R>(make_launch(c, 1), grid_of<R>(c), c->str, ntr, dp, t, rn, rcp, pr, ex, qf, c->gs_partial,
+                    c->gs_sums);
   if ((rc = check_launch(c, "globsum"))) return rc;
   if ((rc = s.finish())) return rc;
-  std::vector<double> h(8 + c->T);
+  std::vector<double> h(8 + ntr);
   CK(cudaMemcpyAsync(h.data(), c->gs_sums, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "globsum out");
   CK(cudaStreamSynchronize(c->stream), "globsum sync");
-  if (qtrcr) for (int q = 0; q < c->T; q++) qtrcr[q] = h[8 + q];
+  if (qtrcr) for (int q = 0; q < ntr; q++) qtrcr[q] = h[8 + q];
   if (out) {
     out->qmass = h[0]; out->qmsqv = h[1]; out->qmsqw = h[2]; out->qmso3 = h[3];
     out->qmste = h[4]; out->qmstr = h[5]; out->qmstrn = h[6]; out->qmstrc = h[7];
   }
   return FIM_OK;
+}
+
+template <typename R>
+int transp0_impl(fim_ctx* c, R* cumufx, const R* dp3d, R* dpinit) {
+  int rc = check_prec<R>(c);
+  if (rc) return rc;
+  const size_t NL = (size_t)c->N * c->L;
+  Stager s(c);
+  R* cu = s.map(cumufx, NL * 6, 2);
+  const R* dp = s.map(dp3d, NL, 0);
+  R* di = s.map(dpinit, NL, 2);
+  if (s.rc) return s.rc;
+  if ((rc = push_sp(c))) return rc;
+  launch_transp0<R>(make_launch(c, 1), grid_of<R>(c), c->str, 0, cu, dp, di);
+  if ((rc = check_launch(c, "transp0"))) return rc;
+  return s.finish();
+}
+
+template <typename R>
+int transp1_impl(fim_ctx* c, R* cumufx, const R* massfx) {
+  int rc = check_prec<R>(c);
+  if (rc) return rc;
+  const size_t NE = (size_t)c->N * c->L * 6;
+  Stager s(c);
+  R* cu = s.map(cumufx, NE, 1);
+  const R* mf = s.map(massfx, NE * 3, 0);
+  if (s.rc) return s.rc;
+  if ((rc = push_sp(c))) return rc;
+  launch_transp1<R>(make_launch(c, 1), grid_of<R>(c), c->str, cu, mf);
+  if ((rc = check_launch(c, "transp1"))) return rc;
+  return s.finish();
+}
+
+template <typename R>
+int transp2_impl(fim_ctx* c, R* tracr, const R* cumufx, const R* dpinit, const R* dpfinl) {
+  int rc = check_prec<R>(c);
+  if (rc) return rc;
+  if (c->TB <= 0) return FIM_OK;
+  if ((rc = ensure_classb(c, c->M))) return rc;
+  const size_t NL = (size_t)c->N * c->L;
+  Stager s(c);
+  R* tr = s.map(tracr, NL * (c->T + c->TB), 1);
+  const R* cu = s.map(cumufx, NL * 6, 0);
+  const R* di = s.map(dpinit, NL, 0);
+  const R* df = s.map(dpfinl, NL, 0);
+  if (s.rc) return s.rc;
+  if ((rc = push_sp(c))) return rc;
+  launch_transp2<R>(make_launch(c, 1), grid_of<R>(c), c->str, classb_scratch<R>(c), 0, c->TB, tr, cu, di, df);
+  if ((rc = check_launch(c, "transp2"))) return rc;
+  return s.finish();
 }
 
 // ---- fused step over the device-resident state ---------------------------
@@ -632,6 +705,14 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
     launch_massadv<R>(l, g, s, cw, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_U_EDG), F<R>(st, FIM_V_EDG),
                       F<R>(st, FIM_DP_EDG), F<R>(st, FIM_LP_EDG), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D),
                       F<R>(st, FIM_EX3D), F<R>(st, FIM_DP_TDCY), F<R>(st, FIM_MASSFX), F<R>(st, FIM_WS3D));
+  if (c->TB > 0) {
+    // class-B transport (dyn_run.F90:388-403); transp2/transp0 act at steps
+    // with mod(its, dtratio) == 0, decided per member on the device
+    launch_transp1<R>(l, g, s, F<R>(st, FIM_CUMUFX), F<R>(st, FIM_MASSFX));
+    launch_transp2<R>(l, g, s, classb_scratch<R>(c), c->dtratio, c->TB, F<R>(st, FIM_TR3D), F<R>(st, FIM_CUMUFX),
+                      F<R>(st, FIM_DPINIT), F<R>(st, FIM_DP3D));
+    launch_transp0<R>(l, g, s, c->dtratio, F<R>(st, FIM_CUMUFX), F<R>(st, FIM_DP3D), F<R>(st, FIM_DPINIT));
+  }
   if (c->kn.hi_order) {
     TrcFusedScratch<R> fw{(R*)c->f_trcr_lo, (R*)c->f_sp, (R*)c->f_sm, (R*)c->f_trold, (R*)c->f_rp, (R*)c->f_rm,
                           c->ftchunk, c->trc_vk};
@@ -650,7 +731,8 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
                    F<R>(st, FIM_MONT_EDG), F<R>(st, FIM_UVSQ_EDG), F<R>(st, FIM_U_TDCY), F<R>(st, FIM_V_TDCY),
                    F<R>(st, FIM_DP3D), st->mpf, (const R*)st->thold);
   // budgets of the state the step returns
-  launch_globsum<R>(l, g, s, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), (const R*)nullptr, (const R*)nullptr,
+  launch_globsum<R>(l, g, s, c->T + c->TB, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), (const R*)nullptr,
+                    (const R*)nullptr,
                     F<R>(st, FIM_PR3D), F<R>(st, FIM_EX3D), (const R*)nullptr, c->gs_partial, st->sums);
   return FIM_OK;
 }
@@ -664,6 +746,7 @@ int ensure_all(fim_ctx* c) {
   if ((rc = ensure_momtum(c, c->M))) return rc;
   if ((rc = ensure_hybgen(c, c->M))) return rc;
   if ((rc = ensure_globsum(c, c->M))) return rc;
+  if ((rc = ensure_classb(c, c->M))) return rc;
   return FIM_OK;
 }
 
@@ -693,6 +776,8 @@ int state_init_impl(fim_ctx* c, fim_state* st, int m0, int nm) {
   CK(cudaMemsetAsync(P(FIM_PTDCY), 0, nm * st->count[FIM_PTDCY] * c->esz, c->stream), "zero ptdcy");
   launch_hystat<R>(l, g, c->str, P(FIM_PH3D), P(FIM_EX3D), P(FIM_MP3D), P(FIM_DP3D), P(FIM_TR3D), P(FIM_TRDP),
                    P(FIM_PSRF), P(FIM_PTDCY), st->mpf ? st->mpf + (size_t)m0 * st->count[FIM_MP3D] : nullptr);
+  if (c->TB > 0)  // dyn_init.F90:1096-1097
+    launch_transp0<R>(l, g, c->str, 0, P(FIM_CUMUFX), P(FIM_DP3D), P(FIM_DPINIT));
   const int zero[] = {FIM_U_TDCY, FIM_V_TDCY, FIM_DP_TDCY, FIM_DPL_TDCY, FIM_TRC_TDCY, FIM_TRL_TDCY, FIM_MASSFX};
   for (int f : zero) CK(cudaMemsetAsync(P(f), 0, nm * st->count[f] * c->esz, c->stream), "zero tendencies");
   for (int m = m0; m < m0 + nm; m++) reset_member(c, m);
@@ -718,6 +803,7 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
   if (cfg->pure_sig) return FIM_ENOTSUP;
   if (cfg->remap_optn < 1 || cfg->remap_optn > 3) return FIM_EINVAL;
   if (cfg->precision != FIM_PREC_F64 && cfg->precision != FIM_PREC_F32) return FIM_EINVAL;
+  if (cfg->ntrb < 0 || cfg->ntra + cfg->ntrb > 32 || (cfg->ntrb > 0 && cfg->dtratio < 1)) return FIM_EINVAL;
   if (!cfg->thetac || !cfg->dpsig || !g->prox || !g->proxs || !g->nprox || !g->area || !g->cs || !g->sn ||
       !g->sidevec_c || !g->sidevec_e || !g->sideln || !g->hfcoef || !g->lat)
     return FIM_EINVAL;
@@ -732,7 +818,9 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
   c->M = cfg->members < 1 ? 1 : cfg->members;
   c->thetac.assign(cfg->thetac, cfg->thetac + c->L);
   c->dpsig.assign(cfg->dpsig, cfg->dpsig + c->L);
-  c->str = make_strides(c->N, c->L, c->T);
+  c->TB = cfg->ntrb;
+  c->dtratio = cfg->dtratio;
+  c->str = make_strides(c->N, c->L, c->T, c->TB);
   // FIM_TRC_VK=1|2|4 pins the levels per thread of the fused tracer kernels
   if (const char* v = getenv("FIM_TRC_VK")) c->trc_vk = atoi(v);
   const int N = c->N, L = c->L;
@@ -977,26 +1065,53 @@ int fim_globsum_r4(fim_ctx* c, int its, const float* dp3d, const float* tr, cons
   return globsum_impl<float>(c, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d, qtrcr, out);
 }
 
+int fim_transp0_r8(fim_ctx* c, int its, double* cumufx, const double* dp3d, double* dpinit) {
+  (void)its;
+  return transp0_impl<double>(c, cumufx, dp3d, dpinit);
+}
+int fim_transp0_r4(fim_ctx* c, int its, float* cumufx, const float* dp3d, float* dpinit) {
+  (void)its;
+  return transp0_impl<float>(c, cumufx, dp3d, dpinit);
+}
+int fim_transp1_r8(fim_ctx* c, int its, double* cumufx, const double* massfx) {
+  (void)its;
+  return transp1_impl<double>(c, cumufx, massfx);
+}
+int fim_transp1_r4(fim_ctx* c, int its, float* cumufx, const float* massfx) {
+  (void)its;
+  return transp1_impl<float>(c, cumufx, massfx);
+}
+int fim_transp2_r8(fim_ctx* c, int its, double* tracr, const double* cumufx, const double* dpinit,
+                   const double* dpfinl) {
+  (void)its;
+  return transp2_impl<double>(c, tracr, cumufx, dpinit, dpfinl);
+}
+int fim_transp2_r4(fim_ctx* c, int its, float* tracr, const float* cumufx, const float* dpinit,
+                   const float* dpfinl) {
+  (void)its;
+  return transp2_impl<float>(c, tracr, cumufx, dpinit, dpfinl);
+}
+
 // ---- state ------------------------------------------------------------------
 int fim_state_alloc(fim_ctx* c, fim_state** out) {
   if (!c || !out) return FIM_EINVAL;
   fim_state* st = new (std::nothrow) fim_state;
   if (!st) return FIM_ENOMEM;
-  const size_t N = c->N, L = c->L, T = c->T, NL = N * L, NI = N * (L + 1);
+  const size_t N = c->N, L = c->L, T = c->T, TB = c->TB, NL = N * L, NI = N * (L + 1);
   const size_t cnt[FIM_NFIELDS] = {
-      NL, NL, NL, NI, NI, NI, NL, NL * T,          // us vs dp pr ex ph mp tr
-      NL * T, NL * 3, NL * 3, NL * 3, NL * 3,      // trdp u_tdcy v_tdcy dp_tdcy dpl_tdcy
+      NL, NL, NL, NI, NI, NI, NL, NL * (T + TB),   // us vs dp pr ex ph mp tr
+      NL * (T + TB), NL * 3, NL * 3, NL * 3, NL * 3,  // trdp u_tdcy v_tdcy dp_tdcy dpl_tdcy
       NL * 3 * T, NL * 3 * T, NL * 6 * 3,          // trc_tdcy trl_tdcy massfx
       NL, NI, NL, N, N * 2,                        // ws sdot relvor psrf ptdcy
       NL * 6, NL * 6, NL * 6, NL * 6, NL * 6, NL * 6, NL * 6,  // edge fields
-      NL * 6 * T};
+      NL * 6 * T, NL * 6, NL};                     // trc_edg cumufx dpinit
   for (int f = 0; f < FIM_NFIELDS; f++) {
     st->count[f] = cnt[f];
     int rc = dalloc(c, &st->f[f], cnt[f] * c->M * c->esz);
     if (rc) { delete st; return rc; }
     cudaMemsetAsync(st->f[f], 0, cnt[f] * c->M * c->esz, c->stream);
   }
-  int rc = dalloc(c, (void**)&st->sums, (size_t)c->M * (8 + c->T) * sizeof(double));
+  int rc = dalloc(c, (void**)&st->sums, (size_t)c->M * (8 + c->T + c->TB) * sizeof(double));
   if (rc) { delete st; return rc; }
   if (c->prec == FIM_PREC_F32) {
     if ((rc = dalloc(c, (void**)&st->mpf, (size_t)c->M * cnt[FIM_MP3D] * sizeof(float2)))) { delete st; return rc; }
@@ -1157,11 +1272,12 @@ int fim_step_active(fim_ctx* c, fim_state* st, int use_graph) {
 
 int fim_state_budget(fim_ctx* c, fim_state* st, int member, double* qtrcr, fim_budget* out) {
   if (!c || !st || member < 0 || member >= c->M) return FIM_EINVAL;
-  std::vector<double> h(8 + c->T);
-  CK(cudaMemcpyAsync(h.data(), st->sums + (size_t)member * (8 + c->T), h.size() * sizeof(double),
+  const int ntr = c->T + c->TB;
+  std::vector<double> h(8 + ntr);
+  CK(cudaMemcpyAsync(h.data(), st->sums + (size_t)member * (8 + ntr), h.size() * sizeof(double),
                      cudaMemcpyDeviceToHost, c->stream), "budget");
   CK(cudaStreamSynchronize(c->stream), "budget sync");
-  if (qtrcr) for (int q = 0; q < c->T; q++) qtrcr[q] = h[8 + q];
+  if (qtrcr) for (int q = 0; q < ntr; q++) qtrcr[q] = h[8 + q];
   if (out) {
     out->qmass = h[0]; out->qmsqv = h[1]; out->qmsqw = h[2]; out->qmso3 = h[3];
     out->qmste = h[4]; out->qmstr = h[5]; out->qmstrn = h[6]; out->qmstrc = h[7];

@@ -988,10 +988,10 @@ template <> struct GsVec<double, 2> {
 
 template <typename R, int VK>
 __global__ void __launch_bounds__(kBlock2) k_globsum_levels(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
-    const R* __restrict__ dp3d, const R* __restrict__ tr, const R* __restrict__ rn2d, const R* __restrict__ rc2d,
+    int T, const R* __restrict__ dp3d, const R* __restrict__ tr, const R* __restrict__ rn2d, const R* __restrict__ rc2d,
     const R* __restrict__ pr3d, const R* __restrict__ ex3d, const R* __restrict__ qf2d,
     double* __restrict__ partial) {
-  const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
+  const int N = g.N, L = g.L, L1 = L + 1;
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active) return;
@@ -1185,22 +1185,22 @@ size_t globsum_partials(int N, int L, int T, int members) {
 }
 
 template <typename R>
-void launch_globsum(const Launch& l, const Grid<R>& g, const Strides& s, const R* dp3d, const R* tr,
+void launch_globsum(const Launch& l, const Grid<R>& g, const Strides& s, int ntr, const R* dp3d, const R* tr,
                     const R* rn2d, const R* rc2d, const R* pr3d, const R* ex3d, const R* qf2d,
                     double* partial, double* sums) {
-  dim3 gl(kGsBlocks, l.members, (g.T + 1 + kGsGroup - 1) / kGsGroup);
+  dim3 gl(kGsBlocks, l.members, (ntr + 1 + kGsGroup - 1) / kGsGroup);
   FIM_KBEGIN(l, "k_globsum_levels");
   constexpr int VK = sizeof(R) == 4 ? 4 : 2;
   const bool vec = g.L % VK == 0 && (uintptr_t)dp3d % (VK * sizeof(R)) == 0 && (uintptr_t)tr % (VK * sizeof(R)) == 0;
   if (vec)
-    k_globsum_levels<R, VK><<<gl, kBlock2, 0, l.stream>>>(g, s, l.sp, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d,
+    k_globsum_levels<R, VK><<<gl, kBlock2, 0, l.stream>>>(g, s, l.sp, ntr, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d,
                                                           partial);
   else
-    k_globsum_levels<R, 1><<<gl, kBlock2, 0, l.stream>>>(g, s, l.sp, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d,
+    k_globsum_levels<R, 1><<<gl, kBlock2, 0, l.stream>>>(g, s, l.sp, ntr, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d,
                                                          partial);
   FIM_KEND(l);
   FIM_KBEGIN(l, "k_globsum_final");
-  k_globsum_final<R><<<l.members, kBlock2, 0, l.stream>>>(l.sp, g.T, partial, kGsBlocks, sums);
+  k_globsum_final<R><<<l.members, kBlock2, 0, l.stream>>>(l.sp, ntr, partial, kGsBlocks, sums);
   FIM_KEND(l);
 }
 
@@ -1218,7 +1218,7 @@ void launch_prdp_from_ex(const Launch& l, const Grid<R>& g, const Strides& s, co
                                  const HybgenScratch<R>&, const R*, R*, R*, R*, R*, R*, R*, R*);            \
   template void launch_hystat<R>(const Launch&, const Grid<R>&, const Strides&, R*, const R*, R*, const R*, \
                                  R*, R*, R*, R*, float2*);                                                  \
-  template void launch_globsum<R>(const Launch&, const Grid<R>&, const Strides&, const R*, const R*,        \
+  template void launch_globsum<R>(const Launch&, const Grid<R>&, const Strides&, int, const R*, const R*,        \
                                   const R*, const R*, const R*, const R*, const R*, double*, double*);      \
   template void launch_prdp_from_ex<R>(const Launch&, const Grid<R>&, const Strides&, const R*, R*, R*);
 INSTANTIATE(float)

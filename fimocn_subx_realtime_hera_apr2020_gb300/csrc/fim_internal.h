@@ -85,20 +85,21 @@ struct Strides {
   size_t intf;   // (L+1)*N
   size_t edge;   // 6*L*N
   size_t ab;     // 3*L*N
-  size_t tr;     // T*L*N
+  size_t tr;     // (T+TB)*L*N: tr3d and trdp
   size_t trab;   // 3*T*L*N
   size_t tredg;  // 6*T*L*N
   size_t mf;     // 3*6*L*N
   size_t col;    // N
 };
 
-inline Strides make_strides(int N, int L, int T) {
+// T class-A tracers (edges, tendencies); tr3d/trdp also hold TB class-B ones
+inline Strides make_strides(int N, int L, int T, int TB = 0) {
   Strides s;
   s.cell = (size_t)L * N;
   s.intf = (size_t)(L + 1) * N;
   s.edge = (size_t)6 * L * N;
   s.ab = (size_t)3 * L * N;
-  s.tr = (size_t)T * L * N;
+  s.tr = (size_t)(T + TB) * L * N;
   s.trab = (size_t)3 * T * L * N;
   s.tredg = (size_t)6 * T * L * N;
   s.mf = (size_t)18 * L * N;
@@ -265,9 +266,25 @@ void launch_hybgen(const Launch&, const Grid<R>&, const Strides&, const Knobs&, 
 template <typename R>
 void launch_hystat(const Launch&, const Grid<R>&, const Strides&, R* ph3d, const R* ex3d, R* mp3d,
                    const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy, float2* mpf = nullptr);
-// sums per member: [member][8 + T] doubles; partial buffer sized by globsum_partials()
+// class-B transport (fim_trb.cu); scratch per member: w (nvl x nip), the
+// other fields (nvl x nip x ntrb)
 template <typename R>
-void launch_globsum(const Launch&, const Grid<R>&, const Strides&, const R* dp3d, const R* tr,
+struct ClassBScratch { R *w, *F, *V, *fmx, *fmn, *flo, *flp, *fln; };
+template <typename R>
+void launch_transp1(const Launch&, const Grid<R>&, const Strides&, R* cumufx, const R* massfx);
+// every > 0: only members at a step its with its % every == 0
+template <typename R>
+void launch_transp0(const Launch&, const Grid<R>&, const Strides&, int every, R* cumufx, const R* dp3d,
+                    R* dpinit);
+template <typename R>
+void launch_transp2(const Launch&, const Grid<R>&, const Strides&, const ClassBScratch<R>&, int every, int ntrb,
+                    R* tracr, const R* cumufx, const R* dpinit, const R* dpfinl);
+template <typename R>
+int prepare_classb(int L);
+// sums per member: [member][8 + T] doubles; partial buffer sized by globsum_partials()
+// ntr: tracers summed (class A and B); sums per member: [member][8 + ntr]
+template <typename R>
+void launch_globsum(const Launch&, const Grid<R>&, const Strides&, int ntr, const R* dp3d, const R* tr,
                     const R* rn2d, const R* rc2d, const R* pr3d, const R* ex3d, const R* qf2d,
                     double* partial, double* sums);
 size_t globsum_partials(int N, int L, int T, int members);

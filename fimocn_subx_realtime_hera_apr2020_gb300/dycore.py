@@ -40,6 +40,7 @@ class Dycore:
                    "fim_ctx_create")
         self.ctx = ctx
         self.N, self.L, self.T = grid.nip, cfg.nvl, cfg.ntra
+        self.TB = cfg.ntrb
         self._sfx = "_r8" if cfg.precision == "f64" else "_r4"
 
     def close(self):
@@ -164,8 +165,17 @@ class Dycore:
     def hystat(self, its, ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy):
         self._call("fim_hystat", its, *map(_ptr, (ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy)))
 
+    def transp0(self, its, cumufx, dp3d, dpinit):
+        self._call("fim_transp0", its, *map(_ptr, (cumufx, dp3d, dpinit)))
+
+    def transp1(self, its, cumufx, massfx):
+        self._call("fim_transp1", its, *map(_ptr, (cumufx, massfx)))
+
+    def transp2(self, its, tracr, cumufx, dpinit, dpfinl):
+        self._call("fim_transp2", its, *map(_ptr, (tracr, cumufx, dpinit, dpfinl)))
+
     def globsum(self, its, dp3d, tr, pr3d, ex3d, rn2d=None, rc2d=None, qf2d=None):
-        qtrcr = np.zeros(self.T, np.float64)
+        qtrcr = np.zeros(self.T + self.TB, np.float64)
         b = _lib.Budget()
         self._call("fim_globsum", its, *map(_ptr, (dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d)), qtrcr.ctypes.data,
                    ctypes.byref(b))
@@ -275,7 +285,7 @@ class DycoreState:
         Returns the file's contents (restart_io.read_restart)."""
         from .restart_io import read_restart
         cfg = self.dyc.cfg
-        r = read_restart(path, self.dyc.grid.nip, cfg.nvl, cfg.ntra)
+        r = read_restart(path, self.dyc.grid.nip, cfg.nvl, cfg.ntra, cfg.ntrb)
         for n, a in r["fields"].items():
             self.upload(n, a, member)
         self.set_step(member, r["itsm1"], r["nf"], r["of"], r["vof"], r["adbash"])
@@ -287,7 +297,7 @@ class DycoreState:
                    self.dyc.ctx)
 
     def budget(self, member=0):
-        qtrcr = np.zeros(self.dyc.T, np.float64)
+        qtrcr = np.zeros(self.dyc.T + self.dyc.TB, np.float64)
         b = _lib.Budget()
         _lib.check(self.lib.fim_state_budget(self.dyc.ctx, self.st, member, qtrcr.ctypes.data, ctypes.byref(b)),
                    "fim_state_budget", self.dyc.ctx)

@@ -25,10 +25,12 @@ logicals are 4 bytes; the scalar records' reals have the build's default
 kind (4 bytes for FIM's -r4 dynamics, `real_bytes`), the array records are
 always real*4 (readarr32_r.F90, writearr32_r.F90).
 
-Fields that belong to the physics or the class-B transport (sst, ice, rain,
-tk3d, rh3d, dpinit, cumufx, ...) are written as zeros unless given in
-`extras`, and returned in `extras` when read.  Only the dynamics section is
-written; reading stops after it, so a full reference restart file is read.
+Fields that belong to the physics (sst, ice, rain, tk3d, rh3d, ...) are
+written as zeros unless given in `extras`, and returned in `extras` when
+read.  Class-B tracers (cfg.ntrb) follow the class-A ones; their AB3
+tendency records, which the class-B transport does not use, are zeros.
+Only the dynamics section is written; reading stops after it, so a full
+reference restart file is read.
 
 Between fim_step calls the library state is the reference's state between
 dyn_run calls, so a restart file written here resumes the same forecast
@@ -43,10 +45,11 @@ _R4 = np.dtype("<f4")
 
 # dynamics fields of the library state that the restart file carries
 STATE_FIELDS = ["u_tdcy", "v_tdcy", "dp_tdcy", "dpl_tdcy", "tr3d", "trdp", "trc_tdcy", "trl_tdcy", "us3d",
-                "vs3d", "ws3d", "mp3d", "dp3d", "relvor", "pr3d", "ex3d", "ph3d", "sdot", "massfx", "psrf", "ptdcy"]
+                "vs3d", "ws3d", "mp3d", "dp3d", "relvor", "pr3d", "ex3d", "ph3d", "sdot", "massfx", "psrf", "ptdcy",
+                "dpinit", "cumufx"]
 _SFC = ["sst_prev", "sst_next", "fice2d_prev", "fice2d_next", "fice2d"]
 _REC6 = ["rn2d", "pw2d", "rc2d", "u10m", "v10m", "runoff"]
-_CELL_EXTRA = ["tk3d", "rh3d", "dpinit"]
+_CELL_EXTRA = ["tk3d", "rh3d"]
 
 
 def _rec(fh, *parts):
@@ -92,15 +95,16 @@ def _f(a, dtype):
     return np.ascontiguousarray(a, dtype=dtype).tobytes()
 
 
-def write_restart(path, grid, cfg, itsm1, nf, of, vof, adbash, fields, extras=None, nvlsig=None, real_bytes=4,
-                  ntrb=0):
+def write_restart(path, grid, cfg, itsm1, nf, of, vof, adbash, fields, extras=None, nvlsig=None, real_bytes=4):
     """Write the dynamics section of a restart file.
 
     `fields`: flat arrays in the library / reference layout (STATE_FIELDS;
-    tracers and their tendencies for ntra + ntrb tracers).  nf/of/vof are in
-    Fortran numbering; adbash = (adbash1, adbash2, adbash3).
+    tr3d and trdp for ntra + ntrb tracers, the tendencies for ntra).  nf/of/vof
+    are in Fortran numbering; adbash = (adbash1, adbash2, adbash3).
     """
-    nip, nvl, ntra = grid.nip, cfg.nvl, cfg.ntra + ntrb
+    nip, nvl = grid.nip, cfg.nvl
+    nta = cfg.ntra
+    ntra = nta + getattr(cfg, "ntrb", 0)
     nvlsig = nvl if nvlsig is None else nvlsig
     ex = dict(extras or {})
     rdt = np.dtype("<f%d" % real_bytes)
@@ -132,8 +136,8 @@ def write_restart(path, grid, cfg, itsm1, nf, of, vof, adbash, fields, extras=No
             _rec(fh, slab("tr3d", t))
             _rec(fh, slab("trdp", t))
             for n in range(3):
-                _rec(fh, slab("trc_tdcy", t * 3 + n))
-                _rec(fh, slab("trl_tdcy", t * 3 + n))
+                for name in ("trc_tdcy", "trl_tdcy"):
+                    _rec(fh, slab(name, t * 3 + n) if t < nta else _f(z(cell), _R4))
         for name in ("us3d", "vs3d", "ws3d", "mp3d", "tk3d", "dp3d", "rh3d", "relvor", "dpinit"):
             src = fields if name in fields else ex
             _rec(fh, _f(np.asarray(src.get(name, z(cell))).reshape(-1)[:cell], _R4))
@@ -141,7 +145,8 @@ def write_restart(path, grid, cfg, itsm1, nf, of, vof, adbash, fields, extras=No
             _rec(fh, slab(name, 0, (nvl + 1) * nip))
         for n in range(3):
             _rec(fh, slab("massfx", n, 6 * cell))
-        _rec(fh, _f(np.asarray(ex.get("cumufx", z(6 * cell))).reshape(-1), _R4))
+        src = fields if "cumufx" in fields else ex
+        _rec(fh, _f(np.asarray(src.get("cumufx", z(6 * cell))).reshape(-1), _R4))
 
 
 def read_restart(path, nip, nvl, ntra, ntrb=0, nvlsig=None, real_bytes=4):
@@ -216,8 +221,10 @@ def read_restart(path, nip, nvl, ntra, ntrb=0, nvlsig=None, real_bytes=4):
             tr.append(arr(cell))
             td.append(arr(cell))
             for n in range(3):
-                tc.append(arr(cell))
-                tl.append(arr(cell))
+                a, b = arr(cell), arr(cell)
+                if t < ntra:  # class-B tendency records carry nothing the transport uses
+                    tc.append(a)
+                    tl.append(b)
         fields["tr3d"], fields["trdp"] = np.concatenate(tr), np.concatenate(td)
         fields["trc_tdcy"], fields["trl_tdcy"] = np.concatenate(tc), np.concatenate(tl)
         for name in ("us3d", "vs3d", "ws3d", "mp3d", "tk3d", "dp3d", "rh3d", "relvor", "dpinit"):
@@ -225,5 +232,5 @@ def read_restart(path, nip, nvl, ntra, ntrb=0, nvlsig=None, real_bytes=4):
         for name in ("pr3d", "ex3d", "ph3d", "sdot"):
             fields[name] = arr((nvl + 1) * nip)
         fields["massfx"] = np.concatenate([arr(6 * cell) for _ in range(3)])
-        extras["cumufx"] = arr(6 * cell)
+        fields["cumufx"] = arr(6 * cell)
     return {"itsm1": itsm1, "nf": nf, "of": of, "vof": vof, "adbash": adbash, "fields": fields, "extras": extras}

@@ -5,7 +5,8 @@ dyn_init.F90:826), which is not in the tree: a hydrostatically balanced
 column per cell with surface pressure 1000 hPa + N(0, sigma_ps), layer
 thicknesses proportional to dpsig, potential temperature rising linearly
 from 300 K to 600 K, zonal wind 35 m/s cos(lat) (+ optional N(0, noise) on
-u and v), tracers 2..ntra drawn U[0, 1e-2], flat topography.  Arrays are
+u and v), tracers 2..ntra and the ntrb class-B tracers drawn U[0, 1e-2],
+flat topography.  Arrays are
 flat in the reference layout (level index fastest).  The start-up hybgen and
 hystat of dyn_init run afterwards on the device (fim_state_init).
 """
@@ -17,7 +18,7 @@ P1000 = 100000.0
 
 
 def synthetic_state(grid, cfg, seed, sigma_ps=200.0, noise=0.0, dtype=np.float64):
-    N, L, T = grid.nip, cfg.nvl, cfg.ntra
+    N, L, T = grid.nip, cfg.nvl, cfg.ntra + getattr(cfg, "ntrb", 0)
     rng = np.random.Generator(np.random.PCG64(seed))
     ps = P1000 + rng.standard_normal(N) * sigma_ps
     dps = cfg.dpsig / cfg.dpsig.sum()

@@ -90,6 +90,9 @@ typedef struct fim_config {
   int pure_sig;            /* [0]; 1 is not supported (FIM_ENOTSUP) */
   const double *thetac;    /* thetac(nvl): hybgen target potential temperature */
   const double *dpsig;     /* dpsig(nvl): minimum layer thickness, Pa */
+  int ntrb;                /* [0] class-B tracers, stored after the ntra class-A ones
+                              (tracer slots ntra+1..ntra+ntrb); ntra+ntrb <= 32 */
+  int dtratio;             /* [6] class-B / class-A time-step ratio (fimnamelist.F90:87) */
 } fim_config;
 
 typedef struct fim_ctx fim_ctx;
@@ -218,6 +221,24 @@ int fim_hystat_r8(fim_ctx *ctx, int its, double *ph3d, const double *ex3d, doubl
 int fim_hystat_r4(fim_ctx *ctx, int its, float *ph3d, const float *ex3d, float *mp3d,
                   const float *dp3d, float *tr3d, float *trdp, float *psrf, float *ptdcy);
 
+/* Class-B tracer transport (module_transp3d, FIMsrc/fim/horizontal/transp3d.F90).
+ * transp0 (transp3d.F90:21): cumufx = 0, dpinit = dp3d.
+ * transp1 (transp3d.F90:43): cumufx += adbash1..3 x massfx(nf,of,vof), with the
+ *   AB3 slots and weights of the context (fim_abstart / fim_set_ab).
+ * transp2 (transp3d.F90:82, fct3d.F90:4): vertical mass flux from the
+ *   time-integrated continuity equation, then 3-D FCT transport of the class-B
+ *   tracers, the slots ntra+1..ntra+ntrb of tracr (nvl,nip,ntra+ntrb).
+ * fim_step calls transp1 after cnuity/mass_adv every step and transp2 and
+ * transp0 at steps its with mod(its,dtratio) == 0 (dyn_run.F90:388-403). */
+int fim_transp0_r8(fim_ctx *ctx, int its, double *cumufx, const double *dp3d, double *dpinit);
+int fim_transp0_r4(fim_ctx *ctx, int its, float *cumufx, const float *dp3d, float *dpinit);
+int fim_transp1_r8(fim_ctx *ctx, int its, double *cumufx, const double *massfx);
+int fim_transp1_r4(fim_ctx *ctx, int its, float *cumufx, const float *massfx);
+int fim_transp2_r8(fim_ctx *ctx, int its, double *tracr, const double *cumufx, const double *dpinit,
+                   const double *dpfinl);
+int fim_transp2_r4(fim_ctx *ctx, int its, float *tracr, const float *cumufx, const float *dpinit,
+                   const float *dpfinl);
+
 /* FIMsrc/fim/horizontal/globsum.F90:39; rn2d, rc2d, qf2d may be NULL (zero);
  * qtrcr(ntra) and the budget are double in both families */
 int fim_globsum_r8(fim_ctx *ctx, int its, const double *dp3d, const double *tr,
@@ -238,10 +259,13 @@ enum fim_field {
   FIM_TRDP, FIM_U_TDCY, FIM_V_TDCY, FIM_DP_TDCY, FIM_DPL_TDCY, FIM_TRC_TDCY, FIM_TRL_TDCY,
   FIM_MASSFX, FIM_WS3D, FIM_SDOT, FIM_RELVOR, FIM_PSRF, FIM_PTDCY,
   FIM_U_EDG, FIM_V_EDG, FIM_DP_EDG, FIM_LP_EDG, FIM_MONT_EDG, FIM_UVSQ_EDG, FIM_GEOP_EDG,
-  FIM_TRC_EDG, FIM_NFIELDS
+  FIM_TRC_EDG, FIM_CUMUFX, FIM_DPINIT, FIM_NFIELDS
 };
 
-/* After a fused step the edge work fields are in the step's internal form:
+/* tr3d and trdp of a state hold ntra+ntrb tracers; cumufx (nvl,6,nip) and
+ * dpinit (nvl,nip) are the class-B transport's flux integral and initial
+ * thickness (module_variables.F90:27,89).
+ * After a fused step the edge work fields are in the step's internal form:
  * trc_edg of tracers 2..ntra holds the own-side reconstructions (edgvar3
  * loop 1) and, in an FP32 context, mont_edg holds edge-minus-cell values. */
 int fim_state_alloc(fim_ctx *ctx, fim_state **out);

@@ -1176,7 +1176,8 @@ void orc_hystat(const orc_ctx *c, int its, double *ph3d, const double *ex3d, dou
 void orc_globsum(const orc_ctx *c, const double *dp3d, const double *tr, const double *rn2d,
                  const double *rc2d, const double *pr3d, const double *ex3d,
                  const double *qf2d, double *qtrcr, double *sums8) {
-  const int N = c->nip, L = c->nvl, L1 = c->nvl + 1, T = c->ntra;
+  /* qtrcr covers the class-A and class-B tracers (dyn_run.F90:80) */
+  const int N = c->nip, L = c->nvl, L1 = c->nvl + 1, T = c->ntra + c->ntrb;
   double summ = 0., smqv = 0., smqw = 0., smo3 = 0., sumr = 0., sume = 0., sumrc = 0., sumrn = 0.;
   for (int t = 0; t < T; t++) qtrcr[t] = 0.;
   for (int ipn = 0; ipn < N; ipn++) {
@@ -1217,4 +1218,220 @@ void orc_prdp_from_ex(const orc_ctx *c, const double *ex3d, double *pr3d, double
       dp3d[C2(k, ipn)] = pr3d[(size_t)ipn * L1 + k] - pr3d[(size_t)ipn * L1 + k + 1];
     }
   }
+}
+
+/* ------------------------------------------------------------------------
+ * Class-B tracer transport (module_transp3d, transp3d.F90:21-241, with
+ * module_fct3d, fct3d.F90:4-482).  Class-B tracers occupy the tracer slots
+ * ntra .. ntra+ntrb-1 (0-based) after the class-A ones; cumufx is an edge
+ * field, dpinit a cell field.
+ * ------------------------------------------------------------------------ */
+
+/* transp0 (transp3d.F90:21-40) */
+void orc_transp0(const orc_ctx *c, double *cumufx, const double *dp3d, double *dpinit) {
+  const int N = c->nip, L = c->nvl;
+  for (size_t q = 0; q < (size_t)N * 6 * L; q++) cumufx[q] = 0.;
+  for (size_t q = 0; q < (size_t)N * L; q++) dpinit[q] = dp3d[q];
+}
+
+/* transp1 (transp3d.F90:43-79): time integral of the mass fluxes */
+void orc_transp1(const orc_ctx *c, double *cumufx, const double *massfx) {
+  const int N = c->nip, L = c->nvl;
+#pragma omp parallel for schedule(static)
+  for (int ico = 0; ico < N; ico++)
+    for (int edg = 0; edg < c->nprox[ico]; edg++)
+      for (int k = 0; k < L; k++)
+        cumufx[E3(k, edg, ico)] = cumufx[E3(k, edg, ico)] + c->ab1 * massfx[MF(k, edg, ico, c->nf)] +
+                                  c->ab2 * massfx[MF(k, edg, ico, c->of)] +
+                                  c->ab3 * massfx[MF(k, edg, ico, c->vof)];
+}
+
+/* fct3d (fct3d.F90:4-482) for tracer slots frst..last (0-based, inclusive):
+ * u = time-integrated edge mass fluxes, w = time-integrated vertical mass
+ * flux (w(k) > 0: mass from layer k to k+1), thko/thkn = old/new thickness.
+ * diagno and recovr are off, as transp2 calls it. */
+static void fct3d(const orc_ctx *c, double *fields, int frst, int last, const double *u, const double *w,
+                  const double *thko, const double *thkn) {
+  const int N = c->nip, L = c->nvl;
+  const double athird = 1. / 3., epsil = 1.e-11, onemu = 1.e-6;
+  double *fld = malloc(sizeof(double) * N * L), *vertfx = malloc(sizeof(double) * N * L);
+  double *vertdv = malloc(sizeof(double) * N * L), *fmx = malloc(sizeof(double) * N * L);
+  double *fmn = malloc(sizeof(double) * N * L), *flp = malloc(sizeof(double) * N * L);
+  double *fln = malloc(sizeof(double) * N * L), *flx = malloc(sizeof(double) * N * 6 * L);
+  double *uan = malloc(sizeof(double) * N * 6 * L);
+  for (int n = frst; n <= last; n++) {
+    /* vertical flux by summing fld over the upstream slab of thickness w */
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < N; i++) {
+      double *f = fld + (size_t)i * L;
+      const double *to = thko + (size_t)i * L;
+      for (int k = 0; k < L; k++) f[k] = fields[T3(k, i, n)];
+      /* fill massless cells with data from the layer above or below */
+      for (int k = L - 2; k >= 0; k--) f[k] = (f[k] * to[k] + f[k + 1] * onemu) / (to[k] + onemu);
+      for (int k = 1; k < L; k++) f[k] = (f[k] * to[k] + f[k - 1] * onemu) / (to[k] + onemu);
+    }
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < N; i++) {
+      const double *f = fld + (size_t)i * L, *to = thko + (size_t)i * L, *wc = w + (size_t)i * L;
+      double *a = malloc(sizeof(double) * L), *b = malloc(sizeof(double) * L), *cc = malloc(sizeof(double) * L);
+      a[0] = f[0]; b[0] = 0.; cc[0] = 0.;
+      a[L - 1] = f[L - 1]; b[L - 1] = 0.; cc[L - 1] = 0.;
+      /* piecewise parabolic fit (fct3d.F90:185-214) */
+      for (int k = 1; k < L - 1; k++) {
+        const double dxlft = dmax(epsil, to[k - 1]), dxmid = dmax(epsil, to[k]), dxrgt = dmax(epsil, to[k + 1]);
+        const double yl = (dxlft * f[k] + dxmid * f[k - 1]) / (dxlft + dxmid);
+        const double yr = (dxrgt * f[k] + dxmid * f[k + 1]) / (dxrgt + dxmid);
+        a[k] = 1.5 * f[k] - .25 * (yl + yr);
+        b[k] = yr - yl;
+        cc[k] = 6. * (.5 * (yl + yr) - f[k]);
+        if (fabs(yr - yl) < 6. * fabs(.5 * (yl + yr) - f[k])) {
+          if (fabs(yr - yl) > 2. * fabs(.5 * (yl + yr) - f[k])) {
+            if ((yr - yl) * (.5 * (yl + yr) - f[k]) > 0.) {
+              a[k] = .25 * (3. * f[k] + yl);
+              cc[k] = 3. * (f[k] - yl);
+              b[k] = cc[k];
+            } else {
+              a[k] = .25 * (3. * f[k] + yr);
+              cc[k] = 3. * (f[k] - yr);
+              b[k] = -cc[k];
+            }
+          } else {
+            a[k] = f[k];
+            b[k] = 0.;
+            cc[k] = 0.;
+          }
+        }
+      }
+      double *vf = vertfx + (size_t)i * L;
+      for (int k = 0; k < L - 1; k++) {
+        double slab = onemu, amount = 0.;
+        if (wc[k] < 0.) { /* interface moves up */
+          amount = slab * f[k + 1];
+          int kp = k;
+          for (;;) {
+            kp++;
+            if (slab >= -wc[k]) break;
+            if (to[kp] > 0.) {
+              const double dslab = dmin(slab + to[kp], -wc[k]) - dmin(slab, -wc[k]);
+              const double dx = dslab / to[kp];
+              const double fcdx = a[kp] + b[kp] * .5 * (dx - 1.) + cc[kp] * (.25 - dx * (.5 - dx * athird));
+              amount = amount + fcdx * dslab;
+              slab = slab + dslab;
+            }
+            if (!(kp < L - 1)) break;
+          }
+        } else if (wc[k] > 0.) { /* interface moves down */
+          amount = slab * f[k];
+          int kp = k + 1;
+          for (;;) {
+            kp--;
+            if (slab >= wc[k]) break;
+            if (to[kp] > 0.) {
+              const double dslab = dmin(slab + to[kp], wc[k]) - dmin(slab, wc[k]);
+              const double dx = dslab / to[kp];
+              const double fcdx = a[kp] + b[kp] * .5 * (1. - dx) + cc[kp] * (.25 - dx * (.5 - dx * athird));
+              amount = amount + fcdx * dslab;
+              slab = slab + dslab;
+            }
+            if (!(kp > 1)) break; /* fct3d.F90:253: the walk stops above layer 1 */
+          }
+        }
+        vf[k] = wc[k] * amount / slab;
+      }
+      vf[L - 1] = 0.; /* no flux through the top */
+      double *vd = vertdv + (size_t)i * L;
+      vd[0] = vf[0];
+      for (int k = 1; k < L; k++) vd[k] = vf[k] - vf[k - 1];
+      free(a); free(b); free(cc);
+    }
+    /* low-order and antidiffusive fluxes, local bounds (fct3d.F90:281-320) */
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < N; i++) {
+      for (int k = 0; k < L; k++) {
+        double mx = fld[C2(k, i)], mn = fld[C2(k, i)];
+        for (int edg = 0; edg < c->nprox[i]; edg++) {
+          const int ix = c->prox[i * 6 + edg], edx = c->proxs[i * 6 + edg];
+          const double ue = u[E3(k, edg, i)], ux = u[E3(k, edx, ix)];
+          flx[E3(k, edg, i)] = 0.5 * ((ue + fabs(ue)) * fld[C2(k, i)] - (ux + fabs(ux)) * fld[C2(k, ix)]);
+          const double q = .5 * (fld[C2(k, i)] + fld[C2(k, ix)]);
+          uan[E3(k, edg, i)] = q * ue - flx[E3(k, edg, i)];
+          mx = dmax(mx, fld[C2(k, ix)]);
+          mn = dmin(mn, fld[C2(k, ix)]);
+        }
+        if (k < L - 1 && w[C2(k, i)] < 0.) {
+          mx = dmax(mx, vertfx[C2(k, i)] / w[C2(k, i)]);
+          mn = dmin(mn, vertfx[C2(k, i)] / w[C2(k, i)]);
+        }
+        if (k > 0 && w[C2(k - 1, i)] > 0.) {
+          mx = dmax(mx, vertfx[C2(k - 1, i)] / w[C2(k - 1, i)]);
+          mn = dmin(mn, vertfx[C2(k - 1, i)] / w[C2(k - 1, i)]);
+        }
+        fmx[C2(k, i)] = mx;
+        fmn[C2(k, i)] = mn;
+      }
+    }
+    /* low-order update, then the limiter ratios (fct3d.F90:322-355) */
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < N; i++) {
+      for (int k = 0; k < L; k++) {
+        double hordiv = 0.;
+        for (int edg = 0; edg < c->nprox[i]; edg++) hordiv = hordiv + flx[E3(k, edg, i)];
+        hordiv = hordiv * c->rarea[i];
+        const size_t ck = C2(k, i);
+        const double q = fld[ck] * thko[ck] - hordiv - vertdv[ck];
+        const double amount = dmax(0., dmax(fmn[ck] * thkn[ck], dmin(q, fmx[ck] * thkn[ck])));
+        fld[ck] = (fld[ck] * onemu + amount) / (onemu + thkn[ck]);
+      }
+      for (int k = 0; k < L; k++) {
+        double totin = 0., totou = 0.;
+        for (int edg = 0; edg < c->nprox[i]; edg++) {
+          totin = totin - dmin(0., uan[E3(k, edg, i)]);
+          totou = totou + dmax(0., uan[E3(k, edg, i)]);
+        }
+        const size_t ck = C2(k, i);
+        flp[ck] = (fmx[ck] - fld[ck]) * thkn[ck] / (totin + epsil) * c->rarea[i];
+        fln[ck] = (fld[ck] - fmn[ck]) * thkn[ck] / (totou + epsil) * c->rarea[i];
+      }
+    }
+    /* limit the antidiffusive fluxes (fct3d.F90:368-389) */
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < N; i++) {
+      for (int k = 0; k < L; k++) {
+        double hordiv = 0.;
+        for (int edg = 0; edg < c->nprox[i]; edg++) {
+          const int ix = c->prox[i * 6 + edg];
+          double clip;
+          if (uan[E3(k, edg, i)] >= 0.) clip = dmin(1., dmin(fln[C2(k, i)], flp[C2(k, ix)]));
+          else clip = dmin(1., dmin(flp[C2(k, i)], fln[C2(k, ix)]));
+          hordiv = hordiv + uan[E3(k, edg, i)] * clip;
+        }
+        hordiv = hordiv * c->rarea[i];
+        const size_t ck = C2(k, i);
+        const double q = fld[ck] * thkn[ck] - hordiv;
+        const double amount = dmax(0., dmax(fmn[ck] * thkn[ck], dmin(q, fmx[ck] * thkn[ck])));
+        fields[T3(k, i, n)] = (fld[ck] * onemu + amount) / (onemu + thkn[ck]);
+      }
+    }
+  }
+  free(fld); free(vertfx); free(vertdv); free(fmx); free(fmn); free(flp); free(fln); free(flx); free(uan);
+}
+
+/* transp2 (transp3d.F90:82-241): the vertical mass flux that closes the
+ * time-integrated continuity equation, then fct3d for the class-B tracers */
+void orc_transp2(const orc_ctx *c, int ntrb, double *tracr, const double *cumufx, const double *dpinit,
+                 const double *dpfinl) {
+  const int N = c->nip, L = c->nvl;
+  if (ntrb <= 0) return;
+  double *w = malloc(sizeof(double) * N * L);
+#pragma omp parallel for schedule(static)
+  for (int ico = 0; ico < N; ico++) {
+    for (int k = 0; k < L; k++) {
+      double hordiv = 0.;
+      for (int edg = 0; edg < c->nprox[ico]; edg++) hordiv = hordiv + cumufx[E3(k, edg, ico)];
+      const double vertdv = (dpinit[C2(k, ico)] - dpfinl[C2(k, ico)]) - hordiv * c->rarea[ico];
+      w[C2(k, ico)] = k == 0 ? vertdv : w[C2(k - 1, ico)] + vertdv;
+    }
+  }
+  fct3d(c, tracr, c->ntra, c->ntra + ntrb - 1, cumufx, w, dpinit, dpfinl);
+  free(w);
 }

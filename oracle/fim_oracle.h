@@ -42,6 +42,7 @@ typedef struct orc_ctx {
   int nf, of, vof;                      /* 0-based AB3 slots */
   double ab1, ab2, ab3;
   long diag_flags;                      /* conservation-check failures seen */
+  int ntrb;                             /* class-B tracers after the ntra class-A ones */
 } orc_ctx;
 
 void orc_derived(int nip, int nvl, int kbl, double dt, double intfc_smooth,
@@ -79,6 +80,12 @@ void orc_hystat(const orc_ctx *c, int its, double *ph3d, const double *ex3d, dou
 void orc_globsum(const orc_ctx *c, const double *dp3d, const double *tr, const double *rn2d,
                  const double *rc2d, const double *pr3d, const double *ex3d,
                  const double *qf2d, double *qtrcr, double *sums8);
+/* class-B tracer transport (transp3d.F90:21-241, fct3d.F90:4-482); class-B
+ * tracers are the slots ntra..ntra+ntrb-1 of tracr; cumufx is an edge field */
+void orc_transp0(const orc_ctx *c, double *cumufx, const double *dp3d, double *dpinit);
+void orc_transp1(const orc_ctx *c, double *cumufx, const double *massfx);
+void orc_transp2(const orc_ctx *c, int ntrb, double *tracr, const double *cumufx, const double *dpinit,
+                 const double *dpfinl);
 /* pressure and thickness from Exner after the start-up hybgen (dyn_init.F90:895-906) */
 void orc_prdp_from_ex(const orc_ctx *c, const double *ex3d, double *pr3d, double *dp3d);
 

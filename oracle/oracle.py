@@ -30,7 +30,7 @@ class OrcCtx(ctypes.Structure):
                 ("dfflen_max", ctypes.c_double),
                 ("nf", ctypes.c_int), ("of", ctypes.c_int), ("vof", ctypes.c_int),
                 ("ab1", ctypes.c_double), ("ab2", ctypes.c_double), ("ab3", ctypes.c_double),
-                ("diag_flags", ctypes.c_long)]
+                ("diag_flags", ctypes.c_long), ("ntrb", ctypes.c_int)]
 
 
 _lib = None
@@ -62,6 +62,9 @@ def load():
             "orc_globsum": [P] * 10,
             "orc_prdp_from_ex": [P] * 4,
             "orc_set_threads": [I],
+            "orc_transp0": [P] * 4,
+            "orc_transp1": [P] * 3,
+            "orc_transp2": [P, I, P, P, P, P],
         }
         for name, args in sigs.items():
             fn = getattr(lib, name)
@@ -115,8 +118,10 @@ class Oracle:
         c.dfflen, c.biharw, c.smoo_coeff = _p(self.dfflen), _p(self.biharw), _p(self.smoo)
         c.dfflen_max = dmax.value
         c.nf, c.of, c.vof = -1, 1, 0
+        c.ntrb = cfg.ntrb
         self.c = c
         self.N, self.L, self.T = N, L, cfg.ntra
+        self.TB = cfg.ntrb
 
     @property
     def diag_flags(self):
@@ -158,12 +163,21 @@ class Oracle:
         self.lib.orc_hystat(ctypes.byref(self.c), its, *map(_p, (ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy)))
 
     def globsum(self, dp3d, tr, pr3d, ex3d, rn2d=None, rc2d=None, qf2d=None):
-        qtrcr = np.zeros(self.T)
+        qtrcr = np.zeros(self.T + self.TB)
         sums = np.zeros(8)
         self.lib.orc_globsum(ctypes.byref(self.c), _p(dp3d), _p(tr), _p(rn2d), _p(rc2d), _p(pr3d), _p(ex3d),
                              _p(qf2d), _p(qtrcr), _p(sums))
         names = ["qmass", "qmsqv", "qmsqw", "qmso3", "qmste", "qmstr", "qmstrn", "qmstrc"]
         return qtrcr, dict(zip(names, sums))
+
+    def transp0(self, cumufx, dp3d, dpinit):
+        self.lib.orc_transp0(ctypes.byref(self.c), _p(cumufx), _p(dp3d), _p(dpinit))
+
+    def transp1(self, cumufx, massfx):
+        self.lib.orc_transp1(ctypes.byref(self.c), _p(cumufx), _p(massfx))
+
+    def transp2(self, tracr, cumufx, dpinit, dpfinl):
+        self.lib.orc_transp2(ctypes.byref(self.c), self.TB, _p(tracr), _p(cumufx), _p(dpinit), _p(dpfinl))
 
     def prdp_from_ex(self, ex3d, pr3d, dp3d):
         self.lib.orc_prdp_from_ex(ctypes.byref(self.c), _p(ex3d), _p(pr3d), _p(dp3d))
@@ -172,7 +186,7 @@ class Oracle:
     def new_state(self, fields):
         N, L, T = self.N, self.L, self.T
         z = lambda n: np.zeros(n)  # noqa: E731
-        s = dict(trdp=z(T * N * L), u_tdcy=z(3 * N * L), v_tdcy=z(3 * N * L), dp_tdcy=z(3 * N * L),
+        s = dict(trdp=z((T + self.TB) * N * L), cumufx=z(6 * N * L), dpinit=z(N * L), u_tdcy=z(3 * N * L), v_tdcy=z(3 * N * L), dp_tdcy=z(3 * N * L),
                  dpl_tdcy=z(3 * N * L), trc_tdcy=z(3 * T * N * L), trl_tdcy=z(3 * T * N * L),
                  massfx=z(18 * N * L), ws3d=z(N * L), sdot=z(N * (L + 1)), relvor=z(N * L), psrf=z(N),
                  ptdcy=z(2 * N), u_edg=z(6 * N * L), v_edg=z(6 * N * L), dp_edg=z(6 * N * L),
@@ -189,6 +203,8 @@ class Oracle:
         s["psrf"][:] = 0.0
         s["ptdcy"][:] = 0.0
         self.hystat(0, s["ph3d"], s["ex3d"], s["mp3d"], s["dp3d"], s["tr3d"], s["trdp"], s["psrf"], s["ptdcy"])
+        if self.TB > 0:
+            self.transp0(s["cumufx"], s["dp3d"], s["dpinit"])  # dyn_init.F90:1096-1097
         self.c.nf, self.c.of, self.c.vof = -1, 1, 0
         return s
 
@@ -212,6 +228,11 @@ class Oracle:
         else:
             self.mass_adv(s["us3d"], s["vs3d"], s["u_edg"], s["v_edg"], s["dp_edg"], s["lp_edg"], s["dp3d"],
                           s["pr3d"], s["ex3d"], s["dp_tdcy"], s["massfx"], s["ws3d"])
+        if self.TB > 0:  # class-B transport (dyn_run.F90:388-403)
+            self.transp1(s["cumufx"], s["massfx"])
+            if its % self.cfg.dtratio == 0:
+                self.transp2(s["tr3d"], s["cumufx"], s["dpinit"], s["dp3d"])
+                self.transp0(s["cumufx"], s["dp3d"], s["dpinit"])
         self.trcadv(s["trc_edg"], s["tr3d"], s["trdp"], s["trc_tdcy"], s["trl_tdcy"], s["massfx"], s["dp3d"])
         self.momtum(s["us3d"], s["vs3d"], s["ex3d"], s["relvor"], s["u_edg"], s["v_edg"], s["trc_edg"],
                     s["mont_edg"], s["uvsq_edg"], s["u_tdcy"], s["v_tdcy"], s["dp3d"])

@@ -15,7 +15,8 @@ def _fields(grid, cfg, seed=3):
     sizes = dict(u_tdcy=3 * N * L, v_tdcy=3 * N * L, dp_tdcy=3 * N * L, dpl_tdcy=3 * N * L, tr3d=T * N * L,
                  trdp=T * N * L, trc_tdcy=3 * T * N * L, trl_tdcy=3 * T * N * L, us3d=N * L, vs3d=N * L,
                  ws3d=N * L, mp3d=N * L, dp3d=N * L, relvor=N * L, pr3d=N * (L + 1), ex3d=N * (L + 1),
-                 ph3d=N * (L + 1), sdot=N * (L + 1), massfx=18 * N * L, psrf=N, ptdcy=2 * N)
+                 ph3d=N * (L + 1), sdot=N * (L + 1), massfx=18 * N * L, psrf=N, ptdcy=2 * N, dpinit=N * L,
+                 cumufx=6 * N * L)
     assert set(sizes) == set(STATE_FIELDS)
     return {k: rng.standard_normal(n).astype(np.float32) for k, n in sizes.items()}
 
