@@ -399,6 +399,104 @@ def serve_arm(args, ws, rank, local):
         print(json.dumps(line))
 
 
+ACC_FIELDS = ["us3d", "vs3d", "dp3d", "pr3d", "ex3d", "ph3d", "mp3d", "tr3d", "trdp"]
+
+
+def accuracy_arm(args, ws, rank, local):
+    """Error of the GPU paths after 1..K steps on one seeded state.
+
+    Reference: the FP64 CPU oracle (workloads up to glvl 6), or the FP64 GPU
+    path (glvl 8, where the oracle would take hours).  Per field: relative L2
+    and max |error|; global mass drift (qmass / qmass(step 0) - 1) and the
+    minimum over tracers 2..ntra of each run."""
+    import torch
+    import fimocn_subx_realtime_hera_apr2020_gb300 as F
+
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    wl = F.WORKLOADS[args.workload]
+    glvl, L, T = wl["glvl"], args.nvl or 64, wl["ntra"]
+    if args.workload.startswith("glvl4"):
+        L = 38
+    grid = F.Grid.cached(glvl)
+    N = grid.nip
+    K = args.accuracy
+    marks = sorted({m for m in (1, 10, 50, 100, K) if m <= K})
+    use_oracle = glvl <= 6
+    mk = lambda prec: F.FimConfig(nvl=L, ntra=T, dt=wl["dt"], precision=prec)  # noqa: E731
+    host = F.synthetic_state(grid, mk("f64"), seed=wl["seed"], sigma_ps=wl["sigma_ps"], noise=wl["noise"])
+    runs = {}
+    for prec in ("f64", "f32"):
+        d = F.Dycore(grid, mk(prec))
+        st = d.state()
+        st.load({k: v.astype(mk(prec).dtype) for k, v in host.items()})
+        st.init()
+        runs[prec] = (d, st)
+    ref = None
+    if use_oracle:
+        import oracle as orc
+        from helpers import oracle_for
+        orc.set_threads(os.cpu_count() or 1)
+        o = oracle_for(grid, mk("f64"))
+        s = o.init_state(o.new_state(host))
+
+    def fields_of(prec):
+        st = runs[prec][1]
+        return {n: st.tensor(n).double() for n in ACC_FIELDS}
+
+    def tracer_min(tr):
+        return float(tr.reshape(T, N, L)[1:].min())
+
+    out = {}
+    qstart = {}
+    for its in range(1, K + 1):
+        for prec in ("f64", "f32"):
+            runs[prec][1].step(its, use_graph=True)
+        if use_oracle:
+            qo = o.step(s, its)[1]["qmass"]
+        if its == 1:
+            for prec in ("f64", "f32"):
+                qstart[prec] = runs[prec][1].budget()[1]["qmass"]
+            if use_oracle:
+                qstart["oracle"] = qo
+        if its not in marks:
+            continue
+        torch.cuda.synchronize()
+        g64, g32 = fields_of("f64"), fields_of("f32")
+        refs = {n: torch.from_numpy(s[n]).cuda() for n in ACC_FIELDS} if use_oracle else g64
+        rec = {}
+        for name, got in (("gpu_f64", g64), ("gpu_f32", g32)):
+            if name == "gpu_f64" and not use_oracle:
+                continue
+            per = {}
+            for n in ACC_FIELDS:
+                d = got[n] - refs[n]
+                per[n] = {"rel_l2": float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(refs[n])),
+                          "max_abs": float(d.abs().max())}
+            rec[name] = per
+        mass = {}
+        for prec in ("f64", "f32"):
+            mass["gpu_" + prec] = runs[prec][1].budget()[1]["qmass"] / qstart[prec] - 1
+        if use_oracle:
+            mass["oracle"] = qo / qstart["oracle"] - 1
+        trmin = {"gpu_f64": tracer_min(g64["tr3d"]), "gpu_f32": tracer_min(g32["tr3d"])}
+        if use_oracle:
+            trmin["oracle"] = float(s["tr3d"].reshape(T, N, L)[1:].min())
+        rec["mass_drift_since_step1"] = mass
+        rec["tracer_min"] = trmin
+        out[str(its)] = rec
+        del g64, g32, refs
+    line = {"metric": "error after K steps against the %s" % ("FP64 CPU oracle" if use_oracle else "FP64 GPU path"),
+            "config": {"workload": args.workload, "glvl": glvl, "nip": N, "nvl": L, "ntra": T, "dt": wl["dt"],
+                       "steps": K, "reference": "oracle" if use_oracle else "gpu_f64"},
+            "checkpoints": out}
+    print(json.dumps(line))
+    for d, st in runs.values():
+        st.free()
+        d.close()
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -416,6 +514,8 @@ def main():
     p.add_argument("--serve-min-steps", type=int, default=24)
     p.add_argument("--serve-max-steps", type=int, default=240)
     p.add_argument("--serve-fp64", action="store_true")
+    p.add_argument("--accuracy", type=int, default=0, help="report the error after this many steps")
+    p.add_argument("--nvl", type=int, default=0)
     args = p.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -425,6 +525,9 @@ def main():
         return
     if args.serve:
         serve_arm(args, ws, rank, local)
+        return
+    if args.accuracy:
+        accuracy_arm(args, ws, rank, local)
         return
     gpu_arm(args, ws, rank, local)
 

@@ -1,15 +1,19 @@
 """Forecast-advance serving with continuous batching.
 
 A request asks to advance a seeded balanced state on grid level glvl with
-nvl layers and ntra tracers by `steps` dynamics steps.  Requests of the same
-(glvl, nvl, ntra, precision) share a pool: one context whose ensemble slots
-are the batch, advanced together by one fused launch sequence per step
-(fim_step_active, one CUDA-graph replay).  Every slot carries its own step
+nvl layers and ntra tracers by `steps` dynamics steps.  Requests on the same
+grid (glvl, nvl) share a pool: one context whose ensemble slots are the
+batch, advanced together by one fused launch sequence per step
+(fim_step_active, one CUDA-graph replay).  A pool carries `max_tracers`
+tracer slots; a request with fewer tracers leaves the rest at zero.  Tracers
+are advected independently of one another, so a request's own tracers evolve
+exactly as in a context of its own size.  Every slot carries its own step
 counter and AB3 slots, so a request admitted while others are mid-forecast
 joins at the next step boundary; a finished slot is freed for the next
-request.  Pools are created while free HBM allows (admission by memory) and
-each pool runs on its own stream, so different grids overlap on the device.
-States stay resident in HBM for the whole forecast.
+request.  Pools are created while free HBM allows (admission by memory; a
+pool takes fewer slots when memory is short) and each pool runs on its own
+stream, so different grids overlap on the device.  States stay resident in
+HBM for the whole forecast.
 """
 import heapq
 import time
@@ -39,7 +43,7 @@ class Request:
 
     @property
     def key(self):
-        return (self.glvl, self.nvl, self.ntra)
+        return (self.glvl, self.nvl)
 
     @property
     def work(self):
@@ -58,10 +62,11 @@ def state_bytes(glvl, nvl, ntra, precision):
 class Pool:
     """One batched context (all slots share the grid and the configuration)."""
 
-    def __init__(self, key, precision, slots, collect):
+    def __init__(self, key, precision, slots, collect, ntra):
         import torch
-        glvl, nvl, ntra = key
+        glvl, nvl = key
         self.key = key
+        self.ntra = ntra
         self.grid = Grid.cached(glvl)
         self.cfg = FimConfig(nvl=nvl, ntra=ntra, dt=default_dt(glvl), precision=precision, members=slots)
         self.dyc = Dycore(self.grid, self.cfg)
@@ -80,8 +85,11 @@ class Pool:
 
     def admit(self, req, now):
         m = self.free_slot()
-        fields = synthetic_state(self.grid, self.cfg, seed=req.seed, sigma_ps=200.0, noise=0.5,
-                                 dtype=self.cfg.dtype)
+        own = FimConfig(nvl=self.cfg.nvl, ntra=req.ntra, dt=self.cfg.dt, precision=self.cfg.precision)
+        fields = synthetic_state(self.grid, own, seed=req.seed, sigma_ps=200.0, noise=0.5, dtype=self.cfg.dtype)
+        tr = np.zeros(self.ntra * self.grid.nip * self.cfg.nvl, self.cfg.dtype)
+        tr[:fields["tr3d"].size] = fields["tr3d"]
+        fields["tr3d"] = tr
         self.st.load(fields, member=m)
         self.st.init_member(m)  # dyn_init for this slot only; activates it
         req.t_admit = now
@@ -103,11 +111,14 @@ class Pool:
     def retire(self, m, now):
         r = self.slots[m]
         res = {}
+        own = r.ntra * self.grid.nip * self.cfg.nvl
         if self.collect:
             for name in self.collect:
-                res[name] = self.st.download(name, m)
+                a = self.st.download(name, m)
+                res[name] = a[:own] if name in ("tr3d", "trdp") else a
         qtrcr, bud = self.st.budget(m)
         res["qmass"] = bud["qmass"]
+        res["qtrcr"] = qtrcr[:r.ntra]
         r.result = res
         r.t_done = now
         self.st.set_active(m, False)
@@ -122,9 +133,10 @@ class Pool:
 class Server:
     """Continuous-batching request loop over resident device states."""
 
-    def __init__(self, precision="f32", slots=8, hbm_fraction=0.8, collect=("us3d", "tr3d")):
+    def __init__(self, precision="f32", slots=8, hbm_fraction=0.8, collect=("us3d", "tr3d"), max_tracers=21):
         self.precision = precision
         self.slots = slots
+        self.max_tracers = max_tracers
         self.hbm_fraction = hbm_fraction
         self.collect = collect
         self.pools = {}
@@ -138,14 +150,20 @@ class Server:
         p = self.pools.get(req.key)
         if p is not None:
             return p
-        need = state_bytes(req.glvl, req.nvl, req.ntra, self.precision) * self.slots
-        if need > self._free_hbm():
+        if req.ntra > self.max_tracers:
+            raise ValueError("request %d has %d tracers, the server at most %d" % (req.rid, req.ntra,
+                                                                                 self.max_tracers))
+        per_slot = state_bytes(req.glvl, req.nvl, self.max_tracers, self.precision)
+        if per_slot > self._free_hbm():
             # evict idle pools first, then refuse for now (the request waits)
             for k in [k for k, v in self.pools.items() if not v.active()]:
                 self.pools.pop(k).close()
-            if need > self._free_hbm():
-                return None
-        p = Pool(req.key, self.precision, self.slots, self.collect)
+        slots = self.slots
+        while slots > 1 and per_slot * slots > self._free_hbm():
+            slots //= 2
+        if per_slot * slots > self._free_hbm():
+            return None
+        p = Pool(req.key, self.precision, slots, self.collect, self.max_tracers)
         self.pools[req.key] = p
         return p
 

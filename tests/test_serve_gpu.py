@@ -21,14 +21,15 @@ def _mix():
 
 @pytest.mark.parametrize("precision", ["f32", "f64"])
 def test_same_alone_and_in_mix(precision):
-    # two slots per pool: later requests wait, join running batches mid-forecast
-    # and reuse freed slots
-    srv = Server(precision=precision, slots=2)
+    # two slots per grid pool, 8 tracer slots: later requests wait, join running
+    # batches mid-forecast and reuse freed slots
+    srv = Server(precision=precision, slots=2, max_tracers=8)
     mixed = {r.rid: r for r in srv.run(copy.deepcopy(_mix()), realtime=False)}
     srv.close()
     assert sorted(mixed) == [0, 1, 2, 3, 4]
     for req in _mix():
-        alone = Server(precision=precision, slots=1)
+        # alone: a context sized for this request only (no padded tracer slots)
+        alone = Server(precision=precision, slots=1, max_tracers=req.ntra)
         (r,) = alone.run([copy.deepcopy(req)], realtime=False)
         alone.close()
         for k, v in r.result.items():
