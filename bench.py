@@ -176,7 +176,8 @@ def gpu_arm(args, ws, rank, local):
     grid = F.Grid.cached(wl["glvl"])
     N, L, T = grid.nip, wl["nvl"], wl["ntra"]
     units = N * L * members  # cell-levels per step per GPU
-    cfg = F.FimConfig(nvl=L, ntra=T, dt=wl["dt"], precision="f32", members=members)
+    group = args.member_group if args.member_group >= 0 else wl.get("member_group", 0)
+    cfg = F.FimConfig(nvl=L, ntra=T, dt=wl["dt"], precision="f32", members=members, member_group=group)
     dyc, st = make_state(F, grid, cfg, wl, np.float32)
     for _ in range(args.warmup):
         st.step(use_graph=True)
@@ -265,7 +266,7 @@ def gpu_arm(args, ws, rank, local):
     # plain FP64 GPU step at the same workload
     fp64 = None
     if args.fp64_steps > 0:
-        cfg64 = F.FimConfig(nvl=L, ntra=T, dt=wl["dt"], precision="f64", members=members)
+        cfg64 = F.FimConfig(nvl=L, ntra=T, dt=wl["dt"], precision="f64", members=members, member_group=group)
         d64, s64 = make_state(F, grid, cfg64, wl, np.float64)
         s64.step(use_graph=True)
         ms64, _ = timed_steps(torch, d64, s64, args.fp64_steps, graph=True)
@@ -285,7 +286,7 @@ def gpu_arm(args, ws, rank, local):
             "data": "synthetic seeded balanced state (no dataset: the reference's GFS initial state is not "
                     "in the tree)",
             "config": {"workload": args.workload, "glvl": wl["glvl"], "nip": N, "nvl": L, "ntra": T,
-                       "dt": wl["dt"], "members_per_gpu": members, "precision": "fp32-mixed",
+                       "dt": wl["dt"], "members_per_gpu": members, "member_group": group or members, "precision": "fp32-mixed",
                        "cuda_graph": True, "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "no flush: state and edge fields (~60 GB) far exceed the 129 MB L2"},
             "gpu_launches": launches, "clocks": clk.summary(), "roofline": roof, "e2e": e2e,
@@ -505,6 +506,7 @@ def main():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="glvl8_nvl64_t20")
     p.add_argument("--members", type=int, default=0)
+    p.add_argument("--member-group", type=int, default=-1, help="members per dynamics group (default: workload's)")
     p.add_argument("--fp64-steps", type=int, default=2)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")

@@ -57,6 +57,7 @@ class FimConfig:
     pure_sig: int = 0
     ntrb: int = 0                   # class-B tracers (transported every dtratio steps by fct3d)
     dtratio: int = 6
+    member_group: int = 0           # members advanced together through the dynamics (0: all)
     thetac: np.ndarray = field(default=None, repr=False)
     dpsig: np.ndarray = field(default=None, repr=False)
 
@@ -94,6 +95,8 @@ WORKLOADS = {
     # FIM's own glvl-8 step (module_control.F90:220, 45 s); 72 s makes the
     # reference algorithm itself diverge within ~10 steps (AB3 gravity-wave limit)
     "glvl8_nvl64_t20": dict(glvl=8, nvl=64, ntra=21, dt=45.0, sigma_ps=200.0, noise=0.0, seed=3000),
+    # 32 members do not fit in HBM with a full set of step work fields each:
+    # the dynamics run in groups of 8 members
     "glvl7_nvl64_t10_x32": dict(glvl=7, nvl=64, ntra=11, dt=default_dt(7), sigma_ps=100.0, noise=0.5,
-                                seed=4000, members=32),
+                                seed=4000, members=32, member_group=8),
 }

@@ -35,6 +35,7 @@ struct DevBuf {
 struct fim_state {
   void* f[FIM_NFIELDS] = {};
   size_t count[FIM_NFIELDS] = {};  // elements per member
+  int slots[FIM_NFIELDS] = {};     // member slots held: M, or the member group for the step's work fields
   double* sums = nullptr;          // [M][8+T]
   float2* mpf = nullptr;           // FP32-mixed: float-float Montgomery potential [M][nvl*nip]
   void* thold = nullptr;           // FP32-mixed: theta seen by edgvar1 this step [M][nvl*nip]
@@ -70,6 +71,7 @@ struct fim_ctx {
   int ftchunk = 0;
   int trc_vk = 0;  // levels per thread of the fused tracer kernels (0: widest that nvl allows)
   int TB = 0, dtratio = 6;  // class-B tracers and their time-step ratio
+  int G = 1;                // members advanced together through the dynamics (member_group)
   void *cb_w = nullptr, *cb_F = nullptr, *cb_V = nullptr, *cb_fmx = nullptr, *cb_fmn = nullptr,
        *cb_flo = nullptr, *cb_flp = nullptr, *cb_fln = nullptr;
   void *du = nullptr, *dv = nullptr, *wu = nullptr, *wv = nullptr;
@@ -428,7 +430,7 @@ int cnuity_impl(fim_ctx* c, const R* u_velo, const R* v_velo, const R* u_edg, co
                 const R* lp_edg, R* delp, R* pres, R* exner, R* dp_tndcy, R* dplo_tndcy, R* massfx, R* omega) {
   int rc = check_prec<R>(c);
   if (rc) return rc;
-  if ((rc = ensure_cnuity(c, c->M))) return rc;
+  if ((rc = ensure_cnuity(c, c->G))) return rc;
   const size_t NL = (size_t)c->N * c->L, NI = (size_t)c->N * (c->L + 1), NE = NL * 6;
   Stager s(c);
   const R* a = s.map(u_velo, NL, 0);
@@ -457,7 +459,7 @@ int massadv_impl(fim_ctx* c, const R* u_velo, const R* v_velo, const R* u_edg, c
                  const R* lp_edg, R* delp, R* pres, R* exner, R* dp_tndcy, R* massfx, R* omega) {
   int rc = check_prec<R>(c);
   if (rc) return rc;
-  if ((rc = ensure_cnuity(c, c->M))) return rc;
+  if ((rc = ensure_cnuity(c, c->G))) return rc;
   const size_t NL = (size_t)c->N * c->L, NI = (size_t)c->N * (c->L + 1), NE = NL * 6;
   Stager s(c);
   const R* a = s.map(u_velo, NL, 0);
@@ -485,7 +487,7 @@ int trcadv_impl(fim_ctx* c, const R* trcr_edg, R* tracr, R* trcdp, R* trc_tdcy, 
                 const R* delp) {
   int rc = check_prec<R>(c);
   if (rc) return rc;
-  if ((rc = ensure_trcadv(c, c->M))) return rc;
+  if ((rc = ensure_trcadv(c, c->G))) return rc;
   const size_t NL = (size_t)c->N * c->L, NE = NL * 6;
   Stager s(c);
   const R* te = s.map(trcr_edg, NE * c->T, 0);
@@ -509,7 +511,7 @@ int momtum_impl(fim_ctx* c, R* u_velo, R* v_velo, const R* exner, R* relvor, con
                 const R* trcr_edg, const R* mont_edg, const R* uvsq_edg, R* u_tndcy, R* v_tndcy, const R* dp3d) {
   int rc = check_prec<R>(c);
   if (rc) return rc;
-  if ((rc = ensure_momtum(c, c->M))) return rc;
+  if ((rc = ensure_momtum(c, c->G))) return rc;
   const size_t NL = (size_t)c->N * c->L, NI = (size_t)c->N * (c->L + 1), NE = NL * 6;
   Stager s(c);
   R* u = s.map(u_velo, NL, 1);
@@ -650,7 +652,7 @@ int transp2_impl(fim_ctx* c, R* tracr, const R* cumufx, const R* dpinit, const R
   int rc = check_prec<R>(c);
   if (rc) return rc;
   if (c->TB <= 0) return FIM_OK;
-  if ((rc = ensure_classb(c, c->M))) return rc;
+  if ((rc = ensure_classb(c, c->G))) return rc;
   const size_t NL = (size_t)c->N * c->L;
   Stager s(c);
   R* tr = s.map(tracr, NL * (c->T + c->TB), 1);
@@ -665,6 +667,13 @@ int transp2_impl(fim_ctx* c, R* tracr, const R* cumufx, const R* dpinit, const R
 }
 
 // ---- fused step over the device-resident state ---------------------------
+// The step's edge work fields are rewritten every step before they are read:
+// with member groups they hold one group at a time.
+bool group_field(int f) {
+  return f == FIM_U_EDG || f == FIM_V_EDG || f == FIM_DP_EDG || f == FIM_LP_EDG || f == FIM_MONT_EDG ||
+         f == FIM_UVSQ_EDG || f == FIM_GEOP_EDG || f == FIM_TRC_EDG;
+}
+
 template <typename R>
 R* F(fim_state* st, int f) { return (R*)st->f[f]; }
 
@@ -684,52 +693,65 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
                    F<R>(st, FIM_SDOT), F<R>(st, FIM_EX3D), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D));
   launch_hystat<R>(lb, g, s, F<R>(st, FIM_PH3D), F<R>(st, FIM_EX3D), F<R>(st, FIM_MP3D), F<R>(st, FIM_DP3D),
                    F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP), F<R>(st, FIM_PSRF), F<R>(st, FIM_PTDCY), st->mpf);
-  launch_edgvar1<R>(l, g, s, c->kn.hi_order, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_DP3D),
-                    F<R>(st, FIM_PR3D), F<R>(st, FIM_MP3D), F<R>(st, FIM_TR3D), F<R>(st, FIM_U_EDG),
-                    F<R>(st, FIM_V_EDG), F<R>(st, FIM_DP_EDG), F<R>(st, FIM_LP_EDG), F<R>(st, FIM_MONT_EDG),
-                    F<R>(st, FIM_UVSQ_EDG), F<R>(st, FIM_TRC_EDG), st->mpf, (R*)st->thold);
-  if (c->kn.hi_order) {
-    // dp edges with edgvar3's two-sided average; tracer edges keep the
-    // own-side values, averaged where the fused tracer kernels use them
-    launch_edgvar3<R>(l, g, s, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), F<R>(st, FIM_DP_EDG), F<R>(st, FIM_TRC_EDG),
-                      1);
-    launch_tracer_own<R>(l, g, s, F<R>(st, FIM_TR3D), F<R>(st, FIM_TRC_EDG), c->trc_vk);
+  // the dynamics of the step, one member group at a time; the edge work
+  // fields and the scratch hold one group, the prognostic fields all members
+  for (int m0 = 0; m0 < M; m0 += c->G) {
+    const int gm = M - m0 < c->G ? M - m0 : c->G;
+    Launch lg = l;
+    lg.members = gm;
+    lg.sp = c->d_sp + m0;
+    lg.flags = c->d_flags + m0;
+    auto P = [&](int f) {
+      return (R*)st->f[f] + (st->slots[f] == M ? (size_t)m0 * st->count[f] : (size_t)0);
+    };
+    float2* mpf = st->mpf ? st->mpf + (size_t)m0 * st->count[FIM_MP3D] : nullptr;
+    launch_edgvar1<R>(lg, g, s, c->kn.hi_order, P(FIM_US3D), P(FIM_VS3D), P(FIM_DP3D),
+                      P(FIM_PR3D), P(FIM_MP3D), P(FIM_TR3D), P(FIM_U_EDG),
+                      P(FIM_V_EDG), P(FIM_DP_EDG), P(FIM_LP_EDG), P(FIM_MONT_EDG),
+                      P(FIM_UVSQ_EDG), P(FIM_TRC_EDG), mpf, (R*)st->thold);
+    if (c->kn.hi_order) {
+      // dp edges with edgvar3's two-sided average; tracer edges keep the
+      // own-side values, averaged where the fused tracer kernels use them
+      launch_edgvar3<R>(lg, g, s, P(FIM_DP3D), P(FIM_TR3D), P(FIM_DP_EDG), P(FIM_TRC_EDG),
+                        1);
+      launch_tracer_own<R>(lg, g, s, P(FIM_TR3D), P(FIM_TRC_EDG), c->trc_vk);
+    }
+    CnuityScratch<R> cw{(R*)c->antifx, (R*)c->delp_lo, (R*)c->p_plus, (R*)c->p_mnus, (R*)c->r_plus, (R*)c->r_mnus};
+    if (c->cfg.flux_conserv_schm == 1)
+      launch_cnuity<R>(lg, g, s, cw, P(FIM_US3D), P(FIM_VS3D), P(FIM_U_EDG), P(FIM_V_EDG),
+                       P(FIM_DP_EDG), P(FIM_LP_EDG), P(FIM_DP3D), P(FIM_PR3D),
+                       P(FIM_EX3D), P(FIM_DP_TDCY), P(FIM_DPL_TDCY), P(FIM_MASSFX),
+                       P(FIM_WS3D));
+    else
+      launch_massadv<R>(lg, g, s, cw, P(FIM_US3D), P(FIM_VS3D), P(FIM_U_EDG), P(FIM_V_EDG),
+                        P(FIM_DP_EDG), P(FIM_LP_EDG), P(FIM_DP3D), P(FIM_PR3D),
+                        P(FIM_EX3D), P(FIM_DP_TDCY), P(FIM_MASSFX), P(FIM_WS3D));
+    if (c->TB > 0) {
+      // class-B transport (dyn_run.F90:388-403); transp2/transp0 act at steps
+      // with mod(its, dtratio) == 0, decided per member on the device
+      launch_transp1<R>(lg, g, s, P(FIM_CUMUFX), P(FIM_MASSFX));
+      launch_transp2<R>(lg, g, s, classb_scratch<R>(c), c->dtratio, c->TB, P(FIM_TR3D), P(FIM_CUMUFX),
+                        P(FIM_DPINIT), P(FIM_DP3D));
+      launch_transp0<R>(lg, g, s, c->dtratio, P(FIM_CUMUFX), P(FIM_DP3D), P(FIM_DPINIT));
+    }
+    if (c->kn.hi_order) {
+      TrcFusedScratch<R> fw{(R*)c->f_trcr_lo, (R*)c->f_sp, (R*)c->f_sm, (R*)c->f_trold, (R*)c->f_rp, (R*)c->f_rm,
+                            c->ftchunk, c->trc_vk};
+      launch_tracers_fused<R>(lg, g, s, fw, P(FIM_TRC_EDG), P(FIM_TR3D), P(FIM_TRDP),
+                              P(FIM_TRC_TDCY), P(FIM_TRL_TDCY), P(FIM_MASSFX),
+                              P(FIM_DP3D));
+    } else {
+      TrcadvScratch<R> tw{(R*)c->t_antiflx, (R*)c->t_trmin, (R*)c->t_trmax, (R*)c->t_trcr_lo, (R*)c->t_rp,
+                          (R*)c->t_rm, c->tchunk};
+      launch_trcadv<R>(lg, g, s, tw, P(FIM_TRC_EDG), P(FIM_TR3D), P(FIM_TRDP),
+                       P(FIM_TRC_TDCY), P(FIM_TRL_TDCY), P(FIM_MASSFX), P(FIM_DP3D));
+    }
+    MomtumScratch<R> mw{(R*)c->du, (R*)c->dv, (R*)c->wu, (R*)c->wv};
+    launch_momtum<R>(lg, g, s, c->kn, mw, P(FIM_US3D), P(FIM_VS3D), P(FIM_EX3D),
+                     P(FIM_RELVOR), P(FIM_U_EDG), P(FIM_V_EDG), P(FIM_TRC_EDG),
+                     P(FIM_MONT_EDG), P(FIM_UVSQ_EDG), P(FIM_U_TDCY), P(FIM_V_TDCY),
+                     P(FIM_DP3D), mpf, (const R*)st->thold);
   }
-  CnuityScratch<R> cw{(R*)c->antifx, (R*)c->delp_lo, (R*)c->p_plus, (R*)c->p_mnus, (R*)c->r_plus, (R*)c->r_mnus};
-  if (c->cfg.flux_conserv_schm == 1)
-    launch_cnuity<R>(l, g, s, cw, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_U_EDG), F<R>(st, FIM_V_EDG),
-                     F<R>(st, FIM_DP_EDG), F<R>(st, FIM_LP_EDG), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D),
-                     F<R>(st, FIM_EX3D), F<R>(st, FIM_DP_TDCY), F<R>(st, FIM_DPL_TDCY), F<R>(st, FIM_MASSFX),
-                     F<R>(st, FIM_WS3D));
-  else
-    launch_massadv<R>(l, g, s, cw, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_U_EDG), F<R>(st, FIM_V_EDG),
-                      F<R>(st, FIM_DP_EDG), F<R>(st, FIM_LP_EDG), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D),
-                      F<R>(st, FIM_EX3D), F<R>(st, FIM_DP_TDCY), F<R>(st, FIM_MASSFX), F<R>(st, FIM_WS3D));
-  if (c->TB > 0) {
-    // class-B transport (dyn_run.F90:388-403); transp2/transp0 act at steps
-    // with mod(its, dtratio) == 0, decided per member on the device
-    launch_transp1<R>(l, g, s, F<R>(st, FIM_CUMUFX), F<R>(st, FIM_MASSFX));
-    launch_transp2<R>(l, g, s, classb_scratch<R>(c), c->dtratio, c->TB, F<R>(st, FIM_TR3D), F<R>(st, FIM_CUMUFX),
-                      F<R>(st, FIM_DPINIT), F<R>(st, FIM_DP3D));
-    launch_transp0<R>(l, g, s, c->dtratio, F<R>(st, FIM_CUMUFX), F<R>(st, FIM_DP3D), F<R>(st, FIM_DPINIT));
-  }
-  if (c->kn.hi_order) {
-    TrcFusedScratch<R> fw{(R*)c->f_trcr_lo, (R*)c->f_sp, (R*)c->f_sm, (R*)c->f_trold, (R*)c->f_rp, (R*)c->f_rm,
-                          c->ftchunk, c->trc_vk};
-    launch_tracers_fused<R>(l, g, s, fw, F<R>(st, FIM_TRC_EDG), F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP),
-                            F<R>(st, FIM_TRC_TDCY), F<R>(st, FIM_TRL_TDCY), F<R>(st, FIM_MASSFX),
-                            F<R>(st, FIM_DP3D));
-  } else {
-    TrcadvScratch<R> tw{(R*)c->t_antiflx, (R*)c->t_trmin, (R*)c->t_trmax, (R*)c->t_trcr_lo, (R*)c->t_rp,
-                        (R*)c->t_rm, c->tchunk};
-    launch_trcadv<R>(l, g, s, tw, F<R>(st, FIM_TRC_EDG), F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP),
-                     F<R>(st, FIM_TRC_TDCY), F<R>(st, FIM_TRL_TDCY), F<R>(st, FIM_MASSFX), F<R>(st, FIM_DP3D));
-  }
-  MomtumScratch<R> mw{(R*)c->du, (R*)c->dv, (R*)c->wu, (R*)c->wv};
-  launch_momtum<R>(l, g, s, c->kn, mw, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_EX3D),
-                   F<R>(st, FIM_RELVOR), F<R>(st, FIM_U_EDG), F<R>(st, FIM_V_EDG), F<R>(st, FIM_TRC_EDG),
-                   F<R>(st, FIM_MONT_EDG), F<R>(st, FIM_UVSQ_EDG), F<R>(st, FIM_U_TDCY), F<R>(st, FIM_V_TDCY),
-                   F<R>(st, FIM_DP3D), st->mpf, (const R*)st->thold);
   // budgets of the state the step returns
   launch_globsum<R>(l, g, s, c->T + c->TB, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), (const R*)nullptr,
                     (const R*)nullptr,
@@ -739,14 +761,14 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
 
 int ensure_all(fim_ctx* c) {
   int rc;
-  if ((rc = ensure_cnuity(c, c->M))) return rc;
+  if ((rc = ensure_cnuity(c, c->G))) return rc;
   if (c->kn.hi_order) {
-    if ((rc = ensure_trc_fused(c, c->M))) return rc;
-  } else if ((rc = ensure_trcadv(c, c->M))) return rc;
-  if ((rc = ensure_momtum(c, c->M))) return rc;
+    if ((rc = ensure_trc_fused(c, c->G))) return rc;
+  } else if ((rc = ensure_trcadv(c, c->G))) return rc;
+  if ((rc = ensure_momtum(c, c->G))) return rc;
   if ((rc = ensure_hybgen(c, c->M))) return rc;
   if ((rc = ensure_globsum(c, c->M))) return rc;
-  if ((rc = ensure_classb(c, c->M))) return rc;
+  if ((rc = ensure_classb(c, c->G))) return rc;
   return FIM_OK;
 }
 
@@ -804,6 +826,7 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
   if (cfg->remap_optn < 1 || cfg->remap_optn > 3) return FIM_EINVAL;
   if (cfg->precision != FIM_PREC_F64 && cfg->precision != FIM_PREC_F32) return FIM_EINVAL;
   if (cfg->ntrb < 0 || cfg->ntra + cfg->ntrb > 32 || (cfg->ntrb > 0 && cfg->dtratio < 1)) return FIM_EINVAL;
+  if (cfg->member_group < 0) return FIM_EINVAL;
   if (!cfg->thetac || !cfg->dpsig || !g->prox || !g->proxs || !g->nprox || !g->area || !g->cs || !g->sn ||
       !g->sidevec_c || !g->sidevec_e || !g->sideln || !g->hfcoef || !g->lat)
     return FIM_EINVAL;
@@ -820,6 +843,7 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
   c->dpsig.assign(cfg->dpsig, cfg->dpsig + c->L);
   c->TB = cfg->ntrb;
   c->dtratio = cfg->dtratio;
+  c->G = (cfg->member_group > 0 && cfg->member_group < c->M) ? cfg->member_group : c->M;
   c->str = make_strides(c->N, c->L, c->T, c->TB);
   // FIM_TRC_VK=1|2|4 pins the levels per thread of the fused tracer kernels
   if (const char* v = getenv("FIM_TRC_VK")) c->trc_vk = atoi(v);
@@ -1107,15 +1131,19 @@ int fim_state_alloc(fim_ctx* c, fim_state** out) {
       NL * 6 * T, NL * 6, NL};                     // trc_edg cumufx dpinit
   for (int f = 0; f < FIM_NFIELDS; f++) {
     st->count[f] = cnt[f];
-    int rc = dalloc(c, &st->f[f], cnt[f] * c->M * c->esz);
+    st->slots[f] = group_field(f) ? c->G : c->M;
+    // the class-B integrals exist only with class-B tracers
+    const size_t n = (f == FIM_CUMUFX || f == FIM_DPINIT) && c->TB == 0 ? 0 : cnt[f] * st->slots[f];
+    if (n == 0) st->count[f] = 0;
+    int rc = dalloc(c, &st->f[f], n * c->esz);
     if (rc) { delete st; return rc; }
-    cudaMemsetAsync(st->f[f], 0, cnt[f] * c->M * c->esz, c->stream);
+    cudaMemsetAsync(st->f[f], 0, n * c->esz + (n == 0 ? 16 : 0), c->stream);
   }
   int rc = dalloc(c, (void**)&st->sums, (size_t)c->M * (8 + c->T + c->TB) * sizeof(double));
   if (rc) { delete st; return rc; }
   if (c->prec == FIM_PREC_F32) {
     if ((rc = dalloc(c, (void**)&st->mpf, (size_t)c->M * cnt[FIM_MP3D] * sizeof(float2)))) { delete st; return rc; }
-    if ((rc = dalloc(c, &st->thold, (size_t)c->M * cnt[FIM_MP3D] * c->esz))) { delete st; return rc; }
+    if ((rc = dalloc(c, &st->thold, (size_t)c->G * cnt[FIM_MP3D] * c->esz))) { delete st; return rc; }
     cudaMemsetAsync(st->mpf, 0, (size_t)c->M * cnt[FIM_MP3D] * sizeof(float2), c->stream);
   }
   if ((rc = ensure_all(c))) { delete st; return rc; }
@@ -1141,6 +1169,8 @@ int fim_state_free(fim_ctx* c, fim_state* st) {
 
 int fim_state_field(fim_ctx* c, fim_state* st, int field, int member, void** dptr, int64_t* count) {
   if (!c || !st || field < 0 || field >= FIM_NFIELDS || member < 0 || member >= c->M) return FIM_EINVAL;
+  if (member >= st->slots[field])
+    return set_err(c, FIM_EINVAL, "the step's edge work fields hold only member_group members");
   if (dptr) *dptr = (char*)st->f[field] + (size_t)member * st->count[field] * c->esz;
   if (count) *count = (int64_t)st->count[field];
   return FIM_OK;

@@ -276,7 +276,7 @@ class DycoreState:
         file (restart_io); returns itsm1."""
         from .restart_io import STATE_FIELDS, write_restart
         itsm1, nf, of, vof, ab = self.get_step(member)
-        fields = {n: self.download(n, member) for n in STATE_FIELDS}
+        fields = {n: self.download(n, member) for n in STATE_FIELDS if self.field_ptr(n, member)[1] > 0}
         write_restart(path, self.dyc.grid, self.dyc.cfg, itsm1, nf, of, vof, ab, fields, extras=extras)
         return itsm1
 
@@ -287,7 +287,8 @@ class DycoreState:
         cfg = self.dyc.cfg
         r = read_restart(path, self.dyc.grid.nip, cfg.nvl, cfg.ntra, cfg.ntrb)
         for n, a in r["fields"].items():
-            self.upload(n, a, member)
+            if self.field_ptr(n, member)[1] > 0:  # the class-B integrals exist only with class-B tracers
+                self.upload(n, a, member)
         self.set_step(member, r["itsm1"], r["nf"], r["of"], r["vof"], r["adbash"])
         return r
 

@@ -138,15 +138,17 @@ def write_restart(path, grid, cfg, itsm1, nf, of, vof, adbash, fields, extras=No
             for n in range(3):
                 for name in ("trc_tdcy", "trl_tdcy"):
                     _rec(fh, slab(name, t * 3 + n) if t < nta else _f(z(cell), _R4))
+        def part(name, n):
+            a = np.asarray(fields[name] if name in fields else ex.get(name, z(n))).reshape(-1)
+            return _f(a[:n] if a.size else z(n), _R4)
+
         for name in ("us3d", "vs3d", "ws3d", "mp3d", "tk3d", "dp3d", "rh3d", "relvor", "dpinit"):
-            src = fields if name in fields else ex
-            _rec(fh, _f(np.asarray(src.get(name, z(cell))).reshape(-1)[:cell], _R4))
+            _rec(fh, part(name, cell))
         for name in ("pr3d", "ex3d", "ph3d", "sdot"):
             _rec(fh, slab(name, 0, (nvl + 1) * nip))
         for n in range(3):
             _rec(fh, slab("massfx", n, 6 * cell))
-        src = fields if "cumufx" in fields else ex
-        _rec(fh, _f(np.asarray(src.get("cumufx", z(6 * cell))).reshape(-1), _R4))
+        _rec(fh, part("cumufx", 6 * cell))
 
 
 def read_restart(path, nip, nvl, ntra, ntrb=0, nvlsig=None, real_bytes=4):

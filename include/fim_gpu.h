@@ -93,6 +93,9 @@ typedef struct fim_config {
   int ntrb;                /* [0] class-B tracers, stored after the ntra class-A ones
                               (tracer slots ntra+1..ntra+ntrb); ntra+ntrb <= 32 */
   int dtratio;             /* [6] class-B / class-A time-step ratio (fimnamelist.F90:87) */
+  int member_group;        /* [0] members advanced together through the dynamics of a
+                              step; 0 = all.  The step's edge work fields and scratch
+                              are held for one group, which bounds their memory */
 } fim_config;
 
 typedef struct fim_ctx fim_ctx;
@@ -264,7 +267,9 @@ enum fim_field {
 
 /* tr3d and trdp of a state hold ntra+ntrb tracers; cumufx (nvl,6,nip) and
  * dpinit (nvl,nip) are the class-B transport's flux integral and initial
- * thickness (module_variables.F90:27,89).
+ * thickness (module_variables.F90:27,89), empty (count 0) without class-B
+ * tracers.  With member_group < members the edge work fields (u_edg ..
+ * trc_edg) exist for member_group members only.
  * After a fused step the edge work fields are in the step's internal form:
  * trc_edg of tracers 2..ntra holds the own-side reconstructions (edgvar3
  * loop 1) and, in an FP32 context, mont_edg holds edge-minus-cell values. */

@@ -169,6 +169,26 @@ def test_members_independent():
         assert np.array_equal(st.download(n, 1), sb.download(n)), n
 
 
+@pytest.mark.parametrize("group", [2, 3])
+def test_member_groups_match_one_batch(group):
+    """member_group < members runs the dynamics group by group with the edge
+    work fields held for one group: bit-identical to one batch of all."""
+    grid = F.Grid.cached(3)
+    mk = lambda **kw: F.FimConfig(nvl=38, ntra=5, dt=400.0, precision="f32", members=4, **kw)  # noqa: E731
+    fields = [F.synthetic_state(grid, mk(), seed=60 + m, sigma_ps=150.0, noise=0.5, dtype=np.float32)
+              for m in range(4)]
+    d1, s1 = _gpu_state(grid, mk(), None, members=4, member_fields=fields)
+    d2, s2 = _gpu_state(grid, mk(member_group=group), None, members=4, member_fields=fields)
+    for its in (1, 2, 3):
+        s1.step(its, use_graph=True)
+        s2.step(its, use_graph=True)
+    for m in range(4):
+        for n in PROGNOSTIC + ["massfx", "trc_tdcy", "u_tdcy"]:
+            assert np.array_equal(s2.download(n, m), s1.download(n, m)), (m, n)
+    with pytest.raises(F._lib.FimError):
+        s2.download("u_edg", 3)
+
+
 def test_fp32_mixed_one_step(case4):
     grid, cfg, fields, o0, s0 = case4
     o = oracle_for(grid, cfg)
