@@ -191,6 +191,7 @@ def gpu_arm(args, ws, rank, local):
     rc, flags = st.check()
     if rc != 0:
         raise SystemExit("device status flags %d after the timed steps" % flags)
+    shape = dyc.tracer_shape()
 
     # per-kernel times (events on the library stream), direct launches
     dyc.profile(True)
@@ -286,7 +287,10 @@ def gpu_arm(args, ws, rank, local):
             "data": "synthetic seeded balanced state (no dataset: the reference's GFS initial state is not "
                     "in the tree)",
             "config": {"workload": args.workload, "glvl": wl["glvl"], "nip": N, "nvl": L, "ntra": T,
-                       "dt": wl["dt"], "members_per_gpu": members, "member_group": group or members, "precision": "fp32-mixed",
+                       "dt": wl["dt"], "members_per_gpu": members, "member_group": group or members,
+                       "tracer_shape_autotuned": {"levels_per_thread": shape[0], "threads_per_block": shape[1],
+                                                  "probe_ms": shape[2]},
+                       "precision": "fp32-mixed",
                        "cuda_graph": True, "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "no flush: state and edge fields (~60 GB) far exceed the 129 MB L2"},
             "gpu_launches": launches, "clocks": clk.summary(), "roofline": roof, "e2e": e2e,

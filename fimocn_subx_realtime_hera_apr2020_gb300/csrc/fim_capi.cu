@@ -70,6 +70,9 @@ struct fim_ctx {
        *f_rm = nullptr;
   int ftchunk = 0;
   int trc_vk = 0;  // levels per thread of the fused tracer kernels (0: widest that nvl allows)
+  int trc_tb = 128;  // threads per block of the fused tracer kernels
+  bool autotune = true, tuned = false;
+  float tune_ms = 0.f;
   int TB = 0, dtratio = 6;  // class-B tracers and their time-step ratio
   int G = 1;                // members advanced together through the dynamics (member_group)
   void *cb_w = nullptr, *cb_F = nullptr, *cb_V = nullptr, *cb_fmx = nullptr, *cb_fmn = nullptr,
@@ -714,7 +717,7 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
       // own-side values, averaged where the fused tracer kernels use them
       launch_edgvar3<R>(lg, g, s, P(FIM_DP3D), P(FIM_TR3D), P(FIM_DP_EDG), P(FIM_TRC_EDG),
                         1);
-      launch_tracer_own<R>(lg, g, s, P(FIM_TR3D), P(FIM_TRC_EDG), c->trc_vk);
+      launch_tracer_own<R>(lg, g, s, P(FIM_TR3D), P(FIM_TRC_EDG), c->trc_vk, c->trc_tb);
     }
     CnuityScratch<R> cw{(R*)c->antifx, (R*)c->delp_lo, (R*)c->p_plus, (R*)c->p_mnus, (R*)c->r_plus, (R*)c->r_mnus};
     if (c->cfg.flux_conserv_schm == 1)
@@ -736,7 +739,7 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
     }
     if (c->kn.hi_order) {
       TrcFusedScratch<R> fw{(R*)c->f_trcr_lo, (R*)c->f_sp, (R*)c->f_sm, (R*)c->f_trold, (R*)c->f_rp, (R*)c->f_rm,
-                            c->ftchunk, c->trc_vk};
+                            c->ftchunk, c->trc_vk, c->trc_tb};
       launch_tracers_fused<R>(lg, g, s, fw, P(FIM_TRC_EDG), P(FIM_TR3D), P(FIM_TRDP),
                               P(FIM_TRC_TDCY), P(FIM_TRL_TDCY), P(FIM_MASSFX),
                               P(FIM_DP3D));
@@ -811,6 +814,38 @@ int state_init_impl(fim_ctx* c, fim_state* st, int m0, int nm) {
 
 }  // namespace
 
+namespace {
+
+// Shape autotuning of the fused tracer kernels, once per context before the
+// first step is captured: the probe runs with every active member's step
+// parameters advanced one slot (as k_step_begin will), so the AB3 tendency
+// slot it writes is the one the coming step overwrites.
+template <typename R>
+int autotune_impl(fim_ctx* c, fim_state* st) {
+  std::vector<StepParams> next = c->h_sp;
+  for (auto& p : next) {
+    p.nf = (p.nf + 1) % 3;
+    p.of = (p.of + 1) % 3;
+    p.vof = (p.vof + 1) % 3;
+  }
+  CK(cudaMemcpyAsync(c->d_sp, next.data(), sizeof(StepParams) * next.size(), cudaMemcpyHostToDevice, c->stream),
+     "tune params");
+  Launch l = make_launch(c, c->G < c->M ? c->G : c->M);
+  TrcFusedScratch<R> fw{(R*)c->f_trcr_lo, (R*)c->f_sp, (R*)c->f_sm, (R*)c->f_trold, (R*)c->f_rp, (R*)c->f_rm,
+                        c->ftchunk, c->trc_vk, c->trc_tb};
+  int vk = c->trc_vk, tb = c->trc_tb;
+  const int e = tune_tracers<R>(l, grid_of<R>(c), c->str, fw, F<R>(st, FIM_TRC_EDG), F<R>(st, FIM_TR3D),
+                                F<R>(st, FIM_TRDP), F<R>(st, FIM_TRC_TDCY), F<R>(st, FIM_TRL_TDCY),
+                                F<R>(st, FIM_MASSFX), F<R>(st, FIM_DP3D), &vk, &tb, &c->tune_ms);
+  if (e) return set_err(c, FIM_ECUDA, "tracer shape autotuning", (cudaError_t)e);
+  c->trc_vk = vk;
+  c->trc_tb = tb;
+  c->tuned = true;
+  return push_sp(c);
+}
+
+}  // namespace
+
 // ============================== extern "C" ==================================
 extern "C" {
 
@@ -845,8 +880,12 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
   c->dtratio = cfg->dtratio;
   c->G = (cfg->member_group > 0 && cfg->member_group < c->M) ? cfg->member_group : c->M;
   c->str = make_strides(c->N, c->L, c->T, c->TB);
-  // FIM_TRC_VK=1|2|4 pins the levels per thread of the fused tracer kernels
+  // FIM_TRC_VK=1|2|4 and FIM_TRC_TB=128|256 pin the fused tracer kernels'
+  // shape; FIM_AUTOTUNE=0 keeps the default shape untimed
   if (const char* v = getenv("FIM_TRC_VK")) c->trc_vk = atoi(v);
+  if (const char* v = getenv("FIM_TRC_TB")) c->trc_tb = atoi(v) == 256 ? 256 : 128;
+  if (const char* v = getenv("FIM_AUTOTUNE")) c->autotune = atoi(v) != 0;
+  if (getenv("FIM_TRC_VK") || getenv("FIM_TRC_TB")) c->autotune = false;
   const int N = c->N, L = c->L;
   // 0-based index tables; validate the Fortran numbering
   std::vector<int> prox(N * 6), proxs(N * 6), nprox(N);
@@ -1251,6 +1290,10 @@ int fim_member_set_step(fim_ctx* c, int member, int itsm1, int nf, int of, int v
 
 static int run_step(fim_ctx* c, fim_state* st, int use_graph) {
   int rc;
+  if (c->autotune && !c->tuned && c->kn.hi_order && c->T > 1) {
+    rc = c->prec == FIM_PREC_F64 ? autotune_impl<double>(c, st) : autotune_impl<float>(c, st);
+    if (rc) return rc;
+  }
   if (use_graph) {
     if (!st->graph) {
       // the step is its-invariant: every step-dependent scalar is read from
@@ -1334,6 +1377,14 @@ int fim_profile_report(fim_ctx* c, char* buf, int len) {
   if ((int)out.size() + 1 > len) return FIM_EINVAL;
   memcpy(buf, out.c_str(), out.size() + 1);
   c->prof.agg.clear();
+  return FIM_OK;
+}
+
+int fim_tracer_shape(const fim_ctx* c, int* levels_per_thread, int* threads_per_block, float* probe_ms) {
+  if (!c) return FIM_EINVAL;
+  if (levels_per_thread) *levels_per_thread = c->trc_vk;
+  if (threads_per_block) *threads_per_block = c->trc_tb;
+  if (probe_ms) *probe_ms = c->tuned ? c->tune_ms : 0.f;
   return FIM_OK;
 }
 

@@ -237,9 +237,19 @@ void launch_trcadv(const Launch&, const Grid<R>&, const Strides&, const TrcadvSc
                    const R* delp);
 // fused tracer path of the step (fim_trc.cu)
 template <typename R>
-struct TrcFusedScratch { R *trcr_lo, *s_plus, *s_mnus, *trold, *r_plus, *r_mnus; int tchunk; int vk; };
+struct TrcFusedScratch {
+  R *trcr_lo, *s_plus, *s_mnus, *trold, *r_plus, *r_mnus;
+  int tchunk;
+  int vk;  // levels per thread (0: widest the layout admits)
+  int tb;  // threads per block, 128 or 256
+};
 template <typename R>
-void launch_tracer_own(const Launch&, const Grid<R>&, const Strides&, const R* tracr, R* trc_edg, int vk);
+void launch_tracer_own(const Launch&, const Grid<R>&, const Strides&, const R* tracr, R* trc_edg, int vk, int tb);
+// times the tracer kernel shapes on the given state (see fim_trc.cu); returns a cudaError_t value
+template <typename R>
+int tune_tracers(const Launch&, const Grid<R>&, const Strides&, const TrcFusedScratch<R>&, R* trc_edg, R* tracr,
+                 R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx, const R* delp, int* best_vk, int* best_tb,
+                 float* best_ms);
 template <typename R>
 void launch_tracers_fused(const Launch&, const Grid<R>&, const Strides&, const TrcFusedScratch<R>&,
                           R* trc_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx,

@@ -25,11 +25,13 @@ template <typename R> __device__ __forceinline__ R tmax(R a, R b) { return a > b
 template <typename R> __device__ __forceinline__ R tmin(R a, R b) { return a < b ? a : b; }
 template <typename R> __device__ __forceinline__ R tabs(R a) { return a < R(0) ? -a : a; }
 
-// 128-thread blocks capped at 64 registers a thread: 32 warps resident per SM
-// keep enough loads in flight for these gather-heavy, latency-bound kernels
-constexpr int kTB = 128;
-constexpr int kTBMin = 8;
-inline unsigned tblocks(long long n) { return (unsigned)((n + kTB - 1) / kTB); }
+// Blocks of up to kTB threads capped at 64 registers a thread (32 resident
+// warps per SM keep enough loads in flight for these gather-heavy,
+// latency-bound kernels); the block size actually launched (128 or 256, the
+// cell patch) and the levels per thread are picked by tune_tracers.
+constexpr int kTB = 256;
+constexpr int kTBMin = 4;
+inline unsigned tblocks(long long n, int tb) { return (unsigned)((n + tb - 1) / tb); }
 
 // VK consecutive levels per thread, moved with one 4/8/16-byte access
 template <typename R, int VK> struct VecOf;
@@ -346,22 +348,24 @@ __global__ void __launch_bounds__(kTB, kTBMin) k_tr_hi(Grid<R> g, Strides s, con
 
 template <typename R, int VK>
 void tracers_fused_vk(const Launch& l, const Grid<R>& g, const Strides& s, const TrcFusedScratch<R>& w,
-                      R* trc_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx, const R* delp) {
+                      R* trc_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx, const R* delp,
+                      int tb, bool probe) {
   const size_t sc = (size_t)g.N * g.L;
   for (int t0 = 0; t0 < g.T; t0 += w.tchunk) {
     const int nt = (g.T - t0 < w.tchunk) ? g.T - t0 : w.tchunk;
-    dim3 grid(tblocks((long long)g.N * (g.L / VK)) * nt, l.members);
+    dim3 grid(tblocks((long long)g.N * (g.L / VK), tb) * nt, l.members);
     FIM_KBEGIN(l, "k_tr_lo");
-    k_tr_lo<R, VK><<<grid, kTB, 0, l.stream>>>(g, s, l.sp, t0, nt, massfx, trc_edg, tracr, trcdp, trl_tdcy, delp,
-                                                w.trcr_lo, w.s_plus, w.s_mnus, w.trold, sc);
+    k_tr_lo<R, VK><<<grid, tb, 0, l.stream>>>(g, s, l.sp, t0, nt, massfx, trc_edg, tracr, trcdp, trl_tdcy, delp,
+                                               w.trcr_lo, w.s_plus, w.s_mnus, w.trold, sc);
     FIM_KEND(l);
     FIM_KBEGIN(l, "k_tr_lim");
-    k_tr_lim<R, VK><<<grid, kTB, 0, l.stream>>>(g, s, l.sp, t0, nt, trc_tdcy, delp, w.trold, w.trcr_lo,
-                                                 w.s_plus, w.s_mnus, w.r_plus, w.r_mnus, sc);
+    k_tr_lim<R, VK><<<grid, tb, 0, l.stream>>>(g, s, l.sp, t0, nt, trc_tdcy, delp, w.trold, w.trcr_lo,
+                                                w.s_plus, w.s_mnus, w.r_plus, w.r_mnus, sc);
     FIM_KEND(l);
+    if (probe) return;  // the first chunk's k_tr_lo and k_tr_lim only
     FIM_KBEGIN(l, "k_tr_hi");
-    k_tr_hi<R, VK><<<grid, kTB, 0, l.stream>>>(g, s, l.sp, t0, nt, massfx, trc_edg, tracr, trcdp, trc_tdcy,
-                                                trl_tdcy, delp, w.trold, w.trcr_lo, w.r_plus, w.r_mnus, sc);
+    k_tr_hi<R, VK><<<grid, tb, 0, l.stream>>>(g, s, l.sp, t0, nt, massfx, trc_edg, tracr, trcdp, trc_tdcy,
+                                               trl_tdcy, delp, w.trold, w.trcr_lo, w.r_plus, w.r_mnus, sc);
     FIM_KEND(l);
   }
 }
@@ -379,42 +383,104 @@ int tracer_vk(const Grid<R>& g, std::initializer_list<const void*> ptrs, int wan
   return vk;
 }
 
+inline int tracer_tb(int tb) { return tb == 256 ? 256 : 128; }
+
+template <typename R>
+void fused_dispatch(const Launch& l, const Grid<R>& g, const Strides& s, const TrcFusedScratch<R>& w, R* trc_edg,
+                    R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx, const R* delp, bool probe) {
+  const int vk = tracer_vk(g, {trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp, w.trcr_lo, w.s_plus,
+                               w.s_mnus, w.trold, w.r_plus, w.r_mnus}, w.vk);
+  const int tb = tracer_tb(w.tb);
+  if (vk == 4)
+    tracers_fused_vk<R, (sizeof(R) == 4 ? 4 : 2)>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx,
+                                                  delp, tb, probe);
+  else if (vk == 2)
+    tracers_fused_vk<R, 2>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp, tb, probe);
+  else
+    tracers_fused_vk<R, 1>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp, tb, probe);
+}
+
 template <typename R>
 void launch_tracers_fused(const Launch& l, const Grid<R>& g, const Strides& s, const TrcFusedScratch<R>& w,
                           R* trc_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx,
                           const R* delp) {
-  const int vk = tracer_vk(g, {trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp, w.trcr_lo, w.s_plus,
-                               w.s_mnus, w.trold, w.r_plus, w.r_mnus}, w.vk);
-  if (vk == 4)
-    tracers_fused_vk<R, (sizeof(R) == 4 ? 4 : 2)>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx,
-                                                  delp);
-  else if (vk == 2)
-    tracers_fused_vk<R, 2>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp);
-  else
-    tracers_fused_vk<R, 1>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp);
+  fused_dispatch<R>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp, false);
 }
 
 template <typename R, int VK>
-void tracer_own_vk(const Launch& l, const Grid<R>& g, const Strides& s, const R* tracr, R* trc_edg) {
-  dim3 grid(tblocks((long long)g.N * (g.L / VK)), l.members, g.T - 1);
+void tracer_own_vk(const Launch& l, const Grid<R>& g, const Strides& s, const R* tracr, R* trc_edg, int tb) {
+  dim3 grid(tblocks((long long)g.N * (g.L / VK), tb), l.members, g.T - 1);
   FIM_KBEGIN(l, "k_tr_own");
-  k_tr_own<R, VK><<<grid, kTB, 0, l.stream>>>(g, s, tracr, trc_edg);
+  k_tr_own<R, VK><<<grid, tb, 0, l.stream>>>(g, s, tracr, trc_edg);
   FIM_KEND(l);
 }
 
 template <typename R>
-void launch_tracer_own(const Launch& l, const Grid<R>& g, const Strides& s, const R* tracr, R* trc_edg, int want) {
+void launch_tracer_own(const Launch& l, const Grid<R>& g, const Strides& s, const R* tracr, R* trc_edg, int want,
+                       int tb) {
   if (g.T < 2) return;
   const int vk = tracer_vk(g, {tracr, trc_edg}, want);
-  if (vk == 4) tracer_own_vk<R, (sizeof(R) == 4 ? 4 : 2)>(l, g, s, tracr, trc_edg);
-  else if (vk == 2) tracer_own_vk<R, 2>(l, g, s, tracr, trc_edg);
-  else tracer_own_vk<R, 1>(l, g, s, tracr, trc_edg);
+  tb = tracer_tb(tb);
+  if (vk == 4) tracer_own_vk<R, (sizeof(R) == 4 ? 4 : 2)>(l, g, s, tracr, trc_edg, tb);
+  else if (vk == 2) tracer_own_vk<R, 2>(l, g, s, tracr, trc_edg, tb);
+  else tracer_own_vk<R, 1>(l, g, s, tracr, trc_edg, tb);
+}
+
+// Autotuner: time k_tr_own + k_tr_lo + k_tr_lim (first tracer chunk) for
+// every (levels per thread, block size) that the layout admits and keep the
+// fastest.  The caller provides step parameters whose nf slot the next step
+// overwrites, so the probe leaves no state behind.
+template <typename R>
+int tune_tracers(const Launch& l, const Grid<R>& g, const Strides& s, const TrcFusedScratch<R>& w, R* trc_edg,
+                 R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx, const R* delp, int* best_vk,
+                 int* best_tb, float* best_ms) {
+  cudaEvent_t a, b;
+  if (cudaEventCreate(&a) != cudaSuccess) return (int)cudaGetLastError();
+  if (cudaEventCreate(&b) != cudaSuccess) { cudaEventDestroy(a); return (int)cudaGetLastError(); }
+  Launch lq = l;
+  lq.prof = nullptr;
+  lq.counter = nullptr;
+  float best = 1e30f;
+  int rc = 0;
+  const int vmax = (int)(16 / sizeof(R));
+  for (int tb : {128, 256}) {
+    for (int vk = 1; vk <= vmax; vk *= 2) {
+      TrcFusedScratch<R> wv = w;
+      wv.vk = vk;
+      wv.tb = tb;
+      if (tracer_vk(g, {trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp, w.trcr_lo}, vk) != vk) continue;
+      float ms = 0.f;
+      for (int rep = 0; rep < 3; rep++) {  // the first repetition warms up
+        cudaEventRecord(a, lq.stream);
+        launch_tracer_own<R>(lq, g, s, tracr, trc_edg, vk, tb);
+        fused_dispatch<R>(lq, g, s, wv, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp, true);
+        cudaEventRecord(b, lq.stream);
+        if (cudaEventSynchronize(b) != cudaSuccess) { rc = (int)cudaGetLastError(); break; }
+        float t = 0.f;
+        cudaEventElapsedTime(&t, a, b);
+        if (rep > 0) ms += t;
+      }
+      if (rc) break;
+      if (ms < best) { best = ms; *best_vk = vk; *best_tb = tb; }
+    }
+    if (rc) break;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (!rc) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = (int)e;
+  }
+  if (best_ms) *best_ms = best / 2;
+  return rc;
 }
 
 #define INSTANTIATE(R)                                                                                        \
   template void launch_tracers_fused<R>(const Launch&, const Grid<R>&, const Strides&,                       \
                                         const TrcFusedScratch<R>&, R*, R*, R*, R*, R*, const R*, const R*);  \
-  template void launch_tracer_own<R>(const Launch&, const Grid<R>&, const Strides&, const R*, R*, int);
+  template void launch_tracer_own<R>(const Launch&, const Grid<R>&, const Strides&, const R*, R*, int, int); \
+  template int tune_tracers<R>(const Launch&, const Grid<R>&, const Strides&, const TrcFusedScratch<R>&, R*, \
+                               R*, R*, R*, R*, const R*, const R*, int*, int*, float*);
 INSTANTIATE(float)
 INSTANTIATE(double)
 

@@ -181,6 +181,13 @@ class Dycore:
                    ctypes.byref(b))
         return qtrcr, {n: getattr(b, n) for n, _ in _lib.Budget._fields_}
 
+    def tracer_shape(self):
+        """(levels per thread, threads per block, probe ms) of the fused tracer kernels."""
+        v, t, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        _lib.check(self.lib.fim_tracer_shape(self.ctx, ctypes.byref(v), ctypes.byref(t), ctypes.byref(ms)),
+                   "fim_tracer_shape", self.ctx)
+        return v.value, t.value, ms.value
+
     def state(self):
         return DycoreState(self)
 

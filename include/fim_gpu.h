@@ -329,6 +329,14 @@ int fim_profile_report(fim_ctx *ctx, char *buf, int len);
 /* Kernel launches issued since the context was created (own kernels only). */
 int64_t fim_launch_count(const fim_ctx *ctx);
 
+/* Shape of the fused tracer kernels (no counterpart in the reference): levels
+ * per thread (1, 2 or 4) and threads per block (128 or 256, the cell patch),
+ * picked by timing the candidates on the state before the first fused step
+ * (0 levels: the widest the layout admits, before tuning); probe_ms is the
+ * winner's time for one probe.  FIM_TRC_VK / FIM_TRC_TB pin the shape and
+ * FIM_AUTOTUNE=0 skips the timing. */
+int fim_tracer_shape(const fim_ctx *ctx, int *levels_per_thread, int *threads_per_block, float *probe_ms);
+
 #ifdef __cplusplus
 }
 #endif
