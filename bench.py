@@ -429,7 +429,8 @@ def accuracy_arm(args, ws, rank, local):
     K = args.accuracy
     marks = sorted({m for m in (1, 10, 50, 100, K) if m <= K})
     use_oracle = glvl <= 6
-    mk = lambda prec: F.FimConfig(nvl=L, ntra=T, dt=wl["dt"], precision=prec)  # noqa: E731
+    dt = args.dt or wl["dt"]
+    mk = lambda prec: F.FimConfig(nvl=L, ntra=T, dt=dt, precision=prec)  # noqa: E731
     host = F.synthetic_state(grid, mk("f64"), seed=wl["seed"], sigma_ps=wl["sigma_ps"], noise=wl["noise"])
     runs = {}
     for prec in ("f64", "f32"):
@@ -493,7 +494,7 @@ def accuracy_arm(args, ws, rank, local):
         out[str(its)] = rec
         del g64, g32, refs
     line = {"metric": "error after K steps against the %s" % ("FP64 CPU oracle" if use_oracle else "FP64 GPU path"),
-            "config": {"workload": args.workload, "glvl": glvl, "nip": N, "nvl": L, "ntra": T, "dt": wl["dt"],
+            "config": {"workload": args.workload, "glvl": glvl, "nip": N, "nvl": L, "ntra": T, "dt": dt,
                        "steps": K, "reference": "oracle" if use_oracle else "gpu_f64"},
             "checkpoints": out}
     print(json.dumps(line))
@@ -522,6 +523,7 @@ def main():
     p.add_argument("--serve-fp64", action="store_true")
     p.add_argument("--accuracy", type=int, default=0, help="report the error after this many steps")
     p.add_argument("--nvl", type=int, default=0)
+    p.add_argument("--dt", type=float, default=0.0, help="time step of the accuracy run (default: workload's)")
     args = p.parse_args()
     if args.warmup < 3:
         args.warmup = 3
