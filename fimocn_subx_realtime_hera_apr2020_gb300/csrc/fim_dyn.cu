@@ -37,7 +37,7 @@ inline unsigned blocks_for(long long n, int b = kBlock) { return (unsigned)((n +
 // into the edge frame, equal-weight interpolate with magnitude correction;
 // mid-layer pressure, Montgomery potential, kinetic energy and tracer 1 (all
 // tracers and dp when hi_order == 0) on the cell's own edges.
-template <typename R>
+template <typename R, int VK>
 __global__ void __launch_bounds__(kBlock) k_edgvar1(Grid<R> g, Strides s, int hi_order,
     const R* __restrict__ u, const R* __restrict__ v, const R* __restrict__ delp,
     const R* __restrict__ pres, const R* __restrict__ montg, const R* __restrict__ tracr,
@@ -45,14 +45,16 @@ __global__ void __launch_bounds__(kBlock) k_edgvar1(Grid<R> g, Strides s, int hi
     R* __restrict__ mont_edg, R* __restrict__ uvsq_edg, R* __restrict__ trc_edg, const float2* __restrict__ mpf,
     R* __restrict__ thold) {
   int i, k;
-  if (!cell_level(g.N, g.L, i, k)) return;
+  if (!cell_levels<VK>(g.N, g.L, i, k)) return;
   const int L = g.L, N = g.N, L1 = L + 1;
   const size_t m = blockIdx.y;
   if (mpf) mpf += m * s.cell;
+  const size_t c = (size_t)i * L + k;
   if (thold) {
     // the potential temperature of this step's edge values, for momtum1
-    thold += m * s.cell;
-    thold[(size_t)i * L + k] = tracr[m * s.tr + (size_t)i * L + k];
+    R th[VK];
+    ldv<VK>(tracr + m * s.tr + c, th);
+    stv<VK>(thold + m * s.cell + c, th);
   }
   u += m * s.cell; v += m * s.cell; delp += m * s.cell; pres += m * s.intf;
   montg += m * s.cell; tracr += m * s.tr;
@@ -61,59 +63,93 @@ __global__ void __launch_bounds__(kBlock) k_edgvar1(Grid<R> g, Strides s, int hi
   const R divby6 = R(1) / R(6), eps = R(0.001), two = R(2), half = R(0.5);
   const int np = g.nprox[i];
   const int* pr = g.prox + i * 6;
-  const R u1 = u[(size_t)i * L + k], v1 = v[(size_t)i * L + k];
-  const R p1a = pres[(size_t)i * L1 + k], p1b = pres[(size_t)i * L1 + k + 1];
-  const R m1 = montg[(size_t)i * L + k];
+  R u1[VK], v1[VK], p1a[VK], p1b[VK], m1[VK];
+  ldv<VK>(u + c, u1);
+  ldv<VK>(v + c, v1);
+  ldv<VK>(montg + c, m1);
+  FOR_V { p1a[j] = pres[(size_t)i * L1 + k + j]; p1b[j] = pres[(size_t)i * L1 + k + j + 1]; }
   for (int e = 0; e < np; e++) {
     const int i2 = pr[e], i3t = pr[e == 0 ? np - 1 : e - 1], i3l = pr[e == np - 1 ? 0 : e + 1];
     const R* cs = g.cs + (i * 6 + e) * 4;
     const R* sn = g.sn + (i * 6 + e) * 4;
-    const R ut = u[(size_t)i3t * L + k], vt = v[(size_t)i3t * L + k];
-    const R u2 = u[(size_t)i2 * L + k], v2 = v[(size_t)i2 * L + k];
-    const R ul = u[(size_t)i3l * L + k], vl = v[(size_t)i3l * L + k];
-    const R u3trl = cs[2] * ut + sn[2] * vt, v3trl = -sn[2] * ut + cs[2] * vt;
-    const R u1ldg = cs[0] * u1 + sn[0] * v1, v1ldg = -sn[0] * u1 + cs[0] * v1;
-    const R u2ldg = cs[1] * u2 + sn[1] * v2, v2ldg = -sn[1] * u2 + cs[1] * v2;
-    const R u3ldg = cs[3] * ul + sn[3] * vl, v3ldg = -sn[3] * ul + cs[3] * vl;
-    R ue = (two * (u1ldg + u2ldg) + u3trl + u3ldg) * divby6;
-    R ve = (two * (v1ldg + v2ldg) + v3trl + v3ldg) * divby6;
-    const R m_1ldg = sqrt(u1ldg * u1ldg + v1ldg * v1ldg);
-    const R m_2ldg = sqrt(u2ldg * u2ldg + v2ldg * v2ldg);
-    const R m_3trl = sqrt(u3trl * u3trl + v3trl * v3trl);
-    const R m_3ldg = sqrt(u3ldg * u3ldg + v3ldg * v3ldg);
-    const R m_1 = sqrt(ue * ue + ve * ve);
-    const R m_2 = (two * (m_1ldg + m_2ldg) + m_3trl + m_3ldg) * divby6;
-    ue = ue * m_2 / rmax(eps, m_1);
-    ve = ve * m_2 / rmax(eps, m_1);
+    R ut[VK], vt[VK], u2[VK], v2[VK], ul[VK], vl[VK];
+    ldv<VK>(u + (size_t)i3t * L + k, ut);
+    ldv<VK>(v + (size_t)i3t * L + k, vt);
+    ldv<VK>(u + (size_t)i2 * L + k, u2);
+    ldv<VK>(v + (size_t)i2 * L + k, v2);
+    ldv<VK>(u + (size_t)i3l * L + k, ul);
+    ldv<VK>(v + (size_t)i3l * L + k, vl);
+    R ue[VK], ve[VK], lp[VK], mo[VK], uv[VK];
+    FOR_V {
+      const R u3trl = cs[2] * ut[j] + sn[2] * vt[j], v3trl = -sn[2] * ut[j] + cs[2] * vt[j];
+      const R u1ldg = cs[0] * u1[j] + sn[0] * v1[j], v1ldg = -sn[0] * u1[j] + cs[0] * v1[j];
+      const R u2ldg = cs[1] * u2[j] + sn[1] * v2[j], v2ldg = -sn[1] * u2[j] + cs[1] * v2[j];
+      const R u3ldg = cs[3] * ul[j] + sn[3] * vl[j], v3ldg = -sn[3] * ul[j] + cs[3] * vl[j];
+      R uu = (two * (u1ldg + u2ldg) + u3trl + u3ldg) * divby6;
+      R vv = (two * (v1ldg + v2ldg) + v3trl + v3ldg) * divby6;
+      const R m_1ldg = sqrt(u1ldg * u1ldg + v1ldg * v1ldg);
+      const R m_2ldg = sqrt(u2ldg * u2ldg + v2ldg * v2ldg);
+      const R m_3trl = sqrt(u3trl * u3trl + v3trl * v3trl);
+      const R m_3ldg = sqrt(u3ldg * u3ldg + v3ldg * v3ldg);
+      const R m_1 = sqrt(uu * uu + vv * vv);
+      const R m_2 = (two * (m_1ldg + m_2ldg) + m_3trl + m_3ldg) * divby6;
+      uu = uu * m_2 / rmax(eps, m_1);
+      vv = vv * m_2 / rmax(eps, m_1);
+      ue[j] = uu;
+      ve[j] = vv;
+      uv[j] = half * (uu * uu + vv * vv);
+      const size_t kk = (size_t)k + j;
+      lp[j] = (p1a[j] + p1b[j] + pres[(size_t)i2 * L1 + kk] + pres[(size_t)i2 * L1 + kk + 1] +
+               half * (pres[(size_t)i3t * L1 + kk] + pres[(size_t)i3t * L1 + kk + 1] +
+                       pres[(size_t)i3l * L1 + kk] + pres[(size_t)i3l * L1 + kk + 1])) * divby6;
+    }
     const size_t o = ((size_t)i * 6 + e) * L + k;
-    u_edg[o] = ue;
-    v_edg[o] = ve;
-    if (!hi_order)
-      dp_edg[o] = (two * (delp[(size_t)i * L + k] + delp[(size_t)i2 * L + k]) + delp[(size_t)i3t * L + k] +
-                   delp[(size_t)i3l * L + k]) * divby6;
-    lp_edg[o] = (p1a + p1b + pres[(size_t)i2 * L1 + k] + pres[(size_t)i2 * L1 + k + 1] +
-                 half * (pres[(size_t)i3t * L1 + k] + pres[(size_t)i3t * L1 + k + 1] +
-                         pres[(size_t)i3l * L1 + k] + pres[(size_t)i3l * L1 + k + 1])) * divby6;
+    stv<VK>(u_edg + o, ue);
+    stv<VK>(v_edg + o, ve);
+    stv<VK>(lp_edg + o, lp);
+    stv<VK>(uvsq_edg + o, uv);
+    if (!hi_order) {
+      R d1[VK], d2[VK], dt[VK], dl[VK], de[VK];
+      ldv<VK>(delp + c, d1);
+      ldv<VK>(delp + (size_t)i2 * L + k, d2);
+      ldv<VK>(delp + (size_t)i3t * L + k, dt);
+      ldv<VK>(delp + (size_t)i3l * L + k, dl);
+      FOR_V de[j] = (two * (d1[j] + d2[j]) + dt[j] + dl[j]) * divby6;
+      stv<VK>(dp_edg + o, de);
+    }
     if (mpf) {
       // edge minus cell value from float-float differences (no cancellation)
-      const float2 mc = mpf[(size_t)i * L + k];
-      mont_edg[o] = R((2.f * ff_diff(mpf[(size_t)i2 * L + k], mc) + ff_diff(mpf[(size_t)i3t * L + k], mc) +
-                       ff_diff(mpf[(size_t)i3l * L + k], mc)) * (1.f / 6.f));
+      FOR_V {
+        const size_t kk = (size_t)k + j;
+        const float2 mc = mpf[(size_t)i * L + kk];
+        mo[j] = R((2.f * ff_diff(mpf[(size_t)i2 * L + kk], mc) + ff_diff(mpf[(size_t)i3t * L + kk], mc) +
+                   ff_diff(mpf[(size_t)i3l * L + kk], mc)) * (1.f / 6.f));
+      }
     } else {
-      mont_edg[o] = (two * (m1 + montg[(size_t)i2 * L + k]) + montg[(size_t)i3t * L + k] +
-                     montg[(size_t)i3l * L + k]) * divby6;
+      R m2[VK], mt[VK], ml[VK];
+      ldv<VK>(montg + (size_t)i2 * L + k, m2);
+      ldv<VK>(montg + (size_t)i3t * L + k, mt);
+      ldv<VK>(montg + (size_t)i3l * L + k, ml);
+      FOR_V mo[j] = (two * (m1[j] + m2[j]) + mt[j] + ml[j]) * divby6;
     }
-    uvsq_edg[o] = half * (ue * ue + ve * ve);
+    stv<VK>(mont_edg + o, mo);
   }
   const int ntr = hi_order ? 1 : g.T;
   for (int t = 0; t < ntr; t++) {
     const R* tr = tracr + (size_t)t * N * L;
     R* te = trc_edg + (size_t)t * N * 6 * L;
-    te[((size_t)i * 6 + 5) * L + k] = R(0);
+    R z[VK], t1[VK];
+    FOR_V z[j] = R(0);
+    stv<VK>(te + ((size_t)i * 6 + 5) * L + k, z);
+    ldv<VK>(tr + c, t1);
     for (int e = 0; e < np; e++) {
       const int i2 = pr[e], i3t = pr[e == 0 ? np - 1 : e - 1], i3l = pr[e == np - 1 ? 0 : e + 1];
-      te[((size_t)i * 6 + e) * L + k] = (two * (tr[(size_t)i * L + k] + tr[(size_t)i2 * L + k]) +
-                                         tr[(size_t)i3t * L + k] + tr[(size_t)i3l * L + k]) * divby6;
+      R t2[VK], tt[VK], tl[VK], out[VK];
+      ldv<VK>(tr + (size_t)i2 * L + k, t2);
+      ldv<VK>(tr + (size_t)i3t * L + k, tt);
+      ldv<VK>(tr + (size_t)i3l * L + k, tl);
+      FOR_V out[j] = (two * (t1[j] + t2[j]) + tt[j] + tl[j]) * divby6;
+      stv<VK>(te + ((size_t)i * 6 + e) * L + k, out);
     }
   }
 }
@@ -122,11 +158,11 @@ __global__ void __launch_bounds__(kBlock) k_edgvar1(Grid<R> g, Strides s, int hi
 // edgvar3 loop 1 with edgvalEval (edgvar3.F90:66-94,136-163): least-squares
 // (hfcoef) reconstruction of dp (field 0) and tracers 2..ntra (field t) on the
 // cell's own edges; pentagons store 0 in the sixth slot.
-template <typename R>
+template <typename R, int VK>
 __global__ void __launch_bounds__(kBlock) k_edgvar3_own(Grid<R> g, Strides s,
     const R* __restrict__ delp, const R* __restrict__ tracr, R* __restrict__ dp_edg, R* __restrict__ trc_edg) {
   int i, k;
-  if (!cell_level(g.N, g.L, i, k)) return;
+  if (!cell_levels<VK>(g.N, g.L, i, k)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
   const int f = blockIdx.z;
@@ -134,32 +170,44 @@ __global__ void __launch_bounds__(kBlock) k_edgvar3_own(Grid<R> g, Strides s,
   R* dst = (f == 0) ? dp_edg + m * s.edge : trc_edg + m * s.tredg + (size_t)f * N * 6 * L;
   const int np = g.nprox[i];
   const int* pr = g.prox + i * 6;
-  const R bc = src[(size_t)i * L + k];
-  R d[6];
+  R bc[VK];
+  ldv<VK>(src + (size_t)i * L + k, bc);
+  R d[6][VK];
 #pragma unroll
-  for (int j = 0; j < 6; j++) d[j] = (j < np) ? src[(size_t)pr[j] * L + k] - bc : R(0);
+  for (int e = 0; e < 6; e++) {
+    if (e < np) {
+      ldv<VK>(src + (size_t)pr[e] * L + k, d[e]);
+      FOR_V d[e][j] = d[e][j] - bc[j];
+    } else {
+      FOR_V d[e][j] = R(0);
+    }
+  }
   const R* hf = g.hfcoef + (size_t)i * 36;
 #pragma unroll
   for (int ie = 0; ie < 6; ie++) {
-    R val = R(0);
+    R val[VK];
+    FOR_V val[j] = R(0);
     if (ie < np) {
-      val = bc;
+      FOR_V val[j] = bc[j];
 #pragma unroll
-      for (int j = 0; j < 6; j++)
-        if (j < np) val = val + d[j] * hf[ie * 6 + j];
+      for (int e = 0; e < 6; e++)
+        if (e < np) {
+          const R h = hf[ie * 6 + e];
+          FOR_V val[j] = val[j] + d[e][j] * h;
+        }
     }
-    dst[((size_t)i * 6 + ie) * L + k] = val;
+    stv<VK>(dst + ((size_t)i * 6 + ie) * L + k, val);
   }
 }
 
 // edgvar3 loop 2 (edgvar3.F90:110-132): the lower-numbered cell of each pair
 // stores the two-sided average in both slots, as the reference does; each slot
 // has exactly one writer, which is also its only reader.
-template <typename R>
+template <typename R, int VK>
 __global__ void __launch_bounds__(kBlock) k_edgvar3_avg(Grid<R> g, Strides s, R* __restrict__ dp_edg,
                                                        R* __restrict__ trc_edg) {
   int i, k;
-  if (!cell_level(g.N, g.L, i, k)) return;
+  if (!cell_levels<VK>(g.N, g.L, i, k)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
   const int f = blockIdx.z;
@@ -170,9 +218,12 @@ __global__ void __launch_bounds__(kBlock) k_edgvar3_avg(Grid<R> g, Strides s, R*
     if (i < nb) {
       const int os = g.proxs[i * 6 + e];
       const size_t a = ((size_t)i * 6 + e) * L + k, b = ((size_t)nb * 6 + os) * L + k;
-      const R w = R(0.5) * (x[a] + x[b]);
-      x[a] = w;
-      x[b] = w;
+      R xa[VK], xb[VK], w[VK];
+      ldv<VK>(x + a, xa);
+      ldv<VK>(x + b, xb);
+      FOR_V w[j] = R(0.5) * (xa[j] + xb[j]);
+      stv<VK>(x + a, w);
+      stv<VK>(x + b, w);
     }
   }
 }
@@ -182,13 +233,13 @@ __global__ void __launch_bounds__(kBlock) k_edgvar3_avg(Grid<R> g, Strides s, R*
 // edge and on the neighbour's copy of it, donor-cell mass flux, antidiffusive
 // flux, low-order tendency and low-order thickness; also the Zalesak sums
 // P+/P- of cnuity3 (cnuity_compute.F90:186-194), which only need own edges.
-template <typename R>
+template <typename R, int VK>
 __global__ void __launch_bounds__(kBlock) k_cnuity12(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     const R* __restrict__ u_edg, const R* __restrict__ v_edg, const R* __restrict__ dp_edg,
     const R* __restrict__ delp, R* __restrict__ massfx, R* __restrict__ dplo_tndcy, R* __restrict__ antifx,
     R* __restrict__ delp_lo, R* __restrict__ p_plus, R* __restrict__ p_mnus) {
   int i, k;
-  if (!cell_level(g.N, g.L, i, k)) return;
+  if (!cell_levels<VK>(g.N, g.L, i, k)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
   sp += m;
@@ -201,44 +252,62 @@ __global__ void __launch_bounds__(kBlock) k_cnuity12(Grid<R> g, Strides s, const
   R* mfn = massfx + (size_t)nf * N * 6 * L;
   const int np = g.nprox[i];
   const R half = R(0.5);
-  const R dpi = delp[(size_t)i * L + k];
-  R sum = R(0), pp = R(0), pm = R(0);
+  R dpi[VK], sum[VK], pp[VK], pm[VK];
+  ldv<VK>(delp + (size_t)i * L + k, dpi);
+  FOR_V { sum[j] = R(0); pp[j] = R(0); pm[j] = R(0); }
   if (np < 6) {
-    mfn[((size_t)i * 6 + 5) * L + k] = R(0);
-    antifx[((size_t)i * 6 + 5) * L + k] = R(0);
+    R z[VK];
+    FOR_V z[j] = R(0);
+    stv<VK>(mfn + ((size_t)i * 6 + 5) * L + k, z);
+    stv<VK>(antifx + ((size_t)i * 6 + 5) * L + k, z);
   }
   for (int e = 0; e < np; e++) {
     const int ipx = g.prox[i * 6 + e], edx = g.proxs[i * 6 + e];
     const R* sv = g.sve + (i * 6 + e) * 2;
     const R* sx = g.sve + (ipx * 6 + edx) * 2;
     const size_t o = ((size_t)i * 6 + e) * L + k, ox = ((size_t)ipx * 6 + edx) * L + k;
-    const R vn = sv[1] * u_edg[o] - sv[0] * v_edg[o];
-    const R vx = sx[1] * u_edg[ox] - sx[0] * v_edg[ox];
-    const R flxhi = vn * dp_edg[o];
-    const R mf = half * ((vn + rabs(vn)) * dpi - (vx + rabs(vx)) * delp[(size_t)ipx * L + k]);
-    mfn[o] = mf;
-    const R a = flxhi - mf;
-    antifx[o] = a;
-    sum = sum + mf;
-    if (a <= R(0)) pp = pp - a;
-    else pm = pm + a;
+    R ue[VK], ve[VK], ux[VK], vx_[VK], de[VK], dx[VK], mf[VK], an[VK];
+    ldv<VK>(u_edg + o, ue);
+    ldv<VK>(v_edg + o, ve);
+    ldv<VK>(u_edg + ox, ux);
+    ldv<VK>(v_edg + ox, vx_);
+    ldv<VK>(dp_edg + o, de);
+    ldv<VK>(delp + (size_t)ipx * L + k, dx);
+    FOR_V {
+      const R vn = sv[1] * ue[j] - sv[0] * ve[j];
+      const R vx = sx[1] * ux[j] - sx[0] * vx_[j];
+      const R flxhi = vn * de[j];
+      mf[j] = half * ((vn + rabs(vn)) * dpi[j] - (vx + rabs(vx)) * dx[j]);
+      const R a = flxhi - mf[j];
+      an[j] = a;
+      sum[j] = sum[j] + mf[j];
+      if (a <= R(0)) pp[j] = pp[j] - a;
+      else pm[j] = pm[j] + a;
+    }
+    stv<VK>(mfn + o, mf);
+    stv<VK>(antifx + o, an);
   }
   const size_t c = (size_t)i * L + k;
-  const R tn = -sum * g.rarea[i];
-  dplo_tndcy[(size_t)nf * N * L + c] = tn;
-  delp_lo[c] = dpi + ab1 * tn + ab2 * dplo_tndcy[(size_t)of * N * L + c] + ab3 * dplo_tndcy[(size_t)vof * N * L + c];
-  p_plus[c] = pp;
-  p_mnus[c] = pm;
+  const R rar = g.rarea[i];
+  R tn[VK], to[VK], tv[VK], lo[VK];
+  FOR_V tn[j] = -sum[j] * rar;
+  stv<VK>(dplo_tndcy + (size_t)nf * N * L + c, tn);
+  ldv<VK>(dplo_tndcy + (size_t)of * N * L + c, to);
+  ldv<VK>(dplo_tndcy + (size_t)vof * N * L + c, tv);
+  FOR_V lo[j] = dpi[j] + ab1 * tn[j] + ab2 * to[j] + ab3 * tv[j];
+  stv<VK>(delp_lo + c, lo);
+  stv<VK>(p_plus + c, pp);
+  stv<VK>(p_mnus + c, pm);
 }
 
 // cnuity3 (cnuity_compute.F90:206-252): 1-ring max/min of old and low-order
 // thickness, Zalesak Q+/Q- and the limiters R+/R-.
-template <typename R>
+template <typename R, int VK>
 __global__ void __launch_bounds__(kBlock) k_cnuity3(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     const R* __restrict__ delp_lo, const R* __restrict__ delp, const R* __restrict__ dp_tndcy,
     const R* __restrict__ p_plus, const R* __restrict__ p_mnus, R* __restrict__ r_plus, R* __restrict__ r_mnus) {
   int i, k;
-  if (!cell_level(g.N, g.L, i, k)) return;
+  if (!cell_levels<VK>(g.N, g.L, i, k)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
   sp += m;
@@ -250,32 +319,43 @@ __global__ void __launch_bounds__(kBlock) k_cnuity3(Grid<R> g, Strides s, const 
   const R thshld = R(1.e-11);
   const size_t c = (size_t)i * L + k;
   const int* pr = g.prox + i * 6;
-  const R dlo = delp_lo[c];
-  R dpmax = rmax(dlo, delp[c]), dpmin = rmin(dlo, delp[c]);
+  R dlo[VK], dc[VK], mx[VK], mn[VK];
+  ldv<VK>(delp_lo + c, dlo);
+  ldv<VK>(delp + c, dc);
+  FOR_V { mx[j] = rmax(dlo[j], dc[j]); mn[j] = rmin(dlo[j], dc[j]); }
 #pragma unroll
   for (int e = 0; e < 6; e++) {
-    const R a = delp_lo[(size_t)pr[e] * L + k], b = delp[(size_t)pr[e] * L + k];
-    dpmax = rmax(dpmax, rmax(a, b));
-    dpmin = rmin(dpmin, rmin(a, b));
+    R a[VK], b[VK];
+    ldv<VK>(delp_lo + (size_t)pr[e] * L + k, a);
+    ldv<VK>(delp + (size_t)pr[e] * L + k, b);
+    FOR_V { mx[j] = rmax(mx[j], rmax(a[j], b[j])); mn[j] = rmin(mn[j], rmin(a[j], b[j])); }
   }
-  dpmax = rmax(R(0), dpmax);
-  dpmin = rmax(R(0), dpmin);
-  const R to = dp_tndcy[(size_t)of * N * L + c], tv = dp_tndcy[(size_t)vof * N * L + c];
-  const R q_plus = (dpmax - dlo - (ab2 * rmin(R(0), to) + ab3 * rmax(R(0), tv))) / ab1 * g.area[i];
-  const R q_mnus = (dlo - dpmin + (ab2 * rmax(R(0), to) + ab3 * rmin(R(0), tv))) / ab1 * g.area[i];
-  r_plus[c] = rmax(R(0), rmin(R(1), q_plus / rmax(p_plus[c], thshld)));
-  r_mnus[c] = rmax(R(0), rmin(R(1), q_mnus / rmax(p_mnus[c], thshld)));
+  R to[VK], tv[VK], pp[VK], pm[VK], rp[VK], rm[VK];
+  ldv<VK>(dp_tndcy + (size_t)of * N * L + c, to);
+  ldv<VK>(dp_tndcy + (size_t)vof * N * L + c, tv);
+  ldv<VK>(p_plus + c, pp);
+  ldv<VK>(p_mnus + c, pm);
+  const R ar = g.area[i];
+  FOR_V {
+    const R dpmax = rmax(R(0), mx[j]), dpmin = rmax(R(0), mn[j]);
+    const R q_plus = (dpmax - dlo[j] - (ab2 * rmin(R(0), to[j]) + ab3 * rmax(R(0), tv[j]))) / ab1 * ar;
+    const R q_mnus = (dlo[j] - dpmin + (ab2 * rmax(R(0), to[j]) + ab3 * rmin(R(0), tv[j]))) / ab1 * ar;
+    rp[j] = rmax(R(0), rmin(R(1), q_plus / rmax(pp[j], thshld)));
+    rm[j] = rmax(R(0), rmin(R(1), q_mnus / rmax(pm[j], thshld)));
+  }
+  stv<VK>(r_plus + c, rp);
+  stv<VK>(r_mnus + c, rm);
 }
 
 // cnuity4 (cnuity_compute.F90:291-369): clip the antidiffusive flux with the
 // own and neighbour limiters, total mass flux, AB3 thickness update.
-template <typename R>
+template <typename R, int VK>
 __global__ void __launch_bounds__(kBlock) k_cnuity4(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     const R* __restrict__ antifx, const R* __restrict__ r_plus, const R* __restrict__ r_mnus,
     R* __restrict__ massfx, const R* __restrict__ dplo_tndcy, R* __restrict__ dp_tndcy, R* __restrict__ delp,
     int* __restrict__ flags) {
   int i, k;
-  if (!cell_level(g.N, g.L, i, k)) return;
+  if (!cell_levels<VK>(g.N, g.L, i, k)) return;
   const int L = g.L, N = g.N;
   const size_t m = blockIdx.y;
   sp += m;
@@ -286,24 +366,42 @@ __global__ void __launch_bounds__(kBlock) k_cnuity4(Grid<R> g, Strides s, const 
   const R ab1 = R(sp->ab1), ab2 = R(sp->ab2), ab3 = R(sp->ab3);
   R* mfn = massfx + (size_t)nf * N * 6 * L;
   const size_t c = (size_t)i * L + k;
-  const R rp = r_plus[c], rm = r_mnus[c];
+  R rp[VK], rm[VK], at[VK];
+  ldv<VK>(r_plus + c, rp);
+  ldv<VK>(r_mnus + c, rm);
+  FOR_V at[j] = R(0);
   const int np = g.nprox[i];
-  R at = R(0);
   for (int e = 0; e < np; e++) {
     const int px = g.prox[i * 6 + e];
     const size_t o = ((size_t)i * 6 + e) * L + k;
-    R a = antifx[o];
-    const R clip = (a >= R(0)) ? rmin(rm, r_plus[(size_t)px * L + k]) : rmin(rp, r_mnus[(size_t)px * L + k]);
-    a = a * clip;
-    mfn[o] = mfn[o] + a;
-    at = at + a;
+    R a[VK], mf[VK], rpx[VK], rmx[VK];
+    ldv<VK>(antifx + o, a);
+    ldv<VK>(mfn + o, mf);
+    ldv<VK>(r_plus + (size_t)px * L + k, rpx);
+    ldv<VK>(r_mnus + (size_t)px * L + k, rmx);
+    FOR_V {
+      const R clip = (a[j] >= R(0)) ? rmin(rm[j], rpx[j]) : rmin(rp[j], rmx[j]);
+      const R ac = a[j] * clip;
+      mf[j] = mf[j] + ac;
+      at[j] = at[j] + ac;
+    }
+    stv<VK>(mfn + o, mf);
   }
-  at = -at * g.rarea[i];
-  const R tn = dplo_tndcy[(size_t)nf * N * L + c] + at;
-  dp_tndcy[(size_t)nf * N * L + c] = tn;
-  const R dn = delp[c] + ab1 * tn + ab2 * dp_tndcy[(size_t)of * N * L + c] + ab3 * dp_tndcy[(size_t)vof * N * L + c];
-  delp[c] = dn;
-  if (!(dn > R(0))) atomicOr(flags + m, kFlagBadDp);
+  const R rar = g.rarea[i];
+  R tl[VK], tn[VK], to[VK], tv[VK], dn[VK];
+  ldv<VK>(dplo_tndcy + (size_t)nf * N * L + c, tl);
+  FOR_V tn[j] = tl[j] + (-at[j] * rar);
+  stv<VK>(dp_tndcy + (size_t)nf * N * L + c, tn);
+  ldv<VK>(dp_tndcy + (size_t)of * N * L + c, to);
+  ldv<VK>(dp_tndcy + (size_t)vof * N * L + c, tv);
+  ldv<VK>(delp + c, dn);
+  bool bad = false;
+  FOR_V {
+    dn[j] = dn[j] + ab1 * tn[j] + ab2 * to[j] + ab3 * tv[j];
+    bad = bad || !(dn[j] > R(0));
+  }
+  stv<VK>(delp + c, dn);
+  if (bad) atomicOr(flags + m, kFlagBadDp);
 }
 
 // cnuity5 (cnuity_compute.F90:408-445): one warp per column; the top-down
@@ -744,12 +842,12 @@ __global__ void __launch_bounds__(kBlock) k_del4prep(Grid<R> g, Strides s, const
 // dissip (momtum_compute.F90:149-208): thickness-weighted harmonic momentum
 // fluxes across the edges, rotated back; increments du, dv. The work fields are
 // u+grndspd, v (momtum.F90:99-106) or the del4prep output when wu != nullptr.
-template <typename R>
+template <typename R, int VK>
 __global__ void __launch_bounds__(kBlock) k_dissip(Grid<R> g, Strides s, const R* __restrict__ u,
     const R* __restrict__ v, const R* __restrict__ wu, const R* __restrict__ wv, const R* __restrict__ delp,
     R* __restrict__ du, R* __restrict__ dv) {
   int i, k;
-  if (!cell_level(g.N, g.L, i, k)) return;
+  if (!cell_levels<VK>(g.N, g.L, i, k)) return;
   const int L = g.L;
   const size_t m = blockIdx.y;
   u += m * s.cell; v += m * s.cell; delp += m * s.cell; du += m * s.cell; dv += m * s.cell;
@@ -757,34 +855,58 @@ __global__ void __launch_bounds__(kBlock) k_dissip(Grid<R> g, Strides s, const R
   if (prep) { wu += m * s.cell; wv += m * s.cell; }
   const R thshld = R(1.e-11), two = R(2);
   const size_t c = (size_t)i * L + k;
-  const R ui = prep ? wu[c] : u[c] + g.grndspd[i];
-  const R vi = prep ? wv[c] : v[c];
-  const R dpi = rmax(delp[c], thshld);
-  const R factor = g.rarea[i] / dpi;
-  const R dfl = g.dfflen[k];
+  R ui[VK], vi[VK], dpi[VK], factor[VK], dfl[VK], su[VK], sv[VK];
+  if (prep) {
+    ldv<VK>(wu + c, ui);
+    ldv<VK>(wv + c, vi);
+  } else {
+    ldv<VK>(u + c, ui);
+    ldv<VK>(v + c, vi);
+    const R gs = g.grndspd[i];
+    FOR_V ui[j] = ui[j] + gs;
+  }
+  ldv<VK>(delp + c, dpi);
+  const R rar = g.rarea[i];
+  FOR_V {
+    dpi[j] = rmax(dpi[j], thshld);
+    factor[j] = rar / dpi[j];
+    dfl[j] = g.dfflen[k + j];
+    su[j] = R(0);
+    sv[j] = R(0);
+  }
   const int np = g.nprox[i];
-  R su = R(0), sv = R(0);
   for (int e = 0; e < np; e++) {
     const int ipx = g.prox[i * 6 + e];
     const R* cs = g.cs + (i * 6 + e) * 4;
     const R* sn = g.sn + (i * 6 + e) * 4;
     const size_t cx = (size_t)ipx * L + k;
-    const R ux = prep ? wu[cx] : u[cx] + g.grndspd[ipx];
-    const R vx = prep ? wv[cx] : v[cx];
-    const R uxy1 = cs[0] * ui + sn[0] * vi, vxy1 = -sn[0] * ui + cs[0] * vi;
-    const R uxy2 = cs[1] * ux + sn[1] * vx, vxy2 = -sn[1] * ux + cs[1] * vx;
-    const R b = rmax(delp[cx], thshld);
-    const R hf = dpi * b / (dpi + b);
+    R ux[VK], vx[VK], bx[VK];
+    if (prep) {
+      ldv<VK>(wu + cx, ux);
+      ldv<VK>(wv + cx, vx);
+    } else {
+      ldv<VK>(u + cx, ux);
+      ldv<VK>(v + cx, vx);
+      const R gx = g.grndspd[ipx];
+      FOR_V ux[j] = ux[j] + gx;
+    }
+    ldv<VK>(delp + cx, bx);
     const R sl = g.sideln[i * 6 + e];
-    const R ufx = (uxy2 - uxy1) * dfl * sl * two * hf;
-    const R vfx = (vxy2 - vxy1) * dfl * sl * two * hf;
-    const R uflux = cs[0] * ufx - sn[0] * vfx;
-    const R vflux = sn[0] * ufx + cs[0] * vfx;
-    su = su + uflux * factor;
-    sv = sv + vflux * factor;
+    FOR_V {
+      const R uxy1 = cs[0] * ui[j] + sn[0] * vi[j], vxy1 = -sn[0] * ui[j] + cs[0] * vi[j];
+      const R uxy2 = cs[1] * ux[j] + sn[1] * vx[j], vxy2 = -sn[1] * ux[j] + cs[1] * vx[j];
+      const R b = rmax(bx[j], thshld);
+      const R hf = dpi[j] * b / (dpi[j] + b);
+      const R ufx = (uxy2 - uxy1) * dfl[j] * sl * two * hf;
+      const R vfx = (vxy2 - vxy1) * dfl[j] * sl * two * hf;
+      const R uflux = cs[0] * ufx - sn[0] * vfx;
+      const R vflux = sn[0] * ufx + cs[0] * vfx;
+      su[j] = su[j] + uflux * factor[j];
+      sv[j] = sv[j] + vflux * factor[j];
+    }
   }
-  du[c] = su;
-  dv[c] = sv;
+  stv<VK>(du + c, su);
+  stv<VK>(dv + c, sv);
 }
 
 // momtum1 (momtum_compute.F90:278-423, janjic=0) after adding the dissipation
@@ -941,22 +1063,27 @@ void launch_edgvar1(const Launch& l, const Grid<R>& g, const Strides& s, int hi_
                     const R* v, const R* delp, const R* pres, const R* montg, const R* tracr,
                     R* u_edg, R* v_edg, R* dp_edg, R* lp_edg, R* mont_edg, R* uvsq_edg, R* trc_edg,
                     const float2* mpf, R* thold) {
-  dim3 grid(blocks_for((long long)g.N * g.L), l.members);
+  const int vk = pick_vk<R>(g.L, {u, v, delp, montg, tracr, u_edg, v_edg, dp_edg, lp_edg, mont_edg, uvsq_edg,
+                                  trc_edg, thold});
   FIM_KBEGIN(l, "k_edgvar1");
-  k_edgvar1<R><<<grid, kBlock, 0, l.stream>>>(g, s, hi_order, u, v, delp, pres, montg, tracr, u_edg, v_edg,
-                                               dp_edg, lp_edg, mont_edg, uvsq_edg, trc_edg, mpf, thold);
+  FIM_VK_DISPATCH(R, vk, (k_edgvar1<R, VK><<<dim3(blocks_for((long long)g.N * (g.L / VK)), l.members), kBlock, 0,
+                                             l.stream>>>(g, s, hi_order, u, v, delp, pres, montg, tracr, u_edg,
+                                                         v_edg, dp_edg, lp_edg, mont_edg, uvsq_edg, trc_edg, mpf,
+                                                         thold)));
   FIM_KEND(l);
 }
 
 template <typename R>
 void launch_edgvar3(const Launch& l, const Grid<R>& g, const Strides& s, const R* delp, const R* tracr,
                     R* dp_edg, R* trc_edg, int nfields) {
-  dim3 grid(blocks_for((long long)g.N * g.L), l.members, nfields);
+  const int vk = pick_vk<R>(g.L, {delp, tracr, dp_edg, trc_edg});
   FIM_KBEGIN(l, "k_edgvar3_own");
-  k_edgvar3_own<R><<<grid, kBlock, 0, l.stream>>>(g, s, delp, tracr, dp_edg, trc_edg);
+  FIM_VK_DISPATCH(R, vk, (k_edgvar3_own<R, VK><<<dim3(blocks_for((long long)g.N * (g.L / VK)), l.members, nfields),
+                                                 kBlock, 0, l.stream>>>(g, s, delp, tracr, dp_edg, trc_edg)));
   FIM_KEND(l);
   FIM_KBEGIN(l, "k_edgvar3_avg");
-  k_edgvar3_avg<R><<<grid, kBlock, 0, l.stream>>>(g, s, dp_edg, trc_edg);
+  FIM_VK_DISPATCH(R, vk, (k_edgvar3_avg<R, VK><<<dim3(blocks_for((long long)g.N * (g.L / VK)), l.members, nfields),
+                                                 kBlock, 0, l.stream>>>(g, s, dp_edg, trc_edg)));
   FIM_KEND(l);
 }
 
@@ -964,18 +1091,22 @@ template <typename R>
 void launch_cnuity(const Launch& l, const Grid<R>& g, const Strides& s, const CnuityScratch<R>& w, const R* u,
                    const R* v, const R* u_edg, const R* v_edg, const R* dp_edg, const R* lp_edg,
                    R* delp, R* pres, R* exner, R* dp_tndcy, R* dplo_tndcy, R* massfx, R* omega) {
-  dim3 grid(blocks_for((long long)g.N * g.L), l.members);
+  const int vk = pick_vk<R>(g.L, {u_edg, v_edg, dp_edg, delp, massfx, dplo_tndcy, dp_tndcy, w.antifx, w.delp_lo,
+                                  w.p_plus, w.p_mnus, w.r_plus, w.r_mnus});
   FIM_KBEGIN(l, "k_cnuity12");
-  k_cnuity12<R><<<grid, kBlock, 0, l.stream>>>(g, s, l.sp, u_edg, v_edg, dp_edg, delp, massfx, dplo_tndcy,
-                                                w.antifx, w.delp_lo, w.p_plus, w.p_mnus);
+  FIM_VK_DISPATCH(R, vk, (k_cnuity12<R, VK><<<dim3(blocks_for((long long)g.N * (g.L / VK)), l.members), kBlock, 0,
+                                              l.stream>>>(g, s, l.sp, u_edg, v_edg, dp_edg, delp, massfx,
+                                                          dplo_tndcy, w.antifx, w.delp_lo, w.p_plus, w.p_mnus)));
   FIM_KEND(l);
   FIM_KBEGIN(l, "k_cnuity3");
-  k_cnuity3<R><<<grid, kBlock, 0, l.stream>>>(g, s, l.sp, w.delp_lo, delp, dp_tndcy, w.p_plus, w.p_mnus,
-                                               w.r_plus, w.r_mnus);
+  FIM_VK_DISPATCH(R, vk, (k_cnuity3<R, VK><<<dim3(blocks_for((long long)g.N * (g.L / VK)), l.members), kBlock, 0,
+                                             l.stream>>>(g, s, l.sp, w.delp_lo, delp, dp_tndcy, w.p_plus, w.p_mnus,
+                                                         w.r_plus, w.r_mnus)));
   FIM_KEND(l);
   FIM_KBEGIN(l, "k_cnuity4");
-  k_cnuity4<R><<<grid, kBlock, 0, l.stream>>>(g, s, l.sp, w.antifx, w.r_plus, w.r_mnus, massfx, dplo_tndcy,
-                                               dp_tndcy, delp, l.flags);
+  FIM_VK_DISPATCH(R, vk, (k_cnuity4<R, VK><<<dim3(blocks_for((long long)g.N * (g.L / VK)), l.members), kBlock, 0,
+                                             l.stream>>>(g, s, l.sp, w.antifx, w.r_plus, w.r_mnus, massfx,
+                                                         dplo_tndcy, dp_tndcy, delp, l.flags)));
   FIM_KEND(l);
   dim3 gw(blocks_for((long long)g.N * 32), l.members);
   FIM_KBEGIN(l, "k_cnuity5");
@@ -1024,8 +1155,10 @@ void launch_momtum(const Launch& l, const Grid<R>& g, const Strides& s, const Kn
       wu = w.wu;
       wv = w.wv;
     }
+    const int vk = pick_vk<R>(g.L, {u, v, wu, wv, dp3d, w.du, w.dv});
     FIM_KBEGIN(l, "k_dissip");
-    k_dissip<R><<<grid, kBlock, 0, l.stream>>>(g, s, u, v, wu, wv, dp3d, w.du, w.dv);
+    FIM_VK_DISPATCH(R, vk, (k_dissip<R, VK><<<dim3(blocks_for((long long)g.N * (g.L / VK)), l.members), kBlock, 0,
+                                              l.stream>>>(g, s, u, v, wu, wv, dp3d, w.du, w.dv)));
     FIM_KEND(l);
     du = w.du;
     dv = w.dv;

@@ -2,8 +2,10 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
 #include <cstddef>
 #include <cstdint>
+#include <initializer_list>
 #include <map>
 #include <string>
 #include <vector>
@@ -166,6 +168,80 @@ struct Launch {
     if ((l).counter) ++*(l).counter;                                     \
   } while (0)
 
+
+// ---- level vectors: VK consecutive levels per thread ----------------------
+// Cell and edge fields are level-fastest, so VK consecutive levels of one
+// column are one 4/8/16-byte access.  pick_vk chooses the widest VK (at most
+// 16 bytes) that nvl and the alignment of every pointer admit.
+template <typename R, int VK> struct VecOf;
+template <typename R> struct VecOf<R, 1> { using T = R; };
+template <> struct VecOf<float, 2> { using T = float2; };
+template <> struct VecOf<float, 4> { using T = float4; };
+template <> struct VecOf<double, 2> { using T = double2; };
+
+template <int VK, typename R>
+__device__ __forceinline__ void ldv(const R* p, R (&r)[VK]) {
+  if constexpr (VK == 1) {
+    r[0] = *p;
+  } else if constexpr (VK == 2) {
+    const typename VecOf<R, 2>::T t = *reinterpret_cast<const typename VecOf<R, 2>::T*>(p);
+    r[0] = t.x; r[1] = t.y;
+  } else {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    r[0] = t.x; r[1] = t.y; r[2] = t.z; r[3] = t.w;
+  }
+}
+
+template <int VK, typename R>
+__device__ __forceinline__ void stv(R* p, const R (&r)[VK]) {
+  if constexpr (VK == 1) {
+    *p = r[0];
+  } else if constexpr (VK == 2) {
+    typename VecOf<R, 2>::T t; t.x = r[0]; t.y = r[1];
+    *reinterpret_cast<typename VecOf<R, 2>::T*>(p) = t;
+  } else {
+    float4 t; t.x = r[0]; t.y = r[1]; t.z = r[2]; t.w = r[3];
+    *reinterpret_cast<float4*>(p) = t;
+  }
+}
+
+#define FOR_V _Pragma("unroll") for (int j = 0; j < VK; j++)
+
+// (cell, first level) of thread gid over nip x (nvl/VK)
+template <int VK>
+__device__ __forceinline__ bool cell_levels(int N, int L, int& i, int& k) {
+  const int LV = L / VK;
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= N * LV) return false;
+  i = gid / LV;
+  k = (gid - i * LV) * VK;
+  return true;
+}
+
+template <typename R>
+inline int pick_vk(int L, std::initializer_list<const void*> ptrs, int want = 0) {
+  int vk = want > 0 ? want : (int)(16 / sizeof(R));
+  if ((int)sizeof(R) * vk > 16) vk = (int)(16 / sizeof(R));
+  while (vk > 1 && L % vk != 0) vk /= 2;
+  for (const void* p : ptrs)
+    while (vk > 1 && p && ((uintptr_t)p % (vk * sizeof(R))) != 0) vk /= 2;
+  return vk;
+}
+
+// run CALL with the compile-time constant VK equal to vk (4 only for float)
+#define FIM_VK_DISPATCH(R, vk, CALL)                          \
+  do {                                                        \
+    if ((vk) >= 4 && sizeof(R) == 4) {                        \
+      constexpr int VK = sizeof(R) == 4 ? 4 : 2;              \
+      CALL;                                                   \
+    } else if ((vk) >= 2) {                                   \
+      constexpr int VK = 2;                                   \
+      CALL;                                                   \
+    } else {                                                  \
+      constexpr int VK = 1;                                   \
+      CALL;                                                   \
+    }                                                         \
+  } while (0)
 
 // ---- float-float arithmetic (FP32-mixed build) ----------------------------
 // A value hi + lo with |lo| <= ulp(hi)/2 carries ~48 significant bits on the

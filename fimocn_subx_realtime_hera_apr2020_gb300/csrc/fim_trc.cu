@@ -14,9 +14,6 @@
 //
 // Every flux is formed from the same operands in the same order as the
 // per-routine kernels, so results are bit-identical to them.
-#include <cstdint>
-#include <initializer_list>
-
 #include "fim_internal.h"
 
 namespace fim {
@@ -32,41 +29,6 @@ template <typename R> __device__ __forceinline__ R tabs(R a) { return a < R(0) ?
 constexpr int kTB = 256;
 constexpr int kTBMin = 4;
 inline unsigned tblocks(long long n, int tb) { return (unsigned)((n + tb - 1) / tb); }
-
-// VK consecutive levels per thread, moved with one 4/8/16-byte access
-template <typename R, int VK> struct VecOf;
-template <typename R> struct VecOf<R, 1> { using T = R; };
-template <> struct VecOf<float, 2> { using T = float2; };
-template <> struct VecOf<float, 4> { using T = float4; };
-template <> struct VecOf<double, 2> { using T = double2; };
-
-template <int VK, typename R>
-__device__ __forceinline__ void ldv(const R* p, R (&r)[VK]) {
-  if constexpr (VK == 1) {
-    r[0] = *p;
-  } else if constexpr (VK == 2) {
-    const typename VecOf<R, 2>::T t = *reinterpret_cast<const typename VecOf<R, 2>::T*>(p);
-    r[0] = t.x; r[1] = t.y;
-  } else {
-    const float4 t = *reinterpret_cast<const float4*>(p);
-    r[0] = t.x; r[1] = t.y; r[2] = t.z; r[3] = t.w;
-  }
-}
-
-template <int VK, typename R>
-__device__ __forceinline__ void stv(R* p, const R (&r)[VK]) {
-  if constexpr (VK == 1) {
-    *p = r[0];
-  } else if constexpr (VK == 2) {
-    typename VecOf<R, 2>::T t; t.x = r[0]; t.y = r[1];
-    *reinterpret_cast<typename VecOf<R, 2>::T*>(p) = t;
-  } else {
-    float4 t; t.x = r[0]; t.y = r[1]; t.z = r[2]; t.w = r[3];
-    *reinterpret_cast<float4*>(p) = t;
-  }
-}
-
-#define FOR_V _Pragma("unroll") for (int j = 0; j < VK; j++)
 
 // own-side least-squares edge values of tracers 1..T-1 (0-based), z = tracer
 template <typename R, int VK>
@@ -344,8 +306,6 @@ __global__ void __launch_bounds__(kTB, kTBMin) k_tr_hi(Grid<R> g, Strides s, con
   stv<VK>(tracr + m * s.tr + (size_t)t * NL + c, out);
 }
 
-#undef FOR_V
-
 template <typename R, int VK>
 void tracers_fused_vk(const Launch& l, const Grid<R>& g, const Strides& s, const TrcFusedScratch<R>& w,
                       R* trc_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx, const R* delp,
@@ -375,12 +335,7 @@ void tracers_fused_vk(const Launch& l, const Grid<R>& g, const Strides& s, const
 // (256-byte aligned), checked here.
 template <typename R>
 int tracer_vk(const Grid<R>& g, std::initializer_list<const void*> ptrs, int want) {
-  int vk = want > 0 ? want : (int)(16 / sizeof(R));
-  if ((int)sizeof(R) * vk > 16) vk = (int)(16 / sizeof(R));
-  while (vk > 1 && g.L % vk != 0) vk /= 2;
-  for (const void* p : ptrs)
-    while (vk > 1 && ((uintptr_t)p % (vk * sizeof(R))) != 0) vk /= 2;
-  return vk;
+  return pick_vk<R>(g.L, ptrs, want);
 }
 
 inline int tracer_tb(int tb) { return tb == 256 ? 256 : 128; }
