@@ -44,7 +44,7 @@ WORDS = {
     "k_trcadv1": lambda T: 27 * T, "k_trcadv2": lambda T: 16 * T, "k_trcadv3": lambda T: 18 * T,
     "k_dissip": lambda T: 5, "k_del4prep": lambda T: 4, "k_momtum1": lambda T: 44,
     "k_regrid": lambda T: 3, "k_dffusn_lev": lambda T: 2, "k_remap": lambda T: 2 * T + 10, "k_inflate": lambda T: 2,
-    "k_hystat": lambda T: 2 * T + 7, "k_globsum_levels": lambda T: T + 1,
+    "k_hystat": lambda T: 7, "k_hystat_trdp": lambda T: 2 * T + 3, "k_globsum_levels": lambda T: T + 1,
 }
 
 E2E_FIELDS = ["us3d", "vs3d", "dp3d", "pr3d", "ex3d", "ph3d", "mp3d", "tr3d", "trdp", "u_tdcy", "v_tdcy",

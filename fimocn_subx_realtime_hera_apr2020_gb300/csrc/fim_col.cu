@@ -815,25 +815,24 @@ int prepare_hybgen(int L) {
 // hystat (hystat.F90:53-109): one warp per column; surface pressure sum and
 // the bottom-up Montgomery potential / geopotential recursion are warp scans
 // in FP64 (FP64 build) or float-float (FP32-mixed build, which also keeps the
-// (hi, lo) Montgomery potential for the pressure gradient); humidity floors
-// and tracer x thickness per level.
+// (hi, lo) Montgomery potential for the pressure gradient).  The humidity
+// floors and tracer x thickness are k_hystat_trdp.
 template <typename R>
 __global__ void __launch_bounds__(kBlock2) k_hystat(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     R* __restrict__ ph3d, const R* __restrict__ ex3d, R* __restrict__ mp3d, const R* __restrict__ dp3d,
-    R* __restrict__ tr3d, R* __restrict__ trdp, R* __restrict__ psrf, R* __restrict__ ptdcy,
+    const R* __restrict__ tr3d, R* __restrict__ psrf, R* __restrict__ ptdcy,
     float2* __restrict__ mpf, int bnd) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
+  const int N = g.N, L = g.L, L1 = L + 1;
   if (warp >= N) return;
   const int i = warp;
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active || (bnd && sp->its <= 1)) return;
   ph3d += m * s.intf; ex3d += m * s.intf; mp3d += m * s.cell; dp3d += m * s.cell; tr3d += m * s.tr;
-  trdp += m * s.tr; psrf += m * s.col; ptdcy += m * 2 * s.col;
+  psrf += m * s.col; ptdcy += m * 2 * s.col;
   if (mpf) mpf += m * s.cell;
   const int its = sp->its - bnd;
-  const size_t NL = (size_t)N * L;
   if constexpr (sizeof(R) == 4) {
     // float-float sums and scan (FP64-accurate on the FP32 pipes)
     FF2 ps{0.f, 0.f};
@@ -918,16 +917,38 @@ __global__ void __launch_bounds__(kBlock2) k_hystat(Grid<R> g, Strides s, const 
       carry += __shfl_sync(0xffffffffu, sc, 31);
     }
   }
+}
+
+// hystat.F90:72-98, the per-level part: humidity floors and tracer x
+// thickness, VK levels per thread (a stream over all tracers of a column
+// slice; kept apart from the column scans so its loads are not serialised
+// behind them)
+template <typename R, int VK>
+__global__ void __launch_bounds__(kBlock2) k_hystat_trdp(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
+    const R* __restrict__ dp3d, R* __restrict__ tr3d, R* __restrict__ trdp, int bnd) {
+  int i, k;
+  if (!cell_levels<VK>(g.N, g.L, i, k)) return;
+  const int N = g.N, L = g.L, T = g.T;
+  const size_t m = blockIdx.y;
+  sp += m;
+  if (!sp->active || (bnd && sp->its <= 1)) return;
+  const size_t NL = (size_t)N * L;
+  const size_t c = (size_t)i * L + k;
+  dp3d += m * s.cell; tr3d += m * s.tr; trdp += m * s.tr;
   const R qvmin = R(kQvmin), qwmin = R(kQwmin);
-  for (int k = lane; k < L; k += 32) {
-    const size_t c = (size_t)i * L + k;
-    const R dp = dp3d[c];
-    for (int t = 0; t < T; t++) {
-      R x = tr3d[(size_t)t * NL + c];
-      if (t == 1) { x = cmax(qvmin, x); tr3d[(size_t)t * NL + c] = x; }
-      if (t == 2) { x = cmax(qwmin, x); tr3d[(size_t)t * NL + c] = x; }
-      trdp[(size_t)t * NL + c] = x * dp;
+  R dp[VK];
+  ldv<VK>(dp3d + c, dp);
+#pragma unroll 4
+  for (int t = 0; t < T; t++) {
+    R x[VK], y[VK];
+    ldv<VK>(tr3d + (size_t)t * NL + c, x);
+    if (t == 1 || t == 2) {
+      const R floor = t == 1 ? qvmin : qwmin;
+      FOR_V x[j] = cmax(floor, x[j]);
+      stv<VK>(tr3d + (size_t)t * NL + c, x);
     }
+    FOR_V y[j] = x[j] * dp[j];
+    stv<VK>(trdp + (size_t)t * NL + c, y);
   }
 }
 
@@ -1174,8 +1195,14 @@ void launch_hystat(const Launch& l, const Grid<R>& g, const Strides& s, R* ph3d,
                    const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy, float2* mpf) {
   dim3 gw(nblocks((long long)g.N * 32, kBlock2), l.members);
   FIM_KBEGIN(l, "k_hystat");
-  k_hystat<R><<<gw, kBlock2, 0, l.stream>>>(g, s, l.sp, ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy, mpf,
+  k_hystat<R><<<gw, kBlock2, 0, l.stream>>>(g, s, l.sp, ph3d, ex3d, mp3d, dp3d, tr3d, psrf, ptdcy, mpf,
                                              l.boundary);
+  FIM_KEND(l);
+  const int vk = pick_vk<R>(g.L, {dp3d, tr3d, trdp});
+  FIM_KBEGIN(l, "k_hystat_trdp");
+  FIM_VK_DISPATCH(R, vk, (k_hystat_trdp<R, VK><<<dim3(nblocks((long long)g.N * (g.L / VK), kBlock2), l.members),
+                                                 kBlock2, 0, l.stream>>>(g, s, l.sp, dp3d, tr3d, trdp,
+                                                                         l.boundary)));
   FIM_KEND(l);
 }
 
