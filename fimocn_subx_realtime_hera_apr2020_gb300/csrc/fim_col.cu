@@ -486,85 +486,40 @@ __global__ void __launch_bounds__(kColBlock) k_remap(Grid<R> g, Strides s, Knobs
   if (bad) atomicOr(flags + m, kFlagColumnIntegral);
 }
 
-// ------------------------------------------------- remap, warp per column --
-// remap_1d for the default knobs (PLM, remap_optn = 2; one-layer migration,
-// miglim = 1).
+// ------------------------------------------ remap, warp per column, lane = levels --
+// remap_1d (hybgen.F90:515-700) for the default knobs: PLM pcwise with
+// one-layer migration (remap_optn = 2, miglim = 1).
 //  k_inflate: inflate, the one serial recursion of the column set-up, lane =
 //             column over 32 columns per warp staged in shared memory;
-//  k_remap_w: one warp per column: lanes over levels build the new interfaces
-//             and the remap geometry, then lane = field (u, v, tracers
-//             2..ntra in pressure, theta in p^(kappa+1)) runs pcwise's
-//             recurrences on its column of a shared-memory tile that is
-//             loaded and stored coalesced.
+//  k_remap_v: each warp runs kColsPerWarp consecutive columns.  Lane l holds
+//             levels l*VL .. l*VL+VL-1 of the field in hand (u, v, tracers
+//             2..ntra in pressure, theta in p^(kappa+1)), so a field's column
+//             is one contiguous read and write.  The three interface arrays
+//             and the fields of the warp's columns stream through a ring of
+//             shared-memory slots filled by cp.async several items ahead,
+//             across column boundaries.
+// Given the filled values, pcwise's flux form is level-parallel: PLM slopes
+// and interface fluxes take the neighbouring levels from the adjacent lanes.
+// The massless-layer fills of pcwise and remap_1d's tracer fill are
+// first-order linear recurrences x(k) = a(k) x(k-+1) + b(k): each lane
+// composes the maps of its levels, a warp scan of the composed maps gives the
+// value entering each lane, and the lane runs the recurrence in the
+// reference's form over its own levels.  The pairwise theta redistribution
+// toward the target (hybgen.F90:648-667) is a nonlinear sweep over the
+// column: it runs after the warp's last column with lane = column.
 // With one-layer migration the donor layer, slab width and dx of every
 // interface depend on the coordinate only, so they are formed once per column
-// and each field's flux pass is branch-free; all fields run one instruction
-// stream (theta differs only in the geometry it reads).  Divisions by the
-// coordinate thicknesses (fco + small, fcn + small) become products with
-// reciprocals formed once per column: results differ from pcwise above by
-// rounding.
-constexpr int kTS = 33;   // tile row stride (32 fields + 1: conflict-free transposes)
-constexpr int kWarpsRemap = 4;
+// and held in registers; divisions by the coordinate thicknesses (fco +
+// small, fcn + small) become products with reciprocals.  Results differ from
+// the serial pcwise by rounding.
 constexpr int kWarpsInflate = 4;
-
-template <typename R, int ML>
-struct RemapGeo {          // one coordinate (pressure or p^(kappa+1))
-  R fo[ML], rfo[ML], rfn[ML];    // fco, 1/(fco+small), 1/(fcn+small)
-  R hx[ML + 1], dsl[ML + 1], nd[ML + 1];  // interface k: (dx-1) or (1-dx), slab width, -delz
-  int ly[ML + 1];                // donor layer of interface k
-  int thin;                      // some layer is thin enough for the massless-layer fill to matter
-};
+constexpr int kWarpsRemapV = 4;
+constexpr int kColsPerWarp = 8;
 
 // pcwise's massless-layer fill moves y(k) by (y(k+-1) - y(k)) * 1e-22 / fco(k):
 // below the rounding of either precision unless fco(k) is under ~1e-4.
 template <typename R>
 __device__ __forceinline__ R fill_thin() { return R(1.2e-4); }
-
-template <typename R, int ML>
-struct RemapSm {
-  R tile[ML * kTS];              // field values, lane = field
-  RemapGeo<R, ML> gp, gk;
-  R exold[ML + 1], exnew[ML + 1], prcol[ML + 1], prnew[ML + 1], pk1col[ML + 1], pk1new[ML + 1];
-  R dpcol[ML];
-};
-
-// pcwise's coordinate quantities for xold -> xnew, lanes over levels
-template <typename R, int ML>
-__device__ void remap_geo(int L, int lane, const R* xold, const R* xnew, RemapGeo<R, ML>& G) {
-  const R small = R(1.e-22);
-  const bool flip = !(xold[0] < xold[L]);
-  bool thin = false;
-  for (int k = lane; k < L; k += 32) {
-    const R fo = flip ? cmax(R(0), (-xold[k + 1]) - (-xold[k])) : cmax(R(0), xold[k + 1] - xold[k]);
-    const R fn = flip ? cmax(R(0), (-xnew[k + 1]) - (-xnew[k])) : cmax(R(0), xnew[k + 1] - xnew[k]);
-    G.fo[k] = fo;
-    G.rfo[k] = R(1) / (fo + small);
-    G.rfn[k] = R(1) / (fn + small);
-    thin = thin || fo < fill_thin<R>();
-  }
-  thin = __any_sync(0xffffffffu, thin);
-  if (lane == 0) G.thin = thin ? 1 : 0;
-  __syncwarp();
-  for (int k = lane; k <= L; k += 32) {
-    const R d = flip ? (-xnew[k]) - (-xold[k]) : xnew[k] - xold[k];
-    int lyr = 0;
-    R hx = R(0), dsl = R(0);
-    if (k >= 1 && k <= L - 1 && d != R(0)) {
-      lyr = d > R(0) ? k : k - 1;
-      const R fl = G.fo[lyr];
-      if (fl > R(0)) {
-        const R dd = d > R(0) ? d : -d;
-        dsl = cmin(R(0) + fl, dd) - cmin(R(0), dd);
-        const R dx = dsl / fl;
-        hx = d > R(0) ? dx - R(1) : R(1) - dx;
-      }
-    }
-    G.ly[k] = lyr;
-    G.hx[k] = hx;
-    G.dsl[k] = dsl;
-    G.nd[k] = -d;
-  }
-}
 
 // PLM slope of a layer from its filled value f and its neighbours' fm, fp
 template <typename R>
@@ -573,60 +528,253 @@ __device__ __forceinline__ R plm_slope(R fm, R f, R fp) {
   return (f <= cmin(fm, fp) || f >= cmax(fm, fp)) ? R(0) : b;
 }
 
-// pcwise (PLM, miglim = 1) in place on one lane's tile column y (stride kTS).
-// The backward massless-layer fill is one pass (skipped for columns without
-// thin layers, where it only rounds); the forward fill, the PLM slopes, the
-// interface fluxes and the update are a second pass over a three-value window
-// held in registers, which writes slot k as soon as its new value is known
-// (later steps read only slots above k).
-// Returns true when the column-integral check fails (FP64 build only).
-template <typename R, int ML>
-__device__ bool pcwise_lane(int kk, R* y, const RemapGeo<R, ML>& G) {
+// asynchronous global -> shared copy of B = 4, 8 or 16 bytes
+template <int B>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(sa), "l"(gmem), "n"(B) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <typename R>
+__device__ __forceinline__ R warp_sum(R v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+// Value entering each lane of a recurrence x <- a x + b whose per-lane
+// composed map is (a, b): from the lanes below (up) or above (down); the
+// first lane of the sweep receives 0 (its own map is constant there).
+template <typename R>
+__device__ __forceinline__ R affine_entry_up(int lane, R a, R b) {
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const R ao = __shfl_up_sync(0xffffffffu, a, off), bo = __shfl_up_sync(0xffffffffu, b, off);
+    if (lane >= off) { b = a * bo + b; a = a * ao; }
+  }
+  const R e = __shfl_up_sync(0xffffffffu, b, 1);
+  return lane == 0 ? R(0) : e;
+}
+template <typename R>
+__device__ __forceinline__ R affine_entry_down(int lane, R a, R b) {
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const R ao = __shfl_down_sync(0xffffffffu, a, off), bo = __shfl_down_sync(0xffffffffu, b, off);
+    if (lane + off < 32) { b = a * bo + b; a = a * ao; }
+  }
+  const R e = __shfl_down_sync(0xffffffffu, b, 1);
+  return lane == 31 ? R(0) : e;
+}
+
+// shared memory of one warp: the copy ring, the column arrays, and theta of
+// the warp's columns awaiting the redistribution (values, p^(kappa+1)
+// thicknesses, their floor and, FP64 build, the input column integrals)
+template <typename R, int VL>
+struct RemapV {
+  static constexpr int S = 32 * VL + 4;                 // slot: nvl + 1 <= 32 VL + 1 values
+  static constexpr int D = sizeof(R) == 4 ? 8 : 6;      // items in flight
+  R ring[D][S];
+  R exold[S], prcol[S], exnew[S], prnew[S], pk1col[S], pk1new[S], dpcol[S], tg[S];
+  R thb[kColsPerWarp][S], dkb[kColsPerWarp][S];
+  R flo[kColsPerWarp], colin[kColsPerWarp], colscl[kColsPerWarp];
+};
+static_assert(sizeof(RemapV<float, 1>) % 16 == 0 && sizeof(RemapV<double, 1>) % 16 == 0,
+              "ring slots of consecutive warps stay 16-byte aligned");
+
+// pcwise's coordinate quantities for one lane's levels and interfaces
+template <typename R, int VL>
+struct LaneGeo {
+  R fo[VL], rfo[VL], rfn[VL];  // level kb+v: fco, 1/(fco+small), 1/(fcn+small)
+  R nd[VL], hh[VL];            // interface kb+v: -delz (0: no flux), (dx-1 | 1-dx)/2
+  unsigned up;                 // bit v: interface kb+v takes layer kb+v as donor
+  bool thin;                   // (warp) some layer is thin enough for the fill to matter
+};
+
+template <typename R>
+__device__ __forceinline__ R coord_thick(bool flip, const R* x, int k) {
+  return flip ? cmax(R(0), (-x[k + 1]) - (-x[k])) : cmax(R(0), x[k + 1] - x[k]);
+}
+
+template <typename R, int VL>
+__device__ __forceinline__ void lane_geo(int L, int lane, const R* xo, const R* xn, LaneGeo<R, VL>& G) {
   const R small = R(1.e-22);
+  const bool flip = !(xo[0] < xo[L]);
+  const int kb = lane * VL;
+  bool thin = false;
+  unsigned up = 0u;
+#pragma unroll
+  for (int v = 0; v < VL; v++) {
+    const int k = kb + v;
+    R fo = R(0), fn = R(0);
+    if (k < L) {
+      fo = coord_thick(flip, xo, k);
+      fn = coord_thick(flip, xn, k);
+      thin = thin || fo < fill_thin<R>();
+    }
+    G.fo[v] = fo;
+    G.rfo[v] = R(1) / (fo + small);
+    G.rfn[v] = R(1) / (fn + small);
+    R nd = R(0), hh = R(0);
+    if (k >= 1 && k <= L - 1) {
+      const R d = flip ? (-xn[k]) - (-xo[k]) : xn[k] - xo[k];
+      if (d != R(0)) {
+        const R fl = coord_thick(flip, xo, d > R(0) ? k : k - 1);
+        if (fl > R(0)) {
+          const R dd = d > R(0) ? d : -d;
+          const R dsl = cmin(R(0) + fl, dd) - cmin(R(0), dd);
+          const R dx = dsl / fl;
+          const R hx = d > R(0) ? dx - R(1) : R(1) - dx;
+          if (dsl != R(0)) {
+            nd = -d;
+            hh = R(.5) * hx;
+          }
+        }
+        if (d > R(0)) up |= 1u << v;
+      }
+    }
+    G.nd[v] = nd;
+    G.hh[v] = hh;
+  }
+  G.up = up;
+  G.thin = __any_sync(0xffffffffu, thin);
+}
+
+// pcwise (PLM, miglim = 1) of one field, lane = levels kb .. kb+VL-1 of y.
+// Returns true when the column-integral check fails (FP64 build only).
+template <typename R, int VL>
+__device__ __forceinline__ bool pcwise_v(int L, int lane, R (&y)[VL], const LaneGeo<R, VL>& G) {
+  const R small = R(1.e-22);
+  const int kb = lane * VL;
   R bfore = R(0), colscl = R(0);
   if (sizeof(R) == 8) {
-    for (int k = 0; k < kk; k++) {
-      bfore = bfore + y[k * kTS] * G.fo[k];
-      colscl = colscl + cabs(y[k * kTS] * G.fo[k]);
+#pragma unroll
+    for (int v = 0; v < VL; v++)
+      if (kb + v < L) {
+        bfore += y[v] * G.fo[v];
+        colscl += cabs(y[v] * G.fo[v]);
+      }
+  }
+  R yf[VL];
+  if (G.thin) {
+    // backward fill: nb(nvl) = y(nvl), nb(k) = (y(k) fco(k) + nb(k+1) small) / (fco(k) + small)
+    R a = R(1), b = R(0);
+#pragma unroll
+    for (int v = VL - 1; v >= 0; v--) {
+      const int k = kb + v;
+      if (k == L - 1) {
+        a = R(0);
+        b = y[v];
+      } else if (k < L) {
+        const R A = small * G.rfo[v];
+        b = A * b + y[v] * G.fo[v] * G.rfo[v];
+        a = A * a;
+      }
+    }
+    R x = affine_entry_down(lane, a, b);
+    R nb[VL];
+#pragma unroll
+    for (int v = VL - 1; v >= 0; v--) {
+      const int k = kb + v;
+      if (k == L - 1) x = y[v];
+      else if (k < L) x = (y[v] * G.fo[v] + x * small) * G.rfo[v];
+      nb[v] = x;
+    }
+    // forward fill: yf(1) = nb(1), yf(k) = (nb(k) fco(k) + yf(k-1) small) / (fco(k) + small)
+    a = R(1);
+    b = R(0);
+#pragma unroll
+    for (int v = 0; v < VL; v++) {
+      const int k = kb + v;
+      if (k == 0) {
+        a = R(0);
+        b = nb[v];
+      } else if (k < L) {
+        const R A = small * G.rfo[v];
+        b = A * b + nb[v] * G.fo[v] * G.rfo[v];
+        a = A * a;
+      }
+    }
+    x = affine_entry_up(lane, a, b);
+#pragma unroll
+    for (int v = 0; v < VL; v++) {
+      const int k = kb + v;
+      if (k == 0) x = nb[v];
+      else if (k < L) x = (nb[v] * G.fo[v] + x * small) * G.rfo[v];
+      yf[v] = x;
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < VL; v++) yf[v] = y[v];
+  }
+  // PLM slopes (zero in the end layers)
+  const R ym = __shfl_up_sync(0xffffffffu, yf[VL - 1], 1);
+  const R yp = __shfl_down_sync(0xffffffffu, yf[0], 1);
+  R bk[VL];
+#pragma unroll
+  for (int v = 0; v < VL; v++) {
+    const int k = kb + v;
+    const R fm = v > 0 ? yf[v - 1] : ym;
+    const R fp = v < VL - 1 ? yf[v + 1] : yp;
+    bk[v] = (k >= 1 && k <= L - 2) ? plm_slope(fm, yf[v], fp) : R(0);
+  }
+  // interface fluxes; one donor layer: vertfx = -dz * (fcdx * slab) / slab = -dz * fcdx
+  const R bm = __shfl_up_sync(0xffffffffu, bk[VL - 1], 1);
+  R fl[VL];
+#pragma unroll
+  for (int v = 0; v < VL; v++) {
+    const bool up = (G.up >> v) & 1u;
+    const R a = up ? yf[v] : (v > 0 ? yf[v - 1] : ym);
+    const R b = up ? bk[v] : (v > 0 ? bk[v - 1] : bm);
+    fl[v] = G.nd[v] != R(0) ? G.nd[v] * (a + b * G.hh[v]) : R(0);
+  }
+  const R fnext = __shfl_down_sync(0xffffffffu, fl[0], 1);
+  R after = R(0);
+#pragma unroll
+  for (int v = 0; v < VL; v++) {
+    const int k = kb + v;
+    if (k < L) {
+      const R vn = (k + 1 < L) ? (v < VL - 1 ? fl[v + 1] : fnext) : R(0);
+      const R amount = yf[v] * G.fo[v] - (vn - fl[v]);
+      after += amount;
+      y[v] = (amount + yf[v] * small) * G.rfn[v];
     }
   }
-  const bool fill = G.thin != 0;
-  if (fill) {
-    R nb = y[(kk - 1) * kTS];
-    for (int k = kk - 2; k >= 0; k--) {
-      nb = (y[k * kTS] * G.fo[k] + nb * small) * G.rfo[k];
-      y[k * kTS] = nb;
+  if (sizeof(R) == 8) {
+    const R dif = warp_sum(bfore - after), scl = warp_sum(colscl);
+    return cabs(dif) > cmax(R(1.e-33), R(1.e-11) * scl);
+  }
+  return false;
+}
+
+// VL consecutive values at p (VL * sizeof(R) bytes, aligned to min(16, that))
+template <typename R, int VL>
+__device__ __forceinline__ void st_lane(R* p, const R (&y)[VL]) {
+  if constexpr (VL * sizeof(R) <= 16) {
+    stv<VL>(p, y);
+  } else {
+#pragma unroll
+    for (int h = 0; h < VL; h += 2) {
+      double2 t;
+      t.x = y[h];
+      t.y = y[h + 1];
+      *reinterpret_cast<double2*>(p + h) = t;
     }
   }
-  // window: y0 = filled(k), y1 = filled(k+1); bk = slope of layer k
-  R y0 = y[0];
-  R y1 = fill ? (y[kTS] * G.fo[1] + y0 * small) * G.rfo[1] : y[kTS];
-  R bk = R(0);
-  R after = R(0), vprev = R(0);
-  for (int k = 0; k < kk; k++) {
-    R y2 = y1;
-    if (k + 2 < kk) {
-      y2 = y[(k + 2) * kTS];
-      if (fill) y2 = (y2 * G.fo[k + 2] + y1 * small) * G.rfo[k + 2];
-    }
-    const R bk1 = (k + 1 >= 1 && k + 1 <= kk - 2) ? plm_slope(y0, y1, y2) : R(0);
-    R vnext = R(0);
-    if (k + 1 < kk) {
-      const R dsl = G.dsl[k + 1];
-      const bool up = G.ly[k + 1] == k + 1;
-      const R a = up ? y1 : y0, b = up ? bk1 : bk;
-      // one donor layer: vertfx = -dz * (fcdx * slab) / slab = -dz * fcdx
-      vnext = dsl != R(0) ? G.nd[k + 1] * (a + b * R(.5) * G.hx[k + 1]) : R(0);
-    }
-    const R amount = y0 * G.fo[k] - (vnext - vprev);
-    after = after + amount;
-    y[k * kTS] = (amount + y0 * small) * G.rfn[k];
-    y0 = y1;
-    y1 = y2;
-    bk = bk1;
-    vprev = vnext;
+}
+
+// one lane's levels of a field column: VL wide when vec, else value by value
+template <typename R, int VL>
+__device__ __forceinline__ void store_levels(R* dst, int L, int kb, int vec, const R (&y)[VL]) {
+  if (vec) {
+    if (kb < L) st_lane<R, VL>(dst + kb, y);
+  } else {
+#pragma unroll
+    for (int v = 0; v < VL; v++)
+      if (kb + v < L) dst[kb + v] = y[v];
   }
-  return sizeof(R) == 8 && cabs(bfore - after) > cmax(R(1.e-33), R(1.e-11) * colscl);
 }
 
 // inflate (hybgen.F90:893-1007) of 32 columns per warp, lane = column
@@ -650,161 +798,283 @@ __global__ void __launch_bounds__(32 * kWarpsInflate) k_inflate(Grid<R> g, Strid
   for (int q = lane; q < ncol * L1; q += 32) exn[(size_t)i0 * L1 + q] = col[q];
 }
 
-template <typename R, int ML>
-__global__ void __launch_bounds__(32 * kWarpsRemap) k_remap_w(Grid<R> g, Strides s, Knobs kn,
+// vec: every field column starts on a min(16, VL*sizeof(R))-byte boundary
+// and nvl is a multiple of VL (the copies and stores are then VL wide)
+template <typename R, int VL>
+__global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Strides s, Knobs kn,
     const StepParams* __restrict__ sp, const R* __restrict__ targt, const R* __restrict__ exsmo,
     R* __restrict__ us3d, R* __restrict__ vs3d, R* __restrict__ tr3d, R* __restrict__ sdot,
-    R* __restrict__ ex3d, R* __restrict__ dp3d, R* __restrict__ pr3d, int* __restrict__ flags, int bnd) {
+    R* __restrict__ ex3d, R* __restrict__ dp3d, R* __restrict__ pr3d, int* __restrict__ flags, int bnd,
+    int vec) {
+  using W = RemapV<R, VL>;
+  constexpr int D = W::D;
+  constexpr int CB = VL * (int)sizeof(R) < 16 ? VL * (int)sizeof(R) : 16;  // bytes per copy
+  constexpr int CE = CB / (int)sizeof(R);                                  // values per copy
   extern __shared__ __align__(16) unsigned char smraw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
-  const int i = blockIdx.x * kWarpsRemap + wib;
-  if (i >= N) return;
+  const int c0 = (blockIdx.x * kWarpsRemapV + wib) * kColsPerWarp;
+  if (c0 >= N) return;
+  const int ncol = (N - c0 < kColsPerWarp) ? N - c0 : kColsPerWarp;
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active || (bnd && sp->its <= 1)) return;
-  RemapSm<R, ML>& S = reinterpret_cast<RemapSm<R, ML>*>(smraw)[wib];
+  W& S = reinterpret_cast<W*>(smraw)[wib];
   exsmo += m * s.intf; us3d += m * s.cell; vs3d += m * s.cell; tr3d += m * s.tr; sdot += m * s.intf;
   ex3d += m * s.intf; dp3d += m * s.cell; pr3d += m * s.intf;
   const int its = sp->its - bnd;
   const R cp = R(kCp), rd = R(kRd), p1000 = R(kP1000), small = R(1.e-6);
-  const size_t ci = (size_t)i * L1;
-  for (int k = lane; k <= L; k += 32) {
-    const R eo = ex3d[ci + k], pc = pr3d[ci + k];
-    R en = exsmo[ci + k];
-    if (its > 0) {
-      const R sl = R(kn.slak);
-      en = sl * en + (R(1) - sl) * eo;
+  const int kb = lane * VL;
+  // items per column: ex3d, pr3d, exsmo, then fields 0 = u, 1 = v,
+  // 2..T = tracers 2..ntra, T+1 = theta
+  const int F = T + 2, I = F + 3;
+  auto field = [&](int f, int i) -> R* {
+    return f == 0 ? us3d + (size_t)i * L : f == 1 ? vs3d + (size_t)i * L
+         : f <= T ? tr3d + ((size_t)(f - 1) * N + i) * L : tr3d + (size_t)i * L;
+  };
+  // copy item j of column c0 + c into ring slot q (an empty group past the last column)
+  auto issue = [&](int c, int j, int q) {
+    if (c < ncol) {
+      const int i = c0 + c;
+      R* slot = S.ring[q];
+      if (j < 3) {
+        const R* src = (j == 0 ? ex3d : j == 1 ? pr3d : exsmo) + (size_t)i * L1;
+        for (int k = lane; k <= L; k += 32) cp_async<sizeof(R)>(slot + k, src + k);
+      } else {
+        const R* src = field(j - 3, i);
+        if (vec) {
+          if (kb < L) {
+#pragma unroll
+            for (int h = 0; h < VL; h += CE) cp_async<CB>(slot + kb + h, src + kb + h);
+          }
+        } else {
+#pragma unroll
+          for (int v = 0; v < VL; v++)
+            if (kb + v < L) cp_async<sizeof(R)>(slot + kb + v, src + kb + v);
+        }
+      }
     }
-    S.exold[k] = eo;
-    S.prcol[k] = pc;
-    S.exnew[k] = en;
-    S.pk1col[k] = eo * pc / cp;
+    cp_async_commit();
+  };
+  for (int k = lane; k < L; k += 32) S.tg[k] = targt[k];
+  int ic = 0, ij = 0;   // next item to copy
+  for (int q = 0; q < D; q++) {
+    issue(ic, ij, q);
+    if (++ij == I) { ij = 0; ++ic; }
   }
-  __syncwarp();
-  // miglim = 1: exnew(2..nvl) between the neighbouring old interfaces
-  for (int k = 2 + lane; k <= L; k += 32)
-    S.exnew[k - 1] = cmax(R(.0001) * S.exold[k - 1] + R(.9999) * S.exold[k],
-                          cmin(R(.0001) * S.exold[k - 1] + R(.9999) * S.exold[k - 2], S.exnew[k - 1]));
-  __syncwarp();
-  for (int k = lane; k <= L; k += 32) S.prnew[k] = p1000 * pow(S.exnew[k] / cp, cp / rd);
-  __syncwarp();
-  for (int k = lane; k <= L; k += 32) {
-    if (k < L) S.dpcol[k] = S.prnew[k] - S.prnew[k + 1];
-    S.pk1new[k] = S.exnew[k] * S.prnew[k] / cp;
-  }
-  __syncwarp();
-  if (lane == 0) {
-    S.prnew[L] = S.prcol[L];
-    S.pk1new[L] = S.pk1col[L];
-    S.prnew[0] = S.prcol[0];
-    S.pk1new[0] = S.pk1col[0];
-  }
-  __syncwarp();
-  remap_geo<R, ML>(L, lane, S.prcol, S.prnew, S.gp);
-  remap_geo<R, ML>(L, lane, S.pk1col, S.pk1new, S.gk);
-  __syncwarp();
-  // fields: 0 = u, 1 = v, 2..T = tracers 2..ntra, T+1 = theta
-  const int F = T + 2;
+  LaneGeo<R, VL> gp;
+  R dpv[VL], qqv[VL];
   bool bad = false;
-  for (int base = 0; base < F; base += 32) {
-    const int nf = (F - base < 32) ? F - base : 32;
-    for (int q = 0; q < nf; q++) {
-      const int f = base + q;
-      const R* col = f == 0 ? us3d + (size_t)i * L : f == 1 ? vs3d + (size_t)i * L
-                   : f <= T ? tr3d + ((size_t)(f - 1) * N + i) * L : tr3d + (size_t)i * L;
-      for (int k = lane; k < L; k += 32) S.tile[k * kTS + q] = col[k];
+  int c = 0, j = 0, qs = 0;   // item in hand: column, item, ring slot
+  while (c < ncol) {
+    cp_async_wait<D - 1>();
+    __syncwarp();
+    const int i = c0 + c;
+    const R* slot = S.ring[qs];
+    R y[VL];
+    if (j < 3) {
+      R* dst = j == 0 ? S.exold : j == 1 ? S.prcol : S.exnew;
+      for (int k = lane; k <= L; k += 32) dst[k] = slot[k];
+    } else {
+#pragma unroll
+      for (int v = 0; v < VL; v++) y[v] = kb + v < L ? slot[kb + v] : R(0);
     }
     __syncwarp();
-    if (lane < nf) {
-      const int f = base + lane;
-      const bool theta = f == T + 1;
-      R* y = S.tile + lane;
-      R colin = R(0), colscl = R(0);
-      if (sizeof(R) == 8 && theta) {
-        for (int k = 0; k < L; k++) {
-          colin = colin + y[k * kTS] * (S.pk1col[k] - S.pk1col[k + 1]);
-          colscl = colscl + cabs(y[k * kTS] * (S.pk1col[k] - S.pk1col[k + 1]));
+    issue(ic, ij, qs);   // D items ahead, into the slot just read
+    if (++ij == I) { ij = 0; ++ic; }
+    if (j == 2) {
+      // new interfaces (exsmo -> exnew), pressures and p^(kappa+1) of the column
+      for (int k = lane; k <= L; k += 32) {
+        const R eo = S.exold[k];
+        R en = S.exnew[k];
+        if (its > 0) {
+          const R sl = R(kn.slak);
+          en = sl * en + (R(1) - sl) * eo;
         }
+        S.exnew[k] = en;
+        S.pk1col[k] = eo * S.prcol[k] / cp;
       }
-      bad |= pcwise_lane<R, ML>(L, y, theta ? S.gk : S.gp);
-      if (f >= 2 && !theta && kn.thktop == 0.) {
-        for (int k = 3; k <= L; k++) {
-          const R qq = R(1) / (S.dpcol[k - 1] + small);
-          y[(k - 1) * kTS] = (y[(k - 1) * kTS] * S.dpcol[k - 1] + y[(k - 2) * kTS] * small) * qq;
-        }
+      __syncwarp();
+      // miglim = 1: exnew(2..nvl) between the neighbouring old interfaces
+      for (int k = 2 + lane; k <= L; k += 32)
+        S.exnew[k - 1] = cmax(R(.0001) * S.exold[k - 1] + R(.9999) * S.exold[k],
+                              cmin(R(.0001) * S.exold[k - 1] + R(.9999) * S.exold[k - 2], S.exnew[k - 1]));
+      __syncwarp();
+      for (int k = lane; k <= L; k += 32) S.prnew[k] = p1000 * pow(S.exnew[k] / cp, cp / rd);
+      __syncwarp();
+      for (int k = lane; k <= L; k += 32) {
+        if (k < L) S.dpcol[k] = S.prnew[k] - S.prnew[k + 1];
+        S.pk1new[k] = S.exnew[k] * S.prnew[k] / cp;
       }
-      if (theta) {
-        for (int k = L; k >= 3; k--) {
-          const R dplo = cmax(S.pk1new[k - 2] - S.pk1new[k - 1], S.pk1new[0] * small);
-          const R dpup = cmax(S.pk1new[k - 1] - S.pk1new[k], S.pk1new[0] * small);
-          const R tha = y[(k - 2) * kTS], thb = y[(k - 1) * kTS];
-          const R devilo = (tha - targt[k - 2]) * dplo;
-          const R deviup = (thb - targt[k - 1]) * dpup;
-          if (deviup > R(0) && devilo < R(0)) {
-            y[(k - 2) * kTS] = tha + cmin(deviup, -devilo) / dplo;
-            y[(k - 1) * kTS] = thb - cmin(deviup, -devilo) / dpup;
-          } else if (deviup < R(0) && devilo > R(0)) {
-            y[(k - 2) * kTS] = tha - cmin(devilo, -deviup) / dplo;
-            y[(k - 1) * kTS] = thb + cmin(devilo, -deviup) / dpup;
+      __syncwarp();
+      if (lane == 0) {
+        S.prnew[L] = S.prcol[L];
+        S.pk1new[L] = S.pk1col[L];
+        S.prnew[0] = S.prcol[0];
+        S.pk1new[0] = S.pk1col[0];
+        S.flo[c] = S.pk1col[0] * small;
+      }
+      __syncwarp();
+      for (int k = lane; k < L; k += 32) S.dkb[c][k] = S.pk1new[k] - S.pk1new[k + 1];
+      lane_geo<R, VL>(L, lane, S.prcol, S.prnew, gp);
+#pragma unroll
+      for (int v = 0; v < VL; v++) {
+        dpv[v] = kb + v < L ? S.dpcol[kb + v] : R(0);
+        qqv[v] = R(1) / (dpv[v] + small);
+      }
+      __syncwarp();
+    } else if (j >= 3) {
+      const int f = j - 3;
+      if (f == T + 1) {
+        // theta in p^(kappa+1), held for the redistribution after the last column
+        LaneGeo<R, VL> gk;
+        lane_geo<R, VL>(L, lane, S.pk1col, S.pk1new, gk);
+        if (sizeof(R) == 8) {
+          R colin = R(0), colscl = R(0);
+#pragma unroll
+          for (int v = 0; v < VL; v++)
+            if (kb + v < L) {
+              const R w = y[v] * (S.pk1col[kb + v] - S.pk1col[kb + v + 1]);
+              colin += w;
+              colscl += cabs(w);
+            }
+          colin = warp_sum(colin);
+          colscl = warp_sum(colscl);
+          if (lane == 0) {
+            S.colin[c] = colin;
+            S.colscl[c] = colscl;
           }
         }
-        if (sizeof(R) == 8) {
-          R clout = R(0);
-          for (int k = 0; k < L; k++) clout = clout + y[k * kTS] * (S.pk1new[k] - S.pk1new[k + 1]);
-          if (cabs(clout - colin) > cmax(R(1.e-33), R(2.e-6) * colscl)) bad = true;
+        bad |= pcwise_v<R, VL>(L, lane, y, gk);
+#pragma unroll
+        for (int v = 0; v < VL; v++)
+          if (kb + v < L) S.thb[c][kb + v] = y[v];
+      } else {
+        bad |= pcwise_v<R, VL>(L, lane, y, gp);
+        if (f >= 2 && kn.thktop == 0.) {
+          // fill thin layers from above: y(k) = (y(k) dp(k) + y(k-1) small) / (dp(k) + small), k = 3..nvl
+          R a = R(1), b = R(0);
+#pragma unroll
+          for (int v = 0; v < VL; v++) {
+            const int k = kb + v;
+            if (k < 2) {
+              a = R(0);
+              b = y[v];
+            } else if (k < L) {
+              const R A = small * qqv[v];
+              b = A * b + y[v] * dpv[v] * qqv[v];
+              a = A * a;
+            }
+          }
+          R x = affine_entry_up(lane, a, b);
+#pragma unroll
+          for (int v = 0; v < VL; v++) {
+            const int k = kb + v;
+            if (k < 2) {
+              x = y[v];
+            } else if (k < L) {
+              x = (y[v] * dpv[v] + x * small) * qqv[v];
+              y[v] = x;
+            }
+          }
         }
+        store_levels<R, VL>(field(f, i), L, kb, vec, y);
       }
     }
-    __syncwarp();
-    for (int q = 0; q < nf; q++) {
-      const int f = base + q;
-      R* col = f == 0 ? us3d + (size_t)i * L : f == 1 ? vs3d + (size_t)i * L
-             : f <= T ? tr3d + ((size_t)(f - 1) * N + i) * L : tr3d + (size_t)i * L;
-      for (int k = lane; k < L; k += 32) col[k] = S.tile[k * kTS + q];
-    }
-    __syncwarp();
-  }
-  // exnew made non-increasing downward: prefix minimum over the interfaces
-  R carry = S.exnew[0];
-  for (int kb = 0; kb <= L; kb += 32) {
-    const int k = kb + lane;
-    R v = k <= L ? S.exnew[k] : carry;
+    if (j == I - 1) {
+      // exnew made non-increasing downward: prefix minimum over the interfaces
+      const size_t ci = (size_t)i * L1;
+      R carry = S.exnew[0];
+      for (int k0 = 0; k0 <= L; k0 += 32) {
+        const int k = k0 + lane;
+        R v = k <= L ? S.exnew[k] : carry;
 #pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      const R o = __shfl_up_sync(0xffffffffu, v, off);
-      if (lane >= off) v = cmin(v, o);
+        for (int off = 1; off < 32; off <<= 1) {
+          const R o = __shfl_up_sync(0xffffffffu, v, off);
+          if (lane >= off) v = cmin(v, o);
+        }
+        v = cmin(v, carry);
+        if (k <= L) {
+          sdot[ci + k] = v - S.exold[k];
+          ex3d[ci + k] = v;
+          pr3d[ci + k] = S.prnew[k];
+          if (k < L) dp3d[(size_t)i * L + k] = S.dpcol[k];
+        }
+        carry = __shfl_sync(0xffffffffu, v, 31);
+      }
+      __syncwarp();
     }
-    v = cmin(v, carry);
-    if (k <= L) {
-      sdot[ci + k] = v - S.exold[k];
-      ex3d[ci + k] = v;
-      pr3d[ci + k] = S.prnew[k];
-      if (k < L) dp3d[(size_t)i * L + k] = S.dpcol[k];
+    if (++j == I) { j = 0; ++c; }
+    if (++qs == D) qs = 0;
+  }
+  cp_async_wait<0>();
+  __syncwarp();
+  // theta redistribution among neighbouring layers (hybgen.F90:648-667),
+  // lane = column: pairs (k-1, k) from the bottom up, each pair seeing the
+  // upper layer of the pair below as already adjusted
+  if (lane < ncol && L >= 3) {
+    R* th = S.thb[lane];
+    const R* dk = S.dkb[lane];
+    const R fl = S.flo[lane];
+    R thb = th[L - 1];
+    for (int k = L; k >= 3; k--) {
+      const R tha = th[k - 2];
+      const R dplo = cmax(dk[k - 2], fl), dpup = cmax(dk[k - 1], fl);
+      const R devilo = (tha - S.tg[k - 2]) * dplo;
+      const R deviup = (thb - S.tg[k - 1]) * dpup;
+      R na = tha, nbv = thb;
+      if (deviup > R(0) && devilo < R(0)) {
+        const R cc = cmin(deviup, -devilo);
+        na = tha + cc / dplo;
+        nbv = thb - cc / dpup;
+      } else if (deviup < R(0) && devilo > R(0)) {
+        const R cc = cmin(devilo, -deviup);
+        na = tha - cc / dplo;
+        nbv = thb + cc / dpup;
+      }
+      th[k - 1] = nbv;
+      thb = na;
     }
-    carry = __shfl_sync(0xffffffffu, v, 31);
+    th[1] = thb;
+    if (sizeof(R) == 8) {
+      R clout = R(0);
+      for (int k = 0; k < L; k++) clout = clout + th[k] * dk[k];
+      if (cabs(clout - S.colin[lane]) > cmax(R(1.e-33), R(2.e-6) * S.colscl[lane])) bad = true;
+    }
+  }
+  __syncwarp();
+  for (int cc = 0; cc < ncol; cc++) {
+    R y[VL];
+#pragma unroll
+    for (int v = 0; v < VL; v++) y[v] = kb + v < L ? S.thb[cc][kb + v] : R(0);
+    store_levels<R, VL>(tr3d + (size_t)(c0 + cc) * L, L, kb, vec, y);
   }
   if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flags + m, kFlagColumnIntegral);
 }
 
-template <typename R, int ML>
-size_t remap_w_smem() { return sizeof(RemapSm<R, ML>) * kWarpsRemap; }
+template <typename R, int VL>
+size_t remap_v_smem() { return sizeof(RemapV<R, VL>) * kWarpsRemapV; }
 template <typename R, int ML>
 size_t inflate_smem() { return sizeof(R) * (32 * (ML + 1) + 1) * kWarpsInflate; }
+
+// levels per lane of k_remap_v
+inline int remap_vl(int L) { return L <= 32 ? 1 : L <= 64 ? 2 : 4; }
 
 template <typename R>
 int prepare_hybgen(int L) {
   cudaError_t e;
-  if (L <= 64) {
-    e = cudaFuncSetAttribute(k_remap_w<R, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)remap_w_smem<R, 64>());
-    if (e == cudaSuccess)
+  const int vl = remap_vl(L);
+  if (vl == 1)
+    e = cudaFuncSetAttribute(k_remap_v<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)remap_v_smem<R, 1>());
+  else if (vl == 2)
+    e = cudaFuncSetAttribute(k_remap_v<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)remap_v_smem<R, 2>());
+  else
+    e = cudaFuncSetAttribute(k_remap_v<R, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)remap_v_smem<R, 4>());
+  if (e == cudaSuccess) {
+    if (L <= 64)
       e = cudaFuncSetAttribute(k_inflate<R, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)inflate_smem<R, 64>());
-  } else {
-    e = cudaFuncSetAttribute(k_remap_w<R, kMaxL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)remap_w_smem<R, kMaxL>());
-    if (e == cudaSuccess)
+    else
       e = cudaFuncSetAttribute(k_inflate<R, kMaxL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)inflate_smem<R, kMaxL>());
   }
@@ -1170,14 +1440,22 @@ void launch_hybgen(const Launch& l, const Grid<R>& g, const Strides& s, const Kn
                                                                                             w.exsmo2, l.boundary);
       FIM_KEND(l);
     }
-    dim3 gw(nblocks(g.N, kWarpsRemap), l.members);
+    dim3 gw(nblocks(g.N, kWarpsRemapV * kColsPerWarp), l.members);
+    const int vl = remap_vl(g.L);
+    const int cb = (int)(vl * sizeof(R) < 16 ? vl * sizeof(R) : 16);
+    int vec = g.L % vl == 0;
+    for (const void* p : {(const void*)us3d, (const void*)vs3d, (const void*)tr3d})
+      if ((uintptr_t)p % cb != 0) vec = 0;
     FIM_KBEGIN(l, "k_remap");
-    if (g.L <= 64)
-      k_remap_w<R, 64><<<gw, 32 * kWarpsRemap, remap_w_smem<R, 64>(), l.stream>>>(
-          g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags, l.boundary);
+    if (vl == 1)
+      k_remap_v<R, 1><<<gw, 32 * kWarpsRemapV, remap_v_smem<R, 1>(), l.stream>>>(
+          g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags, l.boundary, vec);
+    else if (vl == 2)
+      k_remap_v<R, 2><<<gw, 32 * kWarpsRemapV, remap_v_smem<R, 2>(), l.stream>>>(
+          g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags, l.boundary, vec);
     else
-      k_remap_w<R, kMaxL><<<gw, 32 * kWarpsRemap, remap_w_smem<R, kMaxL>(), l.stream>>>(
-          g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags, l.boundary);
+      k_remap_v<R, 4><<<gw, 32 * kWarpsRemapV, remap_v_smem<R, 4>(), l.stream>>>(
+          g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags, l.boundary, vec);
   } else if (g.L <= 64) {
     FIM_KBEGIN(l, "k_remap");
     k_remap<R, 64><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d,

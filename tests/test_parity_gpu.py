@@ -107,6 +107,43 @@ def test_routines_fp64(case4):
     assert not bad, bad
 
 
+def collapse_layers(s, N, L, every=7, k0=12, nl=3):
+    """Layers k0 .. k0+nl-1 of every `every`-th column made massless (their
+    interfaces moved onto interface k0), with pr3d, ex3d and dp3d consistent."""
+    pr = s["pr3d"].reshape(N, L + 1)
+    ex = s["ex3d"].reshape(N, L + 1)
+    cols = np.arange(0, N, every)
+    for j in range(1, nl + 1):
+        pr[cols, k0 + j] = pr[cols, k0]
+        ex[cols, k0 + j] = ex[cols, k0]
+    s["dp3d"].reshape(N, L)[:] = pr[:, :L] - pr[:, 1:]
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", TOL64), ("f32", TOL32)])
+def test_hybgen_massless_layers(precision, tol):
+    """remap_1d on columns with massless layers and thktop = 0: pcwise's
+    massless-layer fills and the tracer fill from above (hybgen.F90:672-680)
+    both act, over two successive regrid/remap passes (the second pass starts
+    from the massless layers the first one leaves)."""
+    grid, cfg, fields = make_case(glvl=4, nvl=38, ntra=5, dt=400.0, seed=1001, noise=1.0, thktop=0.0,
+                                  precision=precision)
+    o = oracle_for(grid, cfg)
+    s = o.init_state(o.new_state(fields))
+    collapse_layers(s, grid.nip, cfg.nvl)
+    dyc = F.Dycore(grid, cfg)
+    dt = torch.float64 if precision == "f64" else torch.float32
+    names = ["us3d", "vs3d", "tr3d", "sdot", "ex3d", "dp3d", "pr3d"]
+    errs = {}
+    for its in (1, 2):
+        g = {n: dev(s[n], dt) for n in names}
+        o.hybgen(its, *[s[n] for n in names])
+        dyc.hybgen(its, None, *[g[n] for n in names])
+        for n in ["us3d", "vs3d", "tr3d", "ex3d", "dp3d", "pr3d"]:
+            errs[(its, n)] = rel_l2(host(g[n]), s[n])
+    bad = {k: v for k, v in errs.items() if not v <= tol}
+    assert not bad, bad
+
+
 def _gpu_state(grid, cfg, fields, members=1, member_fields=None):
     dyc = F.Dycore(grid, cfg)
     st = dyc.state()
