@@ -569,14 +569,15 @@ __device__ __forceinline__ R affine_entry_down(int lane, R a, R b) {
   return lane == 31 ? R(0) : e;
 }
 
-// shared memory of one warp: the copy ring, the column arrays, and theta of
-// the warp's columns awaiting the redistribution (values, p^(kappa+1)
+// shared memory of one warp: the copy ring (an item is the three interface
+// arrays of a column or three of its fields), the column arrays, and theta
+// of the warp's columns awaiting the redistribution (values, p^(kappa+1)
 // thicknesses, their floor and, FP64 build, the input column integrals)
 template <typename R, int VL>
 struct RemapV {
-  static constexpr int S = 32 * VL + 4;                 // slot: nvl + 1 <= 32 VL + 1 values
-  static constexpr int D = sizeof(R) == 4 ? 8 : 6;      // items in flight
-  R ring[D][S];
+  static constexpr int S = 32 * VL + 4;                 // nvl + 1 <= 32 VL + 1 values
+  static constexpr int D = sizeof(R) == 4 ? 4 : 3;      // items in flight
+  R ring[D][3][S];
   R exold[S], prcol[S], exnew[S], prnew[S], pk1col[S], pk1new[S], dpcol[S], tg[S];
   R thb[kColsPerWarp][S], dkb[kColsPerWarp][S];
   R flo[kColsPerWarp], colin[kColsPerWarp], colscl[kColsPerWarp];
@@ -642,111 +643,164 @@ __device__ __forceinline__ void lane_geo(int L, int lane, const R* xo, const R* 
   G.thin = __any_sync(0xffffffffu, thin);
 }
 
-// pcwise (PLM, miglim = 1) of one field, lane = levels kb .. kb+VL-1 of y.
-// Returns true when the column-integral check fails (FP64 build only).
-template <typename R, int VL>
-__device__ __forceinline__ bool pcwise_v(int L, int lane, R (&y)[VL], const LaneGeo<R, VL>& G) {
+// pcwise (PLM, miglim = 1) of NF fields sharing one coordinate, lane =
+// levels kb .. kb+VL-1 of each; the fields' chains are independent and
+// interleave.  Returns true when a column-integral check fails (FP64 build).
+template <typename R, int VL, int NF>
+__device__ __forceinline__ bool pcwise_v(int L, int lane, R (&y)[NF][VL], const LaneGeo<R, VL>& G) {
   const R small = R(1.e-22);
   const int kb = lane * VL;
-  R bfore = R(0), colscl = R(0);
+  R bfore[NF], colscl[NF];
   if (sizeof(R) == 8) {
 #pragma unroll
-    for (int v = 0; v < VL; v++)
-      if (kb + v < L) {
-        bfore += y[v] * G.fo[v];
-        colscl += cabs(y[v] * G.fo[v]);
-      }
+    for (int h = 0; h < NF; h++) {
+      bfore[h] = R(0);
+      colscl[h] = R(0);
+#pragma unroll
+      for (int v = 0; v < VL; v++)
+        if (kb + v < L) {
+          bfore[h] += y[h][v] * G.fo[v];
+          colscl[h] += cabs(y[h][v] * G.fo[v]);
+        }
+    }
   }
-  R yf[VL];
+  R yf[NF][VL];
   if (G.thin) {
     // backward fill: nb(nvl) = y(nvl), nb(k) = (y(k) fco(k) + nb(k+1) small) / (fco(k) + small)
-    R a = R(1), b = R(0);
+    R nb[NF][VL];
 #pragma unroll
-    for (int v = VL - 1; v >= 0; v--) {
-      const int k = kb + v;
-      if (k == L - 1) {
-        a = R(0);
-        b = y[v];
-      } else if (k < L) {
-        const R A = small * G.rfo[v];
-        b = A * b + y[v] * G.fo[v] * G.rfo[v];
-        a = A * a;
+    for (int h = 0; h < NF; h++) {
+      R a = R(1), b = R(0);
+#pragma unroll
+      for (int v = VL - 1; v >= 0; v--) {
+        const int k = kb + v;
+        if (k == L - 1) {
+          a = R(0);
+          b = y[h][v];
+        } else if (k < L) {
+          const R A = small * G.rfo[v];
+          b = A * b + y[h][v] * G.fo[v] * G.rfo[v];
+          a = A * a;
+        }
       }
-    }
-    R x = affine_entry_down(lane, a, b);
-    R nb[VL];
+      R x = affine_entry_down(lane, a, b);
 #pragma unroll
-    for (int v = VL - 1; v >= 0; v--) {
-      const int k = kb + v;
-      if (k == L - 1) x = y[v];
-      else if (k < L) x = (y[v] * G.fo[v] + x * small) * G.rfo[v];
-      nb[v] = x;
+      for (int v = VL - 1; v >= 0; v--) {
+        const int k = kb + v;
+        if (k == L - 1) x = y[h][v];
+        else if (k < L) x = (y[h][v] * G.fo[v] + x * small) * G.rfo[v];
+        nb[h][v] = x;
+      }
     }
     // forward fill: yf(1) = nb(1), yf(k) = (nb(k) fco(k) + yf(k-1) small) / (fco(k) + small)
-    a = R(1);
-    b = R(0);
 #pragma unroll
-    for (int v = 0; v < VL; v++) {
-      const int k = kb + v;
-      if (k == 0) {
-        a = R(0);
-        b = nb[v];
-      } else if (k < L) {
-        const R A = small * G.rfo[v];
-        b = A * b + nb[v] * G.fo[v] * G.rfo[v];
-        a = A * a;
+    for (int h = 0; h < NF; h++) {
+      R a = R(1), b = R(0);
+#pragma unroll
+      for (int v = 0; v < VL; v++) {
+        const int k = kb + v;
+        if (k == 0) {
+          a = R(0);
+          b = nb[h][v];
+        } else if (k < L) {
+          const R A = small * G.rfo[v];
+          b = A * b + nb[h][v] * G.fo[v] * G.rfo[v];
+          a = A * a;
+        }
       }
-    }
-    x = affine_entry_up(lane, a, b);
+      R x = affine_entry_up(lane, a, b);
 #pragma unroll
-    for (int v = 0; v < VL; v++) {
-      const int k = kb + v;
-      if (k == 0) x = nb[v];
-      else if (k < L) x = (nb[v] * G.fo[v] + x * small) * G.rfo[v];
-      yf[v] = x;
+      for (int v = 0; v < VL; v++) {
+        const int k = kb + v;
+        if (k == 0) x = nb[h][v];
+        else if (k < L) x = (nb[h][v] * G.fo[v] + x * small) * G.rfo[v];
+        yf[h][v] = x;
+      }
     }
   } else {
 #pragma unroll
-    for (int v = 0; v < VL; v++) yf[v] = y[v];
-  }
-  // PLM slopes (zero in the end layers)
-  const R ym = __shfl_up_sync(0xffffffffu, yf[VL - 1], 1);
-  const R yp = __shfl_down_sync(0xffffffffu, yf[0], 1);
-  R bk[VL];
+    for (int h = 0; h < NF; h++)
 #pragma unroll
-  for (int v = 0; v < VL; v++) {
-    const int k = kb + v;
-    const R fm = v > 0 ? yf[v - 1] : ym;
-    const R fp = v < VL - 1 ? yf[v + 1] : yp;
-    bk[v] = (k >= 1 && k <= L - 2) ? plm_slope(fm, yf[v], fp) : R(0);
+      for (int v = 0; v < VL; v++) yf[h][v] = y[h][v];
   }
-  // interface fluxes; one donor layer: vertfx = -dz * (fcdx * slab) / slab = -dz * fcdx
-  const R bm = __shfl_up_sync(0xffffffffu, bk[VL - 1], 1);
-  R fl[VL];
+  bool bad = false;
 #pragma unroll
-  for (int v = 0; v < VL; v++) {
-    const bool up = (G.up >> v) & 1u;
-    const R a = up ? yf[v] : (v > 0 ? yf[v - 1] : ym);
-    const R b = up ? bk[v] : (v > 0 ? bk[v - 1] : bm);
-    fl[v] = G.nd[v] != R(0) ? G.nd[v] * (a + b * G.hh[v]) : R(0);
-  }
-  const R fnext = __shfl_down_sync(0xffffffffu, fl[0], 1);
-  R after = R(0);
+  for (int h = 0; h < NF; h++) {
+    // PLM slopes (zero in the end layers)
+    const R ym = __shfl_up_sync(0xffffffffu, yf[h][VL - 1], 1);
+    const R yp = __shfl_down_sync(0xffffffffu, yf[h][0], 1);
+    R bk[VL];
 #pragma unroll
-  for (int v = 0; v < VL; v++) {
-    const int k = kb + v;
-    if (k < L) {
-      const R vn = (k + 1 < L) ? (v < VL - 1 ? fl[v + 1] : fnext) : R(0);
-      const R amount = yf[v] * G.fo[v] - (vn - fl[v]);
-      after += amount;
-      y[v] = (amount + yf[v] * small) * G.rfn[v];
+    for (int v = 0; v < VL; v++) {
+      const int k = kb + v;
+      const R fm = v > 0 ? yf[h][v - 1] : ym;
+      const R fp = v < VL - 1 ? yf[h][v + 1] : yp;
+      bk[v] = (k >= 1 && k <= L - 2) ? plm_slope(fm, yf[h][v], fp) : R(0);
+    }
+    // interface fluxes; one donor layer: vertfx = -dz * (fcdx * slab) / slab = -dz * fcdx
+    const R bm = __shfl_up_sync(0xffffffffu, bk[VL - 1], 1);
+    R fl[VL];
+#pragma unroll
+    for (int v = 0; v < VL; v++) {
+      const bool up = (G.up >> v) & 1u;
+      const R a = up ? yf[h][v] : (v > 0 ? yf[h][v - 1] : ym);
+      const R b = up ? bk[v] : (v > 0 ? bk[v - 1] : bm);
+      fl[v] = G.nd[v] != R(0) ? G.nd[v] * (a + b * G.hh[v]) : R(0);
+    }
+    const R fnext = __shfl_down_sync(0xffffffffu, fl[0], 1);
+    R after = R(0);
+#pragma unroll
+    for (int v = 0; v < VL; v++) {
+      const int k = kb + v;
+      if (k < L) {
+        const R vn = (k + 1 < L) ? (v < VL - 1 ? fl[v + 1] : fnext) : R(0);
+        const R amount = yf[h][v] * G.fo[v] - (vn - fl[v]);
+        after += amount;
+        y[h][v] = (amount + yf[h][v] * small) * G.rfn[v];
+      }
+    }
+    if (sizeof(R) == 8) {
+      const R dif = warp_sum(bfore[h] - after), scl = warp_sum(colscl[h]);
+      bad |= cabs(dif) > cmax(R(1.e-33), R(1.e-11) * scl);
     }
   }
-  if (sizeof(R) == 8) {
-    const R dif = warp_sum(bfore - after), scl = warp_sum(colscl);
-    return cabs(dif) > cmax(R(1.e-33), R(1.e-11) * scl);
+  return bad;
+}
+
+// remap_1d's fill of thin layers from above for tracers 2..ntra (thktop = 0):
+// y(k) = (y(k) dp(k) + y(k-1) small) / (dp(k) + small), k = 3..nvl
+template <typename R, int VL, int NF>
+__device__ __forceinline__ void fill_from_above(int L, int lane, R (&y)[NF][VL], const R (&dpv)[VL],
+                                                const R (&qqv)[VL]) {
+  const R small = R(1.e-6);
+  const int kb = lane * VL;
+#pragma unroll
+  for (int h = 0; h < NF; h++) {
+    R a = R(1), b = R(0);
+#pragma unroll
+    for (int v = 0; v < VL; v++) {
+      const int k = kb + v;
+      if (k < 2) {
+        a = R(0);
+        b = y[h][v];
+      } else if (k < L) {
+        const R A = small * qqv[v];
+        b = A * b + y[h][v] * dpv[v] * qqv[v];
+        a = A * a;
+      }
+    }
+    R x = affine_entry_up(lane, a, b);
+#pragma unroll
+    for (int v = 0; v < VL; v++) {
+      const int k = kb + v;
+      if (k < 2) {
+        x = y[h][v];
+      } else if (k < L) {
+        x = (y[h][v] * dpv[v] + x * small) * qqv[v];
+        y[h][v] = x;
+      }
+    }
   }
-  return false;
 }
 
 // VL consecutive values at p (VL * sizeof(R) bytes, aligned to min(16, that))
@@ -810,6 +864,8 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
   constexpr int D = W::D;
   constexpr int CB = VL * (int)sizeof(R) < 16 ? VL * (int)sizeof(R) : 16;  // bytes per copy
   constexpr int CE = CB / (int)sizeof(R);                                  // values per copy
+  // fields whose pcwise runs interleaved (register budget)
+  constexpr int NT = (sizeof(R) == 4 && VL <= 2) ? 3 : 1;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
@@ -823,34 +879,43 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
   exsmo += m * s.intf; us3d += m * s.cell; vs3d += m * s.cell; tr3d += m * s.tr; sdot += m * s.intf;
   ex3d += m * s.intf; dp3d += m * s.cell; pr3d += m * s.intf;
   const int its = sp->its - bnd;
-  const R cp = R(kCp), rd = R(kRd), p1000 = R(kP1000), small = R(1.e-6);
+  const R rcp = R(1) / R(kCp), kap1 = R(kCp) / R(kRd), p1000 = R(kP1000), small = R(1.e-6);
   const int kb = lane * VL;
-  // items per column: ex3d, pr3d, exsmo, then fields 0 = u, 1 = v,
-  // 2..T = tracers 2..ntra, T+1 = theta
-  const int F = T + 2, I = F + 3;
-  auto field = [&](int f, int i) -> R* {
-    return f == 0 ? us3d + (size_t)i * L : f == 1 ? vs3d + (size_t)i * L
-         : f <= T ? tr3d + ((size_t)(f - 1) * N + i) * L : tr3d + (size_t)i * L;
+  // fields in order o: 0 = theta, 1 = u, 2 = v, 3.. = tracers 2..ntra;
+  // items per column: the interface arrays (ex3d, pr3d, exsmo), then the
+  // fields three by three
+  const int F = T + 2, I = 1 + (F + 2) / 3;
+  auto field = [&](int o, int i) -> R* {
+    return o == 1 ? us3d + (size_t)i * L : o == 2 ? vs3d + (size_t)i * L
+         : tr3d + ((size_t)(o == 0 ? 0 : o - 2) * N + i) * L;
   };
   // copy item j of column c0 + c into ring slot q (an empty group past the last column)
   auto issue = [&](int c, int j, int q) {
     if (c < ncol) {
       const int i = c0 + c;
-      R* slot = S.ring[q];
-      if (j < 3) {
-        const R* src = (j == 0 ? ex3d : j == 1 ? pr3d : exsmo) + (size_t)i * L1;
-        for (int k = lane; k <= L; k += 32) cp_async<sizeof(R)>(slot + k, src + k);
+      if (j == 0) {
+#pragma unroll
+        for (int h = 0; h < 3; h++) {
+          const R* src = (h == 0 ? ex3d : h == 1 ? pr3d : exsmo) + (size_t)i * L1;
+          for (int k = lane; k <= L; k += 32) cp_async<sizeof(R)>(&S.ring[q][h][k], src + k);
+        }
       } else {
-        const R* src = field(j - 3, i);
-        if (vec) {
-          if (kb < L) {
 #pragma unroll
-            for (int h = 0; h < VL; h += CE) cp_async<CB>(slot + kb + h, src + kb + h);
+        for (int h = 0; h < 3; h++) {
+          const int o = 3 * (j - 1) + h;
+          if (o < F) {
+            const R* src = field(o, i);
+            if (vec) {
+              if (kb < L) {
+#pragma unroll
+                for (int e = 0; e < VL; e += CE) cp_async<CB>(&S.ring[q][h][kb + e], src + kb + e);
+              }
+            } else {
+#pragma unroll
+              for (int v = 0; v < VL; v++)
+                if (kb + v < L) cp_async<sizeof(R)>(&S.ring[q][h][kb + v], src + kb + v);
+            }
           }
-        } else {
-#pragma unroll
-          for (int v = 0; v < VL; v++)
-            if (kb + v < L) cp_async<sizeof(R)>(slot + kb + v, src + kb + v);
         }
       }
     }
@@ -870,19 +935,23 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
     cp_async_wait<D - 1>();
     __syncwarp();
     const int i = c0 + c;
-    const R* slot = S.ring[qs];
-    R y[VL];
-    if (j < 3) {
-      R* dst = j == 0 ? S.exold : j == 1 ? S.prcol : S.exnew;
-      for (int k = lane; k <= L; k += 32) dst[k] = slot[k];
+    R y[3][VL];
+    if (j == 0) {
+      for (int k = lane; k <= L; k += 32) {
+        S.exold[k] = S.ring[qs][0][k];
+        S.prcol[k] = S.ring[qs][1][k];
+        S.exnew[k] = S.ring[qs][2][k];
+      }
     } else {
 #pragma unroll
-      for (int v = 0; v < VL; v++) y[v] = kb + v < L ? slot[kb + v] : R(0);
+      for (int h = 0; h < 3; h++)
+#pragma unroll
+        for (int v = 0; v < VL; v++) y[h][v] = kb + v < L ? S.ring[qs][h][kb + v] : R(0);
     }
     __syncwarp();
     issue(ic, ij, qs);   // D items ahead, into the slot just read
     if (++ij == I) { ij = 0; ++ic; }
-    if (j == 2) {
+    if (j == 0) {
       // new interfaces (exsmo -> exnew), pressures and p^(kappa+1) of the column
       for (int k = lane; k <= L; k += 32) {
         const R eo = S.exold[k];
@@ -892,7 +961,7 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
           en = sl * en + (R(1) - sl) * eo;
         }
         S.exnew[k] = en;
-        S.pk1col[k] = eo * S.prcol[k] / cp;
+        S.pk1col[k] = eo * S.prcol[k] * rcp;
       }
       __syncwarp();
       // miglim = 1: exnew(2..nvl) between the neighbouring old interfaces
@@ -900,12 +969,14 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
         S.exnew[k - 1] = cmax(R(.0001) * S.exold[k - 1] + R(.9999) * S.exold[k],
                               cmin(R(.0001) * S.exold[k - 1] + R(.9999) * S.exold[k - 2], S.exnew[k - 1]));
       __syncwarp();
-      for (int k = lane; k <= L; k += 32) S.prnew[k] = p1000 * pow(S.exnew[k] / cp, cp / rd);
-      __syncwarp();
       for (int k = lane; k <= L; k += 32) {
-        if (k < L) S.dpcol[k] = S.prnew[k] - S.prnew[k + 1];
-        S.pk1new[k] = S.exnew[k] * S.prnew[k] / cp;
+        const R en = S.exnew[k];
+        const R pn = p1000 * pow(en * rcp, kap1);
+        S.prnew[k] = pn;
+        S.pk1new[k] = en * pn * rcp;
       }
+      __syncwarp();
+      for (int k = lane; k < L; k += 32) S.dpcol[k] = S.prnew[k] - S.prnew[k + 1];
       __syncwarp();
       if (lane == 0) {
         S.prnew[L] = S.prcol[L];
@@ -923,10 +994,9 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
         qqv[v] = R(1) / (dpv[v] + small);
       }
       __syncwarp();
-    } else if (j >= 3) {
-      const int f = j - 3;
-      if (f == T + 1) {
-        // theta in p^(kappa+1), held for the redistribution after the last column
+    } else if (j == 1) {
+      // theta in p^(kappa+1), held for the redistribution after the last column
+      {
         LaneGeo<R, VL> gk;
         lane_geo<R, VL>(L, lane, S.pk1col, S.pk1new, gk);
         if (sizeof(R) == 8) {
@@ -934,7 +1004,7 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
 #pragma unroll
           for (int v = 0; v < VL; v++)
             if (kb + v < L) {
-              const R w = y[v] * (S.pk1col[kb + v] - S.pk1col[kb + v + 1]);
+              const R w = y[0][v] * (S.pk1col[kb + v] - S.pk1col[kb + v + 1]);
               colin += w;
               colscl += cabs(w);
             }
@@ -945,40 +1015,56 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
             S.colscl[c] = colscl;
           }
         }
-        bad |= pcwise_v<R, VL>(L, lane, y, gk);
+        R t[1][VL];
+#pragma unroll
+        for (int v = 0; v < VL; v++) t[0][v] = y[0][v];
+        bad |= pcwise_v<R, VL, 1>(L, lane, t, gk);
 #pragma unroll
         for (int v = 0; v < VL; v++)
-          if (kb + v < L) S.thb[c][kb + v] = y[v];
+          if (kb + v < L) S.thb[c][kb + v] = t[0][v];
+      }
+      // u, v in pressure
+      if constexpr (NT == 3) {
+        R uv[2][VL];
+#pragma unroll
+        for (int v = 0; v < VL; v++) {
+          uv[0][v] = y[1][v];
+          uv[1][v] = y[2][v];
+        }
+        bad |= pcwise_v<R, VL, 2>(L, lane, uv, gp);
+        store_levels<R, VL>(us3d + (size_t)i * L, L, kb, vec, uv[0]);
+        store_levels<R, VL>(vs3d + (size_t)i * L, L, kb, vec, uv[1]);
       } else {
-        bad |= pcwise_v<R, VL>(L, lane, y, gp);
-        if (f >= 2 && kn.thktop == 0.) {
-          // fill thin layers from above: y(k) = (y(k) dp(k) + y(k-1) small) / (dp(k) + small), k = 3..nvl
-          R a = R(1), b = R(0);
 #pragma unroll
-          for (int v = 0; v < VL; v++) {
-            const int k = kb + v;
-            if (k < 2) {
-              a = R(0);
-              b = y[v];
-            } else if (k < L) {
-              const R A = small * qqv[v];
-              b = A * b + y[v] * dpv[v] * qqv[v];
-              a = A * a;
-            }
-          }
-          R x = affine_entry_up(lane, a, b);
+        for (int h = 1; h < 3; h++) {
+          R t[1][VL];
 #pragma unroll
-          for (int v = 0; v < VL; v++) {
-            const int k = kb + v;
-            if (k < 2) {
-              x = y[v];
-            } else if (k < L) {
-              x = (y[v] * dpv[v] + x * small) * qqv[v];
-              y[v] = x;
-            }
+          for (int v = 0; v < VL; v++) t[0][v] = y[h][v];
+          bad |= pcwise_v<R, VL, 1>(L, lane, t, gp);
+          store_levels<R, VL>(field(h, i), L, kb, vec, t[0]);
+        }
+      }
+    } else {
+      // tracers 2..ntra in pressure
+      const int o0 = 3 * (j - 1);
+      if constexpr (NT == 3) {
+        bad |= pcwise_v<R, VL, 3>(L, lane, y, gp);
+        if (kn.thktop == 0.) fill_from_above<R, VL, 3>(L, lane, y, dpv, qqv);
+#pragma unroll
+        for (int h = 0; h < 3; h++)
+          if (o0 + h < F) store_levels<R, VL>(field(o0 + h, i), L, kb, vec, y[h]);
+      } else {
+#pragma unroll
+        for (int h = 0; h < 3; h++) {
+          if (o0 + h < F) {
+            R t[1][VL];
+#pragma unroll
+            for (int v = 0; v < VL; v++) t[0][v] = y[h][v];
+            bad |= pcwise_v<R, VL, 1>(L, lane, t, gp);
+            if (kn.thktop == 0.) fill_from_above<R, VL, 1>(L, lane, t, dpv, qqv);
+            store_levels<R, VL>(field(o0 + h, i), L, kb, vec, t[0]);
           }
         }
-        store_levels<R, VL>(field(f, i), L, kb, vec, y);
       }
     }
     if (j == I - 1) {
