@@ -26,8 +26,11 @@ template <typename R> __device__ __forceinline__ R tabs(R a) { return a < R(0) ?
 // warps per SM keep enough loads in flight for these gather-heavy,
 // latency-bound kernels); the block size actually launched (128 or 256, the
 // cell patch) and the levels per thread are picked by tune_tracers.
+#ifndef FIM_TRC_MINB
+#define FIM_TRC_MINB 4
+#endif
 constexpr int kTB = 256;
-constexpr int kTBMin = 4;
+constexpr int kTBMin = FIM_TRC_MINB;
 inline unsigned tblocks(long long n, int tb) { return (unsigned)((n + tb - 1) / tb); }
 
 // own-side least-squares edge values of tracers 1..T-1 (0-based), z = tracer
@@ -46,30 +49,26 @@ __global__ void __launch_bounds__(kTB, kTBMin) k_tr_own(Grid<R> g, Strides s, co
   const int* pr = g.prox + i * 6;
   R bc[VK];
   ldv<VK>(src + i * L + k, bc);
+  // every prox slot is a valid cell (a pentagon's slot 5 repeats a
+  // neighbour), so the gathers carry no branch and can all be in flight;
+  // slot 5 of a pentagon is dropped by selects
   R d[6][VK];
 #pragma unroll
   for (int e = 0; e < 6; e++) {
-    if (e < np) {
-      ldv<VK>(src + pr[e] * L + k, d[e]);
-      FOR_V d[e][j] = d[e][j] - bc[j];
-    } else {
-      FOR_V d[e][j] = R(0);
-    }
+    ldv<VK>(src + pr[e] * L + k, d[e]);
+    FOR_V d[e][j] = e < np ? d[e][j] - bc[j] : R(0);
   }
   const R* hf = g.hfcoef + (size_t)i * 36;
 #pragma unroll
   for (int ie = 0; ie < 6; ie++) {
     R val[VK];
-    FOR_V val[j] = R(0);
-    if (ie < np) {
-      FOR_V val[j] = bc[j];
+    FOR_V val[j] = bc[j];
 #pragma unroll
-      for (int e = 0; e < 6; e++)
-        if (e < np) {
-          const R h = hf[ie * 6 + e];
-          FOR_V val[j] = val[j] + d[e][j] * h;
-        }
+    for (int e = 0; e < 6; e++) {
+      const R h = hf[ie * 6 + e];
+      FOR_V val[j] = e < np ? val[j] + d[e][j] * h : val[j];
     }
+    FOR_V val[j] = ie < np ? val[j] : R(0);
     stv<VK>(dst + (i * 6 + ie) * L + k, val);
   }
 }
