@@ -39,7 +39,7 @@ WORDS = {
     # tracers' edge values come from k_tr_own and are averaged in k_tr_lo/hi
     "k_edgvar1": lambda T: 41, "k_edgvar3_own": lambda T: 7, "k_edgvar3_avg": lambda T: 12,
     "k_tr_own": lambda T: 7 * (T - 1), "k_tr_lo": lambda T: 15 * T + 7, "k_tr_lim": lambda T: 8 * T + 1,
-    "k_tr_hi": lambda T: 17 * T + 7,
+    "k_tr_hi": lambda T: 16 * T + 7,
     "k_cnuity12": lambda T: 37, "k_cnuity3": lambda T: 8, "k_cnuity4": lambda T: 26, "k_cnuity5": lambda T: 14,
     "k_trcadv1": lambda T: 27 * T, "k_trcadv2": lambda T: 16 * T, "k_trcadv3": lambda T: 18 * T,
     "k_dissip": lambda T: 5, "k_del4prep": lambda T: 4, "k_momtum1": lambda T: 44,

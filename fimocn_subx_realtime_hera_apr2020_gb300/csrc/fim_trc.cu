@@ -11,6 +11,9 @@
 //   k_tr_lim   trcadv2: bounds relaxed with the 1-ring trcr_lo, Q+/Q-, R+/R-.
 //   k_tr_hi    trcadv3: recomputes each antidiffusive flux, clips it with the
 //              own/neighbour limiters, AB3 update of tracer x thickness, new tracer.
+//              The low-order tendency of this step, which k_tr_lo stored, is
+//              recomputed from the same fluxes in the same order rather than
+//              read back.
 //
 // Every flux is formed from the same operands in the same order as the
 // per-routine kernels, so results are bit-identical to them.
@@ -21,6 +24,9 @@ namespace fim {
 template <typename R> __device__ __forceinline__ R tmax(R a, R b) { return a > b ? a : b; }
 template <typename R> __device__ __forceinline__ R tmin(R a, R b) { return a < b ? a : b; }
 template <typename R> __device__ __forceinline__ R tabs(R a) { return a < R(0) ? -a : a; }
+// product rounded on its own (never contracted into a following add)
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 
 // Blocks of up to kTB threads capped at 64 registers a thread (32 resident
 // warps per SM keep enough loads in flight for these gather-heavy,
@@ -223,7 +229,7 @@ __global__ void __launch_bounds__(kTB, kTBMin) k_tr_lim(Grid<R> g, Strides s, co
 template <typename R, int VK>
 __global__ void __launch_bounds__(kTB, kTBMin) k_tr_hi(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     int t0, int nt, const R* __restrict__ massfx, const R* __restrict__ trc_edg, R* __restrict__ tracr,
-    R* __restrict__ trcdp, R* __restrict__ trc_tdcy, const R* __restrict__ trl_tdcy, const R* __restrict__ delp,
+    R* __restrict__ trcdp, R* __restrict__ trc_tdcy, const R* __restrict__ delp,
     const R* __restrict__ trold, const R* __restrict__ trcr_lo, const R* __restrict__ r_plus,
     const R* __restrict__ r_mnus, size_t sc) {
   int i, k, tz;
@@ -248,12 +254,12 @@ __global__ void __launch_bounds__(kTB, kTBMin) k_tr_hi(Grid<R> g, Strides s, con
   const int np = g.nprox[i];
   const int* pr = g.prox + i * 6;
   const int* ps = g.proxs + i * 6;
-  R tri[VK], rpc[VK], rmc[VK], lc[VK], at[VK], mx[VK], mn[VK];
+  R tri[VK], rpc[VK], rmc[VK], lc[VK], at[VK], sumlo[VK], mx[VK], mn[VK];
   ldv<VK>(to + c, tri);
   ldv<VK>(rp + c, rpc);
   ldv<VK>(rm + c, rmc);
   ldv<VK>(lo + c, lc);
-  FOR_V { at[j] = R(0); mx[j] = tmax(tri[j], lc[j]); mn[j] = tmin(tri[j], lc[j]); }
+  FOR_V { at[j] = R(0); sumlo[j] = R(0); mx[j] = tmax(tri[j], lc[j]); mn[j] = tmin(tri[j], lc[j]); }
 #pragma unroll
   for (int e = 0; e < 6; e++) {
     const int ipx = pr[e];
@@ -278,6 +284,7 @@ __global__ void __launch_bounds__(kTB, kTBMin) k_tr_hi(Grid<R> g, Strides s, con
       FOR_V {
         const R hi = mf[j] * tev[j];
         const R lo_ = half * ((mf[j] + tabs(mf[j])) * tri[j] - (mfx[j] + tabs(mfx[j])) * trx[j]);
+        sumlo[j] = sumlo[j] + lo_;
         R a = hi - lo_;
         if (a >= R(0)) a = a * tmin(rmc[j], rpx[j]);
         else a = a * tmin(rpc[j], rmx[j]);
@@ -288,9 +295,9 @@ __global__ void __launch_bounds__(kTB, kTBMin) k_tr_hi(Grid<R> g, Strides s, con
   const R rar = g.rarea[i];
   R* tc = trc_tdcy + m * s.trab + (size_t)t * 3 * NL;
   R* td = trcdp + m * s.tr + (size_t)t * NL;
-  R tl[VK], tof[VK], tvf[VK], tdv[VK], dp[VK], tn[VK], out[VK];
-  ldv<VK>(trl_tdcy + m * s.trab + (size_t)t * 3 * NL + (size_t)nf * NL + c, tl);
-  FOR_V tn[j] = tl[j] + (-at[j] * rar);
+  R tof[VK], tvf[VK], tdv[VK], dp[VK], tn[VK], out[VK];
+  // -sumlo * rarea is the low-order tendency k_tr_lo stored, rounded alike
+  FOR_V tn[j] = mul_rn(-sumlo[j], rar) + (-at[j] * rar);
   stv<VK>(tc + (size_t)nf * NL + c, tn);
   ldv<VK>(tc + (size_t)of * NL + c, tof);
   ldv<VK>(tc + (size_t)vof * NL + c, tvf);
@@ -324,7 +331,7 @@ void tracers_fused_vk(const Launch& l, const Grid<R>& g, const Strides& s, const
     if (probe) return;  // the first chunk's k_tr_lo and k_tr_lim only
     FIM_KBEGIN(l, "k_tr_hi");
     k_tr_hi<R, VK><<<grid, tb, 0, l.stream>>>(g, s, l.sp, t0, nt, massfx, trc_edg, tracr, trcdp, trc_tdcy,
-                                               trl_tdcy, delp, w.trold, w.trcr_lo, w.r_plus, w.r_mnus, sc);
+                                               delp, w.trold, w.trcr_lo, w.r_plus, w.r_mnus, sc);
     FIM_KEND(l);
   }
 }
