@@ -1171,9 +1171,12 @@ int prepare_hybgen(int L) {
 // hystat (hystat.F90:53-109): one warp per column; surface pressure sum and
 // the bottom-up Montgomery potential / geopotential recursion are warp scans
 // in FP64 (FP64 build) or float-float (FP32-mixed build, which also keeps the
-// (hi, lo) Montgomery potential for the pressure gradient).  The humidity
-// floors and tracer x thickness are k_hystat_trdp.
-template <typename R>
+// (hi, lo) Montgomery potential for the pressure gradient).  Every load of
+// the column (NC chunks of 32 levels) is issued before the first use, so a
+// column costs one memory round trip; theta(k-1) and the Exner function at
+// k+1 come from the neighbouring lanes.  The humidity floors and tracer x
+// thickness are k_hystat_trdp.
+template <typename R, int NC>
 __global__ void __launch_bounds__(kBlock2) k_hystat(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     R* __restrict__ ph3d, const R* __restrict__ ex3d, R* __restrict__ mp3d, const R* __restrict__ dp3d,
     const R* __restrict__ tr3d, R* __restrict__ psrf, R* __restrict__ ptdcy,
@@ -1189,34 +1192,52 @@ __global__ void __launch_bounds__(kBlock2) k_hystat(Grid<R> g, Strides s, const 
   psrf += m * s.col; ptdcy += m * 2 * s.col;
   if (mpf) mpf += m * s.cell;
   const int its = sp->its - bnd;
+  R dp[NC], th[NC], ex[NC];
+#pragma unroll
+  for (int c = 0; c < NC; c++) {
+    const int k = c * 32 + lane;
+    dp[c] = k < L ? dp3d[(size_t)i * L + k] : R(0);
+    th[c] = k < L ? tr3d[(size_t)i * L + k] : R(0);
+    ex[c] = k <= L ? ex3d[(size_t)i * L1 + k] : R(0);
+  }
+  const R exL = ex3d[(size_t)i * L1 + L];
+  const R ph0 = ph3d[(size_t)i * L1];
+  const R work = psrf[i];
+  // theta at k-1 and the Exner function at k+1 of each lane's level
+  R thm[NC], exn[NC];
+#pragma unroll
+  for (int c = 0; c < NC; c++) {
+    const R up = __shfl_up_sync(0xffffffffu, th[c], 1);
+    const R prev = c > 0 ? __shfl_sync(0xffffffffu, th[c > 0 ? c - 1 : 0], 31) : R(0);
+    thm[c] = lane > 0 ? up : prev;
+    const R dn = __shfl_down_sync(0xffffffffu, ex[c], 1);
+    const R next = c + 1 < NC ? __shfl_sync(0xffffffffu, ex[c + 1 < NC ? c + 1 : c], 0) : exL;
+    exn[c] = lane < 31 ? dn : next;
+  }
   if constexpr (sizeof(R) == 4) {
     // float-float sums and scan (FP64-accurate on the FP32 pipes)
     FF2 ps{0.f, 0.f};
-    for (int k = lane; k < L; k += 32) ps = ff_add(ps, FF2{dp3d[(size_t)i * L + k], 0.f});
+#pragma unroll
+    for (int c = 0; c < NC; c++) ps = ff_add(ps, FF2{dp[c], 0.f});
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) ps = ff_add(ps, ff_shfl_xor(ps, off));
     if (lane == 0) {
-      const R work = psrf[i];
       const R pn = ps.hi;
       psrf[i] = pn;
       if (its > 0) ptdcy[(size_t)(its % 2) * N + i] = pn - work;
     }
     FF2 carry{0.f, 0.f};
-    const float ph0 = ph3d[(size_t)i * L1];
-    for (int base = 0; base < L; base += 32) {
-      const int k = base + lane;
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+      const int k = c * 32 + lane;
       const bool act = k < L;
       FF2 term{0.f, 0.f};
-      float th = 0.f, exk1 = 0.f;
       if (act) {
-        th = tr3d[(size_t)i * L + k];
-        const float ex = ex3d[(size_t)i * L1 + k];
-        exk1 = ex3d[(size_t)i * L1 + k + 1];
         if (k == 0) {
-          term = ff_add(two_prod(ex, th), FF2{ph0, 0.f});
+          term = ff_add(two_prod(ex[c], th[c]), FF2{ph0, 0.f});
         } else {
-          const FF2 d = two_sum(th, -tr3d[(size_t)i * L + k - 1]);
-          term = ff_add(two_prod(ex, d.hi), FF2{ex * d.lo, 0.f});
+          const FF2 d = two_sum(th[c], -thm[c]);
+          term = ff_add(two_prod(ex[c], d.hi), FF2{ex[c] * d.lo, 0.f});
         }
       }
       FF2 sc = term;
@@ -1229,7 +1250,7 @@ __global__ void __launch_bounds__(kBlock2) k_hystat(Grid<R> g, Strides s, const 
       if (act) {
         mp3d[(size_t)i * L + k] = mp.hi;
         if (mpf) mpf[(size_t)i * L + k] = make_float2(mp.hi, mp.lo);
-        const FF2 ph = ff_add(mp, ff_neg(two_prod(th, exk1)));
+        const FF2 ph = ff_add(mp, ff_neg(two_prod(th[c], exn[c])));
         ph3d[(size_t)i * L1 + k + 1] = ph.hi;
       }
       carry = ff_add(carry, ff_shfl(sc, 31));
@@ -1237,30 +1258,27 @@ __global__ void __launch_bounds__(kBlock2) k_hystat(Grid<R> g, Strides s, const 
   } else {
     // surface pressure: sum of all layer thicknesses
     double ps = 0.0;
-    for (int k = lane; k < L; k += 32) ps += (double)dp3d[(size_t)i * L + k];
-  #pragma unroll
+#pragma unroll
+    for (int c = 0; c < NC; c++) ps += (double)dp[c];
+#pragma unroll
     for (int off = 16; off > 0; off >>= 1) ps += __shfl_xor_sync(0xffffffffu, ps, off);
     if (lane == 0) {
-      const R work = psrf[i];
       const R pn = R(ps);
       psrf[i] = pn;
       if (its > 0) ptdcy[(size_t)(its % 2) * N + i] = pn - work;
     }
     double carry = 0.0;
-    const double ph0 = (double)ph3d[(size_t)i * L1];
-    for (int base = 0; base < L; base += 32) {
-      const int k = base + lane;
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+      const int k = c * 32 + lane;
       const bool act = k < L;
-      double term = 0.0, th = 0.0, exk1 = 0.0;
+      double term = 0.0;
       if (act) {
-        th = (double)tr3d[(size_t)i * L + k];
-        const double ex = (double)ex3d[(size_t)i * L1 + k];
-        exk1 = (double)ex3d[(size_t)i * L1 + k + 1];
-        if (k == 0) term = ex * th + ph0;
-        else term = ex * (th - (double)tr3d[(size_t)i * L + k - 1]);
+        if (k == 0) term = (double)ex[c] * (double)th[c] + (double)ph0;
+        else term = (double)ex[c] * ((double)th[c] - (double)thm[c]);
       }
       double sc = term;
-  #pragma unroll
+#pragma unroll
       for (int off = 1; off < 32; off <<= 1) {
         const double a = __shfl_up_sync(0xffffffffu, sc, off);
         if (lane >= off) sc += a;
@@ -1268,7 +1286,7 @@ __global__ void __launch_bounds__(kBlock2) k_hystat(Grid<R> g, Strides s, const 
       const double mp = carry + sc;
       if (act) {
         mp3d[(size_t)i * L + k] = R(mp);
-          ph3d[(size_t)i * L1 + k + 1] = R(mp - th * exk1);
+        ph3d[(size_t)i * L1 + k + 1] = R(mp - (double)th[c] * (double)exn[c]);
       }
       carry += __shfl_sync(0xffffffffu, sc, 31);
     }
@@ -1559,8 +1577,14 @@ void launch_hystat(const Launch& l, const Grid<R>& g, const Strides& s, R* ph3d,
                    const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy, float2* mpf) {
   dim3 gw(nblocks((long long)g.N * 32, kBlock2), l.members);
   FIM_KBEGIN(l, "k_hystat");
-  k_hystat<R><<<gw, kBlock2, 0, l.stream>>>(g, s, l.sp, ph3d, ex3d, mp3d, dp3d, tr3d, psrf, ptdcy, mpf,
-                                             l.boundary);
+  const int nc = (g.L + 31) / 32;
+#define FIM_HYSTAT(NC) \
+  k_hystat<R, NC><<<gw, kBlock2, 0, l.stream>>>(g, s, l.sp, ph3d, ex3d, mp3d, dp3d, tr3d, psrf, ptdcy, mpf, l.boundary)
+  if (nc == 1) FIM_HYSTAT(1);
+  else if (nc == 2) FIM_HYSTAT(2);
+  else if (nc == 3) FIM_HYSTAT(3);
+  else FIM_HYSTAT(4);
+#undef FIM_HYSTAT
   FIM_KEND(l);
   const int vk = pick_vk<R>(g.L, {dp3d, tr3d, trdp});
   FIM_KBEGIN(l, "k_hystat_trdp");

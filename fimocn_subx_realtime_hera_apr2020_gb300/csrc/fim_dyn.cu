@@ -1063,8 +1063,10 @@ void launch_edgvar1(const Launch& l, const Grid<R>& g, const Strides& s, int hi_
                     const R* v, const R* delp, const R* pres, const R* montg, const R* tracr,
                     R* u_edg, R* v_edg, R* dp_edg, R* lp_edg, R* mont_edg, R* uvsq_edg, R* trc_edg,
                     const float2* mpf, R* thold) {
+  // 8-byte accesses: at 4 levels a thread the kernel holds ~100 registers and
+  // runs at half the occupancy, which costs more than the wider accesses gain
   const int vk = pick_vk<R>(g.L, {u, v, delp, montg, tracr, u_edg, v_edg, dp_edg, lp_edg, mont_edg, uvsq_edg,
-                                  trc_edg, thold});
+                                  trc_edg, thold}, 2);
   FIM_KBEGIN(l, "k_edgvar1");
   FIM_VK_DISPATCH(R, vk, (k_edgvar1<R, VK><<<dim3(blocks_for((long long)g.N * (g.L / VK)), l.members), kBlock, 0,
                                              l.stream>>>(g, s, hi_order, u, v, delp, pres, montg, tracr, u_edg,
