@@ -912,8 +912,8 @@ __global__ void __launch_bounds__(kBlock) k_dissip(Grid<R> g, Strides s, const R
 // momtum1 (momtum_compute.F90:278-423, janjic=0) after adding the dissipation
 // increments (momtum.F90:130-139); one warp per column so the Rayleigh damping
 // of the top layers can read the updated top three levels.
-template <typename R>
-__global__ void __launch_bounds__(kBlock) k_momtum1(Grid<R> g, Strides s, Knobs kn, const StepParams* __restrict__ sp,
+template <typename R, int NC>
+__global__ void __launch_bounds__(kBlock, 3) k_momtum1(Grid<R> g, Strides s, Knobs kn, const StepParams* __restrict__ sp,
     R* __restrict__ u, R* __restrict__ v, const R* __restrict__ du, const R* __restrict__ dv,
     const R* __restrict__ exner, R* __restrict__ relvor, const R* __restrict__ u_edg, const R* __restrict__ v_edg,
     const R* __restrict__ trc_edg, const R* __restrict__ mont_edg, const R* __restrict__ uvsq_edg,
@@ -938,78 +938,93 @@ __global__ void __launch_bounds__(kBlock) k_momtum1(Grid<R> g, Strides s, Knobs 
   const R ab1 = R(sp->ab1), ab2 = R(sp->ab2), ab3 = R(sp->ab3);
   const size_t NL = (size_t)N * L;
   const int np = g.nprox[i];
+  const int* pr = g.prox + i * 6;
   const R rar = g.rarea[i], cor = g.corio[i];
-  constexpr int kCh = kMaxL / 32;
-  R un[kCh], vn[kCh];
+  // Loads use a clamped level and the six edge slots of every cell (a
+  // pentagon's slot 5 and its prox entry are valid memory), so they carry no
+  // branch and can be issued together; results and stores are masked.
+  R un[NC], vn[NC];
 #pragma unroll
-  for (int ch = 0; ch < kCh; ch++) {
+  for (int ch = 0; ch < NC; ch++) {
     const int k = ch * 32 + lane;
-    un[ch] = R(0); vn[ch] = R(0);
-    if (k < L) {
-      const size_t c = (size_t)i * L + k;
-      R uu = u[c], vv = v[c];
-      if (have_d) { uu = uu + du[c]; vv = vv + dv[c]; }
-      const R exm = R(0.5) * (exner[(size_t)i * L1 + k] + exner[(size_t)i * L1 + k + 1]);
-      R pgfx = R(0), pgfy = R(0), rv = R(0);
-      if (!split) {
-        for (int e = 0; e < np; e++) {
-          const R* svc = g.svc + (i * 6 + e) * 2;
-          const R* sve = g.sve + (i * 6 + e) * 2;
-          const size_t o = ((size_t)i * 6 + e) * L + k;
-          const R mu = mont_edg[o] + uvsq_edg[o];
-          const R th = trc_edg[o];
+    const int kk = k < L ? k : L - 1;
+    const size_t c = (size_t)i * L + kk;
+    R uu = u[c], vv = v[c];
+    if (have_d) { uu = uu + du[c]; vv = vv + dv[c]; }
+    const R exm = R(0.5) * (exner[(size_t)i * L1 + kk] + exner[(size_t)i * L1 + kk + 1]);
+    R pgfx = R(0), pgfy = R(0), rv = R(0);
+    if (!split) {
+#pragma unroll
+      for (int e = 0; e < 6; e++) {
+        const bool live = e < np;
+        const R* svc = g.svc + (i * 6 + e) * 2;
+        const R* sve = g.sve + (i * 6 + e) * 2;
+        const size_t o = ((size_t)i * 6 + e) * L + kk;
+        const R mu = mont_edg[o] + uvsq_edg[o];
+        const R th = trc_edg[o];
+        const R ue = u_edg[o], ve = v_edg[o];
+        if (live) {
           pgfx = pgfx - mu * svc[1] + exm * th * svc[1];
           pgfy = pgfy + mu * svc[0] - exm * th * svc[0];
-          rv = rv + (sve[0] * u_edg[o] + sve[1] * v_edg[o]);
+          rv = rv + (sve[0] * ue + sve[1] * ve);
         }
-      } else {
-        // FP32-mixed: the same line integrals with the cell values split off,
-        // sum_e (M_e + K_e - exm th_e) s_e
-        //   = sum_e (dM_e + K_e - exm dth_e) s_e + (M_c - exm th_c) sum_e s_e,
-        // dM_e, dth_e the edge-minus-cell values (edgvar1's weights applied to
-        // neighbour differences); the large cell term is formed in FP64.
-        const int* pr = g.prox + i * 6;
-        const R thc = tr0[(size_t)i * L + k];
-        R dth[6];
+      }
+    } else {
+      // FP32-mixed: the same line integrals with the cell values split off,
+      // sum_e (M_e + K_e - exm th_e) s_e
+      //   = sum_e (dM_e + K_e - exm dth_e) s_e + (M_c - exm th_c) sum_e s_e,
+      // dM_e, dth_e the edge-minus-cell values (edgvar1's weights applied to
+      // neighbour differences); the large cell term is formed in FP64.
+      const R thc = tr0[(size_t)i * L + kk];
+      R dth[6];
 #pragma unroll
-        for (int j = 0; j < 6; j++) dth[j] = (j < np) ? tr0[(size_t)pr[j] * L + k] - thc : R(0);
-        const R divby6 = R(1) / R(6);
-        for (int e = 0; e < np; e++) {
-          const R* svc = g.svc + (i * 6 + e) * 2;
-          const R* sve = g.sve + (i * 6 + e) * 2;
-          const size_t o = ((size_t)i * 6 + e) * L + k;
-          const int et = e == 0 ? np - 1 : e - 1, el = e == np - 1 ? 0 : e + 1;
-          R dte = R(0);
+      for (int j = 0; j < 6; j++) {
+        const R tn = tr0[(size_t)pr[j] * L + kk];
+        dth[j] = (j < np) ? tn - thc : R(0);
+      }
+      const R divby6 = R(1) / R(6);
 #pragma unroll
-          for (int j = 0; j < 6; j++) {
-            if (j == e) dte = dte + R(2) * dth[j];
-            if (j == et || j == el) dte = dte + dth[j];
-          }
-          dte = dte * divby6;
-          const R w = mont_edg[o] + uvsq_edg[o] - exm * dte;
+      for (int e = 0; e < 6; e++) {
+        const bool live = e < np;
+        const R* svc = g.svc + (i * 6 + e) * 2;
+        const R* sve = g.sve + (i * 6 + e) * 2;
+        const size_t o = ((size_t)i * 6 + e) * L + kk;
+        const int et = e == 0 ? np - 1 : e - 1, el = e == np - 1 ? 0 : e + 1;
+        R dte = R(0);
+#pragma unroll
+        for (int j = 0; j < 6; j++) {
+          if (j == e) dte = dte + R(2) * dth[j];
+          if (j == et || j == el) dte = dte + dth[j];
+        }
+        dte = dte * divby6;
+        const R mo = mont_edg[o], kv = uvsq_edg[o], ue = u_edg[o], ve = v_edg[o];
+        if (live) {
+          const R w = mo + kv - exm * dte;
           pgfx = pgfx - w * svc[1];
           pgfy = pgfy + w * svc[0];
-          rv = rv + (sve[0] * u_edg[o] + sve[1] * v_edg[o]);
+          rv = rv + (sve[0] * ue + sve[1] * ve);
         }
-        // Montgomery potential minus exner x theta, cancellation-free
-        const float2 mp = mpf[(size_t)i * L + k];
-        const FF2 cf = ff_add(FF2{mp.x, mp.y}, ff_neg(two_prod(float(exm), float(thc))));
-        const R cell = R(cf.hi + cf.lo);
-        pgfx = pgfx - cell * g.svsum[i * 2 + 1];
-        pgfy = pgfy + cell * g.svsum[i * 2 + 0];
       }
-      pgfx = pgfx * rar;
-      pgfy = pgfy * rar;
-      rv = rv * rar;
+      // Montgomery potential minus exner x theta, cancellation-free
+      const float2 mp = mpf[(size_t)i * L + kk];
+      const FF2 cf = ff_add(FF2{mp.x, mp.y}, ff_neg(two_prod(float(exm), float(thc))));
+      const R cell = R(cf.hi + cf.lo);
+      pgfx = pgfx - cell * g.svsum[i * 2 + 1];
+      pgfy = pgfy + cell * g.svsum[i * 2 + 0];
+    }
+    pgfx = pgfx * rar;
+    pgfy = pgfy * rar;
+    rv = rv * rar;
+    const R uzeta = (cor + rv) * uu, vzeta = (cor + rv) * vv;
+    const R ut = pgfx + vzeta, vt = pgfy - uzeta;
+    uu = uu + ab1 * ut + ab2 * u_tndcy[(size_t)of * NL + c] + ab3 * u_tndcy[(size_t)vof * NL + c];
+    vv = vv + ab1 * vt + ab2 * v_tndcy[(size_t)of * NL + c] + ab3 * v_tndcy[(size_t)vof * NL + c];
+    un[ch] = uu;
+    vn[ch] = vv;
+    if (k < L) {
       relvor[c] = rv;
-      const R uzeta = (cor + rv) * uu, vzeta = (cor + rv) * vv;
-      const R ut = pgfx + vzeta, vt = pgfy - uzeta;
       u_tndcy[(size_t)nf * NL + c] = ut;
       v_tndcy[(size_t)nf * NL + c] = vt;
-      uu = uu + ab1 * ut + ab2 * u_tndcy[(size_t)of * NL + c] + ab3 * u_tndcy[(size_t)vof * NL + c];
-      vv = vv + ab1 * vt + ab2 * v_tndcy[(size_t)of * NL + c] + ab3 * v_tndcy[(size_t)vof * NL + c];
-      un[ch] = uu;
-      vn[ch] = vv;
       if (k >= L - 3) { top[wib][L - 1 - k][0] = uu; top[wib][L - 1 - k][1] = vv; }
     }
   }
@@ -1024,7 +1039,7 @@ __global__ void __launch_bounds__(kBlock) k_momtum1(Grid<R> g, Strides s, Knobs 
   if (damp) qq = sqrt((qq - R(1)) * qq);
   const R dtf = R(sp->dt) / R(86400.), rl = R(kn.rleigh), rt = R(kn.rltaper);
 #pragma unroll
-  for (int ch = 0; ch < kCh; ch++) {
+  for (int ch = 0; ch < NC; ch++) {
     const int k = ch * 32 + lane;
     if (k < L) {
       R uu = un[ch], vv = vn[ch];
@@ -1167,8 +1182,15 @@ void launch_momtum(const Launch& l, const Grid<R>& g, const Strides& s, const Kn
   }
   dim3 gw(blocks_for((long long)g.N * 32), l.members);
   FIM_KBEGIN(l, "k_momtum1");
-  k_momtum1<R><<<gw, kBlock, 0, l.stream>>>(g, s, kn, l.sp, u, v, du, dv, exner, relvor, u_edg, v_edg, trc_edg,
-                                             mont_edg, uvsq_edg, u_tndcy, v_tndcy, mpf, tr0);
+  const int nc = (g.L + 31) / 32;
+#define FIM_MOMTUM1(NC)                                                                                        \
+  k_momtum1<R, NC><<<gw, kBlock, 0, l.stream>>>(g, s, kn, l.sp, u, v, du, dv, exner, relvor, u_edg, v_edg, trc_edg, \
+                                                 mont_edg, uvsq_edg, u_tndcy, v_tndcy, mpf, tr0)
+  if (nc == 1) FIM_MOMTUM1(1);
+  else if (nc == 2) FIM_MOMTUM1(2);
+  else if (nc == 3) FIM_MOMTUM1(3);
+  else FIM_MOMTUM1(4);
+#undef FIM_MOMTUM1
   FIM_KEND(l);
 }
 
