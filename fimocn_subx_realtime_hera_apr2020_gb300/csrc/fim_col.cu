@@ -328,24 +328,64 @@ __device__ bool pcwise(int kk, const R* xold, const R* yold, const R* xnew, R* y
   return sizeof(R) == 8 && cabs(bfore - after) > cmax(R(1.e-33), R(1.e-11) * colscl);
 }
 
+// A warp's 32 columns (lane = column) move between global memory and the
+// lanes' column arrays through a 32 x 33 shared tile, 32 levels at a time, so
+// the global accesses run along k (128-byte rows) rather than one column per
+// lane.  n values of column i0 + lane start at src + (i0 + lane) * stride.
+template <typename R>
+__device__ __forceinline__ void columns_in(const R* __restrict__ src, size_t stride, int n, int ncol, int i0,
+                                           int lane, R (*tile)[33], R* col) {
+  for (int c0 = 0; c0 < n; c0 += 32) {
+    const int kk = c0 + lane;
+#pragma unroll 8
+    for (int r = 0; r < 32; r++)
+      if (r < ncol && kk < n) tile[r][lane] = src[(size_t)(i0 + r) * stride + kk];
+    __syncwarp();
+    const int m = n - c0 < 32 ? n - c0 : 32;
+    if (lane < ncol)
+      for (int q = 0; q < m; q++) col[c0 + q] = tile[lane][q];
+    __syncwarp();
+  }
+}
+template <typename R>
+__device__ __forceinline__ void columns_out(R* __restrict__ dst, size_t stride, int n, int ncol, int i0, int lane,
+                                            R (*tile)[33], const R* col) {
+  for (int c0 = 0; c0 < n; c0 += 32) {
+    const int m = n - c0 < 32 ? n - c0 : 32;
+    if (lane < ncol)
+      for (int q = 0; q < m; q++) tile[lane][q] = col[c0 + q];
+    __syncwarp();
+    const int kk = c0 + lane;
+#pragma unroll 8
+    for (int r = 0; r < 32; r++)
+      if (r < ncol && kk < n) dst[(size_t)(i0 + r) * stride + kk] = tile[r][lane];
+    __syncwarp();
+  }
+}
+
 template <typename R, int ML>
 __global__ void __launch_bounds__(kColBlock) k_regrid(Grid<R> g, Strides s, Knobs kn,
     const StepParams* __restrict__ sp, const R* __restrict__ targt, const R* __restrict__ tr3d,
     const R* __restrict__ ex3d, const R* __restrict__ pr3d, R* __restrict__ exsmo, int* __restrict__ flags,
     int bnd) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ R tiles[kColBlock / 32][32][33];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int i0 = blockIdx.x * blockDim.x + wib * 32;
   const int N = g.N, L = g.L, L1 = L + 1;
-  if (i >= N) return;
+  if (i0 >= N) return;
+  const int ncol = N - i0 < 32 ? N - i0 : 32;
+  const int i = i0 + lane;
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active || (bnd && sp->its <= 1)) return;
   tr3d += m * s.tr; ex3d += m * s.intf; pr3d += m * s.intf; exsmo += m * s.intf;
   R thcol[ML], excol[ML + 1];
-  for (int k = 0; k < L; k++) thcol[k] = tr3d[(size_t)i * L + k];
-  for (int k = 0; k <= L; k++) excol[k] = ex3d[(size_t)i * L1 + k];
+  columns_in(tr3d, (size_t)L, L, ncol, i0, lane, tiles[wib], thcol);
+  columns_in(ex3d, (size_t)L1, L1, ncol, i0, lane, tiles[wib], excol);
   int bad = 0;
-  regrid_1d<R, ML>(kn, targt, g.dpsig, L, sp->its - bnd, thcol, excol, pr3d[(size_t)i * L1], &bad);
-  for (int k = 0; k <= L; k++) exsmo[(size_t)i * L1 + k] = excol[k];
+  if (lane < ncol)
+    regrid_1d<R, ML>(kn, targt, g.dpsig, L, sp->its - bnd, thcol, excol, pr3d[(size_t)i * L1], &bad);
+  columns_out(exsmo, (size_t)L1, L1, ncol, i0, lane, tiles[wib], excol);
   if (bad) atomicOr(flags + m, kFlagColumnIntegral);
 }
 
