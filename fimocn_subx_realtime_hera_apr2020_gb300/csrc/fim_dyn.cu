@@ -172,30 +172,25 @@ __global__ void __launch_bounds__(kBlock) k_edgvar3_own(Grid<R> g, Strides s,
   const int* pr = g.prox + i * 6;
   R bc[VK];
   ldv<VK>(src + (size_t)i * L + k, bc);
+  // branch-free gathers over the six prox slots (all valid cells); a
+  // pentagon's slot 5 is dropped by selects
   R d[6][VK];
 #pragma unroll
   for (int e = 0; e < 6; e++) {
-    if (e < np) {
-      ldv<VK>(src + (size_t)pr[e] * L + k, d[e]);
-      FOR_V d[e][j] = d[e][j] - bc[j];
-    } else {
-      FOR_V d[e][j] = R(0);
-    }
+    ldv<VK>(src + (size_t)pr[e] * L + k, d[e]);
+    FOR_V d[e][j] = e < np ? d[e][j] - bc[j] : R(0);
   }
   const R* hf = g.hfcoef + (size_t)i * 36;
 #pragma unroll
   for (int ie = 0; ie < 6; ie++) {
     R val[VK];
-    FOR_V val[j] = R(0);
-    if (ie < np) {
-      FOR_V val[j] = bc[j];
+    FOR_V val[j] = bc[j];
 #pragma unroll
-      for (int e = 0; e < 6; e++)
-        if (e < np) {
-          const R h = hf[ie * 6 + e];
-          FOR_V val[j] = val[j] + d[e][j] * h;
-        }
+    for (int e = 0; e < 6; e++) {
+      const R h = hf[ie * 6 + e];
+      FOR_V val[j] = e < np ? val[j] + d[e][j] * h : val[j];
     }
+    FOR_V val[j] = ie < np ? val[j] : R(0);
     stv<VK>(dst + ((size_t)i * 6 + ie) * L + k, val);
   }
 }
@@ -261,8 +256,12 @@ __global__ void __launch_bounds__(kBlock) k_cnuity12(Grid<R> g, Strides s, const
     stv<VK>(mfn + ((size_t)i * 6 + 5) * L + k, z);
     stv<VK>(antifx + ((size_t)i * 6 + 5) * L + k, z);
   }
-  for (int e = 0; e < np; e++) {
-    const int ipx = g.prox[i * 6 + e], edx = g.proxs[i * 6 + e];
+  // branch-free over the six slots: a pentagon's slot 5 reads valid rows
+  // (mirror edge 0) and is neither accumulated nor stored
+#pragma unroll
+  for (int e = 0; e < 6; e++) {
+    const bool live = e < np;
+    const int ipx = g.prox[i * 6 + e], edx = live ? g.proxs[i * 6 + e] : 0;
     const R* sv = g.sve + (i * 6 + e) * 2;
     const R* sx = g.sve + (ipx * 6 + edx) * 2;
     const size_t o = ((size_t)i * 6 + e) * L + k, ox = ((size_t)ipx * 6 + edx) * L + k;
@@ -280,12 +279,14 @@ __global__ void __launch_bounds__(kBlock) k_cnuity12(Grid<R> g, Strides s, const
       mf[j] = half * ((vn + rabs(vn)) * dpi[j] - (vx + rabs(vx)) * dx[j]);
       const R a = flxhi - mf[j];
       an[j] = a;
-      sum[j] = sum[j] + mf[j];
-      if (a <= R(0)) pp[j] = pp[j] - a;
-      else pm[j] = pm[j] + a;
+      sum[j] = live ? sum[j] + mf[j] : sum[j];
+      if (live && a <= R(0)) pp[j] = pp[j] - a;
+      else if (live) pm[j] = pm[j] + a;
     }
-    stv<VK>(mfn + o, mf);
-    stv<VK>(antifx + o, an);
+    if (live) {
+      stv<VK>(mfn + o, mf);
+      stv<VK>(antifx + o, an);
+    }
   }
   const size_t c = (size_t)i * L + k;
   const R rar = g.rarea[i];
@@ -875,7 +876,12 @@ __global__ void __launch_bounds__(kBlock) k_dissip(Grid<R> g, Strides s, const R
     sv[j] = R(0);
   }
   const int np = g.nprox[i];
-  for (int e = 0; e < np; e++) {
+  // all six prox slots hold valid cells (a pentagon's slot 5 repeats a
+  // neighbour), so the gathers carry no branch; slot 5 of a pentagon is
+  // dropped by the selects
+#pragma unroll
+  for (int e = 0; e < 6; e++) {
+    const bool live = e < np;
     const int ipx = g.prox[i * 6 + e];
     const R* cs = g.cs + (i * 6 + e) * 4;
     const R* sn = g.sn + (i * 6 + e) * 4;
@@ -901,8 +907,8 @@ __global__ void __launch_bounds__(kBlock) k_dissip(Grid<R> g, Strides s, const R
       const R vfx = (vxy2 - vxy1) * dfl[j] * sl * two * hf;
       const R uflux = cs[0] * ufx - sn[0] * vfx;
       const R vflux = sn[0] * ufx + cs[0] * vfx;
-      su[j] = su[j] + uflux * factor[j];
-      sv[j] = sv[j] + vflux * factor[j];
+      su[j] = live ? su[j] + uflux * factor[j] : su[j];
+      sv[j] = live ? sv[j] + vflux * factor[j] : sv[j];
     }
   }
   stv<VK>(du + c, su);
