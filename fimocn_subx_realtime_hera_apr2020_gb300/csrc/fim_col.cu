@@ -919,7 +919,7 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
   exsmo += m * s.intf; us3d += m * s.cell; vs3d += m * s.cell; tr3d += m * s.tr; sdot += m * s.intf;
   ex3d += m * s.intf; dp3d += m * s.cell; pr3d += m * s.intf;
   const int its = sp->its - bnd;
-  const R rcp = R(1) / R(kCp), kap1 = R(kCp) / R(kRd), p1000 = R(kP1000), small = R(1.e-6);
+  const R cp = R(kCp), rd = R(kRd), p1000 = R(kP1000), small = R(1.e-6);
   const int kb = lane * VL;
   // fields in order o: 0 = theta, 1 = u, 2 = v, 3.. = tracers 2..ntra;
   // items per column: the interface arrays (ex3d, pr3d, exsmo), then the
@@ -1001,7 +1001,7 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
           en = sl * en + (R(1) - sl) * eo;
         }
         S.exnew[k] = en;
-        S.pk1col[k] = eo * S.prcol[k] * rcp;
+        S.pk1col[k] = eo * S.prcol[k] / cp;
       }
       __syncwarp();
       // miglim = 1: exnew(2..nvl) between the neighbouring old interfaces
@@ -1010,10 +1010,13 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
                               cmin(R(.0001) * S.exold[k - 1] + R(.9999) * S.exold[k - 2], S.exnew[k - 1]));
       __syncwarp();
       for (int k = lane; k <= L; k += 32) {
+        // the reference's own operations: the pressures of unmoved
+        // interfaces then reproduce the old ones exactly, so the layer
+        // thicknesses keep summing to the unchanged column mass
         const R en = S.exnew[k];
-        const R pn = p1000 * pow(en * rcp, kap1);
+        const R pn = p1000 * pow(en / cp, cp / rd);
         S.prnew[k] = pn;
-        S.pk1new[k] = en * pn * rcp;
+        S.pk1new[k] = en * pn / cp;
       }
       __syncwarp();
       for (int k = lane; k < L; k += 32) S.dpcol[k] = S.prnew[k] - S.prnew[k + 1];
@@ -1108,25 +1111,43 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
       }
     }
     if (j == I - 1) {
-      // exnew made non-increasing downward: prefix minimum over the interfaces
+      // exnew made non-increasing downward: prefix minimum over the
+      // interfaces; lane l holds interfaces l*VL .. l*VL+VL-1 (running minimum
+      // within the lane, one warp scan of the lane minima), interface nvl
+      // (when 32*VL == nvl) takes the minimum over all lanes
       const size_t ci = (size_t)i * L1;
-      R carry = S.exnew[0];
-      for (int k0 = 0; k0 <= L; k0 += 32) {
-        const int k = k0 + lane;
-        R v = k <= L ? S.exnew[k] : carry;
+      const R top = S.exnew[0];  // fill: no interface lies above the column top
+      R pm[VL];
 #pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-          const R o = __shfl_up_sync(0xffffffffu, v, off);
-          if (lane >= off) v = cmin(v, o);
-        }
-        v = cmin(v, carry);
+      for (int v = 0; v < VL; v++) {
+        const int k = kb + v;
+        const R x = k <= L ? S.exnew[k] : top;
+        pm[v] = v == 0 ? x : cmin(pm[v - 1], x);
+      }
+      R tot = pm[VL - 1];
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const R o = __shfl_up_sync(0xffffffffu, tot, off);
+        if (lane >= off) tot = cmin(tot, o);
+      }
+      const R above = __shfl_up_sync(0xffffffffu, tot, 1);
+      const R all = __shfl_sync(0xffffffffu, tot, 31);
+#pragma unroll
+      for (int v = 0; v < VL; v++) {
+        const int k = kb + v;
         if (k <= L) {
-          sdot[ci + k] = v - S.exold[k];
-          ex3d[ci + k] = v;
+          const R x = lane > 0 ? cmin(pm[v], above) : pm[v];
+          sdot[ci + k] = x - S.exold[k];
+          ex3d[ci + k] = x;
           pr3d[ci + k] = S.prnew[k];
           if (k < L) dp3d[(size_t)i * L + k] = S.dpcol[k];
         }
-        carry = __shfl_sync(0xffffffffu, v, 31);
+      }
+      if (32 * VL == L && lane == 0) {
+        const R x = cmin(S.exnew[L], all);
+        sdot[ci + L] = x - S.exold[L];
+        ex3d[ci + L] = x;
+        pr3d[ci + L] = S.prnew[L];
       }
       __syncwarp();
     }
