@@ -1413,7 +1413,6 @@ template <> struct Acc<float> {
 };
 
 constexpr int kMaxT = 32;
-constexpr int kGsBlocks = 152 * 4;
 
 // Slots of one block's partial sums: 0 = sum(area*dp), 1+t = sum(area*dp*tr_t)
 // (level sums), kMaxT+1.. = the column sums of globsum.F90:81-85
@@ -1421,9 +1420,15 @@ constexpr int kGsBlocks = 152 * 4;
 constexpr int kGsCol = kMaxT + 1;
 constexpr int kGsSlots = kMaxT + 5;
 
-// Level sums of one group of kGsGroup slots (blockIdx.z), VK levels per
-// access; group 0 also forms the column sums.
-constexpr int kGsGroup = 8;
+// Level sums: a block takes one chunk of kGsChunkPer(VK) cell-levels and
+// one slot q (0: area x dp, 1..ntr: area x dp x tracer q-1); the slots of a
+// chunk are consecutive blocks, so the chunk's thicknesses come from DRAM
+// once and from L2 after.  The slot-0 block of a chunk also forms the column
+// sums of the cells whose first level lies in the chunk.  Partials are per
+// (chunk, slot), reduced in a fixed order: the sums are deterministic.
+constexpr int kGsIter = 16;
+template <int VK>
+__host__ __device__ constexpr int kGsChunkPer() { return kBlock2 * VK * kGsIter; }
 
 template <typename R, int VK> struct GsVec;
 template <typename R> struct GsVec<R, 1> {
@@ -1446,43 +1451,46 @@ template <typename R, int VK>
 __global__ void __launch_bounds__(kBlock2) k_globsum_levels(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     int T, const R* __restrict__ dp3d, const R* __restrict__ tr, const R* __restrict__ rn2d, const R* __restrict__ rc2d,
     const R* __restrict__ pr3d, const R* __restrict__ ex3d, const R* __restrict__ qf2d,
-    double* __restrict__ partial) {
+    double* __restrict__ partial, int nchunk) {
   const int N = g.N, L = g.L, L1 = L + 1;
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active) return;
-  const int q0 = blockIdx.z * kGsGroup;  // first level slot of this group
+  const int nslot = T + 1;
+  const int chunk = blockIdx.x / nslot, q = blockIdx.x - chunk * nslot;
   dp3d += m * s.cell; tr += m * s.tr; pr3d += m * s.intf; ex3d += m * s.intf;
-  const size_t NL = (size_t)N * L, NV = NL / VK;
-  const int LV = L / VK;
-  const size_t gid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, gstride = (size_t)gridDim.x * blockDim.x;
-  Acc<R> acc[kGsGroup];
-  for (size_t v = gid; v < NV; v += gstride) {
-    const size_t idx = v * VK;
-    const R ar = g.area[(int)v / LV];
-    R dp[VK], ad[VK];
-    GsVec<R, VK>::ld(dp3d + idx, dp);
+  const size_t NL = (size_t)N * L;
+  constexpr int CH = kGsChunkPer<VK>();
+  const size_t e0 = (size_t)chunk * CH;
+  const R* x_t = q > 0 ? tr + (size_t)(q - 1) * NL : nullptr;
+  Acc<R> acc;
+#pragma unroll 4
+  for (int it = 0; it < kGsIter; it++) {
+    const size_t idx = e0 + ((size_t)it * kBlock2 + threadIdx.x) * VK;
+    if (idx < NL) {
+      const R ar = g.area[(int)(idx / L)];
+      R dp[VK], ad[VK];
+      GsVec<R, VK>::ld(dp3d + idx, dp);
 #pragma unroll
-    for (int j = 0; j < VK; j++) ad[j] = ar * dp[j];
-#pragma unroll
-    for (int u = 0; u < kGsGroup; u++) {
-      const int q = q0 + u;
-      if (q > T) break;
+      for (int j = 0; j < VK; j++) ad[j] = ar * dp[j];
       if (q == 0) {
 #pragma unroll
-        for (int j = 0; j < VK; j++) acc[u].add(ad[j]);
+        for (int j = 0; j < VK; j++) acc.add(ad[j]);
       } else {
         R x[VK];
-        GsVec<R, VK>::ld(tr + (size_t)(q - 1) * NL + idx, x);
+        GsVec<R, VK>::ld(x_t + idx, x);
 #pragma unroll
-        for (int j = 0; j < VK; j++) acc[u].add(ad[j] * x[j]);
+        for (int j = 0; j < VK; j++) acc.add(ad[j] * x[j]);
       }
     }
   }
   double col[4] = {0., 0., 0., 0.};
-  if (blockIdx.z == 0) {
+  if (q == 0) {
     const double dt = sp->dt, rdcp = kRd / kCp;
-    for (size_t i = gid; i < (size_t)N; i += gstride) {
+    const size_t i0 = (e0 + L - 1) / L;
+    size_t i1 = (e0 + CH + L - 1) / L;
+    if (i1 > (size_t)N) i1 = N;
+    for (size_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
       const double a = g.area_d[i];
       const double rn = rn2d ? (double)rn2d[m * s.col + i] : 0.0;
       const double rc = rc2d ? (double)rc2d[m * s.col + i] : 0.0;
@@ -1496,14 +1504,11 @@ __global__ void __launch_bounds__(kBlock2) k_globsum_levels(Grid<R> g, Strides s
   }
   __shared__ double red[kBlock2 / 32];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  double* out = partial + (m * gridDim.x + blockIdx.x) * kGsSlots;
+  double* out = partial + (m * nchunk + chunk) * kGsSlots;
 #pragma unroll
-  for (int u = 0; u < kGsGroup + 4; u++) {
-    // both conditions are uniform across the block
-    if (u >= kGsGroup && blockIdx.z != 0) break;
-    if (u < kGsGroup && q0 + u > T) continue;
-    const int q = u < kGsGroup ? q0 + u : kGsCol + (u - kGsGroup);
-    double v = u < kGsGroup ? acc[u < kGsGroup ? u : 0].value() : col[u < kGsGroup ? 0 : u - kGsGroup];
+  for (int u = 0; u < 5; u++) {
+    if (u > 0 && q != 0) break;  // uniform across the block
+    double v = u == 0 ? acc.value() : col[u == 0 ? 0 : u - 1];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     if (lane == 0) red[wib] = v;
@@ -1511,7 +1516,7 @@ __global__ void __launch_bounds__(kBlock2) k_globsum_levels(Grid<R> g, Strides s
     if (threadIdx.x == 0) {
       double t = 0.0;
       for (int w = 0; w < kBlock2 / 32; w++) t += red[w];
-      out[q] = t;
+      out[u == 0 ? q : kGsCol + (u - 1)] = t;
     }
     __syncthreads();
   }
@@ -1655,28 +1660,34 @@ void launch_hystat(const Launch& l, const Grid<R>& g, const Strides& s, R* ph3d,
   FIM_KEND(l);
 }
 
+// partial buffer: the most chunks any layout uses (1 level a thread)
 size_t globsum_partials(int N, int L, int T, int members) {
-  (void)N; (void)L; (void)T;
-  return (size_t)members * kGsBlocks * kGsSlots;
+  (void)T;
+  const long long NL = (long long)N * L;
+  return (size_t)members * (size_t)((NL + kGsChunkPer<1>() - 1) / kGsChunkPer<1>()) * kGsSlots;
 }
 
 template <typename R>
 void launch_globsum(const Launch& l, const Grid<R>& g, const Strides& s, int ntr, const R* dp3d, const R* tr,
                     const R* rn2d, const R* rc2d, const R* pr3d, const R* ex3d, const R* qf2d,
                     double* partial, double* sums) {
-  dim3 gl(kGsBlocks, l.members, (ntr + 1 + kGsGroup - 1) / kGsGroup);
   FIM_KBEGIN(l, "k_globsum_levels");
   constexpr int VK = sizeof(R) == 4 ? 4 : 2;
   const bool vec = g.L % VK == 0 && (uintptr_t)dp3d % (VK * sizeof(R)) == 0 && (uintptr_t)tr % (VK * sizeof(R)) == 0;
-  if (vec)
-    k_globsum_levels<R, VK><<<gl, kBlock2, 0, l.stream>>>(g, s, l.sp, ntr, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d,
-                                                          partial);
-  else
-    k_globsum_levels<R, 1><<<gl, kBlock2, 0, l.stream>>>(g, s, l.sp, ntr, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d,
-                                                         partial);
+  const long long NL = (long long)g.N * g.L;
+  int nchunk;
+  if (vec) {
+    nchunk = (int)((NL + kGsChunkPer<VK>() - 1) / kGsChunkPer<VK>());
+    k_globsum_levels<R, VK><<<dim3((unsigned)nchunk * (ntr + 1), l.members), kBlock2, 0, l.stream>>>(
+        g, s, l.sp, ntr, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d, partial, nchunk);
+  } else {
+    nchunk = (int)((NL + kGsChunkPer<1>() - 1) / kGsChunkPer<1>());
+    k_globsum_levels<R, 1><<<dim3((unsigned)nchunk * (ntr + 1), l.members), kBlock2, 0, l.stream>>>(
+        g, s, l.sp, ntr, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d, partial, nchunk);
+  }
   FIM_KEND(l);
   FIM_KBEGIN(l, "k_globsum_final");
-  k_globsum_final<R><<<l.members, kBlock2, 0, l.stream>>>(l.sp, ntr, partial, kGsBlocks, sums);
+  k_globsum_final<R><<<l.members, kBlock2, 0, l.stream>>>(l.sp, ntr, partial, nchunk, sums);
   FIM_KEND(l);
 }
 
