@@ -93,8 +93,9 @@ __global__ void __launch_bounds__(kBlock) k_edgvar1(Grid<R> g, Strides s, int hi
       const R m_3ldg = sqrt(u3ldg * u3ldg + v3ldg * v3ldg);
       const R m_1 = sqrt(uu * uu + vv * vv);
       const R m_2 = (two * (m_1ldg + m_2ldg) + m_3trl + m_3ldg) * divby6;
-      uu = uu * m_2 / rmax(eps, m_1);
-      vv = vv * m_2 / rmax(eps, m_1);
+      const R q = m_2 / rmax(eps, m_1);  // one division for both components
+      uu = uu * q;
+      vv = vv * q;
       ue[j] = uu;
       ve[j] = vv;
       uv[j] = half * (uu * uu + vv * vv);
@@ -317,6 +318,7 @@ __global__ void __launch_bounds__(kBlock) k_cnuity3(Grid<R> g, Strides s, const 
   p_plus += m * s.cell; p_mnus += m * s.cell; r_plus += m * s.cell; r_mnus += m * s.cell;
   const int of = sp->of, vof = sp->vof;
   const R ab1 = R(sp->ab1), ab2 = R(sp->ab2), ab3 = R(sp->ab3);
+  const R rab1 = R(1) / ab1;  // Q+/Q- divide by ab1: one reciprocal
   const R thshld = R(1.e-11);
   const size_t c = (size_t)i * L + k;
   const int* pr = g.prox + i * 6;
@@ -339,8 +341,8 @@ __global__ void __launch_bounds__(kBlock) k_cnuity3(Grid<R> g, Strides s, const 
   const R ar = g.area[i];
   FOR_V {
     const R dpmax = rmax(R(0), mx[j]), dpmin = rmax(R(0), mn[j]);
-    const R q_plus = (dpmax - dlo[j] - (ab2 * rmin(R(0), to[j]) + ab3 * rmax(R(0), tv[j]))) / ab1 * ar;
-    const R q_mnus = (dlo[j] - dpmin + (ab2 * rmax(R(0), to[j]) + ab3 * rmin(R(0), tv[j]))) / ab1 * ar;
+    const R q_plus = (dpmax - dlo[j] - (ab2 * rmin(R(0), to[j]) + ab3 * rmax(R(0), tv[j]))) * rab1 * ar;
+    const R q_mnus = (dlo[j] - dpmin + (ab2 * rmax(R(0), to[j]) + ab3 * rmin(R(0), tv[j]))) * rab1 * ar;
     rp[j] = rmax(R(0), rmin(R(1), q_plus / rmax(pp[j], thshld)));
     rm[j] = rmax(R(0), rmin(R(1), q_mnus / rmax(pm[j], thshld)));
   }
@@ -763,8 +765,9 @@ __global__ void __launch_bounds__(kBlock) k_trcadv2(Grid<R> g, Strides s, const 
   trmin[c] = mn;
   const R dp = delp[c];
   const R to = trc_tdcy[(size_t)of * NL + c], tv = trc_tdcy[(size_t)vof * NL + c];
-  const R q_plus = ((mx - lo) * dp - (ab2 * rmin(R(0), to) + ab3 * rmax(R(0), tv))) / ab1 * g.area[i];
-  const R q_mnus = ((lo - mn) * dp + (ab2 * rmax(R(0), to) + ab3 * rmin(R(0), tv))) / ab1 * g.area[i];
+  const R rab1 = R(1) / ab1;  // one reciprocal, as k_tr_lim
+  const R q_plus = ((mx - lo) * dp - (ab2 * rmin(R(0), to) + ab3 * rmax(R(0), tv))) * rab1 * g.area[i];
+  const R q_mnus = ((lo - mn) * dp + (ab2 * rmax(R(0), to) + ab3 * rmin(R(0), tv))) * rab1 * g.area[i];
   r_plus[c] = rmax(R(0), rmin(R(1), q_plus / rmax(s_plus, thshld)));
   r_mnus[c] = rmax(R(0), rmin(R(1), q_mnus / rmax(s_mnus, thshld)));
 }

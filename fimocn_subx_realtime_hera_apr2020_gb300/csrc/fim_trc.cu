@@ -188,6 +188,7 @@ __global__ void __launch_bounds__(kTB, kTBMin) k_tr_lim(Grid<R> g, Strides s, co
   const size_t NL = (size_t)N * L;
   const int of = sp->of, vof = sp->vof;
   const R ab1 = R(sp->ab1), ab2 = R(sp->ab2), ab3 = R(sp->ab3);
+  const R rab1 = R(1) / ab1;  // Q+/Q- divide by ab1: one reciprocal (as k_trcadv2)
   const R thshld = R(1.e-11);
   const int c = i * L + k;
   const size_t so = (m * nt + tz) * sc;
@@ -216,8 +217,8 @@ __global__ void __launch_bounds__(kTB, kTBMin) k_tr_lim(Grid<R> g, Strides s, co
   const R ar = g.area[i];
   FOR_V {
     const R hx = tmax(R(0), mx[j]), hn = tmax(R(0), mn[j]);
-    const R q_plus = ((hx - lc[j]) * dp[j] - (ab2 * tmin(R(0), tof[j]) + ab3 * tmax(R(0), tvf[j]))) / ab1 * ar;
-    const R q_mnus = ((lc[j] - hn) * dp[j] + (ab2 * tmax(R(0), tof[j]) + ab3 * tmin(R(0), tvf[j]))) / ab1 * ar;
+    const R q_plus = ((hx - lc[j]) * dp[j] - (ab2 * tmin(R(0), tof[j]) + ab3 * tmax(R(0), tvf[j]))) * rab1 * ar;
+    const R q_mnus = ((lc[j] - hn) * dp[j] + (ab2 * tmax(R(0), tof[j]) + ab3 * tmin(R(0), tvf[j]))) * rab1 * ar;
     rp[j] = tmax(R(0), tmin(R(1), q_plus / tmax(spl[j], thshld)));
     rm[j] = tmax(R(0), tmin(R(1), q_mnus / tmax(smn[j], thshld)));
   }
