@@ -578,51 +578,57 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-template <typename R>
+// sum over a segment of W lanes (the lanes of one column)
+template <typename R, int W = 32>
 __device__ __forceinline__ R warp_sum(R v) {
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  for (int off = W / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off, W);
   return v;
 }
+
 
 // Value entering each lane of a recurrence x <- a x + b whose per-lane
 // composed map is (a, b): from the lanes below (up) or above (down); the
 // first lane of the sweep receives 0 (its own map is constant there).
-template <typename R>
+// (lane: the lane within its W-lane segment)
+template <typename R, int W = 32>
 __device__ __forceinline__ R affine_entry_up(int lane, R a, R b) {
 #pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const R ao = __shfl_up_sync(0xffffffffu, a, off), bo = __shfl_up_sync(0xffffffffu, b, off);
+  for (int off = 1; off < W; off <<= 1) {
+    const R ao = __shfl_up_sync(0xffffffffu, a, off, W), bo = __shfl_up_sync(0xffffffffu, b, off, W);
     if (lane >= off) { b = a * bo + b; a = a * ao; }
   }
-  const R e = __shfl_up_sync(0xffffffffu, b, 1);
+  const R e = __shfl_up_sync(0xffffffffu, b, 1, W);
   return lane == 0 ? R(0) : e;
 }
-template <typename R>
+template <typename R, int W = 32>
 __device__ __forceinline__ R affine_entry_down(int lane, R a, R b) {
 #pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const R ao = __shfl_down_sync(0xffffffffu, a, off), bo = __shfl_down_sync(0xffffffffu, b, off);
-    if (lane + off < 32) { b = a * bo + b; a = a * ao; }
+  for (int off = 1; off < W; off <<= 1) {
+    const R ao = __shfl_down_sync(0xffffffffu, a, off, W), bo = __shfl_down_sync(0xffffffffu, b, off, W);
+    if (lane + off < W) { b = a * bo + b; a = a * ao; }
   }
-  const R e = __shfl_down_sync(0xffffffffu, b, 1);
-  return lane == 31 ? R(0) : e;
+  const R e = __shfl_down_sync(0xffffffffu, b, 1, W);
+  return lane == W - 1 ? R(0) : e;
 }
 
-// shared memory of one warp: the copy ring (an item is the three interface
-// arrays of a column or three of its fields), the column arrays, and theta
-// of the warp's columns awaiting the redistribution (values, p^(kappa+1)
-// thicknesses, their floor and, FP64 build, the input column integrals)
-template <typename R, int VL>
+// shared memory of one warp: the copy ring (an item is, for each of the H
+// columns in hand, the three interface arrays or three fields), the column
+// arrays of those columns, and theta of the warp's columns awaiting the
+// redistribution (values, p^(kappa+1) thicknesses, their floor and, FP64
+// build, the input column integrals)
+template <typename R, int VL, int H>
 struct RemapV {
-  static constexpr int S = 32 * VL + 4;                 // nvl + 1 <= 32 VL + 1 values
-  static constexpr int D = sizeof(R) == 4 ? 4 : 3;      // items in flight
-  R ring[D][3][S];
-  R exold[S], prcol[S], exnew[S], prnew[S], pk1col[S], pk1new[S], dpcol[S], tg[S];
+  static constexpr int S = 32 / H * VL + 4;                        // nvl + 1 <= (32/H) VL + 1
+  static constexpr int D = H > 1 ? 2 : (sizeof(R) == 4 ? 4 : 3);   // items in flight
+  R ring[D][H][3][S];
+  R exold[H][S], prcol[H][S], exnew[H][S], prnew[H][S], pk1col[H][S], pk1new[H][S], dpcol[H][S];
+  R tg[S];
   R thb[kColsPerWarp][S], dkb[kColsPerWarp][S];
   R flo[kColsPerWarp], colin[kColsPerWarp], colscl[kColsPerWarp];
 };
-static_assert(sizeof(RemapV<float, 1>) % 16 == 0 && sizeof(RemapV<double, 1>) % 16 == 0,
+static_assert(sizeof(RemapV<float, 1, 1>) % 16 == 0 && sizeof(RemapV<double, 1, 1>) % 16 == 0 &&
+                  sizeof(RemapV<float, 4, 2>) % 16 == 0,
               "ring slots of consecutive warps stay 16-byte aligned");
 
 // pcwise's coordinate quantities for one lane's levels and interfaces
@@ -631,7 +637,7 @@ struct LaneGeo {
   R fo[VL], rfo[VL], rfn[VL];  // level kb+v: fco, 1/(fco+small), 1/(fcn+small)
   R nd[VL], hh[VL];            // interface kb+v: -delz (0: no flux), (dx-1 | 1-dx)/2
   unsigned up;                 // bit v: interface kb+v takes layer kb+v as donor
-  bool thin;                   // (warp) some layer is thin enough for the fill to matter
+  bool thin;                   // (whole warp) some layer is thin enough for the fill to matter
 };
 
 template <typename R>
@@ -639,7 +645,7 @@ __device__ __forceinline__ R coord_thick(bool flip, const R* x, int k) {
   return flip ? cmax(R(0), (-x[k + 1]) - (-x[k])) : cmax(R(0), x[k + 1] - x[k]);
 }
 
-template <typename R, int VL>
+template <typename R, int VL, int W = 32>
 __device__ __forceinline__ void lane_geo(int L, int lane, const R* xo, const R* xn, LaneGeo<R, VL>& G) {
   const R small = R(1.e-22);
   const bool flip = !(xo[0] < xo[L]);
@@ -680,13 +686,16 @@ __device__ __forceinline__ void lane_geo(int L, int lane, const R* xo, const R* 
     G.hh[v] = hh;
   }
   G.up = up;
+  // decided over the whole warp: pcwise's fill branch holds full-warp
+  // shuffles, so both columns of a paired warp must take it together (the
+  // fill is the reference's own step, exact for columns without thin layers)
   G.thin = __any_sync(0xffffffffu, thin);
 }
 
 // pcwise (PLM, miglim = 1) of NF fields sharing one coordinate, lane =
 // levels kb .. kb+VL-1 of each; the fields' chains are independent and
 // interleave.  Returns true when a column-integral check fails (FP64 build).
-template <typename R, int VL, int NF>
+template <typename R, int VL, int NF, int W = 32>
 __device__ __forceinline__ bool pcwise_v(int L, int lane, R (&y)[NF][VL], const LaneGeo<R, VL>& G) {
   const R small = R(1.e-22);
   const int kb = lane * VL;
@@ -723,7 +732,7 @@ __device__ __forceinline__ bool pcwise_v(int L, int lane, R (&y)[NF][VL], const 
           a = A * a;
         }
       }
-      R x = affine_entry_down(lane, a, b);
+      R x = affine_entry_down<R, W>(lane, a, b);
 #pragma unroll
       for (int v = VL - 1; v >= 0; v--) {
         const int k = kb + v;
@@ -748,7 +757,7 @@ __device__ __forceinline__ bool pcwise_v(int L, int lane, R (&y)[NF][VL], const 
           a = A * a;
         }
       }
-      R x = affine_entry_up(lane, a, b);
+      R x = affine_entry_up<R, W>(lane, a, b);
 #pragma unroll
       for (int v = 0; v < VL; v++) {
         const int k = kb + v;
@@ -767,8 +776,8 @@ __device__ __forceinline__ bool pcwise_v(int L, int lane, R (&y)[NF][VL], const 
 #pragma unroll
   for (int h = 0; h < NF; h++) {
     // PLM slopes (zero in the end layers)
-    const R ym = __shfl_up_sync(0xffffffffu, yf[h][VL - 1], 1);
-    const R yp = __shfl_down_sync(0xffffffffu, yf[h][0], 1);
+    const R ym = __shfl_up_sync(0xffffffffu, yf[h][VL - 1], 1, W);
+    const R yp = __shfl_down_sync(0xffffffffu, yf[h][0], 1, W);
     R bk[VL];
 #pragma unroll
     for (int v = 0; v < VL; v++) {
@@ -778,7 +787,7 @@ __device__ __forceinline__ bool pcwise_v(int L, int lane, R (&y)[NF][VL], const 
       bk[v] = (k >= 1 && k <= L - 2) ? plm_slope(fm, yf[h][v], fp) : R(0);
     }
     // interface fluxes; one donor layer: vertfx = -dz * (fcdx * slab) / slab = -dz * fcdx
-    const R bm = __shfl_up_sync(0xffffffffu, bk[VL - 1], 1);
+    const R bm = __shfl_up_sync(0xffffffffu, bk[VL - 1], 1, W);
     R fl[VL];
 #pragma unroll
     for (int v = 0; v < VL; v++) {
@@ -787,7 +796,7 @@ __device__ __forceinline__ bool pcwise_v(int L, int lane, R (&y)[NF][VL], const 
       const R b = up ? bk[v] : (v > 0 ? bk[v - 1] : bm);
       fl[v] = G.nd[v] != R(0) ? G.nd[v] * (a + b * G.hh[v]) : R(0);
     }
-    const R fnext = __shfl_down_sync(0xffffffffu, fl[0], 1);
+    const R fnext = __shfl_down_sync(0xffffffffu, fl[0], 1, W);
     R after = R(0);
 #pragma unroll
     for (int v = 0; v < VL; v++) {
@@ -800,7 +809,7 @@ __device__ __forceinline__ bool pcwise_v(int L, int lane, R (&y)[NF][VL], const 
       }
     }
     if (sizeof(R) == 8) {
-      const R dif = warp_sum(bfore[h] - after), scl = warp_sum(colscl[h]);
+      const R dif = warp_sum<R, W>(bfore[h] - after), scl = warp_sum<R, W>(colscl[h]);
       bad |= cabs(dif) > cmax(R(1.e-33), R(1.e-11) * scl);
     }
   }
@@ -809,7 +818,7 @@ __device__ __forceinline__ bool pcwise_v(int L, int lane, R (&y)[NF][VL], const 
 
 // remap_1d's fill of thin layers from above for tracers 2..ntra (thktop = 0):
 // y(k) = (y(k) dp(k) + y(k-1) small) / (dp(k) + small), k = 3..nvl
-template <typename R, int VL, int NF>
+template <typename R, int VL, int NF, int W = 32>
 __device__ __forceinline__ void fill_from_above(int L, int lane, R (&y)[NF][VL], const R (&dpv)[VL],
                                                 const R (&qqv)[VL]) {
   const R small = R(1.e-6);
@@ -829,7 +838,7 @@ __device__ __forceinline__ void fill_from_above(int L, int lane, R (&y)[NF][VL],
         a = A * a;
       }
     }
-    R x = affine_entry_up(lane, a, b);
+    R x = affine_entry_up<R, W>(lane, a, b);
 #pragma unroll
     for (int v = 0; v < VL; v++) {
       const int k = kb + v;
@@ -894,14 +903,16 @@ __global__ void __launch_bounds__(32 * kWarpsInflate) k_inflate(Grid<R> g, Strid
 
 // vec: every field column starts on a min(16, VL*sizeof(R))-byte boundary
 // and nvl is a multiple of VL (the copies and stores are then VL wide)
-template <typename R, int VL>
+// WL: lanes per column (32, or 16 with two columns per warp in hand)
+template <typename R, int VL, int WL>
 __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Strides s, Knobs kn,
     const StepParams* __restrict__ sp, const R* __restrict__ targt, const R* __restrict__ exsmo,
     R* __restrict__ us3d, R* __restrict__ vs3d, R* __restrict__ tr3d, R* __restrict__ sdot,
     R* __restrict__ ex3d, R* __restrict__ dp3d, R* __restrict__ pr3d, int* __restrict__ flags, int bnd,
     int vec) {
-  using W = RemapV<R, VL>;
-  constexpr int D = W::D;
+  constexpr int H = 32 / WL;  // columns in hand per warp
+  using SW = RemapV<R, VL, H>;
+  constexpr int D = SW::D;
   constexpr int CB = VL * (int)sizeof(R) < 16 ? VL * (int)sizeof(R) : 16;  // bytes per copy
   constexpr int CE = CB / (int)sizeof(R);                                  // values per copy
   // fields whose pcwise runs interleaved (register budget)
@@ -915,12 +926,14 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active || (bnd && sp->its <= 1)) return;
-  W& S = reinterpret_cast<W*>(smraw)[wib];
+  SW& S = reinterpret_cast<SW*>(smraw)[wib];
   exsmo += m * s.intf; us3d += m * s.cell; vs3d += m * s.cell; tr3d += m * s.tr; sdot += m * s.intf;
   ex3d += m * s.intf; dp3d += m * s.cell; pr3d += m * s.intf;
   const int its = sp->its - bnd;
   const R cp = R(kCp), rd = R(kRd), p1000 = R(kP1000), small = R(1.e-6);
-  const int kb = lane * VL;
+  const int hw = lane / WL, ls = lane - hw * WL;  // column in hand, lane within it
+  const int kb = ls * VL;
+  const int ngroups = (ncol + H - 1) / H;            // columns gc*H + hw, gc < ngroups
   // fields in order o: 0 = theta, 1 = u, 2 = v, 3.. = tracers 2..ntra;
   // items per column: the interface arrays (ex3d, pr3d, exsmo), then the
   // fields three by three
@@ -929,15 +942,15 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
     return o == 1 ? us3d + (size_t)i * L : o == 2 ? vs3d + (size_t)i * L
          : tr3d + ((size_t)(o == 0 ? 0 : o - 2) * N + i) * L;
   };
-  // copy item j of column c0 + c into ring slot q (an empty group past the last column)
-  auto issue = [&](int c, int j, int q) {
-    if (c < ncol) {
-      const int i = c0 + c;
+  // copy item j of the columns gc*H + hw into ring slot q (an empty group past the last)
+  auto issue = [&](int gc, int j, int q) {
+    if (gc < ngroups && gc * H + hw < ncol) {
+      const int i = c0 + gc * H + hw;
       if (j == 0) {
 #pragma unroll
         for (int h = 0; h < 3; h++) {
           const R* src = (h == 0 ? ex3d : h == 1 ? pr3d : exsmo) + (size_t)i * L1;
-          for (int k = lane; k <= L; k += 32) cp_async<sizeof(R)>(&S.ring[q][h][k], src + k);
+          for (int k = ls; k <= L; k += WL) cp_async<sizeof(R)>(&S.ring[q][hw][h][k], src + k);
         }
       } else {
 #pragma unroll
@@ -948,12 +961,12 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
             if (vec) {
               if (kb < L) {
 #pragma unroll
-                for (int e = 0; e < VL; e += CE) cp_async<CB>(&S.ring[q][h][kb + e], src + kb + e);
+                for (int e = 0; e < VL; e += CE) cp_async<CB>(&S.ring[q][hw][h][kb + e], src + kb + e);
               }
             } else {
 #pragma unroll
               for (int v = 0; v < VL; v++)
-                if (kb + v < L) cp_async<sizeof(R)>(&S.ring[q][h][kb + v], src + kb + v);
+                if (kb + v < L) cp_async<sizeof(R)>(&S.ring[q][hw][h][kb + v], src + kb + v);
             }
           }
         }
@@ -970,70 +983,72 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
   LaneGeo<R, VL> gp;
   R dpv[VL], qqv[VL];
   bool bad = false;
-  int c = 0, j = 0, qs = 0;   // item in hand: column, item, ring slot
-  while (c < ncol) {
+  int gc = 0, j = 0, qs = 0;   // item in hand: column group, item, ring slot
+  while (gc < ngroups) {
     cp_async_wait<D - 1>();
     __syncwarp();
-    const int i = c0 + c;
+    const int cs = gc * H + hw;            // this lane's column (index within the warp)
+    const bool valid = cs < ncol;          // the second column of a last odd group is idle
+    const int i = c0 + (valid ? cs : 0);
     R y[3][VL];
     if (j == 0) {
-      for (int k = lane; k <= L; k += 32) {
-        S.exold[k] = S.ring[qs][0][k];
-        S.prcol[k] = S.ring[qs][1][k];
-        S.exnew[k] = S.ring[qs][2][k];
+      for (int k = ls; k <= L; k += WL) {
+        S.exold[hw][k] = S.ring[qs][hw][0][k];
+        S.prcol[hw][k] = S.ring[qs][hw][1][k];
+        S.exnew[hw][k] = S.ring[qs][hw][2][k];
       }
     } else {
 #pragma unroll
       for (int h = 0; h < 3; h++)
 #pragma unroll
-        for (int v = 0; v < VL; v++) y[h][v] = kb + v < L ? S.ring[qs][h][kb + v] : R(0);
+        for (int v = 0; v < VL; v++) y[h][v] = kb + v < L ? S.ring[qs][hw][h][kb + v] : R(0);
     }
     __syncwarp();
     issue(ic, ij, qs);   // D items ahead, into the slot just read
     if (++ij == I) { ij = 0; ++ic; }
     if (j == 0) {
       // new interfaces (exsmo -> exnew), pressures and p^(kappa+1) of the column
-      for (int k = lane; k <= L; k += 32) {
-        const R eo = S.exold[k];
-        R en = S.exnew[k];
+      for (int k = ls; k <= L; k += WL) {
+        const R eo = S.exold[hw][k];
+        R en = S.exnew[hw][k];
         if (its > 0) {
           const R sl = R(kn.slak);
           en = sl * en + (R(1) - sl) * eo;
         }
-        S.exnew[k] = en;
-        S.pk1col[k] = eo * S.prcol[k] / cp;
+        S.exnew[hw][k] = en;
+        S.pk1col[hw][k] = eo * S.prcol[hw][k] / cp;
       }
       __syncwarp();
       // miglim = 1: exnew(2..nvl) between the neighbouring old interfaces
-      for (int k = 2 + lane; k <= L; k += 32)
-        S.exnew[k - 1] = cmax(R(.0001) * S.exold[k - 1] + R(.9999) * S.exold[k],
-                              cmin(R(.0001) * S.exold[k - 1] + R(.9999) * S.exold[k - 2], S.exnew[k - 1]));
+      for (int k = 2 + ls; k <= L; k += WL)
+        S.exnew[hw][k - 1] = cmax(R(.0001) * S.exold[hw][k - 1] + R(.9999) * S.exold[hw][k],
+                              cmin(R(.0001) * S.exold[hw][k - 1] + R(.9999) * S.exold[hw][k - 2], S.exnew[hw][k - 1]));
       __syncwarp();
-      for (int k = lane; k <= L; k += 32) {
+      for (int k = ls; k <= L; k += WL) {
         // the reference's own operations: the pressures of unmoved
         // interfaces then reproduce the old ones exactly, so the layer
         // thicknesses keep summing to the unchanged column mass
-        const R en = S.exnew[k];
+        const R en = S.exnew[hw][k];
         const R pn = p1000 * pow(en / cp, cp / rd);
-        S.prnew[k] = pn;
-        S.pk1new[k] = en * pn / cp;
+        S.prnew[hw][k] = pn;
+        S.pk1new[hw][k] = en * pn / cp;
       }
       __syncwarp();
-      for (int k = lane; k < L; k += 32) S.dpcol[k] = S.prnew[k] - S.prnew[k + 1];
+      for (int k = ls; k < L; k += WL) S.dpcol[hw][k] = S.prnew[hw][k] - S.prnew[hw][k + 1];
       __syncwarp();
-      if (lane == 0) {
-        S.prnew[L] = S.prcol[L];
-        S.pk1new[L] = S.pk1col[L];
-        S.prnew[0] = S.prcol[0];
-        S.pk1new[0] = S.pk1col[0];
-        S.flo[c] = S.pk1col[0] * small;
+      if (ls == 0) {
+        S.prnew[hw][L] = S.prcol[hw][L];
+        S.pk1new[hw][L] = S.pk1col[hw][L];
+        S.prnew[hw][0] = S.prcol[hw][0];
+        S.pk1new[hw][0] = S.pk1col[hw][0];
+        S.flo[cs] = S.pk1col[hw][0] * small;
       }
       __syncwarp();
-      for (int k = lane; k < L; k += 32) S.dkb[c][k] = S.pk1new[k] - S.pk1new[k + 1];
-      lane_geo<R, VL>(L, lane, S.prcol, S.prnew, gp);
+      for (int k = ls; k < L; k += WL) S.dkb[cs][k] = S.pk1new[hw][k] - S.pk1new[hw][k + 1];
+      lane_geo<R, VL, WL>(L, ls, S.prcol[hw], S.prnew[hw], gp);
 #pragma unroll
       for (int v = 0; v < VL; v++) {
-        dpv[v] = kb + v < L ? S.dpcol[kb + v] : R(0);
+        dpv[v] = kb + v < L ? S.dpcol[hw][kb + v] : R(0);
         qqv[v] = R(1) / (dpv[v] + small);
       }
       __syncwarp();
@@ -1041,30 +1056,31 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
       // theta in p^(kappa+1), held for the redistribution after the last column
       {
         LaneGeo<R, VL> gk;
-        lane_geo<R, VL>(L, lane, S.pk1col, S.pk1new, gk);
+        lane_geo<R, VL, WL>(L, ls, S.pk1col[hw], S.pk1new[hw], gk);
         if (sizeof(R) == 8) {
           R colin = R(0), colscl = R(0);
 #pragma unroll
           for (int v = 0; v < VL; v++)
             if (kb + v < L) {
-              const R w = y[0][v] * (S.pk1col[kb + v] - S.pk1col[kb + v + 1]);
+              const R w = y[0][v] * (S.pk1col[hw][kb + v] - S.pk1col[hw][kb + v + 1]);
               colin += w;
               colscl += cabs(w);
             }
-          colin = warp_sum(colin);
-          colscl = warp_sum(colscl);
-          if (lane == 0) {
-            S.colin[c] = colin;
-            S.colscl[c] = colscl;
+          colin = warp_sum<R, WL>(colin);
+          colscl = warp_sum<R, WL>(colscl);
+          if (ls == 0) {
+            S.colin[cs] = colin;
+            S.colscl[cs] = colscl;
           }
         }
         R t[1][VL];
 #pragma unroll
         for (int v = 0; v < VL; v++) t[0][v] = y[0][v];
-        bad |= pcwise_v<R, VL, 1>(L, lane, t, gk);
+        const bool bt = pcwise_v<R, VL, 1, WL>(L, ls, t, gk);
+        bad |= valid && bt;
 #pragma unroll
         for (int v = 0; v < VL; v++)
-          if (kb + v < L) S.thb[c][kb + v] = t[0][v];
+          if (kb + v < L) S.thb[cs][kb + v] = t[0][v];
       }
       // u, v in pressure
       if constexpr (NT == 3) {
@@ -1074,28 +1090,33 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
           uv[0][v] = y[1][v];
           uv[1][v] = y[2][v];
         }
-        bad |= pcwise_v<R, VL, 2>(L, lane, uv, gp);
-        store_levels<R, VL>(us3d + (size_t)i * L, L, kb, vec, uv[0]);
-        store_levels<R, VL>(vs3d + (size_t)i * L, L, kb, vec, uv[1]);
+        const bool bu = pcwise_v<R, VL, 2, WL>(L, ls, uv, gp);
+        bad |= valid && bu;
+        if (valid) {
+          store_levels<R, VL>(us3d + (size_t)i * L, L, kb, vec, uv[0]);
+          store_levels<R, VL>(vs3d + (size_t)i * L, L, kb, vec, uv[1]);
+        }
       } else {
 #pragma unroll
         for (int h = 1; h < 3; h++) {
           R t[1][VL];
 #pragma unroll
           for (int v = 0; v < VL; v++) t[0][v] = y[h][v];
-          bad |= pcwise_v<R, VL, 1>(L, lane, t, gp);
-          store_levels<R, VL>(field(h, i), L, kb, vec, t[0]);
+          const bool bu = pcwise_v<R, VL, 1, WL>(L, ls, t, gp);
+          bad |= valid && bu;
+          if (valid) store_levels<R, VL>(field(h, i), L, kb, vec, t[0]);
         }
       }
     } else {
       // tracers 2..ntra in pressure
       const int o0 = 3 * (j - 1);
       if constexpr (NT == 3) {
-        bad |= pcwise_v<R, VL, 3>(L, lane, y, gp);
-        if (kn.thktop == 0.) fill_from_above<R, VL, 3>(L, lane, y, dpv, qqv);
+        const bool bq = pcwise_v<R, VL, 3, WL>(L, ls, y, gp);
+        bad |= valid && bq;
+        if (kn.thktop == 0.) fill_from_above<R, VL, 3, WL>(L, ls, y, dpv, qqv);
 #pragma unroll
         for (int h = 0; h < 3; h++)
-          if (o0 + h < F) store_levels<R, VL>(field(o0 + h, i), L, kb, vec, y[h]);
+          if (valid && o0 + h < F) store_levels<R, VL>(field(o0 + h, i), L, kb, vec, y[h]);
       } else {
 #pragma unroll
         for (int h = 0; h < 3; h++) {
@@ -1103,55 +1124,57 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
             R t[1][VL];
 #pragma unroll
             for (int v = 0; v < VL; v++) t[0][v] = y[h][v];
-            bad |= pcwise_v<R, VL, 1>(L, lane, t, gp);
-            if (kn.thktop == 0.) fill_from_above<R, VL, 1>(L, lane, t, dpv, qqv);
-            store_levels<R, VL>(field(o0 + h, i), L, kb, vec, t[0]);
+            const bool bq = pcwise_v<R, VL, 1, WL>(L, ls, t, gp);
+            bad |= valid && bq;
+            if (kn.thktop == 0.) fill_from_above<R, VL, 1, WL>(L, ls, t, dpv, qqv);
+            if (valid) store_levels<R, VL>(field(o0 + h, i), L, kb, vec, t[0]);
           }
         }
       }
     }
     if (j == I - 1) {
       // exnew made non-increasing downward: prefix minimum over the
-      // interfaces; lane l holds interfaces l*VL .. l*VL+VL-1 (running minimum
-      // within the lane, one warp scan of the lane minima), interface nvl
-      // (when 32*VL == nvl) takes the minimum over all lanes
+      // interfaces; the column's lane l holds interfaces l*VL .. l*VL+VL-1
+      // (running minimum within the lane, one scan of the lane minima over
+      // the column's WL lanes), interface nvl (when WL*VL == nvl) takes the
+      // minimum over all of them
       const size_t ci = (size_t)i * L1;
-      const R top = S.exnew[0];  // fill: no interface lies above the column top
+      const R top = S.exnew[hw][0];  // fill: no interface lies above the column top
       R pm[VL];
 #pragma unroll
       for (int v = 0; v < VL; v++) {
         const int k = kb + v;
-        const R x = k <= L ? S.exnew[k] : top;
+        const R x = k <= L ? S.exnew[hw][k] : top;
         pm[v] = v == 0 ? x : cmin(pm[v - 1], x);
       }
       R tot = pm[VL - 1];
 #pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        const R o = __shfl_up_sync(0xffffffffu, tot, off);
-        if (lane >= off) tot = cmin(tot, o);
+      for (int off = 1; off < WL; off <<= 1) {
+        const R o = __shfl_up_sync(0xffffffffu, tot, off, WL);
+        if (ls >= off) tot = cmin(tot, o);
       }
-      const R above = __shfl_up_sync(0xffffffffu, tot, 1);
-      const R all = __shfl_sync(0xffffffffu, tot, 31);
+      const R above = __shfl_up_sync(0xffffffffu, tot, 1, WL);
+      const R all = __shfl_sync(0xffffffffu, tot, WL - 1, WL);
 #pragma unroll
       for (int v = 0; v < VL; v++) {
         const int k = kb + v;
-        if (k <= L) {
-          const R x = lane > 0 ? cmin(pm[v], above) : pm[v];
-          sdot[ci + k] = x - S.exold[k];
+        if (valid && k <= L) {
+          const R x = ls > 0 ? cmin(pm[v], above) : pm[v];
+          sdot[ci + k] = x - S.exold[hw][k];
           ex3d[ci + k] = x;
-          pr3d[ci + k] = S.prnew[k];
-          if (k < L) dp3d[(size_t)i * L + k] = S.dpcol[k];
+          pr3d[ci + k] = S.prnew[hw][k];
+          if (k < L) dp3d[(size_t)i * L + k] = S.dpcol[hw][k];
         }
       }
-      if (32 * VL == L && lane == 0) {
-        const R x = cmin(S.exnew[L], all);
-        sdot[ci + L] = x - S.exold[L];
+      if (valid && WL * VL == L && ls == 0) {
+        const R x = cmin(S.exnew[hw][L], all);
+        sdot[ci + L] = x - S.exold[hw][L];
         ex3d[ci + L] = x;
-        pr3d[ci + L] = S.prnew[L];
+        pr3d[ci + L] = S.prnew[hw][L];
       }
       __syncwarp();
     }
-    if (++j == I) { j = 0; ++c; }
+    if (++j == I) { j = 0; ++gc; }
     if (++qs == D) qs = 0;
   }
   cp_async_wait<0>();
@@ -1190,7 +1213,7 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
     }
   }
   __syncwarp();
-  for (int cc = 0; cc < ncol; cc++) {
+  for (int cc = hw; cc < ncol; cc += H) {
     R y[VL];
 #pragma unroll
     for (int v = 0; v < VL; v++) y[v] = kb + v < L ? S.thb[cc][kb + v] : R(0);
@@ -1199,24 +1222,36 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
   if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flags + m, kFlagColumnIntegral);
 }
 
-template <typename R, int VL>
-size_t remap_v_smem() { return sizeof(RemapV<R, VL>) * kWarpsRemapV; }
+template <typename R, int VL, int WL>
+size_t remap_v_smem() { return sizeof(RemapV<R, VL, 32 / WL>) * kWarpsRemapV; }
 template <typename R, int ML>
 size_t inflate_smem() { return sizeof(R) * (32 * (ML + 1) + 1) * kWarpsInflate; }
 
 // levels per lane of k_remap_v
 inline int remap_vl(int L) { return L <= 32 ? 1 : L <= 64 ? 2 : 4; }
 
+// two columns per warp (16 lanes x 4 levels) for FP32 with 32 < nvl <= 64:
+// each ring item, scan and shuffle then serves two columns
+template <typename R>
+inline bool remap_paired(int L) { return sizeof(R) == 4 && L > 32 && L <= 64; }
+
 template <typename R>
 int prepare_hybgen(int L) {
-  cudaError_t e;
+  cudaError_t e = cudaSuccess;
   const int vl = remap_vl(L);
-  if (vl == 1)
-    e = cudaFuncSetAttribute(k_remap_v<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)remap_v_smem<R, 1>());
+  if (remap_paired<R>(L)) {
+    if constexpr (sizeof(R) == 4)
+      e = cudaFuncSetAttribute(k_remap_v<R, 4, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)remap_v_smem<R, 4, 16>());
+  } else if (vl == 1)
+    e = cudaFuncSetAttribute(k_remap_v<R, 1, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)remap_v_smem<R, 1, 32>());
   else if (vl == 2)
-    e = cudaFuncSetAttribute(k_remap_v<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)remap_v_smem<R, 2>());
+    e = cudaFuncSetAttribute(k_remap_v<R, 2, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)remap_v_smem<R, 2, 32>());
   else
-    e = cudaFuncSetAttribute(k_remap_v<R, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)remap_v_smem<R, 4>());
+    e = cudaFuncSetAttribute(k_remap_v<R, 4, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)remap_v_smem<R, 4, 32>());
   if (e == cudaSuccess) {
     if (L <= 64)
       e = cudaFuncSetAttribute(k_inflate<R, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1611,21 +1646,22 @@ void launch_hybgen(const Launch& l, const Grid<R>& g, const Strides& s, const Kn
       FIM_KEND(l);
     }
     dim3 gw(nblocks(g.N, kWarpsRemapV * kColsPerWarp), l.members);
-    const int vl = remap_vl(g.L);
+    const bool paired = remap_paired<R>(g.L);
+    const int vl = paired ? 4 : remap_vl(g.L);
     const int cb = (int)(vl * sizeof(R) < 16 ? vl * sizeof(R) : 16);
     int vec = g.L % vl == 0;
     for (const void* p : {(const void*)us3d, (const void*)vs3d, (const void*)tr3d})
       if ((uintptr_t)p % cb != 0) vec = 0;
     FIM_KBEGIN(l, "k_remap");
-    if (vl == 1)
-      k_remap_v<R, 1><<<gw, 32 * kWarpsRemapV, remap_v_smem<R, 1>(), l.stream>>>(
-          g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags, l.boundary, vec);
-    else if (vl == 2)
-      k_remap_v<R, 2><<<gw, 32 * kWarpsRemapV, remap_v_smem<R, 2>(), l.stream>>>(
-          g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags, l.boundary, vec);
-    else
-      k_remap_v<R, 4><<<gw, 32 * kWarpsRemapV, remap_v_smem<R, 4>(), l.stream>>>(
-          g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags, l.boundary, vec);
+#define FIM_REMAP_V(VL, WL)                                                                                  \
+  k_remap_v<R, VL, WL><<<gw, 32 * kWarpsRemapV, remap_v_smem<R, VL, WL>(), l.stream>>>(                       \
+      g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags, l.boundary, vec)
+    if (paired) {
+      if constexpr (sizeof(R) == 4) FIM_REMAP_V(4, 16);
+    } else if (vl == 1) FIM_REMAP_V(1, 32);
+    else if (vl == 2) FIM_REMAP_V(2, 32);
+    else FIM_REMAP_V(4, 32);
+#undef FIM_REMAP_V
   } else if (g.L <= 64) {
     FIM_KBEGIN(l, "k_remap");
     k_remap<R, 64><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d,
