@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(kBlock) k_edgvar1(Grid<R> g, Strides s, int hi
       const R m_3ldg = vmag(u3ldg, v3ldg);
       const R m_1 = vmag(uu, vv);
       const R m_2 = (two * (m_1ldg + m_2ldg) + m_3trl + m_3ldg) * divby6;
-      const R q = m_2 / rmax(eps, m_1);  // one division for both components
+      const R q = fdiv(m_2, rmax(eps, m_1));  // one division for both components
       uu = uu * q;
       vv = vv * q;
       ue[j] = uu;
@@ -354,8 +354,8 @@ __global__ void __launch_bounds__(kBlock) k_cnuity3(Grid<R> g, Strides s, const 
     const R dpmax = rmax(R(0), mx[j]), dpmin = rmax(R(0), mn[j]);
     const R q_plus = (dpmax - dlo[j] - (ab2 * rmin(R(0), to[j]) + ab3 * rmax(R(0), tv[j]))) * rab1 * ar;
     const R q_mnus = (dlo[j] - dpmin + (ab2 * rmax(R(0), to[j]) + ab3 * rmin(R(0), tv[j]))) * rab1 * ar;
-    rp[j] = rmax(R(0), rmin(R(1), q_plus / rmax(pp[j], thshld)));
-    rm[j] = rmax(R(0), rmin(R(1), q_mnus / rmax(pm[j], thshld)));
+    rp[j] = rmax(R(0), rmin(R(1), fdiv(q_plus, rmax(pp[j], thshld))));
+    rm[j] = rmax(R(0), rmin(R(1), fdiv(q_mnus, rmax(pm[j], thshld))));
   }
   stv<VK>(r_plus + c, rp);
   stv<VK>(r_mnus + c, rm);
@@ -729,7 +729,7 @@ __global__ void __launch_bounds__(kBlock) k_trcadv1(Grid<R> g, Strides s, const 
   mn = rmax(R(0), mn);
   trmax[c] = mx;
   trmin[c] = mn;
-  trcr_lo[c] = rmax(mn, rmin(mx, trcdp_lo / rmax(thshld, delp[c])));
+  trcr_lo[c] = rmax(mn, rmin(mx, fdiv(trcdp_lo, rmax(thshld, delp[c]))));
 }
 
 // trcadv2 (trcadv_compute.F90:171-235)
@@ -779,8 +779,8 @@ __global__ void __launch_bounds__(kBlock) k_trcadv2(Grid<R> g, Strides s, const 
   const R rab1 = R(1) / ab1;  // one reciprocal, as k_tr_lim
   const R q_plus = ((mx - lo) * dp - (ab2 * rmin(R(0), to) + ab3 * rmax(R(0), tv))) * rab1 * g.area[i];
   const R q_mnus = ((lo - mn) * dp + (ab2 * rmax(R(0), to) + ab3 * rmin(R(0), tv))) * rab1 * g.area[i];
-  r_plus[c] = rmax(R(0), rmin(R(1), q_plus / rmax(s_plus, thshld)));
-  r_mnus[c] = rmax(R(0), rmin(R(1), q_mnus / rmax(s_mnus, thshld)));
+  r_plus[c] = rmax(R(0), rmin(R(1), fdiv(q_plus, rmax(s_plus, thshld))));
+  r_mnus[c] = rmax(R(0), rmin(R(1), fdiv(q_mnus, rmax(s_mnus, thshld))));
 }
 
 // trcadv3 (trcadv_compute.F90:270-309)
@@ -823,7 +823,7 @@ __global__ void __launch_bounds__(kBlock) k_trcadv3(Grid<R> g, Strides s, const 
   trc_tdcy[(size_t)nf * NL + c] = tn;
   const R td = trcdp[c] + ab1 * tn + ab2 * trc_tdcy[(size_t)of * NL + c] + ab3 * trc_tdcy[(size_t)vof * NL + c];
   trcdp[c] = td;
-  tracr[c] = rmax(trmin[c], rmin(trmax[c], td / rmax(thshld, delp[c])));
+  tracr[c] = rmax(trmin[c], rmin(trmax[c], fdiv(td, rmax(thshld, delp[c]))));
 }
 
 // --------------------------------------------------------------------------

@@ -207,6 +207,16 @@ __device__ __forceinline__ void stv(R* p, const R (&r)[VK]) {
 
 #define FOR_V _Pragma("unroll") for (int j = 0; j < VK; j++)
 
+// a / b for the clamped quotients of the FCT limiters: IEEE division in FP64;
+// __fdividef in the FP32-mixed build (within 2 ulp while |b| < 2^126; the
+// denominators are clamped to >= 1e-11 and are far below that bound).  The
+// fused and the per-routine tracer kernels use it alike, so they stay
+// bit-identical.
+template <typename R>
+__device__ __forceinline__ R fdiv(R a, R b) { return a / b; }
+template <>
+__device__ __forceinline__ float fdiv<float>(float a, float b) { return __fdividef(a, b); }
+
 // (cell, first level) of thread gid over nip x (nvl/VK)
 template <int VK>
 __device__ __forceinline__ bool cell_levels(int N, int L, int& i, int& k) {

@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(kTB, kTBMin) k_tr_lo(Grid<R> g, Strides s, con
   FOR_V {
     const R lo = td[j] + ab1 * tn[j] + ab2 * tlo[j] + ab3 * tlv[j];
     const R hx = tmax(R(0), mx[j]), hn = tmax(R(0), mn[j]);
-    out[j] = tmax(hn, tmin(hx, lo / tmax(thshld, dp[j])));
+    out[j] = tmax(hn, tmin(hx, fdiv(lo, tmax(thshld, dp[j]))));
   }
   stv<VK>(trcr_lo + q, out);
   stv<VK>(s_plus + q, sp_);
@@ -219,8 +219,8 @@ __global__ void __launch_bounds__(kTB, kTBMin) k_tr_lim(Grid<R> g, Strides s, co
     const R hx = tmax(R(0), mx[j]), hn = tmax(R(0), mn[j]);
     const R q_plus = ((hx - lc[j]) * dp[j] - (ab2 * tmin(R(0), tof[j]) + ab3 * tmax(R(0), tvf[j]))) * rab1 * ar;
     const R q_mnus = ((lc[j] - hn) * dp[j] + (ab2 * tmax(R(0), tof[j]) + ab3 * tmin(R(0), tvf[j]))) * rab1 * ar;
-    rp[j] = tmax(R(0), tmin(R(1), q_plus / tmax(spl[j], thshld)));
-    rm[j] = tmax(R(0), tmin(R(1), q_mnus / tmax(smn[j], thshld)));
+    rp[j] = tmax(R(0), tmin(R(1), fdiv(q_plus, tmax(spl[j], thshld))));
+    rm[j] = tmax(R(0), tmin(R(1), fdiv(q_mnus, tmax(smn[j], thshld))));
   }
   stv<VK>(r_plus + so + c, rp);
   stv<VK>(r_mnus + so + c, rm);
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(kTB, kTBMin) k_tr_hi(Grid<R> g, Strides s, con
   FOR_V {
     tdv[j] = tdv[j] + ab1 * tn[j] + ab2 * tof[j] + ab3 * tvf[j];
     const R hx = tmax(R(0), mx[j]), hn = tmax(R(0), mn[j]);
-    out[j] = tmax(hn, tmin(hx, tdv[j] / tmax(thshld, dp[j])));
+    out[j] = tmax(hn, tmin(hx, fdiv(tdv[j], tmax(thshld, dp[j]))));
   }
   stv<VK>(td + c, tdv);
   stv<VK>(tracr + m * s.tr + (size_t)t * NL + c, out);
