@@ -662,8 +662,8 @@ __device__ __forceinline__ void lane_geo(int L, int lane, const R* xo, const R* 
       thin = thin || fo < fill_thin<R>();
     }
     G.fo[v] = fo;
-    G.rfo[v] = R(1) / (fo + small);
-    G.rfn[v] = R(1) / (fn + small);
+    G.rfo[v] = fdiv(R(1), fo + small);
+    G.rfn[v] = fdiv(R(1), fn + small);
     R nd = R(0), hh = R(0);
     if (k >= 1 && k <= L - 1) {
       const R d = flip ? (-xn[k]) - (-xo[k]) : xn[k] - xo[k];
@@ -672,7 +672,7 @@ __device__ __forceinline__ void lane_geo(int L, int lane, const R* xo, const R* 
         if (fl > R(0)) {
           const R dd = d > R(0) ? d : -d;
           const R dsl = cmin(R(0) + fl, dd) - cmin(R(0), dd);
-          const R dx = dsl / fl;
+          const R dx = fdiv(dsl, fl);
           const R hx = d > R(0) ? dx - R(1) : R(1) - dx;
           if (dsl != R(0)) {
             nd = -d;
@@ -1049,7 +1049,7 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
 #pragma unroll
       for (int v = 0; v < VL; v++) {
         dpv[v] = kb + v < L ? S.dpcol[hw][kb + v] : R(0);
-        qqv[v] = R(1) / (dpv[v] + small);
+        qqv[v] = fdiv(R(1), dpv[v] + small);
       }
       __syncwarp();
     } else if (j == 1) {

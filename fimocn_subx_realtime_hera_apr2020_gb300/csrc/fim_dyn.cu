@@ -884,7 +884,7 @@ __global__ void __launch_bounds__(kBlock) k_dissip(Grid<R> g, Strides s, const R
   const R rar = g.rarea[i];
   FOR_V {
     dpi[j] = rmax(dpi[j], thshld);
-    factor[j] = rar / dpi[j];
+    factor[j] = fdiv(rar, dpi[j]);
     dfl[j] = g.dfflen[k + j];
     su[j] = R(0);
     sv[j] = R(0);
@@ -916,7 +916,7 @@ __global__ void __launch_bounds__(kBlock) k_dissip(Grid<R> g, Strides s, const R
       const R uxy1 = cs[0] * ui[j] + sn[0] * vi[j], vxy1 = -sn[0] * ui[j] + cs[0] * vi[j];
       const R uxy2 = cs[1] * ux[j] + sn[1] * vx[j], vxy2 = -sn[1] * ux[j] + cs[1] * vx[j];
       const R b = rmax(bx[j], thshld);
-      const R hf = dpi[j] * b / (dpi[j] + b);
+      const R hf = fdiv(dpi[j] * b, dpi[j] + b);
       const R ufx = (uxy2 - uxy1) * dfl[j] * sl * two * hf;
       const R vfx = (vxy2 - vxy1) * dfl[j] * sl * two * hf;
       const R uflux = cs[0] * ufx - sn[0] * vfx;
