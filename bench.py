@@ -43,7 +43,9 @@ WORDS = {
     "k_cnuity12": lambda T: 37, "k_cnuity3": lambda T: 8, "k_cnuity4": lambda T: 26, "k_cnuity5": lambda T: 14,
     "k_trcadv1": lambda T: 27 * T, "k_trcadv2": lambda T: 16 * T, "k_trcadv3": lambda T: 18 * T,
     "k_dissip": lambda T: 5, "k_del4prep": lambda T: 4, "k_momtum1": lambda T: 44,
-    "k_regrid": lambda T: 3, "k_dffusn_lev": lambda T: 2, "k_remap": lambda T: 2 * T + 10, "k_inflate": lambda T: 2,
+    # in the step the remap also writes tracer x thickness (T words), which
+    # k_hystat_trdp then leaves out
+    "k_regrid": lambda T: 3, "k_dffusn_lev": lambda T: 2, "k_remap": lambda T: 3 * T + 10, "k_inflate": lambda T: 2,
     "k_hystat": lambda T: 7, "k_hystat_trdp": lambda T: 2 * T + 3, "k_globsum_levels": lambda T: T + 1,
 }
 

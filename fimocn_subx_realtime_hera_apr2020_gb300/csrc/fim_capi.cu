@@ -692,10 +692,15 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
   Launch lb = l;
   lb.boundary = 1;
   HybgenScratch<R> hw{(R*)c->exsmo, (R*)c->exsmo2};
-  launch_hybgen<R>(lb, g, s, c->kn, hw, g.thetac, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_TR3D),
-                   F<R>(st, FIM_SDOT), F<R>(st, FIM_EX3D), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D));
+  // the remap also forms hystat's floors and tracer x thickness (one pass
+  // over the tracers instead of two)
+  const bool trdp_done =
+      launch_hybgen<R>(lb, g, s, c->kn, hw, g.thetac, F<R>(st, FIM_US3D), F<R>(st, FIM_VS3D), F<R>(st, FIM_TR3D),
+                       F<R>(st, FIM_SDOT), F<R>(st, FIM_EX3D), F<R>(st, FIM_DP3D), F<R>(st, FIM_PR3D),
+                       F<R>(st, FIM_TRDP));
   launch_hystat<R>(lb, g, s, F<R>(st, FIM_PH3D), F<R>(st, FIM_EX3D), F<R>(st, FIM_MP3D), F<R>(st, FIM_DP3D),
-                   F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP), F<R>(st, FIM_PSRF), F<R>(st, FIM_PTDCY), st->mpf);
+                   F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP), F<R>(st, FIM_PSRF), F<R>(st, FIM_PTDCY), st->mpf,
+                   trdp_done);
   // the dynamics of the step, one member group at a time; the edge work
   // fields and the scratch hold one group, the prognostic fields all members
   for (int m0 = 0; m0 < M; m0 += c->G) {

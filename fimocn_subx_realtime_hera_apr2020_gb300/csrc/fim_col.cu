@@ -625,6 +625,7 @@ struct RemapV {
   R exold[H][S], prcol[H][S], exnew[H][S], prnew[H][S], pk1col[H][S], pk1new[H][S], dpcol[H][S];
   R tg[S];
   R thb[kColsPerWarp][S], dkb[kColsPerWarp][S];
+  R dpb[kColsPerWarp][S];  // new thicknesses, for theta x thickness (trdp) after the redistribution
   R flo[kColsPerWarp], colin[kColsPerWarp], colscl[kColsPerWarp];
 };
 static_assert(sizeof(RemapV<float, 1, 1>) % 16 == 0 && sizeof(RemapV<double, 1, 1>) % 16 == 0 &&
@@ -880,6 +881,23 @@ __device__ __forceinline__ void store_levels(R* dst, int L, int kb, int vec, con
   }
 }
 
+// tracer t (0-based, >= 1) of column i leaving the remap when tracer x
+// thickness is formed here: hystat's floor for tracers 2 and 3 (applied to y,
+// which the caller then stores), then trdp = y * dp (hystat.F90:90-101)
+template <typename R, int VL>
+__device__ __forceinline__ void tracer_out(int t, R qvmin, R qwmin, const R (&dp)[VL], R (&y)[VL], R* trdp,
+                                           size_t NL, int i, int L, int kb, int vec) {
+  if (t == 1 || t == 2) {
+    const R floor = t == 1 ? qvmin : qwmin;
+#pragma unroll
+    for (int v = 0; v < VL; v++) y[v] = cmax(floor, y[v]);
+  }
+  R z[VL];
+#pragma unroll
+  for (int v = 0; v < VL; v++) z[v] = y[v] * dp[v];
+  store_levels<R, VL>(trdp + (size_t)t * NL + (size_t)i * L, L, kb, vec, z);
+}
+
 // inflate (hybgen.F90:893-1007) of 32 columns per warp, lane = column
 template <typename R, int ML>
 __global__ void __launch_bounds__(32 * kWarpsInflate) k_inflate(Grid<R> g, Strides s, Knobs kn,
@@ -909,7 +927,7 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
     const StepParams* __restrict__ sp, const R* __restrict__ targt, const R* __restrict__ exsmo,
     R* __restrict__ us3d, R* __restrict__ vs3d, R* __restrict__ tr3d, R* __restrict__ sdot,
     R* __restrict__ ex3d, R* __restrict__ dp3d, R* __restrict__ pr3d, int* __restrict__ flags, int bnd,
-    int vec) {
+    int vec, R* __restrict__ trdp) {
   constexpr int H = 32 / WL;  // columns in hand per warp
   using SW = RemapV<R, VL, H>;
   constexpr int D = SW::D;
@@ -929,8 +947,11 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
   SW& S = reinterpret_cast<SW*>(smraw)[wib];
   exsmo += m * s.intf; us3d += m * s.cell; vs3d += m * s.cell; tr3d += m * s.tr; sdot += m * s.intf;
   ex3d += m * s.intf; dp3d += m * s.cell; pr3d += m * s.intf;
+  if (trdp) trdp += m * s.tr;
   const int its = sp->its - bnd;
   const R cp = R(kCp), rd = R(kRd), p1000 = R(kP1000), small = R(1.e-6);
+  // hystat's floors of tracers 2 and 3 (hystat.F90:90-93) when trdp is formed here
+  const R qvmin = R(kQvmin), qwmin = R(kQwmin);
   const int hw = lane / WL, ls = lane - hw * WL;  // column in hand, lane within it
   const int kb = ls * VL;
   const int ngroups = (ncol + H - 1) / H;            // columns gc*H + hw, gc < ngroups
@@ -1045,6 +1066,8 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
       }
       __syncwarp();
       for (int k = ls; k < L; k += WL) S.dkb[cs][k] = S.pk1new[hw][k] - S.pk1new[hw][k + 1];
+      if (trdp)
+        for (int k = ls; k < L; k += WL) S.dpb[cs][k] = S.dpcol[hw][k];
       lane_geo<R, VL, WL>(L, ls, S.prcol[hw], S.prnew[hw], gp);
 #pragma unroll
       for (int v = 0; v < VL; v++) {
@@ -1116,7 +1139,10 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
         if (kn.thktop == 0.) fill_from_above<R, VL, 3, WL>(L, ls, y, dpv, qqv);
 #pragma unroll
         for (int h = 0; h < 3; h++)
-          if (valid && o0 + h < F) store_levels<R, VL>(field(o0 + h, i), L, kb, vec, y[h]);
+          if (valid && o0 + h < F) {
+            if (trdp) tracer_out<R, VL>(o0 + h - 2, qvmin, qwmin, dpv, y[h], trdp, (size_t)N * L, i, L, kb, vec);
+            store_levels<R, VL>(field(o0 + h, i), L, kb, vec, y[h]);
+          }
       } else {
 #pragma unroll
         for (int h = 0; h < 3; h++) {
@@ -1127,7 +1153,10 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
             const bool bq = pcwise_v<R, VL, 1, WL>(L, ls, t, gp);
             bad |= valid && bq;
             if (kn.thktop == 0.) fill_from_above<R, VL, 1, WL>(L, ls, t, dpv, qqv);
-            if (valid) store_levels<R, VL>(field(o0 + h, i), L, kb, vec, t[0]);
+            if (valid) {
+              if (trdp) tracer_out<R, VL>(o0 + h - 2, qvmin, qwmin, dpv, t[0], trdp, (size_t)N * L, i, L, kb, vec);
+              store_levels<R, VL>(field(o0 + h, i), L, kb, vec, t[0]);
+            }
           }
         }
       }
@@ -1218,6 +1247,12 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
 #pragma unroll
     for (int v = 0; v < VL; v++) y[v] = kb + v < L ? S.thb[cc][kb + v] : R(0);
     store_levels<R, VL>(tr3d + (size_t)(c0 + cc) * L, L, kb, vec, y);
+    if (trdp) {
+      R z[VL];
+#pragma unroll
+      for (int v = 0; v < VL; v++) z[v] = kb + v < L ? y[v] * S.dpb[cc][kb + v] : R(0);
+      store_levels<R, VL>(trdp + (size_t)(c0 + cc) * L, L, kb, vec, z);
+    }
   }
   if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flags + m, kFlagColumnIntegral);
 }
@@ -1609,8 +1644,9 @@ __global__ void __launch_bounds__(kBlock2) k_prdp_from_ex(Grid<R> g, Strides s, 
 
 
 template <typename R>
-void launch_hybgen(const Launch& l, const Grid<R>& g, const Strides& s, const Knobs& kn, const HybgenScratch<R>& w,
-                   const R* targt, R* us3d, R* vs3d, R* tr3d, R* sdot, R* ex3d, R* dp3d, R* pr3d) {
+bool launch_hybgen(const Launch& l, const Grid<R>& g, const Strides& s, const Knobs& kn, const HybgenScratch<R>& w,
+                   const R* targt, R* us3d, R* vs3d, R* tr3d, R* sdot, R* ex3d, R* dp3d, R* pr3d, R* trdp) {
+  bool trdp_done = false;
   dim3 gc(nblocks(g.N, kColBlock), l.members);
   if (g.L <= 64) {
     FIM_KBEGIN(l, "k_regrid");
@@ -1655,13 +1691,14 @@ void launch_hybgen(const Launch& l, const Grid<R>& g, const Strides& s, const Kn
     FIM_KBEGIN(l, "k_remap");
 #define FIM_REMAP_V(VL, WL)                                                                                  \
   k_remap_v<R, VL, WL><<<gw, 32 * kWarpsRemapV, remap_v_smem<R, VL, WL>(), l.stream>>>(                       \
-      g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags, l.boundary, vec)
+      g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, l.flags, l.boundary, vec, trdp)
     if (paired) {
       if constexpr (sizeof(R) == 4) FIM_REMAP_V(4, 16);
     } else if (vl == 1) FIM_REMAP_V(1, 32);
     else if (vl == 2) FIM_REMAP_V(2, 32);
     else FIM_REMAP_V(4, 32);
 #undef FIM_REMAP_V
+    trdp_done = trdp != nullptr;
   } else if (g.L <= 64) {
     FIM_KBEGIN(l, "k_remap");
     k_remap<R, 64><<<gc, kColBlock, 0, l.stream>>>(g, s, kn, l.sp, targt, ex_in, us3d, vs3d, tr3d, sdot, ex3d,
@@ -1672,11 +1709,12 @@ void launch_hybgen(const Launch& l, const Grid<R>& g, const Strides& s, const Kn
                                                        dp3d, pr3d, l.flags, l.boundary);
   }
   FIM_KEND(l);
+  return trdp_done;
 }
 
 template <typename R>
 void launch_hystat(const Launch& l, const Grid<R>& g, const Strides& s, R* ph3d, const R* ex3d, R* mp3d,
-                   const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy, float2* mpf) {
+                   const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy, float2* mpf, bool trdp_done) {
   dim3 gw(nblocks((long long)g.N * 32, kBlock2), l.members);
   FIM_KBEGIN(l, "k_hystat");
   const int nc = (g.L + 31) / 32;
@@ -1688,6 +1726,7 @@ void launch_hystat(const Launch& l, const Grid<R>& g, const Strides& s, R* ph3d,
   else FIM_HYSTAT(4);
 #undef FIM_HYSTAT
   FIM_KEND(l);
+  if (trdp_done) return;  // the remap formed the floors and tracer x thickness
   const int vk = pick_vk<R>(g.L, {dp3d, tr3d, trdp});
   FIM_KBEGIN(l, "k_hystat_trdp");
   FIM_VK_DISPATCH(R, vk, (k_hystat_trdp<R, VK><<<dim3(nblocks((long long)g.N * (g.L / VK), kBlock2), l.members),
@@ -1737,10 +1776,10 @@ void launch_prdp_from_ex(const Launch& l, const Grid<R>& g, const Strides& s, co
 
 #define INSTANTIATE(R)                                                                                       \
   template int prepare_hybgen<R>(int);                                                                       \
-  template void launch_hybgen<R>(const Launch&, const Grid<R>&, const Strides&, const Knobs&,               \
-                                 const HybgenScratch<R>&, const R*, R*, R*, R*, R*, R*, R*, R*);            \
+  template bool launch_hybgen<R>(const Launch&, const Grid<R>&, const Strides&, const Knobs&,               \
+                                 const HybgenScratch<R>&, const R*, R*, R*, R*, R*, R*, R*, R*, R*);            \
   template void launch_hystat<R>(const Launch&, const Grid<R>&, const Strides&, R*, const R*, R*, const R*, \
-                                 R*, R*, R*, R*, float2*);                                                  \
+                                 R*, R*, R*, R*, float2*, bool);                                                  \
   template void launch_globsum<R>(const Launch&, const Grid<R>&, const Strides&, int, const R*, const R*,        \
                                   const R*, const R*, const R*, const R*, const R*, double*, double*);      \
   template void launch_prdp_from_ex<R>(const Launch&, const Grid<R>&, const Strides&, const R*, R*, R*);

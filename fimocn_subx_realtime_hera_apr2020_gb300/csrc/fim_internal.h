@@ -356,12 +356,17 @@ struct HybgenScratch { R *exsmo, *exsmo2; };
 // returns a cudaError_t value
 template <typename R>
 int prepare_hybgen(int L);
+// trdp != null: the default-knob remap also applies hystat's humidity floors
+// and writes tracer x thickness of the new state (returns true; hystat can
+// then skip that stream)
 template <typename R>
-void launch_hybgen(const Launch&, const Grid<R>&, const Strides&, const Knobs&, const HybgenScratch<R>&,
-                   const R* targt, R* us3d, R* vs3d, R* tr3d, R* sdot, R* ex3d, R* dp3d, R* pr3d);
+bool launch_hybgen(const Launch&, const Grid<R>&, const Strides&, const Knobs&, const HybgenScratch<R>&,
+                   const R* targt, R* us3d, R* vs3d, R* tr3d, R* sdot, R* ex3d, R* dp3d, R* pr3d,
+                   R* trdp = nullptr);
 template <typename R>
 void launch_hystat(const Launch&, const Grid<R>&, const Strides&, R* ph3d, const R* ex3d, R* mp3d,
-                   const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy, float2* mpf = nullptr);
+                   const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy, float2* mpf = nullptr,
+                   bool trdp_done = false);
 // class-B transport (fim_trb.cu); scratch per member: w (nvl x nip), the
 // other fields (nvl x nip x ntrb)
 template <typename R>
