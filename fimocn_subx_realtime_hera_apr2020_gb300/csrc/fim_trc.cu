@@ -24,6 +24,19 @@ namespace fim {
 template <typename R> __device__ __forceinline__ R tmax(R a, R b) { return a > b ? a : b; }
 template <typename R> __device__ __forceinline__ R tmin(R a, R b) { return a < b ? a : b; }
 template <typename R> __device__ __forceinline__ R tabs(R a) { return a < R(0) ? -a : a; }
+// max/min of three (exact; FP32 uses the three-input instructions)
+template <typename R> __device__ __forceinline__ R tmax3(R a, R b, R c) { return tmax(a, tmax(b, c)); }
+template <typename R> __device__ __forceinline__ R tmin3(R a, R b, R c) { return tmin(a, tmin(b, c)); }
+template <> __device__ __forceinline__ float tmax3<float>(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+template <> __device__ __forceinline__ float tmin3<float>(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
 // product rounded on its own (never contracted into a following add)
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
@@ -205,7 +218,7 @@ __global__ void __launch_bounds__(kTB, kTBMin) k_tr_lim(Grid<R> g, Strides s, co
     R a[VK], b[VK];
     ldv<VK>(to + cx, a);
     ldv<VK>(lo + cx, b);
-    FOR_V { mx[j] = tmax(mx[j], tmax(a[j], b[j])); mn[j] = tmin(mn[j], tmin(a[j], b[j])); }
+    FOR_V { mx[j] = tmax3(mx[j], a[j], b[j]); mn[j] = tmin3(mn[j], a[j], b[j]); }
   }
   const R* tc = trc_tdcy + m * s.trab + (size_t)t * 3 * NL;
   R tof[VK], tvf[VK], dp[VK], spl[VK], smn[VK], rp[VK], rm[VK];
@@ -268,7 +281,7 @@ __global__ void __launch_bounds__(kTB, kTBMin) k_tr_hi(Grid<R> g, Strides s, con
     R trx[VK], lox[VK];
     ldv<VK>(to + cx, trx);
     ldv<VK>(lo + cx, lox);
-    FOR_V { mx[j] = tmax(mx[j], tmax(trx[j], lox[j])); mn[j] = tmin(mn[j], tmin(trx[j], lox[j])); }
+    FOR_V { mx[j] = tmax3(mx[j], trx[j], lox[j]); mn[j] = tmin3(mn[j], trx[j], lox[j]); }
     if (e < np) {
       const int own = (i * 6 + e) * L + k, mir = (ipx * 6 + ps[e]) * L + k;
       R mf[VK], mfx[VK], tev[VK], rpx[VK], rmx[VK];
