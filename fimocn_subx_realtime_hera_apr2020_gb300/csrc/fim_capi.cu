@@ -718,10 +718,11 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
                       P(FIM_V_EDG), P(FIM_DP_EDG), P(FIM_LP_EDG), P(FIM_MONT_EDG),
                       P(FIM_UVSQ_EDG), P(FIM_TRC_EDG), mpf, (R*)st->thold);
     if (c->kn.hi_order) {
-      // dp edges with edgvar3's two-sided average; tracer edges keep the
-      // own-side values, averaged where the fused tracer kernels use them
+      // own-side dp and tracer edge values; the two-sided averages are formed
+      // where they are used (k_cnuity12 for dp; k_tr_lo/k_tr_hi for the
+      // tracers); mass_adv reads the averaged dp edges, so it keeps the pass
       launch_edgvar3<R>(lg, g, s, P(FIM_DP3D), P(FIM_TR3D), P(FIM_DP_EDG), P(FIM_TRC_EDG),
-                        1);
+                        1, c->cfg.flux_conserv_schm != 1);
       launch_tracer_own<R>(lg, g, s, P(FIM_TR3D), P(FIM_TRC_EDG), c->trc_vk, c->trc_tb);
     }
     CnuityScratch<R> cw{(R*)c->antifx, (R*)c->delp_lo, (R*)c->p_plus, (R*)c->p_mnus, (R*)c->r_plus, (R*)c->r_mnus};

@@ -282,7 +282,12 @@ __global__ void __launch_bounds__(kBlock) k_cnuity12(Grid<R> g, Strides s, const
     ldv<VK>(v_edg + o, ve);
     ldv<VK>(u_edg + ox, ux);
     ldv<VK>(v_edg + ox, vx_);
+    // edgvar3's two-sided average 0.5*(own + neighbour's own), formed here
+    // (exact also when dp_edg already holds it: 0.5*(w + w) == w)
+    R dm[VK];
     ldv<VK>(dp_edg + o, de);
+    ldv<VK>(dp_edg + ox, dm);
+    FOR_V de[j] = half * (de[j] + dm[j]);
     ldv<VK>(delp + (size_t)ipx * L + k, dx);
     FOR_V {
       const R vn = sv[1] * ue[j] - sv[0] * ve[j];
@@ -1112,12 +1117,13 @@ void launch_edgvar1(const Launch& l, const Grid<R>& g, const Strides& s, int hi_
 
 template <typename R>
 void launch_edgvar3(const Launch& l, const Grid<R>& g, const Strides& s, const R* delp, const R* tracr,
-                    R* dp_edg, R* trc_edg, int nfields) {
+                    R* dp_edg, R* trc_edg, int nfields, bool average) {
   const int vk = pick_vk<R>(g.L, {delp, tracr, dp_edg, trc_edg});
   FIM_KBEGIN(l, "k_edgvar3_own");
   FIM_VK_DISPATCH(R, vk, (k_edgvar3_own<R, VK><<<dim3(blocks_for((long long)g.N * (g.L / VK)), l.members, nfields),
                                                  kBlock, 0, l.stream>>>(g, s, delp, tracr, dp_edg, trc_edg)));
   FIM_KEND(l);
+  if (!average) return;
   FIM_KBEGIN(l, "k_edgvar3_avg");
   FIM_VK_DISPATCH(R, vk, (k_edgvar3_avg<R, VK><<<dim3(blocks_for((long long)g.N * (g.L / VK)), l.members, nfields),
                                                  kBlock, 0, l.stream>>>(g, s, dp_edg, trc_edg)));
@@ -1225,7 +1231,7 @@ void launch_step_begin(const Launch& l, StepParams* sp) {
                                   const R*, const R*, const R*, const R*, R*, R*, R*, R*, R*, R*, R*,          \
                                   const float2*, R*);                                                         \
   template void launch_edgvar3<R>(const Launch&, const Grid<R>&, const Strides&, const R*, const R*, R*, R*,  \
-                                  int);                                                                      \
+                                  int, bool);                                                                \
   template void launch_cnuity<R>(const Launch&, const Grid<R>&, const Strides&, const CnuityScratch<R>&,      \
                                  const R*, const R*, const R*, const R*, const R*, const R*, R*, R*, R*, R*,  \
                                  R*, R*, R*);                                                                 \

@@ -300,10 +300,12 @@ void launch_edgvar1(const Launch&, const Grid<R>&, const Strides&, int hi_order,
                     const R* v, const R* delp, const R* pres, const R* montg, const R* tracr,
                     R* u_edg, R* v_edg, R* dp_edg, R* lp_edg, R* mont_edg, R* uvsq_edg, R* trc_edg,
                     const float2* mpf = nullptr, R* thold = nullptr);
-// nfields: 1 = dp only, T = dp and tracers 2..ntra (edgvar3's full output)
+// nfields: 1 = dp only, T = dp and tracers 2..ntra (edgvar3's full output);
+// average = false leaves the own-side values (k_cnuity12 averages the layer
+// thickness's itself)
 template <typename R>
 void launch_edgvar3(const Launch&, const Grid<R>&, const Strides&, const R* delp, const R* tracr,
-                    R* dp_edg, R* trc_edg, int nfields);
+                    R* dp_edg, R* trc_edg, int nfields, bool average = true);
 template <typename R>
 struct CnuityScratch { R *antifx, *delp_lo, *p_plus, *p_mnus, *r_plus, *r_mnus; };
 template <typename R>
