@@ -390,31 +390,55 @@ __global__ void __launch_bounds__(kColBlock) k_regrid(Grid<R> g, Strides s, Knob
 }
 
 // dffusn_lev (dffusn.F90:37-58 with dffusn_lev.exe) on interfaces kbl+2..nvl,
-// out of place so every cell reads the unsmoothed neighbours.
+// out of place so every cell reads the unsmoothed neighbours.  A thread takes
+// kDffK interfaces of one cell, kg + j*ng (ng = ceil((nvl+1)/kDffK)), so each
+// load of a warp stays contiguous and the neighbour values of all its
+// interfaces are in flight together (all six prox slots hold valid cells; a
+// pentagon's slot 5 is left out of the sum).
+constexpr int kDffK = 4;
 template <typename R>
 __global__ void __launch_bounds__(kBlock2) k_dffusn_lev(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     int bnd, int k1, int k2, const R* __restrict__ fld, R* __restrict__ out) {
   const int N = g.N, L1 = g.L + 1;
+  const int ng = (L1 + kDffK - 1) / kDffK;
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= N * L1) return;
-  const int i = gid / L1, k = gid - i * L1;
+  if (gid >= N * ng) return;
+  const int i = gid / ng, kg = gid - i * ng;
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active || (bnd && sp->its <= 1)) return;
   fld += m * s.intf; out += m * s.intf;
-  const size_t c = (size_t)i * L1 + k;
-  R val = fld[c];
-  if (k >= k1 && k <= k2) {
-    R flxdv = R(0);
-    const int np = g.nprox[i];
-    for (int e = 0; e < np; e++) {
-      const int ipx = g.prox[i * 6 + e];
-      flxdv = flxdv + (val - fld[(size_t)ipx * L1 + k]) * g.sideln[i * 6 + e];
-    }
-    const R factor = -g.smoo[k] * g.rarea[i];
-    val = val + flxdv * factor;
+  const int np = g.nprox[i];
+  const R* col = fld + (size_t)i * L1;
+  const R* nb[6];
+#pragma unroll
+  for (int e = 0; e < 6; e++) nb[e] = fld + (size_t)g.prox[i * 6 + e] * L1;
+  R val[kDffK], x[kDffK][6];
+#pragma unroll
+  for (int j = 0; j < kDffK; j++) {
+    const int k = kg + j * ng;
+    const bool act = k < L1;
+    const int kk = act ? k : 0;
+    val[j] = col[kk];
+#pragma unroll
+    for (int e = 0; e < 6; e++) x[j][e] = nb[e][kk];
   }
-  out[c] = val;
+  const R rar = g.rarea[i];
+#pragma unroll
+  for (int j = 0; j < kDffK; j++) {
+    const int k = kg + j * ng;
+    if (k >= L1) continue;
+    R v = val[j];
+    if (k >= k1 && k <= k2) {
+      R flxdv = R(0);
+#pragma unroll
+      for (int e = 0; e < 6; e++)
+        if (e < np) flxdv = flxdv + (v - x[j][e]) * g.sideln[i * 6 + e];
+      const R factor = -g.smoo[k] * rar;
+      v = v + flxdv * factor;
+    }
+    out[(size_t)i * L1 + k] = v;
+  }
 }
 
 // remap_1d (hybgen.F90:515-789) followed by the hybgen bookkeeping
@@ -1490,12 +1514,15 @@ constexpr int kMaxT = 32;
 constexpr int kGsCol = kMaxT + 1;
 constexpr int kGsSlots = kMaxT + 5;
 
-// Level sums: a block takes one chunk of kGsChunkPer(VK) cell-levels and
-// one slot q (0: area x dp, 1..ntr: area x dp x tracer q-1); the slots of a
-// chunk are consecutive blocks, so the chunk's thicknesses come from DRAM
-// once and from L2 after.  The slot-0 block of a chunk also forms the column
-// sums of the cells whose first level lies in the chunk.  Partials are per
-// (chunk, slot), reduced in a fixed order: the sums are deterministic.
+// Level sums: a block takes one chunk of kGsChunkPer(VK) cell-levels and a
+// group of kGsGroup consecutive slots q (0: area x dp, 1..ntr: area x dp x
+// tracer q-1): it reads the chunk's thicknesses and cell areas once for the
+// group and one tracer array per slot.  The group holding slot 0 also forms
+// the column sums of the cells whose first level lies in the chunk.  Every
+// slot is summed per thread in level order and per block in a fixed order,
+// and the partials are per (chunk, slot): the sums are deterministic and do
+// not depend on the grouping.
+constexpr int kGsGroup = 7;
 constexpr int kGsIter = 16;
 template <int VK>
 __host__ __device__ constexpr int kGsChunkPer() { return kBlock2 * VK * kGsIter; }
@@ -1526,39 +1553,52 @@ __global__ void __launch_bounds__(kBlock2) k_globsum_levels(Grid<R> g, Strides s
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active) return;
-  const int nslot = T + 1;
-  const int chunk = blockIdx.x / nslot, q = blockIdx.x - chunk * nslot;
+  const int ngrp = (T + kGsGroup) / kGsGroup;  // groups of the T + 1 slots
+  const int chunk = blockIdx.x / ngrp, q0 = (blockIdx.x - chunk * ngrp) * kGsGroup;
+  const int nq = (T + 1 - q0 < kGsGroup) ? T + 1 - q0 : kGsGroup;
   dp3d += m * s.cell; tr += m * s.tr; pr3d += m * s.intf; ex3d += m * s.intf;
-  const size_t NL = (size_t)N * L;
+  // N * L < 2^31 (checked on the host): 32-bit cell-level indices
+  const unsigned NL = (unsigned)N * (unsigned)L;
   constexpr int CH = kGsChunkPer<VK>();
-  const size_t e0 = (size_t)chunk * CH;
-  const R* x_t = q > 0 ? tr + (size_t)(q - 1) * NL : nullptr;
-  Acc<R> acc;
-#pragma unroll 4
-  for (int it = 0; it < kGsIter; it++) {
-    const size_t idx = e0 + ((size_t)it * kBlock2 + threadIdx.x) * VK;
-    if (idx < NL) {
-      const R ar = g.area[(int)(idx / L)];
-      R dp[VK], ad[VK];
-      GsVec<R, VK>::ld(dp3d + idx, dp);
+  const unsigned e0 = (unsigned)chunk * CH;
+  Acc<R> acc[kGsGroup];
+  // the group's arrays: slot 0 reads the thicknesses again (an L1 hit) and
+  // adds area x dp; slots past the last repeat slot T and add nothing, so
+  // every load of an iteration is issued before the first sum
+  const R* xp[kGsGroup];
 #pragma unroll
-      for (int j = 0; j < VK; j++) ad[j] = ar * dp[j];
-      if (q == 0) {
+  for (int u = 0; u < kGsGroup; u++) {
+    const int q = q0 + u <= T ? q0 + u : T;
+    xp[u] = q == 0 ? dp3d : tr + (size_t)(q - 1) * NL;
+  }
+  auto sum_at = [&](unsigned idx) {
+    const R ar = g.area[idx / (unsigned)L];
+    R dp[VK], ad[VK], x[kGsGroup][VK];
+    GsVec<R, VK>::ld(dp3d + idx, dp);
 #pragma unroll
-        for (int j = 0; j < VK; j++) acc.add(ad[j]);
-      } else {
-        R x[VK];
-        GsVec<R, VK>::ld(x_t + idx, x);
+    for (int u = 0; u < kGsGroup; u++) GsVec<R, VK>::ld(xp[u] + idx, x[u]);
 #pragma unroll
-        for (int j = 0; j < VK; j++) acc.add(ad[j] * x[j]);
+    for (int j = 0; j < VK; j++) ad[j] = ar * dp[j];
+#pragma unroll
+    for (int u = 0; u < kGsGroup; u++)
+      if (u < nq) {
+#pragma unroll
+        for (int j = 0; j < VK; j++) acc[u].add(u == 0 && q0 == 0 ? ad[j] : ad[j] * x[u][j]);
       }
+  };
+  if (e0 + CH <= NL) {
+    for (int it = 0; it < kGsIter; it++) sum_at(e0 + ((unsigned)it * kBlock2 + threadIdx.x) * VK);
+  } else {
+    for (int it = 0; it < kGsIter; it++) {
+      const unsigned idx = e0 + ((unsigned)it * kBlock2 + threadIdx.x) * VK;
+      if (idx < NL) sum_at(idx);
     }
   }
   double col[4] = {0., 0., 0., 0.};
-  if (q == 0) {
+  if (q0 == 0) {
     const double dt = sp->dt, rdcp = kRd / kCp;
-    const size_t i0 = (e0 + L - 1) / L;
-    size_t i1 = (e0 + CH + L - 1) / L;
+    const size_t i0 = ((size_t)e0 + L - 1) / L;
+    size_t i1 = ((size_t)e0 + CH + L - 1) / L;
     if (i1 > (size_t)N) i1 = N;
     for (size_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
       const double a = g.area_d[i];
@@ -1575,10 +1615,17 @@ __global__ void __launch_bounds__(kBlock2) k_globsum_levels(Grid<R> g, Strides s
   __shared__ double red[kBlock2 / 32];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   double* out = partial + (m * nchunk + chunk) * kGsSlots;
+  const int nout = nq + (q0 == 0 ? 4 : 0);
 #pragma unroll
-  for (int u = 0; u < 5; u++) {
-    if (u > 0 && q != 0) break;  // uniform across the block
-    double v = u == 0 ? acc.value() : col[u == 0 ? 0 : u - 1];
+  for (int u = 0; u < kGsGroup + 4; u++) {
+    if (u >= nout) break;  // uniform across the block
+    double v = 0.;
+#pragma unroll
+    for (int w = 0; w < kGsGroup; w++)
+      if (w == u) v = acc[w].value();
+#pragma unroll
+    for (int w = 0; w < 4; w++)
+      if (u == nq + w) v = col[w];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     if (lane == 0) red[wib] = v;
@@ -1586,7 +1633,7 @@ __global__ void __launch_bounds__(kBlock2) k_globsum_levels(Grid<R> g, Strides s
     if (threadIdx.x == 0) {
       double t = 0.0;
       for (int w = 0; w < kBlock2 / 32; w++) t += red[w];
-      out[u == 0 ? q : kGsCol + (u - 1)] = t;
+      out[u < nq ? q0 + u : kGsCol + (u - nq)] = t;
     }
     __syncthreads();
   }
@@ -1660,7 +1707,7 @@ bool launch_hybgen(const Launch& l, const Grid<R>& g, const Strides& s, const Kn
   FIM_KEND(l);
   const R* ex_in = w.exsmo;
   if (kn.intfc_smooth > 0.) {
-    dim3 gs(nblocks((long long)g.N * (g.L + 1), kBlock2), l.members);
+    dim3 gs(nblocks((long long)g.N * ((g.L + kDffK) / kDffK), kBlock2), l.members);
     // Fortran levels kbl+2..nvl -> 0-based interfaces kbl+1..nvl-1
     FIM_KBEGIN(l, "k_dffusn_lev");
     k_dffusn_lev<R><<<gs, kBlock2, 0, l.stream>>>(g, s, l.sp, l.boundary, kn.kbl + 1, g.L - 1, w.exsmo,
@@ -1750,14 +1797,15 @@ void launch_globsum(const Launch& l, const Grid<R>& g, const Strides& s, int ntr
   constexpr int VK = sizeof(R) == 4 ? 4 : 2;
   const bool vec = g.L % VK == 0 && (uintptr_t)dp3d % (VK * sizeof(R)) == 0 && (uintptr_t)tr % (VK * sizeof(R)) == 0;
   const long long NL = (long long)g.N * g.L;
+  const unsigned ngrp = (unsigned)(ntr + kGsGroup) / kGsGroup;
   int nchunk;
   if (vec) {
     nchunk = (int)((NL + kGsChunkPer<VK>() - 1) / kGsChunkPer<VK>());
-    k_globsum_levels<R, VK><<<dim3((unsigned)nchunk * (ntr + 1), l.members), kBlock2, 0, l.stream>>>(
+    k_globsum_levels<R, VK><<<dim3((unsigned)nchunk * ngrp, l.members), kBlock2, 0, l.stream>>>(
         g, s, l.sp, ntr, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d, partial, nchunk);
   } else {
     nchunk = (int)((NL + kGsChunkPer<1>() - 1) / kGsChunkPer<1>());
-    k_globsum_levels<R, 1><<<dim3((unsigned)nchunk * (ntr + 1), l.members), kBlock2, 0, l.stream>>>(
+    k_globsum_levels<R, 1><<<dim3((unsigned)nchunk * ngrp, l.members), kBlock2, 0, l.stream>>>(
         g, s, l.sp, ntr, dp3d, tr, rn2d, rc2d, pr3d, ex3d, qf2d, partial, nchunk);
   }
   FIM_KEND(l);
