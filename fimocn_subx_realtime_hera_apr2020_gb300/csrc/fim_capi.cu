@@ -907,6 +907,13 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
       if (e < nprox[i] && (q < 1 || q > 6)) { delete c; return FIM_EINVAL; }
     }
   }
+  // every edge has a mirror: prox(proxs(e), prox(e)) == i (edgvar3's two-sided
+  // averages and trcadv's mirror mass fluxes read the neighbour's side through it)
+  for (int i = 0; i < N; i++)
+    for (int e = 0; e < nprox[i]; e++) {
+      const int x = prox[i * 6 + e];
+      if (x == i || prox[x * 6 + proxs[i * 6 + e]] != i) { delete c; return FIM_EINVAL; }
+    }
   // derived fields (dyn_init.F90:309-338,752-767)
   std::vector<double> rarea(N), corio(N), grnd(N), dfflen(L), biharw(L), smoo(L + 1, 0.0);
   for (int i = 0; i < N; i++) {

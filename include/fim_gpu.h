@@ -115,7 +115,9 @@ int fim_grid_build(int glvl, fim_grid_desc *g);
 /* ---- context ---------------------------------------------------------- */
 /* Upload the grid tables and derived fields (dyn_init.F90:311-338,545-549,
  * 752-767) and fix the configuration; replaces GPUinit/copytoGPUinit
- * (FIMsrc/fim/horizontal/cuda/GPUinit.cu:12-54, dyn_init.F90:199,1198). */
+ * (FIMsrc/fim/horizontal/cuda/GPUinit.cu:12-54, dyn_init.F90:199,1198).
+ * FIM_EINVAL when a neighbour number or an edge's mirror slot is out of range,
+ * or an edge has no mirror: prox(proxs(e,i), prox(e,i)) must be i. */
 int fim_ctx_create(const fim_grid_desc *grid, const fim_config *cfg, fim_ctx **out);
 int fim_ctx_destroy(fim_ctx *ctx);
 /* last CUDA error text of the context (GetLastError.cu:6-14 replacement) */

@@ -29,3 +29,20 @@ def test_grid_nip():
     lib = L.load()
     assert [lib.fim_grid_nip(g) for g in (4, 6, 7, 8)] == [2562, 40962, 163842, 655362]
     assert lib.fim_grid_nip(-1) == -1
+
+
+def test_ctx_rejects_edge_without_mirror():
+    """fim_ctx_create checks prox(proxs(e,i), prox(e,i)) == i for every edge
+    before it touches the device, so a broken table fails with FIM_EINVAL."""
+    import numpy as np
+    import pytest
+    import fimocn_subx_realtime_hera_apr2020_gb300 as F
+    g = F.Grid(4)
+    ps = g.proxs.reshape(-1, 6)
+    i = 100
+    ps[i, 0] = ps[i, 0] % 6 + 1  # point edge 0 of cell 100 at the wrong mirror slot
+    cfg = F.FimConfig(nvl=38, ntra=5, dt=400.0, precision="f64")
+    with pytest.raises(L.FimError) as err:
+        F.Dycore(g, cfg)
+    assert err.value.code == L.FIM_EINVAL
+    assert np.all(ps[:, :5] >= 1)
