@@ -1323,23 +1323,29 @@ int prepare_hybgen(int L) {
 }
 
 // ---------------------------------------------------------------- hystat --
-// hystat (hystat.F90:53-109): one warp per column; surface pressure sum and
-// the bottom-up Montgomery potential / geopotential recursion are warp scans
-// in FP64 (FP64 build) or float-float (FP32-mixed build, which also keeps the
-// (hi, lo) Montgomery potential for the pressure gradient).  Every load of
-// the column (NC chunks of 32 levels) is issued before the first use, so a
-// column costs one memory round trip; theta(k-1) and the Exner function at
-// k+1 come from the neighbouring lanes.  The humidity floors and tracer x
-// thickness are k_hystat_trdp.
-template <typename R, int NC>
-__global__ void __launch_bounds__(kBlock2) k_hystat(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
+// hystat (hystat.F90:53-109): lane = column, 32 columns per warp.  The
+// column set-up reads each 32-level chunk of thickness, theta and Exner
+// function of the warp's columns into shared memory in 128-byte rows, then
+// every lane runs the reference's recursions up its own column (surface
+// pressure sum, Montgomery potential bottom-up, geopotential at the interface
+// above), in FP64 (FP64 build) or float-float (FP32-mixed build, which also
+// keeps the (hi, lo) Montgomery potential for the pressure gradient), and the
+// results leave through the same tiles.  The humidity floors and tracer x
+// thickness are k_hystat_trdp.  Warps per block: 2 (FP32) or 1 (FP64), so the
+// static tiles stay within 48 KB.
+template <typename R>
+constexpr int kHyWarps = sizeof(R) == 4 ? 2 : 1;
+template <typename R>
+__global__ void __launch_bounds__(32 * kHyWarps<R>) k_hystat(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     R* __restrict__ ph3d, const R* __restrict__ ex3d, R* __restrict__ mp3d, const R* __restrict__ dp3d,
     const R* __restrict__ tr3d, R* __restrict__ psrf, R* __restrict__ ptdcy,
     float2* __restrict__ mpf, int bnd) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  __shared__ R tiles[kHyWarps<R>][3][32][33];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int N = g.N, L = g.L, L1 = L + 1;
-  if (warp >= N) return;
-  const int i = warp;
+  const int i0 = (blockIdx.x * kHyWarps<R> + wib) * 32;
+  if (i0 >= N) return;
+  const int ncol = N - i0 < 32 ? N - i0 : 32;
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active || (bnd && sp->its <= 1)) return;
@@ -1347,104 +1353,84 @@ __global__ void __launch_bounds__(kBlock2) k_hystat(Grid<R> g, Strides s, const 
   psrf += m * s.col; ptdcy += m * 2 * s.col;
   if (mpf) mpf += m * s.cell;
   const int its = sp->its - bnd;
-  R dp[NC], th[NC], ex[NC];
-#pragma unroll
-  for (int c = 0; c < NC; c++) {
-    const int k = c * 32 + lane;
-    dp[c] = k < L ? dp3d[(size_t)i * L + k] : R(0);
-    th[c] = k < L ? tr3d[(size_t)i * L + k] : R(0);
-    ex[c] = k <= L ? ex3d[(size_t)i * L1 + k] : R(0);
-  }
-  const R exL = ex3d[(size_t)i * L1 + L];
-  const R ph0 = ph3d[(size_t)i * L1];
-  const R work = psrf[i];
-  // theta at k-1 and the Exner function at k+1 of each lane's level
-  R thm[NC], exn[NC];
-#pragma unroll
-  for (int c = 0; c < NC; c++) {
-    const R up = __shfl_up_sync(0xffffffffu, th[c], 1);
-    const R prev = c > 0 ? __shfl_sync(0xffffffffu, th[c > 0 ? c - 1 : 0], 31) : R(0);
-    thm[c] = lane > 0 ? up : prev;
-    const R dn = __shfl_down_sync(0xffffffffu, ex[c], 1);
-    const R next = c + 1 < NC ? __shfl_sync(0xffffffffu, ex[c + 1 < NC ? c + 1 : c], 0) : exL;
-    exn[c] = lane < 31 ? dn : next;
-  }
-  if constexpr (sizeof(R) == 4) {
-    // float-float sums and scan (FP64-accurate on the FP32 pipes)
-    FF2 ps{0.f, 0.f};
-#pragma unroll
-    for (int c = 0; c < NC; c++) ps = ff_add(ps, FF2{dp[c], 0.f});
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) ps = ff_add(ps, ff_shfl_xor(ps, off));
-    if (lane == 0) {
-      const R pn = ps.hi;
-      psrf[i] = pn;
-      if (its > 0) ptdcy[(size_t)(its % 2) * N + i] = pn - work;
-    }
-    FF2 carry{0.f, 0.f};
-#pragma unroll
-    for (int c = 0; c < NC; c++) {
-      const int k = c * 32 + lane;
-      const bool act = k < L;
-      FF2 term{0.f, 0.f};
-      if (act) {
-        if (k == 0) {
-          term = ff_add(two_prod(ex[c], th[c]), FF2{ph0, 0.f});
+  const int i = i0 + lane;
+  const bool live = lane < ncol;
+  R (*tdp)[33] = tiles[wib][0];  // thickness in, Montgomery potential out
+  R (*tth)[33] = tiles[wib][1];  // theta in, low part of the Montgomery potential out (FP32)
+  R (*tex)[33] = tiles[wib][2];  // Exner function in, geopotential out
+  const R ph0 = live ? ph3d[(size_t)i * L1] : R(0);
+  const R exL = live ? ex3d[(size_t)i * L1 + L] : R(0);
+  const R work = live ? psrf[i] : R(0);
+  FF2 psf{0.f, 0.f}, mpff{0.f, 0.f};
+  double psd = 0.0, mpd = 0.0;
+  R thp = R(0);
+  for (int c0 = 0; c0 < L; c0 += 32) {
+    const int kk = c0 + lane;
+    const int nq = L - c0 < 32 ? L - c0 : 32;
+#pragma unroll 8
+    for (int r = 0; r < 32; r++)
+      if (r < ncol && kk < L) {
+        const size_t ic = (size_t)(i0 + r);
+        tdp[r][lane] = dp3d[ic * L + kk];
+        tth[r][lane] = tr3d[ic * L + kk];
+        tex[r][lane] = ex3d[ic * L1 + kk];
+      }
+    __syncwarp();
+    if (live) {
+      for (int q = 0; q < nq; q++) {
+        const int k = c0 + q;
+        const R d = tdp[lane][q], t = tth[lane][q], e = tex[lane][q];
+        if constexpr (sizeof(R) == 4) {
+          // float-float recursions (FP64-accurate on the FP32 pipes)
+          psf = ff_add(psf, FF2{d, 0.f});
+          FF2 term;
+          if (k == 0) {
+            term = ff_add(two_prod(e, t), FF2{ph0, 0.f});
+          } else {
+            tex[lane][q] = ff_add(mpff, ff_neg(two_prod(thp, e))).hi;  // geopotential at interface k
+            const FF2 dd = two_sum(t, -thp);
+            term = ff_add(two_prod(e, dd.hi), FF2{e * dd.lo, 0.f});
+          }
+          mpff = k == 0 ? term : ff_add(mpff, term);
+          tdp[lane][q] = mpff.hi;
+          tth[lane][q] = mpff.lo;
         } else {
-          const FF2 d = two_sum(th[c], -thm[c]);
-          term = ff_add(two_prod(ex[c], d.hi), FF2{ex[c] * d.lo, 0.f});
+          psd += (double)d;
+          double term;
+          if (k == 0) {
+            term = (double)e * (double)t + (double)ph0;
+          } else {
+            tex[lane][q] = R(mpd - (double)thp * (double)e);
+            term = (double)e * ((double)t - (double)thp);
+          }
+          mpd = k == 0 ? term : mpd + term;
+          tdp[lane][q] = R(mpd);
         }
+        thp = t;
       }
-      FF2 sc = term;
-#pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        const FF2 a = ff_shfl_up(sc, off);
-        if (lane >= off) sc = ff_add(sc, a);
-      }
-      const FF2 mp = ff_add(carry, sc);
-      if (act) {
-        mp3d[(size_t)i * L + k] = mp.hi;
-        if (mpf) mpf[(size_t)i * L + k] = make_float2(mp.hi, mp.lo);
-        const FF2 ph = ff_add(mp, ff_neg(two_prod(th[c], exn[c])));
-        ph3d[(size_t)i * L1 + k + 1] = ph.hi;
-      }
-      carry = ff_add(carry, ff_shfl(sc, 31));
     }
-  } else {
-    // surface pressure: sum of all layer thicknesses
-    double ps = 0.0;
-#pragma unroll
-    for (int c = 0; c < NC; c++) ps += (double)dp[c];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) ps += __shfl_xor_sync(0xffffffffu, ps, off);
-    if (lane == 0) {
-      const R pn = R(ps);
-      psrf[i] = pn;
-      if (its > 0) ptdcy[(size_t)(its % 2) * N + i] = pn - work;
+    __syncwarp();
+#pragma unroll 8
+    for (int r = 0; r < 32; r++)
+      if (r < ncol && kk < L) {
+        const size_t ic = (size_t)(i0 + r);
+        mp3d[ic * L + kk] = tdp[r][lane];
+        if (mpf) mpf[ic * L + kk] = make_float2((float)tdp[r][lane], (float)tth[r][lane]);
+        if (kk >= 1) ph3d[ic * L1 + kk] = tex[r][lane];
+      }
+    __syncwarp();
+  }
+  if (live) {
+    R pn;
+    if constexpr (sizeof(R) == 4) {
+      ph3d[(size_t)i * L1 + L] = ff_add(mpff, ff_neg(two_prod(thp, exL))).hi;
+      pn = psf.hi;
+    } else {
+      ph3d[(size_t)i * L1 + L] = R(mpd - (double)thp * (double)exL);
+      pn = R(psd);
     }
-    double carry = 0.0;
-#pragma unroll
-    for (int c = 0; c < NC; c++) {
-      const int k = c * 32 + lane;
-      const bool act = k < L;
-      double term = 0.0;
-      if (act) {
-        if (k == 0) term = (double)ex[c] * (double)th[c] + (double)ph0;
-        else term = (double)ex[c] * ((double)th[c] - (double)thm[c]);
-      }
-      double sc = term;
-#pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        const double a = __shfl_up_sync(0xffffffffu, sc, off);
-        if (lane >= off) sc += a;
-      }
-      const double mp = carry + sc;
-      if (act) {
-        mp3d[(size_t)i * L + k] = R(mp);
-        ph3d[(size_t)i * L1 + k + 1] = R(mp - (double)th[c] * (double)exn[c]);
-      }
-      carry += __shfl_sync(0xffffffffu, sc, 31);
-    }
+    psrf[i] = pn;
+    if (its > 0) ptdcy[(size_t)(its % 2) * N + i] = pn - work;
   }
 }
 
@@ -1762,16 +1748,10 @@ bool launch_hybgen(const Launch& l, const Grid<R>& g, const Strides& s, const Kn
 template <typename R>
 void launch_hystat(const Launch& l, const Grid<R>& g, const Strides& s, R* ph3d, const R* ex3d, R* mp3d,
                    const R* dp3d, R* tr3d, R* trdp, R* psrf, R* ptdcy, float2* mpf, bool trdp_done) {
-  dim3 gw(nblocks((long long)g.N * 32, kBlock2), l.members);
+  dim3 gw(nblocks(g.N, 32 * kHyWarps<R>), l.members);
   FIM_KBEGIN(l, "k_hystat");
-  const int nc = (g.L + 31) / 32;
-#define FIM_HYSTAT(NC) \
-  k_hystat<R, NC><<<gw, kBlock2, 0, l.stream>>>(g, s, l.sp, ph3d, ex3d, mp3d, dp3d, tr3d, psrf, ptdcy, mpf, l.boundary)
-  if (nc == 1) FIM_HYSTAT(1);
-  else if (nc == 2) FIM_HYSTAT(2);
-  else if (nc == 3) FIM_HYSTAT(3);
-  else FIM_HYSTAT(4);
-#undef FIM_HYSTAT
+  k_hystat<R><<<gw, 32 * kHyWarps<R>, 0, l.stream>>>(g, s, l.sp, ph3d, ex3d, mp3d, dp3d, tr3d, psrf, ptdcy, mpf,
+                                                  l.boundary);
   FIM_KEND(l);
   if (trdp_done) return;  // the remap formed the floors and tracer x thickness
   const int vk = pick_vk<R>(g.L, {dp3d, tr3d, trdp});
