@@ -1324,23 +1324,28 @@ int prepare_hybgen(int L) {
 
 // ---------------------------------------------------------------- hystat --
 // hystat (hystat.F90:53-109): lane = column, 32 columns per warp.  The
-// column set-up reads each 32-level chunk of thickness, theta and Exner
-// function of the warp's columns into shared memory in 128-byte rows, then
+// column set-up reads each kHyChunk-level chunk of thickness, theta and
+// Exner function of the warp's columns into shared memory, then
 // every lane runs the reference's recursions up its own column (surface
 // pressure sum, Montgomery potential bottom-up, geopotential at the interface
 // above), in FP64 (FP64 build) or float-float (FP32-mixed build, which also
 // keeps the (hi, lo) Montgomery potential for the pressure gradient), and the
 // results leave through the same tiles.  The humidity floors and tracer x
-// thickness are k_hystat_trdp.  Warps per block: 2 (FP32) or 1 (FP64), so the
-// static tiles stay within 48 KB.
+// thickness are k_hystat_trdp.  A chunk is kHyChunk levels; a load or store
+// instruction of the warp covers 32 / kHyChunk rows (columns).
+#ifndef FIM_HY_CHUNK
+#define FIM_HY_CHUNK 16
+#endif
+constexpr int kHyChunk = FIM_HY_CHUNK;
+constexpr int kHyRows = 32 / kHyChunk;
 template <typename R>
-constexpr int kHyWarps = sizeof(R) == 4 ? 2 : 1;
+constexpr int kHyWarps = sizeof(R) == 4 ? 4 : 2;
 template <typename R>
 __global__ void __launch_bounds__(32 * kHyWarps<R>) k_hystat(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
     R* __restrict__ ph3d, const R* __restrict__ ex3d, R* __restrict__ mp3d, const R* __restrict__ dp3d,
     const R* __restrict__ tr3d, R* __restrict__ psrf, R* __restrict__ ptdcy,
     float2* __restrict__ mpf, int bnd) {
-  __shared__ R tiles[kHyWarps<R>][3][32][33];
+  __shared__ R tiles[kHyWarps<R>][3][32][kHyChunk + 1];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int N = g.N, L = g.L, L1 = L + 1;
   const int i0 = (blockIdx.x * kHyWarps<R> + wib) * 32;
@@ -1355,26 +1360,30 @@ __global__ void __launch_bounds__(32 * kHyWarps<R>) k_hystat(Grid<R> g, Strides 
   const int its = sp->its - bnd;
   const int i = i0 + lane;
   const bool live = lane < ncol;
-  R (*tdp)[33] = tiles[wib][0];  // thickness in, Montgomery potential out
-  R (*tth)[33] = tiles[wib][1];  // theta in, low part of the Montgomery potential out (FP32)
-  R (*tex)[33] = tiles[wib][2];  // Exner function in, geopotential out
+  R (*tdp)[kHyChunk + 1] = tiles[wib][0];  // thickness in, Montgomery potential out
+  R (*tth)[kHyChunk + 1] = tiles[wib][1];  // theta in, low part of the Montgomery potential out (FP32)
+  R (*tex)[kHyChunk + 1] = tiles[wib][2];  // Exner function in, geopotential out
+  // the staging lanes: row (column) rr * kHyRows + lrow, level lk of the chunk
+  const int lrow = lane / kHyChunk, lk = lane - lrow * kHyChunk;
   const R ph0 = live ? ph3d[(size_t)i * L1] : R(0);
   const R exL = live ? ex3d[(size_t)i * L1 + L] : R(0);
   const R work = live ? psrf[i] : R(0);
   FF2 psf{0.f, 0.f}, mpff{0.f, 0.f};
   double psd = 0.0, mpd = 0.0;
   R thp = R(0);
-  for (int c0 = 0; c0 < L; c0 += 32) {
-    const int kk = c0 + lane;
-    const int nq = L - c0 < 32 ? L - c0 : 32;
+  for (int c0 = 0; c0 < L; c0 += kHyChunk) {
+    const int kk = c0 + lk;
+    const int nq = L - c0 < kHyChunk ? L - c0 : kHyChunk;
 #pragma unroll 8
-    for (int r = 0; r < 32; r++)
+    for (int rr = 0; rr < 32 / kHyRows; rr++) {
+      const int r = rr * kHyRows + lrow;
       if (r < ncol && kk < L) {
         const size_t ic = (size_t)(i0 + r);
-        tdp[r][lane] = dp3d[ic * L + kk];
-        tth[r][lane] = tr3d[ic * L + kk];
-        tex[r][lane] = ex3d[ic * L1 + kk];
+        tdp[r][lk] = dp3d[ic * L + kk];
+        tth[r][lk] = tr3d[ic * L + kk];
+        tex[r][lk] = ex3d[ic * L1 + kk];
       }
+    }
     __syncwarp();
     if (live) {
       for (int q = 0; q < nq; q++) {
@@ -1411,13 +1420,15 @@ __global__ void __launch_bounds__(32 * kHyWarps<R>) k_hystat(Grid<R> g, Strides 
     }
     __syncwarp();
 #pragma unroll 8
-    for (int r = 0; r < 32; r++)
+    for (int rr = 0; rr < 32 / kHyRows; rr++) {
+      const int r = rr * kHyRows + lrow;
       if (r < ncol && kk < L) {
         const size_t ic = (size_t)(i0 + r);
-        mp3d[ic * L + kk] = tdp[r][lane];
-        if (mpf) mpf[ic * L + kk] = make_float2((float)tdp[r][lane], (float)tth[r][lane]);
-        if (kk >= 1) ph3d[ic * L1 + kk] = tex[r][lane];
+        mp3d[ic * L + kk] = tdp[r][lk];
+        if (mpf) mpf[ic * L + kk] = make_float2((float)tdp[r][lk], (float)tth[r][lk]);
+        if (kk >= 1) ph3d[ic * L1 + kk] = tex[r][lk];
       }
+    }
     __syncwarp();
   }
   if (live) {

@@ -423,19 +423,26 @@ __global__ void __launch_bounds__(kBlock) k_cnuity4(Grid<R> g, Strides s, const 
   if (bad) atomicOr(flags + m, kFlagBadDp);
 }
 
-// cnuity5 (cnuity_compute.F90:408-445): one warp per column; the top-down
-// pressure sum and the omega flux-convergence integral are warp scans in FP64
-// (FP64 column accumulation in both precisions), then Exner function and the
-// v.grad(p) term per level.
+// cnuity5 (cnuity_compute.F90:408-445) for 32 columns per warp, 32 levels
+// (top-down) at a time.  The layer thickness and pressure tendency of each
+// level are formed with lane = level, one column at a time (128-byte rows),
+// into a shared tile; the top-down pressure sum and the omega flux-convergence
+// integral run with lane = column up the tile in the reference's order (FP64,
+// or float-float in the FP32-mixed build); the Exner function and the
+// v.grad(p) term are formed with lane = level again.
 template <typename R>
-__global__ void __launch_bounds__(kBlock) k_cnuity5(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
-    R* __restrict__ pres, R* __restrict__ delp, R* __restrict__ exner, const R* __restrict__ dp_tndcy,
-    R* __restrict__ omega, const R* __restrict__ lp_edg, const R* __restrict__ u, const R* __restrict__ v,
-    int ab3_delp) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+constexpr int kC5Warps = sizeof(R) == 4 ? 4 : 2;
+template <typename R>
+__global__ void __launch_bounds__(32 * kC5Warps<R>) k_cnuity5(Grid<R> g, Strides s,
+    const StepParams* __restrict__ sp, R* __restrict__ pres, R* __restrict__ delp, R* __restrict__ exner,
+    const R* __restrict__ dp_tndcy, R* __restrict__ omega, const R* __restrict__ lp_edg, const R* __restrict__ u,
+    const R* __restrict__ v, int ab3_delp) {
+  __shared__ R tiles[kC5Warps<R>][2][32][33];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int N = g.N, L = g.L, L1 = L + 1;
-  if (warp >= N) return;
-  const int i = warp;
+  const int i0 = (blockIdx.x * kC5Warps<R> + wib) * 32;
+  if (i0 >= N) return;
+  const int ncol = N - i0 < 32 ? N - i0 : 32;
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active) return;
@@ -444,108 +451,86 @@ __global__ void __launch_bounds__(kBlock) k_cnuity5(Grid<R> g, Strides s, const 
   const int nf = sp->nf, of = sp->of, vof = sp->vof;
   const R ab1 = R(sp->ab1), ab2 = R(sp->ab2), ab3 = R(sp->ab3), dt = R(sp->dt);
   const R cp = R(kCp), p1000 = R(kP1000), rdcp = R(kRd) / R(kCp);
-  const int np = g.nprox[i];
-  const R rar = g.rarea[i];
-  if constexpr (sizeof(R) == 4) {
-    // float-float column sums (FP64-accurate on the FP32 pipes)
-    FF2 carry_p{pres[(size_t)i * L1 + L], 0.f}, carry_c{0.f, 0.f};
-    for (int base = 0; base < L; base += 32) {
-      const int j = base + lane;
-      const bool act = j < L;
-      const int k = L - 1 - j;
-      float d = 0.f, lyr = 0.f;
-      if (act) {
-        const size_t c = (size_t)i * L + k;
-        const R tnf = dp_tndcy[(size_t)nf * N * L + c], tof = dp_tndcy[(size_t)of * N * L + c],
-                tvf = dp_tndcy[(size_t)vof * N * L + c];
+  const size_t NL = (size_t)N * L;
+  R (*tp)[33] = tiles[wib][0];  // thickness in, pressure out
+  R (*tw)[33] = tiles[wib][1];  // layer pressure tendency in, omega's first terms out
+  const bool live = lane < ncol;
+  // the top-down sums of column i0 + lane
+  FF2 pf{0.f, 0.f}, cf{0.f, 0.f};
+  double pd = 0.0, cd = 0.0;
+  if (live) {
+    const R ptop = pres[(size_t)(i0 + lane) * L1 + L];
+    pf = FF2{(float)ptop, 0.f};
+    pd = (double)ptop;
+  }
+  for (int base = 0; base < L; base += 32) {
+    const int j = base + lane;
+    const bool act = j < L;
+    const int k = L - 1 - j;
+    const int nq = L - base < 32 ? L - base : 32;
+#pragma unroll 4
+    for (int r = 0; r < 32; r++)
+      if (r < ncol && act) {
+        const size_t c = (size_t)(i0 + r) * L + k;
+        const R tnf = dp_tndcy[(size_t)nf * NL + c], tof = dp_tndcy[(size_t)of * NL + c],
+                tvf = dp_tndcy[(size_t)vof * NL + c];
+        R d;
         if (ab3_delp) {
           // massflux_newdepth's AB3 thickness update (massadv_compute.F90:85-91)
           R dn = delp[c] + ab1 * tnf + ab2 * tof + ab3 * tvf;
           dn = dn > R(0) ? dn : R(0);
           delp[c] = dn;
+          d = dn;
+        } else {
+          d = delp[c];
         }
-        d = delp[c];
-        lyr = (ab1 * tnf + ab2 * tof + ab3 * tvf) / dt;
+        tp[r][lane] = d;
+        tw[r][lane] = (ab1 * tnf + ab2 * tof + ab3 * tvf) / dt;
       }
-      FF2 sd{d, 0.f}, sl{lyr, 0.f};
-#pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        const FF2 a = ff_shfl_up(sd, off), b = ff_shfl_up(sl, off);
-        if (lane >= off) { sd = ff_add(sd, a); sl = ff_add(sl, b); }
+    __syncwarp();
+    if (live) {
+      for (int q = 0; q < nq; q++) {
+        const R d = tp[lane][q], lyr = tw[lane][q];
+        if constexpr (sizeof(R) == 4) {
+          pf = ff_add(pf, FF2{d, 0.f});
+          tp[lane][q] = pf.hi;
+          // omega = (integral of the layers above) + half of this layer
+          tw[lane][q] = R(cf.hi + cf.lo) + R(0.5) * lyr;
+          cf = ff_add(cf, FF2{lyr, 0.f});
+        } else {
+          pd = pd + (double)d;
+          tp[lane][q] = R(pd);
+          tw[lane][q] = R(cd + 0.5 * (double)lyr);
+          cd = cd + (double)lyr;
+        }
       }
-      if (act) {
+    }
+    __syncwarp();
+#pragma unroll 2
+    for (int r = 0; r < 32; r++)
+      if (r < ncol && act) {
+        const int i = i0 + r;
         const size_t c = (size_t)i * L + k;
-        const FF2 p = ff_add(carry_p, sd);
-        const R pr = p.hi;
+        const R pr = tp[r][lane];
         pres[(size_t)i * L1 + k] = pr;
         exner[(size_t)i * L1 + k] = cp * pow(pr / p1000, rdcp);
-        // omega = (integral of layers above) + half of this layer
-        const FF2 above = ff_add(carry_c, ff_add(sl, FF2{-lyr, 0.f}));
-        R om = R(above.hi + above.lo) + R(0.5) * lyr;
-        R dpdx = R(0), dpdy = R(0);
-        for (int e = 0; e < np; e++) {
-          const R* sv = g.svc + (i * 6 + e) * 2;
-          const R lp = lp_edg[((size_t)i * 6 + e) * L + k];
-          dpdx = dpdx + lp * sv[1];
-          dpdy = dpdy - lp * sv[0];
-        }
-        om = om + (u[c] * dpdx + v[c] * dpdy) * rar;
-        omega[c] = om;
-      }
-      carry_p = ff_add(carry_p, ff_shfl(sd, 31));
-      carry_c = ff_add(carry_c, ff_shfl(sl, 31));
-    }
-    return;
-  }
-  double carry_p = (double)pres[(size_t)i * L1 + L];
-  double carry_c = 0.0;
-  for (int base = 0; base < L; base += 32) {
-    const int j = base + lane;
-    const bool act = j < L;
-    const int k = L - 1 - j;
-    double d = 0.0, lt = 0.0;
-    R lyr = R(0);
-    if (act) {
-      const size_t c = (size_t)i * L + k;
-      const R tnf = dp_tndcy[(size_t)nf * N * L + c], tof = dp_tndcy[(size_t)of * N * L + c],
-              tvf = dp_tndcy[(size_t)vof * N * L + c];
-      if (ab3_delp) {
-        // massflux_newdepth's AB3 thickness update (massadv_compute.F90:85-91)
-        R dn = delp[c] + ab1 * tnf + ab2 * tof + ab3 * tvf;
-        dn = dn > R(0) ? dn : R(0);
-        delp[c] = dn;
-      }
-      d = (double)delp[c];
-      lyr = (ab1 * tnf + ab2 * tof + ab3 * tvf) / dt;
-      lt = (double)lyr;
-    }
-    double sd = d, sl = lt;
+        // pressure gradient over the cell's edges (all six slots hold valid
+        // rows; a pentagon's slot 5 is left out)
+        const int np = g.nprox[i];
+        R lp[6];
 #pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      const double a = __shfl_up_sync(0xffffffffu, sd, off);
-      const double b = __shfl_up_sync(0xffffffffu, sl, off);
-      if (lane >= off) { sd += a; sl += b; }
-    }
-    if (act) {
-      const size_t c = (size_t)i * L + k;
-      const double p = carry_p + sd;
-      const R pr = R(p);
-      pres[(size_t)i * L1 + k] = pr;
-      exner[(size_t)i * L1 + k] = cp * pow(pr / p1000, rdcp);
-      // omega = (integral of layers above) + half of this layer
-      R om = R(carry_c + (sl - lt)) + R(0.5) * lyr;
-      R dpdx = R(0), dpdy = R(0);
-      for (int e = 0; e < np; e++) {
-        const R* sv = g.svc + (i * 6 + e) * 2;
-        const R lp = lp_edg[((size_t)i * 6 + e) * L + k];
-        dpdx = dpdx + lp * sv[1];
-        dpdy = dpdy - lp * sv[0];
+        for (int e = 0; e < 6; e++) lp[e] = lp_edg[((size_t)i * 6 + e) * L + k];
+        R dpdx = R(0), dpdy = R(0);
+#pragma unroll
+        for (int e = 0; e < 6; e++)
+          if (e < np) {
+            const R* sv = g.svc + (i * 6 + e) * 2;
+            dpdx = dpdx + lp[e] * sv[1];
+            dpdy = dpdy - lp[e] * sv[0];
+          }
+        omega[c] = tw[r][lane] + (u[c] * dpdx + v[c] * dpdy) * g.rarea[i];
       }
-      om = om + (u[c] * dpdx + v[c] * dpdy) * rar;
-      omega[c] = om;
-    }
-    carry_p += __shfl_sync(0xffffffffu, sd, 31);
-    carry_c += __shfl_sync(0xffffffffu, sl, 31);
+    __syncwarp();
   }
 }
 
@@ -673,9 +658,10 @@ void launch_massadv(const Launch& l, const Grid<R>& g, const Strides& s, const C
   k_massadv_flux<R><<<grid, kBlock, 0, l.stream>>>(g, s, l.sp, u_edg, v_edg, dp_edg, delp, w.r_plus, w.r_mnus,
                                                     massfx, dp_tndcy);
   FIM_KEND(l);
-  dim3 gw(blocks_for((long long)g.N * 32), l.members);
+  dim3 gw((unsigned)((g.N + 32 * kC5Warps<R> - 1) / (32 * kC5Warps<R>)), l.members);
   FIM_KBEGIN(l, "k_cnuity5");
-  k_cnuity5<R><<<gw, kBlock, 0, l.stream>>>(g, s, l.sp, pres, delp, exner, dp_tndcy, omega, lp_edg, u, v, 1);
+  k_cnuity5<R><<<gw, 32 * kC5Warps<R>, 0, l.stream>>>(g, s, l.sp, pres, delp, exner, dp_tndcy, omega, lp_edg, u,
+                                                      v, 1);
   FIM_KEND(l);
 }
 
@@ -1151,9 +1137,10 @@ void launch_cnuity(const Launch& l, const Grid<R>& g, const Strides& s, const Cn
                                              l.stream>>>(g, s, l.sp, w.antifx, w.r_plus, w.r_mnus, massfx,
                                                          dplo_tndcy, dp_tndcy, delp, l.flags)));
   FIM_KEND(l);
-  dim3 gw(blocks_for((long long)g.N * 32), l.members);
+  dim3 gw((unsigned)((g.N + 32 * kC5Warps<R> - 1) / (32 * kC5Warps<R>)), l.members);
   FIM_KBEGIN(l, "k_cnuity5");
-  k_cnuity5<R><<<gw, kBlock, 0, l.stream>>>(g, s, l.sp, pres, delp, exner, dp_tndcy, omega, lp_edg, u, v, 0);
+  k_cnuity5<R><<<gw, 32 * kC5Warps<R>, 0, l.stream>>>(g, s, l.sp, pres, delp, exner, dp_tndcy, omega, lp_edg, u,
+                                                      v, 0);
   FIM_KEND(l);
 }
 
