@@ -285,7 +285,7 @@ def gpu_arm(args, ws, rank, local):
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 (float-float column scans, FP64 budget reductions)",
+            "vs_baseline": None, "dtype": "f32 (float-float column sums, FP64 budget reductions)",
             "data": "synthetic seeded balanced state (no dataset: the reference's GFS initial state is not "
                     "in the tree)",
             "config": {"workload": args.workload, "glvl": wl["glvl"], "nip": N, "nvl": L, "ntra": T,
