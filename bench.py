@@ -51,6 +51,10 @@ WORDS = {
 
 E2E_FIELDS = ["us3d", "vs3d", "dp3d", "pr3d", "ex3d", "ph3d", "mp3d", "tr3d", "trdp", "u_tdcy", "v_tdcy",
               "dp_tdcy", "dpl_tdcy", "trc_tdcy", "trl_tdcy", "ws3d", "sdot", "relvor", "psrf", "ptdcy"]
+# AB3 tendency fields (a step reads slots of and vof and writes slot nf) and
+# the fields a step writes without reading them
+E2E_AB3 = {"u_tdcy", "v_tdcy", "dp_tdcy", "dpl_tdcy", "trc_tdcy", "trl_tdcy"}
+E2E_OUTPUTS = {"ws3d", "sdot", "relvor", "ptdcy"}
 
 
 def peaks():
@@ -226,7 +230,9 @@ def gpu_arm(args, ws, rank, local):
             "frac": kernels[dom]["gbs"] / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
             "traffic": traffic, "alg_bytes_per_launch": kernels[dom]["alg_bytes"]}
 
-    # end to end through the C-ABI with host buffers: upload the state, step, download it
+    # end to end through the C-ABI with host buffers: every step uploads what it
+    # reads and downloads what it writes (AB3 tendency fields: the two slots it
+    # reads, the one it writes; omega, sdot, relvor and ptdcy are outputs only)
     e2e = None
     if not args.no_e2e:
         bufs = {}
@@ -235,31 +241,52 @@ def gpu_arm(args, ws, rank, local):
             bufs[f] = torch.empty(n * members, dtype=torch.float32, pin_memory=True)
             for m in range(members):
                 st.download(f, m, out=bufs[f][m * n:(m + 1) * n].numpy())
-        bytes_step = sum(b.numel() * 4 for b in bufs.values())
+        lib, ctx, sst, fid = dyc.lib, dyc.ctx, st.st, F.dycore._lib.FIELD_ID
+
+        def one_step():
+            h2d = d2h = 0
+            slots = [st.next_slots(m) for m in range(members)]
+            for f, buf in bufs.items():
+                if f in E2E_OUTPUTS:
+                    continue
+                n = buf.numel() // members
+                for m in range(members):
+                    hp = buf.data_ptr() + m * n * 4
+                    if f in E2E_AB3:
+                        for sl in slots[m][1:]:
+                            _check(lib.fim_state_upload_slot(ctx, sst, fid[f], m, sl, hp), "upload slot")
+                        h2d += 2 * n // 3 * 4
+                    else:
+                        _check(lib.fim_state_upload(ctx, sst, fid[f], m, hp), "upload")
+                        h2d += n * 4
+            st.step(use_graph=True)
+            for f, buf in bufs.items():
+                n = buf.numel() // members
+                for m in range(members):
+                    hp = buf.data_ptr() + m * n * 4
+                    if f in E2E_AB3:
+                        _check(lib.fim_state_download_slot(ctx, sst, fid[f], m, slots[m][0], hp), "download slot")
+                        d2h += n // 3 * 4
+                    else:
+                        _check(lib.fim_state_download(ctx, sst, fid[f], m, hp), "download")
+                        d2h += n * 4
+            return h2d, d2h
+
         stream = torch.cuda.ExternalStream(dyc.stream)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ke = max(1, min(args.steps, 5))
         torch.cuda.synchronize()
         a.record(stream)
         for _ in range(ke):
-            for f, buf in bufs.items():
-                n = buf.numel() // members
-                for m in range(members):
-                    _check(dyc.lib.fim_state_upload(dyc.ctx, st.st, F.dycore._lib.FIELD_ID[f], m,
-                                                    buf.data_ptr() + m * n * 4), "upload")
-            st.step(use_graph=True)
-            for f, buf in bufs.items():
-                n = buf.numel() // members
-                for m in range(members):
-                    _check(dyc.lib.fim_state_download(dyc.ctx, st.st, F.dycore._lib.FIELD_ID[f], m,
-                                                      buf.data_ptr() + m * n * 4), "download")
+            h2d, d2h = one_step()
         b.record(stream)
         b.synchronize()
         e_ms = a.elapsed_time(b) / ke
         e_ms = max_over_ranks(e_ms, ws, torch.device("cuda", local))
         e2e = {"value": units * ws / (e_ms * 1e-3), "unit": UNIT, "ms_per_step": e_ms,
-               "h2d_bytes_per_step": bytes_step, "d2h_bytes_per_step": bytes_step,
-               "path": "fim_state_upload -> fim_step -> fim_state_download (pinned host buffers)"}
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "path": "fim_state_upload(_slot) -> fim_step -> fim_state_download(_slot) (pinned host buffers): "
+                       "the fields the step reads go up, the fields it writes come down"}
         del bufs
     qtrcr, bud = st.budget()
     st.free()

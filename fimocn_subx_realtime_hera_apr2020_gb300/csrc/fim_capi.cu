@@ -1246,6 +1246,39 @@ int fim_state_download(fim_ctx* c, fim_state* st, int field, int member, void* h
   return FIM_OK;
 }
 
+// one AB3 slot of a tendency field: nb blocks of nvl x nip values, the slot's
+// block every third
+static int ab3_slot_copy(fim_ctx* c, fim_state* st, int field, int member, int slot, void* host, bool up) {
+  const bool tr = field == FIM_TRC_TDCY || field == FIM_TRL_TDCY;
+  if (!tr && field != FIM_U_TDCY && field != FIM_V_TDCY && field != FIM_DP_TDCY && field != FIM_DPL_TDCY)
+    return set_err(c, FIM_EINVAL, "not an AB3 tendency field");
+  if (slot < 1 || slot > 3 || !host) return FIM_EINVAL;
+  void* d;
+  int64_t n;
+  int rc = fim_state_field(c, st, field, member, &d, &n);
+  if (rc) return rc;
+  const size_t blk = (size_t)c->N * c->L * c->esz;
+  const size_t nb = tr ? (size_t)c->T : 1;
+  if ((size_t)n * c->esz != 3 * blk * nb) return set_err(c, FIM_EINVAL, "AB3 field size");
+  char* dv = (char*)d + (size_t)(slot - 1) * blk;
+  char* hv = (char*)host + (size_t)(slot - 1) * blk;
+  if (up)
+    CK(cudaMemcpy2DAsync(dv, 3 * blk, hv, 3 * blk, blk, nb, cudaMemcpyHostToDevice, c->stream), "slot upload");
+  else
+    CK(cudaMemcpy2DAsync(hv, 3 * blk, dv, 3 * blk, blk, nb, cudaMemcpyDeviceToHost, c->stream), "slot download");
+  return FIM_OK;
+}
+
+int fim_state_upload_slot(fim_ctx* c, fim_state* st, int field, int member, int slot, const void* host) {
+  if (!c || !st) return FIM_EINVAL;
+  return ab3_slot_copy(c, st, field, member, slot, const_cast<void*>(host), true);
+}
+
+int fim_state_download_slot(fim_ctx* c, fim_state* st, int field, int member, int slot, void* host) {
+  if (!c || !st) return FIM_EINVAL;
+  return ab3_slot_copy(c, st, field, member, slot, host, false);
+}
+
 int fim_state_init(fim_ctx* c, fim_state* st) {
   if (!c || !st) return FIM_EINVAL;
   return c->prec == FIM_PREC_F64 ? state_init_impl<double>(c, st, 0, c->M)

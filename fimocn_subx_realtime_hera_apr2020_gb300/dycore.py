@@ -241,6 +241,33 @@ class DycoreState:
         self.dyc.sync()
         return out
 
+    def upload_slot(self, name, slot, host, member=0):
+        """Upload AB3 slot `slot` (1..3) of a tendency field from the whole-field host array."""
+        ptr, n = self.field_ptr(name, member)
+        host = np.ascontiguousarray(host, dtype=self.dyc.cfg.dtype) if isinstance(host, np.ndarray) else host
+        if isinstance(host, np.ndarray) and host.size != n:
+            raise ValueError("%s: %d elements, expected %d" % (name, host.size, n))
+        _lib.check(self.lib.fim_state_upload_slot(self.dyc.ctx, self.st, _lib.FIELD_ID[name], member, slot,
+                                                  _ptr(host)), "fim_state_upload_slot", self.dyc.ctx)
+        if isinstance(host, np.ndarray):
+            self.dyc.sync()
+
+    def download_slot(self, name, slot, member=0, out=None):
+        """Download AB3 slot `slot` (1..3) of a tendency field into the whole-field host array."""
+        ptr, n = self.field_ptr(name, member)
+        if out is None:
+            out = np.zeros(n, self.dyc.cfg.dtype)
+        _lib.check(self.lib.fim_state_download_slot(self.dyc.ctx, self.st, _lib.FIELD_ID[name], member, slot,
+                                                    _ptr(out)), "fim_state_download_slot", self.dyc.ctx)
+        self.dyc.sync()
+        return out
+
+    def next_slots(self, member=0):
+        """(nf, of, vof) of the member's next step, Fortran numbering: the slot
+        it writes and the two it reads."""
+        _, nf, of, vof, _ = self.get_step(member)
+        return nf % 3 + 1, of % 3 + 1, vof % 3 + 1
+
     def load(self, fields, member=0):
         for k, v in fields.items():
             self.upload(k, v, member)

@@ -282,6 +282,16 @@ int fim_state_field(fim_ctx *ctx, fim_state *st, int field, int member, void **d
 /* host <-> device copy of one member's field (element type per precision) */
 int fim_state_upload(fim_ctx *ctx, fim_state *st, int field, int member, const void *host);
 int fim_state_download(fim_ctx *ctx, fim_state *st, int field, int member, void *host);
+/* The same for one AB3 slot (1..3, Fortran numbering) of a tendency field
+ * (u_tdcy, v_tdcy, dp_tdcy, dpl_tdcy: one nvl x nip block per slot; trc_tdcy,
+ * trl_tdcy: one per tracer).  host holds the whole field as for
+ * fim_state_upload; only the slot's blocks move.  No reference counterpart:
+ * a driver that keeps the state on the host between steps moves the slots the
+ * next step reads (of, vof: fim_member_get_step's slots advanced by one) and
+ * the one it writes (nf) instead of the whole history.  FIM_EINVAL for other
+ * fields or slots. */
+int fim_state_upload_slot(fim_ctx *ctx, fim_state *st, int field, int member, int slot, const void *host);
+int fim_state_download_slot(fim_ctx *ctx, fim_state *st, int field, int member, int slot, void *host);
 
 /* dyn_init.F90:870-906,1037-1094 for every member: trdp, hybgen(its=0),
  * pressure/thickness from Exner, hystat(its=0), zero tendencies, AB3 slots */

@@ -11,6 +11,7 @@ torch = pytest.importorskip("torch")
 
 import fimocn_subx_realtime_hera_apr2020_gb300 as F  # noqa: E402
 from helpers import PROGNOSTIC, make_case, oracle_for, rel_l2  # noqa: E402
+from fimocn_subx_realtime_hera_apr2020_gb300._lib import FimError  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
@@ -308,6 +309,64 @@ def test_fused_step_matches_routine_sequence(case4):
                   g["geop_edg"], g["mont_edg"], g["uvsq_edg"], g["u_tdcy"], g["v_tdcy"], g["dp3d"])
         for n in PROGNOSTIC + ["ws3d", "relvor", "sdot", "trc_tdcy", "trl_tdcy", "massfx"]:
             assert np.array_equal(st.download(n), host(g[n])), (its, n)
+
+
+AB3_FIELDS = ["u_tdcy", "v_tdcy", "dp_tdcy", "dpl_tdcy", "trc_tdcy", "trl_tdcy"]
+STEP_OUTPUTS = ["ws3d", "sdot", "relvor", "ptdcy"]
+
+
+def test_ab3_slot_transfer(case4):
+    """fim_state_upload_slot / fim_state_download_slot move exactly one AB3
+    slot of a tendency field (one block per slot, or one per tracer)."""
+    grid, cfg, fields, o, s = case4
+    dyc, st = _gpu_state(grid, cfg, fields)
+    NL = grid.nip * cfg.nvl
+    rng = np.random.default_rng(11)
+    for name, nb in (("u_tdcy", 1), ("dpl_tdcy", 1), ("trc_tdcy", cfg.ntra), ("trl_tdcy", cfg.ntra)):
+        n = st.field_ptr(name)[1]
+        assert n == nb * 3 * NL
+        full = rng.standard_normal(n)
+        st.upload(name, full)
+        blocks = full.reshape(nb, 3, NL)
+        for slot in (1, 2, 3):
+            got = st.download_slot(name, slot).reshape(nb, 3, NL)
+            assert np.array_equal(got[:, slot - 1], blocks[:, slot - 1])
+            assert not np.any(got[:, [q for q in range(3) if q != slot - 1]])
+        new = full.copy().reshape(nb, 3, NL)
+        new[:, 1] += 1.0
+        new[:, 0] -= 5.0
+        st.upload_slot(name, 2, new.reshape(-1))
+        back = st.download(name).reshape(nb, 3, NL)
+        assert np.array_equal(back[:, 1], new[:, 1])
+        assert np.array_equal(back[:, 0], blocks[:, 0]) and np.array_equal(back[:, 2], blocks[:, 2])
+    with pytest.raises(FimError):
+        st.upload_slot("us3d", 1, st.download("us3d"))
+    with pytest.raises(FimError):
+        st.download_slot("u_tdcy", 4)
+
+
+def test_step_reads_only_uploaded_data(case4):
+    """The end-to-end transfer set is complete: a step reads no AB3 slot other
+    than the two the host uploads (of, vof of the next step) and none of the
+    fields it only writes, so poisoning those with NaN between steps leaves
+    every result bit-identical."""
+    grid, cfg, fields, o0, s0 = case4
+    _, ref = _gpu_state(grid, cfg, fields)
+    _, st = _gpu_state(grid, cfg, fields)
+    for its in range(1, 6):
+        nf, of, vof = st.next_slots()
+        assert len({nf, of, vof}) == 3
+        for f in STEP_OUTPUTS:
+            st.upload(f, np.full(st.field_ptr(f)[1], np.nan))
+        for f in AB3_FIELDS:
+            h = st.download(f)
+            h.reshape(-1, 3, grid.nip * cfg.nvl)[:, nf - 1] = np.nan
+            st.upload_slot(f, nf, h)
+        ref.step(its, use_graph=True)
+        st.step(its, use_graph=True)
+        names = PROGNOSTIC + AB3_FIELDS + ["ws3d", "relvor", "psrf"] + (["sdot"] if its > 1 else [])
+        for n in names:
+            assert np.array_equal(st.download(n), ref.download(n)), (its, n)
 
 
 def test_mass_adv_fp64():
