@@ -532,6 +532,64 @@ def accuracy_arm(args, ws, rank, local):
         d.close()
 
 
+def cpl_arm(args, ws, rank, local):
+    """Physics coupling (fim_cpl_dyn_to_phy / fim_cpl_phy_to_dyn, the default
+    addtend = 0 path) on the workload's FP32-mixed state through the C-ABI with
+    device pointers; CUDA events on the library stream around K calls each."""
+    import ctypes
+    import torch
+    import fimocn_subx_realtime_hera_apr2020_gb300 as F
+
+    torch.cuda.set_device(local)
+    wl = dict(F.WORKLOADS[args.workload])
+    grid = F.Grid.cached(wl["glvl"])
+    N, L, T = grid.nip, wl["nvl"], wl["ntra"]
+    NL = N * L
+    cfg = F.FimConfig(nvl=L, ntra=T, dt=wl["dt"], precision="f32")
+    dyc, st = make_state(F, grid, cfg, wl, np.float32)
+    fp = {n: st.field_ptr(n)[0] for n in ("pr3d", "us3d", "vs3d", "ws3d", "tr3d", "dp3d")}
+    gfs = {n: torch.zeros(N if n == "ps" else NL, dtype=torch.float64, device="cuda") for n in F.Dycore.GFS_NAMES}
+    col = {n: torch.zeros(N, dtype=torch.float64, device="cuda") for n in ("geshem", "rainc", "evap")}
+    c2d = {n: torch.zeros(N, dtype=torch.float32, device="cuda") for n in ("rn2d", "rc2d", "qf2d")}
+    # without physics in between, cpl_phy_to_dyn writes back the state cpl_dyn_to_phy read
+    lib, ctx = dyc.lib, dyc.ctx
+    torch.cuda.synchronize()
+
+    def d2p():
+        _check(lib.fim_cpl_dyn_to_phy_r4(ctx, 1, 1, fp["pr3d"], fp["us3d"], fp["vs3d"], fp["ws3d"], fp["tr3d"],
+                                         *[gfs[n].data_ptr() for n in F.Dycore.GFS_NAMES]), "cpl_dyn_to_phy")
+
+    def p2d():
+        _check(lib.fim_cpl_phy_to_dyn_r4(ctx, 1, 1, 0, 0, ctypes.c_double(wl["dt"]),
+                                         *[gfs[n].data_ptr() for n in ("p", "u", "v", "q", "cld", "oz", "t")],
+                                         *[col[n].data_ptr() for n in ("geshem", "rainc", "evap")], fp["dp3d"],
+                                         fp["us3d"], fp["vs3d"], fp["tr3d"],
+                                         *[c2d[n].data_ptr() for n in ("rn2d", "rc2d", "qf2d")]), "cpl_phy_to_dyn")
+
+    stream = torch.cuda.ExternalStream(dyc.stream)
+    res = {}
+    for name, fn, nbytes in (("cpl_dyn_to_phy", d2p, (8 * 4 + 15 * 8) * NL), ("cpl_phy_to_dyn", p2d, (7 * 8 + 6 * 4) * NL)):
+        for _ in range(args.warmup):
+            fn()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(args.steps):
+            fn()
+        b.record(stream)
+        b.synchronize()
+        ms = a.elapsed_time(b) / args.steps
+        peak, kind = peaks()
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        res[name] = {"ms": ms, "alg_bytes": nbytes, "gbs": gbs, "frac_of_hbm": gbs / peak, "peak_source": kind}
+    if rank == 0:
+        print(json.dumps({"metric": "physics coupling (cpl_run) GB/s", "config": {"workload": args.workload,
+                          "glvl": wl["glvl"], "nip": N, "nvl": L, "ntra": T, "precision": "fp32-mixed"},
+                          "steps": args.steps, "warmup": args.warmup, "coupling": res}))
+    st.free()
+    dyc.close()
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -553,6 +611,7 @@ def main():
     p.add_argument("--accuracy", type=int, default=0, help="report the error after this many steps")
     p.add_argument("--nvl", type=int, default=0)
     p.add_argument("--dt", type=float, default=0.0, help="time step of the accuracy run (default: workload's)")
+    p.add_argument("--cpl", action="store_true", help="time the physics coupling on the workload's state")
     args = p.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -565,6 +624,9 @@ def main():
         return
     if args.accuracy:
         accuracy_arm(args, ws, rank, local)
+        return
+    if args.cpl:
+        cpl_arm(args, ws, rank, local)
         return
     gpu_arm(args, ws, rank, local)
 

@@ -98,6 +98,8 @@ _ROUTINES = {
     "fim_transp0": [_VP, _I] + [_VP] * 3,
     "fim_transp1": [_VP, _I] + [_VP] * 2,
     "fim_transp2": [_VP, _I] + [_VP] * 4,
+    "fim_cpl_dyn_to_phy": [_VP, _I, _I] + [_VP] * 15,
+    "fim_cpl_phy_to_dyn": [_VP, _I, _I, _I, _I, ctypes.c_double] + [_VP] * 17,
 }
 for _name, _args in _ROUTINES.items():
     for _sfx in ("_r8", "_r4"):

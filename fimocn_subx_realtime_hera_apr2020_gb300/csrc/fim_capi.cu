@@ -80,6 +80,7 @@ struct fim_ctx {
   void *du = nullptr, *dv = nullptr, *wu = nullptr, *wv = nullptr;
   void *exsmo = nullptr, *exsmo2 = nullptr;
   double* gs_partial = nullptr;
+  double* cpl_old = nullptr;  // physics coupling: the six gfs_*_old copies (6 nvl nip)
   double* gs_sums = nullptr;  // per-routine globsum output [M][8+T]
   Prof prof;
   std::string err;
@@ -583,6 +584,77 @@ int hystat_impl(fim_ctx* c, int its, R* ph3d, const R* ex3d, R* mp3d, const R* d
   if ((rc = push_sp(c))) return rc;
   launch_hystat<R>(make_launch(c, 1), grid_of<R>(c), c->str, ph, ex, mp, dp, tr, td, ps, pt);
   if ((rc = check_launch(c, "hystat"))) return rc;
+  return s.finish();
+}
+
+// cpl_run.F90:79-208 (callphy branch of cpl_dyn_to_phy)
+template <typename R>
+int cpl_dyn_to_phy_impl(fim_ctx* c, int its, int callphy, const R* pr3d, const R* us3d, const R* vs3d,
+                        const R* ws3d, const R* tr3d, double* const gfs_in[10]) {
+  int rc = check_prec<R>(c);
+  if (rc) return rc;
+  (void)its;
+  if (!callphy) return FIM_OK;
+  for (int q = 0; q < 10; q++)
+    if (!gfs_in[q]) return FIM_EINVAL;
+  if (!pr3d || !us3d || !vs3d || !ws3d || !tr3d) return FIM_EINVAL;
+  const size_t NL = (size_t)c->N * c->L, NI = (size_t)c->N * (c->L + 1);
+  if (!c->cpl_old && (rc = dalloc(c, (void**)&c->cpl_old, 6 * NL * sizeof(double)))) return rc;
+  Stager s(c);
+  const R* pr = s.map(pr3d, NI, 0);
+  const R* u = s.map(us3d, NL, 0);
+  const R* v = s.map(vs3d, NL, 0);
+  const R* w = s.map(ws3d, NL, 0);
+  const R* tr = s.map(tr3d, NL * c->T, 0);
+  double* gfs[10];
+  for (int q = 0; q < 10; q++) gfs[q] = s.map(gfs_in[q], q == 0 ? (size_t)c->N : NL, 2);
+  if (s.rc) return s.rc;
+  launch_cpl_dyn_to_phy<R>(make_launch(c, 1), grid_of<R>(c), pr, u, v, w, tr, gfs, c->cpl_old);
+  if ((rc = check_launch(c, "cpl_dyn_to_phy"))) return rc;
+  return s.finish();
+}
+
+// cpl_run.F90:210-380 (callphy branch of cpl_phy_to_dyn): the dynamics state
+// and the precipitation / evaporation columns
+template <typename R>
+int cpl_phy_to_dyn_impl(fim_ctx* c, int its, int callphy, int addtend, int smoothtend, double dtp,
+                        const double* const gfs_in[7], const double* const col_in[3], const R* dp3d, R* us3d,
+                        R* vs3d, R* tr3d, R* rn2d, R* rc2d, R* qf2d) {
+  int rc = check_prec<R>(c);
+  if (rc) return rc;
+  (void)its;
+  if (!callphy) return FIM_OK;
+  for (int q = 0; q < 7; q++)
+    if (!gfs_in[q]) return FIM_EINVAL;
+  for (int q = 0; q < 3; q++)
+    if (!col_in[q]) return FIM_EINVAL;
+  if (!us3d || !vs3d || !tr3d || !rn2d || !rc2d || !qf2d || (addtend && smoothtend && !dp3d)) return FIM_EINVAL;
+  if (addtend && (!c->cpl_old || !(dtp > 0.)))
+    return set_err(c, FIM_EINVAL, "cpl_phy_to_dyn with addtend needs a preceding cpl_dyn_to_phy and dtp > 0");
+  const size_t NL = (size_t)c->N * c->L;
+  Stager s(c);
+  const double* gfs[7];
+  for (int q = 0; q < 7; q++) gfs[q] = s.map(gfs_in[q], NL, 0);
+  const double* col[3];
+  for (int q = 0; q < 3; q++) col[q] = s.map(col_in[q], (size_t)c->N, 0);
+  const R* dp = s.map(dp3d, NL, 0);
+  R* u = s.map(us3d, NL, 1);
+  R* v = s.map(vs3d, NL, 1);
+  R* tr = s.map(tr3d, NL * c->T, 1);
+  R* rn = s.map(rn2d, (size_t)c->N, 1);
+  R* rcp = s.map(rc2d, (size_t)c->N, 1);
+  R* qf = s.map(qf2d, (size_t)c->N, 1);
+  if (s.rc) return s.rc;
+  double* tend = nullptr;
+  if (addtend) {
+    const size_t bytes = (smoothtend ? 12 : 6) * NL * sizeof(double);
+    cudaError_t e = cudaMallocAsync((void**)&tend, bytes, c->stream);
+    if (e != cudaSuccess) { cudaGetLastError(); return set_err(c, FIM_ENOMEM, "coupling scratch", e); }
+    s.bufs.push_back(tend);
+  }
+  launch_cpl_phy_to_dyn<R>(make_launch(c, 1), grid_of<R>(c), c->cfg.dt, dtp, addtend != 0, smoothtend != 0, gfs,
+                           c->cpl_old, col, dp, u, v, tr, rn, rcp, qf, tend);
+  if ((rc = check_launch(c, "cpl_phy_to_dyn"))) return rc;
   return s.finish();
 }
 
@@ -1128,6 +1200,43 @@ int fim_hystat_r8(fim_ctx* c, int its, double* ph3d, const double* ex3d, double*
 int fim_hystat_r4(fim_ctx* c, int its, float* ph3d, const float* ex3d, float* mp3d, const float* dp3d, float* tr3d,
                   float* trdp, float* psrf, float* ptdcy) {
   return hystat_impl<float>(c, its, ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy);
+}
+
+#define FIM_GFS10 gfs_ps, gfs_dp, gfs_p, gfs_u, gfs_v, gfs_dpdt, gfs_q, gfs_oz, gfs_cld, gfs_t
+int fim_cpl_dyn_to_phy_r8(fim_ctx* c, int its, int callphy, const double* pr3d, const double* us3d,
+                          const double* vs3d, const double* ws3d, const double* tr3d, double* gfs_ps,
+                          double* gfs_dp, double* gfs_p, double* gfs_u, double* gfs_v, double* gfs_dpdt,
+                          double* gfs_q, double* gfs_oz, double* gfs_cld, double* gfs_t) {
+  double* const g[10] = {FIM_GFS10};
+  return cpl_dyn_to_phy_impl<double>(c, its, callphy, pr3d, us3d, vs3d, ws3d, tr3d, g);
+}
+int fim_cpl_dyn_to_phy_r4(fim_ctx* c, int its, int callphy, const float* pr3d, const float* us3d,
+                          const float* vs3d, const float* ws3d, const float* tr3d, double* gfs_ps,
+                          double* gfs_dp, double* gfs_p, double* gfs_u, double* gfs_v, double* gfs_dpdt,
+                          double* gfs_q, double* gfs_oz, double* gfs_cld, double* gfs_t) {
+  double* const g[10] = {FIM_GFS10};
+  return cpl_dyn_to_phy_impl<float>(c, its, callphy, pr3d, us3d, vs3d, ws3d, tr3d, g);
+}
+#undef FIM_GFS10
+int fim_cpl_phy_to_dyn_r8(fim_ctx* c, int its, int callphy, int addtend, int smoothtend, double dtp,
+                          const double* gfs_p, const double* gfs_u, const double* gfs_v, const double* gfs_q,
+                          const double* gfs_cld, const double* gfs_oz, const double* gfs_t, const double* geshem,
+                          const double* rainc, const double* evap, const double* dp3d, double* us3d,
+                          double* vs3d, double* tr3d, double* rn2d, double* rc2d, double* qf2d) {
+  const double* const g[7] = {gfs_p, gfs_u, gfs_v, gfs_q, gfs_cld, gfs_oz, gfs_t};
+  const double* const col[3] = {geshem, rainc, evap};
+  return cpl_phy_to_dyn_impl<double>(c, its, callphy, addtend, smoothtend, dtp, g, col, dp3d, us3d, vs3d, tr3d,
+                                     rn2d, rc2d, qf2d);
+}
+int fim_cpl_phy_to_dyn_r4(fim_ctx* c, int its, int callphy, int addtend, int smoothtend, double dtp,
+                          const double* gfs_p, const double* gfs_u, const double* gfs_v, const double* gfs_q,
+                          const double* gfs_cld, const double* gfs_oz, const double* gfs_t, const double* geshem,
+                          const double* rainc, const double* evap, const float* dp3d, float* us3d, float* vs3d,
+                          float* tr3d, float* rn2d, float* rc2d, float* qf2d) {
+  const double* const g[7] = {gfs_p, gfs_u, gfs_v, gfs_q, gfs_cld, gfs_oz, gfs_t};
+  const double* const col[3] = {geshem, rainc, evap};
+  return cpl_phy_to_dyn_impl<float>(c, its, callphy, addtend, smoothtend, dtp, g, col, dp3d, us3d, vs3d, tr3d,
+                                    rn2d, rc2d, qf2d);
 }
 
 int fim_globsum_r8(fim_ctx* c, int its, const double* dp3d, const double* tr, const double* rn2d, const double* rc2d,

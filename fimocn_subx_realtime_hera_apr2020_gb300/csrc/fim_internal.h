@@ -391,6 +391,17 @@ void launch_globsum(const Launch&, const Grid<R>&, const Strides&, int ntr, cons
                     const R* rn2d, const R* rc2d, const R* pr3d, const R* ex3d, const R* qf2d,
                     double* partial, double* sums);
 size_t globsum_partials(int N, int L, int T, int members);
+// physics coupling (fim_cpl.cu); GFS arrays (nip, nvl), cell fastest, FP64
+// gfs = ps, dp, p, u, v, dpdt, q, oz, cld, t; old6 = u, v, t, q, oz, cld
+template <typename R>
+void launch_cpl_dyn_to_phy(const Launch&, const Grid<R>&, const R* pr3d, const R* us3d, const R* vs3d,
+                           const R* ws3d, const R* tr3d, double* const gfs[10], double* old6);
+// gfs7 = p, u, v, q, cld, oz, t; col3 = geshem, rainc, evap; tend: 12 N L
+// doubles of scratch with addtend (6 N L without smoothtend)
+template <typename R>
+void launch_cpl_phy_to_dyn(const Launch&, const Grid<R>&, double dt, double dtp, bool addtend, bool smoothtend,
+                           const double* const gfs7[7], const double* old6, const double* const col3[3],
+                           const R* dp3d, R* us3d, R* vs3d, R* tr3d, R* rn2d, R* rc2d, R* qf2d, double* tend);
 template <typename R>
 void launch_prdp_from_ex(const Launch&, const Grid<R>&, const Strides&, const R* ex3d, R* pr3d, R* dp3d);
 void launch_step_begin(const Launch&, StepParams* sp);  // advances every active member

@@ -165,6 +165,21 @@ class Dycore:
     def hystat(self, its, ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy):
         self._call("fim_hystat", its, *map(_ptr, (ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy)))
 
+    # physics coupling (cpl_run.F90): GFS arrays are float64 (nip, nvl), cell fastest
+    GFS_NAMES = ("ps", "dp", "p", "u", "v", "dpdt", "q", "oz", "cld", "t")
+
+    def cpl_dyn_to_phy(self, its, pr3d, us3d, vs3d, ws3d, tr3d, gfs, callphy=True):
+        """cpl_dyn_to_phy: fills gfs[name] for the GFS_NAMES (ps: nip values)."""
+        self._call("fim_cpl_dyn_to_phy", its, int(callphy), *map(_ptr, (pr3d, us3d, vs3d, ws3d, tr3d)),
+                   *[_ptr(gfs[n]) for n in self.GFS_NAMES])
+
+    def cpl_phy_to_dyn(self, its, gfs, geshem, rainc, evap, dp3d, us3d, vs3d, tr3d, rn2d, rc2d, qf2d, dtp,
+                       addtend=False, smoothtend=False, callphy=True):
+        """cpl_phy_to_dyn: the dynamics state and the rain / evaporation columns."""
+        self._call("fim_cpl_phy_to_dyn", its, int(callphy), int(addtend), int(smoothtend), ctypes.c_double(dtp),
+                   *[_ptr(gfs[n]) for n in ("p", "u", "v", "q", "cld", "oz", "t")],
+                   *map(_ptr, (geshem, rainc, evap, dp3d, us3d, vs3d, tr3d, rn2d, rc2d, qf2d)))
+
     def transp0(self, its, cumufx, dp3d, dpinit):
         self._call("fim_transp0", its, *map(_ptr, (cumufx, dp3d, dpinit)))
 

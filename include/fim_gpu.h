@@ -226,6 +226,38 @@ int fim_hystat_r8(fim_ctx *ctx, int its, double *ph3d, const double *ex3d, doubl
 int fim_hystat_r4(fim_ctx *ctx, int its, float *ph3d, const float *ex3d, float *mp3d,
                   const float *dp3d, float *tr3d, float *trdp, float *psrf, float *ptdcy);
 
+/* Physics coupling, the dynamics side of phy_run (FIMsrc/fim/horizontal/cpl_run.F90,
+ * cpl_dyn_to_phy :128-208 and cpl_phy_to_dyn :210-380, called from run.F90:325-331).
+ * The GFS physics arrays are double (kind_evod) in both families, (nip, nvl)
+ * with the cell index fastest; gfs_ps is (nip).  callphy = 0 does nothing, as
+ * in the reference.  cpl_dyn_to_phy also keeps, in the context, the six
+ * gfs_*_old copies (u, v, t, q, oz, cld) that cpl_phy_to_dyn's tendency
+ * method (addtend) uses; addtend without a preceding cpl_dyn_to_phy is
+ * FIM_EINVAL.  smoothtend applies dffusn8_lyr (dffusn.F90:110-129) to the
+ * tendencies with length dt*20, dt the context's time step; dtp is the
+ * physics time step.  Of cpl_phy_to_dyn's surface outputs only the columns
+ * globsum reads are formed: rn2d += max(0,geshem)*1000,
+ * rc2d += max(0,rainc)*1000, qf2d = -evap; the others are plain copies of
+ * physics fields that a host driver makes. */
+int fim_cpl_dyn_to_phy_r8(fim_ctx *ctx, int its, int callphy, const double *pr3d, const double *us3d,
+                          const double *vs3d, const double *ws3d, const double *tr3d, double *gfs_ps,
+                          double *gfs_dp, double *gfs_p, double *gfs_u, double *gfs_v, double *gfs_dpdt,
+                          double *gfs_q, double *gfs_oz, double *gfs_cld, double *gfs_t);
+int fim_cpl_dyn_to_phy_r4(fim_ctx *ctx, int its, int callphy, const float *pr3d, const float *us3d,
+                          const float *vs3d, const float *ws3d, const float *tr3d, double *gfs_ps,
+                          double *gfs_dp, double *gfs_p, double *gfs_u, double *gfs_v, double *gfs_dpdt,
+                          double *gfs_q, double *gfs_oz, double *gfs_cld, double *gfs_t);
+int fim_cpl_phy_to_dyn_r8(fim_ctx *ctx, int its, int callphy, int addtend, int smoothtend, double dtp,
+                          const double *gfs_p, const double *gfs_u, const double *gfs_v, const double *gfs_q,
+                          const double *gfs_cld, const double *gfs_oz, const double *gfs_t,
+                          const double *geshem, const double *rainc, const double *evap, const double *dp3d,
+                          double *us3d, double *vs3d, double *tr3d, double *rn2d, double *rc2d, double *qf2d);
+int fim_cpl_phy_to_dyn_r4(fim_ctx *ctx, int its, int callphy, int addtend, int smoothtend, double dtp,
+                          const double *gfs_p, const double *gfs_u, const double *gfs_v, const double *gfs_q,
+                          const double *gfs_cld, const double *gfs_oz, const double *gfs_t,
+                          const double *geshem, const double *rainc, const double *evap, const float *dp3d,
+                          float *us3d, float *vs3d, float *tr3d, float *rn2d, float *rc2d, float *qf2d);
+
 /* Class-B tracer transport (module_transp3d, FIMsrc/fim/horizontal/transp3d.F90).
  * transp0 (transp3d.F90:21): cumufx = 0, dpinit = dp3d.
  * transp1 (transp3d.F90:43): cumufx += adbash1..3 x massfx(nf,of,vof), with the

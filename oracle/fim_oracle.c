@@ -1435,3 +1435,123 @@ void orc_transp2(const orc_ctx *c, int ntrb, double *tracr, const double *cumufx
   fct3d(c, tracr, c->ntra, c->ntra + ntrb - 1, cumufx, w, dpinit, dpfinl);
   free(w);
 }
+
+/* ---- physics coupling (cpl_run.F90), the dynamics side of phy_run ------
+ * GFS arrays are (nip, nvl) with the cell index fastest: g[k*nip + i].
+ * old6 holds the six fields cpl_dyn_to_phy keeps for the tendency method
+ * (gfs_u_old, gfs_v_old, gfs_t_old, gfs_q_old, gfs_oz_old, gfs_cld_old) in
+ * the same layout, one nvl*nip block each. */
+#define G2(i, k) ((size_t)(k) * N + (i))
+
+/* cpl_dyn_to_phy, callphy branch (cpl_run.F90:128-208) */
+void orc_cpl_dyn_to_phy(const orc_ctx *c, const double *pr3d, const double *us3d, const double *vs3d,
+                        const double *ws3d, const double *tr3d, double *gfs_ps, double *gfs_dp,
+                        double *gfs_p, double *gfs_u, double *gfs_v, double *gfs_dpdt, double *gfs_q,
+                        double *gfs_oz, double *gfs_cld, double *gfs_t, double *old6) {
+  const int N = c->nip, L = c->nvl;
+  const size_t NL = (size_t)N * L;
+  const double rocp1 = RD / CP + 1., rocpr = CP / RD;
+#pragma omp parallel for schedule(static)
+  for (int ipn = 0; ipn < N; ipn++) {
+    gfs_ps[ipn] = 0.001 * pr3d[I2(0, ipn)];
+    for (int k = 0; k < L; k++) {
+      const double pk = pr3d[I2(k, ipn)], pk1 = pr3d[I2(k + 1, ipn)];
+      const double q2 = dmax(QVMIN, tr3d[T3(k, ipn, 1)]);
+      const size_t g = G2(ipn, k);
+      gfs_dp[g] = (0.001 * pk) - (0.001 * pk1);
+      gfs_p[g] = pow((pow(pk, rocp1) - pow(pk1, rocp1)) / ((pk - pk1) * rocp1), rocpr);
+      gfs_u[g] = us3d[C2(k, ipn)];
+      gfs_v[g] = vs3d[C2(k, ipn)];
+      gfs_dpdt[g] = 0.001 * ws3d[C2(k, ipn)];
+      gfs_q[g] = q2;
+      gfs_oz[g] = tr3d[T3(k, ipn, 3)];
+      gfs_cld[g] = tr3d[T3(k, ipn, 2)];
+      const double theta_nv = tr3d[T3(k, ipn, 0)] / (1. + 0.6078 * dmax(QVMIN, q2));
+      gfs_t[g] = theta_nv * pow(gfs_p[g] / P1000, RD / CP);
+      old6[0 * NL + g] = gfs_u[g];
+      old6[1 * NL + g] = gfs_v[g];
+      old6[2 * NL + g] = gfs_t[g];
+      old6[3 * NL + g] = gfs_q[g];
+      old6[4 * NL + g] = gfs_oz[g];
+      old6[5 * NL + g] = gfs_cld[g];
+    }
+  }
+}
+
+/* dffusn8_lyr (dffusn.F90:110-129 with dffusn_lyr.exe) on a (nvl, nip) field */
+static void dffusn8_lyr(const orc_ctx *c, double *fld, const double *delp, double dfflen) {
+  const int N = c->nip, L = c->nvl;
+  const double thshld = 1.e-11;
+  double *flxdv = malloc(sizeof(double) * (size_t)N * L);
+#pragma omp parallel for schedule(static)
+  for (int ipn = 0; ipn < N; ipn++) {
+    for (int k = 0; k < L; k++) flxdv[C2(k, ipn)] = 0.;
+    for (int edg = 0; edg < c->nprox[ipn]; edg++) {
+      const int ipx = c->prox[ipn * 6 + edg];
+      for (int k = 0; k < L; k++) {
+        const double a = dmax(delp[C2(k, ipn)], thshld), b = dmax(delp[C2(k, ipx)], thshld);
+        flxdv[C2(k, ipn)] = flxdv[C2(k, ipn)] + (fld[C2(k, ipn)] - fld[C2(k, ipx)]) *
+                                                    c->sideln[ipn * 6 + edg] * 2. * (a * b / (a + b));
+      }
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (int ipn = 0; ipn < N; ipn++)
+    for (int k = 0; k < L; k++) {
+      const double factor = -dfflen * c->rarea[ipn] / dmax(delp[C2(k, ipn)], thshld);
+      fld[C2(k, ipn)] = fld[C2(k, ipn)] + flxdv[C2(k, ipn)] * factor;
+    }
+  free(flxdv);
+}
+
+/* cpl_phy_to_dyn, callphy branch (cpl_run.F90:290-380): the 3-D state and
+ * the precipitation / evaporation columns that globsum reads */
+void orc_cpl_phy_to_dyn(const orc_ctx *c, int addtend, int smoothtend, double dtp, const double *gfs_p,
+                        const double *gfs_u, const double *gfs_v, const double *gfs_q, const double *gfs_cld,
+                        const double *gfs_oz, const double *gfs_t, const double *old6, const double *dp3d,
+                        double *us3d, double *vs3d, double *tr3d, const double *geshem, const double *rainc,
+                        const double *evap, double *rn2d, double *rc2d, double *qf2d) {
+  const int N = c->nip, L = c->nvl;
+  const size_t NL = (size_t)N * L;
+  const double dt = c->dt, kap = RD / CP;
+  double *tdc = NULL; /* u, v, t, q, cld, oz tendencies, (nvl, nip) each */
+  if (addtend) {
+    tdc = malloc(sizeof(double) * 6 * NL);
+    const double *now[6] = {gfs_u, gfs_v, gfs_t, gfs_q, gfs_cld, gfs_oz};
+    const int oi[6] = {0, 1, 2, 3, 5, 4};
+#pragma omp parallel for schedule(static)
+    for (int ipn = 0; ipn < N; ipn++)
+      for (int k = 0; k < L; k++)
+        for (int f = 0; f < 6; f++)
+          tdc[f * NL + C2(k, ipn)] = (now[f][G2(ipn, k)] - old6[oi[f] * NL + G2(ipn, k)]) / dtp;
+    if (smoothtend)
+      for (int f = 0; f < 6; f++) dffusn8_lyr(c, tdc + f * NL, dp3d, dt * 20.);
+  }
+#pragma omp parallel for schedule(static)
+  for (int ipn = 0; ipn < N; ipn++) {
+    for (int k = 0; k < L; k++) {
+      const size_t g = G2(ipn, k), d = C2(k, ipn);
+      if (addtend) {
+        us3d[d] = old6[0 * NL + g] + tdc[0 * NL + d] * dt;
+        vs3d[d] = old6[1 * NL + g] + tdc[1 * NL + d] * dt;
+        tr3d[T3(k, ipn, 0)] = (old6[2 * NL + g] + tdc[2 * NL + d] * dt) * pow(P1000 / gfs_p[g], kap) *
+                              (1. + 0.6078 * dmax(QVMIN, (old6[3 * NL + g] + tdc[3 * NL + d] * dt)));
+        tr3d[T3(k, ipn, 1)] = dmax(QVMIN, (old6[3 * NL + g] + tdc[3 * NL + d] * dt));
+        tr3d[T3(k, ipn, 2)] = dmax(QWMIN, (old6[5 * NL + g] + tdc[4 * NL + d] * dt));
+        tr3d[T3(k, ipn, 3)] = dmax(QVMIN, (old6[4 * NL + g] + tdc[5 * NL + d] * dt));
+      } else {
+        us3d[d] = gfs_u[g];
+        vs3d[d] = gfs_v[g];
+        tr3d[T3(k, ipn, 0)] = gfs_t[g] * pow(P1000 / gfs_p[g], kap) * (1. + 0.6078 * dmax(QVMIN, gfs_q[g]));
+        tr3d[T3(k, ipn, 1)] = dmax(QVMIN, gfs_q[g]);
+        tr3d[T3(k, ipn, 2)] = dmax(QWMIN, gfs_cld[g]);
+        tr3d[T3(k, ipn, 3)] = dmax(QVMIN, gfs_oz[g]);
+      }
+    }
+    rn2d[ipn] = rn2d[ipn] + dmax(0., geshem[ipn]) * 1000.;
+    rc2d[ipn] = rc2d[ipn] + dmax(0., rainc[ipn]) * 1000.;
+    qf2d[ipn] = -evap[ipn];
+  }
+  free(tdc);
+}
+#undef G2

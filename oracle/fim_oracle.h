@@ -86,6 +86,18 @@ void orc_transp0(const orc_ctx *c, double *cumufx, const double *dp3d, double *d
 void orc_transp1(const orc_ctx *c, double *cumufx, const double *massfx);
 void orc_transp2(const orc_ctx *c, int ntrb, double *tracr, const double *cumufx, const double *dpinit,
                  const double *dpfinl);
+/* physics coupling, the dynamics side (cpl_run.F90:128-208, 290-380; dffusn.F90:110-129):
+ * GFS arrays (nip, nvl) with the cell index fastest; old6 = the six fields
+ * cpl_dyn_to_phy keeps (u, v, t, q, oz, cld), one nvl*nip block each */
+void orc_cpl_dyn_to_phy(const orc_ctx *c, const double *pr3d, const double *us3d, const double *vs3d,
+                        const double *ws3d, const double *tr3d, double *gfs_ps, double *gfs_dp,
+                        double *gfs_p, double *gfs_u, double *gfs_v, double *gfs_dpdt, double *gfs_q,
+                        double *gfs_oz, double *gfs_cld, double *gfs_t, double *old6);
+void orc_cpl_phy_to_dyn(const orc_ctx *c, int addtend, int smoothtend, double dtp, const double *gfs_p,
+                        const double *gfs_u, const double *gfs_v, const double *gfs_q, const double *gfs_cld,
+                        const double *gfs_oz, const double *gfs_t, const double *old6, const double *dp3d,
+                        double *us3d, double *vs3d, double *tr3d, const double *geshem, const double *rainc,
+                        const double *evap, double *rn2d, double *rc2d, double *qf2d);
 /* pressure and thickness from Exner after the start-up hybgen (dyn_init.F90:895-906) */
 void orc_prdp_from_ex(const orc_ctx *c, const double *ex3d, double *pr3d, double *dp3d);
 

@@ -65,6 +65,8 @@ def load():
             "orc_transp0": [P] * 4,
             "orc_transp1": [P] * 3,
             "orc_transp2": [P, I, P, P, P, P],
+            "orc_cpl_dyn_to_phy": [P] * 17,
+            "orc_cpl_phy_to_dyn": [P, I, I, D] + [P] * 18,
         }
         for name, args in sigs.items():
             fn = getattr(lib, name)
@@ -178,6 +180,25 @@ class Oracle:
 
     def transp2(self, tracr, cumufx, dpinit, dpfinl):
         self.lib.orc_transp2(ctypes.byref(self.c), self.TB, _p(tracr), _p(cumufx), _p(dpinit), _p(dpfinl))
+
+    # ---- physics coupling (cpl_run.F90), GFS arrays (nip, nvl), cell fastest ----
+    GFS_NAMES = ["ps", "dp", "p", "u", "v", "dpdt", "q", "oz", "cld", "t"]
+
+    def cpl_dyn_to_phy(self, pr3d, us3d, vs3d, ws3d, tr3d):
+        """cpl_dyn_to_phy (callphy): returns (gfs dict, old6)."""
+        NL = self.N * self.L
+        gfs = {n: np.zeros(self.N if n == "ps" else NL) for n in self.GFS_NAMES}
+        old6 = np.zeros(6 * NL)
+        self.lib.orc_cpl_dyn_to_phy(ctypes.byref(self.c), *map(_p, (pr3d, us3d, vs3d, ws3d, tr3d)),
+                                    *[_p(gfs[n]) for n in self.GFS_NAMES], _p(old6))
+        return gfs, old6
+
+    def cpl_phy_to_dyn(self, gfs, old6, dp3d, us3d, vs3d, tr3d, geshem, rainc, evap, rn2d, rc2d, qf2d,
+                       dtp, addtend=False, smoothtend=False):
+        """cpl_phy_to_dyn (callphy): updates us3d, vs3d, tr3d[0:4], rn2d, rc2d, qf2d in place."""
+        self.lib.orc_cpl_phy_to_dyn(ctypes.byref(self.c), int(addtend), int(smoothtend), float(dtp),
+                                    *[_p(gfs[n]) for n in ("p", "u", "v", "q", "cld", "oz", "t")], _p(old6),
+                                    *map(_p, (dp3d, us3d, vs3d, tr3d, geshem, rainc, evap, rn2d, rc2d, qf2d)))
 
     def prdp_from_ex(self, ex3d, pr3d, dp3d):
         self.lib.orc_prdp_from_ex(ctypes.byref(self.c), _p(ex3d), _p(pr3d), _p(dp3d))
