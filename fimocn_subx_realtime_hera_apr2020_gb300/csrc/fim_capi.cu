@@ -587,7 +587,7 @@ int hystat_impl(fim_ctx* c, int its, R* ph3d, const R* ex3d, R* mp3d, const R* d
   return s.finish();
 }
 
-// cpl_run.F90:79-208 (callphy branch of cpl_dyn_to_phy)
+// cpl_run.F90:151-263 (callphy branch of cpl_dyn_to_phy)
 template <typename R>
 int cpl_dyn_to_phy_impl(fim_ctx* c, int its, int callphy, const R* pr3d, const R* us3d, const R* vs3d,
                         const R* ws3d, const R* tr3d, double* const gfs_in[10]) {
@@ -614,7 +614,7 @@ int cpl_dyn_to_phy_impl(fim_ctx* c, int its, int callphy, const R* pr3d, const R
   return s.finish();
 }
 
-// cpl_run.F90:210-380 (callphy branch of cpl_phy_to_dyn): the dynamics state
+// cpl_run.F90:266-536 (callphy branch of cpl_phy_to_dyn): the dynamics state
 // and the precipitation / evaporation columns
 template <typename R>
 int cpl_phy_to_dyn_impl(fim_ctx* c, int its, int callphy, int addtend, int smoothtend, double dtp,

@@ -1,4 +1,4 @@
-// Physics coupling, the dynamics side of phy_run (cpl_run.F90:79-380 with
+// Physics coupling, the dynamics side of phy_run (cpl_run.F90:35-536 with
 // dffusn8_lyr, dffusn.F90:110-129): the conversion of the dynamics state
 // (level fastest) into the GFS physics state (nip, nvl; cell fastest, FP64 as
 // the reference's kind_evod arrays) and back.
@@ -23,7 +23,7 @@ namespace fim {
 constexpr int kCplTile = 32;
 constexpr int kCplRows = 8;
 
-// p^kappa layer mean of the FP64 build, cpl_run.F90:150-151 as written
+// p^kappa layer mean of the FP64 build, cpl_run.F90:236-237 as written
 __device__ __forceinline__ double phillips(double pk, double pk1) {
   const double rocp1 = kRd / kCp + 1., rocpr = kCp / kRd;
   return pow((pow(pk, rocp1) - pow(pk1, rocp1)) / ((pk - pk1) * rocp1), rocpr);
@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(kCplTile * kCplRows) k_cpl_d2p(int N, int L, c
   }
 }
 
-// physics tendencies of u, v, t, q, cld, oz (cpl_run.F90:310-319), level
+// physics tendencies of u, v, t, q, cld, oz (cpl_run.F90:414-425), level
 // fastest: tend[f][i*L + k]
 __global__ void __launch_bounds__(kCplTile * kCplRows) k_cpl_tend(int N, int L, double dtp,
     const double* __restrict__ gfs_u, const double* __restrict__ gfs_v, const double* __restrict__ gfs_t,
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(256) k_cpl_dffusn(Grid<R> g, double dfflen, co
   out[c] = f + flxdv * (-dfflen * (double)g.rarea[i] / a);
 }
 
-// cpl_phy_to_dyn (cpl_run.F90:336-371): the new dynamics state; tend is null
+// cpl_phy_to_dyn (cpl_run.F90:453-480): the new dynamics state; tend is null
 // without addtend
 template <typename R>
 __global__ void __launch_bounds__(kCplTile * kCplRows) k_cpl_p2d(int N, int L, double dt,

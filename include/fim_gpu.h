@@ -227,7 +227,7 @@ int fim_hystat_r4(fim_ctx *ctx, int its, float *ph3d, const float *ex3d, float *
                   const float *dp3d, float *tr3d, float *trdp, float *psrf, float *ptdcy);
 
 /* Physics coupling, the dynamics side of phy_run (FIMsrc/fim/horizontal/cpl_run.F90,
- * cpl_dyn_to_phy :128-208 and cpl_phy_to_dyn :210-380, called from run.F90:325-331).
+ * cpl_dyn_to_phy :151-263 and cpl_phy_to_dyn :266-536, called from run.F90:325-331).
  * The GFS physics arrays are double (kind_evod) in both families, (nip, nvl)
  * with the cell index fastest; gfs_ps is (nip).  callphy = 0 does nothing, as
  * in the reference.  cpl_dyn_to_phy also keeps, in the context, the six

@@ -1443,7 +1443,7 @@ void orc_transp2(const orc_ctx *c, int ntrb, double *tracr, const double *cumufx
  * the same layout, one nvl*nip block each. */
 #define G2(i, k) ((size_t)(k) * N + (i))
 
-/* cpl_dyn_to_phy, callphy branch (cpl_run.F90:128-208) */
+/* cpl_dyn_to_phy, callphy branch (cpl_run.F90:203-260) */
 void orc_cpl_dyn_to_phy(const orc_ctx *c, const double *pr3d, const double *us3d, const double *vs3d,
                         const double *ws3d, const double *tr3d, double *gfs_ps, double *gfs_dp,
                         double *gfs_p, double *gfs_u, double *gfs_v, double *gfs_dpdt, double *gfs_q,
@@ -1504,7 +1504,7 @@ static void dffusn8_lyr(const orc_ctx *c, double *fld, const double *delp, doubl
   free(flxdv);
 }
 
-/* cpl_phy_to_dyn, callphy branch (cpl_run.F90:290-380): the 3-D state and
+/* cpl_phy_to_dyn, callphy branch (cpl_run.F90:407-490): the 3-D state and
  * the precipitation / evaporation columns that globsum reads */
 void orc_cpl_phy_to_dyn(const orc_ctx *c, int addtend, int smoothtend, double dtp, const double *gfs_p,
                         const double *gfs_u, const double *gfs_v, const double *gfs_q, const double *gfs_cld,

@@ -86,7 +86,7 @@ void orc_transp0(const orc_ctx *c, double *cumufx, const double *dp3d, double *d
 void orc_transp1(const orc_ctx *c, double *cumufx, const double *massfx);
 void orc_transp2(const orc_ctx *c, int ntrb, double *tracr, const double *cumufx, const double *dpinit,
                  const double *dpfinl);
-/* physics coupling, the dynamics side (cpl_run.F90:128-208, 290-380; dffusn.F90:110-129):
+/* physics coupling, the dynamics side (cpl_run.F90:151-263, 266-536; dffusn.F90:110-129):
  * GFS arrays (nip, nvl) with the cell index fastest; old6 = the six fields
  * cpl_dyn_to_phy keeps (u, v, t, q, oz, cld), one nvl*nip block each */
 void orc_cpl_dyn_to_phy(const orc_ctx *c, const double *pr3d, const double *us3d, const double *vs3d,

@@ -1,6 +1,6 @@
 """Physics coupling (cpl_run.F90), the dynamics side of phy_run: the C oracle
 against a vectorised NumPy restatement of cpl_dyn_to_phy / cpl_phy_to_dyn
-(cpl_run.F90:128-208, 290-380) and dffusn8_lyr (dffusn.F90:110-129), and the
+(cpl_run.F90:151-263, 266-536) and dffusn8_lyr (dffusn.F90:110-129), and the
 dyn -> phy -> dyn round trip with the physics leaving its state unchanged."""
 import numpy as np
 import pytest
