@@ -23,13 +23,14 @@ constexpr int kBlock2 = 256;
 inline unsigned nblocks(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
 // ---------------------------------------------------------------- hybgen --
-// restp_1d (hybgen.F90:792-890)
+// restp_1d (hybgen.F90:792-890).  The running minimum oldth is formed in
+// place in thold (the caller's column, not read again), so the column set-up
+// holds one work array less in local memory.
 template <typename R, int ML>
-__device__ void restp_1d(const R* thold, const R* pkold, int kold, R* thnew, R* pknew, const R* targt,
+__device__ void restp_1d(R* thold, const R* pkold, int kold, R* thnew, R* pknew, const R* targt,
                          int knew, int* bad) {
-  R oldth[ML];
-  oldth[kold - 1] = thold[kold - 1];
-  for (int k = kold; k >= 2; k--) oldth[k - 2] = cmin(oldth[k - 1], thold[k - 2]);
+  R* oldth = thold;
+  for (int k = kold; k >= 2; k--) oldth[k - 2] = cmin(oldth[k - 1], oldth[k - 2]);
   for (int k = 0; k < knew; k++) thnew[k] = targt[k];
   thnew[0] = cmin(cmin(oldth[0], oldth[kold - 1]), targt[0]);
   thnew[knew - 1] = cmax(cmax(oldth[0], oldth[kold - 1]), targt[knew - 1]);
@@ -149,11 +150,13 @@ __device__ void regrid_1d(const Knobs& kn, const R* targt, const R* dpsig, int L
                           R prcol0, int* bad) {
   const R thin = R(kRd) / R(kP1000), tolrnce = R(0.001), dffudt = R(.1);
   const R eqlb_slak = R(.1) * R(its) / (R(10) + R(its));
-  R exwrk[ML + 1], exnew[ML + 1], thnew[ML], heatfx[ML];
+  // two local work arrays: the column's own excol serves as exwrk, thcol as
+  // restp_1d's oldth, and the heat fluxes are formed as the update runs
+  R exnew[ML + 1], thnew[ML];
   for (int k = 0; k < L; k++)
     if (excol[k] < excol[k + 1] - thin) excol[k + 1] = excol[k];
   for (int k = L - 2; k >= 0; k--) thcol[k] = cmin(thcol[k], thcol[k + 1]);
-  for (int k = 0; k <= L; k++) exwrk[k] = excol[k];
+  R* exwrk = excol;
   const R tt = targt[L - 1];
   for (int k = L; k >= 2; k--) {
     if (thcol[k - 1] <= tt + tolrnce) break;
@@ -172,21 +175,25 @@ __device__ void regrid_1d(const Knobs& kn, const R* targt, const R* dpsig, int L
     }
   }
   restp_1d<R, ML>(thcol, exwrk, L, thnew, exnew, targt, L, bad);
-  heatfx[L - 1] = R(0);
-  heatfx[0] = R(0);
   const R grv = R(kGrvity);
+  // heatfx(j) of hybgen.F90's heat diffusion, from the work copy only (zero
+  // at j = 0 and nvl-1)
+  auto heatfx = [&](int j) -> R {
+    R h = R(0);
+    if (j >= 1 && j <= L - 2 && exwrk[j] < exwrk[0] - R(.01) && exwrk[j + 1] > exwrk[L] + R(.01)) {
+      const R cnv = grv / targt[j];
+      h = dffudt * cnv * cnv * R(.5) * (targt[j + 1] - targt[j - 1]) / cmax(R(.03) * cnv, exwrk[j] - exwrk[j + 1]);
+    }
+    return h;
+  };
   for (int iter = 1; iter <= 3; iter++) {
     for (int k = 0; k <= L; k++) exwrk[k] = exnew[k];
-    for (int k = 2; k <= L - 1; k++) {
-      heatfx[k - 1] = R(0);
-      if (exwrk[k - 1] < exwrk[0] - R(.01) && exwrk[k] > exwrk[L] + R(.01)) {
-        const R cnv = grv / targt[k - 1];
-        heatfx[k - 1] = dffudt * cnv * cnv * R(.5) * (targt[k] - targt[k - 2]) / cmax(R(.03) * cnv, exwrk[k - 1] - exwrk[k]);
-      }
-    }
+    R hprev = R(0);  // heatfx(k - 1)
     for (int k = 1; k <= L - 1; k++) {
+      const R hcur = heatfx(k);
       if (exwrk[k] < exwrk[0] - R(.01) && exwrk[k] > exwrk[L] + R(.01))
-        exnew[k] = cmax(exwrk[k + 1], cmin(exwrk[k - 1], exwrk[k] + (heatfx[k] - heatfx[k - 1]) / (targt[k] - targt[k - 1])));
+        exnew[k] = cmax(exwrk[k + 1], cmin(exwrk[k - 1], exwrk[k] + (hcur - hprev) / (targt[k] - targt[k - 1])));
+      hprev = hcur;
     }
     bool event = false;
     for (int k = 2; k <= L + 1; k++)
