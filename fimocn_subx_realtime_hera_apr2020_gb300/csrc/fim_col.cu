@@ -24,16 +24,16 @@ inline unsigned nblocks(long long n, int b) { return (unsigned)((n + b - 1) / b)
 
 // ---------------------------------------------------------------- hybgen --
 // restp_1d (hybgen.F90:792-890).  The running minimum oldth is formed in
-// place in thold (the caller's column, not read again), so the column set-up
-// holds one work array less in local memory.
+// place in thold (the caller's column, not read again).  The new theta
+// column is targt except its two end layers (hybgen.F90:832-834), so it is
+// not stored: th0 and thL are its ends and tn(k) its layer k.
 template <typename R, int ML>
-__device__ void restp_1d(R* thold, const R* pkold, int kold, R* thnew, R* pknew, const R* targt,
-                         int knew, int* bad) {
+__device__ void restp_1d(R* thold, const R* pkold, int kold, R* pknew, const R* targt, int knew, int* bad) {
   R* oldth = thold;
   for (int k = kold; k >= 2; k--) oldth[k - 2] = cmin(oldth[k - 1], oldth[k - 2]);
-  for (int k = 0; k < knew; k++) thnew[k] = targt[k];
-  thnew[0] = cmin(cmin(oldth[0], oldth[kold - 1]), targt[0]);
-  thnew[knew - 1] = cmax(cmax(oldth[0], oldth[kold - 1]), targt[knew - 1]);
+  const R th0 = cmin(cmin(oldth[0], oldth[kold - 1]), targt[0]);
+  const R thL = cmax(cmax(oldth[0], oldth[kold - 1]), targt[knew - 1]);
+  auto tn = [&](int k) -> R { return k == 0 ? th0 : k == knew - 1 ? thL : targt[k]; };
   pknew[0] = pkold[0];
   pknew[knew] = pkold[kold];
   R colint = R(0), colscl = R(0), cloutt = R(0);
@@ -42,25 +42,28 @@ __device__ void restp_1d(R* thold, const R* pkold, int kold, R* thnew, R* pknew,
     colscl = colscl + cabs(oldth[k] * (pkold[k + 1] - pkold[k]));
   }
   int ko = 0;
+  R tk = th0;
   for (int k = 0; k < knew - 1; k++) {
-    R pinteg = R(0), tha, thb = thnew[k];
+    const R tk1 = tn(k + 1);
+    R pinteg = R(0), tha, thb = tk;
     for (;;) {
       tha = thb;
-      thb = cmin(thnew[k + 1], cmax(thnew[k], oldth[ko]));
+      thb = cmin(tk1, cmax(tk, oldth[ko]));
       pinteg = pinteg + pkold[ko] * (thb - tha);
-      if (oldth[ko] < thnew[k + 1]) {
+      if (oldth[ko] < tk1) {
         if (ko < kold - 1) { ko++; continue; }
         tha = thb;
-        thb = thnew[k + 1];
+        thb = tk1;
         pinteg = pinteg + pkold[kold] * (thb - tha);
       }
       break;
     }
     pknew[k + 1] = pknew[k];
-    if (thnew[k + 1] > thnew[k]) pknew[k + 1] = pinteg / (thnew[k + 1] - thnew[k]);
-    cloutt = cloutt + thnew[k] * (pknew[k + 1] - pknew[k]);
+    if (tk1 > tk) pknew[k + 1] = pinteg / (tk1 - tk);
+    cloutt = cloutt + tk * (pknew[k + 1] - pknew[k]);
+    tk = tk1;
   }
-  cloutt = cloutt + thnew[knew - 1] * (pknew[knew] - pknew[knew - 1]);
+  cloutt = cloutt + thL * (pknew[knew] - pknew[knew - 1]);
   if (sizeof(R) == 8 && cabs(cloutt - colint) > cmax(R(1.e-33), R(1.e-6) * colscl)) *bad = 1;
 }
 
@@ -150,9 +153,10 @@ __device__ void regrid_1d(const Knobs& kn, const R* targt, const R* dpsig, int L
                           R prcol0, int* bad) {
   const R thin = R(kRd) / R(kP1000), tolrnce = R(0.001), dffudt = R(.1);
   const R eqlb_slak = R(.1) * R(its) / (R(10) + R(its));
-  // two local work arrays: the column's own excol serves as exwrk, thcol as
-  // restp_1d's oldth, and the heat fluxes are formed as the update runs
-  R exnew[ML + 1], thnew[ML];
+  // one local work array: the column's own excol serves as exwrk, thcol as
+  // restp_1d's oldth, the new theta column is targt but for its ends (which
+  // equilb does not read), and the heat fluxes are formed as the update runs
+  R exnew[ML + 1];
   for (int k = 0; k < L; k++)
     if (excol[k] < excol[k + 1] - thin) excol[k + 1] = excol[k];
   for (int k = L - 2; k >= 0; k--) thcol[k] = cmin(thcol[k], thcol[k + 1]);
@@ -174,7 +178,7 @@ __device__ void regrid_1d(const Knobs& kn, const R* targt, const R* dpsig, int L
       break;
     }
   }
-  restp_1d<R, ML>(thcol, exwrk, L, thnew, exnew, targt, L, bad);
+  restp_1d<R, ML>(thcol, exwrk, L, exnew, targt, L, bad);
   const R grv = R(kGrvity);
   // heatfx(j) of hybgen.F90's heat diffusion, from the work copy only (zero
   // at j = 0 and nvl-1)
@@ -200,7 +204,7 @@ __device__ void regrid_1d(const Knobs& kn, const R* targt, const R* dpsig, int L
       if (exnew[k - 1] > exnew[k - 2] + thin) event = true;
     if (!event) break;
   }
-  equilb<R>(thnew, exnew, L, eqlb_slak);
+  equilb<R>(targt, exnew, L, eqlb_slak);  // reads layers 1..nvl-2 only
   inflate<R>(kn, dpsig, L, prcol0, exnew);
   for (int k = 0; k <= L; k++) excol[k] = exnew[k];
 }
