@@ -38,6 +38,9 @@ WORDS = {
     # the fused step averages only the layer thickness in edgvar3; the
     # tracers' edge values come from k_tr_own and are averaged in k_tr_lo/hi
     "k_edgvar1": lambda T: 41, "k_edgvar3_own": lambda T: 7, "k_edgvar3_avg": lambda T: 12,
+    # edgvar2 (hiOrderUVComp): speeds and gradient (u, v, 6+6 edge winds in,
+    # 3 out), then the correction (3 + 12 in, 18 out)
+    "k_edgvar2_grad": lambda T: 17, "k_edgvar2": lambda T: 33,
     "k_tr_own": lambda T: 7 * (T - 1), "k_tr_lo": lambda T: 15 * T + 7, "k_tr_lim": lambda T: 8 * T + 1,
     "k_tr_hi": lambda T: 16 * T + 7,
     "k_cnuity12": lambda T: 37, "k_cnuity3": lambda T: 8, "k_cnuity4": lambda T: 26, "k_cnuity5": lambda T: 14,
@@ -183,7 +186,8 @@ def gpu_arm(args, ws, rank, local):
     N, L, T = grid.nip, wl["nvl"], wl["ntra"]
     units = N * L * members  # cell-levels per step per GPU
     group = args.member_group if args.member_group >= 0 else wl.get("member_group", 0)
-    cfg = F.FimConfig(nvl=L, ntra=T, dt=wl["dt"], precision="f32", members=members, member_group=group)
+    cfg = F.FimConfig(nvl=L, ntra=T, dt=wl["dt"], precision="f32", members=members, member_group=group,
+                      hi_order_uv_comp=1 if args.hi_order_uv else 0)
     dyc, st = make_state(F, grid, cfg, wl, np.float32)
     for _ in range(args.warmup):
         st.step(use_graph=True)
@@ -315,7 +319,8 @@ def gpu_arm(args, ws, rank, local):
             "vs_baseline": None, "dtype": "f32 (float-float column sums, FP64 budget reductions)",
             "data": "synthetic seeded balanced state (no dataset: the reference's GFS initial state is not "
                     "in the tree)",
-            "config": {"workload": args.workload, "glvl": wl["glvl"], "nip": N, "nvl": L, "ntra": T,
+            "config": {"workload": args.workload + ("+edgvar2" if args.hi_order_uv else ""), "glvl": wl["glvl"],
+                       "nip": N, "nvl": L, "ntra": T,
                        "dt": wl["dt"], "members_per_gpu": members, "member_group": group or members,
                        "tracer_shape_autotuned": {"levels_per_thread": shape[0], "threads_per_block": shape[1],
                                                   "probe_ms": shape[2]},
@@ -612,6 +617,7 @@ def main():
     p.add_argument("--nvl", type=int, default=0)
     p.add_argument("--dt", type=float, default=0.0, help="time step of the accuracy run (default: workload's)")
     p.add_argument("--cpl", action="store_true", help="time the physics coupling on the workload's state")
+    p.add_argument("--hi-order-uv", action="store_true", help="the step with edgvar2 (hiOrderUVComp)")
     args = p.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -58,6 +58,7 @@ class FimConfig:
     ntrb: int = 0                   # class-B tracers (transported every dtratio steps by fct3d)
     dtratio: int = 6
     member_group: int = 0           # members advanced together through the dynamics (0: all)
+    hi_order_uv_comp: int = 0       # hiOrderUVComp: edgvar2 after edgvar1 in the step
     thetac: np.ndarray = field(default=None, repr=False)
     dpsig: np.ndarray = field(default=None, repr=False)
 

@@ -78,6 +78,7 @@ struct fim_ctx {
   void *cb_w = nullptr, *cb_F = nullptr, *cb_V = nullptr, *cb_fmx = nullptr, *cb_fmn = nullptr,
        *cb_flo = nullptr, *cb_flp = nullptr, *cb_fln = nullptr;
   void *du = nullptr, *dv = nullptr, *wu = nullptr, *wv = nullptr;
+  void* e2w = nullptr;  // edgvar2 in the step: speed and gradient, 3 nvl nip per member of a group
   void *exsmo = nullptr, *exsmo2 = nullptr;
   double* gs_partial = nullptr;
   double* cpl_old = nullptr;  // physics coupling: the six gfs_*_old copies (6 nvl nip)
@@ -172,6 +173,12 @@ int build_grid(fim_ctx* c, const fim_grid_desc* g, const std::vector<double>& ra
   { const R* t_; if ((rc = upload_conv<R>(c, corio.data(), (size_t)N, &t_))) return rc; G.corio = t_; }
   { const R* t_; if ((rc = upload_conv<R>(c, grnd.data(), (size_t)N, &t_))) return rc; G.grndspd = t_; }
   { const R* t_; if ((rc = upload_conv<R>(c, g->hfcoef, (size_t)N * 36, &t_))) return rc; G.hfcoef = t_; }
+  G.cxy = nullptr;
+  if (g->corner_xy) {
+    const R* t_;
+    if ((rc = upload_conv<R>(c, g->corner_xy, (size_t)N * 12, &t_))) return rc;
+    G.cxy = t_;
+  }
   { const double* t_; if ((rc = upload_conv<double>(c, g->area, (size_t)N, &t_))) return rc; G.area_d = t_; }
   {
     std::vector<double> sv((size_t)N * 2, 0.0);
@@ -300,6 +307,7 @@ int ensure_momtum(fim_ctx* c, int members) {
   int rc;
   if ((rc = ensure(c, &c->du, NL))) return rc;
   if ((rc = ensure(c, &c->dv, NL))) return rc;
+  if (c->cfg.hi_order_uv_comp && (rc = ensure(c, &c->e2w, 3 * NL))) return rc;
   if (c->kn.biharm) {
     if ((rc = ensure(c, &c->wu, NL))) return rc;
     if ((rc = ensure(c, &c->wv, NL))) return rc;
@@ -410,6 +418,8 @@ int edgvar_impl(fim_ctx* c, int which, const R* u_vel, const R* v_vel, const R* 
   const R* dpr = s.map(pres, NI, 0);
   const R* dmo = s.map(montg, NL, 0);
   const R* dtr = s.map(tracr, NL * c->T, 0);
+  if (which == 2 && !grid_of<R>(c).cxy)
+    return set_err(c, FIM_EINVAL, "edgvar2 needs the grid's corner_xy table");
   const int io = which == 1 ? 2 : 1;
   R* due = s.map(u_edg, NE, io);
   R* dve = s.map(v_edg, NE, io);
@@ -421,11 +431,18 @@ int edgvar_impl(fim_ctx* c, int which, const R* u_vel, const R* v_vel, const R* 
   if (s.rc) return s.rc;
   Launch l = make_launch(c, 1);
   Grid<R>& g = grid_of<R>(c);
-  if (which == 1)
+  if (which == 1) {
     launch_edgvar1<R>(l, g, c->str, c->kn.hi_order, du, dv, ddp, dpr, dmo, dtr, due, dve, dde, dle, dme, dqe, dte);
-  else
+  } else if (which == 2) {
+    R* w = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&w, 3 * NL * sizeof(R), c->stream);
+    if (e != cudaSuccess) { cudaGetLastError(); return set_err(c, FIM_ENOMEM, "edgvar2 scratch", e); }
+    s.bufs.push_back(w);
+    launch_edgvar2<R>(l, g, c->str, du, dv, due, dve, dqe, w);
+  } else {
     launch_edgvar3<R>(l, g, c->str, ddp, dtr, dde, dte, c->kn.hi_order ? c->T : 1);
-  if ((rc = check_launch(c, which == 1 ? "edgvar1" : "edgvar3"))) return rc;
+  }
+  if ((rc = check_launch(c, which == 1 ? "edgvar1" : which == 2 ? "edgvar2" : "edgvar3"))) return rc;
   return s.finish();
 }
 
@@ -789,6 +806,9 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
                       P(FIM_PR3D), P(FIM_MP3D), P(FIM_TR3D), P(FIM_U_EDG),
                       P(FIM_V_EDG), P(FIM_DP_EDG), P(FIM_LP_EDG), P(FIM_MONT_EDG),
                       P(FIM_UVSQ_EDG), P(FIM_TRC_EDG), mpf, (R*)st->thold);
+    if (c->cfg.hi_order_uv_comp)
+      launch_edgvar2<R>(lg, g, s, P(FIM_US3D), P(FIM_VS3D), P(FIM_U_EDG), P(FIM_V_EDG), P(FIM_UVSQ_EDG),
+                        (R*)c->e2w);
     if (c->kn.hi_order) {
       // own-side dp and tracer edge values; the two-sided averages are formed
       // where they are used (k_cnuity12 for dp; k_tr_lo/k_tr_hi for the
@@ -940,6 +960,7 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
   if (cfg->precision != FIM_PREC_F64 && cfg->precision != FIM_PREC_F32) return FIM_EINVAL;
   if (cfg->ntrb < 0 || cfg->ntra + cfg->ntrb > 32 || (cfg->ntrb > 0 && cfg->dtratio < 1)) return FIM_EINVAL;
   if (cfg->member_group < 0) return FIM_EINVAL;
+  if (cfg->hi_order_uv_comp && !g->corner_xy) return FIM_EINVAL;  // edgvar2 needs corner_xy
   if (!cfg->thetac || !cfg->dpsig || !g->prox || !g->proxs || !g->nprox || !g->area || !g->cs || !g->sn ||
       !g->sidevec_c || !g->sidevec_e || !g->sideln || !g->hfcoef || !g->lat)
     return FIM_EINVAL;
@@ -1120,6 +1141,16 @@ int fim_edgvar3_r8(EDGVAR_ARGS_R(double)) {
   (void)its; (void)exner; (void)geop; (void)geop_edg;
   return edgvar_impl<double>(c, 3, u_vel, v_vel, delp, pres, montg, tracr, u_edg, v_edg, dp_edg, lp_edg, mont_edg,
                              uvsq_edg, trc_edg);
+}
+int fim_edgvar2_r8(EDGVAR_ARGS_R(double)) {
+  (void)its; (void)exner; (void)geop; (void)geop_edg;
+  return edgvar_impl<double>(c, 2, u_vel, v_vel, delp, pres, montg, tracr, u_edg, v_edg, dp_edg, lp_edg, mont_edg,
+                             uvsq_edg, trc_edg);
+}
+int fim_edgvar2_r4(EDGVAR_ARGS_R(float)) {
+  (void)its; (void)exner; (void)geop; (void)geop_edg;
+  return edgvar_impl<float>(c, 2, u_vel, v_vel, delp, pres, montg, tracr, u_edg, v_edg, dp_edg, lp_edg, mont_edg,
+                            uvsq_edg, trc_edg);
 }
 int fim_edgvar3_r4(EDGVAR_ARGS_R(float)) {
   (void)its; (void)exner; (void)geop; (void)geop_edg;

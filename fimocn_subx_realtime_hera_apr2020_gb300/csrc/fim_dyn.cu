@@ -167,6 +167,91 @@ __global__ void __launch_bounds__(kBlock) k_edgvar1(Grid<R> g, Strides s, int hi
 }
 
 // --------------------------------------------------------------------------
+// edgvar2 (edgvar2.F90:24-319, hiOrderUVComp; the MORE_VARS block is compiled
+// out in the reference): the edge wind is rescaled to the mean of the speeds
+// at the edge's two corners seen from the three cells around each corner,
+// each a cell's speed plus its speed-gradient projected on the corner.
+//  k_edgvar2_grad: per cell-level the speed |u| and the gradient of the edge
+//                  speeds (gradient(), edgvar2.F90:231-258) -> w[0..2]
+//  k_edgvar2:      per cell-level and edge, the corner speeds of the cell, the
+//                  neighbour across the edge and the neighbours across the
+//                  adjacent edges, the ratio to |u_edg| (1 below 1e-5), and
+//                  uvsq_edg of the rescaled wind.
+template <typename R>
+__global__ void __launch_bounds__(kBlock) k_edgvar2_grad(Grid<R> g, Strides s, const R* __restrict__ u,
+    const R* __restrict__ v, const R* __restrict__ u_edg, const R* __restrict__ v_edg, R* __restrict__ w) {
+  int i, k;
+  if (!cell_levels<1>(g.N, g.L, i, k)) return;
+  const int L = g.L;
+  const size_t m = blockIdx.y, NL = (size_t)g.N * L;
+  u += m * s.cell; v += m * s.cell; u_edg += m * s.edge; v_edg += m * s.edge; w += m * 3 * NL;
+  const size_t c = (size_t)i * L + k;
+  const int np = g.nprox[i];
+  R g1 = R(0), g2 = R(0);
+  for (int e = 0; e < np; e++) {
+    const size_t o = ((size_t)i * 6 + e) * L + k;
+    const R sp = sqrt(u_edg[o] * u_edg[o] + v_edg[o] * v_edg[o]);
+    g1 = g1 + sp * g.svc[(i * 6 + e) * 2 + 1];
+    g2 = g2 - sp * g.svc[(i * 6 + e) * 2 + 0];
+  }
+  const R rar = g.rarea[i];
+  w[c] = sqrt(u[c] * u[c] + v[c] * v[c]);
+  w[NL + c] = g1 * rar;
+  w[2 * NL + c] = g2 * rar;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlock) k_edgvar2(Grid<R> g, Strides s, const R* __restrict__ w,
+    R* __restrict__ u_edg, R* __restrict__ v_edg, R* __restrict__ uvsq_edg) {
+  int i, k;
+  if (!cell_levels<1>(g.N, g.L, i, k)) return;
+  const int L = g.L;
+  const size_t m = blockIdx.y, NL = (size_t)g.N * L;
+  u_edg += m * s.edge; v_edg += m * s.edge; uvsq_edg += m * s.edge; w += m * 3 * NL;
+  const R divby6 = R(1) / R(6), eps = R(0.00001);
+  const int np = g.nprox[i];
+  // corner q of cell x: its speed plus 0.5 * (grad . corner_xy(q))
+  auto corner = [&](int x, int q) -> R {
+    const size_t cx = (size_t)x * L + k;
+    const R gc = R(0.5) * (w[NL + cx] * g.cxy[(x * 2 + 0) * 6 + q] + w[2 * NL + cx] * g.cxy[(x * 2 + 1) * 6 + q]);
+    return w[cx] + gc;
+  };
+  for (int e = 0; e < np; e++) {
+    const int nba = g.prox[i * 6 + e], nbaedg = g.proxs[i * 6 + e];
+    const int em1 = (e - 1 + np) % np, ep1 = (e + 1) % np;
+    const int nbm1 = g.prox[i * 6 + em1], nbp1 = g.prox[i * 6 + ep1];
+    const R uv1conr1 = corner(i, e);
+    const R uv2conr1 = corner(nba, (nbaedg + 1) % g.nprox[nba]);
+    const R uv3conr1 = corner(nbm1, g.proxs[i * 6 + em1]);
+    const R uv1conr2 = corner(i, ep1);
+    const R uv2conr2 = corner(nba, nbaedg);
+    const R uv3conr2 = corner(nbp1, (g.proxs[i * 6 + ep1] + 1) % g.nprox[nbp1]);
+    const size_t o = ((size_t)i * 6 + e) * L + k;
+    R ue = u_edg[o], ve = v_edg[o];
+    const R uvm1 = sqrt(ue * ue + ve * ve);
+    const R uvm2 = (uv1conr1 + uv2conr1 + uv3conr1 + uv1conr2 + uv2conr2 + uv3conr2) * divby6;
+    const R r_m = uvm1 < eps ? R(1) : uvm2 / uvm1;
+    ue = ue * r_m;
+    ve = ve * r_m;
+    u_edg[o] = ue;
+    v_edg[o] = ve;
+    uvsq_edg[o] = R(.5) * (ue * ue + ve * ve);
+  }
+}
+
+template <typename R>
+void launch_edgvar2(const Launch& l, const Grid<R>& g, const Strides& s, const R* u, const R* v, R* u_edg,
+                    R* v_edg, R* uvsq_edg, R* w) {
+  dim3 grid(blocks_for((long long)g.N * g.L), l.members);
+  FIM_KBEGIN(l, "k_edgvar2_grad");
+  k_edgvar2_grad<R><<<grid, kBlock, 0, l.stream>>>(g, s, u, v, u_edg, v_edg, w);
+  FIM_KEND(l);
+  FIM_KBEGIN(l, "k_edgvar2");
+  k_edgvar2<R><<<grid, kBlock, 0, l.stream>>>(g, s, w, u_edg, v_edg, uvsq_edg);
+  FIM_KEND(l);
+}
+
+// --------------------------------------------------------------------------
 // edgvar3 loop 1 with edgvalEval (edgvar3.F90:66-94,136-163): least-squares
 // (hfcoef) reconstruction of dp (field 0) and tracers 2..ntra (field t) on the
 // cell's own edges; pentagons store 0 in the sixth slot.
@@ -1217,6 +1302,8 @@ void launch_step_begin(const Launch& l, StepParams* sp) {
   template void launch_edgvar1<R>(const Launch&, const Grid<R>&, const Strides&, int, const R*, const R*,      \
                                   const R*, const R*, const R*, const R*, R*, R*, R*, R*, R*, R*, R*,          \
                                   const float2*, R*);                                                         \
+  template void launch_edgvar2<R>(const Launch&, const Grid<R>&, const Strides&, const R*, const R*, R*, R*,  \
+                                  R*, R*);                                                                    \
   template void launch_edgvar3<R>(const Launch&, const Grid<R>&, const Strides&, const R*, const R*, R*, R*,  \
                                   int, bool);                                                                \
   template void launch_cnuity<R>(const Launch&, const Grid<R>&, const Strides&, const CnuityScratch<R>&,      \

@@ -64,6 +64,7 @@ struct Grid {
   const R* __restrict__ corio;
   const R* __restrict__ grndspd;
   const R* __restrict__ hfcoef;   // [N*6*6]: hfcoef[(i*6+edge)*6+j]
+  const R* __restrict__ cxy;      // [N*2*6]: corner_xy(6,2,nip), cxy[(i*2+xy)*6+corner]; null if not given
   const double* __restrict__ area_d;  // [N] double areas for budgets
   const R* __restrict__ svsum;        // [N*2] sum over edges of sidevec_c(1:2), summed in FP64
   // per-level tables
@@ -391,6 +392,10 @@ void launch_globsum(const Launch&, const Grid<R>&, const Strides&, int ntr, cons
                     const R* rn2d, const R* rc2d, const R* pr3d, const R* ex3d, const R* qf2d,
                     double* partial, double* sums);
 size_t globsum_partials(int N, int L, int T, int members);
+// edgvar2 (fim_dyn.cu): w = 3 N L values of scratch
+template <typename R>
+void launch_edgvar2(const Launch&, const Grid<R>&, const Strides&, const R* u, const R* v, R* u_edg, R* v_edg,
+                    R* uvsq_edg, R* w);
 // physics coupling (fim_cpl.cu); GFS arrays (nip, nvl), cell fastest, FP64
 // gfs = ps, dp, p, u, v, dpdt, q, oz, cld, t; old6 = u, v, t, q, oz, cld
 template <typename R>

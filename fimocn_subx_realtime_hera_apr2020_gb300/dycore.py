@@ -124,6 +124,11 @@ class Dycore:
         self._call("fim_edgvar1", its, *map(_ptr, (u_vel, v_vel, delp, pres, exner, geop, montg, tracr, u_edg,
                                                      v_edg, dp_edg, lp_edg, geop_edg, mont_edg, uvsq_edg, trc_edg)))
 
+    def edgvar2(self, its, u_vel, v_vel, delp, pres, exner, geop, montg, tracr, u_edg, v_edg, dp_edg, lp_edg,
+                geop_edg, mont_edg, uvsq_edg, trc_edg):
+        self._call("fim_edgvar2", its, *map(_ptr, (u_vel, v_vel, delp, pres, exner, geop, montg, tracr, u_edg,
+                                                     v_edg, dp_edg, lp_edg, geop_edg, mont_edg, uvsq_edg, trc_edg)))
+
     def edgvar3(self, its, u_vel, v_vel, delp, pres, exner, geop, montg, tracr, u_edg, v_edg, dp_edg, lp_edg,
                 geop_edg, mont_edg, uvsq_edg, trc_edg):
         self._call("fim_edgvar3", its, *map(_ptr, (u_vel, v_vel, delp, pres, exner, geop, montg, tracr, u_edg,

@@ -96,6 +96,8 @@ typedef struct fim_config {
   int member_group;        /* [0] members advanced together through the dynamics of a
                               step; 0 = all.  The step's edge work fields and scratch
                               are held for one group, which bounds their memory */
+  int hi_order_uv_comp;    /* [0] hiOrderUVComp: edgvar2 after edgvar1 in fim_step
+                              (needs the grid's corner_xy) */
 } fim_config;
 
 typedef struct fim_ctx fim_ctx;
@@ -140,6 +142,21 @@ int fim_edgvar1_r8(fim_ctx *ctx, int its, const double *u_vel, const double *v_v
                    double *u_edg, double *v_edg, double *dp_edg, double *lp_edg,
                    double *geop_edg, double *mont_edg, double *uvsq_edg, double *trc_edg);
 int fim_edgvar1_r4(fim_ctx *ctx, int its, const float *u_vel, const float *v_vel,
+                   const float *delp, const float *pres, const float *exner,
+                   const float *geop, const float *montg, const float *tracr,
+                   float *u_edg, float *v_edg, float *dp_edg, float *lp_edg,
+                   float *geop_edg, float *mont_edg, float *uvsq_edg, float *trc_edg);
+
+/* FIMsrc/fim/horizontal/edgvar2.F90:24-27 (hiOrderUVComp; the MORE_VARS block,
+ * compiled out in the reference, is left out): rescales u_edg, v_edg and
+ * updates uvsq_edg; the other edge fields pass through.  Needs the grid's
+ * corner_xy (FIM_EINVAL without it). */
+int fim_edgvar2_r8(fim_ctx *ctx, int its, const double *u_vel, const double *v_vel,
+                   const double *delp, const double *pres, const double *exner,
+                   const double *geop, const double *montg, const double *tracr,
+                   double *u_edg, double *v_edg, double *dp_edg, double *lp_edg,
+                   double *geop_edg, double *mont_edg, double *uvsq_edg, double *trc_edg);
+int fim_edgvar2_r4(fim_ctx *ctx, int its, const float *u_vel, const float *v_vel,
                    const float *delp, const float *pres, const float *exner,
                    const float *geop, const float *montg, const float *tracr,
                    float *u_edg, float *v_edg, float *dp_edg, float *lp_edg,

@@ -176,6 +176,70 @@ static void edgval_eval(const orc_ctx *c, int ipn, const double *b /* [7][L] */,
 }
 
 /* edgvar3.F90:64-133; loop 2 keeps the reference's store-once pairing */
+/* edgvar2 (edgvar2.F90:24-319): uv_speed_edge, gradient, uv_speed, then the
+ * per-edge magnitude correction (the MORE_VARS block is compiled out) */
+void orc_edgvar2(const orc_ctx *c, const double *u, const double *v, double *u_edg, double *v_edg,
+                 double *uvsq_edg) {
+  const int N = c->nip, L = c->nvl;
+  const double divby6 = 1. / 6., eps = 0.00001;
+  double *spe = malloc(sizeof(double) * (size_t)N * 6 * L); /* uv_spd_edg */
+  double *gc = malloc(sizeof(double) * (size_t)N * 6 * L);  /* grad_conr */
+  double *spd = malloc(sizeof(double) * (size_t)N * L);     /* uv_spd */
+#pragma omp parallel for schedule(static)
+  for (int ipn = 0; ipn < N; ipn++) {
+    for (int e = 0; e < c->nprox[ipn]; e++)
+      for (int k = 0; k < L; k++)
+        spe[E3(k, e, ipn)] = sqrt(u_edg[E3(k, e, ipn)] * u_edg[E3(k, e, ipn)] +
+                                  v_edg[E3(k, e, ipn)] * v_edg[E3(k, e, ipn)]);
+    for (int k = 0; k < L; k++)
+      spd[C2(k, ipn)] = sqrt(u[C2(k, ipn)] * u[C2(k, ipn)] + v[C2(k, ipn)] * v[C2(k, ipn)]);
+  }
+  /* gradient (edgvar2.F90:231-258) */
+#pragma omp parallel for schedule(static)
+  for (int ipn = 0; ipn < N; ipn++) {
+    for (int k = 0; k < L; k++) {
+      double g1 = 0., g2 = 0.;
+      for (int e = 0; e < c->nprox[ipn]; e++) {
+        g1 = g1 + spe[E3(k, e, ipn)] * c->sidevec_c[(ipn * 6 + e) * 2 + 1];
+        g2 = g2 - spe[E3(k, e, ipn)] * c->sidevec_c[(ipn * 6 + e) * 2 + 0];
+      }
+      g1 = g1 * c->rarea[ipn];
+      g2 = g2 * c->rarea[ipn];
+      for (int e = 0; e < c->nprox[ipn]; e++)
+        gc[E3(k, e, ipn)] = 0.5 * (g1 * c->corner_xy[(ipn * 2 + 0) * 6 + e] + g2 * c->corner_xy[(ipn * 2 + 1) * 6 + e]);
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (int ipn = 0; ipn < N; ipn++) {
+    const int np = c->nprox[ipn];
+    for (int edg = 0; edg < np; edg++) {
+      const int conr1 = edg, conr2 = (edg + 1) % np;
+      const int nba = c->prox[ipn * 6 + edg], nbaedg = c->proxs[ipn * 6 + edg];
+      const int nbaconr1 = (nbaedg + 1) % c->nprox[nba], nbaconr2 = nbaedg;
+      const int edgm1 = (edg - 1 + np) % np;
+      const int nbm1 = c->prox[ipn * 6 + edgm1], nbm1conr = c->proxs[ipn * 6 + edgm1];
+      const int edgp1 = (edg + 1) % np;
+      const int nbp1 = c->prox[ipn * 6 + edgp1], nbp1conr = (c->proxs[ipn * 6 + edgp1] + 1) % c->nprox[nbp1];
+      for (int k = 0; k < L; k++) {
+        const double uv1conr1 = spd[C2(k, ipn)] + gc[E3(k, conr1, ipn)];
+        const double uv2conr1 = spd[C2(k, nba)] + gc[E3(k, nbaconr1, nba)];
+        const double uv3conr1 = spd[C2(k, nbm1)] + gc[E3(k, nbm1conr, nbm1)];
+        const double uv1conr2 = spd[C2(k, ipn)] + gc[E3(k, conr2, ipn)];
+        const double uv2conr2 = spd[C2(k, nba)] + gc[E3(k, nbaconr2, nba)];
+        const double uv3conr2 = spd[C2(k, nbp1)] + gc[E3(k, nbp1conr, nbp1)];
+        const size_t o = E3(k, edg, ipn);
+        const double uvm1 = sqrt(u_edg[o] * u_edg[o] + v_edg[o] * v_edg[o]);
+        const double uvm2 = (uv1conr1 + uv2conr1 + uv3conr1 + uv1conr2 + uv2conr2 + uv3conr2) * divby6;
+        const double r_m = uvm1 < eps ? 1.0 : uvm2 / uvm1;
+        u_edg[o] = u_edg[o] * r_m;
+        v_edg[o] = v_edg[o] * r_m;
+        uvsq_edg[o] = .5 * (u_edg[o] * u_edg[o] + v_edg[o] * v_edg[o]);
+      }
+    }
+  }
+  free(spe); free(gc); free(spd);
+}
+
 void orc_edgvar3(const orc_ctx *c, const double *delp, const double *tracr, double *dp_edg,
                  double *trc_edg) {
   const int N = c->nip, L = c->nvl;

@@ -43,6 +43,7 @@ typedef struct orc_ctx {
   double ab1, ab2, ab3;
   long diag_flags;                      /* conservation-check failures seen */
   int ntrb;                             /* class-B tracers after the ntra class-A ones */
+  const double *corner_xy;              /* [nip][2][6]: corner_xy(6,2,nip), for edgvar2 */
 } orc_ctx;
 
 void orc_derived(int nip, int nvl, int kbl, double dt, double intfc_smooth,
@@ -58,6 +59,10 @@ void orc_edgvar1(const orc_ctx *c, const double *u, const double *v, const doubl
                  const double *montg, const double *tracr, double *u_edg, double *v_edg,
                  double *dp_edg, double *lp_edg, double *geop_edg, double *mont_edg,
                  double *uvsq_edg, double *trc_edg);
+/* edgvar2 (edgvar2.F90:24-319, MORE_VARS off): rescale the edge wind to the
+ * corner-gradient speed average; u_edg, v_edg, uvsq_edg in place */
+void orc_edgvar2(const orc_ctx *c, const double *u, const double *v, double *u_edg, double *v_edg,
+                 double *uvsq_edg);
 void orc_edgvar3(const orc_ctx *c, const double *delp, const double *tracr,
                  double *dp_edg, double *trc_edg);
 void orc_cnuity(const orc_ctx *c, const double *u, const double *v, const double *u_edg,

@@ -30,7 +30,7 @@ class OrcCtx(ctypes.Structure):
                 ("dfflen_max", ctypes.c_double),
                 ("nf", ctypes.c_int), ("of", ctypes.c_int), ("vof", ctypes.c_int),
                 ("ab1", ctypes.c_double), ("ab2", ctypes.c_double), ("ab3", ctypes.c_double),
-                ("diag_flags", ctypes.c_long), ("ntrb", ctypes.c_int)]
+                ("diag_flags", ctypes.c_long), ("ntrb", ctypes.c_int), ("corner_xy", _VP)]
 
 
 _lib = None
@@ -53,6 +53,7 @@ def load():
             "orc_abstart": [P, I],
             "orc_edgvar1": [P] + [P] * 16,
             "orc_edgvar3": [P] * 5,
+            "orc_edgvar2": [P] * 6,
             "orc_cnuity": [P] * 14,
             "orc_trcadv": [P] * 8,
             "orc_mass_adv": [P] * 13,
@@ -108,7 +109,7 @@ class Oracle:
         c = OrcCtx()
         c.nip, c.nvl, c.ntra = N, L, cfg.ntra
         c.prox, c.proxs, c.nprox = _p(prox), _p(proxs), _p(nprox)
-        for n in ("cs", "sn", "sidevec_c", "sidevec_e", "sideln", "area", "hfcoef"):
+        for n in ("cs", "sn", "sidevec_c", "sidevec_e", "sideln", "area", "hfcoef", "corner_xy"):
             setattr(c, n, _p(getattr(grid, n)))
         c.rarea, c.corio, c.grndspd = _p(self.rarea), _p(self.corio), _p(self.grndspd)
         c.dt, c.kbl, c.hi_order = cfg.dt, cfg.kbl, cfg.hi_order_flux_comp
@@ -160,6 +161,9 @@ class Oracle:
     def hybgen(self, its, us3d, vs3d, tr3d, sdot, ex3d, dp3d, pr3d, targt=None):
         self.lib.orc_hybgen(ctypes.byref(self.c), its, _p(targt), *map(_p, (us3d, vs3d, tr3d, sdot, ex3d, dp3d,
                                                                              pr3d)))
+
+    def edgvar2(self, u, v, u_edg, v_edg, uvsq_edg):
+        self.lib.orc_edgvar2(ctypes.byref(self.c), *map(_p, (u, v, u_edg, v_edg, uvsq_edg)))
 
     def hystat(self, its, ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy):
         self.lib.orc_hystat(ctypes.byref(self.c), its, *map(_p, (ph3d, ex3d, mp3d, dp3d, tr3d, trdp, psrf, ptdcy)))
@@ -241,6 +245,8 @@ class Oracle:
         self.edgvar1(s["us3d"], s["vs3d"], s["dp3d"], s["pr3d"], s["ex3d"], s["ph3d"], s["mp3d"], s["tr3d"],
                      s["u_edg"], s["v_edg"], s["dp_edg"], s["lp_edg"], s["geop_edg"], s["mont_edg"], s["uvsq_edg"],
                      s["trc_edg"])
+        if getattr(self.cfg, "hi_order_uv_comp", 0):
+            self.edgvar2(s["us3d"], s["vs3d"], s["u_edg"], s["v_edg"], s["uvsq_edg"])
         if self.cfg.hi_order_flux_comp:
             self.edgvar3(s["dp3d"], s["tr3d"], s["dp_edg"], s["trc_edg"])
         if self.cfg.flux_conserv_schm == 1:

@@ -311,6 +311,44 @@ def test_fused_step_matches_routine_sequence(case4):
             assert np.array_equal(st.download(n), host(g[n])), (its, n)
 
 
+EDG1_NAMES = ["us3d", "vs3d", "dp3d", "pr3d", "ex3d", "ph3d", "mp3d", "tr3d", "u_edg", "v_edg", "dp_edg",
+              "lp_edg", "geop_edg", "mont_edg", "uvsq_edg", "trc_edg"]
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", TOL64), ("f32", TOL32)])
+def test_edgvar2_routine(precision, tol):
+    """fim_edgvar2 (hiOrderUVComp) on the oracle's edgvar1 output."""
+    grid, cfg, fields = make_case(glvl=4, nvl=38, ntra=5, dt=400.0, seed=1401, noise=1.0, precision=precision)
+    o = oracle_for(grid, cfg)
+    s = o.init_state(o.new_state(fields))
+    o.abstart(1)
+    o.edgvar1(*[s[n] for n in EDG1_NAMES])
+    rt = torch.float32 if precision == "f32" else torch.float64
+    g = {n: dev(s[n], rt) for n in EDG1_NAMES}
+    dyc = F.Dycore(grid, cfg)
+    dyc.edgvar2(1, *[g[n] for n in EDG1_NAMES])
+    ue0 = s["u_edg"].copy()
+    o.edgvar2(s["us3d"], s["vs3d"], s["u_edg"], s["v_edg"], s["uvsq_edg"])
+    assert rel_l2(s["u_edg"], ue0) > 1e-6  # the correction acts on this state
+    for n in ("u_edg", "v_edg", "uvsq_edg"):
+        assert rel_l2(host(g[n]), s[n]) <= tol, n
+
+
+def test_fused_step_with_edgvar2_fp64():
+    """fim_step with hi_order_uv_comp runs edgvar2 between edgvar1 and
+    edgvar3, as dyn_run.F90:353-360 does."""
+    grid, cfg, fields = make_case(glvl=4, nvl=38, ntra=5, dt=400.0, seed=1402, noise=1.0, hi_order_uv_comp=1)
+    o = oracle_for(grid, cfg)
+    s = o.init_state(o.new_state(fields))
+    dyc, st = _gpu_state(grid, cfg, fields)
+    for its in range(1, 3):
+        o.step(s, its)
+        st.step(its, use_graph=True)
+        errs = {n: rel_l2(st.download(n), s[n]) for n in PROGNOSTIC + ["ws3d", "relvor"]}
+        bad = {k: v for k, v in errs.items() if not v <= TOL64}
+        assert not bad, (its, bad)
+
+
 AB3_FIELDS = ["u_tdcy", "v_tdcy", "dp_tdcy", "dpl_tdcy", "trc_tdcy", "trl_tdcy"]
 STEP_OUTPUTS = ["ws3d", "sdot", "relvor", "ptdcy"]
 
