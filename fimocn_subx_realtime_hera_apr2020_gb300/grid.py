@@ -49,7 +49,8 @@ class Grid:
         d.glvl = self.glvl
         d.nip = self.nip
         for n in self.NAMES_I + self.NAMES_D:
-            setattr(d, n, getattr(self, n).ctypes.data)
+            a = getattr(self, n)
+            setattr(d, n, a.ctypes.data if a is not None else None)  # optional tables may be absent
         return d
 
     def zero_based(self):

@@ -46,3 +46,30 @@ def test_ctx_rejects_edge_without_mirror():
         F.Dycore(g, cfg)
     assert err.value.code == L.FIM_EINVAL
     assert np.all(ps[:, :5] >= 1)
+
+
+def test_ctx_rejects_bad_configurations():
+    """Configuration checks of fim_ctx_create run before any device call."""
+    import pytest
+    import fimocn_subx_realtime_hera_apr2020_gb300 as F
+    g = F.Grid(4)
+    base = dict(nvl=38, ntra=5, dt=400.0, precision="f64")
+    cases = [
+        (dict(base, ntra=3), L.FIM_EINVAL),                    # theta + at least 3 tracers
+        (dict(base, flux_conserv_schm=3), L.FIM_ENOTSUP),
+        (dict(base, pure_sig=1), L.FIM_ENOTSUP),
+        (dict(base, remap_optn=4), L.FIM_EINVAL),
+        (dict(base, ntrb=-1), L.FIM_EINVAL),
+        (dict(base, ntra=20, ntrb=13), L.FIM_EINVAL),          # ntra + ntrb <= 32
+        (dict(base, dt=0.0), L.FIM_EINVAL),
+    ]
+    for kw, code in cases:
+        with pytest.raises(L.FimError) as err:
+            F.Dycore(g, F.FimConfig(**kw))
+        assert err.value.code == code, kw
+    # edgvar2 in the step needs the grid's corner_xy table
+    g2 = F.Grid(4)
+    g2.corner_xy = None
+    with pytest.raises(L.FimError) as err:
+        F.Dycore(g2, F.FimConfig(**dict(base, hi_order_uv_comp=1)))
+    assert err.value.code == L.FIM_EINVAL
