@@ -76,3 +76,48 @@ def test_globsum_matches_numpy():
     ex0 = s["ex3d"].reshape(N, L + 1)[:, 0]
     den = pr0 / ((RD / CP) * ex0 * tr[0][:, 0])
     np.testing.assert_allclose(b["qmste"], (a * den * qf * cfg.dt / (1.25 * 2.5e6)).sum(), rtol=1e-12)
+
+
+def test_edgvar3_matches_numpy():
+    """edgvar3.F90:64-133: edgvalEval's least-squares edge values of dp and
+    tracers 2..ntra, then the two-sided average stored in both slots."""
+    grid, cfg, o, s = _case()
+    N, L, T = grid.nip, cfg.nvl, cfg.ntra
+    prox = np.asarray(grid.prox).reshape(N, 6) - 1
+    proxs = np.asarray(grid.proxs).reshape(N, 6) - 1
+    npx = np.asarray(grid.nprox)
+    hf = np.asarray(grid.hfcoef).reshape(N, 6, 6)
+    rng = np.random.default_rng(1503)
+    s["tr3d"][N * L:] += rng.uniform(0, 1e-3, (T - 1) * N * L)
+
+    def own(f):  # f (N, L) -> own-side edge values (N, 6, L)
+        out = np.zeros((N, 6, L))
+        for i in range(N):
+            n = npx[i]
+            d = f[prox[i, :n]] - f[i][None]
+            for e in range(n):
+                acc = f[i].copy()
+                for j in range(n):
+                    acc = acc + d[j] * hf[i, e, j]
+                out[i, e] = acc
+        return out
+
+    def average(x):
+        y = x.copy()
+        for i in range(N):
+            for e in range(npx[i]):
+                nb, os_ = prox[i, e], proxs[i, e]
+                if i < nb:
+                    w = 0.5 * (x[i, e] + x[nb, os_])
+                    y[i, e] = w
+                    y[nb, os_] = w
+        return y
+
+    dp_ref = average(own(s["dp3d"].reshape(N, L)))
+    tr = s["tr3d"].reshape(T, N, L)
+    tr_ref = [average(own(tr[t])) for t in range(1, T)]
+    o.edgvar3(s["dp3d"], s["tr3d"], s["dp_edg"], s["trc_edg"])
+    assert np.array_equal(s["dp_edg"].reshape(N, 6, L), dp_ref)
+    te = s["trc_edg"].reshape(T, N, 6, L)
+    for t in range(1, T):
+        assert np.array_equal(te[t], tr_ref[t - 1]), t
