@@ -121,3 +121,90 @@ def test_edgvar3_matches_numpy():
     te = s["trc_edg"].reshape(T, N, 6, L)
     for t in range(1, T):
         assert np.array_equal(te[t], tr_ref[t - 1]), t
+
+
+def test_cnuity_matches_numpy():
+    """cnuity_compute.F90 cnuity1..5: donor-cell and high-order mass fluxes,
+    Zalesak limiter over the 1-ring, AB3 thickness update, top-down pressure,
+    Exner function and omega."""
+    grid, cfg, o, s = _case()
+    N, L = grid.nip, cfg.nvl
+    prox = np.asarray(grid.prox).reshape(N, 6) - 1
+    proxs = np.asarray(grid.proxs).reshape(N, 6) - 1
+    npx = np.asarray(grid.nprox)
+    sve = np.asarray(grid.sidevec_e).reshape(N, 6, 2)
+    svc = np.asarray(grid.sidevec_c).reshape(N, 6, 2)
+    area = np.asarray(grid.area)
+    rarea = 1.0 / area
+    for its in (1, 2, 3):  # Euler, AB2, AB3 weights
+        o.abstart(its)
+        o.edgvar1(s["us3d"], s["vs3d"], s["dp3d"], s["pr3d"], s["ex3d"], s["ph3d"], s["mp3d"], s["tr3d"],
+                  s["u_edg"], s["v_edg"], s["dp_edg"], s["lp_edg"], s["geop_edg"], s["mont_edg"], s["uvsq_edg"],
+                  s["trc_edg"])
+        o.edgvar3(s["dp3d"], s["tr3d"], s["dp_edg"], s["trc_edg"])
+        nf, of, vof = o.c.nf, o.c.of, o.c.vof
+        ab1, ab2, ab3, dt = o.c.ab1, o.c.ab2, o.c.ab3, o.c.dt
+        ue, ve = s["u_edg"].reshape(N, 6, L), s["v_edg"].reshape(N, 6, L)
+        dpe, lpe = s["dp_edg"].reshape(N, 6, L), s["lp_edg"].reshape(N, 6, L)
+        delp = s["dp3d"].reshape(N, L).copy()
+        pres = s["pr3d"].reshape(N, L + 1).copy()
+        dpt = s["dp_tdcy"].reshape(3, N, L).copy()
+        dplt = s["dpl_tdcy"].reshape(3, N, L).copy()
+        u, v = s["us3d"].reshape(N, L), s["vs3d"].reshape(N, L)
+        live = np.arange(6)[None, :] < npx[:, None]
+        vn = sve[:, :, 1:2] * ue - sve[:, :, 0:1] * ve
+        psl = np.where(live, proxs, 0)            # a pentagon's slot 5 has no mirror: masked below
+        vx = vn[prox, psl]                        # the neighbour's normal velocity on the shared edge
+        mass = 0.5 * ((vn + np.abs(vn)) * delp[:, None, :] - (vx + np.abs(vx)) * delp[prox])
+        mass = np.where(live[:, :, None], mass, 0.0)
+        anti = np.where(live[:, :, None], vn * dpe - mass, 0.0)
+        acc = np.zeros((N, L))
+        for e in range(6):
+            acc = acc + mass[:, e]
+        dplt[nf] = -acc * rarea[:, None]
+        dlo = delp + ab1 * dplt[nf] + ab2 * dplt[of] + ab3 * dplt[vof]
+        pp, pm = np.zeros((N, L)), np.zeros((N, L))
+        for e in range(6):
+            a = anti[:, e]
+            pp = np.where(live[:, e:e + 1] & (a <= 0), pp - a, pp)
+            pm = np.where(live[:, e:e + 1] & (a > 0), pm + a, pm)
+        dmx, dmn = np.maximum(dlo, delp), np.minimum(dlo, delp)
+        for e in range(6):
+            dmx, dmn = np.maximum(dmx, dlo[prox[:, e]]), np.minimum(dmn, dlo[prox[:, e]])
+        for e in range(6):
+            dmx, dmn = np.maximum(dmx, delp[prox[:, e]]), np.minimum(dmn, delp[prox[:, e]])
+        dmx, dmn = np.maximum(0.0, dmx), np.maximum(0.0, dmn)
+        qp = (dmx - dlo - (ab2 * np.minimum(0.0, dpt[of]) + ab3 * np.maximum(0.0, dpt[vof]))) / ab1 * area[:, None]
+        qm = (dlo - dmn + (ab2 * np.maximum(0.0, dpt[of]) + ab3 * np.minimum(0.0, dpt[vof]))) / ab1 * area[:, None]
+        rp = np.maximum(0.0, np.minimum(1.0, qp / np.maximum(pp, 1e-11)))
+        rm = np.maximum(0.0, np.minimum(1.0, qm / np.maximum(pm, 1e-11)))
+        clip = np.where(anti >= 0, np.minimum(rm[:, None, :], rp[prox]), np.minimum(rp[:, None, :], rm[prox]))
+        anti = anti * clip
+        mass = mass + anti
+        at = np.zeros((N, L))
+        for e in range(6):
+            at = at + np.where(live[:, e:e + 1], anti[:, e], 0.0)
+        dpt[nf] = dplt[nf] + (-at * rarea[:, None])
+        delp = delp + ab1 * dpt[nf] + ab2 * dpt[of] + ab3 * dpt[vof]
+        omega = np.zeros((N, L))
+        col = np.zeros(N)
+        for k in range(L - 1, -1, -1):
+            pres[:, k] = pres[:, k + 1] + delp[:, k]
+            lyr = (ab1 * dpt[nf][:, k] + ab2 * dpt[of][:, k] + ab3 * dpt[vof][:, k]) / dt
+            om = col + 0.5 * lyr
+            col = col + lyr
+            dx, dy = np.zeros(N), np.zeros(N)
+            for e in range(6):
+                dx = np.where(live[:, e], dx + lpe[:, e, k] * svc[:, e, 1], dx)
+                dy = np.where(live[:, e], dy - lpe[:, e, k] * svc[:, e, 0], dy)
+            omega[:, k] = om + (u[:, k] * dx + v[:, k] * dy) * rarea
+        exner = CP * (pres / 100000.0) ** (RD / CP)
+        o.cnuity(s["us3d"], s["vs3d"], s["u_edg"], s["v_edg"], s["dp_edg"], s["lp_edg"], s["dp3d"], s["pr3d"],
+                 s["ex3d"], s["dp_tdcy"], s["dpl_tdcy"], s["massfx"], s["ws3d"])
+        mf = s["massfx"].reshape(3, N, 6, L)[nf]
+        np.testing.assert_allclose(mf[live], mass[live], rtol=1e-12, atol=1e-9)
+        np.testing.assert_allclose(s["dp3d"].reshape(N, L), delp, rtol=1e-13)
+        np.testing.assert_allclose(s["dp_tdcy"].reshape(3, N, L)[nf], dpt[nf], rtol=1e-11, atol=1e-11)
+        np.testing.assert_allclose(s["pr3d"].reshape(N, L + 1), pres, rtol=1e-13)
+        np.testing.assert_allclose(s["ex3d"].reshape(N, L + 1)[:, :L], exner[:, :L], rtol=1e-13)
+        np.testing.assert_allclose(s["ws3d"].reshape(N, L), omega, rtol=1e-9, atol=1e-9)
