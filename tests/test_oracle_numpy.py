@@ -288,3 +288,58 @@ def test_trcadv_matches_numpy():
         o.trcadv(s["trc_edg"], s["tr3d"], s["trdp"], s["trc_tdcy"], s["trl_tdcy"], s["massfx"], s["dp3d"])
         for k in ("tr3d", "trdp", "trc_tdcy", "trl_tdcy"):
             np.testing.assert_allclose(s[k], ref[k], rtol=1e-11, atol=1e-15, err_msg="%d %s" % (its, k))
+
+
+def test_edgvar1_matches_numpy():
+    """edgvar1.F90:156-511 (eqwgt, janjic=0): rotated four-cell wind with the
+    magnitude correction, mid-layer pressure, Montgomery potential, kinetic
+    energy and theta on the cell's own edges."""
+    grid, cfg, o, s = _case()
+    N, L, T = grid.nip, cfg.nvl, cfg.ntra
+    prox = np.asarray(grid.prox).reshape(N, 6) - 1
+    npx = np.asarray(grid.nprox)
+    cs = np.asarray(grid.cs).reshape(N, 6, 4)
+    sn = np.asarray(grid.sn).reshape(N, 6, 4)
+    u, v = s["us3d"].reshape(N, L), s["vs3d"].reshape(N, L)
+    pr, mo = s["pr3d"].reshape(N, L + 1), s["mp3d"].reshape(N, L)
+    th = s["tr3d"].reshape(T, N, L)[0]
+    plev = pr[:, :L] + pr[:, 1:]
+    ue = np.zeros((N, 6, L)); ve = np.zeros((N, 6, L)); lp = np.zeros((N, 6, L))
+    me = np.zeros((N, 6, L)); uv = np.zeros((N, 6, L)); te = np.zeros((N, 6, L))
+    d6 = 1.0 / 6.0
+    idx = np.arange(N)
+    for e in range(6):
+        live = e < npx
+        i2 = prox[:, e]
+        i3t = prox[idx, (e - 1 + npx) % npx]
+        i3l = prox[idx, (e + 1) % npx]
+        c, sg = cs[:, e, :], sn[:, e, :]
+        rot = lambda q, x: (c[:, q:q + 1] * u[x] + sg[:, q:q + 1] * v[x],  # noqa: E731
+                            -sg[:, q:q + 1] * u[x] + c[:, q:q + 1] * v[x])
+        u3t, v3t = rot(2, i3t)
+        u1, v1 = rot(0, idx)
+        u2, v2 = rot(1, i2)
+        u3l, v3l = rot(3, i3l)
+        a = (2.0 * (u1 + u2) + u3t + u3l) * d6
+        b = (2.0 * (v1 + v2) + v3t + v3l) * d6
+        m2 = (2.0 * (np.sqrt(u1 * u1 + v1 * v1) + np.sqrt(u2 * u2 + v2 * v2)) + np.sqrt(u3t * u3t + v3t * v3t)
+              + np.sqrt(u3l * u3l + v3l * v3l)) * d6
+        m1 = np.sqrt(a * a + b * b)
+        a = a * m2 / np.maximum(0.001, m1)
+        b = b * m2 / np.maximum(0.001, m1)
+        w = live[:, None]
+        ue[:, e] = np.where(w, a, 0.0)
+        ve[:, e] = np.where(w, b, 0.0)
+        lp[:, e] = np.where(w, (plev[idx] + plev[i2] + 0.5 * (plev[i3t] + plev[i3l])) * d6, 0.0)
+        me[:, e] = np.where(w, (2.0 * (mo[idx] + mo[i2]) + mo[i3t] + mo[i3l]) * d6, 0.0)
+        uv[:, e] = np.where(w, 0.5 * (a * a + b * b), 0.0)
+        te[:, e] = np.where(w, (2.0 * (th[idx] + th[i2]) + th[i3t] + th[i3l]) * d6, 0.0)
+    for k in ("u_edg", "v_edg", "lp_edg", "mont_edg", "uvsq_edg"):
+        s[k][:] = 0.0
+    s["trc_edg"][:] = 0.0
+    o.abstart(1)
+    o.edgvar1(s["us3d"], s["vs3d"], s["dp3d"], s["pr3d"], s["ex3d"], s["ph3d"], s["mp3d"], s["tr3d"], s["u_edg"],
+              s["v_edg"], s["dp_edg"], s["lp_edg"], s["geop_edg"], s["mont_edg"], s["uvsq_edg"], s["trc_edg"])
+    for k, ref in (("u_edg", ue), ("v_edg", ve), ("lp_edg", lp), ("mont_edg", me), ("uvsq_edg", uv)):
+        np.testing.assert_allclose(s[k].reshape(N, 6, L), ref, rtol=1e-13, atol=1e-9, err_msg=k)
+    np.testing.assert_allclose(s["trc_edg"].reshape(T, N, 6, L)[0], te, rtol=1e-13, err_msg="trc_edg")
