@@ -343,3 +343,81 @@ def test_edgvar1_matches_numpy():
     for k, ref in (("u_edg", ue), ("v_edg", ve), ("lp_edg", lp), ("mont_edg", me), ("uvsq_edg", uv)):
         np.testing.assert_allclose(s[k].reshape(N, 6, L), ref, rtol=1e-13, atol=1e-9, err_msg=k)
     np.testing.assert_allclose(s["trc_edg"].reshape(T, N, 6, L)[0], te, rtol=1e-13, err_msg="trc_edg")
+
+
+def test_momtum_matches_numpy():
+    """momtum.F90:86-152 with dissip (momtum_compute.F90:102-229) and momtum1
+    (231-450): ground-speed-shifted harmonic dissipation, Montgomery PGF and
+    vorticity line integrals, Coriolis, AB3 update and the Rayleigh damping of
+    the top quarter of the layers (forced here by a 120 m/s top jet)."""
+    grid, cfg, o, s = _case()
+    N, L, T = grid.nip, cfg.nvl, cfg.ntra
+    prox = np.asarray(grid.prox).reshape(N, 6) - 1
+    npx = np.asarray(grid.nprox)
+    cs = np.asarray(grid.cs).reshape(N, 6, 4)
+    sn = np.asarray(grid.sn).reshape(N, 6, 4)
+    svc = np.asarray(grid.sidevec_c).reshape(N, 6, 2)
+    sve = np.asarray(grid.sidevec_e).reshape(N, 6, 2)
+    sl = np.asarray(grid.sideln).reshape(N, 6)
+    rarea, corio, grnd, dfflen = o.rarea, o.corio, o.grndspd, o.dfflen
+    u3 = s["us3d"].reshape(N, L)
+    u3[:, L - 3:] = 120.0  # above rlthresh: the damping acts
+    for its in (1, 2, 3):
+        o.abstart(its)
+        o.edgvar1(s["us3d"], s["vs3d"], s["dp3d"], s["pr3d"], s["ex3d"], s["ph3d"], s["mp3d"], s["tr3d"],
+                  s["u_edg"], s["v_edg"], s["dp_edg"], s["lp_edg"], s["geop_edg"], s["mont_edg"], s["uvsq_edg"],
+                  s["trc_edg"])
+        nf, of, vof, ab1, ab2, ab3, dt = o.c.nf, o.c.of, o.c.vof, o.c.ab1, o.c.ab2, o.c.ab3, o.c.dt
+        u, v = s["us3d"].reshape(N, L).copy(), s["vs3d"].reshape(N, L).copy()
+        dp = np.maximum(s["dp3d"].reshape(N, L), 1e-11)
+        ex = s["ex3d"].reshape(N, L + 1)
+        ue, ve = s["u_edg"].reshape(N, 6, L), s["v_edg"].reshape(N, 6, L)
+        me, uv = s["mont_edg"].reshape(N, 6, L), s["uvsq_edg"].reshape(N, 6, L)
+        te = s["trc_edg"].reshape(T, N, 6, L)[0]
+        ut, vt = s["u_tdcy"].reshape(3, N, L).copy(), s["v_tdcy"].reshape(3, N, L).copy()
+        # dissip on the ground-speed-shifted wind
+        wu, wv = u + grnd[:, None], v.copy()
+        su, sv = np.zeros((N, L)), np.zeros((N, L))
+        factor = rarea[:, None] / dp
+        for e in range(6):
+            live = (e < npx)[:, None]
+            x = prox[:, e]
+            c0, s0, c1, s1 = cs[:, e, 0:1], sn[:, e, 0:1], cs[:, e, 1:2], sn[:, e, 1:2]
+            uxy1, vxy1 = c0 * wu + s0 * wv, -s0 * wu + c0 * wv
+            uxy2, vxy2 = c1 * wu[x] + s1 * wv[x], -s1 * wu[x] + c1 * wv[x]
+            hf = dp * dp[x] / (dp + dp[x])
+            ufx = (uxy2 - uxy1) * dfflen[None, :] * sl[:, e:e + 1] * 2.0 * hf
+            vfx = (vxy2 - vxy1) * dfflen[None, :] * sl[:, e:e + 1] * 2.0 * hf
+            su = np.where(live, su + (c0 * ufx - s0 * vfx) * factor, su)
+            sv = np.where(live, sv + (s0 * ufx + c0 * vfx) * factor, sv)
+        u, v = u + su, v + sv
+        # momtum1
+        exm = 0.5 * (ex[:, :L] + ex[:, 1:])
+        pgx, pgy, rv = np.zeros((N, L)), np.zeros((N, L)), np.zeros((N, L))
+        for e in range(6):
+            live = (e < npx)[:, None]
+            mu = me[:, e] + uv[:, e]
+            pgx = np.where(live, pgx - mu * svc[:, e, 1:2] + exm * te[:, e] * svc[:, e, 1:2], pgx)
+            pgy = np.where(live, pgy + mu * svc[:, e, 0:1] - exm * te[:, e] * svc[:, e, 0:1], pgy)
+            rv = np.where(live, rv + (sve[:, e, 0:1] * ue[:, e] + sve[:, e, 1:2] * ve[:, e]), rv)
+        pgx, pgy, rv = pgx * rarea[:, None], pgy * rarea[:, None], rv * rarea[:, None]
+        ut[nf] = pgx + (corio[:, None] + rv) * v
+        vt[nf] = pgy - (corio[:, None] + rv) * u
+        u = u + ab1 * ut[nf] + ab2 * ut[of] + ab3 * ut[vof]
+        v = v + ab1 * vt[nf] + ab2 * vt[of] + ab3 * vt[vof]
+        q = np.maximum(np.maximum(u[:, L - 1] ** 2 + v[:, L - 1] ** 2, u[:, L - 2] ** 2 + v[:, L - 2] ** 2),
+                       u[:, L - 3] ** 2 + v[:, L - 3] ** 2) / (cfg.rlthresh * cfg.rlthresh)
+        damp = q > 1.0
+        qq = np.sqrt(np.where(damp, (q - 1.0) * q, 0.0))
+        ndamp = int(0.25 * L)
+        for k in range(L - 1 - ndamp, L):
+            f = 1.0 - (dt / 86400.0) * cfg.rleigh * qq * 2.0 ** (cfg.rltaper * (k + 1 - L))
+            u[:, k] = np.where(damp, u[:, k] * f, u[:, k])
+            v[:, k] = np.where(damp, v[:, k] * f, v[:, k])
+        assert damp.any()
+        o.momtum(s["us3d"], s["vs3d"], s["ex3d"], s["relvor"], s["u_edg"], s["v_edg"], s["trc_edg"],
+                 s["mont_edg"], s["uvsq_edg"], s["u_tdcy"], s["v_tdcy"], s["dp3d"])
+        np.testing.assert_allclose(s["relvor"].reshape(N, L), rv, rtol=1e-11, atol=1e-17, err_msg=str(its))
+        np.testing.assert_allclose(s["u_tdcy"].reshape(3, N, L)[nf], ut[nf], rtol=1e-10, atol=1e-13)
+        np.testing.assert_allclose(s["us3d"].reshape(N, L), u, rtol=1e-12, atol=1e-10, err_msg=str(its))
+        np.testing.assert_allclose(s["vs3d"].reshape(N, L), v, rtol=1e-12, atol=1e-10, err_msg=str(its))
