@@ -421,3 +421,96 @@ def test_momtum_matches_numpy():
         np.testing.assert_allclose(s["u_tdcy"].reshape(3, N, L)[nf], ut[nf], rtol=1e-10, atol=1e-13)
         np.testing.assert_allclose(s["us3d"].reshape(N, L), u, rtol=1e-12, atol=1e-10, err_msg=str(its))
         np.testing.assert_allclose(s["vs3d"].reshape(N, L), v, rtol=1e-12, atol=1e-10, err_msg=str(its))
+
+
+def test_mass_adv_matches_numpy():
+    """mass_adv (flux_conserv_schm = 2): flux_limiter.F90 edge normal velocity
+    and the M1 limiter, massflux_newdepth and update_pres, three AB steps."""
+    grid, cfg, fields = make_case(glvl=3, nvl=38, ntra=5, seed=1505, flux_conserv_schm=2)
+    o = oracle_for(grid, cfg)
+    s = o.init_state(o.new_state(fields))
+    N, L = grid.nip, cfg.nvl
+    prox = np.asarray(grid.prox).reshape(N, 6) - 1
+    npx = np.asarray(grid.nprox)
+    sve = np.asarray(grid.sidevec_e).reshape(N, 6, 2)
+    svc = np.asarray(grid.sidevec_c).reshape(N, 6, 2)
+    rarea = o.rarea
+    idx = np.arange(N)
+    for its in (1, 2, 3):
+        o.abstart(its)
+        o.edgvar1(s["us3d"], s["vs3d"], s["dp3d"], s["pr3d"], s["ex3d"], s["ph3d"], s["mp3d"], s["tr3d"],
+                  s["u_edg"], s["v_edg"], s["dp_edg"], s["lp_edg"], s["geop_edg"], s["mont_edg"], s["uvsq_edg"],
+                  s["trc_edg"])
+        o.edgvar3(s["dp3d"], s["tr3d"], s["dp_edg"], s["trc_edg"])
+        nf, of, vof, ab1, ab2, ab3, dt = o.c.nf, o.c.of, o.c.vof, o.c.ab1, o.c.ab2, o.c.ab3, o.c.dt
+        ue, ve = s["u_edg"].reshape(N, 6, L), s["v_edg"].reshape(N, 6, L)
+        dpe = s["dp_edg"].reshape(N, 6, L).copy()
+        lpe = s["lp_edg"].reshape(N, 6, L)
+        g = s["dp3d"].reshape(N, L).copy()
+        pres = s["pr3d"].reshape(N, L + 1).copy()
+        dpt = s["dp_tdcy"].reshape(3, N, L).copy()
+        u, v = s["us3d"].reshape(N, L), s["vs3d"].reshape(N, L)
+        vn = sve[:, :, 1:2] * ue - sve[:, :, 0:1] * ve
+        cn = np.abs(vn) * dt * rarea[:, None, None]
+        qs = np.zeros((N, 6, L))
+        for e in range(6):
+            x = prox[:, e]
+            m1 = prox[idx, (e - 1 + npx) % npx]
+            p1 = prox[idx, (e + 1) % npx]
+            qmn = np.minimum(np.minimum(np.minimum(g, g[x]), g[m1]), g[p1])
+            qmx = np.maximum(np.maximum(np.maximum(g, g[x]), g[m1]), g[p1])
+            qs[:, e] = np.maximum(qmn, np.minimum(qmx, dpe[:, e]))
+        qminin = np.full((N, L), np.finfo(np.float64).max)
+        qmaxin, cqmin, cqmax, cin, cout = (np.zeros((N, L)) for _ in range(5))
+        for e in range(6):
+            live = (e < npx)[:, None]
+            out = live & (vn[:, e] > 0)
+            inn = live & ~(vn[:, e] > 0)
+            x = prox[:, e]
+            cout = np.where(out, cout + cn[:, e], cout)
+            qmn = np.minimum(qs[:, e], g[x])
+            qmx = np.maximum(qs[:, e], g[x])
+            cin = np.where(inn, cin + cn[:, e], cin)
+            qminin = np.where(inn, np.minimum(qminin, qmn), qminin)
+            qmaxin = np.where(inn, np.maximum(qmaxin, qmx), qmaxin)
+            cqmin = np.where(inn, cqmin + cn[:, e] * qmn, cqmin)
+            cqmax = np.where(inn, cqmax + cn[:, e] * qmx, cqmax)
+        qmin_next, qmax_next = np.minimum(g, qminin), np.maximum(g, qmaxin)
+        tail = ab2 * dpt[of] + ab3 * dpt[vof]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            qmo = (g + ab1 / dt * cqmax - qmax_next * (1.0 + cin - cout) + tail) / cout / ab1 * dt
+            qxo = (g + ab1 / dt * cqmin - qmin_next * (1.0 + cin - cout) + tail) / cout / ab1 * dt
+        qmo = np.where(cout != 0.0, qmo, -100000.0)
+        qxo = np.where(cout != 0.0, qxo, 100000.0)
+        mf = np.zeros((N, 6, L))
+        for e in range(6):
+            src = np.where(vn[:, e] > 0, idx[:, None], prox[:, e][:, None])
+            kk = np.arange(L)[None, :]
+            dpe[:, e] = np.maximum(qmo[src, kk], np.minimum(qxo[src, kk], qs[:, e]))
+            mf[:, e] = np.where((e < npx)[:, None], vn[:, e] * dpe[:, e], 0.0)
+        tsum = np.zeros((N, L))
+        for e in range(6):
+            tsum = tsum + mf[:, e]
+        dpt[nf] = -tsum * rarea[:, None]
+        g = np.maximum(g + ab1 * dpt[nf] + ab2 * dpt[of] + ab3 * dpt[vof], 0.0)
+        omega = np.zeros((N, L))
+        col = np.zeros(N)
+        for k in range(L - 1, -1, -1):
+            pres[:, k] = pres[:, k + 1] + g[:, k]
+            lyr = (ab1 * dpt[nf][:, k] + ab2 * dpt[of][:, k] + ab3 * dpt[vof][:, k]) / dt
+            om = col + 0.5 * lyr
+            col = col + lyr
+            dx, dy = np.zeros(N), np.zeros(N)
+            for e in range(6):
+                live = e < npx
+                dx = np.where(live, dx + lpe[:, e, k] * svc[:, e, 1], dx)
+                dy = np.where(live, dy - lpe[:, e, k] * svc[:, e, 0], dy)
+            omega[:, k] = om + (u[:, k] * dx + v[:, k] * dy) * rarea
+        o.mass_adv(s["us3d"], s["vs3d"], s["u_edg"], s["v_edg"], s["dp_edg"], s["lp_edg"], s["dp3d"], s["pr3d"],
+                   s["ex3d"], s["dp_tdcy"], s["massfx"], s["ws3d"])
+        live = np.arange(6)[None, :] < npx[:, None]
+        np.testing.assert_allclose(s["dp_edg"].reshape(N, 6, L)[live], dpe[live], rtol=1e-13, err_msg=str(its))
+        np.testing.assert_allclose(s["massfx"].reshape(3, N, 6, L)[nf][live], mf[live], rtol=1e-12, atol=1e-9)
+        np.testing.assert_allclose(s["dp3d"].reshape(N, L), g, rtol=1e-13)
+        np.testing.assert_allclose(s["pr3d"].reshape(N, L + 1), pres, rtol=1e-13)
+        np.testing.assert_allclose(s["ws3d"].reshape(N, L), omega, rtol=1e-9, atol=1e-9)
