@@ -24,10 +24,17 @@
 //     here with Householder QR (Golub & Van Loan, Matrix Computations, 5.2),
 //     which gives the same Moore-Penrose inverse for a full-column-rank system.
 //
-// The cell numbering is the rhombus IJ order (curve = 0); the neighbour search
-// is generic (it walks the triangulation), not the reference's index patterns,
-// so every table is cross-checked against a brute-force geometric search by the
-// test suite.
+// Cell numbering and neighbour slot order are the reference's (curve = 0, the
+// IJ order): the north pole is cell 1, then the rhombi in the order U0, L0, U1,
+// L1, ..., U4, L4 (upper rhombus k between the north pole and upper vertices
+// k, k+1; lower rhombus k below it), sl*sl cells each in rows of sl, and the
+// south pole last (icos.F90:174-239, the rhombus offsets of proc_grid).  The
+// neighbours of a cell are found by walking the triangulation and are listed
+// counter-clockwise seen from outside the sphere, starting where the
+// reference's pattern tables of GridGen.F90:98-217,529-623 start (see
+// first_neighbour), so prox, proxs and nprox equal the reference's tables
+// entry for entry; the tests check them against a restatement of the
+// reference generator.
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -154,6 +161,30 @@ struct Builder {
   std::vector<int> nprox;
   std::vector<std::array<int, 6>> ring;
 
+  // 0-based index of the first cell of rhombus d (d = 0..4 upper, 5..9
+  // lower): rhombus pairs (upper k, lower k) follow each other
+  // (icos.F90:212-237: offsets 2k*sl^2 and (2k+1)*sl^2 after the north pole).
+  int base(int d) const { return 1 + (2 * (d % 5) + (d >= 5 ? 1 : 0)) * sl * sl; }
+
+  // 0-based index of the neighbour the reference lists first for the cell
+  // (d, i, j), 1 <= i <= sl, 0 <= j < sl (GridGen.F90:98-217 and
+  // special_points, :529-623).  Inside a rhombus and along its j-boundaries
+  // that is the cell before it in its row (index - 1); along the rhombus's
+  // i-boundaries (i = 1 or i = sl) it is the cell of the previous row
+  // (index - sl), which for the first row of a lower rhombus is the last row
+  // of the upper rhombus above it.  Exceptions: the first row's ends in an
+  // upper rhombus (i = 1 next to the north pole starts at the pole, i = sl,
+  // a pentagon, at index - 1) and the pentagon at the end of a lower
+  // rhombus's first row (index - 1).
+  int first_neighbour(int d, int i, int j) const {
+    const bool upper = d < 5;
+    const int idx = base(d) + j * sl + (i - 1);
+    if (upper && i == 1 && j == 0) return 0;  // north pole
+    const bool iedge = (i == 1 || i == sl);
+    const bool first_row_end = (j == 0) && (upper || i == sl);
+    return (iedge && !first_row_end) ? idx - sl : idx - 1;
+  }
+
   // global 0-based index of the closed-rhombus lattice point (d, i, j),
   // 0 <= i, j <= sl; d = 0..4 upper rhombi, 5..9 lower rhombi.
   int owner(int d, int i, int j) const {
@@ -164,12 +195,12 @@ struct Builder {
         if (i == 0 && j == 0) return 0;                     // north pole
         if (i == 0) { d = (k + 1) % 5; i = j; j = 0; continue; }   // edge N-U(k+1)
         if (j == sl) { d = 5 + k; j = 0; continue; }         // edge U(k+1)-L(k)
-        return 1 + d * sl * sl + j * sl + (i - 1);
+        return base(d) + j * sl + (i - 1);
       } else {
         if (i == sl && j == sl) return nip - 1;             // south pole
         if (i == 0) { d = (k + 1) % 5; i = sl; continue; }   // edge U(k+1)-L(k+1)
         if (j == sl) { d = 5 + (k + 1) % 5; j = i; i = sl; continue; }  // edge L(k+1)-S
-        return 1 + d * sl * sl + j * sl + (i - 1);
+        return base(d) + j * sl + (i - 1);
       }
     }
   }
@@ -206,7 +237,7 @@ struct Builder {
     };
     for (int d = 0; d < 10; d++)
       for (int j = 0; j < sl; j++)
-        for (int i = 1; i <= sl; i++) xyz[1 + d * sl * sl + j * sl + (i - 1)] = pos(d, i, j);
+        for (int i = 1; i <= sl; i++) xyz[base(d) + j * sl + (i - 1)] = pos(d, i, j);
 
     // successor map around every vertex from consistently oriented triangles
     std::vector<std::array<int, 12>> succ(nip);  // pairs (b, c): c follows b CCW
@@ -233,14 +264,22 @@ struct Builder {
           add_tri(p00, p10, p01);
           add_tri(p10, p11, p01);
         }
+    // the neighbour each cell's ring starts with
+    std::vector<int> first(nip, -1);
+    first[0] = base(0);                // north pole: first cell of U0
+    first[nip - 1] = base(9) + sl * sl - 1;  // south pole: last cell of L4
+    for (int d = 0; d < 10; d++)
+      for (int j = 0; j < sl; j++)
+        for (int i = 1; i <= sl; i++) first[base(d) + j * sl + (i - 1)] = first_neighbour(d, i, j);
     nprox.assign(nip, 0);
     ring.assign(nip, std::array<int, 6>{-1, -1, -1, -1, -1, -1});
     for (int v = 0; v < nip; v++) {
       int n = nsucc[v];
       if (n != 5 && n != 6) return -1;
-      // start the ring at the smallest neighbour index
-      int start = succ[v][0];
-      for (int q = 1; q < n; q++) start = std::min(start, succ[v][2 * q]);
+      const int start = first[v];
+      bool found = false;
+      for (int q = 0; q < n; q++) found = found || (succ[v][2 * q] == start);
+      if (!found) return -4;
       int cur = start;
       for (int e = 0; e < n; e++) {
         ring[v][e] = cur;

@@ -6,11 +6,14 @@
  * smoke check and the CPU-baseline leg of bench.py as the checker.  The
  * product library never links or calls it.
  *
- * Parity status: UNPINNED.  The reference ships no golden vectors or unit
- * fixtures for this path and cannot be compiled here (Fortran, no compiler);
- * the restatement is pinned only by the reference's own in-code invariants
- * (column-integral conservation in hybgen, FCT positivity/monotonicity,
- * global mass conservation) which the tests check.
+ * Parity status: the floating-point routines are UNPINNED.  The reference
+ * ships no golden vectors or unit fixtures for this path and cannot be
+ * compiled on either machine (Fortran, no compiler); the restatement is
+ * pinned only by the reference's own in-code invariants (column-integral
+ * conservation in hybgen, FCT positivity/monotonicity, global mass
+ * conservation) which the tests check.  The integer grid tables the oracle
+ * and the product read (prox, proxs, nprox) are pinned bit for bit against a
+ * restatement of the reference's grid generator (grid_ref.py).
  *
  * Index conventions: 0-based, reference layout with the level index fastest.
  *   cell field (nvl,nip):        f[i*nvl + k]

@@ -1,7 +1,8 @@
 """ctypes wrapper of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
 
 Used by tests/, __graft_entry__.smoke() and the cpu_baseline / reference arm
-of bench.py as the checker.  Parity status: unpinned (see fim_oracle.h).
+of bench.py as the checker.  Parity status: the routines are unpinned, the
+integer grid tables pinned (see fim_oracle.h).
 Arrays are float64 numpy, flat, in the reference layout.
 """
 import ctypes
