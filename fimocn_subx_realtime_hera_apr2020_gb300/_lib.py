@@ -80,6 +80,7 @@ _SIGS = {
     "fim_state_budget": ([_VP, _VP, _I, _VP, _VP], _I),
     "fim_check": ([_VP, _VP, _VP], _I),
     "fim_launch_count": ([_VP], ctypes.c_int64),
+    "fim_ctx_device_bytes": ([_VP], ctypes.c_int64),
     "fim_tracer_shape": ([_VP, _VP, _VP, _VP], _I),
     "fim_profile_enable": ([_VP, _I], _I),
     "fim_profile_report": ([_VP, ctypes.c_char_p, _I], _I),

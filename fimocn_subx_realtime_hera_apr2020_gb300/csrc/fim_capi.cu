@@ -49,7 +49,8 @@ struct fim_ctx {
   int N = 0, L = 0, T = 0, M = 1;
   size_t esz = 8;
   cudaStream_t stream = nullptr;
-  std::vector<void*> owned;  // device allocations freed at destroy
+  std::vector<void*> owned;          // device allocations freed at destroy
+  std::vector<size_t> owned_bytes;   // their sizes, entry for entry
   Grid<double> gd{};
   Grid<float> gf{};
   Strides str{};
@@ -120,6 +121,7 @@ int dalloc(fim_ctx* c, void** p, size_t bytes) {
     return set_err(c, e == cudaErrorMemoryAllocation ? FIM_ENOMEM : FIM_ECUDA, "cudaMalloc", e);
   }
   c->owned.push_back(*p);
+  c->owned_bytes.push_back(bytes);
   return FIM_OK;
 }
 
@@ -944,6 +946,10 @@ int autotune_impl(fim_ctx* c, fim_state* st) {
 
 }  // namespace
 
+// Device address of the allocation-free cnuity's static scratch array on the
+// current device (defined with fim_cnuity_noalloc below).
+int cnuity_static_addr(fim_ctx* c, unsigned char** out);
+
 // ============================== extern "C" ==================================
 extern "C" {
 
@@ -1070,6 +1076,17 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
     fim_ctx_destroy(c);
     return rc;
   }
+  // Look up the static scratch array of fim_cnuity_noalloc now: under lazy
+  // module loading that lookup loads the module that holds the array and
+  // commits its memory, which is then done while the caller may still
+  // allocate.  A failure is not fatal here (contexts that never call
+  // fim_cnuity_noalloc do not need the array); that entry point retries the
+  // lookup and reports the error.
+  unsigned char* stat = nullptr;
+  if (cnuity_static_addr(c, &stat) != FIM_OK) {
+    cudaGetLastError();
+    c->err.clear();
+  }
   *out = c;
   return FIM_OK;
 }
@@ -1086,6 +1103,12 @@ int fim_ctx_destroy(fim_ctx* c) {
 const char* fim_ctx_last_error(const fim_ctx* c) { return c ? c->err.c_str() : "null context"; }
 void* fim_ctx_stream(fim_ctx* c) { return c ? (void*)c->stream : nullptr; }
 int64_t fim_launch_count(const fim_ctx* c) { return c ? c->launches : -1; }
+int64_t fim_ctx_device_bytes(const fim_ctx* c) {
+  if (!c) return -1;
+  int64_t b = 0;
+  for (size_t q : c->owned_bytes) b += (int64_t)q;
+  return b;
+}
 
 int fim_get_ab(const fim_ctx* c, int* nf, int* of, int* vof, double* ab1, double* ab2, double* ab3) {
   if (!c) return FIM_EINVAL;
@@ -1348,13 +1371,17 @@ int fim_state_free(fim_ctx* c, fim_state* st) {
   if (!c || !st) return FIM_EINVAL;
   cudaStreamSynchronize(c->stream);
   if (st->graph) cudaGraphExecDestroy(st->graph);
-  for (int f = 0; f < FIM_NFIELDS; f++) {
-    for (auto it = c->owned.begin(); it != c->owned.end(); ++it)
-      if (*it == st->f[f]) { cudaFree(*it); c->owned.erase(it); break; }
-  }
-  for (void* extra : {(void*)st->sums, (void*)st->mpf, st->thold})
-    for (auto it = c->owned.begin(); it != c->owned.end(); ++it)
-      if (extra && *it == extra) { cudaFree(*it); c->owned.erase(it); break; }
+  auto release = [c](void* q) {
+    for (size_t k = 0; q && k < c->owned.size(); k++)
+      if (c->owned[k] == q) {
+        cudaFree(q);
+        c->owned.erase(c->owned.begin() + k);
+        c->owned_bytes.erase(c->owned_bytes.begin() + k);
+        return;
+      }
+  };
+  for (int f = 0; f < FIM_NFIELDS; f++) release(st->f[f]);
+  for (void* extra : {(void*)st->sums, (void*)st->mpf, st->thold}) release(extra);
   delete st;
   return FIM_OK;
 }
@@ -1612,6 +1639,8 @@ static __device__ __align__(256) unsigned char g_cnuity_static[kCnuityStaticByte
 std::mutex g_static_mu;
 void* g_static_addr[kStaticMaxDevices] = {};
 
+}  // namespace
+
 // Device address of g_cnuity_static on the current device, looked up once per
 // device (the host-side name is only a handle for the runtime, not an address).
 int cnuity_static_addr(fim_ctx* c, unsigned char** out) {
@@ -1629,6 +1658,8 @@ int cnuity_static_addr(fim_ctx* c, unsigned char** out) {
   *out = (unsigned char*)g_static_addr[dev];
   return FIM_OK;
 }
+
+namespace {
 
 size_t round256(size_t b) { return (b + 255) / 256 * 256; }
 

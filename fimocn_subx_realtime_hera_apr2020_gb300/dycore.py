@@ -67,6 +67,10 @@ class Dycore:
     def launches(self):
         return self.lib.fim_launch_count(self.ctx)
 
+    def device_bytes(self):
+        """Device memory the context and its states currently own."""
+        return self.lib.fim_ctx_device_bytes(self.ctx)
+
     def profile(self, on):
         _lib.check(self.lib.fim_profile_enable(self.ctx, 1 if on else 0), "fim_profile_enable", self.ctx)
 

@@ -126,6 +126,10 @@ int fim_ctx_destroy(fim_ctx *ctx);
 const char *fim_ctx_last_error(const fim_ctx *ctx);
 /* device stream the context launches on (a cudaStream_t) */
 void *fim_ctx_stream(fim_ctx *ctx);
+/* bytes of device memory the context (and its states) currently own: grid
+ * tables, state fields and every scratch buffer allocated so far (no
+ * counterpart in the reference, which allocates host arrays) */
+int64_t fim_ctx_device_bytes(const fim_ctx *ctx);
 /* AB3 slots (Fortran numbering 1..3) and weights of the context */
 int fim_get_ab(const fim_ctx *ctx, int *nf, int *of, int *vof, double *ab1, double *ab2, double *ab3);
 int fim_set_ab(fim_ctx *ctx, int nf, int of, int vof, double ab1, double ab2, double ab3);
@@ -193,10 +197,14 @@ int fim_cnuity_r4(fim_ctx *ctx, int its, const float *u_velo, const float *v_vel
  * pointers; host_pointers contexts are rejected.  Like those, it advances
  * member 0.  The scratch takes 11 x nip x nvl values: glvl 5 / nvl 64 fits in
  * FP64, glvl 6 / nvl 64 does not fit in either precision and is rejected with
- * FIM_EINVAL.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress) and should come before any stream
- * capture.  All calls on a device share the array: calls whose kernels
- * overlap on the GPU race. */
+ * FIM_EINVAL.  fim_ctx_create looks up the array's device address
+ * (cudaGetSymbolAddress) on its device; under lazy module loading that is
+ * when the module holding the array loads and its 64 MiB are committed, so
+ * a caller that creates its contexts during start-up allocates nothing
+ * later.  If that lookup failed, the first fim_cnuity_noalloc call on the
+ * device retries it; that call should then come before any stream capture.
+ * All calls on a device share the array: calls whose kernels overlap on the
+ * GPU race. */
 int fim_cnuity_noalloc(fim_ctx *ctx, int its, const void *u_velo, const void *v_velo,
                        const void *u_edg, const void *v_edg, const void *dp_edg,
                        const void *lp_edg, void *delp, void *pres, void *exner,
