@@ -470,7 +470,9 @@ def accuracy_arm(args, ws, rank, local):
     for prec in ("f64", "f32"):
         d = F.Dycore(grid, mk(prec))
         st = d.state()
-        st.load({k: v.astype(mk(prec).dtype) for k, v in host.items()})
+        # the FP64 fields as given: an FP32-mixed state keeps them for its
+        # FP64 initial adjustment (fim_state_upload_f64)
+        st.load(host)
         st.init()
         runs[prec] = (d, st)
     ref = None

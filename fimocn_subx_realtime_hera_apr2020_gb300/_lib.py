@@ -67,6 +67,7 @@ _SIGS = {
     "fim_state_field": ([_VP, _VP, _I, _I, _VP, _VP], _I),
     "fim_state_upload": ([_VP, _VP, _I, _I, _VP], _I),
     "fim_state_download": ([_VP, _VP, _I, _I, _VP], _I),
+    "fim_state_upload_f64": ([_VP, _VP, _I, _I, _VP], _I),
     "fim_state_upload_slot": ([_VP, _VP, _I, _I, _I, _VP], _I),
     "fim_state_download_slot": ([_VP, _VP, _I, _I, _I, _VP], _I),
     "fim_state_init": ([_VP, _VP], _I),

@@ -39,6 +39,9 @@ struct fim_state {
   double* sums = nullptr;          // [M][8+T]
   float2* mpf = nullptr;           // FP32-mixed: float-float Montgomery potential [M][nvl*nip]
   void* thold = nullptr;           // FP32-mixed: theta seen by edgvar1 this step [M][nvl*nip]
+  // FP32-mixed: FP64 copies of initial fields (fim_state_upload_f64), held
+  // until the member's initial adjustment consumes them; [field * M + member]
+  std::vector<double*> init64;
   cudaGraphExec_t graph = nullptr;
   long long graph_kernels = 0;
 };
@@ -123,6 +126,46 @@ int dalloc(fim_ctx* c, void** p, size_t bytes) {
   c->owned.push_back(*p);
   c->owned_bytes.push_back(bytes);
   return FIM_OK;
+}
+
+// frees a buffer dalloc gave out (no-op for null or unknown pointers)
+void dfree(fim_ctx* c, void* p) {
+  for (size_t k = 0; p && k < c->owned.size(); k++)
+    if (c->owned[k] == p) {
+      cudaFree(p);
+      c->owned.erase(c->owned.begin() + k);
+      c->owned_bytes.erase(c->owned_bytes.begin() + k);
+      return;
+    }
+}
+
+// element-wise precision changes between the FP32-mixed state and FP64 work
+// arrays
+__global__ void k_widen(const float* __restrict__ a, double* __restrict__ b, size_t n) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    b[q] = (double)a[q];
+}
+__global__ void k_narrow(const double* __restrict__ a, float* __restrict__ b, size_t n) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    b[q] = (float)a[q];
+}
+// x -> nearest float hi and the float nearest to the remainder: hi + lo
+// carries x to ~48 bits (the float-float Montgomery potential)
+__global__ void k_split(const double* __restrict__ a, float2* __restrict__ b, size_t n) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    const double x = a[q];
+    const float hi = (float)x;
+    b[q] = make_float2(hi, (float)(x - (double)hi));
+  }
+}
+// x -> the FP32 value the state will hold, kept in FP64
+__global__ void k_round_f32(double* __restrict__ a, size_t n) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    a[q] = (double)(float)a[q];
+}
+dim3 conv_grid(size_t n) {
+  const size_t b = (n + 255) / 256;
+  return dim3((unsigned)(b < 152 * 16 ? (b ? b : 1) : 152 * 16));
 }
 
 template <typename R>
@@ -878,6 +921,89 @@ int ensure_all(fim_ctx* c) {
 template <typename R>
 R* FM(fim_ctx* c, fim_state* st, int f, int m) { return (R*)st->f[f] + (size_t)m * st->count[f]; }
 
+// The initial fields dyn_init's adjustment reads (besides the state it
+// recomputes): winds, thicknesses, pressures, Exner function, surface
+// geopotential (ph3d's bottom interface) and tracers.
+bool init_input(int f) {
+  return f == FIM_US3D || f == FIM_VS3D || f == FIM_DP3D || f == FIM_PR3D || f == FIM_EX3D || f == FIM_PH3D ||
+         f == FIM_TR3D;
+}
+
+// dyn_init.F90:870-906,1037 for member m of an FP32-mixed state, in FP64:
+// hybgen, the pressures and thicknesses of the new interfaces and hystat run
+// on FP64 copies of the member's fields (the fim_state_upload_f64 copies
+// where given, else the FP32 fields widened), and the results are rounded
+// into the state once; hystat runs on the rounded tracers and thicknesses,
+// and the Montgomery potential keeps its float-float pair.
+// Run once per member, so the state a forecast starts from does not carry
+// the FP32 rounding of the adjustment's column arithmetic (the Exner
+// function in particular, which the pressure gradient sees through the
+// Montgomery potential).
+int adjust_member_f64(fim_ctx* c, fim_state* st, int m) {
+  const int used[] = {FIM_US3D, FIM_VS3D, FIM_DP3D, FIM_PR3D, FIM_EX3D, FIM_PH3D,
+                      FIM_MP3D, FIM_TR3D, FIM_TRDP, FIM_SDOT, FIM_PSRF, FIM_PTDCY};
+  const size_t NI = (size_t)c->N * (c->L + 1);
+  size_t total = 2 * NI;  // hybgen's two smoothed-interface scratch arrays
+  for (int f : used) total += st->count[f];
+  void* blk = nullptr;
+  int rc = dalloc(c, &blk, total * sizeof(double));
+  if (rc) return rc;
+  double* w[FIM_NFIELDS] = {};
+  double* q = (double*)blk;
+  for (int f : used) {
+    w[f] = q;
+    q += st->count[f];
+  }
+  HybgenScratch<double> hw{q, q + NI};
+  cudaStream_t str = c->stream;
+  for (int f : used) {
+    const size_t n = st->count[f];
+    float* src = (float*)st->f[f] + (size_t)m * n;
+    double* staged = st->init64[(size_t)f * c->M + m];
+    if (staged)
+      CK(cudaMemcpyAsync(w[f], staged, n * sizeof(double), cudaMemcpyDeviceToDevice, str), "adjustment input");
+    else
+      k_widen<<<conv_grid(n), 256, 0, str>>>(src, w[f], n);
+  }
+  const int e = prepare_hybgen<double>(c->L);
+  if (e) { dfree(c, blk); return set_err(c, FIM_ECUDA, "hybgen kernel attributes", (cudaError_t)e); }
+  Launch l = make_launch(c, 1);
+  l.sp = c->d_sp + m;
+  l.flags = c->d_flags + m;
+  Grid<double>& g = c->gd;
+  launch_hybgen<double>(l, g, c->str, c->kn, hw, g.thetac, w[FIM_US3D], w[FIM_VS3D], w[FIM_TR3D], w[FIM_SDOT],
+                        w[FIM_EX3D], w[FIM_DP3D], w[FIM_PR3D]);
+  launch_prdp_from_ex<double>(l, g, c->str, w[FIM_EX3D], w[FIM_PR3D], w[FIM_DP3D]);
+  // hystat then sees the potential temperature, tracers, thicknesses and
+  // surface geopotential the FP32 state will hold: the Montgomery potential
+  // is exact for that theta, so the step's pressure gradient -grad(M) +
+  // Pi grad(theta) does not pick up theta's rounding (x Pi ~ 1000) as a
+  // force.  The Exner function stays FP64 here.
+  for (int f : {FIM_TR3D, FIM_DP3D, FIM_PH3D})
+    k_round_f32<<<conv_grid(st->count[f]), 256, 0, str>>>(w[f], st->count[f]);
+  CK(cudaMemsetAsync(w[FIM_PSRF], 0, st->count[FIM_PSRF] * sizeof(double), str), "zero psrf");
+  CK(cudaMemsetAsync(w[FIM_PTDCY], 0, st->count[FIM_PTDCY] * sizeof(double), str), "zero ptdcy");
+  launch_hystat<double>(l, g, c->str, w[FIM_PH3D], w[FIM_EX3D], w[FIM_MP3D], w[FIM_DP3D], w[FIM_TR3D],
+                        w[FIM_TRDP], w[FIM_PSRF], w[FIM_PTDCY]);
+  for (int f : used) {
+    const size_t n = st->count[f];
+    k_narrow<<<conv_grid(n), 256, 0, str>>>(w[f], (float*)st->f[f] + (size_t)m * n, n);
+  }
+  const size_t nm = st->count[FIM_MP3D];
+  k_split<<<conv_grid(nm), 256, 0, str>>>(w[FIM_MP3D], st->mpf + (size_t)m * nm, nm);
+  if ((rc = check_launch(c, "FP64 initial adjustment"))) return rc;
+  // the work arrays and the member's FP64 inputs are released once the
+  // kernels reading them are done
+  CK(cudaStreamSynchronize(str), "FP64 initial adjustment");
+  dfree(c, blk);
+  for (int f = 0; f < FIM_NFIELDS; f++) {
+    double*& p = st->init64[(size_t)f * c->M + m];
+    dfree(c, p);
+    p = nullptr;
+  }
+  return FIM_OK;
+}
+
 // dyn_init.F90:870-906,1037-1094 for members [m0, m0+nm)
 template <typename R>
 int state_init_impl(fim_ctx* c, fim_state* st, int m0, int nm) {
@@ -894,13 +1020,18 @@ int state_init_impl(fim_ctx* c, fim_state* st, int m0, int nm) {
   Grid<R>& g = grid_of<R>(c);
   HybgenScratch<R> hw{(R*)c->exsmo, (R*)c->exsmo2};
   auto P = [&](int f) { return FM<R>(c, st, f, m0); };
-  launch_hybgen<R>(l, g, c->str, c->kn, hw, g.thetac, P(FIM_US3D), P(FIM_VS3D), P(FIM_TR3D), P(FIM_SDOT),
-                   P(FIM_EX3D), P(FIM_DP3D), P(FIM_PR3D));
-  launch_prdp_from_ex<R>(l, g, c->str, P(FIM_EX3D), P(FIM_PR3D), P(FIM_DP3D));
-  CK(cudaMemsetAsync(P(FIM_PSRF), 0, nm * st->count[FIM_PSRF] * c->esz, c->stream), "zero psrf");
-  CK(cudaMemsetAsync(P(FIM_PTDCY), 0, nm * st->count[FIM_PTDCY] * c->esz, c->stream), "zero ptdcy");
-  launch_hystat<R>(l, g, c->str, P(FIM_PH3D), P(FIM_EX3D), P(FIM_MP3D), P(FIM_DP3D), P(FIM_TR3D), P(FIM_TRDP),
-                   P(FIM_PSRF), P(FIM_PTDCY), st->mpf ? st->mpf + (size_t)m0 * st->count[FIM_MP3D] : nullptr);
+  if constexpr (sizeof(R) == 4) {
+    for (int m = m0; m < m0 + nm; m++)
+      if ((rc = adjust_member_f64(c, st, m))) return rc;
+  } else {
+    launch_hybgen<R>(l, g, c->str, c->kn, hw, g.thetac, P(FIM_US3D), P(FIM_VS3D), P(FIM_TR3D), P(FIM_SDOT),
+                     P(FIM_EX3D), P(FIM_DP3D), P(FIM_PR3D));
+    launch_prdp_from_ex<R>(l, g, c->str, P(FIM_EX3D), P(FIM_PR3D), P(FIM_DP3D));
+    CK(cudaMemsetAsync(P(FIM_PSRF), 0, nm * st->count[FIM_PSRF] * c->esz, c->stream), "zero psrf");
+    CK(cudaMemsetAsync(P(FIM_PTDCY), 0, nm * st->count[FIM_PTDCY] * c->esz, c->stream), "zero ptdcy");
+    launch_hystat<R>(l, g, c->str, P(FIM_PH3D), P(FIM_EX3D), P(FIM_MP3D), P(FIM_DP3D), P(FIM_TR3D), P(FIM_TRDP),
+                     P(FIM_PSRF), P(FIM_PTDCY));
+  }
   if (c->TB > 0)  // dyn_init.F90:1096-1097
     launch_transp0<R>(l, g, c->str, 0, P(FIM_CUMUFX), P(FIM_DP3D), P(FIM_DPINIT));
   const int zero[] = {FIM_U_TDCY, FIM_V_TDCY, FIM_DP_TDCY, FIM_DPL_TDCY, FIM_TRC_TDCY, FIM_TRL_TDCY, FIM_MASSFX};
@@ -1061,9 +1192,11 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
     delete c;
     return FIM_ECUDA;
   }
-  int rc = (c->prec == FIM_PREC_F64)
-               ? build_grid<double>(c, g, rarea, corio, grnd, dfflen, biharw, smoo, prox, proxs, nprox)
-               : build_grid<float>(c, g, rarea, corio, grnd, dfflen, biharw, smoo, prox, proxs, nprox);
+  // FP64 tables in both precisions: the FP32-mixed build runs the one-time
+  // initial adjustment (hybgen, pressures, hystat) in FP64
+  int rc = build_grid<double>(c, g, rarea, corio, grnd, dfflen, biharw, smoo, prox, proxs, nprox);
+  if (!rc && c->prec == FIM_PREC_F32)
+    rc = build_grid<float>(c, g, rarea, corio, grnd, dfflen, biharw, smoo, prox, proxs, nprox);
   if (!rc) rc = dalloc(c, (void**)&c->d_sp, sizeof(StepParams) * c->M);
   if (!rc) rc = dalloc(c, (void**)&c->d_flags, sizeof(int) * c->M);
   if (!rc) {
@@ -1356,6 +1489,7 @@ int fim_state_alloc(fim_ctx* c, fim_state** out) {
   }
   int rc = dalloc(c, (void**)&st->sums, (size_t)c->M * (8 + c->T + c->TB) * sizeof(double));
   if (rc) { delete st; return rc; }
+  st->init64.assign((size_t)FIM_NFIELDS * c->M, nullptr);
   if (c->prec == FIM_PREC_F32) {
     if ((rc = dalloc(c, (void**)&st->mpf, (size_t)c->M * cnt[FIM_MP3D] * sizeof(float2)))) { delete st; return rc; }
     if ((rc = dalloc(c, &st->thold, (size_t)c->G * cnt[FIM_MP3D] * c->esz))) { delete st; return rc; }
@@ -1371,17 +1505,9 @@ int fim_state_free(fim_ctx* c, fim_state* st) {
   if (!c || !st) return FIM_EINVAL;
   cudaStreamSynchronize(c->stream);
   if (st->graph) cudaGraphExecDestroy(st->graph);
-  auto release = [c](void* q) {
-    for (size_t k = 0; q && k < c->owned.size(); k++)
-      if (c->owned[k] == q) {
-        cudaFree(q);
-        c->owned.erase(c->owned.begin() + k);
-        c->owned_bytes.erase(c->owned_bytes.begin() + k);
-        return;
-      }
-  };
-  for (int f = 0; f < FIM_NFIELDS; f++) release(st->f[f]);
-  for (void* extra : {(void*)st->sums, (void*)st->mpf, st->thold}) release(extra);
+  for (int f = 0; f < FIM_NFIELDS; f++) dfree(c, st->f[f]);
+  for (void* extra : {(void*)st->sums, (void*)st->mpf, st->thold}) dfree(c, extra);
+  for (double* p : st->init64) dfree(c, p);
   delete st;
   return FIM_OK;
 }
@@ -1402,6 +1528,22 @@ int fim_state_upload(fim_ctx* c, fim_state* st, int field, int member, const voi
   if (rc) return rc;
   CK(cudaMemcpyAsync(d, host, (size_t)n * c->esz, cudaMemcpyHostToDevice, c->stream), "state upload");
   return FIM_OK;
+}
+
+int fim_state_upload_f64(fim_ctx* c, fim_state* st, int field, int member, const double* host) {
+  if (!c || !st || !host) return FIM_EINVAL;
+  if (c->prec == FIM_PREC_F64) return fim_state_upload(c, st, field, member, host);
+  if (!init_input(field))
+    return set_err(c, FIM_EINVAL, "fim_state_upload_f64 takes the initial fields us3d vs3d dp3d pr3d ex3d ph3d tr3d");
+  void* d;
+  int64_t n;
+  int rc = fim_state_field(c, st, field, member, &d, &n);
+  if (rc) return rc;
+  double*& s = st->init64[(size_t)field * c->M + member];
+  if (!s && (rc = dalloc(c, (void**)&s, (size_t)n * sizeof(double)))) return rc;
+  CK(cudaMemcpyAsync(s, host, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream), "state upload f64");
+  k_narrow<<<conv_grid((size_t)n), 256, 0, c->stream>>>(s, (float*)d, (size_t)n);
+  return check_launch(c, "state upload f64");
 }
 
 int fim_state_download(fim_ctx* c, fim_state* st, int field, int member, void* host) {

@@ -64,7 +64,7 @@ __device__ void restp_1d(R* thold, const R* pkold, int kold, R* pknew, const R* 
     tk = tk1;
   }
   cloutt = cloutt + thL * (pknew[knew] - pknew[knew - 1]);
-  if (sizeof(R) == 8 && cabs(cloutt - colint) > cmax(R(1.e-33), R(1.e-6) * colscl)) *bad = 1;
+  if (cabs(cloutt - colint) > cmax(R(1.e-33), col_tol<R>(1.e-6) * colscl)) *bad = 1;
 }
 
 // equilb scenario 1 (hybgen.F90:1316-1363); in place on pres
@@ -336,7 +336,7 @@ __device__ bool pcwise(int kk, const R* xold, const R* yold, const R* xnew, R* y
     ynew[k] = (amount + fldnew[k] * small) / (fcn[k] + small);
     after = after + amount;
   }
-  return sizeof(R) == 8 && cabs(bfore - after) > cmax(R(1.e-33), R(1.e-11) * colscl);
+  return cabs(bfore - after) > cmax(R(1.e-33), col_tol<R>(1.e-11) * colscl);
 }
 
 // A warp's 32 columns (lane = column) move between global memory and the
@@ -539,14 +539,14 @@ __global__ void __launch_bounds__(kColBlock) k_remap(Grid<R> g, Strides s, Knobs
         ynew[k - 1] = thb + cmin(devilo, -deviup) / dpup;
       }
     }
-    if (sizeof(R) == 8) {
+    {
       R colin = R(0), clout = R(0), colscl = R(0);
       for (int k = 0; k < L; k++) {
         colin = colin + yold[k] * (pk1col[k] - pk1col[k + 1]);
         clout = clout + ynew[k] * (pk1new[k] - pk1new[k + 1]);
         colscl = colscl + cabs(yold[k] * (pk1col[k] - pk1col[k + 1]));
       }
-      if (cabs(clout - colin) > cmax(R(1.e-33), R(2.e-6) * colscl)) bad = true;
+      if (cabs(clout - colin) > cmax(R(1.e-33), col_tol<R>(2.e-6) * colscl)) bad = true;
     }
     for (int k = 0; k < L; k++) col[k] = ynew[k];
   }
@@ -736,7 +736,7 @@ __device__ __forceinline__ bool pcwise_v(int L, int lane, R (&y)[NF][VL], const 
   const R small = R(1.e-22);
   const int kb = lane * VL;
   R bfore[NF], colscl[NF];
-  if (sizeof(R) == 8) {
+  {
 #pragma unroll
     for (int h = 0; h < NF; h++) {
       bfore[h] = R(0);
@@ -844,9 +844,9 @@ __device__ __forceinline__ bool pcwise_v(int L, int lane, R (&y)[NF][VL], const 
         y[h][v] = (amount + yf[h][v] * small) * G.rfn[v];
       }
     }
-    if (sizeof(R) == 8) {
+    {
       const R dif = warp_sum<R, W>(bfore[h] - after), scl = warp_sum<R, W>(colscl[h]);
-      bad |= cabs(dif) > cmax(R(1.e-33), R(1.e-11) * scl);
+      bad |= cabs(dif) > cmax(R(1.e-33), col_tol<R>(1.e-11) * scl);
     }
   }
   return bad;
@@ -1115,7 +1115,7 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
       {
         LaneGeo<R, VL> gk;
         lane_geo<R, VL, WL>(L, ls, S.pk1col[hw], S.pk1new[hw], gk);
-        if (sizeof(R) == 8) {
+        {
           R colin = R(0), colscl = R(0);
 #pragma unroll
           for (int v = 0; v < VL; v++)
@@ -1270,10 +1270,10 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
       thb = na;
     }
     th[1] = thb;
-    if (sizeof(R) == 8) {
+    {
       R clout = R(0);
       for (int k = 0; k < L; k++) clout = clout + th[k] * dk[k];
-      if (cabs(clout - S.colin[lane]) > cmax(R(1.e-33), R(2.e-6) * S.colscl[lane])) bad = true;
+      if (cabs(clout - S.colin[lane]) > cmax(R(1.e-33), col_tol<R>(2.e-6) * S.colscl[lane])) bad = true;
     }
   }
   __syncwarp();

@@ -292,9 +292,30 @@ class DycoreState:
         _, nf, of, vof, _ = self.get_step(member)
         return nf % 3 + 1, of % 3 + 1, vof % 3 + 1
 
+    # fields dyn_init's adjustment reads; FP64 arrays of these go to an
+    # FP32-mixed state through fim_state_upload_f64
+    INIT_INPUTS = ("us3d", "vs3d", "dp3d", "pr3d", "ex3d", "ph3d", "tr3d")
+
+    def upload_f64(self, name, host, member=0):
+        """FP64 initial field: the FP32 copy is set and the FP64 values feed
+        the next initial adjustment (fim_state_upload_f64)."""
+        ptr, n = self.field_ptr(name, member)
+        host = np.ascontiguousarray(host, dtype=np.float64)
+        if host.size != n:
+            raise ValueError("%s: %d elements, expected %d" % (name, host.size, n))
+        _lib.check(self.lib.fim_state_upload_f64(self.dyc.ctx, self.st, _lib.FIELD_ID[name], member, _ptr(host)),
+                   "fim_state_upload_f64", self.dyc.ctx)
+        self.dyc.sync()
+
     def load(self, fields, member=0):
+        """Upload a member's fields; FP64 arrays of the initial fields keep
+        their precision for the initial adjustment of an FP32-mixed state."""
+        f32 = self.dyc.cfg.precision != "f64"
         for k, v in fields.items():
-            self.upload(k, v, member)
+            if f32 and k in self.INIT_INPUTS and isinstance(v, np.ndarray) and v.dtype == np.float64:
+                self.upload_f64(k, v, member)
+            else:
+                self.upload(k, v, member)
 
     def init(self):
         _lib.check(self.lib.fim_state_init(self.dyc.ctx, self.st), "fim_state_init", self.dyc.ctx)

@@ -339,6 +339,17 @@ int fim_state_field(fim_ctx *ctx, fim_state *st, int field, int member, void **d
 /* host <-> device copy of one member's field (element type per precision) */
 int fim_state_upload(fim_ctx *ctx, fim_state *st, int field, int member, const void *host);
 int fim_state_download(fim_ctx *ctx, fim_state *st, int field, int member, void *host);
+/* FP64 initial field for an FP32-mixed state (no counterpart in the
+ * reference, whose -r4 build reads its initial state in real*4): the field's
+ * FP32 copy is set as by fim_state_upload, and the FP64 values are kept
+ * until fim_state_init / fim_state_init_member, whose initial adjustment
+ * (hybgen, pressures from the Exner function, hystat) then starts from them.
+ * That adjustment runs in FP64 in both precisions; fields given only in FP32
+ * enter it widened.  Only the fields the adjustment reads are taken: us3d,
+ * vs3d, dp3d, pr3d, ex3d, ph3d (its bottom interface, the surface
+ * geopotential) and tr3d; FIM_EINVAL otherwise.  In an FP64 context this is
+ * fim_state_upload. */
+int fim_state_upload_f64(fim_ctx *ctx, fim_state *st, int field, int member, const double *host);
 /* The same for one AB3 slot (1..3, Fortran numbering) of a tendency field
  * (u_tdcy, v_tdcy, dp_tdcy, dpl_tdcy: one nvl x nip block per slot; trc_tdcy,
  * trl_tdcy: one per tracer).  host holds the whole field as for
@@ -351,7 +362,10 @@ int fim_state_upload_slot(fim_ctx *ctx, fim_state *st, int field, int member, in
 int fim_state_download_slot(fim_ctx *ctx, fim_state *st, int field, int member, int slot, void *host);
 
 /* dyn_init.F90:870-906,1037-1094 for every member: trdp, hybgen(its=0),
- * pressure/thickness from Exner, hystat(its=0), zero tendencies, AB3 slots */
+ * pressure/thickness from Exner, hystat(its=0), zero tendencies, AB3 slots.
+ * In an FP32-mixed context the adjustment (hybgen to hystat) runs in FP64 on
+ * the member's fields (see fim_state_upload_f64) and its results are rounded
+ * into the state once, the Montgomery potential into its float-float pair. */
 int fim_state_init(fim_ctx *ctx, fim_state *st);
 
 /* One dyn_run iteration of every member (dyn_run.F90:119-425): hybgen and
