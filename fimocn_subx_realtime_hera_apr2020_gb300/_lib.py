@@ -73,6 +73,8 @@ _SIGS = {
     "fim_state_init": ([_VP, _VP], _I),
     "fim_step": ([_VP, _VP, _I, _I], _I),
     "fim_step_active": ([_VP, _VP, _I], _I),
+    "fim_state_set_host": ([_VP, _VP, _I, _I, _VP], _I),
+    "fim_step_io": ([_VP, _VP, _I, _VP, _VP], _I),
     "fim_state_init_member": ([_VP, _VP, _I], _I),
     "fim_member_set_active": ([_VP, _VP, _I, _I], _I),
     "fim_member_its": ([_VP, _I], _I),

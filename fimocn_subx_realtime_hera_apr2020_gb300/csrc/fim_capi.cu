@@ -42,6 +42,8 @@ struct fim_state {
   // FP32-mixed: FP64 copies of initial fields (fim_state_upload_f64), held
   // until the member's initial adjustment consumes them; [field * M + member]
   std::vector<double*> init64;
+  // host buffers of fim_step_io, [field * M + member]
+  std::vector<void*> host;
   cudaGraphExec_t graph = nullptr;
   long long graph_kernels = 0;
 };
@@ -52,6 +54,9 @@ struct fim_ctx {
   int N = 0, L = 0, T = 0, M = 1;
   size_t esz = 8;
   cudaStream_t stream = nullptr;
+  // fim_step_io's copy streams (host to device, device to host) and events
+  cudaStream_t io_in = nullptr, io_out = nullptr;
+  std::vector<cudaEvent_t> io_ev;
   std::vector<void*> owned;          // device allocations freed at destroy
   std::vector<size_t> owned_bytes;   // their sizes, entry for entry
   Grid<double> gd{};
@@ -814,12 +819,171 @@ bool group_field(int f) {
 template <typename R>
 R* F(fim_state* st, int f) { return (R*)st->f[f]; }
 
+// ---- the step with host transfers (fim_step_io) ------------------------------
+// Each field a caller keeps on the host goes up before the first kernel that
+// reads or writes it and comes down once its last writer of the step is done,
+// on two copy streams beside the compute stream.  Stages of the step, in
+// dyn_run order: A = hybgen + hystat (of the previous step) and the edge
+// interpolation; C = cnuity or mass_adv (+ class-B transport); T = the tracer
+// transport, chunk by chunk; U = momtum; E = the budget sums.
+enum IoStage { kIoNone = 0, kIoA, kIoC, kIoT, kIoU, kIoE };
+struct IoClass {
+  int up;     // stage before which the field must be on the device (kIoNone: output only)
+  int down;   // stage after which it is final
+  bool ab3;   // AB3 tendency field: slots of, vof up, slot nf down
+};
+
+bool io_class(int f, IoClass* k) {
+  switch (f) {
+    case FIM_US3D: case FIM_VS3D: *k = {kIoA, kIoU, false}; return true;
+    case FIM_DP3D: case FIM_PR3D: case FIM_EX3D: case FIM_MASSFX: *k = {kIoA, kIoC, false}; return true;
+    // hystat writes one of ptdcy's two time levels a step: the other goes up too
+    case FIM_PH3D: case FIM_MP3D: case FIM_PSRF: case FIM_PTDCY: *k = {kIoA, kIoA, false}; return true;
+    case FIM_TR3D: case FIM_TRDP: *k = {kIoA, kIoT, false}; return true;
+    case FIM_CUMUFX: case FIM_DPINIT: *k = {kIoA, kIoE, false}; return true;
+    case FIM_SDOT: *k = {kIoNone, kIoA, false}; return true;
+    case FIM_WS3D: *k = {kIoNone, kIoC, false}; return true;
+    case FIM_RELVOR: *k = {kIoNone, kIoU, false}; return true;
+    case FIM_DP_TDCY: case FIM_DPL_TDCY: *k = {kIoC, kIoC, true}; return true;
+    case FIM_TRC_TDCY: case FIM_TRL_TDCY: *k = {kIoT, kIoT, true}; return true;
+    case FIM_U_TDCY: case FIM_V_TDCY: *k = {kIoU, kIoU, true}; return true;
+    default: return false;  // the edge work fields live on the device only
+  }
+}
+
+struct StepIo {
+  fim_ctx* c = nullptr;
+  fim_state* st = nullptr;
+  std::vector<int> nf, of;  // per member, 0-based slots of the step (after its abstart)
+  std::vector<int> vof;
+  int tchunk = 1;
+  int nev = 0;              // events handed out
+  int64_t h2d = 0, d2h = 0;
+  cudaEvent_t up_ev[kIoE + 1] = {};
+  std::vector<cudaEvent_t> up_chunk;  // per tracer chunk
+  int rc = FIM_OK;
+  ChunkHook hook;
+};
+
+cudaEvent_t io_event(StepIo& io) {
+  fim_ctx* c = io.c;
+  if (io.nev == (int)c->io_ev.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+    c->io_ev.push_back(e);
+  }
+  return c->io_ev[io.nev++];
+}
+
+// copy of one member's field: whole (slot < 0, tracers [t0, t0+nt) for the
+// tracer fields) or one AB3 slot of tracers [t0, t0+nt)
+int io_copy(StepIo& io, int f, int m, int slot, int t0, int nt, bool up) {
+  fim_ctx* c = io.c;
+  fim_state* st = io.st;
+  char* h = (char*)st->host[(size_t)f * c->M + m];
+  if (!h) return FIM_OK;
+  char* d = (char*)st->f[f] + (size_t)m * st->count[f] * c->esz;
+  const size_t blk = (size_t)c->N * c->L * c->esz;
+  cudaStream_t q = up ? c->io_in : c->io_out;
+  const cudaMemcpyKind kind = up ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+  cudaError_t e;
+  size_t bytes;
+  if (slot >= 0) {  // nt blocks of nvl x nip values, pitch three blocks
+    const size_t off = ((size_t)t0 * 3 + slot) * blk;
+    e = up ? cudaMemcpy2DAsync(d + off, 3 * blk, h + off, 3 * blk, blk, nt, kind, q)
+           : cudaMemcpy2DAsync(h + off, 3 * blk, d + off, 3 * blk, blk, nt, kind, q);
+    bytes = blk * nt;
+  } else {
+    size_t off = 0, n = st->count[f] * c->esz;
+    if (f == FIM_TR3D || f == FIM_TRDP) {
+      off = (size_t)t0 * blk;
+      n = (size_t)nt * blk;
+    }
+    e = up ? cudaMemcpyAsync(d + off, h + off, n, kind, q) : cudaMemcpyAsync(h + off, d + off, n, kind, q);
+    bytes = n;
+  }
+  if (e != cudaSuccess) return set_err(c, FIM_ECUDA, up ? "step io upload" : "step io download", e);
+  (up ? io.h2d : io.d2h) += (int64_t)bytes;
+  return FIM_OK;
+}
+
+// uploads needed before stage `stage` (tracers [t0, t0+nt) for kIoT), then an
+// event the compute stream waits on
+int io_upload(StepIo& io, int stage, int t0, int nt, cudaEvent_t* done) {
+  fim_ctx* c = io.c;
+  int rc;
+  for (int f = 0; f < FIM_NFIELDS; f++) {
+    IoClass k;
+    if (!io_class(f, &k) || k.up != stage) continue;
+    for (int m = 0; m < c->M; m++) {
+      if (k.ab3) {
+        const int n = (f == FIM_TRC_TDCY || f == FIM_TRL_TDCY) ? nt : 1, a = n == 1 && stage != kIoT ? 0 : t0;
+        if ((rc = io_copy(io, f, m, io.of[m], a, n, true))) return rc;
+        if ((rc = io_copy(io, f, m, io.vof[m], a, n, true))) return rc;
+      } else if ((rc = io_copy(io, f, m, -1, 0, c->T + c->TB, true))) {
+        return rc;
+      }
+    }
+  }
+  *done = io_event(io);
+  if (!*done) return set_err(c, FIM_ECUDA, "step io event");
+  CK(cudaEventRecord(*done, c->io_in), "step io record");
+  return FIM_OK;
+}
+
+// downloads of the fields final after stage `stage`, behind the compute
+// stream's work so far
+int io_download(StepIo& io, int stage, int t0, int nt) {
+  fim_ctx* c = io.c;
+  cudaEvent_t e = io_event(io);
+  if (!e) return set_err(c, FIM_ECUDA, "step io event");
+  CK(cudaEventRecord(e, c->stream), "step io record");
+  CK(cudaStreamWaitEvent(c->io_out, e, 0), "step io wait");
+  int rc;
+  for (int f = 0; f < FIM_NFIELDS; f++) {
+    IoClass k;
+    if (!io_class(f, &k)) continue;
+    // class-B tracers (after the class-A ones) come down with the budgets
+    const bool trf = f == FIM_TR3D || f == FIM_TRDP;
+    const bool here = k.down == stage || (trf && stage == kIoE && c->TB > 0);
+    if (!here) continue;
+    for (int m = 0; m < c->M; m++) {
+      if (k.ab3) {
+        const int n = (f == FIM_TRC_TDCY || f == FIM_TRL_TDCY) ? nt : 1, a = n == 1 && stage != kIoT ? 0 : t0;
+        if ((rc = io_copy(io, f, m, io.nf[m], a, n, false))) return rc;
+      } else if (trf) {
+        const int a = stage == kIoE ? c->T : t0, n = stage == kIoE ? c->TB : nt;
+        if ((rc = io_copy(io, f, m, -1, a, n, false))) return rc;
+      } else if ((rc = io_copy(io, f, m, -1, 0, 0, false))) {
+        return rc;
+      }
+    }
+  }
+  return FIM_OK;
+}
+
+int io_wait(StepIo& io, cudaEvent_t e) {
+  fim_ctx* c = io.c;
+  CK(cudaStreamWaitEvent(c->stream, e, 0), "step io wait");
+  return FIM_OK;
+}
+
+void io_chunk_hook(void* arg, int phase, int t0, int nt) {
+  StepIo& io = *(StepIo*)arg;
+  if (io.rc) return;
+  const int ci = t0 / io.tchunk;
+  if (phase == 0) io.rc = io_wait(io, io.up_chunk[ci]);
+  else io.rc = io_download(io, kIoT, t0, nt);
+}
+
 template <typename R>
-int enqueue_step(fim_ctx* c, fim_state* st) {
+int enqueue_step(fim_ctx* c, fim_state* st, StepIo* io = nullptr) {
   const int M = c->M;
   Launch l = make_launch(c, M);
   Grid<R>& g = grid_of<R>(c);
   const Strides& s = c->str;
+  int rc;
+  if (io && (rc = io_wait(*io, io->up_ev[kIoA]))) return rc;
   launch_step_begin(l, c->d_sp);
   // dyn_run.F90:119-132: the step opens with hybgen and hystat of step its-1
   // (skipped at a member's first step, after dyn_init's own adjustment)
@@ -835,6 +999,7 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
   launch_hystat<R>(lb, g, s, F<R>(st, FIM_PH3D), F<R>(st, FIM_EX3D), F<R>(st, FIM_MP3D), F<R>(st, FIM_DP3D),
                    F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP), F<R>(st, FIM_PSRF), F<R>(st, FIM_PTDCY), st->mpf,
                    trdp_done);
+  if (io && (rc = io_download(*io, kIoA, 0, 0))) return rc;
   // the dynamics of the step, one member group at a time; the edge work
   // fields and the scratch hold one group, the prognostic fields all members
   for (int m0 = 0; m0 < M; m0 += c->G) {
@@ -863,6 +1028,7 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
       launch_tracer_own<R>(lg, g, s, P(FIM_TR3D), P(FIM_TRC_EDG), c->trc_vk, c->trc_tb);
     }
     CnuityScratch<R> cw{(R*)c->antifx, (R*)c->delp_lo, (R*)c->p_plus, (R*)c->p_mnus, (R*)c->r_plus, (R*)c->r_mnus};
+    if (io && (rc = io_wait(*io, io->up_ev[kIoC]))) return rc;
     if (c->cfg.flux_conserv_schm == 1)
       launch_cnuity<R>(lg, g, s, cw, P(FIM_US3D), P(FIM_VS3D), P(FIM_U_EDG), P(FIM_V_EDG),
                        P(FIM_DP_EDG), P(FIM_LP_EDG), P(FIM_DP3D), P(FIM_PR3D),
@@ -880,28 +1046,35 @@ int enqueue_step(fim_ctx* c, fim_state* st) {
                         P(FIM_DPINIT), P(FIM_DP3D));
       launch_transp0<R>(lg, g, s, c->dtratio, P(FIM_CUMUFX), P(FIM_DP3D), P(FIM_DPINIT));
     }
+    if (io && (rc = io_download(*io, kIoC, 0, 0))) return rc;
     if (c->kn.hi_order) {
       TrcFusedScratch<R> fw{(R*)c->f_trcr_lo, (R*)c->f_sp, (R*)c->f_sm, (R*)c->f_trold, (R*)c->f_rp, (R*)c->f_rm,
-                            c->ftchunk, c->trc_vk, c->trc_tb};
+                            io ? io->tchunk : c->ftchunk, c->trc_vk, c->trc_tb};
       launch_tracers_fused<R>(lg, g, s, fw, P(FIM_TRC_EDG), P(FIM_TR3D), P(FIM_TRDP),
                               P(FIM_TRC_TDCY), P(FIM_TRL_TDCY), P(FIM_MASSFX),
-                              P(FIM_DP3D));
+                              P(FIM_DP3D), io ? &io->hook : nullptr);
     } else {
       TrcadvScratch<R> tw{(R*)c->t_antiflx, (R*)c->t_trmin, (R*)c->t_trmax, (R*)c->t_trcr_lo, (R*)c->t_rp,
                           (R*)c->t_rm, c->tchunk};
+      if (io) io_chunk_hook(io, 0, 0, c->T);
       launch_trcadv<R>(lg, g, s, tw, P(FIM_TRC_EDG), P(FIM_TR3D), P(FIM_TRDP),
                        P(FIM_TRC_TDCY), P(FIM_TRL_TDCY), P(FIM_MASSFX), P(FIM_DP3D));
+      if (io) io_chunk_hook(io, 1, 0, c->T);
     }
+    if (io && io->rc) return io->rc;
+    if (io && (rc = io_wait(*io, io->up_ev[kIoU]))) return rc;
     MomtumScratch<R> mw{(R*)c->du, (R*)c->dv, (R*)c->wu, (R*)c->wv};
     launch_momtum<R>(lg, g, s, c->kn, mw, P(FIM_US3D), P(FIM_VS3D), P(FIM_EX3D),
                      P(FIM_RELVOR), P(FIM_U_EDG), P(FIM_V_EDG), P(FIM_TRC_EDG),
                      P(FIM_MONT_EDG), P(FIM_UVSQ_EDG), P(FIM_U_TDCY), P(FIM_V_TDCY),
                      P(FIM_DP3D), mpf, (const R*)st->thold);
+    if (io && (rc = io_download(*io, kIoU, 0, 0))) return rc;
   }
   // budgets of the state the step returns
   launch_globsum<R>(l, g, s, c->T + c->TB, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), (const R*)nullptr,
                     (const R*)nullptr,
                     F<R>(st, FIM_PR3D), F<R>(st, FIM_EX3D), (const R*)nullptr, c->gs_partial, st->sums);
+  if (io && (rc = io_download(*io, kIoE, 0, 0))) return rc;
   return FIM_OK;
 }
 
@@ -1227,6 +1400,12 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
 int fim_ctx_destroy(fim_ctx* c) {
   if (!c) return FIM_EINVAL;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  for (cudaStream_t q : {c->io_in, c->io_out})
+    if (q) {
+      cudaStreamSynchronize(q);
+      cudaStreamDestroy(q);
+    }
+  for (cudaEvent_t e : c->io_ev) cudaEventDestroy(e);
   for (void* p : c->owned) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -1490,6 +1669,7 @@ int fim_state_alloc(fim_ctx* c, fim_state** out) {
   int rc = dalloc(c, (void**)&st->sums, (size_t)c->M * (8 + c->T + c->TB) * sizeof(double));
   if (rc) { delete st; return rc; }
   st->init64.assign((size_t)FIM_NFIELDS * c->M, nullptr);
+  st->host.assign((size_t)FIM_NFIELDS * c->M, nullptr);
   if (c->prec == FIM_PREC_F32) {
     if ((rc = dalloc(c, (void**)&st->mpf, (size_t)c->M * cnt[FIM_MP3D] * sizeof(float2)))) { delete st; return rc; }
     if ((rc = dalloc(c, &st->thold, (size_t)c->G * cnt[FIM_MP3D] * c->esz))) { delete st; return rc; }
@@ -1689,6 +1869,76 @@ int fim_step(fim_ctx* c, fim_state* st, int its, int use_graph) {
   }
   if (dirty && (rc = push_sp(c))) return rc;
   return run_step(c, st, use_graph);
+}
+
+int fim_state_set_host(fim_ctx* c, fim_state* st, int field, int member, void* host) {
+  if (!c || !st || field < 0 || field >= FIM_NFIELDS || member < 0 || member >= c->M) return FIM_EINVAL;
+  IoClass k;
+  if (!io_class(field, &k))
+    return set_err(c, FIM_EINVAL, "the edge work fields stay on the device (fim_state_set_host)");
+  st->host[(size_t)field * c->M + member] = host;
+  return FIM_OK;
+}
+
+int fim_step_io(fim_ctx* c, fim_state* st, int its, int64_t* h2d_bytes, int64_t* d2h_bytes) {
+  if (!c || !st || its < 1) return FIM_EINVAL;
+  if (c->G != c->M) return set_err(c, FIM_ENOTSUP, "fim_step_io runs all members in one group");
+  int rc = ensure_all(c);
+  if (rc) return rc;
+  if (c->autotune && !c->tuned && c->kn.hi_order && c->T > 1) {
+    rc = c->prec == FIM_PREC_F64 ? autotune_impl<double>(c, st) : autotune_impl<float>(c, st);
+    if (rc) return rc;
+  }
+  for (cudaStream_t* q : {&c->io_in, &c->io_out})
+    if (!*q) CK(cudaStreamCreateWithFlags(q, cudaStreamNonBlocking), "step io stream");
+  for (auto& p : c->h_sp) {
+    p.active = 1;
+    p.its = its - 1;
+  }
+  if ((rc = push_sp(c))) return rc;
+  StepIo io;
+  io.c = c;
+  io.st = st;
+  for (int m = 0; m < c->M; m++) {  // the slots after the step's abstart
+    const StepParams& p = c->h_sp[m];
+    io.nf.push_back((p.nf + 1) % 3);
+    io.of.push_back((p.of + 1) % 3);
+    io.vof.push_back((p.vof + 1) % 3);
+  }
+  // tracer chunks of about a quarter of the tracers: the slots of a chunk go
+  // up while the chunk before it is transported, its results come down while
+  // the next one is
+  io.tchunk = c->kn.hi_order ? std::max(1, std::min(c->ftchunk, (c->T + 3) / 4)) : c->T;
+  io.hook.fn = io_chunk_hook;
+  io.hook.arg = &io;
+  // the copies start behind the work already queued on the compute stream
+  cudaEvent_t start = io_event(io);
+  if (!start) return set_err(c, FIM_ECUDA, "step io event");
+  CK(cudaEventRecord(start, c->stream), "step io record");
+  CK(cudaStreamWaitEvent(c->io_in, start, 0), "step io wait");
+  CK(cudaStreamWaitEvent(c->io_out, start, 0), "step io wait");
+  if ((rc = io_upload(io, kIoA, 0, 0, &io.up_ev[kIoA]))) return rc;
+  if ((rc = io_upload(io, kIoC, 0, 0, &io.up_ev[kIoC]))) return rc;
+  for (int t0 = 0; t0 < c->T; t0 += io.tchunk) {
+    cudaEvent_t e;
+    if ((rc = io_upload(io, kIoT, t0, std::min(io.tchunk, c->T - t0), &e))) return rc;
+    io.up_chunk.push_back(e);
+  }
+  if ((rc = io_upload(io, kIoU, 0, 0, &io.up_ev[kIoU]))) return rc;
+  rc = c->prec == FIM_PREC_F64 ? enqueue_step<double>(c, st, &io) : enqueue_step<float>(c, st, &io);
+  if (rc) return rc;
+  if ((rc = check_launch(c, "step io"))) return rc;
+  // the step ends when its last download has landed
+  cudaEvent_t done = io_event(io);
+  if (!done) return set_err(c, FIM_ECUDA, "step io event");
+  CK(cudaEventRecord(done, c->io_out), "step io record");
+  CK(cudaStreamWaitEvent(c->stream, done, 0), "step io wait");
+  for (auto& p : c->h_sp)
+    if (p.active) host_abstart(p, p.its + 1);
+  CK(cudaStreamSynchronize(c->stream), "step io");
+  if (h2d_bytes) *h2d_bytes = io.h2d;
+  if (d2h_bytes) *d2h_bytes = io.d2h;
+  return FIM_OK;
 }
 
 int fim_step_active(fim_ctx* c, fim_state* st, int use_graph) {

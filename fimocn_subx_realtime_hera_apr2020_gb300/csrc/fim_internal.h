@@ -349,10 +349,17 @@ template <typename R>
 int tune_tracers(const Launch&, const Grid<R>&, const Strides&, const TrcFusedScratch<R>&, R* trc_edg, R* tracr,
                  R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx, const R* delp, int* best_vk, int* best_tb,
                  float* best_ms);
+// Called by launch_tracers_fused before (phase 0) and after (phase 1) the
+// kernels of each tracer chunk [t0, t0 + nt): the step with host transfers
+// (fim_step_io) orders the chunk's AB3 slot uploads and its downloads there.
+struct ChunkHook {
+  void (*fn)(void* arg, int phase, int t0, int nt) = nullptr;
+  void* arg = nullptr;
+};
 template <typename R>
 void launch_tracers_fused(const Launch&, const Grid<R>&, const Strides&, const TrcFusedScratch<R>&,
                           R* trc_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx,
-                          const R* delp);
+                          const R* delp, const ChunkHook* hook = nullptr);
 template <typename R>
 struct MomtumScratch { R *du, *dv, *wu, *wv; };
 // With mpf != null (FP32-mixed step) the pressure-gradient line integrals use

@@ -329,10 +329,11 @@ __global__ void __launch_bounds__(kTB, kTBMin) k_tr_hi(Grid<R> g, Strides s, con
 template <typename R, int VK>
 void tracers_fused_vk(const Launch& l, const Grid<R>& g, const Strides& s, const TrcFusedScratch<R>& w,
                       R* trc_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx, const R* delp,
-                      int tb, bool probe) {
+                      int tb, bool probe, const ChunkHook* hook) {
   const size_t sc = (size_t)g.N * g.L;
   for (int t0 = 0; t0 < g.T; t0 += w.tchunk) {
     const int nt = (g.T - t0 < w.tchunk) ? g.T - t0 : w.tchunk;
+    if (hook && hook->fn) hook->fn(hook->arg, 0, t0, nt);
     dim3 grid(tblocks((long long)g.N * (g.L / VK), tb) * nt, l.members);
     FIM_KBEGIN(l, "k_tr_lo");
     k_tr_lo<R, VK><<<grid, tb, 0, l.stream>>>(g, s, l.sp, t0, nt, massfx, trc_edg, tracr, trcdp, trl_tdcy, delp,
@@ -347,6 +348,7 @@ void tracers_fused_vk(const Launch& l, const Grid<R>& g, const Strides& s, const
     k_tr_hi<R, VK><<<grid, tb, 0, l.stream>>>(g, s, l.sp, t0, nt, massfx, trc_edg, tracr, trcdp, trc_tdcy,
                                                delp, w.trold, w.trcr_lo, w.r_plus, w.r_mnus, sc);
     FIM_KEND(l);
+    if (hook && hook->fn) hook->fn(hook->arg, 1, t0, nt);
   }
 }
 
@@ -362,24 +364,25 @@ inline int tracer_tb(int tb) { return tb == 256 ? 256 : 128; }
 
 template <typename R>
 void fused_dispatch(const Launch& l, const Grid<R>& g, const Strides& s, const TrcFusedScratch<R>& w, R* trc_edg,
-                    R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx, const R* delp, bool probe) {
+                    R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx, const R* delp, bool probe,
+                    const ChunkHook* hook = nullptr) {
   const int vk = tracer_vk(g, {trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp, w.trcr_lo, w.s_plus,
                                w.s_mnus, w.trold, w.r_plus, w.r_mnus}, w.vk);
   const int tb = tracer_tb(w.tb);
   if (vk == 4)
     tracers_fused_vk<R, (sizeof(R) == 4 ? 4 : 2)>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx,
-                                                  delp, tb, probe);
+                                                  delp, tb, probe, hook);
   else if (vk == 2)
-    tracers_fused_vk<R, 2>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp, tb, probe);
+    tracers_fused_vk<R, 2>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp, tb, probe, hook);
   else
-    tracers_fused_vk<R, 1>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp, tb, probe);
+    tracers_fused_vk<R, 1>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp, tb, probe, hook);
 }
 
 template <typename R>
 void launch_tracers_fused(const Launch& l, const Grid<R>& g, const Strides& s, const TrcFusedScratch<R>& w,
                           R* trc_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx,
-                          const R* delp) {
-  fused_dispatch<R>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp, false);
+                          const R* delp, const ChunkHook* hook) {
+  fused_dispatch<R>(l, g, s, w, trc_edg, tracr, trcdp, trc_tdcy, trl_tdcy, massfx, delp, false, hook);
 }
 
 template <typename R, int VK>
@@ -452,7 +455,8 @@ int tune_tracers(const Launch& l, const Grid<R>& g, const Strides& s, const TrcF
 
 #define INSTANTIATE(R)                                                                                        \
   template void launch_tracers_fused<R>(const Launch&, const Grid<R>&, const Strides&,                       \
-                                        const TrcFusedScratch<R>&, R*, R*, R*, R*, R*, const R*, const R*);  \
+                                        const TrcFusedScratch<R>&, R*, R*, R*, R*, R*, const R*, const R*,   \
+                                        const ChunkHook*);                                                    \
   template void launch_tracer_own<R>(const Launch&, const Grid<R>&, const Strides&, const R*, R*, int, int); \
   template int tune_tracers<R>(const Launch&, const Grid<R>&, const Strides&, const TrcFusedScratch<R>&, R*, \
                                R*, R*, R*, R*, const R*, const R*, int*, int*, float*);

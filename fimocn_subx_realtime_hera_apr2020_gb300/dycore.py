@@ -326,6 +326,27 @@ class DycoreState:
         _lib.check(self.lib.fim_step(self.dyc.ctx, self.st, its, 1 if use_graph else 0), "fim_step", self.dyc.ctx)
         self.its = its
 
+    def set_host(self, name, host, member=0):
+        """Register the host copy of a member's field for step_io (a pinned
+        torch tensor or numpy array of the field's size; None unregisters)."""
+        ptr, n = self.field_ptr(name, member)
+        if host is not None:
+            size = host.numel() if hasattr(host, "numel") else host.size
+            if size != n:
+                raise ValueError("%s: %d elements, expected %d" % (name, size, n))
+        _lib.check(self.lib.fim_state_set_host(self.dyc.ctx, self.st, _lib.FIELD_ID[name], member, _ptr(host)),
+                   "fim_state_set_host", self.dyc.ctx)
+
+    def step_io(self, its=None):
+        """One step with the registered fields moved in and out around it
+        (fim_step_io); returns the (host-to-device, device-to-host) bytes."""
+        its = self.its + 1 if its is None else its
+        up, down = ctypes.c_int64(0), ctypes.c_int64(0)
+        _lib.check(self.lib.fim_step_io(self.dyc.ctx, self.st, its, ctypes.byref(up), ctypes.byref(down)),
+                   "fim_step_io", self.dyc.ctx)
+        self.its = its
+        return up.value, down.value
+
     def init_member(self, member):
         """Initialise (dyn_init) and activate one member slot after its upload."""
         _lib.check(self.lib.fim_state_init_member(self.dyc.ctx, self.st, member), "fim_state_init_member",

@@ -397,6 +397,27 @@ int fim_member_set_step(fim_ctx *ctx, int member, int itsm1, int nf, int of, int
                         double adbash1, double adbash2, double adbash3);
 int fim_step_active(fim_ctx *ctx, fim_state *st, int use_graph);
 
+/* The step with the state on the host (no counterpart in the reference,
+ * whose state lives in host memory).  fim_state_set_host registers the host
+ * copy of one member's field (null unregisters); pinned memory (cudaHostAlloc
+ * or cudaHostRegister) lets the copies run beside the kernels.  The edge work
+ * fields stay on the device (FIM_EINVAL).  fim_step_io(its) then runs
+ * fim_step(its) with the registered fields moved in and out: each goes up
+ * before the first kernel that reads or writes it and comes down as soon as
+ * the step's last writer of it is done, on two copy streams beside the
+ * compute stream.  The step is cut at the stages of dyn_run: hybgen + hystat
+ * + edge interpolation, cnuity (its AB3 slots arrive just before it), the
+ * tracer transport in chunks of about a quarter of the tracers (each chunk's
+ * AB3 slots arrive while the chunk before it runs; its results leave while
+ * the next one runs), momtum.  AB3 tendency fields move only the slots the
+ * step reads (of, vof) and writes (nf); ws3d, sdot and relvor, which the
+ * step rewrites whole, only come down (ptdcy, of whose two time levels a step
+ * writes one, goes both ways).  Returns when every download has landed; *h2d_bytes and
+ * *d2h_bytes (may be null) get the bytes moved.  FIM_ENOTSUP with
+ * member_group < members. */
+int fim_state_set_host(fim_ctx *ctx, fim_state *st, int field, int member, void *host);
+int fim_step_io(fim_ctx *ctx, fim_state *st, int its, int64_t *h2d_bytes, int64_t *d2h_bytes);
+
 /* Member budgets after the last step (qmass, tracer integrals qtrcr(ntra)). */
 int fim_state_budget(fim_ctx *ctx, fim_state *st, int member, double *qtrcr, fim_budget *out);
 

@@ -379,7 +379,7 @@ def test_fused_step_with_edgvar2_fp64():
 
 
 AB3_FIELDS = ["u_tdcy", "v_tdcy", "dp_tdcy", "dpl_tdcy", "trc_tdcy", "trl_tdcy"]
-STEP_OUTPUTS = ["ws3d", "sdot", "relvor", "ptdcy"]
+STEP_OUTPUTS = ["ws3d", "sdot", "relvor"]
 
 
 def test_ab3_slot_transfer(case4):

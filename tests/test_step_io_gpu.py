@@ -1,0 +1,83 @@
+"""fim_step_io: the step with the state kept in host buffers.
+
+The fields a step reads go up stage by stage and the fields it writes come
+down as soon as they are final, on copy streams beside the kernels.  Before
+every step the device copy of every registered field is overwritten with
+NaN, so any field (or AB3 slot) that the step read without having uploaded
+it, or any upload that landed after a kernel wrote the field, would show up
+in the results.  Five steps must equal a resident run bit for bit.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import fimocn_subx_realtime_hera_apr2020_gb300 as F  # noqa: E402
+from helpers import make_case  # noqa: E402
+from fimocn_subx_realtime_hera_apr2020_gb300._lib import FimError  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["us3d", "vs3d", "dp3d", "pr3d", "ex3d", "ph3d", "mp3d", "tr3d", "trdp", "u_tdcy", "v_tdcy", "dp_tdcy",
+          "dpl_tdcy", "trc_tdcy", "trl_tdcy", "ws3d", "sdot", "relvor", "psrf", "ptdcy"]
+AB3 = {"u_tdcy", "v_tdcy", "dp_tdcy", "dpl_tdcy", "trc_tdcy", "trl_tdcy"}
+OUT = {"ws3d", "sdot", "relvor"}
+
+
+def _state(grid, cfg, fields):
+    d = F.Dycore(grid, cfg)
+    st = d.state()
+    st.load(fields)
+    st.init()
+    return d, st
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_step_io_matches_resident(precision):
+    grid, cfg, fields = make_case(glvl=4, nvl=38, ntra=5, dt=400.0, seed=1601, noise=1.0, precision=precision)
+    _, ref = _state(grid, cfg, fields)
+    _, st = _state(grid, cfg, fields)
+    tdt = torch.float64 if precision == "f64" else torch.float32
+    NL = grid.nip * cfg.nvl
+    host = {}
+    for f in FIELDS:
+        n = st.field_ptr(f)[1]
+        host[f] = torch.empty(n, dtype=tdt, pin_memory=True)
+        st.download(f, out=host[f].numpy())
+        st.set_host(f, host[f])
+    esz = 8 if precision == "f64" else 4
+    want_up = sum(host[f].numel() for f in FIELDS if f not in OUT and f not in AB3) * esz + \
+        sum(2 * host[f].numel() // 3 for f in AB3) * esz
+    want_down = sum(host[f].numel() for f in FIELDS if f not in AB3) * esz + \
+        sum(host[f].numel() // 3 for f in AB3) * esz
+    for its in range(1, 6):
+        for f in FIELDS:
+            st.upload(f, np.full(host[f].numel(), np.nan))
+        up, down = st.step_io(its)
+        ref.step(its, use_graph=True)
+        assert (up, down) == (want_up, want_down)
+        for f in FIELDS:
+            got = host[f].numpy()
+            want = ref.download(f)
+            if f in AB3:
+                # the slot the step wrote; the others are the host's own copies
+                nf = st.get_step()[1] - 1  # slot the step just done wrote, 0-based
+                nb = want.size // (3 * NL)
+                got = got.reshape(nb, 3, NL)[:, nf]
+                want = want.reshape(nb, 3, NL)[:, nf]
+            if f == "sdot" and its == 1:
+                continue  # hybgen does not run at the first step: the poison stays
+            assert np.array_equal(got, want), (its, f)
+    rc, flags = st.check()
+    assert rc == 0 and flags == 0
+
+
+def test_step_io_rejects_member_groups():
+    grid = F.Grid.cached(3)
+    cfg = F.FimConfig(nvl=38, ntra=5, dt=400.0, precision="f32", members=2, member_group=1)
+    d = F.Dycore(grid, cfg)
+    st = d.state()
+    with pytest.raises(FimError):
+        st.step_io(1)
+    with pytest.raises(FimError):
+        st.set_host("u_edg", None)
