@@ -1047,6 +1047,21 @@ int enqueue_step(fim_ctx* c, fim_state* st, StepIo* io = nullptr) {
       launch_transp0<R>(lg, g, s, c->dtratio, P(FIM_CUMUFX), P(FIM_DP3D), P(FIM_DPINIT));
     }
     if (io && (rc = io_download(*io, kIoC, 0, 0))) return rc;
+    // momtum reads theta's edge values (edgvar1), the edge winds and the new
+    // thicknesses, none of which the tracer transport writes, and writes
+    // nothing it reads: with host transfers it runs first, so the step ends on
+    // the tracer chunks whose results stream out as they finish
+    auto momentum = [&]() -> int {
+      if (io && (rc = io_wait(*io, io->up_ev[kIoU]))) return rc;
+      MomtumScratch<R> mw{(R*)c->du, (R*)c->dv, (R*)c->wu, (R*)c->wv};
+      launch_momtum<R>(lg, g, s, c->kn, mw, P(FIM_US3D), P(FIM_VS3D), P(FIM_EX3D),
+                       P(FIM_RELVOR), P(FIM_U_EDG), P(FIM_V_EDG), P(FIM_TRC_EDG),
+                       P(FIM_MONT_EDG), P(FIM_UVSQ_EDG), P(FIM_U_TDCY), P(FIM_V_TDCY),
+                       P(FIM_DP3D), mpf, (const R*)st->thold);
+      if (io && (rc = io_download(*io, kIoU, 0, 0))) return rc;
+      return FIM_OK;
+    };
+    if (io && (rc = momentum())) return rc;
     if (c->kn.hi_order) {
       TrcFusedScratch<R> fw{(R*)c->f_trcr_lo, (R*)c->f_sp, (R*)c->f_sm, (R*)c->f_trold, (R*)c->f_rp, (R*)c->f_rm,
                             io ? io->tchunk : c->ftchunk, c->trc_vk, c->trc_tb};
@@ -1062,13 +1077,7 @@ int enqueue_step(fim_ctx* c, fim_state* st, StepIo* io = nullptr) {
       if (io) io_chunk_hook(io, 1, 0, c->T);
     }
     if (io && io->rc) return io->rc;
-    if (io && (rc = io_wait(*io, io->up_ev[kIoU]))) return rc;
-    MomtumScratch<R> mw{(R*)c->du, (R*)c->dv, (R*)c->wu, (R*)c->wv};
-    launch_momtum<R>(lg, g, s, c->kn, mw, P(FIM_US3D), P(FIM_VS3D), P(FIM_EX3D),
-                     P(FIM_RELVOR), P(FIM_U_EDG), P(FIM_V_EDG), P(FIM_TRC_EDG),
-                     P(FIM_MONT_EDG), P(FIM_UVSQ_EDG), P(FIM_U_TDCY), P(FIM_V_TDCY),
-                     P(FIM_DP3D), mpf, (const R*)st->thold);
-    if (io && (rc = io_download(*io, kIoU, 0, 0))) return rc;
+    if (!io && (rc = momentum())) return rc;
   }
   // budgets of the state the step returns
   launch_globsum<R>(l, g, s, c->T + c->TB, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), (const R*)nullptr,
@@ -1919,12 +1928,12 @@ int fim_step_io(fim_ctx* c, fim_state* st, int its, int64_t* h2d_bytes, int64_t*
   CK(cudaStreamWaitEvent(c->io_out, start, 0), "step io wait");
   if ((rc = io_upload(io, kIoA, 0, 0, &io.up_ev[kIoA]))) return rc;
   if ((rc = io_upload(io, kIoC, 0, 0, &io.up_ev[kIoC]))) return rc;
+  if ((rc = io_upload(io, kIoU, 0, 0, &io.up_ev[kIoU]))) return rc;
   for (int t0 = 0; t0 < c->T; t0 += io.tchunk) {
     cudaEvent_t e;
     if ((rc = io_upload(io, kIoT, t0, std::min(io.tchunk, c->T - t0), &e))) return rc;
     io.up_chunk.push_back(e);
   }
-  if ((rc = io_upload(io, kIoU, 0, 0, &io.up_ev[kIoU]))) return rc;
   rc = c->prec == FIM_PREC_F64 ? enqueue_step<double>(c, st, &io) : enqueue_step<float>(c, st, &io);
   if (rc) return rc;
   if ((rc = check_launch(c, "step io"))) return rc;
