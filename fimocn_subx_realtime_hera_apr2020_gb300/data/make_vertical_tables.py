@@ -4,15 +4,13 @@ The hybgen target potential temperatures (theta_coor<nvl>.txt) and minimum
 layer thicknesses (dpsig<nvl>.txt) are inputs the reference reads at start-up
 (FIMsrc/fim/horizontal/dyn_init.F90:789-816).  Each file lists the nvl values
 first and alternative choices after a separator line; only the first nvl
-numbers are taken.  Run from the repository root with the reference tree at
-REF (default /root/reference); the JSON is committed so nothing reads the
+numbers are taken.  Usage: python make_vertical_tables.py REF, with REF the
+root of the reference tree; the JSON is committed so nothing reads the
 reference at run time.
 """
 import json
 import os
 import sys
-
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
 
 
 def first_numbers(path, n):
@@ -30,6 +28,9 @@ def first_numbers(path, n):
 
 
 def main():
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python make_vertical_tables.py REF  (REF: root of the reference tree)")
+    REF = sys.argv[1]
     out = {}
     for nvl in (38, 64):
         th = first_numbers(os.path.join(REF, "FIMrun", f"theta_coor{nvl}.txt"), nvl)
