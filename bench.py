@@ -233,6 +233,15 @@ def gpu_arm(args, ws, rank, local):
     roof = {"bound": "hbm", "kernel": dom, "achieved": kernels[dom]["gbs"], "peak": peak, "unit": "GB/s",
             "frac": kernels[dom]["gbs"] / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
             "traffic": traffic, "alg_bytes_per_launch": kernels[dom]["alg_bytes"]}
+    # the whole step against its compulsory traffic: every state word read and
+    # written once (29 + 10 ntra words per cell-level) plus the grid tables
+    # read once (118 FP32 metric values and 49 int32 index values per cell)
+    step_bytes = (29 + 10 * T) * w * N * L * members + (118 * w + 49 * 4) * N
+    roof["step"] = {"compulsory_bytes": step_bytes, "ms_per_step": ms_max,
+                    "achieved": step_bytes / (ms_max * 1e-3) / 1e9, "unit": "GB/s",
+                    "frac": step_bytes / (ms_max * 1e-3) / 1e9 / peak,
+                    "kernel_words_per_cell_level": sum(WORDS[k](T) for k in kernels),
+                    "compulsory_words_per_cell_level": 29 + 10 * T}
 
     # end to end through the C-ABI with host buffers: every step uploads what it
     # reads and downloads what it writes (AB3 tendency fields: the two slots it

@@ -210,8 +210,7 @@ __device__ void regrid_1d(const Knobs& kn, const R* targt, const R* dpsig, int L
 }
 
 // pcwise (hybgen.F90:1010-1279): 1-D PCM/PLM/PPM remap of yold from cell
-// boundaries xold to xnew.  Returns true when the column-integral check fails
-// (evaluated in the FP64 build only).
+// boundaries xold to xnew.  Returns true when the column-integral check fails.
 template <typename R, int ML>
 __device__ bool pcwise(int kk, const R* xold, const R* yold, const R* xnew, R* ynew, int miglim, int remap_optn) {
   R delz[ML + 1], fco[ML], fcn[ML], vertfx[ML + 1], fldnew[ML], a[ML], b[ML], cc[ML];
@@ -730,13 +729,18 @@ __device__ __forceinline__ void lane_geo(int L, int lane, const R* xo, const R* 
 
 // pcwise (PLM, miglim = 1) of NF fields sharing one coordinate, lane =
 // levels kb .. kb+VL-1 of each; the fields' chains are independent and
-// interleave.  Returns true when a column-integral check fails (FP64 build).
+// interleave.  Returns true when pcwise's column-integral check
+// (hybgen.F90:1262) fails.  That check compares two sums of the same
+// telescoping fluxes; in FP32 it would only measure the rounding of those
+// sums and cost 0.49 ms a step at glvl 8 (a tenth of the remap), so it runs
+// in the FP64 build, and the FP32-mixed build keeps the two physical column
+// checks (restp_1d's, and remap_1d's theta integral).
 template <typename R, int VL, int NF, int W = 32>
 __device__ __forceinline__ bool pcwise_v(int L, int lane, R (&y)[NF][VL], const LaneGeo<R, VL>& G) {
   const R small = R(1.e-22);
   const int kb = lane * VL;
   R bfore[NF], colscl[NF];
-  {
+  if (sizeof(R) == 8) {
 #pragma unroll
     for (int h = 0; h < NF; h++) {
       bfore[h] = R(0);
@@ -844,7 +848,7 @@ __device__ __forceinline__ bool pcwise_v(int L, int lane, R (&y)[NF][VL], const 
         y[h][v] = (amount + yf[h][v] * small) * G.rfn[v];
       }
     }
-    {
+    if (sizeof(R) == 8) {
       const R dif = warp_sum<R, W>(bfore[h] - after), scl = warp_sum<R, W>(colscl[h]);
       bad |= cabs(dif) > cmax(R(1.e-33), col_tol<R>(1.e-11) * scl);
     }

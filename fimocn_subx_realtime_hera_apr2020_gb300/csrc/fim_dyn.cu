@@ -1007,9 +1007,11 @@ __global__ void __launch_bounds__(kBlock) k_dissip(Grid<R> g, Strides s, const R
 
 // momtum1 (momtum_compute.F90:278-423, janjic=0) after adding the dissipation
 // increments (momtum.F90:130-139); one warp per column so the Rayleigh damping
-// of the top layers can read the updated top three levels.
+// of the top layers can read the updated top three levels.  Four blocks a
+// SM (64 registers, a few spilled) measured 1.77 ms at glvl 8 against 1.96
+// at three (80 registers).
 template <typename R, int NC>
-__global__ void __launch_bounds__(kBlock, 3) k_momtum1(Grid<R> g, Strides s, Knobs kn, const StepParams* __restrict__ sp,
+__global__ void __launch_bounds__(kBlock, 4) k_momtum1(Grid<R> g, Strides s, Knobs kn, const StepParams* __restrict__ sp,
     R* __restrict__ u, R* __restrict__ v, const R* __restrict__ du, const R* __restrict__ dv,
     const R* __restrict__ exner, R* __restrict__ relvor, const R* __restrict__ u_edg, const R* __restrict__ v_edg,
     const R* __restrict__ trc_edg, const R* __restrict__ mont_edg, const R* __restrict__ uvsq_edg,

@@ -50,8 +50,8 @@ enum : int {
 // Relative tolerance of hybgen's column-integral checks: the reference's own
 // in FP64 (acurcy of restp_1d 1e-6, hybgen.F90:873; of remap_1d 2e-6, :694;
 // of the real*8 pcwise 1e-11, :1262); in the FP32-mixed build one bound for
-// all three, ~500 float epsilons, well above the rounding of a column sum of
-// nvl <= 128 FP32 terms and well below a lost or doubled layer.
+// the checks it runs, ~500 float epsilons, well above the rounding of a
+// column sum of nvl <= 128 FP32 terms and well below a lost or doubled layer.
 template <typename R>
 __host__ __device__ constexpr R col_tol(double ref) {
   return R(sizeof(R) == 8 ? ref : 3.e-5);
