@@ -44,6 +44,8 @@ WORDS = {
     "k_tr_own": lambda T: 7 * (T - 1), "k_tr_lo": lambda T: 15 * T + 7, "k_tr_lim": lambda T: 8 * T + 1,
     "k_tr_hi": lambda T: 16 * T + 7,
     "k_cnuity12": lambda T: 37, "k_cnuity3": lambda T: 8, "k_cnuity4": lambda T: 26, "k_cnuity5": lambda T: 14,
+    # cnuity1..4 as one persistent launch (--persistent): the three kernels' words
+    "k_cnuity_coop": lambda T: 37 + 8 + 26,
     "k_trcadv1": lambda T: 27 * T, "k_trcadv2": lambda T: 16 * T, "k_trcadv3": lambda T: 18 * T,
     "k_dissip": lambda T: 5, "k_del4prep": lambda T: 4, "k_momtum1": lambda T: 44,
     # in the step the remap also writes tracer x thickness (T words), which
@@ -189,6 +191,8 @@ def gpu_arm(args, ws, rank, local):
     cfg = F.FimConfig(nvl=L, ntra=T, dt=wl["dt"], precision="f32", members=members, member_group=group,
                       hi_order_uv_comp=1 if args.hi_order_uv else 0)
     dyc, st = make_state(F, grid, cfg, wl, np.float32)
+    if args.persistent:
+        dyc.set_persistent(True)
     for _ in range(args.warmup):
         st.step(use_graph=True)
     torch.cuda.synchronize()
@@ -345,7 +349,8 @@ def gpu_arm(args, ws, rank, local):
             "vs_baseline": None, "dtype": "f32 (float-float column sums, FP64 budget reductions)",
             "data": "synthetic seeded balanced state (no dataset: the reference's GFS initial state is not "
                     "in the tree)",
-            "config": {"workload": args.workload + ("+edgvar2" if args.hi_order_uv else ""), "glvl": wl["glvl"],
+            "config": {"workload": args.workload + ("+edgvar2" if args.hi_order_uv else "") +
+                                   ("+persistent-cnuity" if args.persistent else ""), "glvl": wl["glvl"],
                        "nip": N, "nvl": L, "ntra": T,
                        "dt": wl["dt"], "members_per_gpu": members, "member_group": group or members,
                        "tracer_shape_autotuned": {"levels_per_thread": shape[0], "threads_per_block": shape[1],
@@ -646,6 +651,7 @@ def main():
     p.add_argument("--dt", type=float, default=0.0, help="time step of the accuracy run (default: workload's)")
     p.add_argument("--cpl", action="store_true", help="time the physics coupling on the workload's state")
     p.add_argument("--hi-order-uv", action="store_true", help="the step with edgvar2 (hiOrderUVComp)")
+    p.add_argument("--persistent", action="store_true", help="cnuity1..4 as one cooperative persistent launch")
     args = p.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -75,6 +75,8 @@ _SIGS = {
     "fim_step_active": ([_VP, _VP, _I], _I),
     "fim_state_set_host": ([_VP, _VP, _I, _I, _VP], _I),
     "fim_step_io": ([_VP, _VP, _I, _VP, _VP], _I),
+    "fim_set_persistent": ([_VP, _I, ctypes.c_double], _I),
+    "fim_set_barrier_test": ([_VP, _I], _I),
     "fim_state_init_member": ([_VP, _VP, _I], _I),
     "fim_member_set_active": ([_VP, _VP, _I, _I], _I),
     "fim_member_its": ([_VP, _I], _I),

@@ -46,6 +46,7 @@ struct fim_state {
   std::vector<void*> host;
   cudaGraphExec_t graph = nullptr;
   long long graph_kernels = 0;
+  int graph_gen = 0;  // the context's graph_gen the graph was captured under
 };
 
 struct fim_ctx {
@@ -54,6 +55,11 @@ struct fim_ctx {
   int N = 0, L = 0, T = 0, M = 1;
   size_t esz = 8;
   cudaStream_t stream = nullptr;
+  // persistent cnuity1..4 (fim_set_persistent); graph_gen counts the changes,
+  // so a state's step graph is captured again after one
+  bool coop_on = false;
+  CoopCfg coop{nullptr, 0u, 1000000000ull};
+  int graph_gen = 0;
   // fim_step_io's copy streams (host to device, device to host) and events
   cudaStream_t io_in = nullptr, io_out = nullptr;
   std::vector<cudaEvent_t> io_ev;
@@ -257,6 +263,7 @@ Launch make_launch(fim_ctx* c, int members) {
   l.flags = c->d_flags;
   l.counter = &c->launches;
   l.prof = &c->prof;
+  l.coop = c->coop_on ? &c->coop : nullptr;
   return l;
 }
 
@@ -1839,6 +1846,10 @@ static int run_step(fim_ctx* c, fim_state* st, int use_graph) {
     if (rc) return rc;
   }
   if (use_graph) {
+    if (st->graph && st->graph_gen != c->graph_gen) {
+      cudaGraphExecDestroy(st->graph);
+      st->graph = nullptr;
+    }
     if (!st->graph) {
       // the step is its-invariant: every step-dependent scalar is read from
       // the per-member device parameter block that k_step_begin advances
@@ -1850,6 +1861,7 @@ static int run_step(fim_ctx* c, fim_state* st, int use_graph) {
       if (rc) return rc;
       if (e != cudaSuccess) return set_err(c, FIM_ECUDA, "end capture", e);
       st->graph_kernels = c->launches - before;
+      st->graph_gen = c->graph_gen;
       c->launches = before;
       e = cudaGraphInstantiate(&st->graph, graph, 0);
       cudaGraphDestroy(graph);
@@ -1878,6 +1890,25 @@ int fim_step(fim_ctx* c, fim_state* st, int its, int use_graph) {
   }
   if (dirty && (rc = push_sp(c))) return rc;
   return run_step(c, st, use_graph);
+}
+
+int fim_set_persistent(fim_ctx* c, int on, double timeout_s) {
+  if (!c || !(timeout_s > 0.) || timeout_s > 60.) return FIM_EINVAL;
+  if (on && !c->coop.barrier) {
+    int rc = dalloc(c, (void**)&c->coop.barrier, sizeof(unsigned));
+    if (rc) return rc;
+  }
+  c->coop_on = on != 0;
+  c->coop.limit_ns = (unsigned long long)(timeout_s * 1e9);
+  c->graph_gen++;
+  return FIM_OK;
+}
+
+int fim_set_barrier_test(fim_ctx* c, int phantom_arrivals) {
+  if (!c || phantom_arrivals < 0 || phantom_arrivals > 1) return FIM_EINVAL;
+  c->coop.extra = (unsigned)phantom_arrivals;
+  c->graph_gen++;
+  return FIM_OK;
 }
 
 int fim_state_set_host(fim_ctx* c, fim_state* st, int field, int member, void* host) {
@@ -2012,6 +2043,7 @@ int fim_check(fim_ctx* c, fim_state* st, int* flags) {
   int f = 0;
   for (int v : h) f |= v;
   if (flags) *flags = f;
+  if (f & kFlagTimeout) return FIM_ETIMEDOUT;
   return (f & kFlagBadDp) ? FIM_ENUMERIC : FIM_OK;
 }
 

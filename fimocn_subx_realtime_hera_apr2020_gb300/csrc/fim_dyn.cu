@@ -325,15 +325,18 @@ __global__ void __launch_bounds__(kBlock) k_edgvar3_avg(Grid<R> g, Strides s, R*
 // edge and on the neighbour's copy of it, donor-cell mass flux, antidiffusive
 // flux, low-order tendency and low-order thickness; also the Zalesak sums
 // P+/P- of cnuity3 (cnuity_compute.F90:186-194), which only need own edges.
+// The bodies of cnuity12/3/4 take the (virtual) block index, so the persistent
+// variant below runs the same code; their pointers carry no __restrict__ (the
+// persistent variant reads in one stage what another block wrote in the
+// stage before, which read-only loads must not do).
 template <typename R, int VK>
-__global__ void __launch_bounds__(kBlock) k_cnuity12(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
-    const R* __restrict__ u_edg, const R* __restrict__ v_edg, const R* __restrict__ dp_edg,
-    const R* __restrict__ delp, R* __restrict__ massfx, R* __restrict__ dplo_tndcy, R* __restrict__ antifx,
-    R* __restrict__ delp_lo, R* __restrict__ p_plus, R* __restrict__ p_mnus) {
+__device__ __forceinline__ void cnuity12_body(int bx, int by, const Grid<R>& g, const Strides& s,
+    const StepParams* sp, const R* u_edg, const R* v_edg, const R* dp_edg, const R* delp, R* massfx,
+    R* dplo_tndcy, R* antifx, R* delp_lo, R* p_plus, R* p_mnus) {
   int i, k;
-  if (!cell_levels<VK>(g.N, g.L, i, k)) return;
+  if (!cell_levels_at<VK>(g.N, g.L, bx, i, k)) return;
   const int L = g.L, N = g.N;
-  const size_t m = blockIdx.y;
+  const size_t m = by;
   sp += m;
   if (!sp->active) return;
   u_edg += m * s.edge; v_edg += m * s.edge; dp_edg += m * s.edge; delp += m * s.cell;
@@ -402,17 +405,25 @@ __global__ void __launch_bounds__(kBlock) k_cnuity12(Grid<R> g, Strides s, const
   stv<VK>(p_plus + c, pp);
   stv<VK>(p_mnus + c, pm);
 }
+template <typename R, int VK>
+__global__ void __launch_bounds__(kBlock) k_cnuity12(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
+    const R* __restrict__ u_edg, const R* __restrict__ v_edg, const R* __restrict__ dp_edg,
+    const R* __restrict__ delp, R* __restrict__ massfx, R* __restrict__ dplo_tndcy, R* __restrict__ antifx,
+    R* __restrict__ delp_lo, R* __restrict__ p_plus, R* __restrict__ p_mnus) {
+  cnuity12_body<R, VK>(blockIdx.x, blockIdx.y, g, s, sp, u_edg, v_edg, dp_edg, delp, massfx, dplo_tndcy, antifx,
+                       delp_lo, p_plus, p_mnus);
+}
 
 // cnuity3 (cnuity_compute.F90:206-252): 1-ring max/min of old and low-order
 // thickness, Zalesak Q+/Q- and the limiters R+/R-.
 template <typename R, int VK>
-__global__ void __launch_bounds__(kBlock) k_cnuity3(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
-    const R* __restrict__ delp_lo, const R* __restrict__ delp, const R* __restrict__ dp_tndcy,
-    const R* __restrict__ p_plus, const R* __restrict__ p_mnus, R* __restrict__ r_plus, R* __restrict__ r_mnus) {
+__device__ __forceinline__ void cnuity3_body(int bx, int by, const Grid<R>& g, const Strides& s,
+    const StepParams* sp, const R* delp_lo, const R* delp, const R* dp_tndcy, const R* p_plus, const R* p_mnus,
+    R* r_plus, R* r_mnus) {
   int i, k;
-  if (!cell_levels<VK>(g.N, g.L, i, k)) return;
+  if (!cell_levels_at<VK>(g.N, g.L, bx, i, k)) return;
   const int L = g.L, N = g.N;
-  const size_t m = blockIdx.y;
+  const size_t m = by;
   sp += m;
   if (!sp->active) return;
   delp_lo += m * s.cell; delp += m * s.cell; dp_tndcy += m * s.ab;
@@ -450,18 +461,23 @@ __global__ void __launch_bounds__(kBlock) k_cnuity3(Grid<R> g, Strides s, const 
   stv<VK>(r_plus + c, rp);
   stv<VK>(r_mnus + c, rm);
 }
+template <typename R, int VK>
+__global__ void __launch_bounds__(kBlock) k_cnuity3(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
+    const R* __restrict__ delp_lo, const R* __restrict__ delp, const R* __restrict__ dp_tndcy,
+    const R* __restrict__ p_plus, const R* __restrict__ p_mnus, R* __restrict__ r_plus, R* __restrict__ r_mnus) {
+  cnuity3_body<R, VK>(blockIdx.x, blockIdx.y, g, s, sp, delp_lo, delp, dp_tndcy, p_plus, p_mnus, r_plus, r_mnus);
+}
 
 // cnuity4 (cnuity_compute.F90:291-369): clip the antidiffusive flux with the
 // own and neighbour limiters, total mass flux, AB3 thickness update.
 template <typename R, int VK>
-__global__ void __launch_bounds__(kBlock) k_cnuity4(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
-    const R* __restrict__ antifx, const R* __restrict__ r_plus, const R* __restrict__ r_mnus,
-    R* __restrict__ massfx, const R* __restrict__ dplo_tndcy, R* __restrict__ dp_tndcy, R* __restrict__ delp,
-    int* __restrict__ flags) {
+__device__ __forceinline__ void cnuity4_body(int bx, int by, const Grid<R>& g, const Strides& s,
+    const StepParams* sp, const R* antifx, const R* r_plus, const R* r_mnus, R* massfx, const R* dplo_tndcy,
+    R* dp_tndcy, R* delp, int* flags) {
   int i, k;
-  if (!cell_levels<VK>(g.N, g.L, i, k)) return;
+  if (!cell_levels_at<VK>(g.N, g.L, bx, i, k)) return;
   const int L = g.L, N = g.N;
-  const size_t m = blockIdx.y;
+  const size_t m = by;
   sp += m;
   if (!sp->active) return;
   antifx += m * s.edge; r_plus += m * s.cell; r_mnus += m * s.cell; massfx += m * s.mf;
@@ -506,6 +522,73 @@ __global__ void __launch_bounds__(kBlock) k_cnuity4(Grid<R> g, Strides s, const 
   }
   stv<VK>(delp + c, dn);
   if (bad) atomicOr(flags + m, kFlagBadDp);
+}
+template <typename R, int VK>
+__global__ void __launch_bounds__(kBlock) k_cnuity4(Grid<R> g, Strides s, const StepParams* __restrict__ sp,
+    const R* __restrict__ antifx, const R* __restrict__ r_plus, const R* __restrict__ r_mnus,
+    R* __restrict__ massfx, const R* __restrict__ dplo_tndcy, R* __restrict__ dp_tndcy, R* __restrict__ delp,
+    int* __restrict__ flags) {
+  cnuity4_body<R, VK>(blockIdx.x, blockIdx.y, g, s, sp, antifx, r_plus, r_mnus, massfx, dplo_tndcy, dp_tndcy, delp,
+                      flags);
+}
+
+// ---- persistent variant of cnuity1..4 ---------------------------------------
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid-wide barrier of a cooperative launch.  Every block adds one to *ctr
+// and waits until it reaches target; the wait gives up after limit_ns (and
+// after 2^22 polls whatever the timer says), sets kFlagTimeout in *flags and
+// returns false, so the kernel ends and the host reads FIM_ETIMEDOUT.
+__device__ bool coop_barrier(unsigned* ctr, unsigned target, unsigned long long limit_ns, int* flags) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(ctr, 1u);
+    int good = 1;
+    const unsigned long long t0 = global_ns();
+    for (unsigned it = 0;; it++) {
+      if (*(volatile unsigned*)ctr >= target) break;
+      if (it >= (1u << 22) || global_ns() - t0 > limit_ns) {
+        good = 0;
+        break;
+      }
+      __nanosleep(64);
+    }
+    if (!good) atomicOr(flags, kFlagTimeout);
+    __threadfence();
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// cnuity1..4 of every member in one cooperative launch: the blocks resident
+// on the GPU walk the virtual blocks of each stage, with a grid barrier
+// between the stages in place of kernel boundaries.  extra arrivals are added
+// to each barrier's target (a barrier that can never complete: the test of
+// the time limit).
+template <typename R, int VK>
+__global__ void __launch_bounds__(kBlock) k_cnuity_coop(Grid<R> g, Strides s, const StepParams* sp, int members,
+    const R* u_edg, const R* v_edg, const R* dp_edg, R* delp, R* massfx, R* dplo_tndcy, R* dp_tndcy, R* antifx,
+    R* delp_lo, R* p_plus, R* p_mnus, R* r_plus, R* r_mnus, int* flags, unsigned* bar, unsigned extra,
+    unsigned long long limit_ns) {
+  const int nvb = (int)(((long long)g.N * (g.L / VK) + kBlock - 1) / kBlock);
+  const int total = nvb * members;
+  for (int w = blockIdx.x; w < total; w += gridDim.x)
+    cnuity12_body<R, VK>(w % nvb, w / nvb, g, s, sp, u_edg, v_edg, dp_edg, delp, massfx, dplo_tndcy, antifx,
+                         delp_lo, p_plus, p_mnus);
+  if (!coop_barrier(bar, gridDim.x + extra, limit_ns, flags)) return;
+  for (int w = blockIdx.x; w < total; w += gridDim.x)
+    cnuity3_body<R, VK>(w % nvb, w / nvb, g, s, sp, delp_lo, delp, dp_tndcy, p_plus, p_mnus, r_plus, r_mnus);
+  if (!coop_barrier(bar, 2 * gridDim.x + extra, limit_ns, flags)) return;
+  for (int w = blockIdx.x; w < total; w += gridDim.x)
+    cnuity4_body<R, VK>(w % nvb, w / nvb, g, s, sp, antifx, r_plus, r_mnus, massfx, dplo_tndcy, dp_tndcy, delp,
+                        flags);
 }
 
 // cnuity5 (cnuity_compute.F90:408-445) for 32 columns per warp, 32 levels
@@ -1209,6 +1292,32 @@ void launch_cnuity(const Launch& l, const Grid<R>& g, const Strides& s, const Cn
                    R* delp, R* pres, R* exner, R* dp_tndcy, R* dplo_tndcy, R* massfx, R* omega) {
   const int vk = pick_vk<R>(g.L, {u_edg, v_edg, dp_edg, delp, massfx, dplo_tndcy, dp_tndcy, w.antifx, w.delp_lo,
                                   w.p_plus, w.p_mnus, w.r_plus, w.r_mnus});
+  if (l.coop) {
+    // one cooperative launch of as many blocks as the GPU holds at once
+    FIM_KBEGIN(l, "k_cnuity_coop");
+    cudaMemsetAsync(l.coop->barrier, 0, sizeof(unsigned), l.stream);
+    FIM_VK_DISPATCH(R, vk, ({
+      int dev = 0, sms = 0, per = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cnuity_coop<R, VK>, kBlock, 0);
+      const long long need = (long long)blocks_for((long long)g.N * (g.L / VK)) * l.members;
+      const unsigned nb = (unsigned)(need < (long long)sms * per ? need : (long long)sms * per);
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(nb > 0 ? nb : 1);
+      cfg.blockDim = dim3(kBlock);
+      cfg.stream = l.stream;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeCooperative;
+      attr[0].val.cooperative = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      cudaLaunchKernelEx(&cfg, k_cnuity_coop<R, VK>, g, s, l.sp, l.members, u_edg, v_edg, dp_edg, delp, massfx,
+                         dplo_tndcy, dp_tndcy, w.antifx, w.delp_lo, w.p_plus, w.p_mnus, w.r_plus, w.r_mnus,
+                         l.flags, l.coop->barrier, l.coop->extra, l.coop->limit_ns);
+    }));
+    FIM_KEND(l);
+  } else {
   FIM_KBEGIN(l, "k_cnuity12");
   FIM_VK_DISPATCH(R, vk, (k_cnuity12<R, VK><<<dim3(blocks_for((long long)g.N * (g.L / VK)), l.members), kBlock, 0,
                                               l.stream>>>(g, s, l.sp, u_edg, v_edg, dp_edg, delp, massfx,
@@ -1224,6 +1333,7 @@ void launch_cnuity(const Launch& l, const Grid<R>& g, const Strides& s, const Cn
                                              l.stream>>>(g, s, l.sp, w.antifx, w.r_plus, w.r_mnus, massfx,
                                                          dplo_tndcy, dp_tndcy, delp, l.flags)));
   FIM_KEND(l);
+  }
   dim3 gw((unsigned)((g.N + 32 * kC5Warps<R> - 1) / (32 * kC5Warps<R>)), l.members);
   FIM_KBEGIN(l, "k_cnuity5");
   k_cnuity5<R><<<gw, 32 * kC5Warps<R>, 0, l.stream>>>(g, s, l.sp, pres, delp, exner, dp_tndcy, omega, lp_edg, u,

@@ -45,6 +45,7 @@ enum : int {
   kFlagBadDp = 1,       // non-positive or NaN layer thickness after cnuity
   kFlagColumnIntegral = 2,  // hybgen column-integral conservation check failed
   kFlagNaN = 4,
+  kFlagTimeout = 8,     // a grid barrier of a persistent launch gave up waiting
 };
 
 // Relative tolerance of hybgen's column-integral checks: the reference's own
@@ -159,6 +160,7 @@ struct Prof {
 };
 
 // Launch context handed to every launcher.
+struct CoopCfg;
 struct Launch {
   cudaStream_t stream;
   int members;         // gridDim.y
@@ -170,6 +172,17 @@ struct Launch {
   // of step its-1): the column kernels then act for its-1 and skip a member
   // at its first step, where dyn_init's adjustment stands in
   int boundary = 0;
+  // non-null: cnuity1..4 run as one cooperative persistent launch
+  const CoopCfg* coop = nullptr;
+};
+
+// The persistent cnuity1..4 launch: its grid barrier's counter (device),
+// arrivals added to each barrier's target (0; a test sets 1 so that the first
+// barrier never completes) and the barrier's time limit.
+struct CoopCfg {
+  unsigned* barrier;
+  unsigned extra;
+  unsigned long long limit_ns;
 };
 
 #define FIM_KBEGIN(l, name) do { if ((l).prof && (l).prof->on) (l).prof->begin(name, (l).stream); } while (0)
@@ -227,6 +240,18 @@ template <typename R>
 __device__ __forceinline__ R fdiv(R a, R b) { return a / b; }
 template <>
 __device__ __forceinline__ float fdiv<float>(float a, float b) { return __fdividef(a, b); }
+
+// (cell, first level) of thread threadIdx.x of (virtual) block bx over
+// nip x (nvl/VK)
+template <int VK>
+__device__ __forceinline__ bool cell_levels_at(int N, int L, int bx, int& i, int& k) {
+  const int LV = L / VK;
+  const int gid = bx * blockDim.x + threadIdx.x;
+  if (gid >= N * LV) return false;
+  i = gid / LV;
+  k = (gid - i * LV) * VK;
+  return true;
+}
 
 // (cell, first level) of thread gid over nip x (nvl/VK)
 template <int VK>

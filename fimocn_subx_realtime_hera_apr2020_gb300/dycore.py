@@ -67,6 +67,16 @@ class Dycore:
     def launches(self):
         return self.lib.fim_launch_count(self.ctx)
 
+    def set_persistent(self, on, timeout_s=1.0):
+        """cnuity1..4 as one cooperative persistent launch (fim_set_persistent)."""
+        _lib.check(self.lib.fim_set_persistent(self.ctx, 1 if on else 0, float(timeout_s)), "fim_set_persistent",
+                   self.ctx)
+
+    def set_barrier_test(self, phantom_arrivals):
+        """1: the persistent launch's barriers wait for a block that never
+        arrives, so their time limit runs out (fim_set_barrier_test)."""
+        _lib.check(self.lib.fim_set_barrier_test(self.ctx, int(phantom_arrivals)), "fim_set_barrier_test", self.ctx)
+
     def device_bytes(self):
         """Device memory the context and its states currently own."""
         return self.lib.fim_ctx_device_bytes(self.ctx)

@@ -417,6 +417,21 @@ int fim_step_active(fim_ctx *ctx, fim_state *st, int use_graph);
  * Returns when every download has landed; *h2d_bytes and *d2h_bytes (may be
  * null) get the bytes moved.  FIM_ENOTSUP with member_group < members. */
 int fim_state_set_host(fim_ctx *ctx, fim_state *st, int field, int member, void *host);
+
+/* Persistent cnuity (no counterpart in the reference).  With on = 1, cnuity1
+ * to cnuity4 (cnuity_compute.F90:17-374) of every member run as one
+ * cooperative launch of as many blocks as the GPU holds at once, the stages
+ * separated by grid barriers instead of kernel boundaries; results are the
+ * kernel-per-stage path's bit for bit.  Each barrier gives up after timeout_s
+ * seconds (0 < timeout_s <= 60): the launch then ends, and fim_check returns
+ * FIM_ETIMEDOUT (that step's results are not valid; the context stays
+ * usable).  Applies to fim_step, fim_step_io and the per-routine cnuity from
+ * the next call on; a state's step graph is captured again.
+ * fim_set_barrier_test(ctx, 1) makes each barrier wait for one block more than
+ * the launch has, so that it runs out (the test of the time limit); 0 restores
+ * it. */
+int fim_set_persistent(fim_ctx *ctx, int on, double timeout_s);
+int fim_set_barrier_test(fim_ctx *ctx, int phantom_arrivals);
 int fim_step_io(fim_ctx *ctx, fim_state *st, int its, int64_t *h2d_bytes, int64_t *d2h_bytes);
 
 /* Member budgets after the last step (qmass, tracer integrals qtrcr(ntra)). */
