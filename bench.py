@@ -431,7 +431,10 @@ def reference_arm(args, ws, rank):
     sec = (time.perf_counter() - t0) / args.steps
     value = grid.nip * L / sec
     sample = ("CPU oracle (C restatement of the reference Fortran dycore routines, OpenMP, %d threads) on a "
-              "glvl-6 sample (40,962 cells) of the glvl-8 workload, nvl 64, 21 tracers, dt 180 s" % cores)
+              "glvl-6 sample (40,962 cells) of the glvl-8 workload: nvl 64, 21 tracers, dt 180 s (the glvl-8 "
+              "Courant number at 45 s), seed 3000, no wind noise; rates per cell-level compare with the GPU "
+              "arm's glvl-8 run; grid tables from this project's builder (the reference's numbering and "
+              "neighbour order, bit for bit), no GPU work" % cores)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic seeded balanced state",
