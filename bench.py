@@ -36,13 +36,20 @@ UNIT = "cell-level-steps/s"
 # L1/L2), summed over the tracers it handles.  Used for roofline.achieved.
 WORDS = {
     # the fused step averages only the layer thickness in edgvar3; the
-    # tracers' edge values come from k_tr_own and are averaged in k_tr_lo/hi
+    # tracers' edge values are formed on chip by k_trf_lo/k_trf_hi
     "k_edgvar1": lambda T: 41, "k_edgvar3_own": lambda T: 7, "k_edgvar3_avg": lambda T: 12,
     # edgvar2 (hiOrderUVComp): speeds and gradient (u, v, 6+6 edge winds in,
     # 3 out), then the correction (3 + 12 in, 18 out)
     "k_edgvar2_grad": lambda T: 17, "k_edgvar2": lambda T: 33,
-    "k_tr_own": lambda T: 7 * (T - 1), "k_tr_lo": lambda T: 15 * T + 7, "k_tr_lim": lambda T: 8 * T + 1,
-    "k_tr_hi": lambda T: 16 * T + 7,
+    # tracer transport on cell patches: per tracer, k_trf_lo reads the tracer,
+    # tracer x thickness and two low-order AB3 slots and writes one slot,
+    # trcr_lo, S+, S-, the old tracer's copy and six antidiffusive fluxes
+    # (15), and reads the mass fluxes (6), the thickness and theta's six edge
+    # values (13); k_trf_hi reads the copy, trcr_lo, S+, S-, two AB3 slots,
+    # the six fluxes, the low-order tendency and tracer x thickness and writes
+    # one slot, tracer x thickness and the tracer (17), and reads the
+    # thickness (1)
+    "k_trf_lo": lambda T: 15 * T + 13, "k_trf_hi": lambda T: 17 * T + 1,
     "k_cnuity12": lambda T: 37, "k_cnuity3": lambda T: 8, "k_cnuity4": lambda T: 26, "k_cnuity5": lambda T: 14,
     # cnuity1..4 as one persistent launch (--persistent): the three kernels' words
     "k_cnuity_coop": lambda T: 37 + 8 + 26,

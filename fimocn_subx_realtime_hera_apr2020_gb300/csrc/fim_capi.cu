@@ -82,10 +82,11 @@ struct fim_ctx {
        *t_rm = nullptr;
   int tchunk = 0;
   void *f_trcr_lo = nullptr, *f_sp = nullptr, *f_sm = nullptr, *f_trold = nullptr, *f_rp = nullptr,
-       *f_rm = nullptr;
+       *f_rm = nullptr, *f_af = nullptr;
   int ftchunk = 0;
   int trc_vk = 0;  // levels per thread of the fused tracer kernels (0: widest that nvl allows)
-  int trc_tb = 128;  // threads per block of the fused tracer kernels
+  int trc_gc = 4;   // threads per cell of a patch: level tile of trc_vk * trc_gc levels
+  FrameTab ftab{};  // cell patches of the fused tracer kernels (device tables)
   bool autotune = true, tuned = false;
   float tune_ms = 0.f;
   int TB = 0, dtratio = 6;  // class-B tracers and their time-step ratio
@@ -206,6 +207,37 @@ template <>
 Grid<double>& grid_of<double>(fim_ctx* c) { return c->gd; }
 template <>
 Grid<float>& grid_of<float>(fim_ctx* c) { return c->gf; }
+
+// The cell patches of the fused tracer kernels: 8 x 8 cells of a rhombus,
+// with the frame tables uploaded once per context.
+int build_patches(fim_ctx* c, const std::vector<int>& prox, const std::vector<int>& proxs,
+                  const std::vector<int>& nprox) {
+  FrameHost h;
+  int side = 8;
+  while (build_frames(c->N, prox.data(), proxs.data(), nprox.data(), side, &h) != 0) {
+    if (--side < 1) return set_err(c, FIM_EINVAL, "tracer patches: a frame exceeds 255 cells");
+  }
+  FrameTab& f = c->ftab;
+  f.ntile = h.ntile; f.S2 = h.S2; f.S1 = h.S1; f.SC = h.SC; f.SE = h.SE; f.SR = h.SR;
+  void* p;
+  int rc;
+  if ((rc = dalloc(c, &p, h.cells.size() * sizeof(int)))) return rc;
+  CK(cudaMemcpy(p, h.cells.data(), h.cells.size() * sizeof(int), cudaMemcpyHostToDevice), "patch cells");
+  f.cells = (const int*)p;
+  if ((rc = dalloc(c, &p, h.nbr.size() * sizeof(uint32_t)))) return rc;
+  CK(cudaMemcpy(p, h.nbr.data(), h.nbr.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "patch neighbours");
+  f.nbr = (const uint2*)p;
+  if ((rc = dalloc(c, &p, h.cnt.size() * sizeof(int)))) return rc;
+  CK(cudaMemcpy(p, h.cnt.data(), h.cnt.size() * sizeof(int), cudaMemcpyHostToDevice), "patch counts");
+  f.cnt = (const int4*)p;
+  if ((rc = dalloc(c, &p, h.mir.size() * sizeof(uint16_t)))) return rc;
+  CK(cudaMemcpy(p, h.mir.data(), h.mir.size() * sizeof(uint16_t), cudaMemcpyHostToDevice), "patch mirrors");
+  f.mir = (const unsigned short*)p;
+  if ((rc = dalloc(c, &p, h.red.size() * sizeof(uint16_t)))) return rc;
+  CK(cudaMemcpy(p, h.red.data(), h.red.size() * sizeof(uint16_t), cudaMemcpyHostToDevice), "patch ring edges");
+  f.redge = (const unsigned short*)p;
+  return FIM_OK;
+}
 
 template <typename R>
 int build_grid(fim_ctx* c, const fim_grid_desc* g, const std::vector<double>& rarea, const std::vector<double>& corio,
@@ -343,10 +375,16 @@ int ensure_trcadv(fim_ctx* c, int members) {
 
 int ensure_trc_fused(fim_ctx* c, int members) {
   if (c->f_trcr_lo) return FIM_OK;
+  {
+    const int e = c->prec == FIM_PREC_F64 ? prepare_tracers<double>(c->ftab) : prepare_tracers<float>(c->ftab);
+    if (e) return set_err(c, FIM_ECUDA, "tracer kernel attributes", (cudaError_t)e);
+  }
   const size_t NL = (size_t)c->N * c->L;
-  size_t per_tracer = NL * members * 6 * c->esz;
+  // per tracer of a chunk: trcr_lo, S+, S-, the old tracer, the probe's two
+  // outputs and six antidiffusive fluxes; chunks of at most ~24 GB
+  size_t per_tracer = NL * members * 12 * c->esz;
   int tch = c->T;
-  while (tch > 1 && per_tracer * tch > (size_t)12 << 30) tch = (tch + 1) / 2;
+  while (tch > 1 && per_tracer * tch > (size_t)24 << 30) tch = (tch + 1) / 2;
   c->ftchunk = tch;
   const size_t n = NL * members * tch;
   int rc;
@@ -356,6 +394,7 @@ int ensure_trc_fused(fim_ctx* c, int members) {
   if ((rc = ensure(c, &c->f_trold, n))) return rc;
   if ((rc = ensure(c, &c->f_rp, n))) return rc;
   if ((rc = ensure(c, &c->f_rm, n))) return rc;
+  if ((rc = ensure(c, &c->f_af, n * 6))) return rc;
   return FIM_OK;
 }
 
@@ -1027,12 +1066,12 @@ int enqueue_step(fim_ctx* c, fim_state* st, StepIo* io = nullptr) {
       launch_edgvar2<R>(lg, g, s, P(FIM_US3D), P(FIM_VS3D), P(FIM_U_EDG), P(FIM_V_EDG), P(FIM_UVSQ_EDG),
                         (R*)c->e2w);
     if (c->kn.hi_order) {
-      // own-side dp and tracer edge values; the two-sided averages are formed
-      // where they are used (k_cnuity12 for dp; k_tr_lo/k_tr_hi for the
-      // tracers); mass_adv reads the averaged dp edges, so it keeps the pass
+      // own-side dp edge values; the two-sided average is formed where it is
+      // used (k_cnuity12); mass_adv reads the averaged dp edges, so it keeps
+      // the pass.  The tracers' edge values are formed on chip by the tracer
+      // kernels
       launch_edgvar3<R>(lg, g, s, P(FIM_DP3D), P(FIM_TR3D), P(FIM_DP_EDG), P(FIM_TRC_EDG),
                         1, c->cfg.flux_conserv_schm != 1);
-      launch_tracer_own<R>(lg, g, s, P(FIM_TR3D), P(FIM_TRC_EDG), c->trc_vk, c->trc_tb);
     }
     CnuityScratch<R> cw{(R*)c->antifx, (R*)c->delp_lo, (R*)c->p_plus, (R*)c->p_mnus, (R*)c->r_plus, (R*)c->r_mnus};
     if (io && (rc = io_wait(*io, io->up_ev[kIoC]))) return rc;
@@ -1071,7 +1110,8 @@ int enqueue_step(fim_ctx* c, fim_state* st, StepIo* io = nullptr) {
     if (io && (rc = momentum())) return rc;
     if (c->kn.hi_order) {
       TrcFusedScratch<R> fw{(R*)c->f_trcr_lo, (R*)c->f_sp, (R*)c->f_sm, (R*)c->f_trold, (R*)c->f_rp, (R*)c->f_rm,
-                            io ? io->tchunk : c->ftchunk, c->trc_vk, c->trc_tb};
+                            (R*)c->f_af,
+                            io ? io->tchunk : c->ftchunk, c->trc_vk, c->trc_gc, c->ftab};
       launch_tracers_fused<R>(lg, g, s, fw, P(FIM_TRC_EDG), P(FIM_TR3D), P(FIM_TRDP),
                               P(FIM_TRC_TDCY), P(FIM_TRL_TDCY), P(FIM_MASSFX),
                               P(FIM_DP3D), io ? &io->hook : nullptr);
@@ -1252,14 +1292,15 @@ int autotune_impl(fim_ctx* c, fim_state* st) {
      "tune params");
   Launch l = make_launch(c, c->G < c->M ? c->G : c->M);
   TrcFusedScratch<R> fw{(R*)c->f_trcr_lo, (R*)c->f_sp, (R*)c->f_sm, (R*)c->f_trold, (R*)c->f_rp, (R*)c->f_rm,
-                        c->ftchunk, c->trc_vk, c->trc_tb};
-  int vk = c->trc_vk, tb = c->trc_tb;
+                            (R*)c->f_af,
+                        c->ftchunk, c->trc_vk, c->trc_gc, c->ftab};
+  int vk = c->trc_vk, gc = c->trc_gc;
   const int e = tune_tracers<R>(l, grid_of<R>(c), c->str, fw, F<R>(st, FIM_TRC_EDG), F<R>(st, FIM_TR3D),
                                 F<R>(st, FIM_TRDP), F<R>(st, FIM_TRC_TDCY), F<R>(st, FIM_TRL_TDCY),
-                                F<R>(st, FIM_MASSFX), F<R>(st, FIM_DP3D), &vk, &tb, &c->tune_ms);
+                                F<R>(st, FIM_MASSFX), F<R>(st, FIM_DP3D), &vk, &gc, &c->tune_ms);
   if (e) return set_err(c, FIM_ECUDA, "tracer shape autotuning", (cudaError_t)e);
   c->trc_vk = vk;
-  c->trc_tb = tb;
+  c->trc_gc = gc;
   c->tuned = true;
   return push_sp(c);
 }
@@ -1305,12 +1346,13 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
   c->dtratio = cfg->dtratio;
   c->G = (cfg->member_group > 0 && cfg->member_group < c->M) ? cfg->member_group : c->M;
   c->str = make_strides(c->N, c->L, c->T, c->TB);
-  // FIM_TRC_VK=1|2|4 and FIM_TRC_TB=128|256 pin the fused tracer kernels'
-  // shape; FIM_AUTOTUNE=0 keeps the default shape untimed
+  // FIM_TRC_VK=1|2|4 and FIM_TRC_GC=2|4 pin the fused tracer kernels'
+  // shape (levels per thread, threads per cell); FIM_AUTOTUNE=0 keeps the
+  // default shape untimed
   if (const char* v = getenv("FIM_TRC_VK")) c->trc_vk = atoi(v);
-  if (const char* v = getenv("FIM_TRC_TB")) c->trc_tb = atoi(v) == 256 ? 256 : 128;
+  if (const char* v = getenv("FIM_TRC_GC")) c->trc_gc = atoi(v) >= 4 ? 4 : 2;
   if (const char* v = getenv("FIM_AUTOTUNE")) c->autotune = atoi(v) != 0;
-  if (getenv("FIM_TRC_VK") || getenv("FIM_TRC_TB")) c->autotune = false;
+  if (getenv("FIM_TRC_VK") || getenv("FIM_TRC_GC")) c->autotune = false;
   const int N = c->N, L = c->L;
   // 0-based index tables; validate the Fortran numbering
   std::vector<int> prox(N * 6), proxs(N * 6), nprox(N);
@@ -1386,6 +1428,7 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
   int rc = build_grid<double>(c, g, rarea, corio, grnd, dfflen, biharw, smoo, prox, proxs, nprox);
   if (!rc && c->prec == FIM_PREC_F32)
     rc = build_grid<float>(c, g, rarea, corio, grnd, dfflen, biharw, smoo, prox, proxs, nprox);
+  if (!rc && c->kn.hi_order) rc = build_patches(c, prox, proxs, nprox);
   if (!rc) rc = dalloc(c, (void**)&c->d_sp, sizeof(StepParams) * c->M);
   if (!rc) rc = dalloc(c, (void**)&c->d_flags, sizeof(int) * c->M);
   if (!rc) {
@@ -2028,7 +2071,7 @@ int fim_profile_report(fim_ctx* c, char* buf, int len) {
 int fim_tracer_shape(const fim_ctx* c, int* levels_per_thread, int* threads_per_block, float* probe_ms) {
   if (!c) return FIM_EINVAL;
   if (levels_per_thread) *levels_per_thread = c->trc_vk;
-  if (threads_per_block) *threads_per_block = c->trc_tb;
+  if (threads_per_block) *threads_per_block = c->ftab.SC * c->trc_gc;
   if (probe_ms) *probe_ms = c->tuned ? c->tune_ms : 0.f;
   return FIM_OK;
 }

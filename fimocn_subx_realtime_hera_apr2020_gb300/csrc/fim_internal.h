@@ -359,20 +359,49 @@ template <typename R>
 void launch_trcadv(const Launch&, const Grid<R>&, const Strides&, const TrcadvScratch<R>&,
                    const R* trc_edg, R* tracr, R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx,
                    const R* delp);
+// Cell patches of the fused tracer kernels (fim_trc.cu).  A patch is a set
+// of interior cells; its frame lists them first, then every other cell one
+// neighbour step away (ring 1), then two steps away (ring 2), so a block can
+// stage the frame in shared memory and find every neighbour it needs there.
+struct FrameTab {
+  int ntile = 0;
+  // capacities: frame cells, interior + ring-1 cells, interior cells,
+  // edge-value rows (6 per interior cell + ring edges), ring edges
+  int S2 = 0, S1 = 0, SC = 0, SE = 0, SR = 0;
+  const int* cells = nullptr;            // [ntile][S2] cell index, frame order
+  const uint2* nbr = nullptr;            // [ntile][S1] frame-local index of prox slots 0..5, a byte each
+  const int4* cnt = nullptr;             // [ntile] interior cells, + ring 1, + ring 2, ring edges
+  const unsigned short* mir = nullptr;   // [ntile][SC][6] edge-value row of the other side of each edge
+  const unsigned short* redge = nullptr; // [ntile][SR] ring edges: (frame-local cell << 3) | slot
+};
+struct FrameHost {
+  int ntile = 0, S2 = 0, S1 = 0, SC = 0, SE = 0, SR = 0;
+  std::vector<int> cells, cnt;
+  std::vector<uint32_t> nbr;
+  std::vector<uint16_t> mir, red;
+};
+// patches of side x side cells of each rhombus (the reference's IJ
+// numbering), else grown breadth-first; 0 on success
+int build_frames(int N, const int* prox, const int* proxs, const int* nprox, int side, FrameHost* out);
 // fused tracer path of the step (fim_trc.cu)
 template <typename R>
 struct TrcFusedScratch {
-  R *trcr_lo, *s_plus, *s_mnus, *trold, *r_plus, *r_mnus;
+  R *trcr_lo, *s_plus, *s_mnus, *trold;
+  R *r_plus, *r_mnus;  // scratch for the shape probe's outputs
+  R* antifx;           // antidiffusive fluxes (6 per cell-level) of the chunk
   int tchunk;
   int vk;  // levels per thread (0: widest the layout admits)
-  int tb;  // threads per block, 128 or 256
+  int gc;  // threads per cell and level tile: the tile is vk * gc levels
+  FrameTab ft;
 };
+// one-time launch attributes (shared-memory size) of the tracer kernels for
+// these patches; returns a cudaError_t value
 template <typename R>
-void launch_tracer_own(const Launch&, const Grid<R>&, const Strides&, const R* tracr, R* trc_edg, int vk, int tb);
+int prepare_tracers(const FrameTab& ft);
 // times the tracer kernel shapes on the given state (see fim_trc.cu); returns a cudaError_t value
 template <typename R>
 int tune_tracers(const Launch&, const Grid<R>&, const Strides&, const TrcFusedScratch<R>&, R* trc_edg, R* tracr,
-                 R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx, const R* delp, int* best_vk, int* best_tb,
+                 R* trcdp, R* trc_tdcy, R* trl_tdcy, const R* massfx, const R* delp, int* best_vk, int* best_gc,
                  float* best_ms);
 // Called by launch_tracers_fused before (phase 0) and after (phase 1) the
 // kernels of each tracer chunk [t0, t0 + nt): the step with host transfers
