@@ -79,17 +79,19 @@ __device__ __forceinline__ int nb_at(uint2 nb, int e) {
 
 // Shared-memory layout of the two kernels (offsets in elements of R, then the
 // patch tables after a 16-byte boundary).
-//   lo: tracer frame x 2 buffers [S2][LK]; edge values [SE][LK]; the patch
-//       cells' low-order AB3 slots of and vof and tracer x thickness, x 2
-//       buffers [3][SC][LK]; least-squares coefficients, 36 per patch cell
-//       (row stride 36), then 6 per ring edge.
+//   lo: tracer frame x 2 buffers [S2][LK]; edge values [SE][LK]; mass
+//       fluxes [SE][LK] in the rows of the edge values (the patch cells' six
+//       slots, then the ring edges' neighbour sides); the patch cells'
+//       low-order AB3 slots of and vof and tracer x thickness, x 2 buffers
+//       [3][SC][LK]; least-squares coefficients, 36 per patch cell (row
+//       stride 36), then 6 per ring edge.
 //   hi: old-tracer and trcr_lo frames [S2][LK]; the ring-1 frame's AB3 slots
 //       of and vof, S+ and S- [4][S1][LK]; R+, R- [S1][LK]; the patch cells'
 //       antidiffusive fluxes [SC][6][LK], low-order tendency and tracer x
 //       thickness [SC][LK]; the ring-1 frame's thickness [S1][LK] and cell
 //       areas [S1].
 struct PatchLayout {
-  size_t trs, E, ops, hf;                              // lo
+  size_t trs, E, mf, ops, hf;                          // lo
   size_t TO, TL, opq, Rp, Rm, af, tlt, tdb, dpf, arf;  // hi
   size_t r_elems, tab, bytes;
   template <typename R>
@@ -100,6 +102,7 @@ struct PatchLayout {
     if (!hi) {
       p.trs = o; o += 2 * S2 * LK;
       p.E = o; o += SE * LK;
+      p.mf = o; o += SE * LK;
       p.ops = o; o += 2 * 3 * SC * LK;
       p.hf = o; o += SC * 36 + SR * 6;
     } else {
@@ -234,18 +237,17 @@ __device__ __forceinline__ void ring_value(const R* T, const FrameSm& fs, const 
 }
 
 // The thread's patch cell and levels (one per thread: the block has SC * GC
-// threads), with the tracer-independent operands it keeps in registers for
-// the whole tracer loop: the mass fluxes of its six edges, own side and
-// neighbour side, and the layer thickness.
+// threads), with the layer thickness, which it keeps in registers for the
+// whole tracer loop.
 template <typename R, int VK>
 struct CellItem {
   bool on;
   int i, x, v, k, c, np;
   R rar;
-  R mf[6][VK], mfx[6][VK], dp[VK];
+  R dp[VK];
   template <int GC>
   __device__ __forceinline__ void load(const Grid<R>& g, const Strides& s, const FrameSm& fs, size_t m,
-                                       const R* mfn, const R* delp, int C, int k0, int lk) {
+                                       const R* delp, int C, int k0, int lk) {
     x = threadIdx.x / GC;
     v = (threadIdx.x - x * GC) * VK;
     on = x < C && v < lk;
@@ -256,16 +258,6 @@ struct CellItem {
     c = i * L + k;
     np = fs.np[x];
     rar = g.rarea[i];
-    const uint2 nb = fs.nbr[x];
-#pragma unroll
-    for (int e = 0; e < 6; e++) {
-      if (e < 5 || e < np) {
-        ldv<VK>(mfn + (i * 6 + e) * L + k, mf[e]);
-        ldv<VK>(mfn + (fs.cells[nb_at(nb, e)] * 6 + g.proxs[i * 6 + e]) * L + k, mfx[e]);
-      } else {
-        FOR_V { mf[e][j] = R(0); mfx[e][j] = R(0); }
-      }
-    }
     ldv<VK>(delp + m * s.cell + c, dp);
   }
 };
@@ -293,6 +285,7 @@ __global__ void __launch_bounds__(64 * GC, 8 / GC) k_trf_lo(Grid<R> g, Strides s
   R* const sr = reinterpret_cast<R*>(fsm);
   R* const trs = sr + lay.trs;
   R* const E = sr + lay.E;
+  R* const MF = sr + lay.mf;
   R* const ops = sr + lay.ops;
   R* const hf = sr + lay.hf;
   const FrameSm fs = load_tables<R>(g, ft, fsm, lay.tab, tile, C, n1, n2, nre);
@@ -315,9 +308,25 @@ __global__ void __launch_bounds__(64 * GC, 8 / GC) k_trf_lo(Grid<R> g, Strides s
     stage_rows<R, VK, GC>(o + 2 * ft.SC * LK, trcdp + m * s.tr + (size_t)t * NL + k0, fs.cells, C, lk, L);
     stage_commit();
   };
+  // the mass fluxes of the patch cells' edges and of the ring edges'
+  // neighbour sides (tracer independent), with the first tracer's operands
+  for (int it = threadIdx.x; it < (6 * C + nre) * GC; it += blockDim.x) {
+    const int r = it / GC, v = (it - r * GC) * VK;
+    if (v >= lk) continue;
+    int cell, slot;
+    if (r < 6 * C) {
+      cell = fs.cells[r / 6];
+      slot = r % 6;
+    } else {
+      const int code = fs.red[r - 6 * C];
+      cell = fs.cells[code >> 3];
+      slot = code & 7;
+    }
+    stage_copy<VK * (int)sizeof(R)>(MF + r * LK + v, mfn + (cell * 6 + slot) * L + k0 + v);
+  }
   stage(t0, 0);
   CellItem<R, VK> ci;
-  ci.template load<GC>(g, s, fs, m, mfn, delp, C, k0, lk);
+  ci.template load<GC>(g, s, fs, m, delp, C, k0, lk);
   for (int tz = 0; tz < nt; tz++) {
     const int t = t0 + tz, b = tz & 1;
     stage_wait();
@@ -366,8 +375,11 @@ __global__ void __launch_bounds__(64 * GC, 8 / GC) k_trf_lo(Grid<R> g, Strides s
           ldv<VK>(te0 + (i * 6 + e) * L + ci.k, tev);
         }
         R anti[VK];
+        R mfo[VK], mfm[VK];
+        ldv<VK>(MF + (x * 6 + e) * LK + v, mfo);
+        ldv<VK>(MF + fs.mir[x * 6 + e] * LK + v, mfm);
         FOR_V {
-          const R mf = ci.mf[e][j], mfx = ci.mfx[e][j];
+          const R mf = mfo[j], mfx = mfm[j];
           const R hi = mf * tev[j];
           const R lo = half * ((mf + tabs(mf)) * tri[j] - (mfx + tabs(mfx)) * trx[j]);
           anti[j] = hi - lo;
