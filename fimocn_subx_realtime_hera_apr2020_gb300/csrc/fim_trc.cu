@@ -72,6 +72,13 @@ __device__ __forceinline__ void stage_copy(void* smem, const void* gmem) {
 __device__ __forceinline__ void stage_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// Row of slot e of patch cell x in the edge-indexed shared arrays (edge
+// values, mass fluxes, antidiffusive fluxes): the slots of odd cells are
+// swapped in pairs, so the same slot of two consecutive cells falls in
+// different halves of the shared-memory banks (rows of 64 bytes).  The
+// patch tables' mirror rows use the same mapping.
+__host__ __device__ __forceinline__ int erow(int x, int e) { return x * 6 + (e ^ (x & 1)); }
+
 // frame-local index of prox slot e (one byte each, slots 0..3 in x, 4..5 in y)
 __device__ __forceinline__ int nb_at(uint2 nb, int e) {
   return e < 4 ? (int)((nb.x >> (8 * e)) & 255u) : (int)((nb.y >> (8 * (e - 4))) & 255u);
@@ -210,7 +217,7 @@ __device__ __forceinline__ void own_values(const R* hf, int x, int v, const R (&
       FOR_V val[j] = (e < 5 || e < np) ? val[j] + d[e][j] * h[e] : val[j];
     }
     FOR_V val[j] = (ie < 5 || ie < np) ? val[j] : R(0);
-    stv<VK>(E + (x * 6 + ie) * LK + v, val);
+    stv<VK>(E + erow(x, ie) * LK + v, val);
   }
 }
 
@@ -313,16 +320,18 @@ __global__ void __launch_bounds__(64 * GC, 8 / GC) k_trf_lo(Grid<R> g, Strides s
   for (int it = threadIdx.x; it < (6 * C + nre) * GC; it += blockDim.x) {
     const int r = it / GC, v = (it - r * GC) * VK;
     if (v >= lk) continue;
-    int cell, slot;
+    int cell, slot, row = r;
     if (r < 6 * C) {
-      cell = fs.cells[r / 6];
-      slot = r % 6;
+      const int x = r / 6;
+      cell = fs.cells[x];
+      slot = r - x * 6;
+      row = erow(x, slot);
     } else {
       const int code = fs.red[r - 6 * C];
       cell = fs.cells[code >> 3];
       slot = code & 7;
     }
-    stage_copy<VK * (int)sizeof(R)>(MF + r * LK + v, mfn + (cell * 6 + slot) * L + k0 + v);
+    stage_copy<VK * (int)sizeof(R)>(MF + row * LK + v, mfn + (cell * 6 + slot) * L + k0 + v);
   }
   stage(t0, 0);
   CellItem<R, VK> ci;
@@ -368,7 +377,7 @@ __global__ void __launch_bounds__(64 * GC, 8 / GC) k_trf_lo(Grid<R> g, Strides s
         R tev[VK];
         if (t != 0) {
           R tem[VK];
-          ldv<VK>(E + (x * 6 + e) * LK + v, tev);
+          ldv<VK>(E + erow(x, e) * LK + v, tev);
           ldv<VK>(E + fs.mir[x * 6 + e] * LK + v, tem);
           FOR_V tev[j] = half * (tev[j] + tem[j]);
         } else {
@@ -376,7 +385,7 @@ __global__ void __launch_bounds__(64 * GC, 8 / GC) k_trf_lo(Grid<R> g, Strides s
         }
         R anti[VK];
         R mfo[VK], mfm[VK];
-        ldv<VK>(MF + (x * 6 + e) * LK + v, mfo);
+        ldv<VK>(MF + erow(x, e) * LK + v, mfo);
         ldv<VK>(MF + fs.mir[x * 6 + e] * LK + v, mfm);
         FOR_V {
           const R mf = mfo[j], mfx = mfm[j];
@@ -527,8 +536,8 @@ __global__ void __launch_bounds__(64 * GC) k_trf_hi(Grid<R> g, Strides s, FrameT
     const R* a = antifx + (m * nt + tz) * 6 * sc + k0;
     for (int it = threadIdx.x; it < C * 6 * GC; it += blockDim.x) {
       const int r = it / GC, v = (it - r * GC) * VK;  // r = x * 6 + e
-      const int x = r / 6;
-      if (v < lk) stage_copy<VK * (int)sizeof(R)>(af + r * LK + v, a + (fs.cells[x] * 6 + (r - x * 6)) * L + v);
+      const int x = r / 6, e = r - x * 6;
+      if (v < lk) stage_copy<VK * (int)sizeof(R)>(af + erow(x, e) * LK + v, a + (fs.cells[x] * 6 + e) * L + v);
     }
     const size_t tt = (size_t)(t0 + tz);
     stage_rows<R, VK, GC>(tlt, trl_tdcy + m * s.trab + tt * 3 * NL + (size_t)nf * NL + k0, fs.cells, C, lk, L);
@@ -571,7 +580,7 @@ __global__ void __launch_bounds__(64 * GC) k_trf_hi(Grid<R> g, Strides s, FrameT
       if (e < 5 || e < np) {
         const int y = nb_at(nb, e);
         R a[VK], rpx[VK], rmx[VK];
-        ldv<VK>(af + (x * 6 + e) * LK + v, a);
+        ldv<VK>(af + erow(x, e) * LK + v, a);
         ldv<VK>(Rp + y * LK + v, rpx);
         ldv<VK>(Rm + y * LK + v, rmx);
         FOR_V {
@@ -760,10 +769,10 @@ int build_frames(int N, const int* prox, const int* proxs, const int* nprox, int
     for (int x = 0; x < f.C; x++) {
       const int c = f.cells[x];
       for (int e = 0; e < 6; e++) {
-        if (e >= nprox[c]) { f.mir[(size_t)x * 6 + e] = (uint16_t)(x * 6 + e); continue; }
+        if (e >= nprox[c]) { f.mir[(size_t)x * 6 + e] = (uint16_t)erow(x, e); continue; }
         const int y = loc[prox[c * 6 + e]], p = proxs[c * 6 + e];
         if (y < f.C) {
-          f.mir[(size_t)x * 6 + e] = (uint16_t)(y * 6 + p);
+          f.mir[(size_t)x * 6 + e] = (uint16_t)erow(y, p);
         } else {
           f.mir[(size_t)x * 6 + e] = (uint16_t)(6 * f.C + f.red.size());
           f.red.push_back((uint16_t)((y << 3) | p));
