@@ -381,10 +381,11 @@ int ensure_trc_fused(fim_ctx* c, int members) {
   }
   const size_t NL = (size_t)c->N * c->L;
   // per tracer of a chunk: trcr_lo, S+, S-, the old tracer, the probe's two
-  // outputs and six antidiffusive fluxes; chunks of at most ~24 GB
+  // outputs and six antidiffusive fluxes; chunks of at most ~48 GB (glvl 8,
+  // nvl 64, 21 tracers: one chunk of 42 GB)
   size_t per_tracer = NL * members * 12 * c->esz;
   int tch = c->T;
-  while (tch > 1 && per_tracer * tch > (size_t)24 << 30) tch = (tch + 1) / 2;
+  while (tch > 1 && per_tracer * tch > (size_t)48 << 30) tch = (tch + 1) / 2;
   c->ftchunk = tch;
   const size_t n = NL * members * tch;
   int rc;
