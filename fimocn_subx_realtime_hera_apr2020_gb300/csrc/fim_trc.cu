@@ -187,6 +187,44 @@ __device__ __forceinline__ void stage_rows(R* dst, const R* src, const int* cell
   }
 }
 
+// The frame rows a thread copies.  The block has SC * GC threads and GC
+// threads take one row, so thread (x0, v) takes rows x0, x0 + SC, x0 + 2 SC
+// of every frame field (the frame lists interior, ring-1 and ring-2 cells in
+// that order, so a field over its first n rows takes the rows below n).  The
+// element offsets of those rows' level tiles are formed once per block; a
+// copy is then an add and one cp.async.  Frames of more than 3 SC cells (the
+// small patches of coarse grids) take the general loop.
+template <typename R, int VK, int GC>
+struct RowPlan {
+  int x0, v, off[3];
+  bool fast;
+  __device__ __forceinline__ void init(const FrameSm& fs, int SC, int n2, int lk, int L) {
+    x0 = threadIdx.x / GC;
+    v = (threadIdx.x - x0 * GC) * VK;
+    fast = n2 <= 3 * SC;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const int x = x0 + j * SC;
+      off[j] = (x < n2 && v < lk) ? fs.cells[x] * L + v : -1;
+    }
+  }
+  // rows [0, n) of the field at src (offset to the tile's first level) into
+  // dst[x * LK + level]
+  __device__ __forceinline__ void copy(R* dst, const R* src, const FrameSm& fs, int SC, int n, int lk,
+                                       int L) const {
+    constexpr int LK = VK * GC;
+    if (fast) {
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        const int x = x0 + j * SC;
+        if (x < n && off[j] >= 0) stage_copy<VK * (int)sizeof(R)>(dst + x * LK + v, src + off[j]);
+      }
+    } else {
+      stage_rows<R, VK, GC>(dst, src, fs.cells, n, lk, L);
+    }
+  }
+};
+
 // six coefficients hf[0..6) as three pairs (8- or 16-byte shared loads)
 template <typename R>
 __device__ __forceinline__ void coef6(const R* hf, R (&h)[6]) {
@@ -306,13 +344,15 @@ __global__ void __launch_bounds__(64 * GC, 8 / GC) k_trf_lo(Grid<R> g, Strides s
   const R* te0 = trc_edg + m * s.tredg;  // theta (t = 0): edgvar1's edge values
   // this step's tracer t: its frame, and the patch cells' AB3 slots of/vof
   // and tracer x thickness
+  RowPlan<R, VK, GC> rp;
+  rp.init(fs, ft.SC, n2, lk, L);
   auto stage = [&](int t, int b) {
-    stage_rows<R, VK, GC>(trs + b * ft.S2 * LK, tracr + m * s.tr + (size_t)t * NL + k0, fs.cells, n2, lk, L);
+    rp.copy(trs + b * ft.S2 * LK, tracr + m * s.tr + (size_t)t * NL + k0, fs, ft.SC, n2, lk, L);
     const R* tl = trl_tdcy + m * s.trab + (size_t)t * 3 * NL + k0;
     R* o = ops + b * 3 * ft.SC * LK;
-    stage_rows<R, VK, GC>(o, tl + (size_t)of * NL, fs.cells, C, lk, L);
-    stage_rows<R, VK, GC>(o + ft.SC * LK, tl + (size_t)vof * NL, fs.cells, C, lk, L);
-    stage_rows<R, VK, GC>(o + 2 * ft.SC * LK, trcdp + m * s.tr + (size_t)t * NL + k0, fs.cells, C, lk, L);
+    rp.copy(o, tl + (size_t)of * NL, fs, ft.SC, C, lk, L);
+    rp.copy(o + ft.SC * LK, tl + (size_t)vof * NL, fs, ft.SC, C, lk, L);
+    rp.copy(o + 2 * ft.SC * LK, trcdp + m * s.tr + (size_t)t * NL + k0, fs, ft.SC, C, lk, L);
     stage_commit();
   };
   // the mass fluxes of the patch cells' edges and of the ring edges'
@@ -519,29 +559,33 @@ __global__ void __launch_bounds__(64 * GC) k_trf_hi(Grid<R> g, Strides s, FrameT
   const R rab1 = R(1) / ab1;  // Q+/Q- divide by ab1: one reciprocal (as k_trcadv2)
   const R thshld = R(1.e-11);
   // the limiters' operands of tracer t0 + tz
+  RowPlan<R, VK, GC> rp;
+  rp.init(fs, ft.SC, n2, lk, L);
   auto stage_lim = [&](int tz) {
     const size_t so = (m * nt + tz) * sc + k0;
-    stage_rows<R, VK, GC>(TO, trold + so, fs.cells, n2, lk, L);
-    stage_rows<R, VK, GC>(TL, trcr_lo + so, fs.cells, n2, lk, L);
+    rp.copy(TO, trold + so, fs, ft.SC, n2, lk, L);
+    rp.copy(TL, trcr_lo + so, fs, ft.SC, n2, lk, L);
     const R* tc = trc_tdcy + m * s.trab + (size_t)(t0 + tz) * 3 * NL + k0;
-    stage_rows<R, VK, GC>(opq, tc + (size_t)of * NL, fs.cells, n1, lk, L);
-    stage_rows<R, VK, GC>(opq + ft.S1 * LK, tc + (size_t)vof * NL, fs.cells, n1, lk, L);
-    stage_rows<R, VK, GC>(opq + 2 * ft.S1 * LK, s_plus + so, fs.cells, n1, lk, L);
-    stage_rows<R, VK, GC>(opq + 3 * ft.S1 * LK, s_mnus + so, fs.cells, n1, lk, L);
+    rp.copy(opq, tc + (size_t)of * NL, fs, ft.SC, n1, lk, L);
+    rp.copy(opq + ft.S1 * LK, tc + (size_t)vof * NL, fs, ft.SC, n1, lk, L);
+    rp.copy(opq + 2 * ft.S1 * LK, s_plus + so, fs, ft.SC, n1, lk, L);
+    rp.copy(opq + 3 * ft.S1 * LK, s_mnus + so, fs, ft.SC, n1, lk, L);
     stage_commit();
   };
   // the clip's operands: the patch cells' six fluxes, low-order tendency
   // (slot nf) and tracer x thickness
+  // (each thread copies the six flux rows of its own cell)
+  const int afo = (rp.x0 < C && rp.v < lk) ? fs.cells[rp.x0] * 6 * L + rp.v : -1;
   auto stage_clip = [&](int tz) {
     const R* a = antifx + (m * nt + tz) * 6 * sc + k0;
-    for (int it = threadIdx.x; it < C * 6 * GC; it += blockDim.x) {
-      const int r = it / GC, v = (it - r * GC) * VK;  // r = x * 6 + e
-      const int x = r / 6, e = r - x * 6;
-      if (v < lk) stage_copy<VK * (int)sizeof(R)>(af + erow(x, e) * LK + v, a + (fs.cells[x] * 6 + e) * L + v);
+    if (afo >= 0) {
+#pragma unroll
+      for (int e = 0; e < 6; e++)
+        stage_copy<VK * (int)sizeof(R)>(af + erow(rp.x0, e) * LK + rp.v, a + afo + e * L);
     }
     const size_t tt = (size_t)(t0 + tz);
-    stage_rows<R, VK, GC>(tlt, trl_tdcy + m * s.trab + tt * 3 * NL + (size_t)nf * NL + k0, fs.cells, C, lk, L);
-    stage_rows<R, VK, GC>(tdb, trcdp + m * s.tr + tt * NL + k0, fs.cells, C, lk, L);
+    rp.copy(tlt, trl_tdcy + m * s.trab + tt * 3 * NL + (size_t)nf * NL + k0, fs, ft.SC, C, lk, L);
+    rp.copy(tdb, trcdp + m * s.tr + tt * NL + k0, fs, ft.SC, C, lk, L);
     stage_commit();
   };
   stage_rows<R, VK, GC>(dpf, delp + m * s.cell + k0, fs.cells, n1, lk, L);
