@@ -87,6 +87,7 @@ _SIGS = {
     "fim_launch_count": ([_VP], ctypes.c_int64),
     "fim_ctx_device_bytes": ([_VP], ctypes.c_int64),
     "fim_tracer_shape": ([_VP, _VP, _VP, _VP], _I),
+    "fim_grid_patches": ([_VP, _I, _VP, _VP, _VP, _VP], _I),
     "fim_profile_enable": ([_VP, _I], _I),
     "fim_profile_report": ([_VP, ctypes.c_char_p, _I], _I),
     "fim_cnuity_noalloc": ([_VP, _I] + [_VP] * 13, _I),

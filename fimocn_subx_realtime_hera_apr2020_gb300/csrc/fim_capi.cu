@@ -208,6 +208,36 @@ Grid<double>& grid_of<double>(fim_ctx* c) { return c->gd; }
 template <>
 Grid<float>& grid_of<float>(fim_ctx* c) { return c->gf; }
 
+// 0-based index tables from the grid's Fortran ones, validated: nprox 5 or
+// 6, neighbours in range, and every edge has a mirror, prox(proxs(e),
+// prox(e)) == i (edgvar3's two-sided averages and trcadv's mirror mass
+// fluxes read the neighbour's side through it).
+int index_tables(const fim_grid_desc* g, std::vector<int>& prox, std::vector<int>& proxs, std::vector<int>& nprox) {
+  const int N = g->nip;
+  if (N < 12 || !g->prox || !g->proxs || !g->nprox) return FIM_EINVAL;
+  prox.assign((size_t)N * 6, 0);
+  proxs.assign((size_t)N * 6, 0);
+  nprox.assign(N, 0);
+  for (int i = 0; i < N; i++) {
+    nprox[i] = g->nprox[i];
+    if (nprox[i] != 5 && nprox[i] != 6) return FIM_EINVAL;
+    for (int e = 0; e < 6; e++) {
+      const int p = g->prox[i * 6 + e] - 1;
+      if (p < 0 || p >= N) return FIM_EINVAL;
+      prox[i * 6 + e] = p;
+      const int q = g->proxs[i * 6 + e];
+      proxs[i * 6 + e] = (e < nprox[i]) ? q - 1 : -1;
+      if (e < nprox[i] && (q < 1 || q > 6)) return FIM_EINVAL;
+    }
+  }
+  for (int i = 0; i < N; i++)
+    for (int e = 0; e < nprox[i]; e++) {
+      const int x = prox[i * 6 + e];
+      if (x == i || prox[x * 6 + proxs[i * 6 + e]] != i) return FIM_EINVAL;
+    }
+  return FIM_OK;
+}
+
 // The cell patches of the fused tracer kernels: 8 x 8 cells of a rhombus,
 // with the frame tables uploaded once per context.
 int build_patches(fim_ctx* c, const std::vector<int>& prox, const std::vector<int>& proxs,
@@ -1355,27 +1385,8 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
   if (const char* v = getenv("FIM_AUTOTUNE")) c->autotune = atoi(v) != 0;
   if (getenv("FIM_TRC_VK") || getenv("FIM_TRC_GC")) c->autotune = false;
   const int N = c->N, L = c->L;
-  // 0-based index tables; validate the Fortran numbering
-  std::vector<int> prox(N * 6), proxs(N * 6), nprox(N);
-  for (int i = 0; i < N; i++) {
-    nprox[i] = g->nprox[i];
-    if (nprox[i] != 5 && nprox[i] != 6) { delete c; return FIM_EINVAL; }
-    for (int e = 0; e < 6; e++) {
-      int p = g->prox[i * 6 + e] - 1;
-      if (p < 0 || p >= N) { delete c; return FIM_EINVAL; }
-      prox[i * 6 + e] = p;
-      int q = g->proxs[i * 6 + e];
-      proxs[i * 6 + e] = (e < nprox[i]) ? q - 1 : -1;
-      if (e < nprox[i] && (q < 1 || q > 6)) { delete c; return FIM_EINVAL; }
-    }
-  }
-  // every edge has a mirror: prox(proxs(e), prox(e)) == i (edgvar3's two-sided
-  // averages and trcadv's mirror mass fluxes read the neighbour's side through it)
-  for (int i = 0; i < N; i++)
-    for (int e = 0; e < nprox[i]; e++) {
-      const int x = prox[i * 6 + e];
-      if (x == i || prox[x * 6 + proxs[i * 6 + e]] != i) { delete c; return FIM_EINVAL; }
-    }
+  std::vector<int> prox, proxs, nprox;
+  if (index_tables(g, prox, proxs, nprox) != FIM_OK) { delete c; return FIM_EINVAL; }
   // derived fields (dyn_init.F90:309-338,752-767)
   std::vector<double> rarea(N), corio(N), grnd(N), dfflen(L), biharw(L), smoo(L + 1, 0.0);
   for (int i = 0; i < N; i++) {
@@ -2066,6 +2077,27 @@ int fim_profile_report(fim_ctx* c, char* buf, int len) {
   if ((int)out.size() + 1 > len) return FIM_EINVAL;
   memcpy(buf, out.c_str(), out.size() + 1);
   c->prof.agg.clear();
+  return FIM_OK;
+}
+
+int fim_grid_patches(const fim_grid_desc* g, int side, int* npatch, int* max_cells, int* max_frame,
+                     int* max_ring_edges) {
+  if (!g || side < 1 || side > 8) return FIM_EINVAL;
+  std::vector<int> prox, proxs, nprox;
+  if (index_tables(g, prox, proxs, nprox) != FIM_OK) return FIM_EINVAL;
+  FrameHost h;
+  if (build_frames(g->nip, prox.data(), proxs.data(), nprox.data(), side, &h) != 0) return FIM_EINVAL;
+  if (check_frames(g->nip, prox.data(), proxs.data(), nprox.data(), h) != 0) return FIM_EINVAL;
+  int mc = 0, mf = 0, mr = 0;
+  for (int t = 0; t < h.ntile; t++) {
+    mc = std::max(mc, h.cnt[(size_t)t * 4]);
+    mf = std::max(mf, h.cnt[(size_t)t * 4 + 2]);
+    mr = std::max(mr, h.cnt[(size_t)t * 4 + 3]);
+  }
+  if (npatch) *npatch = h.ntile;
+  if (max_cells) *max_cells = mc;
+  if (max_frame) *max_frame = mf;
+  if (max_ring_edges) *max_ring_edges = mr;
   return FIM_OK;
 }
 

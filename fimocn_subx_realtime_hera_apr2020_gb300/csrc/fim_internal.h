@@ -383,6 +383,9 @@ struct FrameHost {
 // patches of side x side cells of each rhombus (the reference's IJ
 // numbering), else grown breadth-first; 0 on success
 int build_frames(int N, const int* prox, const int* proxs, const int* nprox, int side, FrameHost* out);
+// 0 if every cell is in exactly one patch and every frame neighbour and edge
+// mirror of the tables resolves to prox/proxs
+int check_frames(int N, const int* prox, const int* proxs, const int* nprox, const FrameHost& f);
 // fused tracer path of the step (fim_trc.cu)
 template <typename R>
 struct TrcFusedScratch {

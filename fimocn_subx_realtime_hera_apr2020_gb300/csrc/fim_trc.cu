@@ -852,6 +852,46 @@ int build_frames(int N, const int* prox, const int* proxs, const int* nprox, int
   return 0;
 }
 
+int check_frames(int N, const int* prox, const int* proxs, const int* nprox, const FrameHost& F) {
+  std::vector<int> seen(N, 0);
+  for (int t = 0; t < F.ntile; t++) {
+    const int C = F.cnt[(size_t)t * 4], n1 = F.cnt[(size_t)t * 4 + 1], n2 = F.cnt[(size_t)t * 4 + 2],
+              nre = F.cnt[(size_t)t * 4 + 3];
+    if (C < 1 || C > F.SC || n1 > F.S1 || n2 > F.S2 || nre > F.SR || 6 * C + nre > F.SE) return 1;
+    const int* cells = &F.cells[(size_t)t * F.S2];
+    for (int x = 0; x < n2; x++)
+      if (cells[x] < 0 || cells[x] >= N) return 2;
+    for (int x = 0; x < C; x++) seen[cells[x]]++;
+    for (int x = 0; x < n1; x++)
+      for (int e = 0; e < 6; e++) {
+        const int y = (F.nbr[((size_t)t * F.S1 + x) * 2 + e / 4] >> (8 * (e % 4))) & 255;
+        if (y >= n2 || cells[y] != prox[cells[x] * 6 + e]) return 3;
+      }
+    for (int x = 0; x < C; x++) {
+      const int c = cells[x];
+      for (int e = 0; e < nprox[c]; e++) {
+        const int row = F.mir[((size_t)t * F.SC + x) * 6 + e];
+        int y, p;
+        if (row < 6 * C) {
+          y = row / 6;
+          p = (row % 6) ^ (y & 1);
+        } else {
+          const int r = row - 6 * C;
+          if (r >= nre) return 4;
+          const int code = F.red[(size_t)t * F.SR + r];
+          y = code >> 3;
+          p = code & 7;
+          if (y < C || y >= n1) return 5;
+        }
+        if (cells[y] != prox[c * 6 + e] || p != proxs[c * 6 + e]) return 6;
+      }
+    }
+  }
+  for (int i = 0; i < N; i++)
+    if (seen[i] != 1) return 7;
+  return 0;
+}
+
 template <typename R>
 int prepare_tracers(const FrameTab& ft) {
   int e;

@@ -450,12 +450,26 @@ int fim_profile_report(fim_ctx *ctx, char *buf, int len);
 int64_t fim_launch_count(const fim_ctx *ctx);
 
 /* Shape of the fused tracer kernels (no counterpart in the reference): levels
- * per thread (1, 2 or 4) and threads per block (128 or 256, the cell patch),
- * picked by timing the candidates on the state before the first fused step
- * (0 levels: the widest the layout admits, before tuning); probe_ms is the
- * winner's time for one probe.  FIM_TRC_VK / FIM_TRC_TB pin the shape and
- * FIM_AUTOTUNE=0 skips the timing. */
+ * per thread (1, 2 or 4) and threads per block (the cell patch's cells times
+ * 2 or 4 threads a cell; a block covers levels-per-thread x threads-a-cell
+ * levels), picked by timing the candidates on the state before the first
+ * fused step (0 levels: the widest the layout admits, before tuning);
+ * probe_ms is the winner's time for one probe.  FIM_TRC_VK / FIM_TRC_GC pin
+ * the shape and FIM_AUTOTUNE=0 skips the timing. */
 int fim_tracer_shape(const fim_ctx *ctx, int *levels_per_thread, int *threads_per_block, float *probe_ms);
+
+/* Cell patches of the fused tracer kernels for a grid (no counterpart in the
+ * reference), built as fim_ctx_create builds them and checked on the host:
+ * every cell in exactly one patch, every frame neighbour equal to prox and
+ * every edge's other side equal to prox/proxs.  No device use.  Patches are
+ * side x side cells of one rhombus (1 <= side <= 8; each pole is a patch of
+ * its own), or grown breadth-first for another cell numbering.  Outputs (each
+ * may be null): the number of patches, the largest patch, the largest frame
+ * (a patch and its two neighbour rings) and the most ring edges of a patch.
+ * FIM_OK, or FIM_EINVAL for malformed tables, a side out of range or a frame
+ * over 255 cells. */
+int fim_grid_patches(const fim_grid_desc *grid, int side, int *npatch, int *max_cells, int *max_frame,
+                     int *max_ring_edges);
 
 #ifdef __cplusplus
 }
