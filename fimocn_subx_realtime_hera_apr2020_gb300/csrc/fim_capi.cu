@@ -2000,10 +2000,11 @@ int fim_step_io(fim_ctx* c, fim_state* st, int its, int64_t* h2d_bytes, int64_t*
     io.of.push_back((p.of + 1) % 3);
     io.vof.push_back((p.vof + 1) % 3);
   }
-  // tracer chunks of about a quarter of the tracers: the slots of a chunk go
+  // tracer chunks of about a seventh of the tracers: the slots of a chunk go
   // up while the chunk before it is transported, its results come down while
-  // the next one is
-  io.tchunk = c->kn.hi_order ? std::max(1, std::min(c->ftchunk, (c->T + 3) / 4)) : c->T;
+  // the next one is; what is left after the last upload is that chunk's
+  // transport and its downloads (at glvl 8, 3 tracers: ~2 GB, ~10 ms)
+  io.tchunk = c->kn.hi_order ? std::max(1, std::min(c->ftchunk, (c->T + 6) / 7)) : c->T;
   io.hook.fn = io_chunk_hook;
   io.hook.arg = &io;
   // the copies start behind the work already queued on the compute stream
