@@ -180,6 +180,26 @@ def test_fused_step_fp64(case4):
     assert rc == 0 and flags == 0
 
 
+@pytest.mark.parametrize("precision,steps,tol", [("f64", 3, TOL64), ("f32", 1, TOL32)])
+def test_fused_step_odd_nvl(precision, steps, tol):
+    """nvl 37: one level a thread in every kernel, and level tiles of the
+    tracer kernels that the column height does not fill."""
+    th, dp = F.vertical_tables(38)
+    grid, cfg, fields = make_case(glvl=3, nvl=37, ntra=5, dt=400.0, seed=37, noise=1.0, precision=precision,
+                                  thetac=th[:37], dpsig=dp[:37])
+    o = oracle_for(grid, cfg)
+    s = o.init_state(o.new_state(fields))
+    dyc, st = _gpu_state(grid, cfg, fields)
+    for its in range(1, steps + 1):
+        o.step(s, its)
+        st.step(its)
+        errs = {n: rel_l2(st.download(n), s[n]) for n in PROGNOSTIC}
+        bad = {k: v for k, v in errs.items() if not v <= tol}
+        assert not bad, (its, bad)
+    rc, flags = st.check()
+    assert rc == 0 and flags == 0
+
+
 def test_graph_replay_matches_direct(case4):
     grid, cfg, fields, _, _ = case4
     d1, s1 = _gpu_state(grid, cfg, fields)
