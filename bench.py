@@ -67,6 +67,9 @@ E2E_FIELDS = ["us3d", "vs3d", "dp3d", "pr3d", "ex3d", "ph3d", "mp3d", "tr3d", "t
 # the fields a step writes without reading them
 E2E_AB3 = {"u_tdcy", "v_tdcy", "dp_tdcy", "dpl_tdcy", "trc_tdcy", "trl_tdcy"}
 E2E_OUTPUTS = {"ws3d", "sdot", "relvor"}  # rewritten whole by every step (ptdcy: one of its two levels)
+# rewritten whole by the step's opening hystat from a member's second step on
+# (the timed steps): they only come down
+E2E_RECOMPUTED = {"mp3d", "trdp"}
 
 
 def peaks():
@@ -256,7 +259,8 @@ def gpu_arm(args, ws, rank, local):
 
     # end to end through the C-ABI with host buffers: every step uploads what it
     # reads and downloads what it writes (AB3 tendency fields: the two slots it
-    # reads, the one it writes; omega, sdot and relvor are outputs only)
+    # reads, the one it writes; omega, sdot and relvor are outputs only, and so
+    # are the Montgomery potential and tracer x thickness at the timed steps)
     e2e = None
     if not args.no_e2e:
         bufs = {}
@@ -271,7 +275,7 @@ def gpu_arm(args, ws, rank, local):
             h2d = d2h = 0
             slots = [st.next_slots(m) for m in range(members)]
             for f, buf in bufs.items():
-                if f in E2E_OUTPUTS:
+                if f in E2E_OUTPUTS or f in E2E_RECOMPUTED:
                     continue
                 n = buf.numel() // members
                 for m in range(members):

@@ -931,6 +931,7 @@ bool io_class(int f, IoClass* k) {
 struct StepIo {
   fim_ctx* c = nullptr;
   fim_state* st = nullptr;
+  int its = 1;
   std::vector<int> nf, of;  // per member, 0-based slots of the step (after its abstart)
   std::vector<int> vof;
   int tchunk = 1;
@@ -992,6 +993,13 @@ int io_upload(StepIo& io, int stage, int t0, int nt, cudaEvent_t* done) {
   for (int f = 0; f < FIM_NFIELDS; f++) {
     IoClass k;
     if (!io_class(f, &k) || k.up != stage) continue;
+    // From a member's second step on, the step opens with hybgen and hystat
+    // of the step before (dyn_run.F90:119-132), which rewrite the Montgomery
+    // potential and tracer x thickness whole before anything reads them
+    // (hystat.F90:58-101; the remap forms trdp as it stores each tracer):
+    // the host's copies are not needed.  Class-B tracers' trdp is not
+    // recomputed, so with ntrb > 0 trdp goes up.
+    if (io.its > 1 && (f == FIM_MP3D || (f == FIM_TRDP && c->TB == 0))) continue;
     for (int m = 0; m < c->M; m++) {
       if (k.ab3) {
         const int n = (f == FIM_TRC_TDCY || f == FIM_TRL_TDCY) ? nt : 1, a = n == 1 && stage != kIoT ? 0 : t0;
@@ -1994,6 +2002,7 @@ int fim_step_io(fim_ctx* c, fim_state* st, int its, int64_t* h2d_bytes, int64_t*
   StepIo io;
   io.c = c;
   io.st = st;
+  io.its = its;
   for (int m = 0; m < c->M; m++) {  // the slots after the step's abstart
     const StepParams& p = c->h_sp[m];
     io.nf.push_back((p.nf + 1) % 3);

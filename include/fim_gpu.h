@@ -408,12 +408,15 @@ int fim_step_active(fim_ctx *ctx, fim_state *st, int use_graph);
  * compute stream.  The step is cut at the stages of dyn_run: hybgen + hystat
  * + edge interpolation, cnuity (its AB3 slots arrive just before it), momtum
  * (which shares no field with the tracer transport, so it runs before it
- * here), the tracer transport in chunks of about a quarter of the tracers (each
- * chunk's AB3 slots arrive while the chunk before it runs; its results leave
- * while the next one runs).  Results equal fim_step's bit for bit.  AB3
+ * here), the tracer transport in chunks of about a seventh of the tracers
+ * (each chunk's AB3 slots arrive while the chunk before it runs; its results
+ * leave while the next one runs).  Results equal fim_step's bit for bit.  AB3
  * tendency fields move only the slots the step reads (of, vof) and writes
  * (nf); ws3d, sdot and relvor, which the step rewrites whole, only come down
- * (ptdcy, of whose two time levels a step writes one, goes both ways).
+ * (ptdcy, of whose two time levels a step writes one, goes both ways); from
+ * its = 2 on, mp3d and trdp (the class-A tracers' part; with ntrb = 0) only
+ * come down too, because the step's opening hystat rewrites them before any
+ * read.
  * Returns when every download has landed; *h2d_bytes and *d2h_bytes (may be
  * null) get the bytes moved.  FIM_ENOTSUP with member_group < members. */
 int fim_state_set_host(fim_ctx *ctx, fim_state *st, int field, int member, void *host);

@@ -22,6 +22,9 @@ FIELDS = ["us3d", "vs3d", "dp3d", "pr3d", "ex3d", "ph3d", "mp3d", "tr3d", "trdp"
           "dpl_tdcy", "trc_tdcy", "trl_tdcy", "ws3d", "sdot", "relvor", "psrf", "ptdcy"]
 AB3 = {"u_tdcy", "v_tdcy", "dp_tdcy", "dpl_tdcy", "trc_tdcy", "trl_tdcy"}
 OUT = {"ws3d", "sdot", "relvor"}
+# rewritten whole by the step's opening hystat from the second step on, so
+# they go up only at the first step (the poison then shows they are not read)
+RECOMPUTED = {"mp3d", "trdp"}
 
 
 def _state(grid, cfg, fields):
@@ -46,8 +49,10 @@ def test_step_io_matches_resident(precision):
         st.download(f, out=host[f].numpy())
         st.set_host(f, host[f])
     esz = 8 if precision == "f64" else 4
-    want_up = sum(host[f].numel() for f in FIELDS if f not in OUT and f not in AB3) * esz + \
-        sum(2 * host[f].numel() // 3 for f in AB3) * esz
+    def want_up(its):
+        return sum(host[f].numel() for f in FIELDS
+                   if f not in OUT and f not in AB3 and not (its > 1 and f in RECOMPUTED)) * esz + \
+            sum(2 * host[f].numel() // 3 for f in AB3) * esz
     want_down = sum(host[f].numel() for f in FIELDS if f not in AB3) * esz + \
         sum(host[f].numel() // 3 for f in AB3) * esz
     for its in range(1, 6):
@@ -55,7 +60,7 @@ def test_step_io_matches_resident(precision):
             st.upload(f, np.full(host[f].numel(), np.nan))
         up, down = st.step_io(its)
         ref.step(its, use_graph=True)
-        assert (up, down) == (want_up, want_down)
+        assert (up, down) == (want_up(its), want_down)
         for f in FIELDS:
             got = host[f].numpy()
             want = ref.download(f)
