@@ -74,3 +74,24 @@ def test_renumbered_grid_gives_renumbered_results(precision):
             got = cells_first(a1, n)
         assert np.array_equal(got, want), name
     assert s0.check()[0] == 0 and s1.check()[0] == 0
+
+
+def test_coarse_grid_small_patches():
+    """glvl 2 (162 cells): patches of 4 x 4 cells whose frames exceed three
+    rows a thread, so the tracer kernels stage through their general loop;
+    three FP64 steps against the oracle."""
+    from helpers import oracle_for, rel_l2
+    grid, cfg, fields = make_case(glvl=2, nvl=38, ntra=5, dt=1200.0, seed=202, noise=1.0)
+    o = oracle_for(grid, cfg)
+    s = o.init_state(o.new_state(fields))
+    d = F.Dycore(grid, cfg)
+    st = d.state()
+    st.load(fields)
+    st.init()
+    for its in (1, 2, 3):
+        o.step(s, its)
+        st.step(its)
+        errs = {n: rel_l2(st.download(n), s[n]) for n in PROGNOSTIC}
+        bad = {k: v for k, v in errs.items() if not v <= 1e-12}
+        assert not bad, (its, bad)
+    assert st.check()[0] == 0
