@@ -95,3 +95,30 @@ def test_coarse_grid_small_patches():
         bad = {k: v for k, v in errs.items() if not v <= 1e-12}
         assert not bad, (its, bad)
     assert st.check()[0] == 0
+
+
+@pytest.mark.parametrize("precision,shapes", [
+    ("f32", [(4, 4), (4, 2), (2, 4), (2, 2), (1, 4), (1, 2)]),
+    ("f64", [(2, 4), (2, 2), (1, 4), (1, 2)]),
+])
+def test_every_tracer_shape_same_results(precision, shapes, monkeypatch):
+    """Every shape the tracer kernels' autotuner can pick (levels a thread x
+    threads a cell, so the level tile and the block) forms each cell-level's
+    values in the same order: three steps agree bit for bit."""
+    grid, cfg, fields = make_case(glvl=3, nvl=64, ntra=5, dt=400.0, seed=64, noise=1.0, precision=precision)
+    results = []
+    for vk, gc in shapes:
+        monkeypatch.setenv("FIM_TRC_VK", str(vk))
+        monkeypatch.setenv("FIM_TRC_GC", str(gc))
+        d = F.Dycore(grid, cfg)
+        st = d.state()
+        st.load(fields)
+        st.init()
+        for its in (1, 2, 3):
+            st.step(its)
+        assert d.tracer_shape()[0] == vk, (vk, gc)
+        results.append({n: st.download(n) for n in PROGNOSTIC})
+        assert st.check()[0] == 0
+    for (vk, gc), r in zip(shapes[1:], results[1:]):
+        for n in PROGNOSTIC:
+            assert np.array_equal(r[n], results[0][n]), (vk, gc, n)
