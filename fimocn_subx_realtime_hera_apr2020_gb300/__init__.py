@@ -8,4 +8,4 @@ per-routine / fused-step calls.
 from .config import FimConfig, WORKLOADS, default_dt, vertical_tables  # noqa: F401
 from .grid import Grid  # noqa: F401
 from .dycore import Dycore, DycoreState, FIELDS  # noqa: F401
-from .state import synthetic_state  # noqa: F401
+from .state import synthetic_state, synthetic_state_device  # noqa: F401

@@ -41,7 +41,8 @@ class Config(ctypes.Structure):
                 ("biharm_frst", ctypes.c_int), ("biharm_last", ctypes.c_int), ("rleigh", ctypes.c_double),
                 ("rlthresh", ctypes.c_double), ("rltaper", ctypes.c_double), ("pure_sig", ctypes.c_int),
                 ("thetac", ctypes.c_void_p), ("dpsig", ctypes.c_void_p), ("ntrb", ctypes.c_int),
-                ("dtratio", ctypes.c_int), ("member_group", ctypes.c_int), ("hi_order_uv_comp", ctypes.c_int)]
+                ("dtratio", ctypes.c_int), ("member_group", ctypes.c_int), ("hi_order_uv_comp", ctypes.c_int),
+                ("stream_priority", ctypes.c_int)]
 
 
 class Budget(ctypes.Structure):

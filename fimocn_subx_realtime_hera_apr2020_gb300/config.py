@@ -59,6 +59,7 @@ class FimConfig:
     dtratio: int = 6
     member_group: int = 0           # members advanced together through the dynamics (0: all)
     hi_order_uv_comp: int = 0       # hiOrderUVComp: edgvar2 after edgvar1 in the step
+    stream_priority: int = 0        # CUDA priority of the context's streams (lower runs first)
     thetac: np.ndarray = field(default=None, repr=False)
     dpsig: np.ndarray = field(default=None, repr=False)
 

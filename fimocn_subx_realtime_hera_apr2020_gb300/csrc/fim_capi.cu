@@ -62,6 +62,7 @@ struct fim_ctx {
   int graph_gen = 0;
   // fim_step_io's copy streams (host to device, device to host) and events
   cudaStream_t io_in = nullptr, io_out = nullptr;
+  int prio = 0;  // priority of the streams above (fim_config.stream_priority, clamped)
   std::vector<cudaEvent_t> io_ev;
   std::vector<void*> owned;          // device allocations freed at destroy
   std::vector<size_t> owned_bytes;   // their sizes, entry for entry
@@ -1437,7 +1438,12 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
   c->kn.dfflen_max = dmax;
   c->kn.biharm = biharm;
 
-  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  int least = 0, greatest = 0;
+  cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  if (e == cudaSuccess) {
+    c->prio = std::max(greatest, std::min(least, cfg->stream_priority));
+    e = cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, c->prio);
+  }
   if (e != cudaSuccess) {
     cudaGetLastError();
     delete c;
@@ -1993,7 +1999,7 @@ int fim_step_io(fim_ctx* c, fim_state* st, int its, int64_t* h2d_bytes, int64_t*
     if (rc) return rc;
   }
   for (cudaStream_t* q : {&c->io_in, &c->io_out})
-    if (!*q) CK(cudaStreamCreateWithFlags(q, cudaStreamNonBlocking), "step io stream");
+    if (!*q) CK(cudaStreamCreateWithPriority(q, cudaStreamNonBlocking, c->prio), "step io stream");
   for (auto& p : c->h_sp) {
     p.active = 1;
     p.its = its - 1;

@@ -1,7 +1,9 @@
 """Forecast-advance serving with continuous batching.
 
-A request asks to advance a seeded balanced state on grid level glvl with
-nvl layers and ntra tracers by `steps` dynamics steps.  Requests on the same
+A request asks to advance a state on grid level glvl with nvl layers and
+ntra tracers by `steps` dynamics steps: its own host state, or a seeded
+balanced state that is made on the device in the slot it is admitted to
+(milliseconds, where the numpy generator takes seconds at glvl 7).  Requests on the same
 grid (glvl, nvl) share a pool: one context whose ensemble slots are the
 batch, advanced together by one fused launch sequence per step
 (fim_step_active, one CUDA-graph replay).  A pool carries `max_tracers`
@@ -24,7 +26,7 @@ import numpy as np
 from .config import FimConfig, default_dt
 from .dycore import Dycore
 from .grid import Grid
-from .state import synthetic_state
+from .state import synthetic_state_device
 
 
 @dataclass(order=True)
@@ -36,6 +38,10 @@ class Request:
     ntra: int = field(compare=False)
     steps: int = field(compare=False)
     seed: int = field(compare=False, default=0)
+    # the request's own initial state (host arrays in the reference layout,
+    # as State.load takes them); None: the seeded balanced state made on
+    # the device
+    fields: dict = field(compare=False, default=None, repr=False)
     t_queue: float = field(compare=False, default=None)
     t_admit: float = field(compare=False, default=None)
     t_done: float = field(compare=False, default=None)
@@ -62,13 +68,14 @@ def state_bytes(glvl, nvl, ntra, precision):
 class Pool:
     """One batched context (all slots share the grid and the configuration)."""
 
-    def __init__(self, key, precision, slots, collect, ntra):
+    def __init__(self, key, precision, slots, collect, ntra, priority=0):
         import torch
         glvl, nvl = key
         self.key = key
         self.ntra = ntra
         self.grid = Grid.cached(glvl)
-        self.cfg = FimConfig(nvl=nvl, ntra=ntra, dt=default_dt(glvl), precision=precision, members=slots)
+        self.cfg = FimConfig(nvl=nvl, ntra=ntra, dt=default_dt(glvl), precision=precision, members=slots,
+                             stream_priority=priority)
         self.dyc = Dycore(self.grid, self.cfg)
         self.st = self.dyc.state()
         for m in range(slots):
@@ -84,19 +91,30 @@ class Pool:
         return -1
 
     def admit(self, req, now):
+        import torch
         m = self.free_slot()
-        own = FimConfig(nvl=self.cfg.nvl, ntra=req.ntra, dt=self.cfg.dt, precision=self.cfg.precision)
-        fields = synthetic_state(self.grid, own, seed=req.seed, sigma_ps=200.0, noise=0.5, dtype=self.cfg.dtype)
-        tr = np.zeros(self.ntra * self.grid.nip * self.cfg.nvl, self.cfg.dtype)
-        tr[:fields["tr3d"].size] = fields["tr3d"]
-        fields["tr3d"] = tr
-        self.st.load(fields, member=m)
+        if req.fields is None:
+            own = FimConfig(nvl=self.cfg.nvl, ntra=req.ntra, dt=self.cfg.dt, precision=self.cfg.precision)
+            # on the pool's stream, ahead of the slot's initialisation
+            with torch.cuda.stream(self.stream):
+                synthetic_state_device(self.st, m, self.grid, own, req.seed, sigma_ps=200.0, noise=0.5)
+        else:
+            fields = dict(req.fields)
+            src = np.asarray(fields["tr3d"]).reshape(-1)
+            tr = np.zeros(self.ntra * self.grid.nip * self.cfg.nvl, src.dtype)
+            tr[:src.size] = src
+            fields["tr3d"] = tr
+            self.st.load(fields, member=m)
         self.st.init_member(m)  # dyn_init for this slot only; activates it
         req.t_admit = now
         self.slots[m] = req
 
     def active(self):
         return any(r is not None for r in self.slots)
+
+    def idle(self):
+        """Nothing of the pool's is still running on the device."""
+        return self.stream.query()
 
     def step(self):
         self.st.step_active(use_graph=True)
@@ -133,9 +151,13 @@ class Pool:
 class Server:
     """Continuous-batching request loop over resident device states."""
 
-    def __init__(self, precision="f32", slots=8, hbm_fraction=0.8, collect=("us3d", "tr3d"), max_tracers=21):
+    def __init__(self, precision="f32", slots=8, hbm_fraction=0.8, collect=("us3d", "tr3d"), max_tracers=21,
+                 priorities=True):
         self.precision = precision
         self.slots = slots
+        # pools on smaller grids get higher stream priorities: their short
+        # steps' blocks go first when blocks of a larger grid's step finish
+        self.priorities = priorities
         self.max_tracers = max_tracers
         self.hbm_fraction = hbm_fraction
         self.collect = collect
@@ -163,7 +185,8 @@ class Server:
             slots //= 2
         if per_slot * slots > self._free_hbm():
             return None
-        p = Pool(req.key, self.precision, slots, self.collect, self.max_tracers)
+        prio = -max(0, 8 - req.glvl) if self.priorities else 0
+        p = Pool(req.key, self.precision, slots, self.collect, self.max_tracers, priority=prio)
         self.pools[req.key] = p
         return p
 
@@ -186,25 +209,33 @@ class Server:
                 waiting.append(r)
                 if not realtime:
                     break
+            # each pool goes at its own pace: a pool whose last step is done
+            # retires its finished requests, takes waiting ones into its free
+            # slots and enqueues its next step on its own stream, while the
+            # steps of other pools are still running
+            idle = {k: p.idle() for k, p in self.pools.items()}
+            for k, p in self.pools.items():
+                if idle[k]:
+                    for m in p.finished():
+                        done.append(p.retire(m, now()))
             still = []
             for r in waiting:
                 p = self._pool_for(r)
-                if p is not None and p.free_slot() >= 0:
+                if p is not None and p.free_slot() >= 0 and idle.get(r.key, True):
                     p.admit(r, now())
                 else:
                     still.append(r)
             waiting = still
-            busy = [p for p in self.pools.values() if p.active()]
-            if not busy:
-                if pending and realtime:
+            launched = False
+            for k, p in self.pools.items():
+                if idle.get(k, True) and p.active():
+                    p.step()
+                    launched = True
+            if not launched:
+                if not any(p.active() for p in self.pools.values()) and pending and realtime:
                     time.sleep(max(0.0, min(pending[0].arrival - now(), 0.01)))
-                continue
-            for p in busy:
-                p.step()  # enqueued on the pool's own stream: pools overlap
-            for p in busy:
-                p.stream.synchronize()
-                for m in p.finished():
-                    done.append(p.retire(m, now()))
+                else:
+                    time.sleep(2e-4)  # every active pool's step is still running
         torch.cuda.synchronize()
         return done
 

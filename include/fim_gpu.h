@@ -98,6 +98,10 @@ typedef struct fim_config {
                               are held for one group, which bounds their memory */
   int hi_order_uv_comp;    /* [0] hiOrderUVComp: edgvar2 after edgvar1 in fim_step
                               (needs the grid's corner_xy) */
+  int stream_priority;     /* [0] CUDA priority of the context's streams (lower runs
+                              first; clamped to the device's range): contexts that
+                              share a GPU, e.g. serving pools of different grids,
+                              can let the short steps through first */
 } fim_config;
 
 typedef struct fim_ctx fim_ctx;

@@ -6,6 +6,8 @@ import pytest
 
 pytest.importorskip("torch")
 
+import fimocn_subx_realtime_hera_apr2020_gb300 as F  # noqa: E402
+from fimocn_subx_realtime_hera_apr2020_gb300.config import default_dt  # noqa: E402
 from fimocn_subx_realtime_hera_apr2020_gb300.serve import Request, Server, latency_stats  # noqa: E402
 
 pytestmark = pytest.mark.gpu
@@ -36,3 +38,83 @@ def test_same_alone_and_in_mix(precision):
             assert np.array_equal(np.asarray(v), np.asarray(mixed[req.rid].result[k])), (req.rid, k)
     st = latency_stats(list(mixed.values()))
     assert st["p99_s"] >= st["p50_s"] > 0
+
+
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_own_state_matches_plain_context(precision):
+    """A request that brings its own host state, served beside seeded
+    requests on a pool with padded tracer slots (joining mid-forecast), ends
+    where a context of its own size stepping the same state ends, bit for
+    bit."""
+    grid = F.Grid.cached(2)
+    cfg = F.FimConfig(nvl=38, ntra=5, dt=default_dt(2), precision=precision)
+    fields = F.synthetic_state(grid, cfg, seed=77, sigma_ps=200.0, noise=0.5, dtype=cfg.dtype)
+    own = Request(arrival=0.15, rid=9, glvl=2, nvl=38, ntra=5, steps=6, fields=fields)
+    srv = Server(precision=precision, slots=2, max_tracers=8)
+    done = {r.rid: r for r in srv.run(copy.deepcopy(_mix()[:2]) + [own], realtime=False)}
+    srv.close()
+    d = F.Dycore(grid, cfg)
+    st = d.state()
+    st.load(fields)
+    st.init()
+    for its in range(1, 7):
+        st.step(its)
+    for name in ("us3d", "tr3d"):
+        assert np.array_equal(np.asarray(done[9].result[name]), st.download(name)), name
+    st.free()
+    d.close()
+
+
+def test_device_state_is_seeded_and_balanced():
+    """The seeded state made on the device in a member slot: hydrostatic
+    columns from the drawn surface pressure, the slot's extra tracers zero,
+    the same seed the same state and another seed another."""
+    import torch
+    grid = F.Grid.cached(3)
+    N, L = grid.nip, 38
+    d = F.Dycore(grid, F.FimConfig(nvl=L, ntra=6, dt=400.0, members=2))
+    st = d.state()
+    own = F.FimConfig(nvl=L, ntra=4, dt=400.0)
+
+    def make(seed):
+        F.synthetic_state_device(st, 1, grid, own, seed, sigma_ps=200.0, noise=0.5)
+        torch.cuda.synchronize()
+        return {n: st.download(n, 1) for n in ("us3d", "vs3d", "dp3d", "pr3d", "ex3d", "ph3d", "mp3d", "tr3d")}
+
+    a = make(3)
+    pr = a["pr3d"].reshape(N, L + 1)
+    assert np.all(pr[:, L] == own.ptop)
+    assert np.array_equal(a["dp3d"].reshape(N, L), pr[:, :L] - pr[:, 1:])
+    assert np.all(a["dp3d"] > 0)
+    dps = own.dpsig / own.dpsig.sum()
+    assert np.allclose(a["dp3d"].reshape(N, L), (pr[:, :1] - own.ptop) * dps[None, :], rtol=1e-12)
+    ps = pr[:, 0]
+    assert abs(ps.mean() - 1e5) < 50.0 and 150.0 < ps.std() < 250.0
+    assert np.allclose(a["ex3d"], F.state.CP * (a["pr3d"] / F.state.P1000) ** (F.state.RD / F.state.CP),
+                       rtol=1e-14)
+    du = a["us3d"].reshape(N, L) - 35.0 * np.cos(grid.lat)[:, None]
+    assert 0.4 < du.std() < 0.6 and 0.4 < a["vs3d"].std() < 0.6
+    assert not a["ph3d"].any() and not a["mp3d"].any()
+    tr = a["tr3d"].reshape(6, N, L)
+    assert np.array_equal(tr[0], np.broadcast_to(300.0 + 300.0 * np.arange(L) / (L - 1), (N, L)))
+    assert tr[1:4].min() >= 0.0 and tr[1:4].max() < 1e-2 and tr[1:4].std() > 1e-3
+    assert not tr[4:].any()
+    b = make(3)
+    assert all(np.array_equal(a[n], b[n]) for n in a)
+    c = make(4)
+    assert not np.array_equal(a["us3d"], c["us3d"]) and not np.array_equal(a["tr3d"], c["tr3d"])
+    st.free()
+    d.close()
+
+
+def test_stream_priority():
+    """fim_config.stream_priority sets the context stream's CUDA priority,
+    clamped to the device's range (0 the lowest; -100 gives the highest)."""
+    import torch
+    grid = F.Grid.cached(2)
+    got = {}
+    for want in (0, -1, -100, 5):
+        d = F.Dycore(grid, F.FimConfig(nvl=38, ntra=5, dt=400.0, stream_priority=want))
+        got[want] = torch.cuda.ExternalStream(d.stream).priority
+        d.close()
+    assert got[0] == 0 and got[-1] == -1 and got[-100] < -1 and got[5] == 0
