@@ -905,6 +905,8 @@ R* F(fim_state* st, int f) { return (R*)st->f[f]; }
 // interpolation; C = cnuity or mass_adv (+ class-B transport); T = the tracer
 // transport, chunk by chunk; U = momtum; E = the budget sums.
 enum IoStage { kIoNone = 0, kIoA, kIoC, kIoT, kIoU, kIoE };
+// names of the stages in the profiler's timeline marks
+static const char* const kIoStageName[] = {"-", "A", "C", "T", "U", "E"};
 struct IoClass {
   int up;     // stage before which the field must be on the device (kIoNone: output only)
   int down;   // stage after which it is final
@@ -988,9 +990,16 @@ int io_copy(StepIo& io, int f, int m, int slot, int t0, int nt, bool up) {
 
 // uploads needed before stage `stage` (tracers [t0, t0+nt) for kIoT), then an
 // event the compute stream waits on
+// a timeline mark on stream q when the profiler is on: "<what>.<stage>.<t0>"
+void io_mark(StepIo& io, const char* what, int stage, int t0, cudaStream_t q) {
+  fim_ctx* c = io.c;
+  if (c->prof.on) c->prof.mark(std::string(what) + "." + kIoStageName[stage] + "." + std::to_string(t0), q);
+}
+
 int io_upload(StepIo& io, int stage, int t0, int nt, cudaEvent_t* done) {
   fim_ctx* c = io.c;
   int rc;
+  io_mark(io, "up_begin", stage, t0, c->io_in);
   for (int f = 0; f < FIM_NFIELDS; f++) {
     IoClass k;
     if (!io_class(f, &k) || k.up != stage) continue;
@@ -1011,6 +1020,7 @@ int io_upload(StepIo& io, int stage, int t0, int nt, cudaEvent_t* done) {
       }
     }
   }
+  io_mark(io, "up_end", stage, t0, c->io_in);
   *done = io_event(io);
   if (!*done) return set_err(c, FIM_ECUDA, "step io event");
   CK(cudaEventRecord(*done, c->io_in), "step io record");
@@ -1021,10 +1031,12 @@ int io_upload(StepIo& io, int stage, int t0, int nt, cudaEvent_t* done) {
 // stream's work so far
 int io_download(StepIo& io, int stage, int t0, int nt) {
   fim_ctx* c = io.c;
+  io_mark(io, "computed", stage, t0, c->stream);
   cudaEvent_t e = io_event(io);
   if (!e) return set_err(c, FIM_ECUDA, "step io event");
   CK(cudaEventRecord(e, c->stream), "step io record");
   CK(cudaStreamWaitEvent(c->io_out, e, 0), "step io wait");
+  io_mark(io, "down_begin", stage, t0, c->io_out);
   int rc;
   for (int f = 0; f < FIM_NFIELDS; f++) {
     IoClass k;
@@ -1045,6 +1057,7 @@ int io_download(StepIo& io, int stage, int t0, int nt) {
       }
     }
   }
+  io_mark(io, "down_end", stage, t0, c->io_out);
   return FIM_OK;
 }
 
@@ -2026,6 +2039,7 @@ int fim_step_io(fim_ctx* c, fim_state* st, int its, int64_t* h2d_bytes, int64_t*
   cudaEvent_t start = io_event(io);
   if (!start) return set_err(c, FIM_ECUDA, "step io event");
   CK(cudaEventRecord(start, c->stream), "step io record");
+  if (c->prof.on) c->prof.mark("start", c->stream);
   CK(cudaStreamWaitEvent(c->io_in, start, 0), "step io wait");
   CK(cudaStreamWaitEvent(c->io_out, start, 0), "step io wait");
   if ((rc = io_upload(io, kIoA, 0, 0, &io.up_ev[kIoA]))) return rc;
@@ -2046,7 +2060,9 @@ int fim_step_io(fim_ctx* c, fim_state* st, int its, int64_t* h2d_bytes, int64_t*
   CK(cudaStreamWaitEvent(c->stream, done, 0), "step io wait");
   for (auto& p : c->h_sp)
     if (p.active) host_abstart(p, p.its + 1);
+  if (c->prof.on) c->prof.mark("end", c->stream);
   CK(cudaStreamSynchronize(c->stream), "step io");
+  if (c->prof.on) c->prof.collect_marks();
   if (h2d_bytes) *h2d_bytes = io.h2d;
   if (d2h_bytes) *d2h_bytes = io.d2h;
   return FIM_OK;

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cstddef>
 #include <cstdint>
 #include <initializer_list>
@@ -153,9 +154,38 @@ struct Prof {
     }
     pending.clear();
   }
+  // fim_step_io's timeline: host time stamps taken by callbacks queued on
+  // the compute and copy streams, kept as offsets from the step's first
+  // mark; each name accumulates (steps, ms) in agg as "io:<name>"
+  struct Mark { std::string name; double ms = 0.0; };
+  std::vector<Mark*> marks;
+  static void CUDART_CB stamp(void* p) {
+    static_cast<Mark*>(p)->ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+  }
+  void mark(const std::string& name, cudaStream_t s) {
+    Mark* m = new Mark{name};
+    if (cudaLaunchHostFunc(s, stamp, m) != cudaSuccess) {
+      cudaGetLastError();
+      delete m;
+      return;
+    }
+    marks.push_back(m);
+  }
+  // once the streams holding the marks are idle
+  void collect_marks() {
+    for (Mark* m : marks) {
+      auto& a = agg["io:" + m->name];
+      a.first += 1;
+      a.second += m->ms - marks[0]->ms;
+    }
+    for (Mark* m : marks) delete m;
+    marks.clear();
+  }
   ~Prof() {
     for (auto& r : pending) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
     for (auto e : pool) cudaEventDestroy(e);
+    for (Mark* m : marks) delete m;
   }
 };
 

@@ -450,7 +450,11 @@ int fim_check(fim_ctx *ctx, fim_state *st, int *flags);
 /* Per-kernel CUDA-event timing on the context stream (for measurement;
  * steps must run without graph replay while it is on). */
 int fim_profile_enable(fim_ctx *ctx, int on);
-/* "kernel launches total_ms" lines accumulated since the last report */
+/* "kernel launches total_ms" lines accumulated since the last report; with
+ * fim_step_io also its timeline, "io:<mark> steps total_ms" with each mark's
+ * time from the step's start (up_begin/up_end of each stage's uploads,
+ * computed when a stage's last kernel is done, down_begin/down_end of its
+ * downloads, end) */
 int fim_profile_report(fim_ctx *ctx, char *buf, int len);
 
 /* Kernel launches issued since the context was created (own kernels only). */

@@ -86,3 +86,34 @@ def test_step_io_rejects_member_groups():
         st.step_io(1)
     with pytest.raises(FimError):
         st.set_host("u_edg", None)
+
+
+def test_step_io_timeline():
+    """With the profiler on, fim_step_io reports its timeline: each stage's
+    uploads end before its kernels are done, the downloads of a stage end
+    after its kernels, and the step ends last; a second step with the same
+    marks doubles their counts."""
+    grid, cfg, fields = make_case(glvl=3, nvl=38, ntra=7, dt=400.0, seed=1602, noise=1.0, precision="f32")
+    d, st = _state(grid, cfg, fields)
+    for f in FIELDS:
+        n = st.field_ptr(f)[1]
+        h = torch.empty(n, dtype=torch.float32, pin_memory=True)
+        st.download(f, out=h.numpy())
+        st.set_host(f, h)
+    d.profile(True)
+    st.step_io(1)
+    st.step_io(2)
+    rep = d.profile_report()
+    d.profile(False)
+    io = {k[3:]: (n, ms / n) for k, (n, ms) in rep.items() if k.startswith("io:")}
+    assert io["start"] == (2, 0.0)
+    end = io["end"][1]
+    stages = {k.split(".", 1)[1] for k in io if k.startswith("computed.")}
+    assert {"A.0", "C.0", "U.0", "E.0"} <= stages and any(s.startswith("T.") for s in stages)
+    for s in stages:
+        assert io["computed." + s][0] == 2
+        assert io["computed." + s][1] <= io["down_begin." + s][1] <= io["down_end." + s][1] <= end, s
+        if "up_end." + s in io:
+            assert io["up_end." + s][1] <= io["computed." + s][1] + 1e-6, s
+    # kernel timings are reported beside the marks
+    assert any(not k.startswith("io:") for k in rep)
