@@ -81,6 +81,7 @@ _SIGS = {
     "fim_state_init_member": ([_VP, _VP, _I], _I),
     "fim_member_set_active": ([_VP, _VP, _I, _I], _I),
     "fim_member_its": ([_VP, _I], _I),
+    "fim_member_set_tracers": ([_VP, _I, _I], _I),
     "fim_member_get_step": ([_VP, _I] + [_VP] * 7, _I),
     "fim_member_set_step": ([_VP, _I, _I, _I, _I, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double], _I),
     "fim_state_budget": ([_VP, _VP, _I, _VP, _VP], _I),

@@ -1885,6 +1885,15 @@ int fim_member_set_active(fim_ctx* c, fim_state* st, int member, int active) {
   return push_sp(c);
 }
 
+int fim_member_set_tracers(fim_ctx* c, int member, int ntr) {
+  if (!c || member < 0 || member >= c->M || ntr < 1 || ntr > c->T) return FIM_EINVAL;
+  if (ntr < c->T && (c->TB > 0 || !c->kn.hi_order))
+    return set_err(c, FIM_ENOTSUP, "a member's own tracer count needs the fused tracer transport "
+                                   "(hi_order_flux_comp) and no class-B tracers");
+  c->h_sp[member].ntr = ntr;
+  return push_sp(c);
+}
+
 int fim_member_its(const fim_ctx* c, int member) {
   if (!c || member < 0 || member >= c->M) return -1;
   return c->h_sp[member].its;

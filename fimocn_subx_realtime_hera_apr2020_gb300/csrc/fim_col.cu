@@ -459,11 +459,12 @@ __global__ void __launch_bounds__(kColBlock) k_remap(Grid<R> g, Strides s, Knobs
     R* __restrict__ us3d, R* __restrict__ vs3d, R* __restrict__ tr3d, R* __restrict__ sdot,
     R* __restrict__ ex3d, R* __restrict__ dp3d, R* __restrict__ pr3d, int* __restrict__ flags, int bnd) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int N = g.N, L = g.L, L1 = L + 1, T = g.T;
+  const int N = g.N, L = g.L, L1 = L + 1;
   if (i >= N) return;
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active || (bnd && sp->its <= 1)) return;
+  const int T = min(g.T, sp->ntr);
   exsmo += m * s.intf; us3d += m * s.cell; vs3d += m * s.cell; tr3d += m * s.tr; sdot += m * s.intf;
   ex3d += m * s.intf; dp3d += m * s.cell; pr3d += m * s.intf;
   const int its = sp->its - bnd;
@@ -997,7 +998,7 @@ __global__ void __launch_bounds__(32 * kWarpsRemapV) k_remap_v(Grid<R> g, Stride
   // fields in order o: 0 = theta, 1 = u, 2 = v, 3.. = tracers 2..ntra;
   // items per column: the interface arrays (ex3d, pr3d, exsmo), then the
   // fields three by three
-  const int F = T + 2, I = 1 + (F + 2) / 3;
+  const int F = min(T, sp->ntr) + 2, I = 1 + (F + 2) / 3;
   auto field = [&](int o, int i) -> R* {
     return o == 1 ? us3d + (size_t)i * L : o == 2 ? vs3d + (size_t)i * L
          : tr3d + ((size_t)(o == 0 ? 0 : o - 2) * N + i) * L;
@@ -1469,10 +1470,11 @@ __global__ void __launch_bounds__(kBlock2) k_hystat_trdp(Grid<R> g, Strides s, c
     const R* __restrict__ dp3d, R* __restrict__ tr3d, R* __restrict__ trdp, int bnd) {
   int i, k;
   if (!cell_levels<VK>(g.N, g.L, i, k)) return;
-  const int N = g.N, L = g.L, T = g.T;
+  const int N = g.N, L = g.L;
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active || (bnd && sp->its <= 1)) return;
+  const int T = min(g.T, sp->ntr);
   const size_t NL = (size_t)N * L;
   const size_t c = (size_t)i * L + k;
   dp3d += m * s.cell; tr3d += m * s.tr; trdp += m * s.tr;
@@ -1578,10 +1580,12 @@ __global__ void __launch_bounds__(kBlock2) k_globsum_levels(Grid<R> g, Strides s
   // adds area x dp; slots past the last repeat slot T and add nothing, so
   // every load of an iteration is issued before the first sum
   const R* xp[kGsGroup];
+  // tracers past the member's own count add nothing (and are not read)
+  const int ntm = min(T, sp->ntr);
 #pragma unroll
   for (int u = 0; u < kGsGroup; u++) {
     const int q = q0 + u <= T ? q0 + u : T;
-    xp[u] = q == 0 ? dp3d : tr + (size_t)(q - 1) * NL;
+    xp[u] = (q == 0 || q > ntm) ? dp3d : tr + (size_t)(q - 1) * NL;
   }
   auto sum_at = [&](unsigned idx) {
     const R ar = g.area[idx / (unsigned)L];
@@ -1593,7 +1597,7 @@ __global__ void __launch_bounds__(kBlock2) k_globsum_levels(Grid<R> g, Strides s
     for (int j = 0; j < VK; j++) ad[j] = ar * dp[j];
 #pragma unroll
     for (int u = 0; u < kGsGroup; u++)
-      if (u < nq) {
+      if (u < nq && q0 + u <= ntm) {
 #pragma unroll
         for (int j = 0; j < VK; j++) acc[u].add(u == 0 && q0 == 0 ? ad[j] : ad[j] * x[u][j]);
       }

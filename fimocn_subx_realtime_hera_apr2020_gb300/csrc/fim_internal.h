@@ -38,7 +38,9 @@ struct StepParams {
   double ab1, ab2, ab3; // AB3 weights (s)
   double dt;
   int active;           // 0: the member's slot is idle, kernels skip it
-  int pad_;
+  // tracers the member transports (fim_member_set_tracers): the tracer
+  // transport, the remap and the budget sums leave slots ntr.. as they are
+  int ntr = 0x7fffffff;
 };
 
 // device status bits

@@ -318,6 +318,10 @@ __global__ void __launch_bounds__(64 * GC, 8 / GC) k_trf_lo(Grid<R> g, Strides s
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active) return;
+  // the member's tracers in this chunk (fim_member_set_tracers); the
+  // scratch keeps the chunk's layout
+  const int ntm = min(nt, sp->ntr - t0);
+  if (ntm <= 0) return;
   const int L = g.L, N = g.N;
   const int nlc = (L + LK - 1) / LK;
   const int tile = blockIdx.x / nlc;
@@ -376,11 +380,11 @@ __global__ void __launch_bounds__(64 * GC, 8 / GC) k_trf_lo(Grid<R> g, Strides s
   stage(t0, 0);
   CellItem<R, VK> ci;
   ci.template load<GC>(g, s, fs, m, delp, C, k0, lk);
-  for (int tz = 0; tz < nt; tz++) {
+  for (int tz = 0; tz < ntm; tz++) {
     const int t = t0 + tz, b = tz & 1;
     stage_wait();
     __syncthreads();
-    if (tz + 1 < nt) stage(t + 1, b ^ 1);
+    if (tz + 1 < ntm) stage(t + 1, b ^ 1);
     const R* T = trs + b * ft.S2 * LK;
     if (t != 0) {
       // edge values: the six of the thread's patch cell, then the ring cells'
@@ -530,6 +534,10 @@ __global__ void __launch_bounds__(64 * GC) k_trf_hi(Grid<R> g, Strides s, FrameT
   const size_t m = blockIdx.y;
   sp += m;
   if (!sp->active) return;
+  // the member's tracers in this chunk (fim_member_set_tracers); the
+  // scratch keeps the chunk's layout
+  const int ntm = min(nt, sp->ntr - t0);
+  if (ntm <= 0) return;
   const int L = g.L, N = g.N;
   const int nlc = (L + LK - 1) / LK;
   const int tile = blockIdx.x / nlc;
@@ -592,7 +600,7 @@ __global__ void __launch_bounds__(64 * GC) k_trf_hi(Grid<R> g, Strides s, FrameT
   stage_lim(0);
   const int x = threadIdx.x / GC, v = (threadIdx.x - x * GC) * VK;
   const bool on = x < C && v < lk;
-  for (int tz = 0; tz < nt; tz++) {
+  for (int tz = 0; tz < ntm; tz++) {
     const int t = t0 + tz;
     stage_wait();
     __syncthreads();
@@ -609,7 +617,7 @@ __global__ void __launch_bounds__(64 * GC) k_trf_hi(Grid<R> g, Strides s, FrameT
     }
     stage_wait();
     __syncthreads();
-    if (tz + 1 < nt) stage_lim(tz + 1);
+    if (tz + 1 < ntm) stage_lim(tz + 1);
     if (!on) continue;
     const int i = fs.cells[x];
     const int c = i * L + k0 + v;

@@ -366,6 +366,12 @@ class DycoreState:
         _lib.check(self.lib.fim_member_set_active(self.dyc.ctx, self.st, member, 1 if active else 0),
                    "fim_member_set_active", self.dyc.ctx)
 
+    def set_tracers(self, member, ntr):
+        """Member `member` carries ntr tracers (theta included): later steps
+        leave its tracer slots ntr.. untouched and do no work for them."""
+        _lib.check(self.lib.fim_member_set_tracers(self.dyc.ctx, member, ntr), "fim_member_set_tracers",
+                   self.dyc.ctx)
+
     def member_its(self, member):
         return self.lib.fim_member_its(self.dyc.ctx, member)
 

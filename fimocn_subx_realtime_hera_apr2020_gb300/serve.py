@@ -105,6 +105,8 @@ class Pool:
             tr[:src.size] = src
             fields["tr3d"] = tr
             self.st.load(fields, member=m)
+        # the slot's padded tracers (zero) are left out of every step's work
+        self.st.set_tracers(m, req.ntra)
         self.st.init_member(m)  # dyn_init for this slot only; activates it
         req.t_admit = now
         self.slots[m] = req

@@ -389,6 +389,13 @@ int fim_step(fim_ctx *ctx, fim_state *st, int its, int use_graph);
 int fim_state_init_member(fim_ctx *ctx, fim_state *st, int member);
 int fim_member_set_active(fim_ctx *ctx, fim_state *st, int member, int active);
 int fim_member_its(const fim_ctx *ctx, int member);
+/* A member that carries fewer tracers than the context (ntr of ntra, theta
+ * included): the tracer transport, the remap and the budget sums of later
+ * steps leave its tracer slots ntr..ntra-1 as they are (zero, for a slot
+ * padded with zeros) and do no work for them; its tracers 1..ntr evolve as
+ * in a context of ntr tracers.  FIM_ENOTSUP without hi_order_flux_comp or
+ * with class-B tracers.  No counterpart in the reference (serving). */
+int fim_member_set_tracers(fim_ctx *ctx, int member, int ntr);
 
 /* Step state of one member for restart files: the completed step count
  * (itsm1, restart.F90:58), the AB3 slots nf/of/vof in Fortran numbering and

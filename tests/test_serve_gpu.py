@@ -118,3 +118,63 @@ def test_stream_priority():
         got[want] = torch.cuda.ExternalStream(d.stream).priority
         d.close()
     assert got[0] == 0 and got[-1] == -1 and got[-100] < -1 and got[5] == 0
+
+
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_member_with_fewer_tracers(precision):
+    """fim_member_set_tracers: a member carrying 5 of a context's 8 tracers
+    evolves as in a context of 5 tracers, bit for bit (fields, tracers and
+    budgets), leaves its other tracer slots as they are, and changes nothing
+    for the member beside it."""
+    from helpers import PROGNOSTIC
+    grid = F.Grid.cached(3)
+    L, NL = 38, grid.nip * 38
+    cfg = lambda n, **kw: F.FimConfig(nvl=L, ntra=n, dt=400.0, precision=precision, **kw)  # noqa: E731
+    f8 = F.synthetic_state(grid, cfg(8), seed=31, noise=1.0)
+    f5 = F.synthetic_state(grid, cfg(5), seed=32, noise=1.0)
+    pad = dict(f5)
+    pad["tr3d"] = np.concatenate([f5["tr3d"], np.full(3 * NL, 7.0)])
+    d = F.Dycore(grid, cfg(8, members=2))
+    st = d.state()
+    st.load(f8, member=0)
+    st.load(pad, member=1)
+    st.set_tracers(1, 5)
+    st.init()
+    alone = {}
+    for n, f in ((8, f8), (5, f5)):
+        da = F.Dycore(grid, cfg(n))
+        sa = da.state()
+        sa.load(f)
+        sa.init()
+        alone[n] = (da, sa)
+    for its in (1, 2, 3):
+        st.step(its, use_graph=True)
+        for n in alone:
+            alone[n][1].step(its)
+    s8, s5 = alone[8][1], alone[5][1]
+    for name in PROGNOSTIC:
+        assert np.array_equal(st.download(name, 0), s8.download(name)), name
+        got, want = st.download(name, 1), s5.download(name)
+        if name in ("tr3d", "trdp"):
+            got = got[:5 * NL]
+        assert np.array_equal(got, want), name
+    assert np.all(st.download("tr3d", 1)[5 * NL:] == 7.0)
+    q1, b1 = st.budget(1)
+    q5, b5 = s5.budget()
+    assert np.array_equal(q1[:5], q5) and not q1[5:].any() and b1["qmass"] == b5["qmass"]
+    assert np.array_equal(st.budget(0)[0], s8.budget()[0])
+    assert st.check()[0] == 0
+
+
+def test_set_tracers_rejects():
+    grid = F.Grid.cached(2)
+    d = F.Dycore(grid, F.FimConfig(nvl=38, ntra=6, dt=400.0, members=2))
+    st = d.state()
+    from fimocn_subx_realtime_hera_apr2020_gb300._lib import FimError
+    for m, n in ((0, 0), (0, 7), (2, 3)):
+        with pytest.raises(FimError):
+            st.set_tracers(m, n)
+    st.set_tracers(1, 6)
+    d2 = F.Dycore(grid, F.FimConfig(nvl=38, ntra=6, dt=400.0, ntrb=2))
+    with pytest.raises(FimError):
+        d2.state().set_tracers(0, 3)
