@@ -48,3 +48,91 @@ def test_state_bytes_scales():
     assert state_bytes(6, 64, 11, "f64") == 2 * b32 or abs(state_bytes(6, 64, 11, "f64") - 2 * b32) <= 1
     assert state_bytes(7, 64, 11, "f32") > 3.9 * b32
     assert state_bytes(6, 64, 21, "f32") > b32
+
+
+class _FakePool:
+    """Stands in for serve.Pool: a step of a pool on grid level glvl stays in
+    flight for glvl - 4 polls of its stream."""
+    made = []
+
+    def __init__(self, key, precision, slots, collect, ntra, priority=0):
+        self.key, self.priority = key, priority
+        self.slots = [None] * slots
+        self.its = [0] * slots
+        self.inflight = 0
+        self.steps_launched = 0
+        _FakePool.made.append(self)
+
+    def free_slot(self):
+        return next((i for i, r in enumerate(self.slots) if r is None), -1)
+
+    def admit(self, req, now):
+        assert self.inflight == 0, "admitted while a step was in flight"
+        m = self.free_slot()
+        self.slots[m], self.its[m] = req, 0
+        req.t_admit = now
+
+    def active(self):
+        return any(r is not None for r in self.slots)
+
+    def idle(self):
+        if self.inflight:
+            self.inflight -= 1
+        return self.inflight == 0
+
+    def step(self):
+        assert self.inflight == 0, "stepped while a step was in flight"
+        for m, r in enumerate(self.slots):
+            if r is not None:
+                self.its[m] += 1
+        self.inflight = self.key[0] - 4
+        self.steps_launched += 1
+
+    def finished(self):
+        return [m for m, r in enumerate(self.slots) if r is not None and self.its[m] >= r.steps]
+
+    def retire(self, m, now):
+        assert self.inflight == 0, "retired while a step was in flight"
+        r = self.slots[m]
+        assert self.its[m] == r.steps
+        r.t_done, r.result = now, {"steps": self.its[m]}
+        self.slots[m] = None
+        return r
+
+    def close(self):
+        pass
+
+
+def _run_fake(monkeypatch, priorities):
+    import torch
+    import fimocn_subx_realtime_hera_apr2020_gb300.serve as S
+    _FakePool.made = []
+    monkeypatch.setattr(S, "Pool", _FakePool)
+    monkeypatch.setattr(S.Server, "_free_hbm", lambda self: 1e15)
+    monkeypatch.setattr(torch.cuda, "synchronize", lambda *a, **k: None)
+    reqs = [Request(arrival=0.0, rid=i, glvl=g, nvl=38, ntra=5, steps=n)
+            for i, (g, n) in enumerate([(7, 12), (5, 12), (7, 6), (5, 20), (5, 3), (6, 9), (5, 7)])]
+    srv = S.Server(slots=2, priorities=priorities)
+    done = srv.run(reqs, realtime=False)
+    srv.close()
+    return done
+
+
+def test_serving_loop_pools_at_their_own_pace(monkeypatch):
+    """The request loop on fake pools: every request runs its steps, a pool is
+    admitted to, stepped and retired only between its steps, a small grid's
+    pool takes several steps while a larger grid's step is in flight, and
+    smaller grids get higher stream priorities."""
+    done = _run_fake(monkeypatch, priorities=True)
+    assert sorted(r.rid for r in done) == list(range(7))
+    assert all(r.result["steps"] == r.steps for r in done)
+    pools = {p.key[0]: p for p in _FakePool.made}
+    assert {g: p.priority for g, p in pools.items()} == {5: -3, 6: -2, 7: -1}
+    # 42 steps of glvl-5 requests on 2 slots against 18 of glvl 7
+    assert pools[5].steps_launched > pools[7].steps_launched
+    # the glvl-5 requests do not wait for the glvl-7 ones: the last glvl-5
+    # request is done before the last glvl-7 one
+    by = {g: max(r.t_done for r in done if r.glvl == g) for g in (5, 7)}
+    assert by[5] < by[7]
+    _run_fake(monkeypatch, priorities=False)
+    assert {p.priority for p in _FakePool.made} == {0}
