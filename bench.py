@@ -371,6 +371,15 @@ def gpu_arm(args, ws, rank, local):
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_baseline(args, threads_all=True)
 
+    # the served half of the metric: the default request stream, FP32-mixed
+    served = None
+    if ws == 1 and not args.no_serve:
+        n = args.serve or 40
+        served = {"requests": n, "rate_per_s": args.serve_rate, "slots_per_pool": args.serve_slots,
+                  "glvl": [5, 6, 7], "nvl": [38, 64], "tracers": [4, 20],
+                  "steps": [args.serve_min_steps, args.serve_max_steps], "precision": "fp32-mixed",
+                  **serve_stats(args, n, "f32")}
+
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (float-float column sums, FP64 budget reductions)",
@@ -386,7 +395,7 @@ def gpu_arm(args, ws, rank, local):
                        "cuda_graph": True, "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "no flush: state and edge fields (~60 GB) far exceed the 129 MB L2"},
             "gpu_launches": launches, "clocks": clk.summary(), "roofline": roof, "e2e": e2e,
-            "cpu_baseline": cpu, "fp64": fp64, "kernels": kernels,
+            "cpu_baseline": cpu, "fp64": fp64, "serve": served, "kernels": kernels,
             "budget": {"qmass": bud["qmass"], "qtrcr_theta": qtrcr[0]}}
     if rank == 0:
         print(json.dumps(line))
@@ -472,23 +481,27 @@ def reference_arm(args, ws, rank):
     print(json.dumps(line))
 
 
+def serve_stats(args, n, prec):
+    """p50/p99 latency and aggregate throughput of n served requests (the
+    seeded Poisson stream), arrivals replayed in real time."""
+    from fimocn_subx_realtime_hera_apr2020_gb300.serve import Server, latency_stats, poisson_requests
+    reqs = poisson_requests(n, rate=args.serve_rate, seed=5000, steps=(args.serve_min_steps, args.serve_max_steps))
+    srv = Server(precision=prec, slots=args.serve_slots, collect=())
+    done = srv.run(reqs, realtime=True)
+    pools = {"glvl%d_nvl%d" % k: len(p.slots) for k, p in sorted(srv.pools.items())}
+    srv.close()
+    return {**latency_stats(done), "pool_slots": pools}
+
+
 def serve_arm(args, ws, rank, local):
     """Served forecast-advance requests: a seeded Poisson stream of the mixed
     glvl 5/6/7, nvl 38/64, 4-20 tracer workload, continuous batching."""
     import torch
-    from fimocn_subx_realtime_hera_apr2020_gb300.serve import Server, latency_stats, poisson_requests
 
     torch.cuda.set_device(local)
-    reqs = poisson_requests(args.serve, rate=args.serve_rate, seed=5000, steps=(args.serve_min_steps,
-                                                                                 args.serve_max_steps))
     out = {}
     for prec in ("f32", "f64") if args.serve_fp64 else ("f32",):
-        srv = Server(precision=prec, slots=args.serve_slots, collect=())
-        done = srv.run(reqs, realtime=True)
-        srv.close()
-        out[prec] = latency_stats(done)
-        for r in reqs:
-            r.t_admit = r.t_done = r.result = None
+        out[prec] = serve_stats(args, args.serve, prec)
     line = {"metric": "served forecast-advance latency (p50/p99) and aggregate cell-level-steps/s",
             "value": out["f32"]["p50_s"], "unit": "s", "higher_is_better": False,
             "config": {"requests": args.serve, "rate_per_s": args.serve_rate, "slots_per_pool": args.serve_slots,
@@ -676,6 +689,7 @@ def main():
     p.add_argument("--serve-min-steps", type=int, default=24)
     p.add_argument("--serve-max-steps", type=int, default=240)
     p.add_argument("--serve-fp64", action="store_true")
+    p.add_argument("--no-serve", action="store_true", help="leave the served stream out of the default line")
     p.add_argument("--accuracy", type=int, default=0, help="report the error after this many steps")
     p.add_argument("--nvl", type=int, default=0)
     p.add_argument("--dt", type=float, default=0.0, help="time step of the accuracy run (default: workload's)")

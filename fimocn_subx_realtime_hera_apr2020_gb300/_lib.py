@@ -42,7 +42,7 @@ class Config(ctypes.Structure):
                 ("rlthresh", ctypes.c_double), ("rltaper", ctypes.c_double), ("pure_sig", ctypes.c_int),
                 ("thetac", ctypes.c_void_p), ("dpsig", ctypes.c_void_p), ("ntrb", ctypes.c_int),
                 ("dtratio", ctypes.c_int), ("member_group", ctypes.c_int), ("hi_order_uv_comp", ctypes.c_int),
-                ("stream_priority", ctypes.c_int)]
+                ("stream_priority", ctypes.c_int), ("tracer_chunk", ctypes.c_int)]
 
 
 class Budget(ctypes.Structure):
@@ -82,6 +82,7 @@ _SIGS = {
     "fim_member_set_active": ([_VP, _VP, _I, _I], _I),
     "fim_member_its": ([_VP, _I], _I),
     "fim_member_set_tracers": ([_VP, _I, _I], _I),
+    "fim_state_synthetic": ([_VP, _VP, _I, ctypes.c_ulonglong, _I, ctypes.c_double, ctypes.c_double], _I),
     "fim_member_get_step": ([_VP, _I] + [_VP] * 7, _I),
     "fim_member_set_step": ([_VP, _I, _I, _I, _I, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double], _I),
     "fim_state_budget": ([_VP, _VP, _I, _VP, _VP], _I),

@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIBNAME = "libfimgpu.so"
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-CU_SOURCES = ["fim_dyn.cu", "fim_col.cu", "fim_trc.cu", "fim_trb.cu", "fim_cpl.cu", "fim_capi.cu"]
+CU_SOURCES = ["fim_dyn.cu", "fim_col.cu", "fim_trc.cu", "fim_trb.cu", "fim_cpl.cu", "fim_synth.cu", "fim_capi.cu"]
 CPP_SOURCES = ["fim_grid.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

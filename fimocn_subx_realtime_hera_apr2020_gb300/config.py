@@ -60,6 +60,7 @@ class FimConfig:
     member_group: int = 0           # members advanced together through the dynamics (0: all)
     hi_order_uv_comp: int = 0       # hiOrderUVComp: edgvar2 after edgvar1 in the step
     stream_priority: int = 0        # CUDA priority of the context's streams (lower runs first)
+    tracer_chunk: int = 0           # tracers per launch of the fused tracer kernels (0: auto)
     thetac: np.ndarray = field(default=None, repr=False)
     dpsig: np.ndarray = field(default=None, repr=False)
 

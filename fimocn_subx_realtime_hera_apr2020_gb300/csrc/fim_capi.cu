@@ -71,6 +71,8 @@ struct fim_ctx {
   Strides str{};
   Knobs kn{};
   std::vector<double> thetac, dpsig;
+  std::vector<double> lat;           // cell latitudes (radians), for fim_state_synthetic
+  double* d_synth = nullptr;         // device: lat [N], dpsig / sum(dpsig) [L]
   void* d_thetac = nullptr;
   std::vector<StepParams> h_sp;  // one per member
   StepParams* d_sp = nullptr;
@@ -404,6 +406,14 @@ int ensure_trcadv(fim_ctx* c, int members) {
   return FIM_OK;
 }
 
+// The strides of a state's fields in the step: with the fused tracer
+// transport trc_edg holds theta's edge values only, 6 nvl nip a member.
+Strides step_strides(const fim_ctx* c) {
+  Strides s = c->str;
+  if (c->kn.hi_order) s.tredg = (size_t)6 * c->L * c->N;
+  return s;
+}
+
 int ensure_trc_fused(fim_ctx* c, int members) {
   if (c->f_trcr_lo) return FIM_OK;
   {
@@ -415,7 +425,7 @@ int ensure_trc_fused(fim_ctx* c, int members) {
   // outputs and six antidiffusive fluxes; chunks of at most ~48 GB (glvl 8,
   // nvl 64, 21 tracers: one chunk of 42 GB)
   size_t per_tracer = NL * members * 12 * c->esz;
-  int tch = c->T;
+  int tch = c->cfg.tracer_chunk > 0 ? std::min(c->T, c->cfg.tracer_chunk) : c->T;
   while (tch > 1 && per_tracer * tch > (size_t)48 << 30) tch = (tch + 1) / 2;
   c->ftchunk = tch;
   const size_t n = NL * members * tch;
@@ -1080,7 +1090,7 @@ int enqueue_step(fim_ctx* c, fim_state* st, StepIo* io = nullptr) {
   const int M = c->M;
   Launch l = make_launch(c, M);
   Grid<R>& g = grid_of<R>(c);
-  const Strides& s = c->str;
+  const Strides s = step_strides(c);
   int rc;
   if (io && (rc = io_wait(*io, io->up_ev[kIoA]))) return rc;
   launch_step_begin(l, c->d_sp);
@@ -1348,7 +1358,7 @@ int autotune_impl(fim_ctx* c, fim_state* st) {
                             (R*)c->f_af,
                         c->ftchunk, c->trc_vk, c->trc_gc, c->ftab};
   int vk = c->trc_vk, gc = c->trc_gc;
-  const int e = tune_tracers<R>(l, grid_of<R>(c), c->str, fw, F<R>(st, FIM_TRC_EDG), F<R>(st, FIM_TR3D),
+  const int e = tune_tracers<R>(l, grid_of<R>(c), step_strides(c), fw, F<R>(st, FIM_TRC_EDG), F<R>(st, FIM_TR3D),
                                 F<R>(st, FIM_TRDP), F<R>(st, FIM_TRC_TDCY), F<R>(st, FIM_TRL_TDCY),
                                 F<R>(st, FIM_MASSFX), F<R>(st, FIM_DP3D), &vk, &gc, &c->tune_ms);
   if (e) return set_err(c, FIM_ECUDA, "tracer shape autotuning", (cudaError_t)e);
@@ -1395,6 +1405,7 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
   c->M = cfg->members < 1 ? 1 : cfg->members;
   c->thetac.assign(cfg->thetac, cfg->thetac + c->L);
   c->dpsig.assign(cfg->dpsig, cfg->dpsig + c->L);
+  c->lat.assign(g->lat, g->lat + c->N);
   c->TB = cfg->ntrb;
   c->dtratio = cfg->dtratio;
   c->G = (cfg->member_group > 0 && cfg->member_group < c->M) ? cfg->member_group : c->M;
@@ -1753,7 +1764,9 @@ int fim_state_alloc(fim_ctx* c, fim_state** out) {
       NL * 3 * T, NL * 3 * T, NL * 6 * 3,          // trc_tdcy trl_tdcy massfx
       NL, NI, NL, N, N * 2,                        // ws sdot relvor psrf ptdcy
       NL * 6, NL * 6, NL * 6, NL * 6, NL * 6, NL * 6, NL * 6,  // edge fields
-      NL * 6 * T, NL * 6, NL};                     // trc_edg cumufx dpinit
+      // trc_edg: theta's edge values only with the fused tracer transport
+      // (the tracer kernels form the others on chip)
+      NL * 6 * (c->kn.hi_order ? 1 : T), NL * 6, NL};  // trc_edg cumufx dpinit
   for (int f = 0; f < FIM_NFIELDS; f++) {
     st->count[f] = cnt[f];
     st->slots[f] = group_field(f) ? c->G : c->M;
@@ -1883,6 +1896,45 @@ int fim_member_set_active(fim_ctx* c, fim_state* st, int member, int active) {
   if (!c || member < 0 || member >= c->M) return FIM_EINVAL;
   c->h_sp[member].active = active ? 1 : 0;
   return push_sp(c);
+}
+
+int fim_state_synthetic(fim_ctx* c, fim_state* st, int member, unsigned long long seed, int ntra, double sigma_ps,
+                        double noise) {
+  if (!c || !st || member < 0 || member >= c->M || ntra < 1 || ntra > c->T + c->TB || !(sigma_ps >= 0.0) ||
+      !(noise >= 0.0))
+    return FIM_EINVAL;
+  if (!c->d_synth) {
+    std::vector<double> h(c->lat);
+    double sum = 0.0;
+    for (double d : c->dpsig) sum += d;
+    for (double d : c->dpsig) h.push_back(d / sum);
+    int rc = dalloc(c, (void**)&c->d_synth, h.size() * sizeof(double));
+    if (rc) return rc;
+    // pageable source: staged before the call returns
+    CK(cudaMemcpyAsync(c->d_synth, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+       "synthetic state tables");
+  }
+  void* f[FIM_NFIELDS] = {};
+  for (int k : {FIM_US3D, FIM_VS3D, FIM_DP3D, FIM_PR3D, FIM_EX3D, FIM_PH3D, FIM_MP3D, FIM_TR3D}) {
+    int rc = fim_state_field(c, st, k, member, &f[k], nullptr);
+    if (rc) return rc;
+  }
+  const double* lat = c->d_synth;
+  const double* dps = c->d_synth + c->N;
+  const int nslot = c->T + c->TB;
+  int e;
+  if (c->prec == FIM_PREC_F64)
+    e = launch_synthetic<double>(c->stream, c->N, c->L, nslot, ntra, lat, dps, seed, sigma_ps, noise, c->kn.ptop,
+                                 (double*)f[FIM_US3D], (double*)f[FIM_VS3D], (double*)f[FIM_DP3D],
+                                 (double*)f[FIM_PR3D], (double*)f[FIM_EX3D], (double*)f[FIM_PH3D],
+                                 (double*)f[FIM_MP3D], (double*)f[FIM_TR3D]);
+  else
+    e = launch_synthetic<float>(c->stream, c->N, c->L, nslot, ntra, lat, dps, seed, sigma_ps, noise, c->kn.ptop,
+                                (float*)f[FIM_US3D], (float*)f[FIM_VS3D], (float*)f[FIM_DP3D], (float*)f[FIM_PR3D],
+                                (float*)f[FIM_EX3D], (float*)f[FIM_PH3D], (float*)f[FIM_MP3D],
+                                (float*)f[FIM_TR3D]);
+  if (e) return set_err(c, FIM_ECUDA, "synthetic state", (cudaError_t)e);
+  return FIM_OK;
 }
 
 int fim_member_set_tracers(fim_ctx* c, int member, int ntr) {

@@ -517,4 +517,10 @@ template <typename R>
 void launch_prdp_from_ex(const Launch&, const Grid<R>&, const Strides&, const R* ex3d, R* pr3d, R* dp3d);
 void launch_step_begin(const Launch&, StepParams* sp);  // advances every active member
 
+// fim_synth.cu: the seeded balanced state of one member slot
+template <typename R>
+int launch_synthetic(cudaStream_t stream, int N, int L, int nslot, int ntra, const double* lat,
+                     const double* dps, unsigned long long seed, double sigma_ps, double noise, double ptop,
+                     R* us3d, R* vs3d, R* dp3d, R* pr3d, R* ex3d, R* ph3d, R* mp3d, R* tr3d);
+
 }  // namespace fim

@@ -94,6 +94,16 @@ class Dycore:
             out[name] = (int(n), float(ms))
         return out
 
+    def _need_tracer_edges(self, a, what):
+        """The per-routine entry points take the reference's trc_edg(nvl, 6,
+        nip, ntra): refuse a smaller array (e.g. a fused-step state's trc_edg,
+        which holds theta's edge values only) rather than let a kernel write
+        past its end."""
+        n = a.numel() if hasattr(a, "numel") else getattr(a, "size", None)
+        need = 6 * self.cfg.nvl * self.grid.nip * self.T
+        if n is not None and n < need:
+            raise ValueError("%s: %d values, the routine needs nvl x 6 x nip x ntra = %d" % (what, n, need))
+
     def _call(self, name, *args):
         """Run one entry point.  Device arrays written by torch on its own
         stream are complete before the library's stream starts, and the
@@ -140,11 +150,13 @@ class Dycore:
 
     def edgvar2(self, its, u_vel, v_vel, delp, pres, exner, geop, montg, tracr, u_edg, v_edg, dp_edg, lp_edg,
                 geop_edg, mont_edg, uvsq_edg, trc_edg):
+        self._need_tracer_edges(trc_edg, "trc_edg")
         self._call("fim_edgvar2", its, *map(_ptr, (u_vel, v_vel, delp, pres, exner, geop, montg, tracr, u_edg,
                                                      v_edg, dp_edg, lp_edg, geop_edg, mont_edg, uvsq_edg, trc_edg)))
 
     def edgvar3(self, its, u_vel, v_vel, delp, pres, exner, geop, montg, tracr, u_edg, v_edg, dp_edg, lp_edg,
                 geop_edg, mont_edg, uvsq_edg, trc_edg):
+        self._need_tracer_edges(trc_edg, "trc_edg")
         self._call("fim_edgvar3", its, *map(_ptr, (u_vel, v_vel, delp, pres, exner, geop, montg, tracr, u_edg,
                                                      v_edg, dp_edg, lp_edg, geop_edg, mont_edg, uvsq_edg, trc_edg)))
 
@@ -171,6 +183,7 @@ class Dycore:
                                                       exner, dp_tndcy, massfx, omega)))
 
     def trcadv(self, its, trcr_edg, tracr, trcdp, trc_tdcy, trclo_tdcy, massfx, delp):
+        self._need_tracer_edges(trcr_edg, "trcr_edg")
         self._call("fim_trcadv", its, *map(_ptr, (trcr_edg, tracr, trcdp, trc_tdcy, trclo_tdcy, massfx, delp)))
 
     def momtum(self, its, u_velo, v_velo, exner, relvor, u_edg, v_edg, trcr_edg, geop_edg, mont_edg, uvsq_edg,
@@ -365,6 +378,12 @@ class DycoreState:
     def set_active(self, member, active):
         _lib.check(self.lib.fim_member_set_active(self.dyc.ctx, self.st, member, 1 if active else 0),
                    "fim_member_set_active", self.dyc.ctx)
+
+    def synthetic(self, member, seed, ntra, sigma_ps=200.0, noise=0.0):
+        """The seeded balanced state made on the device in member slot
+        `member` (fim_state_synthetic; asynchronous on the library stream)."""
+        _lib.check(self.lib.fim_state_synthetic(self.dyc.ctx, self.st, member, int(seed) & (2 ** 64 - 1), ntra,
+                                                float(sigma_ps), float(noise)), "fim_state_synthetic", self.dyc.ctx)
 
     def set_tracers(self, member, ntr):
         """Member `member` carries ntr tracers (theta included): later steps

@@ -2,8 +2,9 @@
 
 A request asks to advance a state on grid level glvl with nvl layers and
 ntra tracers by `steps` dynamics steps: its own host state, or a seeded
-balanced state that is made on the device in the slot it is admitted to
-(milliseconds, where the numpy generator takes seconds at glvl 7).  Requests on the same
+balanced state that the library's kernels make on the device in the slot it
+is admitted to (milliseconds, where the numpy generator takes seconds at
+glvl 7).  Requests on the same
 grid (glvl, nvl) share a pool: one context whose ensemble slots are the
 batch, advanced together by one fused launch sequence per step
 (fim_step_active, one CUDA-graph replay).  A pool carries `max_tracers`
@@ -57,12 +58,34 @@ class Request:
         return (10 * 4 ** self.glvl + 2) * self.nvl * self.steps
 
 
-def state_bytes(glvl, nvl, ntra, precision):
-    """Device bytes of one member slot (state, edge fields, scratch)."""
+# tracers a launch of a pool's fused tracer kernels takes (0: the library's
+# choice, all of them while their scratch stays under ~48 GB).  Short chunks
+# would leave room for more slots, but each launch stages a patch's tables,
+# coefficients and mass fluxes once for its tracers: pools with 3-tracer
+# chunks served the default stream at 8.5e8 cell-level-steps/s against
+# 1.0e9 with whole chunks.
+POOL_TRACER_CHUNK = 0
+
+
+def state_bytes(glvl, nvl, ntra, precision, tracer_chunk=POOL_TRACER_CHUNK):
+    """Device bytes of one member slot of a pool context: the state's fields,
+    the step's edge fields and the kernels' scratch, as the library allocates
+    them (fused tracer transport, no class-B tracers), plus 5%; with the
+    library's tracer chunks the scratch is counted for every tracer."""
     nip = 10 * 4 ** glvl + 2
     w = 8 if precision == "f64" else 4
-    words = 6 + 4 + 2 * ntra + 12 + 6 * ntra + 18 + 7 * 6 + 6 * ntra + 6 * ntra + 20
-    return int(nip * nvl * words * w * 1.1)
+    T = ntra
+    tch = min(ntra, tracer_chunk) if tracer_chunk > 0 else ntra
+    intf = (nvl + 1) / nvl
+    words = (3 + 3 * intf + 1          # us vs dp, pr ex ph, mp
+             + 2 * T + 12 + 6 * T       # tr trdp, u v dp dpl AB3, trc trl AB3
+             + 18 + 1 + intf + 1        # massfx, ws sdot relvor
+             + 7 * 6 + 6                # edge fields, theta's trc_edg
+             + 12 * tch                 # fused tracer scratch
+             + 11 + 2 + 2 * intf)       # cnuity, momtum, hybgen scratch
+    if precision != "f64":
+        words += 3                      # float-float Montgomery potential, theta of the edge values
+    return int(nip * nvl * words * w * 1.05)
 
 
 class Pool:
@@ -75,7 +98,7 @@ class Pool:
         self.ntra = ntra
         self.grid = Grid.cached(glvl)
         self.cfg = FimConfig(nvl=nvl, ntra=ntra, dt=default_dt(glvl), precision=precision, members=slots,
-                             stream_priority=priority)
+                             stream_priority=priority, tracer_chunk=POOL_TRACER_CHUNK)
         self.dyc = Dycore(self.grid, self.cfg)
         self.st = self.dyc.state()
         for m in range(slots):
@@ -91,13 +114,11 @@ class Pool:
         return -1
 
     def admit(self, req, now):
-        import torch
         m = self.free_slot()
         if req.fields is None:
             own = FimConfig(nvl=self.cfg.nvl, ntra=req.ntra, dt=self.cfg.dt, precision=self.cfg.precision)
             # on the pool's stream, ahead of the slot's initialisation
-            with torch.cuda.stream(self.stream):
-                synthetic_state_device(self.st, m, self.grid, own, req.seed, sigma_ps=200.0, noise=0.5)
+            synthetic_state_device(self.st, m, self.grid, own, req.seed, sigma_ps=200.0, noise=0.5)
         else:
             fields = dict(req.fields)
             src = np.asarray(fields["tr3d"]).reshape(-1)

@@ -49,38 +49,12 @@ def synthetic_state(grid, cfg, seed, sigma_ps=200.0, noise=0.0, dtype=np.float64
 
 def synthetic_state_device(st, member, grid, cfg, seed, sigma_ps=200.0, noise=0.0):
     """The balanced state of synthetic_state, made on the device straight
-    into member slot `member` of a State: the same recipe drawn from torch's
-    seeded CUDA generator (so other random numbers than the host PCG64
-    stream; the same seed and sizes give the same state).  Tracers of the
-    slot past cfg.ntra + cfg.ntrb are zeroed.  Runs on torch's current
-    stream; nothing is synchronised."""
-    import torch
-    dev = torch.device("cuda", torch.cuda.current_device())
-    f64 = torch.float64
-    g = torch.Generator(device=dev)
-    g.manual_seed(int(seed))
-    N, L, T = grid.nip, cfg.nvl, cfg.ntra + getattr(cfg, "ntrb", 0)
-    ps = P1000 + torch.randn(N, generator=g, device=dev, dtype=f64) * sigma_ps
-    dps = torch.as_tensor(cfg.dpsig / cfg.dpsig.sum(), device=dev)
-    dp = (ps[:, None] - cfg.ptop) * dps[None, :]
-    pr = torch.empty((N, L + 1), device=dev, dtype=f64)
-    pr[:, L] = cfg.ptop
-    pr[:, :L] = cfg.ptop + torch.flip(torch.cumsum(torch.flip(dp, [1]), 1), [1])  # top-down sums
-    u = (35.0 * torch.cos(torch.as_tensor(grid.lat, device=dev)))[:, None].expand(N, L).clone()
-    v = torch.zeros((N, L), device=dev, dtype=f64)
-    if noise > 0.0:
-        u += torch.randn((N, L), generator=g, device=dev, dtype=f64) * noise
-        v += torch.randn((N, L), generator=g, device=dev, dtype=f64) * noise
-    out = dict(us3d=u, vs3d=v, dp3d=pr[:, :L] - pr[:, 1:], pr3d=pr, ex3d=CP * (pr / P1000) ** (RD / CP))
-    for name, a in out.items():
-        st.tensor(name, member).copy_(a.reshape(-1))
-    for name in ("ph3d", "mp3d"):
-        st.tensor(name, member).zero_()
-    tr = st.tensor("tr3d", member).view(-1, N, L)
-    if tr.shape[0] < T:
-        raise ValueError("member slot holds %d tracers, the state %d" % (tr.shape[0], T))
-    theta = torch.as_tensor(300.0 + 300.0 * np.arange(L) / (L - 1), device=dev)
-    tr[0].copy_(theta[None, :].expand(N, L))
-    for t in range(1, T):
-        tr[t].copy_(torch.rand((N, L), generator=g, device=dev, dtype=tr.dtype) * 1e-2)
-    tr[T:].zero_()
+    into member slot `member` of a State by the library's own kernels
+    (fim_state_synthetic): the same recipe, drawn from a counter-based
+    generator (so other random numbers than the host PCG64 stream; the same
+    seed and grid give the same state in any slot or context).  Tracers of
+    the slot past cfg.ntra + cfg.ntrb are zeroed.  Asynchronous on the
+    library's stream."""
+    if grid.nip != st.dyc.grid.nip or cfg.nvl != st.dyc.cfg.nvl:
+        raise ValueError("the state's grid and levels differ from the context's")
+    st.synthetic(member, seed, cfg.ntra + getattr(cfg, "ntrb", 0), sigma_ps=sigma_ps, noise=noise)

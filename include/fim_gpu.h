@@ -102,6 +102,9 @@ typedef struct fim_config {
                               first; clamped to the device's range): contexts that
                               share a GPU, e.g. serving pools of different grids,
                               can let the short steps through first */
+  int tracer_chunk;        /* [0] tracers a launch of the fused tracer kernels takes
+                              (their scratch is 12 nvl nip values a tracer and member);
+                              0: as many as ~48 GB of scratch allows */
 } fim_config;
 
 typedef struct fim_ctx fim_ctx;
@@ -333,9 +336,11 @@ enum fim_field {
  * thickness (module_variables.F90:27,89), empty (count 0) without class-B
  * tracers.  With member_group < members the edge work fields (u_edg ..
  * trc_edg) exist for member_group members only.
- * After a fused step the edge work fields are in the step's internal form:
- * trc_edg of tracers 2..ntra holds the own-side reconstructions (edgvar3
- * loop 1) and, in an FP32 context, mont_edg holds edge-minus-cell values. */
+ * With hi_order_flux_comp (the fused tracer transport, which forms the
+ * tracers' edge values on chip) trc_edg holds theta's edge values only
+ * (6 nvl nip values a member).  After a fused step the edge work fields are
+ * in the step's internal form: in an FP32 context mont_edg holds
+ * edge-minus-cell values. */
 int fim_state_alloc(fim_ctx *ctx, fim_state **out);
 int fim_state_free(fim_ctx *ctx, fim_state *st);
 /* device pointer and element count of one member's field */
@@ -396,6 +401,16 @@ int fim_member_its(const fim_ctx *ctx, int member);
  * in a context of ntr tracers.  FIM_ENOTSUP without hi_order_flux_comp or
  * with class-B tracers.  No counterpart in the reference (serving). */
 int fim_member_set_tracers(fim_ctx *ctx, int member, int ntr);
+/* A seeded balanced initial state made on the device in one member slot
+ * (no counterpart in the reference, whose initial state comes from GFS data,
+ * dyn_init.F90:826): surface pressure 1000 hPa + N(0, sigma_ps) Pa,
+ * thicknesses proportional to dpsig, theta 300 -> 600 K, u = 35 m/s cos(lat)
+ * (+ N(0, noise) m/s on u and v), tracers 2..ntra U[0, 1e-2), the slot's
+ * tracers past ntra zero, ph3d and mp3d zero.  A counter-based generator:
+ * the state depends only on the seed and the grid.  Asynchronous on the
+ * context stream; fim_state_init(_member) follows as after an upload. */
+int fim_state_synthetic(fim_ctx *ctx, fim_state *st, int member, unsigned long long seed, int ntra,
+                        double sigma_ps, double noise);
 
 /* Step state of one member for restart files: the completed step count
  * (itsm1, restart.F90:58), the AB3 slots nf/of/vof in Fortran numbering and

@@ -336,6 +336,11 @@ def test_fused_step_matches_routine_sequence(case4):
              "dp_tdcy", "dpl_tdcy", "trc_tdcy", "trl_tdcy", "massfx", "ws3d", "sdot", "relvor", "psrf", "ptdcy",
              "u_edg", "v_edg", "dp_edg", "lp_edg", "mont_edg", "uvsq_edg", "geop_edg", "trc_edg"]
     g = {n: dev(st.download(n)) for n in names}
+    # the routines take the reference's trc_edg of every tracer; the fused
+    # step's state keeps theta's only (its first nvl x 6 x nip values)
+    te = np.zeros(6 * grid.nip * cfg.nvl * cfg.ntra)
+    te[:g["trc_edg"].numel()] = st.download("trc_edg")
+    g["trc_edg"] = dev(te)
     d2.set_ab(3, 2, 1, 0.0, 0.0, 0.0)  # the post-init slots (Fortran 0,2,1 before the first abstart)
     for its in range(1, 5):
         st.step(its, use_graph=True)

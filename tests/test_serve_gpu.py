@@ -178,3 +178,22 @@ def test_set_tracers_rejects():
     d2 = F.Dycore(grid, F.FimConfig(nvl=38, ntra=6, dt=400.0, ntrb=2))
     with pytest.raises(FimError):
         d2.state().set_tracers(0, 3)
+
+
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_state_bytes_matches_the_library(precision):
+    """serve.state_bytes (what admission by free HBM counts a slot at)
+    covers one more member slot of a pool context, within 12%."""
+    from fimocn_subx_realtime_hera_apr2020_gb300.serve import POOL_TRACER_CHUNK, state_bytes
+    grid = F.Grid.cached(4)
+    got = []
+    for slots in (1, 3):
+        d = F.Dycore(grid, F.FimConfig(nvl=64, ntra=9, dt=300.0, precision=precision, members=slots,
+                                       tracer_chunk=POOL_TRACER_CHUNK))
+        st = d.state()
+        got.append(d.device_bytes())
+        st.free()
+        d.close()
+    per_slot = (got[1] - got[0]) / 2
+    est = state_bytes(4, 64, 9, precision)
+    assert per_slot <= est <= 1.12 * per_slot, (per_slot, est)

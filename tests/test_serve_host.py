@@ -45,7 +45,9 @@ def test_latency_stats():
 
 def test_state_bytes_scales():
     b32 = state_bytes(6, 64, 11, "f32")
-    assert state_bytes(6, 64, 11, "f64") == 2 * b32 or abs(state_bytes(6, 64, 11, "f64") - 2 * b32) <= 1
+    # FP64 words are twice as wide; the FP32-mixed state keeps three more
+    # values a cell-level (float-float Montgomery potential, theta copy)
+    assert 1.9 < state_bytes(6, 64, 11, "f64") / b32 < 2.0
     assert state_bytes(7, 64, 11, "f32") > 3.9 * b32
     assert state_bytes(6, 64, 21, "f32") > b32
 
