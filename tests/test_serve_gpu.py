@@ -197,3 +197,51 @@ def test_state_bytes_matches_the_library(precision):
     per_slot = (got[1] - got[0]) / 2
     est = state_bytes(4, 64, 9, precision)
     assert per_slot <= est <= 1.12 * per_slot, (per_slot, est)
+
+
+def _draw(seed, stream, idx):
+    """numpy restatement of the generator of fim_state_synthetic (SplitMix64's
+    output function on a Weyl sequence keyed by seed and stream)."""
+    g = np.uint64(0x9E3779B97F4A7C15)
+
+    def mix(z):
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+    with np.errstate(over="ignore"):
+        key = mix(np.uint64(seed) * g + np.uint64(stream))
+        return mix(key + (np.asarray(idx, dtype=np.uint64) + np.uint64(1)) * g)
+
+
+def _unit(x, plus_one=False):
+    return ((x >> np.uint64(11)) + np.uint64(1 if plus_one else 0)).astype(np.float64) * 2.0 ** -53
+
+
+def test_synthetic_state_generator():
+    """fim_state_synthetic against its numpy restatement: the drawn tracers
+    bit for bit, the surface pressure and winds (Box-Muller through log and
+    cos) to 1e-12."""
+    grid = F.Grid.cached(3)
+    N, L, T, seed = grid.nip, 38, 5, 4242
+    d = F.Dycore(grid, F.FimConfig(nvl=L, ntra=T, dt=400.0))
+    st = d.state()
+    st.synthetic(0, seed, T, sigma_ps=200.0, noise=0.5)
+    c = np.arange(N * L)
+    tr = st.download("tr3d").reshape(T, N * L)
+    for t in range(1, T):
+        assert np.array_equal(tr[t], _unit(_draw(seed, 16 + t, c)) * 1e-2), t
+
+    def normal(stream, idx):
+        u1 = _unit(_draw(seed, stream, 2 * idx), plus_one=True)
+        u2 = _unit(_draw(seed, stream, 2 * idx + 1))
+        return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+
+    ps = st.download("pr3d").reshape(N, L + 1)[:, 0]
+    assert np.allclose(ps, 1e5 + normal(1, np.arange(N)) * 200.0, rtol=1e-12, atol=0)
+    u = st.download("us3d")
+    want_u = np.repeat(35.0 * np.cos(grid.lat), L) + normal(2, c) * 0.5
+    assert np.allclose(u, want_u, rtol=0, atol=1e-11)
+    assert np.allclose(st.download("vs3d"), normal(3, c) * 0.5, rtol=0, atol=1e-12)
+    st.free()
+    d.close()
