@@ -67,9 +67,9 @@ E2E_FIELDS = ["us3d", "vs3d", "dp3d", "pr3d", "ex3d", "ph3d", "mp3d", "tr3d", "t
 # the fields a step writes without reading them
 E2E_AB3 = {"u_tdcy", "v_tdcy", "dp_tdcy", "dpl_tdcy", "trc_tdcy", "trl_tdcy"}
 E2E_OUTPUTS = {"ws3d", "sdot", "relvor"}  # rewritten whole by every step (ptdcy: one of its two levels)
-# rewritten whole by the step's opening hystat from a member's second step on
-# (the timed steps): they only come down
-E2E_RECOMPUTED = {"mp3d", "trdp"}
+# rewritten whole by the step's opening hybgen and hystat from a member's
+# second step on (the timed steps): they only come down
+E2E_RECOMPUTED = {"mp3d", "trdp", "dp3d"}
 
 
 def peaks():

@@ -1014,12 +1014,13 @@ int io_upload(StepIo& io, int stage, int t0, int nt, cudaEvent_t* done) {
     IoClass k;
     if (!io_class(f, &k) || k.up != stage) continue;
     // From a member's second step on, the step opens with hybgen and hystat
-    // of the step before (dyn_run.F90:119-132), which rewrite the Montgomery
-    // potential and tracer x thickness whole before anything reads them
-    // (hystat.F90:58-101; the remap forms trdp as it stores each tracer):
-    // the host's copies are not needed.  Class-B tracers' trdp is not
-    // recomputed, so with ntrb > 0 trdp goes up.
-    if (io.its > 1 && (f == FIM_MP3D || (f == FIM_TRDP && c->TB == 0))) continue;
+    // of the step before (dyn_run.F90:119-132), which rewrite the layer
+    // thicknesses, the Montgomery potential and tracer x thickness whole
+    // before anything reads them (hybgen.F90:189-191, hystat.F90:58-101; the
+    // remap forms trdp as it stores each tracer): the host's copies are not
+    // needed.  Class-B tracers' trdp is not recomputed, so with ntrb > 0 trdp
+    // goes up.
+    if (io.its > 1 && (f == FIM_MP3D || f == FIM_DP3D || (f == FIM_TRDP && c->TB == 0))) continue;
     for (int m = 0; m < c->M; m++) {
       if (k.ab3) {
         const int n = (f == FIM_TRC_TDCY || f == FIM_TRL_TDCY) ? nt : 1, a = n == 1 && stage != kIoT ? 0 : t0;

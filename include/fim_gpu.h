@@ -440,9 +440,9 @@ int fim_step_active(fim_ctx *ctx, fim_state *st, int use_graph);
  * tendency fields move only the slots the step reads (of, vof) and writes
  * (nf); ws3d, sdot and relvor, which the step rewrites whole, only come down
  * (ptdcy, of whose two time levels a step writes one, goes both ways); from
- * its = 2 on, mp3d and trdp (the class-A tracers' part; with ntrb = 0) only
- * come down too, because the step's opening hystat rewrites them before any
- * read.
+ * its = 2 on, dp3d, mp3d and trdp (the class-A tracers' part; with ntrb = 0)
+ * only come down too, because the step's opening hybgen and hystat rewrite
+ * them before any read.
  * Returns when every download has landed; *h2d_bytes and *d2h_bytes (may be
  * null) get the bytes moved.  FIM_ENOTSUP with member_group < members. */
 int fim_state_set_host(fim_ctx *ctx, fim_state *st, int field, int member, void *host);

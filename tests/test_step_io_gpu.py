@@ -22,9 +22,10 @@ FIELDS = ["us3d", "vs3d", "dp3d", "pr3d", "ex3d", "ph3d", "mp3d", "tr3d", "trdp"
           "dpl_tdcy", "trc_tdcy", "trl_tdcy", "ws3d", "sdot", "relvor", "psrf", "ptdcy"]
 AB3 = {"u_tdcy", "v_tdcy", "dp_tdcy", "dpl_tdcy", "trc_tdcy", "trl_tdcy"}
 OUT = {"ws3d", "sdot", "relvor"}
-# rewritten whole by the step's opening hystat from the second step on, so
-# they go up only at the first step (the poison then shows they are not read)
-RECOMPUTED = {"mp3d", "trdp"}
+# rewritten whole by the step's opening hybgen and hystat from the second
+# step on, so they go up only at the first step (the poison then shows they
+# are not read)
+RECOMPUTED = {"mp3d", "trdp", "dp3d"}
 
 
 def _state(grid, cfg, fields):
