@@ -174,7 +174,7 @@ class Pool:
 class Server:
     """Continuous-batching request loop over resident device states."""
 
-    def __init__(self, precision="f32", slots=8, hbm_fraction=0.8, collect=("us3d", "tr3d"), max_tracers=21,
+    def __init__(self, precision="f32", slots=8, hbm_fraction=0.9, collect=("us3d", "tr3d"), max_tracers=21,
                  priorities=True):
         self.precision = precision
         self.slots = slots
