@@ -62,6 +62,10 @@ struct fim_ctx {
   int graph_gen = 0;
   // fim_step_io's copy streams (host to device, device to host) and events
   cudaStream_t io_in = nullptr, io_out = nullptr;
+  // the branch of a step that forms the budget sums beside momtum (they share
+  // no written data), forked from and joined to the step's stream
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int prio = 0;  // priority of the streams above (fim_config.stream_priority, clamped)
   std::vector<cudaEvent_t> io_ev;
   std::vector<void*> owned;          // device allocations freed at destroy
@@ -1110,6 +1114,8 @@ int enqueue_step(fim_ctx* c, fim_state* st, StepIo* io = nullptr) {
                    F<R>(st, FIM_TR3D), F<R>(st, FIM_TRDP), F<R>(st, FIM_PSRF), F<R>(st, FIM_PTDCY), st->mpf,
                    trdp_done);
   if (io && (rc = io_download(*io, kIoA, 0, 0))) return rc;
+  // one member group and no host transfers: the budget sums run beside momtum
+  const bool branch = !io && c->G == c->M && c->aux;
   // the dynamics of the step, one member group at a time; the edge work
   // fields and the scratch hold one group, the prognostic fields all members
   for (int m0 = 0; m0 < M; m0 += c->G) {
@@ -1188,18 +1194,40 @@ int enqueue_step(fim_ctx* c, fim_state* st, StepIo* io = nullptr) {
       if (io) io_chunk_hook(io, 1, 0, c->T);
     }
     if (io && io->rc) return io->rc;
+    if (branch) {
+      // budgets of the state the step returns, on the branch stream beside
+      // momtum: they read the thicknesses and tracers, which momtum does not
+      // write, and momtum reads nothing they write
+      CK(cudaEventRecord(c->ev_fork, c->stream), "step fork");
+      CK(cudaStreamWaitEvent(c->aux, c->ev_fork, 0), "step fork");
+      Launch la = l;
+      la.stream = c->aux;
+      launch_globsum<R>(la, g, s, c->T + c->TB, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), (const R*)nullptr,
+                        (const R*)nullptr, F<R>(st, FIM_PR3D), F<R>(st, FIM_EX3D), (const R*)nullptr,
+                        c->gs_partial, st->sums);
+      CK(cudaEventRecord(c->ev_join, c->aux), "step join");
+    }
     if (!io && (rc = momentum())) return rc;
   }
-  // budgets of the state the step returns
-  launch_globsum<R>(l, g, s, c->T + c->TB, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), (const R*)nullptr,
-                    (const R*)nullptr,
-                    F<R>(st, FIM_PR3D), F<R>(st, FIM_EX3D), (const R*)nullptr, c->gs_partial, st->sums);
+  if (branch) {
+    CK(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "step join");
+  } else {
+    // budgets of the state the step returns
+    launch_globsum<R>(l, g, s, c->T + c->TB, F<R>(st, FIM_DP3D), F<R>(st, FIM_TR3D), (const R*)nullptr,
+                      (const R*)nullptr,
+                      F<R>(st, FIM_PR3D), F<R>(st, FIM_EX3D), (const R*)nullptr, c->gs_partial, st->sums);
+  }
   if (io && (rc = io_download(*io, kIoE, 0, 0))) return rc;
   return FIM_OK;
 }
 
 int ensure_all(fim_ctx* c) {
   int rc;
+  if (!c->aux) {
+    CK(cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, c->prio), "step branch stream");
+    CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "step branch event");
+    CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "step branch event");
+  }
   if ((rc = ensure_cnuity(c, c->G))) return rc;
   if (c->kn.hi_order) {
     if ((rc = ensure_trc_fused(c, c->G))) return rc;
@@ -1510,12 +1538,14 @@ int fim_ctx_create(const fim_grid_desc* g, const fim_config* cfg, fim_ctx** out)
 int fim_ctx_destroy(fim_ctx* c) {
   if (!c) return FIM_EINVAL;
   if (c->stream) cudaStreamSynchronize(c->stream);
-  for (cudaStream_t q : {c->io_in, c->io_out})
+  for (cudaStream_t q : {c->io_in, c->io_out, c->aux})
     if (q) {
       cudaStreamSynchronize(q);
       cudaStreamDestroy(q);
     }
   for (cudaEvent_t e : c->io_ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : {c->ev_fork, c->ev_join})
+    if (e) cudaEventDestroy(e);
   for (void* p : c->owned) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
