@@ -340,12 +340,23 @@ def gpu_arm(args, ws, rank, local):
         dyc.profile(False)
         tl_keys = [k for k in tl if k.startswith(("up_end", "computed", "down_end"))] + ["end"]
         timeline = {k: round(tl[k], 2) for k in sorted(tl_keys, key=lambda k: tl[k]) if k in tl}
+        # the same path for a driver that leaves the dynamics' own AB3
+        # tendency history on the device (not registered: the step reads and
+        # writes the device slots, which hold the current values)
+        for f in E2E_AB3:
+            for m in range(members):
+                st.set_host(f, None, m)
+        st.step_io()
+        r_ms, (rh2d, rd2h) = timed(st.step_io)
+        resident = {"value": units * ws / (r_ms * 1e-3), "unit": UNIT, "ms_per_step": r_ms,
+                    "h2d_bytes_per_step": rh2d, "d2h_bytes_per_step": rd2h,
+                    "path": "fim_step_io with the six AB3 tendency fields left on the device"}
         e2e = {"value": units * ws / (e_ms * 1e-3), "unit": UNIT, "ms_per_step": e_ms,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "path": "fim_state_set_host (pinned host buffers) + fim_step_io: the fields the step reads go up "
                        "before the stage that first needs them, the fields it writes come down as soon as "
                        "they are final, on two copy streams beside the kernels",
-               "serial_ms_per_step": s_ms, "timeline_ms": timeline,
+               "serial_ms_per_step": s_ms, "timeline_ms": timeline, "tendencies_on_device": resident,
                "serial_path": "fim_state_upload(_slot) -> fim_step -> fim_state_download(_slot), one after the "
                               "other"}
         del bufs
