@@ -497,7 +497,7 @@ def serve_stats(args, n, prec):
     seeded Poisson stream), arrivals replayed in real time."""
     from fimocn_subx_realtime_hera_apr2020_gb300.serve import Server, latency_stats, poisson_requests
     reqs = poisson_requests(n, rate=args.serve_rate, seed=5000, steps=(args.serve_min_steps, args.serve_max_steps))
-    srv = Server(precision=prec, slots=args.serve_slots, collect=())
+    srv = Server(precision=prec, slots=args.serve_slots, collect=(), grids=(5, 6, 7))
     done = srv.run(reqs, realtime=True)
     pools = {"glvl%d_nvl%d" % k: len(p.slots) for k, p in sorted(srv.pools.items())}
     srv.close()

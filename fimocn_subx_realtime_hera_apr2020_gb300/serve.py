@@ -175,7 +175,11 @@ class Server:
     """Continuous-batching request loop over resident device states."""
 
     def __init__(self, precision="f32", slots=8, hbm_fraction=0.9, collect=("us3d", "tr3d"), max_tracers=21,
-                 priorities=True):
+                 priorities=True, grids=()):
+        # grid levels whose tables are built at start-up rather than by the
+        # first request on them (glvl 7: ~0.4 s of host work)
+        for glvl in grids:
+            Grid.cached(glvl)
         self.precision = precision
         self.slots = slots
         # pools on smaller grids get higher stream priorities: their short
